@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark of the PFEM per-time-step solve on one GB300.
+
+Workload (the reference's headline configuration that fits one GPU): the 2D weakly
+compressible dam break - 1.0 x 2.0 m water column in a 4.0 x 3.0 m tank, nodes on an h = 0.005 m
+lattice jittered +-0.1h (seeded), Delaunay + alpha shape (alpha = 1.2): ~82k nodes, ~160k
+triangles; Tait-Murnaghan EOS (rho* = 1000, K0 = 2.2e7 Pa, K0' = 7), CDS_dpdt with Meduri
+stabilisation, CFL security coefficient 0.3, adaptive dt.  One "step" is one explicit time step
+of the whole mesh (SolverWCompNewton::solveOneTimeStep without the host remesh) followed by
+the CFL dt update (computeNextDT).  The state is FP32 by default ("FP32 state with FP64 mass
+sums"), --precision fp64 runs the plain FP64 form.
+
+Timing: W warm-up steps, then K steps, each timed with CUDA events on the library's own
+stream, with a 256 MB write between steps to flush L2 (the state is ~7 MB and would otherwise
+stay L2-resident).  value = steps / sum(step times).  e2e times the same step through the C ABI
+with host buffers: per step, pfg_set_states from pinned host memory, pfg_wc_step and
+pfg_get_states back to pinned memory.
+
+--impl reference times the CPU restatement of the reference's path (the FP64 C++/OpenMP oracle,
+all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-steps/s (2D WC dam break, CDS_dpdt explicit step)"
+UNIT = "steps/s"
+H = 0.005
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload_config(mesh, precision):
+    return {
+        "workload": "2D weakly compressible dam break (C2)",
+        "h_m": H, "nodes": int(mesh.n_nodes), "elements": int(mesh.n_elems),
+        "dof_per_step": int(3 * mesh.n_nodes), "state": precision, "dt": "adaptive CFL 0.3",
+        "l2": "flushed between timed steps (256 MB write)", "remesh": "excluded (host side)",
+        "parallelism": "replicas only",
+    }
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def wc_phase_bytes(d, N, E, s):
+    """Algorithmic bytes per launch of each WC kernel (s = state bytes; positions FP64; int32
+    indices; one flag byte per node).  Each node/element datum counted once."""
+    inc = E * (d + 1)
+    return {
+        "WC predict": N * (3 * d * s + 16 * d + 1),
+        "WC continuity element": E * (d + 1) * 4 + N * (8 * d + (d + 1) * s) + 2 * (d + 1) * E * s,
+        "WC continuity node": 2 * (d + 1) * E * s + inc * 5 + (N + 1) * 4 + N + 2 * N * s,
+        "WC momentum element": E * (d + 1) * 4 + N * (8 * d + (d + 2) * s) + (d + 1) ** 2 * E * s,
+        "WC momentum node": (d + 1) ** 2 * E * s + inc * 5 + (N + 1) * 4 + N + 8 * d * N + d * s * N + 2 * d * s * N,
+        "WC time step": E * (d + 1) * 4 + N * (8 * d + (d + 2) * s),
+    }
+
+
+def step_bytes(d, N, E, s):
+    """Algorithmic bytes of one whole step: connectivity once, x, v, a, p, rho read and written
+    once, flags once (each node datum once)."""
+    return E * (d + 1) * 4 + 2 * N * (3 * d + 2) * s + N
+
+
+def time_oracle(mesh, s0, seconds, max_steps, threads=None):
+    """Oracle WC steps (with the CFL dt update) for up to `seconds`; returns (steps, elapsed, threads)."""
+    from oracle import oracle as O
+
+    if threads:
+        O.set_threads(threads)
+    om = O.OracleMesh(mesh)
+    p = O.wc_params()
+    s = s0.copy()
+    dt = O.wc_next_dt(om, p, s)
+    O.wc_step(om, p, dt, s)  # warm caches / thread pool
+    dt = O.wc_next_dt(om, p, s)
+    n = 0
+    t0 = time.perf_counter()
+    while n < max_steps:
+        O.wc_step(om, p, dt, s)
+        dt = O.wc_next_dt(om, p, s)
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    return n, time.perf_counter() - t0, O.num_threads()
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from pfem_gb300 import mesh as M
+
+    mesh = M.dam_break_2d(H)
+    s0 = M.wc_initial_states(mesh)
+    from oracle import oracle as O
+
+    O.build()
+    # warm-up steps untimed, then a bounded sample of K steps (at most ~120 s)
+    time_oracle(mesh, s0, 1e9, max(0, min(args.warmup, 3)))
+    n, el, thr = time_oracle(mesh, s0, 120.0, args.steps)
+    v = n / el
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": n,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice)",
+        "config": workload_config(mesh, "fp64"),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+                         "sample": f"{n} full C2 steps (the {args.steps} asked, capped at 120 s of CPU time)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from pfem_gb300 import api, build
+    from pfem_gb300 import mesh as M
+
+    build.build()
+    mesh = M.dam_break_2d(H)
+    s0 = M.wc_initial_states(mesh)
+    d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
+    prec = api.PREC_MIXED if args.precision == "fp32" else api.PREC_FP64
+    sbytes = 4 if args.precision == "fp32" else 8
+
+    def make(precision):
+        p = api.default_params(api.KIND_WC_CDS_DPDT, 2)
+        p.precision = precision
+        ctx = api.Context(p)
+        ctx.upload_mesh(mesh)
+        ctx.set_states(s0)
+        ctx.set_time(0.0, ctx.next_dt())
+        return ctx
+
+    ctx = make(prec)
+    ext = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MB > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    # warm-up
+    ctx.wc_step_async(0.0, args.warmup)
+    ctx.synchronize()
+    # timed region: K steps, L2 flushed between steps, events on the library stream
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    ctx.set_profiling(True)
+    ctx.reset_phase_times()
+    barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(ext):
+        for k in range(K):
+            flush.fill_(k & 0xFF)
+            ev[k][0].record(ext)
+            ctx.wc_step_async(0.0, 1)
+            ev[k][1].record(ext)
+    st = ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    phases = ctx.phase_times()
+    ctx.set_profiling(False)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * K / (total_ms / 1e3)
+
+    # L2-resident throughput (steps back to back, no flush) for context
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(ext):
+        e0.record(ext)
+        ctx.wc_step_async(0.0, K)
+        e1.record(ext)
+    ctx.synchronize()
+    warm_value = K / (e0.elapsed_time(e1) / 1e3)
+
+    # end to end through the C ABI with host buffers
+    nst = ctx.nstates * N
+    h_in = torch.empty(nst, dtype=torch.float64, pin_memory=True).numpy()
+    h_out = torch.empty(nst, dtype=torch.float64, pin_memory=True).numpy()
+    h_in[:] = ctx.get_states()
+    Ke = min(K, 300)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        ctx.set_states(h_in)
+        ctx.wc_step(0.0, 1)
+        ctx.get_states(out=h_out)
+        h_in, h_out = h_out, h_in
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clk = clocks.stop()
+
+    # accuracy of the timed form against the FP64 plain form (fixed dt, same steps)
+    acc = None
+    if rank == 0:
+        ref = make(api.PREC_FP64)
+        tst = make(prec)
+        dt0 = ref.next_dt()
+        S = min(K, 2000)
+        ref.wc_step(dt0, S)
+        tst.wc_step(dt0, S)
+        a, b = ref.get_states(), tst.get_states()
+        names = ["vx", "vy", "p", "rho", "ax", "ay"]
+        acc = {nm: float(np.linalg.norm(b[i * N:(i + 1) * N] - a[i * N:(i + 1) * N]) /
+                         max(np.linalg.norm(a[i * N:(i + 1) * N]), 1e-300)) for i, nm in enumerate(names)}
+        xa, xb = ref.get_positions(), tst.get_positions()
+        acc["x"] = float(np.abs(xb - xa).max() / np.abs(xa).max())
+        acc["mass_rel"] = abs(tst.mass() - ref.mass()) / ref.mass()
+        acc["steps"] = S
+        ref.close()
+        tst.close()
+
+    # roofline of the dominant kernel (phase timers are CUDA events on the library stream)
+    pb = wc_phase_bytes(d, N, E, sbytes)
+    dom = max(phases.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_n) = dom
+    peak, peak_kind = hbm_peak()
+    achieved = pb[dom_name] / (dom_ms / dom_n / 1e3) / 1e9
+    step_gbs = step_bytes(d, N, E, sbytes) / (total_ms / K / 1e3) / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n, el, thr = time_oracle(mesh, s0, args.cpu_sample_seconds, 100000)
+        cpu = {"value": n / el, "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"{n} full C2 steps of the FP64 C++/OpenMP oracle ({el:.1f} s)"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32" if args.precision == "fp32" else "f64",
+            "data": "synthetic (seeded jittered lattice, no .msh shipped by the reference)",
+            "config": workload_config(mesh, args.precision),
+            "dof_per_s": value * 3 * N,
+            "value_l2_resident": warm_value,
+            "step_hbm_gbs": step_gbs,
+            "e2e": {"value": Ke / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h_in.nbytes),
+                    "d2h_bytes_per_step": int(h_out.nbytes)},
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "algorithmic_bytes": pb[dom_name],
+                         "avg_launch_us": 1e3 * dom_ms / dom_n},
+            "phases_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in phases.items()},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(sum(v[1] for v in phases.values())),
+            "err_vs_fp64": acc,
+            "last_dt": st.dt,
+        }
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

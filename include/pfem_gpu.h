@@ -1,0 +1,221 @@
+/*
+ * pfem_gpu.h - C ABI of the GB300 PFEM per-time-step solve library (libpfemgpu.so).
+ *
+ * The library replaces the per-step work behind the reference's solver classes
+ * (ImperatorS79/PFEM, paths relative to its project root):
+ *
+ *   Solver::solveOneTimeStep / computeNextDT      srcs/simulation/Solver.hpp:53,56
+ *   Equation::solve / preCompute                  srcs/simulation/Equation.hpp:65,68
+ *   Mesh geometry + position updates              srcs/mesh/Mesh.hpp:46-267
+ *
+ * A host-side solver subclass (C++, C or any FFI) keeps the reference's time loop and its
+ * remeshing; after every remesh it hands this library the new connectivity and node arrays.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: 0 (PFG_OK) or a negative PFG_ERR_* code.
+ *     Nothing throws across the ABI; pfg_last_error() gives the message of the last failure.
+ *   - Numerical failure of a step (Picard not converged, NaN) is NOT an error code: it is
+ *     reported in pfg_step_status.converged = 0, mirroring the reference's `bool` return
+ *     (PicardAlgo.cpp:55-66,79-86).  The library then restores the saved node positions and
+ *     states itself, like Mesh::restoreNodesList.
+ *   - One context per host thread; each context owns one CUDA stream and all of its device
+ *     memory.  Calls on one context must not overlap.
+ *   - All host arrays are plain pointers: positions and fields are structure-of-arrays
+ *     ("field-major"): x[d*N + n]; element connectivity conn[k*E + e], k = 0..dim.
+ *   - The library never calls back into the host.
+ */
+#ifndef PFEM_GPU_H
+#define PFEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFG_API __attribute__((visibility("default")))
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define PFG_OK 0
+#define PFG_ERR_INVALID (-1)     /* bad argument (sizes, indices, null pointers)          */
+#define PFG_ERR_CUDA (-2)        /* a CUDA call failed                                     */
+#define PFG_ERR_NOMEM (-3)       /* device allocation failed or HBM budget exceeded        */
+#define PFG_ERR_STATE (-4)       /* call out of order (e.g. step before mesh upload)       */
+#define PFG_ERR_UNSUPPORTED (-5) /* option not implemented for this configuration          */
+#define PFG_ERR_DEVICE (-6)      /* a kernel reported an internal error (e.g. valence cap) */
+
+/* ---- node flags (one byte per node) ------------------------------------------------ */
+#define PFG_NODE_BOUND 1u        /* Node::isBound           srcs/mesh/Node.hpp:101        */
+#define PFG_NODE_FREE_SURFACE 2u /* Node::isOnFreeSurface                                  */
+#define PFG_NODE_FIXED 4u        /* Node::isFixed: position never updated                 */
+#define PFG_NODE_DIRICHLET 8u    /* bound node whose tag has a velocity BC
+                                    (Solver::m_bcTagFlags bit 0, Solver.hpp:78)            */
+#define PFG_NODE_FREE 16u        /* output only: node in no element (Node::isFree)        */
+
+/* ---- configuration --------------------------------------------------------------- */
+typedef enum {
+    PFG_KIND_INCOMP_PSPG = 0,  /* SolverIncompNewton, id "PSPG", problem IncompNewtonNoT  */
+    PFG_KIND_WC_CDS_DPDT = 1   /* SolverWCompNewton, id "CDS_dpdt", problem WCompNewtonNoT */
+} pfg_kind;
+
+typedef enum {
+    PFG_PREC_FP64 = 0,         /* plain form: FP64 everywhere                              */
+    PFG_PREC_MIXED = 1         /* FP32 assembly/Krylov/state, FP64 geometry, refinement
+                                  residual and global sums                                 */
+} pfg_precision;
+
+typedef enum {
+    PFG_LINSOLVE_BICGSTAB = 0, /* Jacobi-preconditioned BiCGSTAB                           */
+    PFG_LINSOLVE_LU = 1        /* device sparse LU (plain form; reference: Eigen SparseLU) */
+} pfg_linsolve;
+
+typedef enum {
+    PFG_RES_AX_F = 0,          /* ||A q - b||_2            MomContEquationPSPG.inl:366-371 */
+    PFG_RES_U = 1,             /* relative velocity change                        :319-342 */
+    PFG_RES_U_P = 2            /* max(rel. velocity change, rel. pressure change) :343-364 */
+} pfg_residual;
+
+typedef struct pfg_params {
+    int32_t dim;               /* 2 (triangles) or 3 (tetrahedra)                          */
+    int32_t kind;              /* pfg_kind                                                 */
+    int32_t precision;         /* pfg_precision                                            */
+    int32_t linear_solver;     /* pfg_linsolve (incompressible only)                       */
+    double gravity[3];         /* bodyForce                                                */
+    double mu;                 /* dynamic viscosity (both kinds)                           */
+    /* incompressible (MomContEq): */
+    double rho;
+    int32_t picard_max_iter;   /* maxIter                                                  */
+    int32_t residual;          /* pfg_residual                                             */
+    double picard_min_res;     /* minRes                                                   */
+    int32_t krylov_max_iter;   /* per linear solve                                         */
+    int32_t pad0;
+    double krylov_rel_tol;     /* stop when ||r|| <= max(rel_tol*||b||, abs_tol)           */
+    double krylov_abs_tol;
+    /* weakly compressible (ContEq + MomEq): */
+    double K0, K0p, rho_star;  /* Tait-Murnaghan                                           */
+    double security_coeff;     /* securityCoeff (CFL)                                      */
+    double max_dt;             /* maxDT                                                    */
+    int32_t meduri;            /* ContEq stabilization: 1 = "Meduri", 0 = "None"           */
+    int32_t pad1;
+    /* resources: */
+    size_t hbm_budget_bytes;   /* 0 = no limit                                             */
+} pfg_params;
+
+typedef struct pfg_step_status {
+    int32_t converged;         /* 1 = step accepted (reference: solveOneTimeStep() true)   */
+    int32_t picard_iterations; /* Picard solves performed                                  */
+    int32_t krylov_iterations; /* total Krylov iterations in the step                      */
+    int32_t steps_done;        /* WC: explicit steps completed                             */
+    double residual;           /* last Picard residual                                     */
+    double dt;                 /* time step used by the last step                          */
+    double time;               /* device-side simulated time after the call                */
+} pfg_step_status;
+
+typedef struct pfg_ctx pfg_ctx;
+
+/* Fill *p with the reference's dam-break defaults for `kind` and `dim`.
+ * (damBreakKoshizukaIncomp.lua / damBreakKoshizukaComp.lua, examples/2D/damBreakKoshizuka) */
+PFG_API int pfg_default_params(int32_t kind, int32_t dim, pfg_params* p);
+
+/* Create a context on the current CUDA device.  Replaces the construction of the
+ * Solver/Equation pair: SolverIncompNewton::SolverIncompNewton (IncompNewton/Solver.cpp:12-193)
+ * and SolverWCompNewton::SolverWCompNewton (WCompNewton/Solver.cpp:15-165). */
+PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out);
+PFG_API int pfg_destroy(pfg_ctx* ctx);
+PFG_API const char* pfg_last_error(const pfg_ctx* ctx);   /* never NULL */
+
+/* Hand the library a (re)meshed domain.  Replaces what Mesh::remesh leaves behind
+ * (Mesh.cpp:919-926; triangulateAlphaShape2D/3D, Mesh2D.cpp:32-251, Mesh3D.cpp:36-286):
+ * positions (dim x N), node flags, and (dim+1) x E positively oriented elements.  Rebuilds
+ * the node-element incidence, node adjacency and the sparsity pattern on the device.
+ * Node states are reset to zero; set them with pfg_set_states afterwards. */
+PFG_API int pfg_upload_mesh(pfg_ctx* ctx, int32_t n_nodes, const double* pos, const uint8_t* flags,
+                            int32_t n_elems, const int32_t* conn);
+
+/* Node states, field-major.  Incompressible: (dim+1)*N values [v_0..v_{d-1}, p]
+ * (getQFromNodesStates / setNodesStatesfromQ, StatesFromToQ.hpp:9-34).
+ * WC: (2*dim+2)*N values [v, p, rho, a] (WCompNewton/Problem.cpp:18). */
+PFG_API int pfg_set_states(pfg_ctx* ctx, const double* states);
+PFG_API int pfg_get_states(pfg_ctx* ctx, double* states);
+PFG_API int pfg_get_positions(pfg_ctx* ctx, double* pos);          /* dim*N */
+PFG_API int pfg_get_flags(pfg_ctx* ctx, uint8_t* flags);           /* N, PFG_NODE_FREE set */
+
+/* Dirichlet velocities V_bc(pos, t + dt) of n Dirichlet nodes, values[d*n + i] (field-major
+ * over the listed nodes).  Stands in for the Lua BoundaryV calls of m_applyBCPSPG
+ * (MomContEquationPSPG.inl:206-231) and MomEqWCompNewton::m_applyBC (MomEquation.inl:355-371).
+ * Nodes not listed keep their previous value (initially 0). */
+PFG_API int pfg_set_dirichlet(pfg_ctx* ctx, int32_t n, const int32_t* nodes, const double* values);
+
+/* One incompressible PSPG time step: MomContEqIncompNewton::solve + PicardAlgo::solve
+ * (MomContEquation.inl:287-309 [.inl offsets], PicardAlgo.cpp:31-95,
+ * MomContEquationPSPG.inl:261-373).  On non-convergence the positions and states are
+ * restored and status->converged = 0. */
+PFG_API int pfg_picard_step(pfg_ctx* ctx, double dt, pfg_step_status* status);
+
+/* nsteps weakly compressible CDS_dpdt steps (WCompNewton/Solver.cpp:236-276 without the
+ * remesh).  dt > 0 uses that fixed step for every step; dt <= 0 uses the device-side CFL step
+ * of computeNextDT (WCompNewton/Solver.cpp:192-234), which is refreshed after every step.
+ * Returns after all steps with a single host synchronisation. */
+PFG_API int pfg_wc_step(pfg_ctx* ctx, double dt, int32_t nsteps, pfg_step_status* status);
+
+/* Asynchronous form of pfg_wc_step: enqueues nsteps steps on the context's stream and returns
+ * without waiting.  pfg_synchronize waits for all enqueued work and fills the status (dt and
+ * time of the last step).  Lets a caller keep the GPU busy while it prepares other work. */
+PFG_API int pfg_wc_step_async(pfg_ctx* ctx, double dt, int32_t nsteps);
+PFG_API int pfg_synchronize(pfg_ctx* ctx, pfg_step_status* status);
+/* The CUDA stream (cudaStream_t) every kernel of this context is launched on, for callers
+ * that order their own GPU work against the library's. */
+PFG_API int pfg_get_stream(pfg_ctx* ctx, void** stream);
+
+/* CFL time step of the current WC state (SolverWCompNewton::computeNextDT). */
+PFG_API int pfg_next_dt(pfg_ctx* ctx, double* dt);
+/* Device-side time-step seed for pfg_wc_step(dt <= 0) (Solver::m_initialDT). */
+PFG_API int pfg_set_time(pfg_ctx* ctx, double time, double next_dt);
+
+/* Global sums and extractor values, reduced on the device in FP64:
+ *   volume  = sum |e|                    (ProbIncompNewton mass, IncompNewton/Problem.cpp:173-189)
+ *   mass    = sum |e| * mean(rho)        (ProbWCompNewton mass, WCompNewton/Problem.cpp:216-244)
+ *   tip     = max/min coordinate over non-bound, non-free nodes (MinMaxExtractor.cpp:28-62) */
+PFG_API int pfg_volume(pfg_ctx* ctx, double* volume);
+PFG_API int pfg_mass(pfg_ctx* ctx, double* mass);
+PFG_API int pfg_tip(pfg_ctx* ctx, int32_t coord, int32_t want_max, double* value);
+
+/* ---- inspection (parity tests) ---------------------------------------------------- */
+/* Assemble the PSPG system at the current positions: element tau from q_iter, right-hand
+ * side from q_prev (m_buildAbPSPG, MomContEquationPSPG.inl:6-146), then, when apply_bc != 0,
+ * m_applyBCPSPG (:148-235).  NULL q_iter / q_prev use the current device states. */
+PFG_API int pfg_pspg_assemble(pfg_ctx* ctx, double dt, const double* q_iter, const double* q_prev,
+                              int32_t apply_bc);
+/* Read the assembled system in CSR form.  Call with NULL arrays to get *n_rows and *nnz. */
+PFG_API int pfg_get_csr(pfg_ctx* ctx, int32_t* n_rows, int64_t* nnz, int64_t* row_ptr, int32_t* col_idx,
+                        double* values, double* rhs);
+/* Element geometry of the current positions: detJ[E], invJ[E*9] (row-major 3x3). */
+PFG_API int pfg_get_geometry(pfg_ctx* ctx, double* detJ, double* invJ);
+/* Solve A x = b for the assembled system with the configured linear solver (x: initial guess
+ * in, solution out, length R).  Returns iterations and the final ||A x - b|| in *res. */
+PFG_API int pfg_linear_solve(pfg_ctx* ctx, double* x, int32_t* iterations, double* res);
+
+/* ---- phase timers ----------------------------------------------------------------- */
+/* GPU time per phase of the path, measured with CUDA events on the context's stream while
+ * profiling is enabled.  Mirrors the reference's per-category timers (Solver::m_accumalatedTimes,
+ * Solver.hpp:253, printed by Solver::displayTimeStats, Solver.cpp:79-91).  Phases:
+ *   0 WC predict            1 WC continuity/element   2 WC continuity/node
+ *   3 WC momentum/element   4 WC momentum/node        5 WC time step
+ *   6 PSPG element prep     7 PSPG right-hand side    8 PSPG matrix (node pairs)
+ *   9 Krylov iteration     10 Picard residual        11 position update        */
+#define PFG_NUM_PHASES 12
+PFG_API int pfg_set_profiling(pfg_ctx* ctx, int32_t enable);
+/* Accumulated milliseconds and launch counts per phase since the last reset. */
+PFG_API int pfg_get_phase_times(pfg_ctx* ctx, double* ms, int64_t* launches);
+PFG_API int pfg_reset_phase_times(pfg_ctx* ctx);
+PFG_API const char* pfg_phase_name(int32_t phase);
+
+/* Library version string. */
+PFG_API const char* pfg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFEM_GPU_H */

@@ -1,0 +1,309 @@
+"""Python driver of the FP64 CPU oracle (test infrastructure only).
+
+Wraps `oracle/pfem_oracle.cpp` (built into `oracle/build/liboracle.so`) and restates the
+two control loops of the reference that sit above the element kernels:
+
+* the PSPG Picard loop, `PicardAlgo::solve` (`srcs/simulation/nonLinearAlgo/PicardAlgo.cpp:31-95`)
+  with the closures of `MomContEqIncompNewton::m_setupPicardPSPG`
+  (`srcs/simulation/physics/IncompNewton/MomContEquationPSPG.inl:261-373`).  The linear solve
+  is SuperLU with COLAMD column ordering (scipy.sparse.linalg.splu), standing in for Eigen 3.3's
+  `SparseLU<SparseMatrix<double>, COLAMDOrdering<int>>` (a port of the same supernodal SuperLU
+  algorithm; `MomContEquation.hpp:11`).  Eigen is not available here;
+* the incompressible time loop, `SolverIncompNewton::m_solveIncompNewtonNoT` and
+  `computeNextDT` (`srcs/simulation/physics/IncompNewton/Solver.cpp:216-247`), without the
+  remesh.
+
+Parity status: UNPINNED (the reference has no tests or golden vectors and cannot be built
+here).  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs may import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "pfem_oracle.cpp")
+LIB = os.path.join(HERE, "build", "liboracle.so")
+
+
+def build(force=False):
+    """Compile the oracle shared library (g++, OpenMP, no FMA contraction so x86 and Arm agree)."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    tmp = LIB + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", SRC, "-o", tmp]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class PspgParams(C.Structure):
+    _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double), ("g", C.c_double * 3)]
+
+
+class WcParams(C.Structure):
+    _fields_ = [("K0", C.c_double), ("K0p", C.c_double), ("rhoStar", C.c_double), ("mu", C.c_double),
+                ("g", C.c_double * 3), ("meduri", C.c_int), ("sc", C.c_double), ("maxDT", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        dp, ip, u8p, vp = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint8), C.c_void_p
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [C.c_int, C.c_int, dp, u8p, C.c_int, ip]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_num_threads.restype = C.c_int
+        L.orc_set_num_threads.argtypes = [C.c_int]
+        for name in ("orc_get_positions", "orc_set_positions", "orc_update_positions_from_save",
+                     "orc_update_positions"):
+            getattr(L, name).argtypes = [vp, dp]
+        L.orc_get_is_free.argtypes = [vp, u8p]
+        L.orc_get_geometry.argtypes = [vp, dp, dp, dp]
+        L.orc_save_nodes.argtypes = [vp]
+        L.orc_restore_nodes.argtypes = [vp]
+        L.orc_pspg_element.argtypes = [vp, C.c_int, C.POINTER(PspgParams), dp, dp, dp, dp]
+        L.orc_pspg_assemble.restype = C.c_int
+        L.orc_pspg_assemble.argtypes = [vp, C.POINTER(PspgParams), dp, dp, dp, C.c_int]
+        L.orc_pspg_get.argtypes = [vp, ip, ip, dp, dp]
+        L.orc_wc_step.argtypes = [vp, C.POINTER(WcParams), C.c_double, dp, dp]
+        L.orc_wc_next_dt.restype = C.c_double
+        L.orc_wc_next_dt.argtypes = [vp, C.POINTER(WcParams), dp]
+        L.orc_volume.restype = C.c_double
+        L.orc_volume.argtypes = [vp]
+        L.orc_wc_mass.restype = C.c_double
+        L.orc_wc_mass.argtypes = [vp, dp]
+        L.orc_tip.restype = C.c_double
+        L.orc_tip.argtypes = [vp, C.c_int, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def set_threads(n):
+    lib().orc_set_num_threads(int(n))
+
+
+def num_threads():
+    return lib().orc_num_threads()
+
+
+class OracleMesh:
+    """The reference's `Mesh` as far as the hot path uses it: node positions (with a saved
+    copy), flags, connectivity and per-element J/detJ/invJ."""
+
+    def __init__(self, mesh):
+        self.dim, self.N, self.E = mesh.dim, mesh.n_nodes, mesh.n_elems
+        self._pos = np.ascontiguousarray(mesh.pos, dtype=np.float64)
+        self._flags = np.ascontiguousarray(mesh.flags, dtype=np.uint8)
+        self._conn = np.ascontiguousarray(mesh.conn, dtype=np.int32)
+        self.h = lib().orc_create(self.dim, self.N, _dp(self._pos),
+                                  self._flags.ctypes.data_as(C.POINTER(C.c_uint8)), self.E, _ip(self._conn))
+        if not self.h:
+            raise ValueError("oracle: invalid mesh")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_destroy(self.h)
+            self.h = None
+
+    @property
+    def positions(self):
+        out = np.empty((self.dim, self.N))
+        lib().orc_get_positions(self.h, _dp(out))
+        return out
+
+    def set_positions(self, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        lib().orc_set_positions(self.h, _dp(pos))
+
+    def is_free(self):
+        out = np.empty(self.N, np.uint8)
+        lib().orc_get_is_free(self.h, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return out.astype(bool)
+
+    def geometry(self):
+        J = np.empty((self.E, 3, 3))
+        inv = np.empty((self.E, 3, 3))
+        det = np.empty(self.E)
+        lib().orc_get_geometry(self.h, _dp(J), _dp(det), _dp(inv))
+        return J, det, inv
+
+    def save(self):
+        lib().orc_save_nodes(self.h)
+
+    def restore(self):
+        lib().orc_restore_nodes(self.h)
+
+    def update_from_save(self, delta):
+        delta = np.ascontiguousarray(delta, dtype=np.float64)
+        lib().orc_update_positions_from_save(self.h, _dp(delta))
+
+    def volume(self):
+        return lib().orc_volume(self.h)
+
+    def tip(self, coord=0, want_max=True):
+        return lib().orc_tip(self.h, coord, int(want_max))
+
+
+def pspg_params(rho, mu, dt, g):
+    p = PspgParams()
+    p.rho, p.mu, p.dt = rho, mu, dt
+    for i, x in enumerate(g):
+        p.g[i] = x
+    return p
+
+
+def pspg_element(om, e, rho, mu, dt, g, q_iter, q_prev):
+    npe = om.dim + 1
+    nt = (om.dim + 1) * npe
+    Ae = np.empty((nt, nt))
+    be = np.empty(nt)
+    p = pspg_params(rho, mu, dt, g)
+    lib().orc_pspg_element(om.h, e, C.byref(p), _dp(np.ascontiguousarray(q_iter, float)),
+                           _dp(np.ascontiguousarray(q_prev, float)), _dp(Ae), _dp(be))
+    return Ae, be
+
+
+def pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc=None, apply_bc=True):
+    """A (scipy CSC, Eigen's storage order) and b of m_buildAbPSPG (+ m_applyBCPSPG)."""
+    import scipy.sparse as sp
+
+    R = (om.dim + 1) * om.N
+    if vbc is None:
+        vbc = np.zeros(om.dim * om.N)
+    p = pspg_params(rho, mu, dt, g)
+    q_iter = np.ascontiguousarray(q_iter, float)
+    q_prev = np.ascontiguousarray(q_prev, float)
+    vbc = np.ascontiguousarray(vbc, float)
+    nnz = lib().orc_pspg_assemble(om.h, C.byref(p), _dp(q_iter), _dp(q_prev), _dp(vbc), int(apply_bc))
+    colptr = np.empty(R + 1, np.int32)
+    rowidx = np.empty(nnz, np.int32)
+    vals = np.empty(nnz)
+    b = np.empty(R)
+    lib().orc_pspg_get(om.h, _ip(colptr), _ip(rowidx), _dp(vals), _dp(b))
+    return sp.csc_matrix((vals, rowidx, colptr), shape=(R, R)), b
+
+
+class PicardResult:
+    def __init__(self):
+        self.converged = False
+        self.iterations = 0
+        self.residuals = []
+        self.times = {}
+
+
+def _tick(times, key, t0):
+    times[key] = times.get(key, 0.0) + time.perf_counter() - t0
+
+
+def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=None, max_iter=10,
+                     min_res=1e-6, times=None):
+    """One `MomContEqIncompNewton::solve` with PSPG (Picard, residual "Ax_f").
+
+    Mutates the oracle mesh positions.  Returns (q, PicardResult); on failure the positions
+    are restored and q is q_prev (the node states are restored with the node list in the
+    reference, `Mesh::restoreNodesList`)."""
+    from scipy.sparse.linalg import splu
+
+    res = PicardResult()
+    times = res.times if times is None else times
+    g = tuple(g) + (0.0,) * (3 - len(g))
+    q_prev = np.asarray(q_prev, float)
+    # prepare (:264-277)
+    t0 = time.perf_counter()
+    om.save()
+    _tick(times, "Save/restore nodelist", t0)
+    t0 = time.perf_counter()
+    A, b = pspg_assemble(om, rho, mu, dt, g, q_prev, q_prev, vbc)
+    _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
+    q_iter = np.zeros_like(q_prev)
+    r = float("inf")
+    it = 0
+    while r > min_res:
+        if it > max_iter:
+            om.restore()
+            res.iterations = it
+            return q_prev.copy(), res
+        # solve closure (:278-313)
+        t0 = time.perf_counter()
+        try:
+            lu = splu(A, permc_spec="COLAMD")
+        except RuntimeError:
+            _tick(times, "Factorize A matrix", t0)
+            om.restore()
+            res.iterations = it
+            return q_prev.copy(), res
+        _tick(times, "Factorize A matrix", t0)
+        t0 = time.perf_counter()
+        q_iter = lu.solve(b)
+        _tick(times, "Solve system", t0)
+        t0 = time.perf_counter()
+        om.update_from_save(q_iter * dt)
+        _tick(times, "Update solutions", t0)
+        t0 = time.perf_counter()
+        A, b = pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc)
+        _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
+        # residual closure, "Ax_f" (:366-371)
+        t0 = time.perf_counter()
+        r = float(np.linalg.norm(A @ q_iter - b))
+        _tick(times, "Compute Picard Algo residual", t0)
+        res.residuals.append(r)
+        if np.isnan(r):
+            om.restore()
+            res.iterations = it + 1
+            return q_prev.copy(), res
+        it += 1
+    res.converged = True
+    res.iterations = it
+    return q_iter, res
+
+
+def wc_params(K0=2.2e7, K0p=7.0, rho_star=1000.0, mu=1e-3, g=(0.0, -9.81), meduri=True, sc=0.3, max_dt=1e-3):
+    p = WcParams()
+    p.K0, p.K0p, p.rhoStar, p.mu = K0, K0p, rho_star, mu
+    gg = tuple(g) + (0.0,) * (3 - len(g))
+    for i in range(3):
+        p.g[i] = gg[i]
+    p.meduri = int(meduri)
+    p.sc = sc
+    p.maxDT = max_dt
+    return p
+
+
+def wc_step(om, params, dt, states, vbc=None):
+    """In-place WC explicit step (CDS_dpdt) on `states` (float64, (2d+2)*N)."""
+    if vbc is None:
+        vbc = np.zeros(om.dim * om.N)
+    assert states.dtype == np.float64 and states.flags.c_contiguous
+    lib().orc_wc_step(om.h, C.byref(params), float(dt), _dp(states), _dp(np.ascontiguousarray(vbc, float)))
+
+
+def wc_next_dt(om, params, states):
+    return lib().orc_wc_next_dt(om.h, C.byref(params), _dp(np.ascontiguousarray(states, float)))
+
+
+def wc_mass(om, states):
+    return lib().orc_wc_mass(om.h, _dp(np.ascontiguousarray(states, float)))
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

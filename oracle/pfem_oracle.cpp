@@ -1,0 +1,880 @@
+// PFEM per-time-step oracle: an FP64 CPU restatement of the reference's hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker that the GPU library is compared
+// against (tests/, __graft_entry__.smoke(), bench.py's cpu_baseline / --impl reference leg).
+// No product code path links or calls it.
+//
+// Parity status: UNPINNED.  The reference (ImperatorS79/PFEM) ships no tests, golden
+// vectors or fixtures, and it cannot be built here (Eigen, CGAL, gmsh, sol2 and Lua are
+// absent).  This restatement follows the cited reference lines; its element matrices are
+// additionally checked against closed forms (tests/golden/make_golden.py).
+//
+// Every function cites the reference file:line it restates.  Paths are relative to the
+// reference project root.  OpenMP is used at the reference's own parallel sites; the
+// serial loops (triplet collapse, RHS scatter, WC scatters) stay serial because their
+// order defines the floating-point summation order.
+//
+// Layouts (shared with the GPU library):
+//   positions  pos[d*N + n]                     (structure of arrays)
+//   connectivity conn[k*E + e], k = 0..dim      (structure of arrays)
+//   incompressible states q[f*N + n], f = 0..dim (v_0..v_{d-1}, p)   StatesFromToQ.hpp:9-34
+//   WC states s[f*N + n], f = 0..2d+1 (v, p, rho, a)                 WCompNewton/Problem.cpp:18
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr uint8_t BOUND = 1, FREE_SURFACE = 2, FIXED = 4, DIRICHLET = 8;
+
+// ---------------------------------------------------------------------------------------
+// Gauss tables: srcs/mesh/Mesh.cpp:342-530 (values copied as the reference states them)
+// ---------------------------------------------------------------------------------------
+struct GaussTable {
+    int n;
+    double pts[4][3];
+    double w[4];
+    double sf[4][4];     // shape functions at each point (Mesh::getShapeFunctions)
+    double refSize;
+};
+
+GaussTable gaussTable(int dim) {
+    GaussTable t{};
+    if (dim == 2) {
+        t.n = 3;
+        const double p[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}, {2.0 / 3.0, 1.0 / 6.0}};
+        for (int g = 0; g < 3; ++g) {
+            t.pts[g][0] = p[g][0];
+            t.pts[g][1] = p[g][1];
+            t.w[g] = 1.0 / 3.0;
+            t.sf[g][0] = 1 - p[g][0] - p[g][1];
+            t.sf[g][1] = p[g][0];
+            t.sf[g][2] = p[g][1];
+        }
+        t.refSize = 0.5;
+    } else {
+        t.n = 4;
+        const double a = 0.585410196624968, b = 0.138196601125011;
+        const double p[4][3] = {{a, b, b}, {b, a, b}, {b, b, a}, {b, b, b}};
+        for (int g = 0; g < 4; ++g) {
+            for (int k = 0; k < 3; ++k) t.pts[g][k] = p[g][k];
+            t.w[g] = 0.25;
+            t.sf[g][0] = 1 - p[g][0] - p[g][1] - p[g][2];
+            t.sf[g][1] = p[g][0];
+            t.sf[g][2] = p[g][1];
+            t.sf[g][3] = p[g][2];
+        }
+        t.refSize = 0.16666666666666666666666666666667;
+    }
+    return t;
+}
+
+// Small dense row-major matrix with runtime sizes up to 16x16.
+struct Mat {
+    int r = 0, c = 0;
+    double a[16 * 16];
+    Mat() {}
+    Mat(int rr, int cc) : r(rr), c(cc) { std::memset(a, 0, sizeof(a)); }
+    double& operator()(int i, int j) { return a[i * 16 + j]; }
+    double operator()(int i, int j) const { return a[i * 16 + j]; }
+};
+
+Mat mul(const Mat& A, const Mat& B) {
+    Mat C(A.r, B.c);
+    for (int i = 0; i < A.r; ++i)
+        for (int j = 0; j < B.c; ++j) {
+            double s = 0;
+            for (int k = 0; k < A.c; ++k) s += A(i, k) * B(k, j);
+            C(i, j) = s;
+        }
+    return C;
+}
+
+Mat transpose(const Mat& A) {
+    Mat T(A.c, A.r);
+    for (int i = 0; i < A.r; ++i)
+        for (int j = 0; j < A.c; ++j) T(j, i) = A(i, j);
+    return T;
+}
+
+struct ElemGeom {
+    double J[3][3];
+    double invJ[3][3];
+    double detJ;
+};
+
+struct PspgParams {
+    double rho, mu, dt;
+    double g[3];
+};
+
+struct WcParams {
+    double K0, K0p, rhoStar, mu;
+    double g[3];
+    int meduri;        // ContEq stabilization "Meduri" (1) or "None" (0)
+    double sc;         // securityCoeff
+    double maxDT;
+};
+
+}  // namespace
+
+struct OrcMesh {
+    int dim, N, E, npe;
+    std::vector<double> pos, posSave;
+    std::vector<uint8_t> flags;
+    std::vector<uint8_t> isFree;
+    std::vector<int32_t> conn;
+    std::vector<ElemGeom> geom;
+    GaussTable gt;
+    // assembled PSPG system, Eigen column-major (CSC) storage
+    std::vector<int32_t> colptr, rowidx;
+    std::vector<double> vals, b;
+
+    bool bound(int n) const { return flags[n] & BOUND; }
+    bool fixed(int n) const { return flags[n] & FIXED; }
+    bool dirichlet(int n) const { return (flags[n] & BOUND) && (flags[n] & DIRICHLET); }
+    int node(int e, int k) const { return conn[(size_t)k * E + e]; }
+    double x(int n, int d) const { return pos[(size_t)d * N + n]; }
+};
+
+namespace {
+
+// Element::computeJ / computeDetJ / computeInvJ, srcs/mesh/Element.cpp:15-135
+void computeGeometry(const OrcMesh& m, int e, ElemGeom& g) {
+    std::memset(&g, 0, sizeof(g));
+    if (m.dim == 2) {
+        int n0 = m.node(e, 0), n1 = m.node(e, 1), n2 = m.node(e, 2);
+        double x0 = m.x(n0, 0), x1 = m.x(n1, 0), x2 = m.x(n2, 0);
+        double y0 = m.x(n0, 1), y1 = m.x(n1, 1), y2 = m.x(n2, 1);
+        g.J[0][0] = x1 - x0; g.J[0][1] = x2 - x0;
+        g.J[1][0] = y1 - y0; g.J[1][1] = y2 - y0;
+        g.detJ = g.J[0][0] * g.J[1][1] - g.J[1][0] * g.J[0][1];
+        g.invJ[0][0] = g.J[1][1] / g.detJ;
+        g.invJ[0][1] = -g.J[0][1] / g.detJ;
+        g.invJ[1][0] = -g.J[1][0] / g.detJ;
+        g.invJ[1][1] = g.J[0][0] / g.detJ;
+    } else {
+        int nn[4] = {m.node(e, 0), m.node(e, 1), m.node(e, 2), m.node(e, 3)};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) g.J[r][c] = m.x(nn[c + 1], r) - m.x(nn[0], r);
+        auto& J = g.J;
+        g.detJ = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] + J[0][2] * J[1][0] * J[2][1]
+               - J[2][0] * J[1][1] * J[0][2] - J[2][1] * J[1][2] * J[0][0] - J[2][2] * J[1][0] * J[0][1];
+        double d = g.detJ;
+        g.invJ[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / d;
+        g.invJ[0][1] = (J[2][1] * J[0][2] - J[2][2] * J[0][1]) / d;
+        g.invJ[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / d;
+        g.invJ[1][0] = (J[2][0] * J[1][2] - J[1][0] * J[2][2]) / d;
+        g.invJ[1][1] = (J[0][0] * J[2][2] - J[2][0] * J[0][2]) / d;
+        g.invJ[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) / d;
+        g.invJ[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) / d;
+        g.invJ[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) / d;
+        g.invJ[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) / d;
+    }
+}
+
+// Mesh::updateNodesPosition* element loop, srcs/mesh/Mesh.cpp:1258-1264
+void computeAllGeometry(OrcMesh& m) {
+#pragma omp parallel for
+    for (int e = 0; e < m.E; ++e) computeGeometry(m, e, m.geom[e]);
+}
+
+// MatrixBuilder::getGradN, srcs/simulation/matricesBuilder/MatricesBuilder.inl:92-127
+Mat getGradN(int dim, const ElemGeom& g) {
+    Mat G(dim, dim + 1);
+    for (int r = 0; r < dim; ++r) {
+        double s = 0;
+        for (int k = 0; k < dim; ++k) s += g.invJ[k][r];
+        G(r, 0) = -s;
+        for (int k = 0; k < dim; ++k) G(r, k + 1) = g.invJ[k][r];
+    }
+    return G;
+}
+
+// MatrixBuilder::getB (Voigt strain rate), MatricesBuilder.inl:129-164
+Mat getB(int dim, const Mat& G) {
+    const int npe = dim + 1;
+    if (dim == 2) {
+        Mat B(3, 6);
+        for (int j = 0; j < 3; ++j) {
+            B(0, j) = B(2, 3 + j) = G(0, j);
+            B(1, 3 + j) = B(2, j) = G(1, j);
+        }
+        return B;
+    }
+    Mat B(6, 12);
+    for (int j = 0; j < npe; ++j) {
+        B(0, j) = B(3, 4 + j) = B(4, 8 + j) = G(0, j);
+        B(1, 4 + j) = B(3, j) = B(5, 8 + j) = G(1, j);
+        B(2, 8 + j) = B(4, j) = B(5, 4 + j) = G(2, j);
+    }
+    return B;
+}
+
+// N row at Gauss point g and Ntilde (dim x dim*npe), MatricesBuilder.inl:5-84
+Mat getNtilde(int dim, const GaussTable& t, int g) {
+    Mat Nt(dim, dim * (dim + 1));
+    for (int f = 0; f < dim; ++f)
+        for (int j = 0; j <= dim; ++j) Nt(f, f * (dim + 1) + j) = t.sf[g][j];
+    return Nt;
+}
+
+double nDot(const GaussTable& t, int g, const double* vals, int npe) {
+    double s = 0;
+    for (int j = 0; j < npe; ++j) s += t.sf[g][j] * vals[j];
+    return s;
+}
+
+// getM with a per-Gauss-point factor, MatricesBuilder.inl:216-229
+template <class F>
+Mat getM(const OrcMesh& m, const ElemGeom& geo, F factor) {
+    const int npe = m.npe;
+    Mat M(npe, npe);
+    for (int g = 0; g < m.gt.n; ++g) {
+        double f = factor(g) * m.gt.w[g];
+        for (int i = 0; i < npe; ++i)
+            for (int j = 0; j < npe; ++j) M(i, j) += f * m.gt.sf[g][i] * m.gt.sf[g][j];
+    }
+    double s = geo.detJ * m.gt.refSize;
+    for (int i = 0; i < npe; ++i)
+        for (int j = 0; j < npe; ++j) M(i, j) *= s;
+    return M;
+}
+
+// getK = |e| * (sum_g f w) * B^T Ddev B, MatricesBuilder.inl:276-290
+Mat getK(const OrcMesh& m, const ElemGeom& geo, double factorSum, const Mat& B, const Mat& ddev) {
+    Mat K = mul(mul(transpose(B), ddev), B);
+    double s = geo.detJ * m.gt.refSize * factorSum;
+    for (int i = 0; i < K.r; ++i)
+        for (int j = 0; j < K.c; ++j) K(i, j) *= s;
+    return K;
+}
+
+// getD = |e| * (sum_g f w N^T) m^T B, MatricesBuilder.inl:292-306
+template <class F>
+Mat getD(const OrcMesh& m, const ElemGeom& geo, F factor, const Mat& B) {
+    const int npe = m.npe, dim = m.dim;
+    double sumWNT[4] = {0, 0, 0, 0};
+    for (int g = 0; g < m.gt.n; ++g) {
+        double f = factor(g) * m.gt.w[g];
+        for (int i = 0; i < npe; ++i) sumWNT[i] += f * m.gt.sf[g][i];
+    }
+    // m^T B : m = [1,...,1 (dim), 0, ...]
+    double mB[12];
+    for (int j = 0; j < dim * npe; ++j) {
+        double s = 0;
+        for (int k = 0; k < dim; ++k) s += B(k, j);
+        mB[j] = s;
+    }
+    Mat D(npe, dim * npe);
+    double s = geo.detJ * m.gt.refSize;
+    for (int i = 0; i < npe; ++i)
+        for (int j = 0; j < dim * npe; ++j) D(i, j) = s * sumWNT[i] * mB[j];
+    return D;
+}
+
+// getC = |e| gradN^T (sum_g f w Ntilde_g), MatricesBuilder.inl:324-338
+Mat getC(const OrcMesh& m, const ElemGeom& geo, double factor, const Mat& G) {
+    const int npe = m.npe, dim = m.dim;
+    Mat sumNW(dim, dim * npe);
+    for (int g = 0; g < m.gt.n; ++g) {
+        Mat Nt = getNtilde(dim, m.gt, g);
+        for (int r = 0; r < dim; ++r)
+            for (int c = 0; c < dim * npe; ++c) sumNW(r, c) += factor * Nt(r, c) * m.gt.w[g];
+    }
+    Mat C = mul(transpose(G), sumNW);
+    double s = geo.detJ * m.gt.refSize;
+    for (int i = 0; i < C.r; ++i)
+        for (int j = 0; j < C.c; ++j) C(i, j) *= s;
+    return C;
+}
+
+// getL = |e| (sum_g f w) gradN^T gradN, MatricesBuilder.inl:308-322
+Mat getL(const OrcMesh& m, const ElemGeom& geo, double factorSum, const Mat& G) {
+    Mat L = mul(transpose(G), G);
+    double s = geo.detJ * m.gt.refSize * factorSum;
+    for (int i = 0; i < L.r; ++i)
+        for (int j = 0; j < L.c; ++j) L(i, j) *= s;
+    return L;
+}
+
+// getF = |e| sum_g f w Ntilde_g^T vec, MatricesBuilder.inl:340-355
+template <class F>
+void getF(const OrcMesh& m, const ElemGeom& geo, F factor, const double* vec, double* out) {
+    const int npe = m.npe, dim = m.dim;
+    for (int i = 0; i < dim * npe; ++i) out[i] = 0;
+    for (int g = 0; g < m.gt.n; ++g) {
+        Mat Nt = getNtilde(dim, m.gt, g);
+        double f = factor(g) * m.gt.w[g];
+        for (int c = 0; c < dim * npe; ++c) {
+            double s = 0;
+            for (int r = 0; r < dim; ++r) s += Nt(r, c) * vec[r];
+            out[c] += f * s;
+        }
+    }
+    double s = geo.detJ * m.gt.refSize;
+    for (int i = 0; i < dim * npe; ++i) out[i] *= s;
+}
+
+// getH = |e| sum_g f w gradN^T vec, MatricesBuilder.inl:372-386
+void getH(const OrcMesh& m, const ElemGeom& geo, double factor, const Mat& G, const double* vec, double* out) {
+    const int npe = m.npe, dim = m.dim;
+    for (int i = 0; i < npe; ++i) out[i] = 0;
+    for (int g = 0; g < m.gt.n; ++g) {
+        for (int i = 0; i < npe; ++i) {
+            double s = 0;
+            for (int r = 0; r < dim; ++r) s += G(r, i) * vec[r];
+            out[i] += factor * s * m.gt.w[g];
+        }
+    }
+    double s = geo.detJ * m.gt.refSize;
+    for (int i = 0; i < npe; ++i) out[i] *= s;
+}
+
+Mat ddevIncomp(int dim) {  // MomContEquation.inl:73-94 (file offsets of the .inl)
+    int nv = dim == 2 ? 3 : 6;
+    Mat D(nv, nv);
+    for (int i = 0; i < dim; ++i) D(i, i) = 2;
+    for (int i = dim; i < nv; ++i) D(i, i) = 1;
+    return D;
+}
+
+Mat ddevWC(int dim) {  // WCompNewton/MomEquation.inl:63-83
+    int nv = dim == 2 ? 3 : 6;
+    Mat D(nv, nv);
+    for (int i = 0; i < dim; ++i)
+        for (int j = 0; j < dim; ++j) D(i, j) = (i == j) ? 4.0 / 3 : -2.0 / 3;
+    for (int i = dim; i < nv; ++i) D(i, i) = 1;
+    return D;
+}
+
+// MomContEqIncompNewton::m_computeTauPSPG, MomContEquationPSPG.inl:237-259
+double computeTau(const OrcMesh& m, int e, const ElemGeom& geo, const PspgParams& p, const double* q) {
+    const double h = std::sqrt(m.gt.refSize * geo.detJ / M_PI);
+    double U = 0;
+    for (int k = 0; k < m.npe; ++k) {
+        int n = m.node(e, k);
+        double nodeU = 0;
+        for (int d = 0; d < m.dim; ++d) {
+            double v = q[(size_t)d * m.N + n];
+            nodeU += v * v;
+        }
+        U += std::sqrt(nodeU);
+    }
+    U /= (m.dim + 1);
+    const double dt = p.dt;
+    return 1 / std::sqrt((2 / dt) * (2 / dt) + (2 * U / h) * (2 * U / h)
+                         + 9 * (4 * p.mu / (h * h * p.rho)) * (4 * p.mu / (h * h * p.rho)));
+}
+
+// Element matrix Ae ((d+1)npe)^2 and vector be of m_buildAbPSPG, MomContEquationPSPG.inl:26-53
+void pspgElement(const OrcMesh& m, int e, const PspgParams& p, const double* qIter, const double* qPrev,
+                 Mat& Ae, double* be) {
+    const int dim = m.dim, npe = m.npe;
+    const ElemGeom& geo = m.geom[e];
+    const double dt = p.dt;
+    double tau = computeTau(m, e, geo, p, qIter);
+    Mat G = getGradN(dim, geo);
+    Mat B = getB(dim, G);
+    Mat Ms = getM(m, geo, [&](int) { return p.rho; });
+    for (int i = 0; i < npe; ++i)
+        for (int j = 0; j < npe; ++j) Ms(i, j) *= (1 / dt);
+    double sumW = 0;
+    for (int g = 0; g < m.gt.n; ++g) sumW += p.mu * m.gt.w[g];
+    Mat K = getK(m, geo, sumW, B, ddevIncomp(dim));
+    Mat D = getD(m, geo, [](int) { return 1.0; }, B);
+    Mat C = getC(m, geo, 1.0, G);
+    for (int i = 0; i < C.r; ++i)
+        for (int j = 0; j < C.c; ++j) C(i, j) *= (tau / dt);
+    double lsum = 0;
+    for (int g = 0; g < m.gt.n; ++g) lsum += (1 / p.rho) * m.gt.w[g];
+    Mat L = getL(m, geo, lsum, G);
+    double Fe[12], He[4];
+    getF(m, geo, [&](int) { return p.rho; }, p.g, Fe);
+    getH(m, geo, 1.0, G, p.g, He);
+    for (int i = 0; i < npe; ++i) He[i] *= tau;
+
+    const int nv = dim * npe, nt = (dim + 1) * npe;
+    Ae = Mat(nt, nt);
+    // [Me_dt + Ke, -De^T ; Ce_dt + De, tau*Le]
+    for (int i = 0; i < nv; ++i)
+        for (int j = 0; j < nv; ++j) {
+            double md = ((i / npe) == (j / npe)) ? Ms(i % npe, j % npe) : 0.0;
+            Ae(i, j) = md + K(i, j);
+        }
+    for (int i = 0; i < nv; ++i)
+        for (int j = 0; j < npe; ++j) Ae(i, nv + j) = -D(j, i);
+    for (int i = 0; i < npe; ++i)
+        for (int j = 0; j < nv; ++j) Ae(nv + i, j) = C(i, j) + D(i, j);
+    for (int i = 0; i < npe; ++i)
+        for (int j = 0; j < npe; ++j) Ae(nv + i, nv + j) = tau * L(i, j);
+
+    double vPrev[12];
+    for (int f = 0; f < dim; ++f)
+        for (int k = 0; k < npe; ++k) vPrev[f * npe + k] = qPrev[(size_t)f * m.N + m.node(e, k)];
+    for (int i = 0; i < nv; ++i) {
+        double s = 0;
+        for (int j = 0; j < nv; ++j) {
+            double md = ((i / npe) == (j / npe)) ? Ms(i % npe, j % npe) : 0.0;
+            s += md * vPrev[j];
+        }
+        be[i] = Fe[i] + s;
+    }
+    for (int i = 0; i < npe; ++i) {
+        double s = 0;
+        for (int j = 0; j < nv; ++j) s += C(i, j) * vPrev[j];
+        be[nv + i] = He[i] + s;
+    }
+}
+
+struct Triplet {
+    int32_t row, col;
+    double val;
+};
+
+}  // namespace
+
+extern "C" {
+
+OrcMesh* orc_create(int dim, int N, const double* pos, const uint8_t* flags, int E, const int32_t* conn) {
+    if ((dim != 2 && dim != 3) || N <= 0 || E < 0) return nullptr;
+    OrcMesh* m = new OrcMesh();
+    m->dim = dim;
+    m->N = N;
+    m->E = E;
+    m->npe = dim + 1;
+    m->pos.assign(pos, pos + (size_t)dim * N);
+    m->posSave = m->pos;
+    m->flags.assign(flags, flags + N);
+    m->conn.assign(conn, conn + (size_t)(dim + 1) * E);
+    m->isFree.assign(N, 1);
+    for (size_t i = 0; i < m->conn.size(); ++i) m->isFree[m->conn[i]] = 0;
+    m->geom.resize(E);
+    m->gt = gaussTable(dim);
+    computeAllGeometry(*m);
+    return m;
+}
+
+void orc_destroy(OrcMesh* m) { delete m; }
+
+int orc_num_threads() {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+void orc_get_positions(const OrcMesh* m, double* out) { std::copy(m->pos.begin(), m->pos.end(), out); }
+
+void orc_set_positions(OrcMesh* m, const double* in) {
+    std::copy(in, in + m->pos.size(), m->pos.begin());
+    computeAllGeometry(*m);
+}
+
+void orc_get_is_free(const OrcMesh* m, uint8_t* out) { std::copy(m->isFree.begin(), m->isFree.end(), out); }
+
+// Element geometry export: J (9 per element, row-major 3x3), detJ, invJ (9 per element).
+void orc_get_geometry(const OrcMesh* m, double* J, double* detJ, double* invJ) {
+    for (int e = 0; e < m->E; ++e) {
+        const ElemGeom& g = m->geom[e];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                J[9 * e + 3 * r + c] = g.J[r][c];
+                invJ[9 * e + 3 * r + c] = g.invJ[r][c];
+            }
+        detJ[e] = g.detJ;
+    }
+}
+
+// Mesh::saveNodesList / restoreNodesList (positions), srcs/mesh/Mesh.cpp:1019-1053
+void orc_save_nodes(OrcMesh* m) { m->posSave = m->pos; }
+
+void orc_restore_nodes(OrcMesh* m) {
+    m->pos = m->posSave;
+    computeAllGeometry(*m);
+}
+
+// Mesh::updateNodesPositionFromSave(Eigen::VectorXd), srcs/mesh/Mesh.cpp:1238-1277
+void orc_update_positions_from_save(OrcMesh* m, const double* delta) {
+    const int N = m->N;
+#pragma omp parallel for
+    for (int n = 0; n < N; ++n)
+        if (!m->fixed(n))
+            for (int d = 0; d < m->dim; ++d)
+                m->pos[(size_t)d * N + n] = m->posSave[(size_t)d * N + n] + delta[(size_t)d * N + n];
+    computeAllGeometry(*m);
+}
+
+// Mesh::updateNodesPosition(Eigen::VectorXd), srcs/mesh/Mesh.cpp:1101-1137
+void orc_update_positions(OrcMesh* m, const double* delta) {
+    const int N = m->N;
+#pragma omp parallel for
+    for (int n = 0; n < N; ++n)
+        if (!m->fixed(n))
+            for (int d = 0; d < m->dim; ++d) m->pos[(size_t)d * N + n] += delta[(size_t)d * N + n];
+    computeAllGeometry(*m);
+}
+
+// Element matrix/vector for one element (for known-answer tests).
+void orc_pspg_element(const OrcMesh* m, int e, const PspgParams* p, const double* qIter, const double* qPrev,
+                      double* Ae, double* be) {
+    Mat A;
+    pspgElement(*m, e, *p, qIter, qPrev, A, be);
+    for (int i = 0; i < A.r; ++i)
+        for (int j = 0; j < A.c; ++j) Ae[i * A.c + j] = A(i, j);
+}
+
+// m_buildAbPSPG (MomContEquationPSPG.inl:6-146) followed, when apply_bc != 0, by
+// m_applyBCPSPG (:148-235, gamma = 0 so no surface tension).  vbc holds the Dirichlet
+// velocity of every node (dim x N field-major; read only at Dirichlet nodes), standing in
+// for the Lua BoundaryV(pos, t + dt) call.  Returns nnz of the compressed matrix.
+int orc_pspg_assemble(OrcMesh* m, const PspgParams* p, const double* qIter, const double* qPrev, const double* vbc,
+                      int apply_bc) {
+    const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    const int R = (dim + 1) * N;
+    const size_t tripletPerElm = (size_t)(dim + 1) * npe * (dim + 1) * npe;
+    const size_t doubletPerElm = (size_t)(dim + 1) * npe;
+    // default-constructed Eigen::Triplet is (0, 0, 0.0): unassigned slots keep it (:17)
+    std::vector<Triplet> indexA(tripletPerElm * E, Triplet{0, 0, 0.0});
+    std::vector<std::pair<int32_t, double>> indexb(doubletPerElm * E);
+    m->b.assign(R, 0.0);
+
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        Mat Ae;
+        double be[16];
+        pspgElement(*m, e, *p, qIter, qPrev, Ae, be);
+        size_t countA = 0, countb = 0;
+        for (int i = 0; i < npe; ++i) {
+            const int ni = m->node(e, i);
+            const bool skipV = m->bound(ni) || m->isFree[ni];
+            for (int j = 0; j < npe; ++j) {
+                const int nj = m->node(e, j);
+                for (int d1 = 0; d1 < dim; ++d1)
+                    for (int d2 = 0; d2 <= dim; ++d2) {
+                        if (!skipV)
+                            indexA[tripletPerElm * e + countA] =
+                                Triplet{ni + d1 * N, nj + d2 * N, Ae(i + d1 * npe, j + d2 * npe)};
+                        countA++;
+                    }
+                for (int d2 = 0; d2 <= dim; ++d2) {
+                    if (!m->isFree[ni])
+                        indexA[tripletPerElm * e + countA] =
+                            Triplet{ni + dim * N, nj + d2 * N, Ae(i + dim * npe, j + d2 * npe)};
+                    countA++;
+                }
+            }
+            for (int d = 0; d <= dim; ++d) {
+                indexb[doubletPerElm * e + countb] = {ni + d * N, be[i + d * npe]};
+                countb++;
+            }
+        }
+    }
+    // identity rows of free and bound nodes (:108-128)
+    for (int n = 0; n < N; ++n) {
+        if (m->isFree[n]) indexA.push_back(Triplet{n + dim * N, n + dim * N, 1.0});
+        if (m->bound(n) || m->isFree[n])
+            for (int d = 0; d < dim; ++d) indexA.push_back(Triplet{n + d * N, n + d * N, 1.0});
+    }
+    // setFromTriplets (:136): duplicates are summed in triplet order, storage is
+    // column-major with sorted row indices.  A stable sort by (col, row) keeps triplet order
+    // inside each duplicate group, then the group is summed left to right.
+    std::vector<uint32_t> order(indexA.size());
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        const Triplet &ta = indexA[a], &tb = indexA[b];
+        return ta.col != tb.col ? ta.col < tb.col : ta.row < tb.row;
+    });
+    m->colptr.assign(R + 1, 0);
+    m->rowidx.clear();
+    m->vals.clear();
+    m->rowidx.reserve(indexA.size() / 3);
+    m->vals.reserve(indexA.size() / 3);
+    for (size_t k = 0; k < order.size();) {
+        const Triplet& t = indexA[order[k]];
+        double s = t.val;
+        size_t k2 = k + 1;
+        while (k2 < order.size() && indexA[order[k2]].col == t.col && indexA[order[k2]].row == t.row)
+            s += indexA[order[k2++]].val;
+        m->rowidx.push_back(t.row);
+        m->vals.push_back(s);
+        m->colptr[t.col + 1]++;
+        k = k2;
+    }
+    for (int c = 0; c < R; ++c) m->colptr[c + 1] += m->colptr[c];
+    // RHS scatter in doublet order (:140-144)
+    for (const auto& d : indexb) m->b[d.first] += d.second;
+
+    if (apply_bc) {
+        // m_applyBCPSPG node loop (:189-232)
+        for (int n = 0; n < N; ++n) {
+            if (m->isFree[n]) {
+                m->b[n + dim * N] = 0;
+                if (!m->bound(n))
+                    for (int d = 0; d < dim; ++d) m->b[n + d * N] = qPrev[n + (size_t)d * N] + p->dt * p->g[d];
+            }
+            if (m->dirichlet(n)) {
+                for (int d = 0; d < dim; ++d) {
+                    const double r = vbc[(size_t)d * N + n];
+                    const int col = n + d * N;
+                    m->b[col] = r;
+                    for (int k = m->colptr[col]; k < m->colptr[col + 1]; ++k) {
+                        if (m->rowidx[k] == col) continue;
+                        m->b[m->rowidx[k]] -= m->vals[k] * r;
+                        m->vals[k] = 0;
+                    }
+                }
+            }
+        }
+    }
+    return (int)m->vals.size();
+}
+
+void orc_pspg_get(const OrcMesh* m, int32_t* colptr, int32_t* rowidx, double* vals, double* b) {
+    if (colptr) std::copy(m->colptr.begin(), m->colptr.end(), colptr);
+    if (rowidx) std::copy(m->rowidx.begin(), m->rowidx.end(), rowidx);
+    if (vals) std::copy(m->vals.begin(), m->vals.end(), vals);
+    if (b) std::copy(m->b.begin(), m->b.end(), b);
+}
+
+// ---------------------------------------------------------------------------------------
+// Weakly compressible explicit step (CDS_dpdt), SolverWCompNewton::m_solveWCompNewtonNoT
+// srcs/simulation/physics/WCompNewton/Solver.cpp:236-276 without the remesh at :266-272.
+// s = [v (d), p, rho, a (d)] field-major.  vbc: Dirichlet velocities (d x N).
+// ---------------------------------------------------------------------------------------
+void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const double* vbc) {
+    const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    double* v = s;
+    double* P = s + (size_t)dim * N;
+    double* rho = s + (size_t)(dim + 1) * N;
+    double* a = s + (size_t)(dim + 2) * N;
+
+    // v1/2 = v + dt/2 a ; x += dt v1/2 (:249-253, Mesh.cpp:1101-1137)
+    std::vector<double> delta((size_t)dim * N);
+#pragma omp parallel for
+    for (int n = 0; n < N; ++n)
+        for (int d = 0; d < dim; ++d) {
+            v[(size_t)d * N + n] = v[(size_t)d * N + n] + 0.5 * dt * a[(size_t)d * N + n];
+            delta[(size_t)d * N + n] = v[(size_t)d * N + n] * dt;
+        }
+    orc_update_positions(m, delta.data());
+
+    // ContEqWCompNewton::m_buildSystemdpdt, ContEquation.inl:353-413
+    std::vector<double> MeL((size_t)E * npe), F0e((size_t)E * npe);
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        const ElemGeom& geo = m->geom[e];
+        Mat Me = getM(*m, geo, [](int) { return 1.0; });
+        double Pe[4], Ve[12];
+        for (int k = 0; k < npe; ++k) Pe[k] = P[m->node(e, k)];
+        for (int f = 0; f < dim; ++f)
+            for (int k = 0; k < npe; ++k) Ve[f * npe + k] = v[(size_t)f * N + m->node(e, k)];
+        Mat G = getGradN(dim, geo);
+        Mat B = getB(dim, G);
+        Mat D = getD(*m, geo, [&](int g) { return p->K0 + p->K0p * nDot(m->gt, g, Pe, npe); }, B);
+        for (int i = 0; i < npe; ++i) {
+            double lumped = 0;
+            for (int j = 0; j < npe; ++j) lumped += Me(i, j);
+            MeL[(size_t)e * npe + i] = lumped;
+            double dv = 0;
+            for (int j = 0; j < dim * npe; ++j) dv += D(i, j) * Ve[j];
+            double f = -dt * dv;
+            if (p->meduri) {
+                double mp = 0;
+                for (int j = 0; j < npe; ++j) mp += Me(i, j) * Pe[j];
+                f += mp;
+            } else {
+                f += lumped * Pe[i];
+            }
+            F0e[(size_t)e * npe + i] = f;
+        }
+    }
+    std::vector<double> invM(N, 0.0), F0(N, 0.0);
+    for (int e = 0; e < E; ++e)
+        for (int i = 0; i < npe; ++i) {
+            invM[m->node(e, i)] += MeL[(size_t)e * npe + i];
+            F0[m->node(e, i)] += F0e[(size_t)e * npe + i];
+        }
+    for (int n = 0; n < N; ++n) invM[n] = 1 / invM[n];
+    // m_applyBCdpdt (:334-351)
+    for (int n = 0; n < N; ++n)
+        if (m->isFree[n]) {
+            F0[n] = 0;
+            invM[n] = 1;
+        }
+    // p = invM F0 ; rho from Tait-Murnaghan (:139-146, :319-332)
+#pragma omp parallel for
+    for (int n = 0; n < N; ++n) {
+        P[n] = invM[n] * F0[n];
+        rho[n] = std::pow((p->K0p / p->K0) * P[n] + 1, 1 / p->K0p) * p->rhoStar;
+    }
+
+    // MomEqWCompNewton::m_buildSystem, MomEquation.inl:229-302
+    Mat ddev = ddevWC(dim);
+    std::vector<double> MeD((size_t)E * dim * npe), FT((size_t)E * dim * npe);
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        const ElemGeom& geo = m->geom[e];
+        double Pe[4], Re[4], Ve[12];
+        for (int k = 0; k < npe; ++k) {
+            Pe[k] = P[m->node(e, k)];
+            Re[k] = rho[m->node(e, k)];
+        }
+        for (int f = 0; f < dim; ++f)
+            for (int k = 0; k < npe; ++k) Ve[f * npe + k] = v[(size_t)f * N + m->node(e, k)];
+        Mat G = getGradN(dim, geo);
+        Mat B = getB(dim, G);
+        Mat Mt = getM(*m, geo, [&](int g) { return nDot(m->gt, g, Re, npe); });
+        double sumMu = 0;
+        for (int g = 0; g < m->gt.n; ++g) sumMu += p->mu * m->gt.w[g];
+        Mat K = getK(*m, geo, sumMu, B, ddev);
+        Mat D = getD(*m, geo, [](int) { return 1.0; }, B);
+        double Fe[12];
+        getF(*m, geo, [&](int g) { return nDot(m->gt, g, Re, npe); }, p->g, Fe);
+        for (int r = 0; r < dim * npe; ++r) {
+            int i = r % npe;
+            double lumped = 0;  // diagBlock + lump: row sum of the scalar block
+            for (int j = 0; j < npe; ++j) lumped += Mt(i, j);
+            MeD[(size_t)e * dim * npe + r] = lumped;
+            double kv = 0;
+            for (int c = 0; c < dim * npe; ++c) kv += K(r, c) * Ve[c];
+            double dp = 0;
+            for (int j = 0; j < npe; ++j) dp += D(j, r) * Pe[j];
+            FT[(size_t)e * dim * npe + r] = -kv + dp + Fe[r];
+        }
+    }
+    std::vector<double> invMv((size_t)dim * N, 0.0), F((size_t)dim * N, 0.0);
+    for (int e = 0; e < E; ++e)
+        for (int i = 0; i < npe; ++i)
+            for (int d = 0; d < dim; ++d) {
+                int n = m->node(e, i);
+                invMv[n + (size_t)d * N] += MeD[(size_t)e * dim * npe + i + d * npe];
+                F[n + (size_t)d * N] += FT[(size_t)e * dim * npe + i + d * npe];
+            }
+    for (size_t k = 0; k < invMv.size(); ++k) invMv[k] = 1 / invMv[k];
+    // m_applyBC (:305-374), gamma = 0
+    for (int n = 0; n < N; ++n) {
+        if (m->isFree[n] && !m->bound(n)) {
+            for (int d = 0; d < dim; ++d) {
+                F[n + (size_t)d * N] = p->g[d];
+                invMv[n + (size_t)d * N] = 1;
+            }
+        } else if (m->dirichlet(n)) {
+            for (int d = 0; d < dim; ++d) {
+                F[n + (size_t)d * N] = vbc[(size_t)d * N + n];
+                invMv[n + (size_t)d * N] = 1;
+            }
+        }
+    }
+    // a = invM F ; v = v1/2 + dt/2 a (:216-222)
+#pragma omp parallel for
+    for (int n = 0; n < N; ++n)
+        for (int d = 0; d < dim; ++d) {
+            size_t k = n + (size_t)d * N;
+            double acc = invMv[k] * F[k];
+            a[k] = acc;
+            v[k] = v[k] + 0.5 * dt * acc;
+        }
+}
+
+// SolverWCompNewton::computeNextDT, WCompNewton/Solver.cpp:192-234 (adaptDT = true).
+double orc_wc_next_dt(const OrcMesh* m, const WcParams* p, const double* s) {
+    const int dim = m->dim, N = m->N, E = m->E, npe = m->npe;
+    const double* v = s;
+    const double* P = s + (size_t)dim * N;
+    const double* rho = s + (size_t)(dim + 1) * N;
+    double dt2 = std::numeric_limits<double>::max();
+#pragma omp parallel for reduction(min : dt2)
+    for (int e = 0; e < E; ++e) {
+        // Element::getRin, Element.cpp:226-294
+        double he;
+        const ElemGeom& geo = m->geom[e];
+        double size = geo.detJ * m->gt.refSize;
+        auto dist = [&](int a, int b) {
+            double s2 = 0;
+            for (int d = 0; d < dim; ++d) {
+                double t = m->x(a, d) - m->x(b, d);
+                s2 += t * t;
+            }
+            return std::sqrt(s2);
+        };
+        int n0 = m->node(e, 0), n1 = m->node(e, 1), n2 = m->node(e, 2);
+        if (dim == 2) {
+            double sp = (dist(n0, n1) + dist(n1, n2) + dist(n0, n2)) / 2;
+            he = 2 * (size / sp);
+        } else {
+            int n3 = m->node(e, 3);
+            auto X = [&](int n, int d) { return m->x(n, d); };
+            auto nrm = [&](int a0, int a1, int a2) {  // |(a1-a0) x (a2-a0)|
+                double ux = X(a1, 0) - X(a0, 0), uy = X(a1, 1) - X(a0, 1), uz = X(a1, 2) - X(a0, 2);
+                double wx = X(a2, 0) - X(a0, 0), wy = X(a2, 1) - X(a0, 1), wz = X(a2, 2) - X(a0, 2);
+                double cx = uy * wz - uz * wy, cy = uz * wx - ux * wz, cz = ux * wy - uy * wx;
+                return std::sqrt(cx * cx + cy * cy + cz * cz);
+            };
+            double sum = nrm(n0, n1, n2) + nrm(n0, n3, n2) + nrm(n0, n1, n3) + nrm(n3, n1, n2);
+            he = 2 * (6 * size / sum);
+        }
+        double maxSq = 0;
+        for (int k = 0; k < npe; ++k) {
+            int n = m->node(e, k);
+            double c2 = (p->K0 + p->K0p * P[n]) / rho[n];
+            double u2 = 0;
+            for (int d = 0; d < dim; ++d) u2 += v[(size_t)d * N + n] * v[(size_t)d * N + n];
+            double alpha = p->mu / rho[n];
+            maxSq = std::max(std::max(u2, c2), maxSq);
+            maxSq = std::max(maxSq, 4 * alpha * alpha / (he * he));
+        }
+        dt2 = std::min(dt2, p->sc * p->sc * he * he / maxSq);
+    }
+    return std::min(std::sqrt(dt2), p->maxDT);
+}
+
+// ProbIncompNewton::getGlobalWrittableData("mass"): sum of element sizes,
+// IncompNewton/Problem.cpp:173-189
+double orc_volume(const OrcMesh* m) {
+    double s = 0;
+    for (int e = 0; e < m->E; ++e) s += m->geom[e].detJ * m->gt.refSize;
+    return s;
+}
+
+// ProbWCompNewton::getGlobalWrittableData("mass"), WCompNewton/Problem.cpp:216-244
+double orc_wc_mass(const OrcMesh* m, const double* s) {
+    const double* rho = s + (size_t)(m->dim + 1) * m->N;
+    double mass = 0;
+    for (int e = 0; e < m->E; ++e) {
+        double mid = 0;
+        for (int k = 0; k < m->npe; ++k) mid += rho[m->node(e, k)];
+        mid /= (double)m->npe;
+        mass += mid * m->geom[e].detJ * m->gt.refSize;
+    }
+    return mass;
+}
+
+// MinMaxExtractor::update, extractors/MinMaxExtractor.cpp:28-62
+double orc_tip(const OrcMesh* m, int coord, int wantMax) {
+    double v = wantMax ? 0.0 : std::numeric_limits<double>::max();
+    for (int n = 0; n < m->N; ++n)
+        if (!m->bound(n) && !m->isFree[n])
+            v = wantMax ? std::max(v, m->x(n, coord)) : std::min(v, m->x(n, coord));
+    return v;
+}
+
+}  // extern "C"

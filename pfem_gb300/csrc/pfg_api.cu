@@ -1,0 +1,598 @@
+// C ABI entry points of libpfemgpu.so (declared in include/pfem_gpu.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <new>
+
+#include "pfg_device.cuh"
+#include "pfg_internal.cuh"
+
+namespace pfg {
+
+int fail(pfg_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_fail(pfg_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, PFG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int ensure(pfg_ctx* c, DBuf& b, size_t bytes) {
+    if (bytes <= b.cap) return PFG_OK;
+    size_t newcap = std::max(bytes, b.cap + b.cap / 4);
+    newcap = (newcap + 255) & ~(size_t)255;
+    if (c->prm.hbm_budget_bytes && c->bytes_in_use - b.cap + newcap > c->prm.hbm_budget_bytes)
+        return fail(c, PFG_ERR_NOMEM, "HBM budget of %zu bytes exceeded", c->prm.hbm_budget_bytes);
+    if (b.p) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(b.p);
+        c->bytes_in_use -= b.cap;
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, newcap);
+    if (e != cudaSuccess) return fail(c, PFG_ERR_NOMEM, "cudaMalloc(%zu): %s", newcap, cudaGetErrorString(e));
+    b.p = p;
+    b.cap = newcap;
+    c->bytes_in_use += newcap;
+    return PFG_OK;
+}
+
+static cudaEvent_t take_event(pfg_ctx* c) {
+    if (c->ev_used == c->ev_pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        c->ev_pool.push_back(e);
+    }
+    return c->ev_pool[c->ev_used++];
+}
+
+void prof_begin(pfg_ctx* c, int phase) {
+    if (!c->prof) return;
+    if (c->ev_used + 2 > 4096) prof_flush(c);
+    cudaEvent_t e = take_event(c);
+    if (!e) return;
+    cudaEventRecord(e, c->stream);
+    c->marks.push_back(phase);
+    c->marks.push_back((int)c->ev_used - 1);
+    c->marks.push_back(-1);
+}
+
+void prof_end(pfg_ctx* c, int phase) {
+    if (!c->prof || c->marks.size() < 3) return;
+    // close the most recent open mark of this phase
+    for (size_t i = c->marks.size(); i >= 3; i -= 3) {
+        if (c->marks[i - 3] == phase && c->marks[i - 1] < 0) {
+            cudaEvent_t e = take_event(c);
+            if (!e) return;
+            cudaEventRecord(e, c->stream);
+            c->marks[i - 1] = (int)c->ev_used - 1;
+            return;
+        }
+    }
+}
+
+int prof_flush(pfg_ctx* c) {
+    if (c->marks.empty()) {
+        c->ev_used = 0;
+        return PFG_OK;
+    }
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i + 2 < c->marks.size(); i += 3) {
+        const int ph = c->marks[i], a = c->marks[i + 1], b = c->marks[i + 2];
+        if (b < 0) continue;
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, c->ev_pool[a], c->ev_pool[b]) == cudaSuccess) {
+            c->phase_ms[ph] += ms;
+            c->phase_n[ph] += 1;
+        }
+    }
+    c->marks.clear();
+    c->ev_used = 0;
+    return PFG_OK;
+}
+
+void release(DBuf& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+// Gauss rules of the element kernels (3 points in 2D, 4 in 3D; MomContEquation.inl:12-23)
+// with the reference's decimal values (Mesh.cpp:375-378, :396-399, :444, :459, :480-483).
+GaussConst gauss_const(int dim) {
+    GaussConst g{};
+    if (dim == 2) {
+        g.n = 3;
+        const double p[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}, {2.0 / 3.0, 1.0 / 6.0}};
+        for (int k = 0; k < 3; ++k) {
+            g.w[k] = 1.0 / 3.0;
+            g.N[k][0] = 1 - p[k][0] - p[k][1];
+            g.N[k][1] = p[k][0];
+            g.N[k][2] = p[k][1];
+        }
+        g.refSize = 0.5;
+    } else {
+        g.n = 4;
+        const double a = 0.585410196624968, b = 0.138196601125011;
+        const double p[4][3] = {{a, b, b}, {b, a, b}, {b, b, a}, {b, b, b}};
+        for (int k = 0; k < 4; ++k) {
+            g.w[k] = 0.25;
+            g.N[k][0] = 1 - p[k][0] - p[k][1] - p[k][2];
+            g.N[k][1] = p[k][0];
+            g.N[k][2] = p[k][1];
+            g.N[k][3] = p[k][2];
+        }
+        g.refSize = 0.16666666666666666666666666666667;
+    }
+    const int npe = dim + 1;
+    g.sumw = 0;
+    for (int k = 0; k < g.n; ++k) g.sumw += g.w[k];
+    for (int i = 0; i < npe; ++i) {
+        g.s[i] = 0;
+        for (int k = 0; k < g.n; ++k) g.s[i] += g.w[k] * g.N[k][i];
+        for (int j = 0; j < npe; ++j) {
+            g.MM[i][j] = 0;
+            for (int k = 0; k < g.n; ++k) g.MM[i][j] += g.N[k][i] * g.N[k][j] * g.w[k];
+        }
+    }
+    return g;
+}
+
+}  // namespace pfg
+
+using namespace pfg;
+
+namespace {
+
+__global__ void k_scatter_dirichlet(int n, const int* __restrict__ nodes, const double* __restrict__ vals, int N,
+                                    int dim, double* __restrict__ vbc) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int node = nodes[i];
+    for (int d = 0; d < dim; ++d) vbc[(size_t)d * N + node] = vals[(size_t)d * n + i];
+}
+
+int check_ctx(pfg_ctx* c) {
+    if (!c) return PFG_ERR_INVALID;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+    return PFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+PFG_API const char* pfg_version(void) { return "pfem_gb300 0.1 (sm_103a)"; }
+
+PFG_API const char* pfg_phase_name(int32_t phase) {
+    static const char* names[PFG_NUM_PHASES] = {
+        "WC predict", "WC continuity element", "WC continuity node", "WC momentum element", "WC momentum node",
+        "WC time step", "PSPG element prep", "PSPG right-hand side", "PSPG matrix", "Krylov iteration",
+        "Picard residual", "Position update"};
+    return (phase >= 0 && phase < PFG_NUM_PHASES) ? names[phase] : "";
+}
+
+PFG_API int pfg_set_profiling(pfg_ctx* c, int32_t enable) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prof && !enable) prof_flush(c);
+    c->prof = enable != 0;
+    return PFG_OK;
+}
+
+PFG_API int pfg_get_phase_times(pfg_ctx* c, double* ms, int64_t* launches) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if ((rc = prof_flush(c))) return rc;
+    for (int i = 0; i < PFG_NUM_PHASES; ++i) {
+        if (ms) ms[i] = c->phase_ms[i];
+        if (launches) launches[i] = c->phase_n[i];
+    }
+    return PFG_OK;
+}
+
+PFG_API int pfg_reset_phase_times(pfg_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if ((rc = prof_flush(c))) return rc;
+    for (int i = 0; i < PFG_NUM_PHASES; ++i) {
+        c->phase_ms[i] = 0;
+        c->phase_n[i] = 0;
+    }
+    return PFG_OK;
+}
+
+PFG_API int pfg_default_params(int32_t kind, int32_t dim, pfg_params* p) {
+    if (!p || (dim != 2 && dim != 3) || (kind != PFG_KIND_INCOMP_PSPG && kind != PFG_KIND_WC_CDS_DPDT))
+        return PFG_ERR_INVALID;
+    std::memset(p, 0, sizeof(*p));
+    p->dim = dim;
+    p->kind = kind;
+    p->precision = PFG_PREC_FP64;
+    p->linear_solver = PFG_LINSOLVE_BICGSTAB;
+    p->gravity[dim - 1] = -9.81;
+    p->mu = 1e-3;
+    p->rho = 1000.0;
+    p->picard_max_iter = 10;
+    p->residual = PFG_RES_AX_F;
+    p->picard_min_res = 1e-6;
+    p->krylov_max_iter = 5000;
+    p->krylov_rel_tol = 1e-14;
+    p->krylov_abs_tol = 1e-10;
+    p->K0 = 2.2e7;
+    p->K0p = 7.0;
+    p->rho_star = 1000.0;
+    p->security_coeff = 0.3;
+    p->max_dt = 1e-3;
+    p->meduri = 1;
+    p->hbm_budget_bytes = 0;
+    return PFG_OK;
+}
+
+PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
+    if (!params || !out) return PFG_ERR_INVALID;
+    *out = nullptr;
+    if (params->dim != 2 && params->dim != 3) return PFG_ERR_INVALID;
+    if (params->kind != PFG_KIND_INCOMP_PSPG && params->kind != PFG_KIND_WC_CDS_DPDT) return PFG_ERR_INVALID;
+    if (params->precision != PFG_PREC_FP64 && params->precision != PFG_PREC_MIXED) return PFG_ERR_INVALID;
+    if (params->linear_solver != PFG_LINSOLVE_BICGSTAB) return PFG_ERR_UNSUPPORTED;
+    pfg_ctx* c = new (std::nothrow) pfg_ctx();
+    if (!c) return PFG_ERR_NOMEM;
+    c->prm = *params;
+    c->dim = params->dim;
+    c->npe = params->dim + 1;
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64 * sizeof(double));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e != cudaSuccess) {
+        if (c->stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return PFG_ERR_CUDA;
+    }
+    c->max_grid = c->num_sms * 8;
+    if (ensure(c, c->err_word, 64) || ensure(c, c->red, sizeof(double) * (size_t)(c->max_grid * 4 + 256))) {
+        pfg_destroy(c);
+        return PFG_ERR_NOMEM;
+    }
+    cudaMemsetAsync(c->red.p, 0, c->red.cap, c->stream);
+    cudaMemsetAsync(c->err_word.p, 0, c->err_word.cap, c->stream);
+    cudaStreamSynchronize(c->stream);
+    *out = c;
+    return PFG_OK;
+}
+
+PFG_API int pfg_destroy(pfg_ctx* c) {
+    if (!c) return PFG_ERR_INVALID;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DBuf* bufs[] = {&c->pos, &c->pos_save, &c->flags, &c->conn, &c->ne_ptr, &c->ne_elem, &c->ne_loc,
+                    &c->nbr_ptr, &c->nbr, &c->pair_node, &c->row_ptr, &c->col, &c->val, &c->val32,
+                    &c->diag_pos, &c->rhs, &c->edata, &c->edata32, &c->q, &c->q_prev, &c->q_iter_prev,
+                    &c->vbc, &c->kv, &c->kv32, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
+                    &c->stage};
+    for (DBuf* b : bufs) release(*b);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    if (c->h_scalars) cudaFreeHost(c->h_scalars);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return PFG_OK;
+}
+
+PFG_API const char* pfg_last_error(const pfg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, const uint8_t* flags, int32_t n_elems,
+                            const int32_t* conn) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (n_nodes <= 0 || n_elems < 0 || !pos || !flags || (n_elems > 0 && !conn))
+        return fail(c, PFG_ERR_INVALID, "pfg_upload_mesh: invalid sizes or null pointers");
+    const int npe = c->npe, dim = c->dim;
+    // validate connectivity on the host: indices in range and distinct within an element
+    for (int e = 0; e < n_elems; ++e) {
+        for (int k = 0; k < npe; ++k) {
+            const int v = conn[(size_t)k * n_elems + e];
+            if (v < 0 || v >= n_nodes) return fail(c, PFG_ERR_INVALID, "element %d references node %d", e, v);
+            for (int j = 0; j < k; ++j)
+                if (conn[(size_t)j * n_elems + e] == v)
+                    return fail(c, PFG_ERR_INVALID, "element %d repeats node %d", e, v);
+        }
+    }
+    c->has_mesh = false;
+    c->has_system = false;
+    c->N = n_nodes;
+    c->E = n_elems;
+    c->R = (dim + 1) * n_nodes;
+    c->nstates = (c->prm.kind == PFG_KIND_INCOMP_PSPG) ? (dim + 1) : (2 * dim + 2);
+    const size_t N = n_nodes, E = n_elems;
+    if ((rc = ensure(c, c->pos, sizeof(double) * dim * N)) || (rc = ensure(c, c->pos_save, sizeof(double) * dim * N)) ||
+        (rc = ensure(c, c->flags, N)) || (rc = ensure(c, c->conn, sizeof(int) * std::max<size_t>(npe * E, 1))) ||
+        (rc = ensure(c, c->vbc, sizeof(double) * dim * N)))
+        return rc;
+    c->h_flags.assign(flags, flags + N);
+    PFG_CUDA(c, cudaMemcpyAsync(c->pos.p, pos, sizeof(double) * dim * N, cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->pos_save.p, pos, sizeof(double) * dim * N, cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->flags.p, flags, N, cudaMemcpyHostToDevice, c->stream));
+    if (E) PFG_CUDA(c, cudaMemcpyAsync(c->conn.p, conn, sizeof(int) * npe * E, cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemsetAsync(c->vbc.p, 0, sizeof(double) * dim * N, c->stream));
+    if ((rc = build_topology(c))) return rc;
+    if (c->prm.kind == PFG_KIND_INCOMP_PSPG) {
+        if ((rc = pspg_alloc(c)) || (rc = krylov_alloc(c))) return rc;
+    } else {
+        if ((rc = wc_alloc(c))) return rc;
+    }
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->has_mesh = true;
+    return PFG_OK;
+}
+
+PFG_API int pfg_set_states(pfg_ctx* c, const double* states) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!states) return fail(c, PFG_ERR_INVALID, "null states");
+    if (c->prm.kind == PFG_KIND_INCOMP_PSPG) {
+        PFG_CUDA(c, cudaMemcpyAsync(c->q.p, states, sizeof(double) * c->R, cudaMemcpyHostToDevice, c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        return PFG_OK;
+    }
+    return wc_set_states(c, states);
+}
+
+PFG_API int pfg_get_states(pfg_ctx* c, double* states) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!states) return fail(c, PFG_ERR_INVALID, "null states");
+    if (c->prm.kind == PFG_KIND_INCOMP_PSPG) {
+        PFG_CUDA(c, cudaMemcpyAsync(states, c->q.p, sizeof(double) * c->R, cudaMemcpyDeviceToHost, c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        return PFG_OK;
+    }
+    return wc_get_states(c, states);
+}
+
+PFG_API int pfg_get_positions(pfg_ctx* c, double* pos) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!pos) return fail(c, PFG_ERR_INVALID, "null positions");
+    PFG_CUDA(c, cudaMemcpyAsync(pos, c->pos.p, sizeof(double) * c->dim * c->N, cudaMemcpyDeviceToHost, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+PFG_API int pfg_get_flags(pfg_ctx* c, uint8_t* flags) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!flags) return fail(c, PFG_ERR_INVALID, "null flags");
+    PFG_CUDA(c, cudaMemcpyAsync(flags, c->flags.p, c->N, cudaMemcpyDeviceToHost, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+PFG_API int pfg_set_dirichlet(pfg_ctx* c, int32_t n, const int32_t* nodes, const double* values) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (n < 0 || (n > 0 && (!nodes || !values))) return fail(c, PFG_ERR_INVALID, "pfg_set_dirichlet: bad arguments");
+    if (n == 0) return PFG_OK;
+    for (int i = 0; i < n; ++i)
+        if (nodes[i] < 0 || nodes[i] >= c->N) return fail(c, PFG_ERR_INVALID, "Dirichlet node %d out of range", nodes[i]);
+    DBuf tmp;
+    const size_t nb = sizeof(int) * n, vb = sizeof(double) * c->dim * n;
+    if ((rc = ensure(c, tmp, nb + vb + 256))) return rc;
+    char* base = ptr<char>(tmp);
+    int* dn = reinterpret_cast<int*>(base);
+    double* dv = reinterpret_cast<double*>(base + ((nb + 255) & ~(size_t)255));
+    cudaError_t e = cudaMemcpyAsync(dn, nodes, nb, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dv, values, vb, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        k_scatter_dirichlet<<<div_up(n, BLOCK), BLOCK, 0, c->stream>>>(n, dn, dv, c->N, c->dim, ptr<double>(c->vbc));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    c->bytes_in_use -= tmp.cap;
+    release(tmp);
+    if (e != cudaSuccess) return cuda_fail(c, e, "pfg_set_dirichlet");
+    return PFG_OK;
+}
+
+PFG_API int pfg_picard_step(pfg_ctx* c, double dt, pfg_step_status* st) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG) return fail(c, PFG_ERR_STATE, "context is not incompressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!(dt > 0) || !st) return fail(c, PFG_ERR_INVALID, "pfg_picard_step: dt must be > 0 and status non-null");
+    return picard_step(c, dt, st);
+}
+
+PFG_API int pfg_wc_step(pfg_ctx* c, double dt, int32_t nsteps, pfg_step_status* st) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (nsteps < 0 || !st) return fail(c, PFG_ERR_INVALID, "pfg_wc_step: bad arguments");
+    return wc_steps(c, dt, nsteps, st);
+}
+
+PFG_API int pfg_wc_step_async(pfg_ctx* c, double dt, int32_t nsteps) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (nsteps < 0) return fail(c, PFG_ERR_INVALID, "pfg_wc_step_async: nsteps < 0");
+    return wc_enqueue(c, dt, nsteps);
+}
+
+PFG_API int pfg_synchronize(pfg_ctx* c, pfg_step_status* st) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!st) return fail(c, PFG_ERR_INVALID, "null status");
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT && c->has_mesh) return wc_sync(c, st);
+    std::memset(st, 0, sizeof(*st));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+PFG_API int pfg_get_stream(pfg_ctx* c, void** stream) {
+    if (!c || !stream) return PFG_ERR_INVALID;
+    *stream = (void*)c->stream;
+    return PFG_OK;
+}
+
+PFG_API int pfg_next_dt(pfg_ctx* c, double* dt) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!dt) return fail(c, PFG_ERR_INVALID, "null dt");
+    return wc_next_dt(c, dt);
+}
+
+PFG_API int pfg_set_time(pfg_ctx* c, double time, double next_dt) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    double h[2] = {next_dt, time};
+    PFG_CUDA(c, cudaMemcpyAsync(c->wc_dt.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->host_time = time;
+    return PFG_OK;
+}
+
+PFG_API int pfg_volume(pfg_ctx* c, double* v) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!v) return fail(c, PFG_ERR_INVALID, "null output");
+    return volume(c, v);
+}
+
+PFG_API int pfg_mass(pfg_ctx* c, double* m) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!m) return fail(c, PFG_ERR_INVALID, "null output");
+    if (c->prm.kind == PFG_KIND_INCOMP_PSPG) return volume(c, m);
+    return wc_mass(c, m);
+}
+
+PFG_API int pfg_tip(pfg_ctx* c, int32_t coord, int32_t want_max, double* v) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!v || coord < 0 || coord >= c->dim) return fail(c, PFG_ERR_INVALID, "bad coordinate");
+    return tip(c, coord, want_max, v);
+}
+
+PFG_API int pfg_pspg_assemble(pfg_ctx* c, double dt, const double* q_iter, const double* q_prev, int32_t apply_bc) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG) return fail(c, PFG_ERR_STATE, "context is not incompressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!(dt > 0)) return fail(c, PFG_ERR_INVALID, "dt must be > 0");
+    double* kv = ptr<double>(c->kv);
+    const size_t R = c->R;
+    // stage host vectors in Krylov workspace slots 8 and 9
+    const double* di = ptr<double>(c->q);
+    const double* dp = ptr<double>(c->q);
+    if (q_iter) {
+        PFG_CUDA(c, cudaMemcpyAsync(kv + 8 * R, q_iter, sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
+        di = kv + 8 * R;
+    }
+    if (q_prev) {
+        PFG_CUDA(c, cudaMemcpyAsync(kv + 9 * R, q_prev, sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
+        dp = kv + 9 * R;
+    }
+    rc = pspg_assemble(c, dt, di, dp, apply_bc != 0);
+    if (rc) return rc;
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+PFG_API int pfg_get_csr(pfg_ctx* c, int32_t* n_rows, int64_t* nnz, int64_t* row_ptr, int32_t* col_idx,
+                        double* values, double* rhs) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG) return fail(c, PFG_ERR_STATE, "context is not incompressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (n_rows) *n_rows = c->R;
+    if (nnz) *nnz = c->nnz;
+    if (row_ptr) {
+        std::vector<int> tmp(c->R + 1);
+        PFG_CUDA(c, cudaMemcpyAsync(tmp.data(), c->row_ptr.p, sizeof(int) * (c->R + 1), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int i = 0; i <= c->R; ++i) row_ptr[i] = tmp[i];
+    }
+    if (col_idx)
+        PFG_CUDA(c, cudaMemcpyAsync(col_idx, c->col.p, sizeof(int) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
+    if (values || rhs) {
+        if (!c->has_system) return fail(c, PFG_ERR_STATE, "no assembled system");
+        if (values)
+            PFG_CUDA(c, cudaMemcpyAsync(values, c->val.p, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
+        if (rhs) PFG_CUDA(c, cudaMemcpyAsync(rhs, c->rhs.p, sizeof(double) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    }
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+PFG_API int pfg_get_geometry(pfg_ctx* c, double* detJ, double* invJ) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!detJ || !invJ) return fail(c, PFG_ERR_INVALID, "null output");
+    DBuf tmp;
+    if ((rc = ensure(c, tmp, sizeof(double) * 10 * (size_t)std::max(c->E, 1)))) return rc;
+    double* d = ptr<double>(tmp);
+    rc = compute_geometry(c, d, d + c->E);
+    cudaError_t e = cudaSuccess;
+    if (!rc) e = cudaMemcpyAsync(detJ, d, sizeof(double) * c->E, cudaMemcpyDeviceToHost, c->stream);
+    if (!rc && e == cudaSuccess)
+        e = cudaMemcpyAsync(invJ, d + c->E, sizeof(double) * 9 * c->E, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    c->bytes_in_use -= tmp.cap;
+    release(tmp);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(c, e, "pfg_get_geometry");
+    return PFG_OK;
+}
+
+PFG_API int pfg_linear_solve(pfg_ctx* c, double* x, int32_t* iterations, double* res) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG) return fail(c, PFG_ERR_STATE, "context is not incompressible");
+    if (!c->has_system) return fail(c, PFG_ERR_STATE, "no assembled system");
+    if (!x) return fail(c, PFG_ERR_INVALID, "null x");
+    double* kv = ptr<double>(c->kv);
+    double* dx = kv + 8 * (size_t)c->R;
+    PFG_CUDA(c, cudaMemcpyAsync(dx, x, sizeof(double) * c->R, cudaMemcpyHostToDevice, c->stream));
+    int it = 0;
+    double r = 0;
+    rc = bicgstab(c, dx, &it, &r);
+    if (rc) return rc;
+    PFG_CUDA(c, cudaMemcpyAsync(x, dx, sizeof(double) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (iterations) *iterations = it;
+    if (res) *res = r;
+    return PFG_OK;
+}
+
+}  // extern "C"

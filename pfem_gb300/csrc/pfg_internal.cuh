@@ -1,0 +1,183 @@
+// Internal declarations of the PFEM GB300 library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/pfem_gpu.h"
+
+namespace pfg {
+
+constexpr uint8_t F_BOUND = PFG_NODE_BOUND;
+constexpr uint8_t F_FREE_SURFACE = PFG_NODE_FREE_SURFACE;
+constexpr uint8_t F_FIXED = PFG_NODE_FIXED;
+constexpr uint8_t F_DIRICHLET = PFG_NODE_DIRICHLET;
+constexpr uint8_t F_FREE = PFG_NODE_FREE;
+
+// Upper bound on distinct neighbours (including itself) of one node.  Delaunay meshes have
+// mean valence ~6 (2D) / ~14 (3D); the cap leaves room for badly shaped post-remesh stars.
+constexpr int MAX_NBR = 128;
+
+// Device error word bits (ctx->d_err).
+constexpr int ERR_NBR_OVERFLOW = 1;
+constexpr int ERR_KRYLOV_BREAKDOWN = 2;
+constexpr int ERR_NONFINITE = 4;
+
+// Gauss-point tables of the element rules (Mesh::getGaussPoints/Weight/ShapeFunctions,
+// srcs/mesh/Mesh.cpp:342-530) and the sums the closed-form element kernels need.
+struct GaussConst {
+    int n;            // points
+    double w[4];      // weights
+    double N[4][4];   // N[g][i]
+    double MM[4][4];  // sum_g w_g N_i N_j
+    double s[4];      // sum_g w_g N_i
+    double sumw;      // sum_g w_g
+    double refSize;   // reference element size
+};
+
+// Grow-only device buffer.
+struct DBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+struct Reducer;  // fwd
+
+}  // namespace pfg
+
+struct pfg_ctx {
+    pfg_params prm{};
+    int dim = 0, npe = 0;
+    int N = 0, E = 0;
+    int R = 0;          // incompressible unknowns (dim+1)*N
+    int nstates = 0;    // per-node states of the kind
+    bool has_mesh = false;
+    bool has_system = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    size_t bytes_in_use = 0;
+
+    // mesh
+    pfg::DBuf pos, pos_save, flags, conn;
+    // node -> element incidence (ascending element per node)
+    pfg::DBuf ne_ptr, ne_elem, ne_loc;
+    // node adjacency (sorted, includes the node) and the node-pair list
+    pfg::DBuf nbr_ptr, nbr, pair_node;
+    int P = 0;
+    // CSR system
+    pfg::DBuf row_ptr, col, val, val32, diag_pos, rhs;
+    int64_t nnz = 0;
+    // element data: detJ, tau, gradN (SoA)
+    pfg::DBuf edata, edata32;
+    // incompressible states
+    pfg::DBuf q, q_prev, q_iter_prev, vbc;
+    // Krylov workspace
+    pfg::DBuf kv;          // 10 vectors of R doubles
+    pfg::DBuf kv32;        // FP32 workspace (mixed precision)
+    pfg::DBuf red;         // reduction partials + scalars + counters
+    pfg::DBuf err_word;    // int device error word
+    // WC
+    pfg::DBuf ws;          // states (2d+2)*N of the working precision
+    pfg::DBuf wc_el;       // element -> node partial values
+    pfg::DBuf wc_dt;       // [dt_next, time, dt_min_bits]
+    pfg::DBuf stage;       // FP64 staging for host<->device precision conversion
+    int wc_pending = 0;    // steps enqueued since the last synchronize
+    double host_time = 0.0;
+    // host mirrors for validation
+    std::vector<uint8_t> h_flags;
+    // pinned host scratch for scalar readbacks
+    double* h_scalars = nullptr;
+    int max_grid = 0;      // blocks for grid-stride loops (multiple of the SM count)
+    int num_sms = 0;
+    // phase timers
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<int> marks;  // (phase, ev_start, ev_stop) triples
+    double phase_ms[PFG_NUM_PHASES] = {};
+    long long phase_n[PFG_NUM_PHASES] = {};
+};
+
+namespace pfg {
+
+// ---- allocation / error helpers (pfg_api.cu) -----------------------------------------
+int fail(pfg_ctx* c, int code, const char* fmt, ...);
+int cuda_fail(pfg_ctx* c, cudaError_t e, const char* what);
+int ensure(pfg_ctx* c, DBuf& b, size_t bytes);
+void release(DBuf& b);
+
+template <class T>
+inline T* ptr(const DBuf& b) {
+    return static_cast<T*>(b.p);
+}
+
+#define PFG_CUDA(ctx, call)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return pfg::cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+#define PFG_CHECK_LAUNCH(ctx) PFG_CUDA(ctx, cudaGetLastError())
+
+// ---- phase timers (pfg_api.cu) ---------------------------------------------------------
+enum Phase : int {
+    PH_WC_PREDICT = 0,
+    PH_WC_CONT_ELEM,
+    PH_WC_CONT_NODE,
+    PH_WC_MOM_ELEM,
+    PH_WC_MOM_NODE,
+    PH_WC_DT,
+    PH_PSPG_ELEM,
+    PH_PSPG_RHS,
+    PH_PSPG_PAIRS,
+    PH_KRYLOV_ITER,
+    PH_RESIDUAL,
+    PH_POSITIONS
+};
+void prof_begin(pfg_ctx* c, int phase);
+void prof_end(pfg_ctx* c, int phase);
+int prof_flush(pfg_ctx* c);
+
+// ---- scans (pfg_mesh.cu) ---------------------------------------------------------------
+// Exclusive prefix sum of n ints into out (n+1 entries; out[n] = total).  Uses tmp space.
+int scan_exclusive(pfg_ctx* c, const int* in, int* out, int n, DBuf& tmp);
+
+// ---- mesh build (pfg_mesh.cu) --------------------------------------------------------
+int build_topology(pfg_ctx* c);
+
+// ---- constants (pfg_api.cu) ----------------------------------------------------------
+GaussConst gauss_const(int dim);
+void upload_constants(int dim);
+
+// ---- PSPG (pfg_pspg.cu) --------------------------------------------------------------
+int pspg_alloc(pfg_ctx* c);
+int pspg_assemble(pfg_ctx* c, double dt, const double* d_qiter, const double* d_qprev, bool apply_bc);
+int pspg_update_positions(pfg_ctx* c, double dt, const double* d_q);
+int pspg_residual(pfg_ctx* c, const double* d_q, double* res_out);
+int picard_step(pfg_ctx* c, double dt, pfg_step_status* st);
+int compute_geometry(pfg_ctx* c, double* d_detJ, double* d_invJ);
+int volume(pfg_ctx* c, double* out);
+int tip(pfg_ctx* c, int coord, int want_max, double* out);
+
+// ---- Krylov (pfg_krylov.cu) ----------------------------------------------------------
+int krylov_alloc(pfg_ctx* c);
+// Solve A x = b (x in/out, device).  Returns iterations in *iters and ||b - A x|| in *res.
+int bicgstab(pfg_ctx* c, double* d_x, int* iters, double* res);
+int spmv_residual_norm(pfg_ctx* c, const double* d_x, double* res);
+
+// ---- WC (pfg_wc.cu) -------------------------------------------------------------------
+int wc_alloc(pfg_ctx* c);
+int wc_set_states(pfg_ctx* c, const double* h);
+int wc_get_states(pfg_ctx* c, double* h);
+int wc_steps(pfg_ctx* c, double dt, int nsteps, pfg_step_status* st);
+int wc_enqueue(pfg_ctx* c, double dt, int nsteps);
+int wc_sync(pfg_ctx* c, pfg_step_status* st);
+int wc_next_dt(pfg_ctx* c, double* dt);
+int wc_mass(pfg_ctx* c, double* out);
+
+}  // namespace pfg

@@ -1,0 +1,131 @@
+"""CPU checks of the FP64 oracle: known-answer element tests, the sparsity-pattern rule,
+physics invariants (hydrostatic rest, mass conservation) and the Picard failure path."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pfem_gb300 import mesh as M
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "kat_elements.npz")
+
+
+def _single_element_mesh(X):
+    d = X.shape[1]
+    return M.HostMesh(d, X.T.copy(), np.zeros(d + 1, np.uint8), np.arange(d + 1, dtype=np.int32).reshape(d + 1, 1))
+
+
+@pytest.mark.parametrize("name", ["tri", "tri_skew", "tet", "tet_skew"])
+def test_element_matrices_match_closed_forms(name):
+    z = np.load(GOLDEN)
+    rho, mu, dt = z["params"]
+    X = z[name + "_X"]
+    d = X.shape[1]
+    om = O.OracleMesh(_single_element_mesh(X))
+    N = d + 1
+    qi = np.zeros((d + 1) * N)
+    qp = np.zeros((d + 1) * N)
+    qi[:d * N] = z[name + "_viter"].T.reshape(-1)
+    qp[:d * N] = z[name + "_vprev"].T.reshape(-1)
+    g = (0.0, -9.81, 0.0) if d == 2 else (0.0, 0.0, -9.81)
+    Ae, be = O.pspg_element(om, 0, rho, mu, dt, g, qi, qp)
+    tol = 1e-13 if d == 2 else 1e-12  # 3D Gauss points are 15-digit decimals in the reference
+    assert np.abs(Ae - z[name + "_Ae"]).max() <= tol * np.abs(z[name + "_Ae"]).max()
+    assert np.abs(be - z[name + "_be"]).max() <= tol * np.abs(z[name + "_be"]).max()
+    _, det, _ = om.geometry()
+    assert det[0] == pytest.approx(float(z[name + "_detJ"]), rel=1e-14)
+
+
+def rule_pattern(mesh):
+    """CSR pattern from the adjacency rule used by the GPU library (pfg_mesh.cu)."""
+    d, N = mesh.dim, mesh.n_nodes
+    free = mesh.is_free()
+    bound = (mesh.flags & M.BOUND) != 0
+    nbr = [set([n]) for n in range(N)]
+    for e in range(mesh.n_elems):
+        nodes = mesh.conn[:, e]
+        for a in nodes:
+            nbr[a].update(int(b) for b in nodes)
+    rows, cols = [], []
+    for f in range(d + 1):
+        for n in range(N):
+            r = n + f * N
+            if free[n] or (bound[n] and f < d):
+                rows.append(r)
+                cols.append(r)
+                continue
+            ns = sorted(nbr[n])
+            for f2 in range(d + 1):
+                for m in ns:
+                    rows.append(r)
+                    cols.append(m + f2 * N)
+    return np.array(rows), np.array(cols)
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_pattern_rule_matches_set_from_triplets(which, c1_mesh, small3d_mesh):
+    mesh = c1_mesh if which == "c1" else small3d_mesh
+    om = O.OracleMesh(mesh)
+    d, N = mesh.dim, mesh.n_nodes
+    q = np.zeros((d + 1) * N)
+    g = (0.0, -9.81) if d == 2 else (0.0, 0.0, -9.81)
+    A, _ = O.pspg_assemble(om, 1000.0, 1e-3, 1e-3, g, q, q)
+    csr = A.tocsr()
+    csr.sort_indices()
+    rows, cols = rule_pattern(mesh)
+    R = (d + 1) * N
+    order = np.lexsort((cols, rows))
+    rows, cols = rows[order], cols[order]
+    rp = np.zeros(R + 1, np.int64)
+    np.add.at(rp, rows + 1, 1)
+    rp = np.cumsum(rp)
+    assert np.array_equal(csr.indptr, rp)
+    assert np.array_equal(csr.indices, cols)
+
+
+def test_hydrostatic_column_stays_at_rest():
+    """KAT-3: a column filling the tank width is at equilibrium under hydrostatic pressure."""
+    mesh = M.dam_break_2d(0.05, tank=(1.05, 3.0))
+    om = O.OracleMesh(mesh)
+    q0 = M.incomp_initial_states(mesh)
+    q, res = O.pspg_picard_step(om, q0, 1e-3)
+    N = mesh.n_nodes
+    assert res.converged
+    assert np.abs(q[:2 * N]).max() < 5e-3           # m/s, after one step from rest
+    inner = ~mesh.is_free() & ((mesh.flags & M.FREE_SURFACE) == 0)
+    p_err = np.abs(q[2 * N:] - q0[2 * N:])[inner]
+    assert p_err.max() < 0.02 * q0[2 * N:].max()
+
+
+def test_wc_mass_conserved_over_steps(wc_small_mesh):
+    """KAT-4: the WC step keeps sum |e| mean(rho) nearly constant over many steps."""
+    mesh = wc_small_mesh
+    om = O.OracleMesh(mesh)
+    s = M.wc_initial_states(mesh)
+    p = O.wc_params()
+    m0 = O.wc_mass(om, s)
+    dt = O.wc_next_dt(om, p, s)
+    for _ in range(50):
+        O.wc_step(om, p, dt, s)
+        dt = O.wc_next_dt(om, p, s)
+    m1 = O.wc_mass(om, s)
+    assert np.all(np.isfinite(s))
+    assert abs(m1 - m0) / m0 < 1e-4
+    assert 0 < dt <= p.maxDT
+
+
+def test_picard_failure_restores_positions(c1_mesh):
+    om = O.OracleMesh(c1_mesh)
+    q0 = M.incomp_initial_states(c1_mesh)
+    x0 = om.positions.copy()
+    q, res = O.pspg_picard_step(om, q0, 1e-3, max_iter=0, min_res=1e-30)
+    assert not res.converged
+    assert np.array_equal(om.positions, x0)
+    assert np.array_equal(q, q0)
+
+
+def test_volume_and_tip(c1_mesh):
+    om = O.OracleMesh(c1_mesh)
+    assert om.volume() == pytest.approx(2.0, rel=2e-2)
+    assert 0.95 < om.tip() < 1.06
