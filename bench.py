@@ -61,7 +61,8 @@ def workload_config(mesh, precision):
     return {
         "workload": "2D weakly compressible dam break (C2)",
         "h_m": H, "nodes": int(mesh.n_nodes), "elements": int(mesh.n_elems),
-        "dof_per_step": int(3 * mesh.n_nodes), "state": precision, "dt": "adaptive CFL 0.3",
+        "dof_per_step": int(3 * mesh.n_nodes), "state": "fp64",
+        "element_arithmetic": precision, "dt": "adaptive CFL 0.3",
         "l2": "flushed between timed steps (256 MB write)", "remesh": "excluded (host side)",
         "parallelism": "replicas only",
     }
@@ -124,24 +125,29 @@ class ClockSampler:
                 "samples": len(rows), "reasons": sorted(reasons)}
 
 
-def wc_phase_bytes(d, N, E, s):
-    """Algorithmic bytes per launch of each WC kernel (s = state bytes; positions FP64; int32
-    indices; one flag byte per node).  Each node/element datum counted once."""
+def wc_phase_bytes(d, N, E, r):
+    """Algorithmic bytes per launch of each WC kernel.  Node state (x, v, p, rho, a) is FP64;
+    element partials are r bytes (4 mixed, 8 plain) plus d(d+1) FP64 area gradients; int32
+    connectivity and incidence lists, uint8 local indices and flags.  Each datum counted once."""
     inc = E * (d + 1)
+    npe = d + 1
+    el_cont = 2 * npe * r
+    el_mom = (npe + d * npe) * r + d * npe * 8
     return {
-        "WC predict": N * (3 * d * s + 16 * d + 1),
-        "WC continuity element": E * (d + 1) * 4 + N * (8 * d + (d + 1) * s) + 2 * (d + 1) * E * s,
-        "WC continuity node": 2 * (d + 1) * E * s + inc * 5 + (N + 1) * 4 + N + 2 * N * s,
-        "WC momentum element": E * (d + 1) * 4 + N * (8 * d + (d + 2) * s) + (d + 1) ** 2 * E * s,
-        "WC momentum node": (d + 1) ** 2 * E * s + inc * 5 + (N + 1) * 4 + N + 8 * d * N + d * s * N + 2 * d * s * N,
-        "WC time step": E * (d + 1) * 4 + N * (8 * d + (d + 2) * s),
+        "WC predict": N * (3 * d * 8 + 16 * d + 1),
+        "WC continuity element": E * npe * 4 + N * (8 * d + 8 * d + 8) + E * el_cont,
+        "WC continuity node": E * el_cont + inc * 5 + (N + 1) * 4 + N + N * 24,
+        "WC momentum element": E * npe * 4 + N * (8 * d + 8 * d + 16) + E * el_mom,
+        "WC momentum node": E * el_mom + inc * 5 + (N + 1) * 4 + N + N * (8 * d + 16 + 8 * d) + N * 16 * d
+                            + 2 * N * r,
+        "WC time step": E * npe * 4 + N * 8 * d + 2 * N * r,
     }
 
 
-def step_bytes(d, N, E, s):
-    """Algorithmic bytes of one whole step: connectivity once, x, v, a, p, rho read and written
-    once, flags once (each node datum once)."""
-    return E * (d + 1) * 4 + 2 * N * (3 * d + 2) * s + N
+def step_bytes(d, N, E):
+    """Algorithmic bytes of one whole step: connectivity once, x, v, a, p, rho (FP64) read and
+    written once, flags once."""
+    return E * (d + 1) * 4 + 2 * N * (3 * d + 2) * 8 + N
 
 
 def time_oracle(mesh, s0, seconds, max_steps, threads=None):
@@ -214,7 +220,7 @@ def run_gpu(args):
     s0 = M.wc_initial_states(mesh)
     d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
     prec = api.PREC_MIXED if args.precision == "fp32" else api.PREC_FP64
-    sbytes = 4 if args.precision == "fp32" else 8
+    rbytes = 4 if args.precision == "fp32" else 8
 
     def make(precision):
         p = api.default_params(api.KIND_WC_CDS_DPDT, 2)
@@ -241,23 +247,33 @@ def run_gpu(args):
     # timed region: K steps, L2 flushed between steps, events on the library stream
     K = args.steps
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    ctx.set_profiling(True)
-    ctx.reset_phase_times()
     barrier()
     torch.cuda.synchronize()
     with torch.cuda.stream(ext):
         for k in range(K):
             flush.fill_(k & 0xFF)
             ev[k][0].record(ext)
-            ctx.wc_step_async(0.0, 1)
+            ctx.wc_step_async(0.0, 1)   # one CUDA-graph launch of the step's kernels
             ev[k][1].record(ext)
     st = ctx.synchronize()
     torch.cuda.synchronize()
     barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
+
+    # per-kernel durations: same steps launched without the graph, with the library's phase
+    # timers (CUDA events on its stream) between kernels, L2 flushed between steps
+    Kp = min(K, 500)
+    ctx.set_profiling(True)
+    ctx.reset_phase_times()
+    with torch.cuda.stream(ext):
+        for k in range(Kp):
+            flush.fill_(k & 0xFF)
+            ctx.wc_step_async(0.0, 1)
+    ctx.synchronize()
     phases = ctx.phase_times()
     ctx.set_profiling(False)
+    launches_per_step = sum(v[1] for v in phases.values()) / Kp
     if world > 1:
         t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -311,12 +327,12 @@ def run_gpu(args):
         tst.close()
 
     # roofline of the dominant kernel (phase timers are CUDA events on the library stream)
-    pb = wc_phase_bytes(d, N, E, sbytes)
+    pb = wc_phase_bytes(d, N, E, rbytes)
     dom = max(phases.items(), key=lambda kv: kv[1][0])
     dom_name, (dom_ms, dom_n) = dom
     peak, peak_kind = hbm_peak()
     achieved = pb[dom_name] / (dom_ms / dom_n / 1e3) / 1e9
-    step_gbs = step_bytes(d, N, E, sbytes) / (total_ms / K / 1e3) / 1e9
+    step_gbs = step_bytes(d, N, E) / (total_ms / K / 1e3) / 1e9
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -343,7 +359,7 @@ def run_gpu(args):
             "phases_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in phases.items()},
             "cpu_baseline": cpu,
             "clocks": clk,
-            "gpu_launches": int(sum(v[1] for v in phases.values())),
+            "gpu_launches": int(round(launches_per_step * K)),
             "err_vs_fp64": acc,
             "last_dt": st.dt,
         }

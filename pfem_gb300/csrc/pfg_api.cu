@@ -283,8 +283,9 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
     DBuf* bufs[] = {&c->pos, &c->pos_save, &c->flags, &c->conn, &c->ne_ptr, &c->ne_elem, &c->ne_loc,
                     &c->nbr_ptr, &c->nbr, &c->pair_node, &c->row_ptr, &c->col, &c->val, &c->val32,
                     &c->diag_pos, &c->rhs, &c->edata, &c->edata32, &c->q, &c->q_prev, &c->q_iter_prev,
-                    &c->vbc, &c->kv, &c->kv32, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
-                    &c->stage};
+                    &c->vbc, &c->kv, &c->kv32, &c->binv, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
+                    &c->stage, &c->wc_eld, &c->wc_nodal};
+    wc_release_graphs(c);
     for (DBuf* b : bufs) release(*b);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->h_scalars) cudaFreeHost(c->h_scalars);

@@ -79,6 +79,7 @@ struct pfg_ctx {
     // Krylov workspace
     pfg::DBuf kv;          // 10 vectors of R doubles
     pfg::DBuf kv32;        // FP32 workspace (mixed precision)
+    pfg::DBuf binv;        // node-block Jacobi inverses, (dim+1)^2 x N
     pfg::DBuf red;         // reduction partials + scalars + counters
     pfg::DBuf err_word;    // int device error word
     // WC
@@ -101,6 +102,9 @@ struct pfg_ctx {
     std::vector<int> marks;  // (phase, ev_start, ev_stop) triples
     double phase_ms[PFG_NUM_PHASES] = {};
     long long phase_n[PFG_NUM_PHASES] = {};
+    // WC: FP64 element partials, per-node CFL quantities, captured step graphs [fixed, adaptive]
+    pfg::DBuf wc_eld, wc_nodal;
+    cudaGraphExec_t wc_graph[2] = {nullptr, nullptr};
 };
 
 namespace pfg {
@@ -172,6 +176,7 @@ int spmv_residual_norm(pfg_ctx* c, const double* d_x, double* res);
 
 // ---- WC (pfg_wc.cu) -------------------------------------------------------------------
 int wc_alloc(pfg_ctx* c);
+void wc_release_graphs(pfg_ctx* c);
 int wc_set_states(pfg_ctx* c, const double* h);
 int wc_get_states(pfg_ctx* c, double* h);
 int wc_steps(pfg_ctx* c, double dt, int nsteps, pfg_step_status* st);

@@ -5,19 +5,27 @@
 // :334-413), MomEqWCompNewton::m_buildSystem/m_applyBC/solve (MomEquation.inl:201-374) and
 // SolverWCompNewton::computeNextDT (Solver.cpp:192-234).
 //
-// One step is five kernels (six with the CFL time step):
+// One step is six kernels, captured once into a CUDA graph:
 //   predict   (node)    v1/2 = v + dt/2 a ; x += dt v1/2 for non-fixed nodes
-//   cont_elem (element) lumped mass and F0e = -dt D(K0+K0'p) v + M p   (Meduri) per element node
+//   cont_elem (element) per element node: lumped mass and the continuity right-hand side
 //   cont_node (node)    gather over the node's elements in element order -> p, rho (Tait)
-//   mom_elem  (element) lumped rho-mass and FTot = -K v + D^T p + F(rho g) per element node
+//   mom_elem  (element) per element node: lumped rho-mass and FTot = -K v + D^T p + F(rho g)
 //   mom_node  (node)    gather -> a = F / M (with BCs), v = v1/2 + dt/2 a
 //   dt        (element) min over elements of sc^2 h^2 / max(u^2, c^2, 4 alpha^2/h^2) -> next dt
-// The element->node gathers sum in ascending element order, the order of the reference's
-// serial scatter loops, so results do not depend on scheduling.  The state is a template
-// type (double for the plain form, float for the mixed form); positions and element geometry
-// stay FP64.
+//
+// Precision.  Node state (x, v, p, rho, a) is FP64 in both forms; geometry (J, detJ, the
+// area-weighted shape gradients A_fi = |e| dN_i/dx_f) is FP64; the element arithmetic type R
+// is double (plain form) or float (mixed form).  The two terms that nearly cancel node by node
+// are written as differences from the node's own value so that FP32 arithmetic keeps them
+// accurate; both rewrites are exact algebra:
+//   continuity (Meduri):  sum_e sum_j M_ij p_j = p_i ML_i + sum_e sum_j M_ij (p_j - p_i)
+//   momentum pressure:    sum_e A_fi pbar_e   = p_i S sum_e A_fi + sum_e A_fi sum_j s_j (p_j - p_i)
+// (S = sum_j s_j = sum_g w_g).  The p_i-weighted parts are formed in FP64 at the node.
+// Element partials are summed at the node in ascending element order (the order of the
+// reference's serial scatters), so results do not depend on scheduling.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -32,13 +40,11 @@ struct WcConst {
     double K0, K0p, rho_star, mu, sc, max_dt;
     double g[3];
     int meduri;
-    int ng;
-    double w[4];
-    double N[4][4];
-    double MM[4][4];
-    double s[4];
+    double MM[4][4];   // sum_g w N_i N_j
+    double s[4];       // sum_g w N_i
+    double S;          // sum_i s_i
     double refSize;
-    double mu_sum;
+    double mu_sum;     // sum_g mu w_g (getK factor)
 };
 
 WcConst make_const(pfg_ctx* c) {
@@ -52,14 +58,11 @@ WcConst make_const(pfg_ctx* c) {
     k.max_dt = c->prm.max_dt;
     for (int f = 0; f < 3; ++f) k.g[f] = c->prm.gravity[f];
     k.meduri = c->prm.meduri;
-    k.ng = gc.n;
-    for (int q = 0; q < 4; ++q) {
-        k.w[q] = gc.w[q];
-        k.s[q] = gc.s[q];
-        for (int i = 0; i < 4; ++i) {
-            k.N[q][i] = gc.N[q][i];
-            k.MM[q][i] = gc.MM[q][i];
-        }
+    k.S = 0;
+    for (int i = 0; i < 4; ++i) {
+        k.s[i] = gc.s[i];
+        if (i <= c->dim) k.S += gc.s[i];
+        for (int j = 0; j < 4; ++j) k.MM[i][j] = gc.MM[i][j];
     }
     k.refSize = gc.refSize;
     k.mu_sum = 0;
@@ -70,9 +73,73 @@ WcConst make_const(pfg_ctx* c) {
 // slots of ctx->wc_dt (doubles)
 enum : int { T_DT = 0, T_TIME = 1, T_MIN = 2, T_TICKET = 3 };
 
-template <int DIM, class T>
-__global__ void k_wc_predict(int N, const uint8_t* __restrict__ flags, T* __restrict__ s, double* __restrict__ pos,
-                             double* __restrict__ tdt) {
+// Element partial layout (array of structures, one record per element):
+//   R  part: [ML_0..ML_d, cont_0..cont_d, MLrho_0..MLrho_d, Fs_{f,i}...]   (dim+3)(dim+1) values
+//   FP64 part: [W_{f,i}] = A_{f,i}                                         dim(dim+1) values
+template <int DIM>
+struct ElLayout {
+    static constexpr int NPE = DIM + 1;
+    static constexpr int ML = 0, CONT = NPE, MLR = 2 * NPE, FS = 3 * NPE;
+    static constexpr int NR = 3 * NPE + DIM * NPE;
+    static constexpr int ND = DIM * NPE;
+};
+
+// Area-weighted shape gradients A[f][i] = |e| dN_i/dx_f from the FP64 Jacobian: no division.
+// 2D: |e| = detJ/2 and invJ = adj(J)/detJ; 3D: |e| = detJ/6 with the cofactors of J.
+template <int DIM>
+__device__ __forceinline__ void area_gradients(const Geom<DIM>& g, double refSize, double (&A)[DIM][DIM + 1]) {
+    if constexpr (DIM == 2) {
+        const auto& J = g.J;
+        // invJ * detJ = [[J11, -J01], [-J10, J00]]; dN_{k+1}/dx_f = invJ[k][f]
+        const double adj[2][2] = {{J[1][1], -J[0][1]}, {-J[1][0], J[0][0]}};
+#pragma unroll
+        for (int f = 0; f < 2; ++f) {
+            A[f][1] = refSize * adj[0][f];
+            A[f][2] = refSize * adj[1][f];
+            A[f][0] = -(A[f][1] + A[f][2]);
+        }
+    } else {
+        const auto& J = g.J;
+        double adj[3][3];
+        adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        adj[0][1] = J[2][1] * J[0][2] - J[2][2] * J[0][1];
+        adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+        adj[1][0] = J[2][0] * J[1][2] - J[1][0] * J[2][2];
+        adj[1][1] = J[0][0] * J[2][2] - J[2][0] * J[0][2];
+        adj[1][2] = J[1][0] * J[0][2] - J[0][0] * J[1][2];
+        adj[2][0] = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+        adj[2][1] = J[2][0] * J[0][1] - J[0][0] * J[2][1];
+        adj[2][2] = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            A[f][1] = refSize * adj[0][f];
+            A[f][2] = refSize * adj[1][f];
+            A[f][3] = refSize * adj[2][f];
+            A[f][0] = -(A[f][1] + A[f][2] + A[f][3]);
+        }
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void jacobian(const double* __restrict__ pos, int N, const int (&nd)[DIM + 1], Geom<DIM>& g) {
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+        const double o = pos[(size_t)r * N + nd[0]];
+#pragma unroll
+        for (int cc = 0; cc < DIM; ++cc) g.J[r][cc] = pos[(size_t)r * N + nd[cc + 1]] - o;
+    }
+    if constexpr (DIM == 2) {
+        g.detJ = g.J[0][0] * g.J[1][1] - g.J[1][0] * g.J[0][1];
+    } else {
+        const auto& J = g.J;
+        g.detJ = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] + J[0][2] * J[1][0] * J[2][1]
+               - J[2][0] * J[1][1] * J[0][2] - J[2][1] * J[1][2] * J[0][0] - J[2][2] * J[1][0] * J[0][1];
+    }
+}
+
+template <int DIM>
+__global__ void k_wc_predict(int N, const uint8_t* __restrict__ flags, double* __restrict__ s,
+                             double* __restrict__ pos, double* __restrict__ tdt) {
     const double dt = tdt[T_DT];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n == 0) tdt[T_TIME] += dt;  // Problem::updateTime with the step's dt
@@ -80,19 +147,22 @@ __global__ void k_wc_predict(int N, const uint8_t* __restrict__ flags, T* __rest
     const bool fixed = flags[n] & F_FIXED;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        T* v = s + (size_t)d * N;
-        const T* a = s + (size_t)(DIM + 2 + d) * N;
-        const T vh = v[n] + (T)(0.5 * dt) * a[n];
+        double* v = s + (size_t)d * N;
+        const double a = s[(size_t)(DIM + 2 + d) * N + n];
+        const double vh = v[n] + 0.5 * dt * a;
         v[n] = vh;
-        if (!fixed) pos[(size_t)d * N + n] += (double)vh * dt;
+        if (!fixed) pos[(size_t)d * N + n] += vh * dt;
     }
 }
 
-template <int DIM, class T>
+// Continuity (m_buildSystemdpdt): per element node i, ML_i = |e| s_i and
+//   cont_i = -dt (K0 s_i + K0' sum_j MM_ij p_j) |e| div v  [+ |e| sum_j MM_ij (p_j - p_i)  (Meduri)]
+template <int DIM, class R>
 __global__ void __launch_bounds__(BLOCK) k_wc_cont_elem(int E, int N, const int* __restrict__ conn,
-                                                        const double* __restrict__ pos, const T* __restrict__ s,
+                                                        const double* __restrict__ pos, const double* __restrict__ s,
                                                         const double* __restrict__ tdt, WcConst k,
-                                                        T* __restrict__ el) {
+                                                        R* __restrict__ elr) {
+    using L = ElLayout<DIM>;
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -100,163 +170,185 @@ __global__ void __launch_bounds__(BLOCK) k_wc_cont_elem(int E, int N, const int*
     int nd[NPE];
     load_nodes<DIM>(conn, E, e, nd);
     Geom<DIM> g;
-    compute_geom<DIM>(pos, N, nd, g);
-    double G[DIM][NPE];
-    grad_n<DIM>(g, G);
+    jacobian<DIM>(pos, N, nd, g);
+    double A[DIM][NPE];
+    area_gradients<DIM>(g, k.refSize, A);
     const double ae = g.detJ * k.refSize;
     double P[NPE];
-    double divv = 0;
+    R adiv = 0;  // |e| div v
 #pragma unroll
     for (int j = 0; j < NPE; ++j) {
-        P[j] = (double)s[(size_t)DIM * N + nd[j]];
+        P[j] = s[(size_t)DIM * N + nd[j]];
 #pragma unroll
-        for (int f = 0; f < DIM; ++f) divv += G[f][j] * (double)s[(size_t)f * N + nd[j]];
+        for (int f = 0; f < DIM; ++f) adiv += (R)A[f][j] * (R)s[(size_t)f * N + nd[j]];
     }
-    // sum_g w_g (K0 + K0' p(g)) N_i(g)
-    double swn[NPE];
-#pragma unroll
-    for (int i = 0; i < NPE; ++i) swn[i] = 0;
-    for (int q = 0; q < k.ng; ++q) {
-        double pg = 0;
-#pragma unroll
-        for (int j = 0; j < NPE; ++j) pg += k.N[q][j] * P[j];
-        const double fac = (k.K0 + k.K0p * pg) * k.w[q];
-#pragma unroll
-        for (int i = 0; i < NPE; ++i) swn[i] += fac * k.N[q][i];
-    }
+    R* out = elr + (size_t)e * L::NR;
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
-        double lumped = 0, mp = 0;
+        R mp = 0, mdp = 0;
 #pragma unroll
         for (int j = 0; j < NPE; ++j) {
-            const double mij = k.MM[i][j] * ae;
-            lumped += mij;
-            mp += mij * P[j];
+            mp += (R)k.MM[i][j] * (R)P[j];
+            mdp += (R)k.MM[i][j] * (R)(P[j] - P[i]);
         }
-        const double dv = ae * swn[i] * divv;
-        const double f0 = -dt * dv + (k.meduri ? mp : lumped * P[i]);
-        el[(size_t)i * E + e] = (T)lumped;
-        el[(size_t)(NPE + i) * E + e] = (T)f0;
+        const R swn = (R)(k.K0 * k.s[i]) + (R)k.K0p * mp;  // sum_g w (K0 + K0' p_g) N_i
+        R cont = -(R)dt * swn * adiv;
+        if (k.meduri) cont += (R)ae * mdp;
+        out[L::ML + i] = (R)(ae * k.s[i]);
+        out[L::CONT + i] = cont;
     }
 }
 
-template <int DIM, class T>
-__global__ void k_wc_cont_node(int N, int E, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
+// p = p_i + sum cont / sum ML (Meduri) or sum cont / sum ML + p_i*0 (lumped); free nodes p = 0
+// (m_applyBCdpdt, ContEquation.inl:343-348); rho from Tait-Murnaghan (:319-332).
+template <int DIM, class R>
+__global__ void k_wc_cont_node(int N, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
                                const uint8_t* __restrict__ ne_loc, const uint8_t* __restrict__ flags,
-                               const T* __restrict__ el, WcConst k, T* __restrict__ s) {
-    constexpr int NPE = DIM + 1;
+                               const R* __restrict__ elr, WcConst k, double* __restrict__ s) {
+    using L = ElLayout<DIM>;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     double m = 0, f0 = 0;
     for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        const int e = ne_elem[q], i = ne_loc[q];
-        m += (double)el[(size_t)i * E + e];
-        f0 += (double)el[(size_t)(NPE + i) * E + e];
+        const R* rec = elr + (size_t)ne_elem[q] * L::NR;
+        const int i = ne_loc[q];
+        m += (double)rec[L::ML + i];
+        f0 += (double)rec[L::CONT + i];
     }
-    double inv = 1 / m;
-    if (flags[n] & F_FREE) {  // m_applyBCdpdt (ContEquation.inl:343-348)
-        f0 = 0;
-        inv = 1;
+    double* P = s + (size_t)DIM * N;
+    double* rho = s + (size_t)(DIM + 1) * N;
+    if (flags[n] & F_FREE) {
+        P[n] = 0.0;
+        rho[n] = k.rho_star;  // ((K0'/K0) 0 + 1)^(1/K0') rho*
+        return;
     }
-    const double p = inv * f0;
-    const double rho = pow((k.K0p / k.K0) * p + 1, 1 / k.K0p) * k.rho_star;
-    s[(size_t)DIM * N + n] = (T)p;
-    s[(size_t)(DIM + 1) * N + n] = (T)rho;
+    // both forms: p_i ML + sum_e (...) over ML  ->  p_i + (sum)/ML   (Meduri);
+    // lumped form: (p_i ML - dt D v)/ML = p_i + (sum)/ML as well
+    const double inv = 1 / m;
+    const double p = P[n] + inv * f0;
+    P[n] = p;
+    if constexpr (sizeof(R) == 8) {
+        rho[n] = pow((k.K0p / k.K0) * p + 1, 1 / k.K0p) * k.rho_star;
+    } else {
+        // rho - rho* = rho* expm1(log1p(K0' p / K0) / K0'), evaluated in FP32
+        const float x = (float)((k.K0p / k.K0) * p);
+        const float d = expm1f(log1pf(x) * (float)(1 / k.K0p));
+        rho[n] = k.rho_star + k.rho_star * (double)d;
+    }
 }
 
-template <int DIM, class T>
+// Momentum (m_buildSystem): per element node i and direction f,
+//   MLrho_i = |e| sum_j MM_ij rho_j                      (diagBlock + lump of the rho-mass)
+//   Fs_fi   = -(K v)_fi + A_fi sum_j s_j (p_j - p_i) + MLrho_i g_f
+//   W_fi    = A_fi                                       (FP64; times p_i S at the node)
+template <int DIM, class R>
 __global__ void __launch_bounds__(BLOCK) k_wc_mom_elem(int E, int N, const int* __restrict__ conn,
-                                                       const double* __restrict__ pos, const T* __restrict__ s,
-                                                       WcConst k, T* __restrict__ el) {
+                                                       const double* __restrict__ pos, const double* __restrict__ s,
+                                                       WcConst k, R* __restrict__ elr, double* __restrict__ eld) {
+    using L = ElLayout<DIM>;
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[NPE];
     load_nodes<DIM>(conn, E, e, nd);
     Geom<DIM> g;
-    compute_geom<DIM>(pos, N, nd, g);
-    double G[DIM][NPE];
-    grad_n<DIM>(g, G);
+    jacobian<DIM>(pos, N, nd, g);
+    double Ad[DIM][NPE];
+    area_gradients<DIM>(g, k.refSize, Ad);
     const double ae = g.detJ * k.refSize;
-    double P[NPE], Rh[NPE], V[DIM][NPE];
+    R A[DIM][NPE], V[DIM][NPE], Rh[NPE];
+    double P[NPE];
 #pragma unroll
     for (int j = 0; j < NPE; ++j) {
-        P[j] = (double)s[(size_t)DIM * N + nd[j]];
-        Rh[j] = (double)s[(size_t)(DIM + 1) * N + nd[j]];
+        P[j] = s[(size_t)DIM * N + nd[j]];
+        Rh[j] = (R)s[(size_t)(DIM + 1) * N + nd[j]];
 #pragma unroll
-        for (int f = 0; f < DIM; ++f) V[f][j] = (double)s[(size_t)f * N + nd[j]];
-    }
-    // sum_g w rho(g) N_i(g) N_j(g)  and  sum_g w rho(g) N_i(g)
-    double mt[NPE][NPE], fr[NPE];
-#pragma unroll
-    for (int i = 0; i < NPE; ++i) {
-        fr[i] = 0;
-#pragma unroll
-        for (int j = 0; j < NPE; ++j) mt[i][j] = 0;
-    }
-    for (int q = 0; q < k.ng; ++q) {
-        double rg = 0;
-#pragma unroll
-        for (int j = 0; j < NPE; ++j) rg += k.N[q][j] * Rh[j];
-        const double fw = rg * k.w[q];
-#pragma unroll
-        for (int i = 0; i < NPE; ++i) {
-            fr[i] += fw * k.N[q][i];
-#pragma unroll
-            for (int j = 0; j < NPE; ++j) mt[i][j] += fw * k.N[q][i] * k.N[q][j];
+        for (int f = 0; f < DIM; ++f) {
+            V[f][j] = (R)s[(size_t)f * N + nd[j]];
+            A[f][j] = (R)Ad[f][j];
         }
     }
-    // sum_j s_j p_j (pressure term D^T p: |e| dN_i/dx_f sum_j s_j p_j)
-    double sp = 0;
+    // velocity gradient times |e|: Lg[a][b] = sum_j A[b][j] v_a(j); divA = trace
+    R Lg[DIM][DIM];
+    R divA = 0;
 #pragma unroll
-    for (int j = 0; j < NPE; ++j) sp += k.s[j] * P[j];
-    const double kf = ae * k.mu_sum;
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) {
+            R t = 0;
+#pragma unroll
+            for (int j = 0; j < NPE; ++j) t += A[b][j] * V[a][j];
+            Lg[a][b] = t;
+        }
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) divA += Lg[a][a];
+    // K v with Ddev = [4/3 -2/3; -2/3 4/3] (normal) and 1 (shear), MomEquation.inl:63-83:
+    //   (K v)_{f1,i} = mu_sum/|e| [ sum_j (A_i.A_j) v_f1(j) + sum_f2 A_f2,i Lg[f2][f1] - 2/3 A_f1,i divA ]
+    const R kf = (R)(k.mu_sum / ae);
+    R* out = elr + (size_t)e * L::NR;
+    double* outd = eld + (size_t)e * L::ND;
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
-        double lumped = 0;
+        R mr = 0, dp = 0;
 #pragma unroll
-        for (int j = 0; j < NPE; ++j) lumped += mt[i][j] * ae;
-        el[(size_t)i * E + e] = (T)lumped;
+        for (int j = 0; j < NPE; ++j) {
+            mr += (R)k.MM[i][j] * Rh[j];
+            dp += (R)k.s[j] * (R)(P[j] - P[i]);
+        }
+        const R mlr = (R)ae * mr;
+        out[L::MLR + i] = mlr;
+        R gg[NPE];
+#pragma unroll
+        for (int j = 0; j < NPE; ++j) {
+            R t = 0;
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) t += A[f][i] * A[f][j];
+            gg[j] = t;
+        }
 #pragma unroll
         for (int f1 = 0; f1 < DIM; ++f1) {
-            // (K v)(i f1) with Ddev = [4/3 -2/3 ..; ..] (normal) and 1 (shear), MomEquation.inl:63-83
-            double kv = 0;
+            R kv = 0;
 #pragma unroll
-            for (int j = 0; j < NPE; ++j) {
-                double dot = 0;
+            for (int j = 0; j < NPE; ++j) kv += gg[j] * V[f1][j];
 #pragma unroll
-                for (int f = 0; f < DIM; ++f) dot += G[f][i] * G[f][j];
-#pragma unroll
-                for (int f2 = 0; f2 < DIM; ++f2) {
-                    const double kk = (f1 == f2 ? dot : 0.0) + G[f2][i] * G[f1][j] - (2.0 / 3.0) * G[f1][i] * G[f2][j];
-                    kv += kf * kk * V[f2][j];
-                }
-            }
-            const double dtp = ae * G[f1][i] * sp;
-            const double F = ae * fr[i] * k.g[f1];
-            el[(size_t)(NPE + f1 * NPE + i) * E + e] = (T)(-kv + dtp + F);
+            for (int f2 = 0; f2 < DIM; ++f2) kv += A[f2][i] * Lg[f2][f1];
+            kv -= (R)(2.0 / 3.0) * A[f1][i] * divA;
+            out[L::FS + f1 * NPE + i] = -kf * kv + A[f1][i] * dp + mlr * (R)k.g[f1];
+            outd[f1 * NPE + i] = Ad[f1][i];
         }
     }
 }
 
-template <int DIM, class T>
-__global__ void k_wc_mom_node(int N, int E, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
+// a = F / M with the momentum BCs (MomEquation.inl:341-372); v = v1/2 + dt/2 a.  Also the
+// per-node quantities of computeNextDT: max(u^2, c^2) and mu/rho.
+template <int DIM, class R>
+__global__ void k_wc_mom_node(int N, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
                               const uint8_t* __restrict__ ne_loc, const uint8_t* __restrict__ flags,
-                              const T* __restrict__ el, const double* __restrict__ vbc, const double* __restrict__ tdt,
-                              WcConst k, T* __restrict__ s) {
+                              const R* __restrict__ elr, const double* __restrict__ eld,
+                              const double* __restrict__ vbc, const double* __restrict__ tdt, WcConst k,
+                              double* __restrict__ s, R* __restrict__ nodal) {
+    using L = ElLayout<DIM>;
     constexpr int NPE = DIM + 1;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     const double dt = tdt[T_DT];
-    double m = 0, F[DIM];
+    double m = 0, F[DIM], W[DIM];
 #pragma unroll
-    for (int f = 0; f < DIM; ++f) F[f] = 0;
+    for (int f = 0; f < DIM; ++f) F[f] = W[f] = 0;
     for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
         const int e = ne_elem[q], i = ne_loc[q];
-        m += (double)el[(size_t)i * E + e];
+        const R* rec = elr + (size_t)e * L::NR;
+        const double* recd = eld + (size_t)e * L::ND;
+        m += (double)rec[L::MLR + i];
 #pragma unroll
-        for (int f = 0; f < DIM; ++f) F[f] += (double)el[(size_t)(NPE + f * NPE + i) * E + e];
+        for (int f = 0; f < DIM; ++f) {
+            F[f] += (double)rec[L::FS + f * NPE + i];
+            W[f] += recd[f * NPE + i];
+        }
     }
+    const double pS = s[(size_t)DIM * N + n] * k.S;
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) F[f] += pS * W[f];
     double inv = 1 / m;
     const uint8_t fl = flags[n];
     if ((fl & F_FREE) && !(fl & F_BOUND)) {  // free fall (MomEquation.inl:347-354)
@@ -268,20 +360,29 @@ __global__ void k_wc_mom_node(int N, int E, const int* __restrict__ ne_ptr, cons
         for (int f = 0; f < DIM; ++f) F[f] = vbc[(size_t)f * N + n];
         inv = 1;
     }
+    double u2 = 0;
 #pragma unroll
     for (int f = 0; f < DIM; ++f) {
         const double a = inv * F[f];
-        T* v = s + (size_t)f * N;
-        s[(size_t)(DIM + 2 + f) * N + n] = (T)a;
-        v[n] = (T)((double)v[n] + 0.5 * dt * a);
+        s[(size_t)(DIM + 2 + f) * N + n] = a;
+        const double v = s[(size_t)f * N + n] + 0.5 * dt * a;
+        s[(size_t)f * N + n] = v;
+        u2 += v * v;
+    }
+    if (nodal) {
+        const double p = s[(size_t)DIM * N + n], rho = s[(size_t)(DIM + 1) * N + n];
+        const double c2 = (k.K0 + k.K0p * p) / rho;
+        nodal[n] = (R)fmax(u2, c2);
+        nodal[(size_t)N + n] = (R)(k.mu / rho);
     }
 }
 
-// computeNextDT: one thread per element, block min, grid min by the last block.
-template <int DIM, class T>
+// computeNextDT: dt^2_e = sc^2 he^2 / max_nodes(max(u^2, c^2), 4 alpha^2/he^2), he = 2 Rin;
+// block min, grid min by the last block, dt = min(sqrt(min), maxDT).
+template <int DIM, class R>
 __global__ void __launch_bounds__(BLOCK) k_wc_dt(int E, int N, const int* __restrict__ conn,
-                                                 const double* __restrict__ pos, const T* __restrict__ s, WcConst k,
-                                                 double* __restrict__ partials, double* __restrict__ tdt) {
+                                                 const double* __restrict__ pos, const R* __restrict__ nodal,
+                                                 WcConst k, double* __restrict__ partials, double* __restrict__ tdt) {
     __shared__ double sh[32];
     double best = 1.79769313486231570e308;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
@@ -292,45 +393,38 @@ __global__ void __launch_bounds__(BLOCK) k_wc_dt(int E, int N, const int* __rest
         for (int a = 0; a <= DIM; ++a)
 #pragma unroll
             for (int d = 0; d < DIM; ++d) X[a][d] = pos[(size_t)d * N + nd[a]];
-        Geom<DIM> g;
-        compute_geom<DIM>(pos, N, nd, g);
-        const double size = g.detJ * k.refSize;
-        double he;
+        R he;
         if constexpr (DIM == 2) {  // Element::getRin 2D (Element.cpp:228-241)
+            const double j00 = X[1][0] - X[0][0], j01 = X[2][0] - X[0][0];
+            const double j10 = X[1][1] - X[0][1], j11 = X[2][1] - X[0][1];
+            const R size = (R)((j00 * j11 - j10 * j01) * k.refSize);
             auto dist = [&](int a, int b) {
-                const double dx = X[a][0] - X[b][0], dy = X[a][1] - X[b][1];
+                const R dx = (R)(X[a][0] - X[b][0]), dy = (R)(X[a][1] - X[b][1]);
                 return sqrt(dx * dx + dy * dy);
             };
-            const double sp = (dist(0, 1) + dist(1, 2) + dist(0, 2)) / 2;
-            he = 2 * (size / sp);
+            const R sp = (dist(0, 1) + dist(1, 2) + dist(0, 2)) / (R)2;
+            he = (R)2 * (size / sp);
         } else {  // Element::getRin 3D (Element.cpp:242-293)
+            Geom<3> g;
+            jacobian<3>(pos, N, nd, g);
+            const R size = (R)(g.detJ * k.refSize);
             auto nrm = [&](int a0, int a1, int a2) {
-                const double ux = X[a1][0] - X[a0][0], uy = X[a1][1] - X[a0][1], uz = X[a1][2] - X[a0][2];
-                const double wx = X[a2][0] - X[a0][0], wy = X[a2][1] - X[a0][1], wz = X[a2][2] - X[a0][2];
-                const double cx = uy * wz - uz * wy, cy = uz * wx - ux * wz, cz = ux * wy - uy * wx;
+                const R ux = (R)(X[a1][0] - X[a0][0]), uy = (R)(X[a1][1] - X[a0][1]), uz = (R)(X[a1][2] - X[a0][2]);
+                const R wx = (R)(X[a2][0] - X[a0][0]), wy = (R)(X[a2][1] - X[a0][1]), wz = (R)(X[a2][2] - X[a0][2]);
+                const R cx = uy * wz - uz * wy, cy = uz * wx - ux * wz, cz = ux * wy - uy * wx;
                 return sqrt(cx * cx + cy * cy + cz * cz);
             };
-            const double sum = nrm(0, 1, 2) + nrm(0, 3, 2) + nrm(0, 1, 3) + nrm(3, 1, 2);
-            he = 2 * (6 * size / sum);
+            const R sum = nrm(0, 1, 2) + nrm(0, 3, 2) + nrm(0, 1, 3) + nrm(3, 1, 2);
+            he = (R)2 * ((R)6 * size / sum);
         }
-        double maxSq = 0;
+        R m1 = 0, m2 = 0;
 #pragma unroll
         for (int a = 0; a <= DIM; ++a) {
-            const int n = nd[a];
-            const double p = (double)s[(size_t)DIM * N + n];
-            const double rho = (double)s[(size_t)(DIM + 1) * N + n];
-            const double c2 = (k.K0 + k.K0p * p) / rho;
-            double u2 = 0;
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                const double v = (double)s[(size_t)d * N + n];
-                u2 += v * v;
-            }
-            const double alpha = k.mu / rho;
-            maxSq = fmax(fmax(u2, c2), maxSq);
-            maxSq = fmax(maxSq, 4 * alpha * alpha / (he * he));
+            m1 = fmax(m1, nodal[nd[a]]);
+            m2 = fmax(m2, nodal[(size_t)N + nd[a]]);
         }
-        best = fmin(best, k.sc * k.sc * he * he / maxSq);
+        const R maxSq = fmax(m1, (R)4 * m2 * m2 / (he * he));
+        best = fmin(best, (double)((R)(k.sc * k.sc) * he * he / maxSq));
     }
     best = block_min<BLOCK>(best, sh);
     __shared__ bool last;
@@ -343,19 +437,31 @@ __global__ void __launch_bounds__(BLOCK) k_wc_dt(int E, int N, const int* __rest
     __syncthreads();
     if (!last) return;
     __threadfence();
-    double m = 1.79769313486231570e308;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += BLOCK) m = fmin(m, ((volatile double*)partials)[i]);
-    m = block_min<BLOCK>(m, sh);
+    double mn = 1.79769313486231570e308;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += BLOCK) mn = fmin(mn, ((volatile double*)partials)[i]);
+    mn = block_min<BLOCK>(mn, sh);
     if (threadIdx.x == 0) {
-        tdt[T_DT] = fmin(sqrt(m), k.max_dt);
-        tdt[T_MIN] = m;
+        tdt[T_DT] = fmin(sqrt(mn), k.max_dt);
+        tdt[T_MIN] = mn;
         *ticket = 0u;
     }
 }
 
+// per-node dt quantities from the current state (for pfg_next_dt outside a step)
+template <class R>
+__global__ void k_wc_nodal(int N, int dim, const double* __restrict__ s, WcConst k, R* __restrict__ nodal) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    double u2 = 0;
+    for (int f = 0; f < dim; ++f) u2 += s[(size_t)f * N + n] * s[(size_t)f * N + n];
+    const double p = s[(size_t)dim * N + n], rho = s[(size_t)(dim + 1) * N + n];
+    nodal[n] = (R)fmax(u2, (k.K0 + k.K0p * p) / rho);
+    nodal[(size_t)N + n] = (R)(k.mu / rho);
+}
+
 template <int DIM>
 __global__ void k_wc_mass(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
-                          const void* __restrict__ sv, int fp32, double refSize, double* partials, unsigned* ticket,
+                          const double* __restrict__ s, double refSize, double* partials, unsigned* ticket,
                           double* out) {
     __shared__ double sh[32];
     double acc = 0;
@@ -363,69 +469,57 @@ __global__ void k_wc_mass(int E, int N, const int* __restrict__ conn, const doub
         int nd[DIM + 1];
         load_nodes<DIM>(conn, E, e, nd);
         Geom<DIM> g;
-        compute_geom<DIM>(pos, N, nd, g);
+        jacobian<DIM>(pos, N, nd, g);
         double mid = 0;
 #pragma unroll
-        for (int a = 0; a <= DIM; ++a) {
-            const size_t k = (size_t)(DIM + 1) * N + nd[a];
-            mid += fp32 ? (double)static_cast<const float*>(sv)[k] : static_cast<const double*>(sv)[k];
-        }
+        for (int a = 0; a <= DIM; ++a) mid += s[(size_t)(DIM + 1) * N + nd[a]];
         mid /= (double)(DIM + 1);
         acc += mid * (g.detJ * refSize);
     }
     grid_sum_last<BLOCK>(acc, partials, ticket, sh, out);
 }
 
-template <class T>
-__global__ void k_convert_in(size_t n, const double* __restrict__ src, T* __restrict__ dst) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = (T)src[i];
-}
-
-template <class T>
-__global__ void k_convert_out(size_t n, const T* __restrict__ src, double* __restrict__ dst) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = (double)src[i];
-}
-
-bool fp32(pfg_ctx* c) { return c->prm.precision == PFG_PREC_MIXED; }
-
 __global__ void k_set_value(double* p, double v) { *p = v; }
 
-template <int DIM, class T>
+bool mixed(pfg_ctx* c) { return c->prm.precision == PFG_PREC_MIXED; }
+
+template <int DIM, class R>
 int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
     const int N = c->N, E = c->E;
-    T* s = ptr<T>(c->ws);
-    T* el = ptr<T>(c->wc_el);
+    double* s = ptr<double>(c->ws);
+    R* elr = ptr<R>(c->wc_el);
+    double* eld = ptr<double>(c->wc_eld);
+    R* nodal = ptr<R>(c->wc_nodal);
     double* tdt = ptr<double>(c->wc_dt);
     const int gn = div_up(N, BLOCK), ge = std::max(1, div_up(E, BLOCK));
     prof_begin(c, PH_WC_PREDICT);
-    k_wc_predict<DIM, T><<<gn, BLOCK, 0, c->stream>>>(N, ptr<uint8_t>(c->flags), s, ptr<double>(c->pos), tdt);
+    k_wc_predict<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<uint8_t>(c->flags), s, ptr<double>(c->pos), tdt);
     prof_end(c, PH_WC_PREDICT);
     if (E > 0) {
         prof_begin(c, PH_WC_CONT_ELEM);
-        k_wc_cont_elem<DIM, T><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, tdt, k,
-                                                            el);
+        k_wc_cont_elem<DIM, R><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, tdt, k,
+                                                            elr);
         prof_end(c, PH_WC_CONT_ELEM);
     }
     prof_begin(c, PH_WC_CONT_NODE);
-    k_wc_cont_node<DIM, T><<<gn, BLOCK, 0, c->stream>>>(N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
-                                                        ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags), el, k, s);
+    k_wc_cont_node<DIM, R><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
+                                                        ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags), elr, k, s);
     prof_end(c, PH_WC_CONT_NODE);
     if (E > 0) {
         prof_begin(c, PH_WC_MOM_ELEM);
-        k_wc_mom_elem<DIM, T><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, k, el);
+        k_wc_mom_elem<DIM, R><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, k, elr,
+                                                           eld);
         prof_end(c, PH_WC_MOM_ELEM);
     }
     prof_begin(c, PH_WC_MOM_NODE);
-    k_wc_mom_node<DIM, T><<<gn, BLOCK, 0, c->stream>>>(N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
-                                                       ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags), el,
-                                                       ptr<double>(c->vbc), tdt, k, s);
+    k_wc_mom_node<DIM, R><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
+                                                       ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags), elr, eld,
+                                                       ptr<double>(c->vbc), tdt, k, s, adapt ? nodal : nullptr);
     prof_end(c, PH_WC_MOM_NODE);
     if (adapt && E > 0) {
         const int grid = std::min(c->max_grid, ge);
         prof_begin(c, PH_WC_DT);
-        k_wc_dt<DIM, T><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, k,
+        k_wc_dt<DIM, R><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), nodal, k,
                                                        ptr<double>(c->red), tdt);
         prof_end(c, PH_WC_DT);
     }
@@ -433,27 +527,70 @@ int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
     return PFG_OK;
 }
 
-template <int DIM, class T>
+int launch_any(pfg_ctx* c, bool adapt, const WcConst& k) {
+    if (c->dim == 2) return mixed(c) ? launch_step<2, float>(c, adapt, k) : launch_step<2, double>(c, adapt, k);
+    return mixed(c) ? launch_step<3, float>(c, adapt, k) : launch_step<3, double>(c, adapt, k);
+}
+
+template <int DIM, class R>
 int dt_only(pfg_ctx* c, const WcConst& k) {
-    const int E = c->E;
+    const int E = c->E, N = c->N;
     if (E == 0) return fail(c, PFG_ERR_STATE, "no elements");
+    k_wc_nodal<R><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, DIM, ptr<double>(c->ws), k, ptr<R>(c->wc_nodal));
     const int grid = std::min(c->max_grid, div_up(E, BLOCK));
-    k_wc_dt<DIM, T><<<grid, BLOCK, 0, c->stream>>>(E, c->N, ptr<int>(c->conn), ptr<double>(c->pos), ptr<T>(c->ws), k,
-                                                   ptr<double>(c->red), ptr<double>(c->wc_dt));
+    k_wc_dt<DIM, R><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), ptr<R>(c->wc_nodal),
+                                                   k, ptr<double>(c->red), ptr<double>(c->wc_dt));
     PFG_CHECK_LAUNCH(c);
+    return PFG_OK;
+}
+
+// Capture one step (per dt mode) into a CUDA graph; replayed for every step.
+int step_graph(pfg_ctx* c, bool adapt, cudaGraphExec_t* out) {
+    cudaGraphExec_t& ex = c->wc_graph[adapt ? 1 : 0];
+    if (!ex) {
+        const WcConst k = make_const(c);
+        cudaGraph_t g = nullptr;
+        PFG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = launch_any(c, adapt, k);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            ex = nullptr;
+            return cuda_fail(c, e, "cudaGraphInstantiate");
+        }
+    }
+    *out = ex;
     return PFG_OK;
 }
 
 }  // namespace
 
+void wc_release_graphs(pfg_ctx* c) {
+    for (auto& g : c->wc_graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
 int wc_alloc(pfg_ctx* c) {
-    const size_t es = fp32(c) ? sizeof(float) : sizeof(double);
+    const size_t rs = mixed(c) ? sizeof(float) : sizeof(double);
     const size_t N = c->N, E = std::max(c->E, 1);
+    const int nr = c->dim == 2 ? ElLayout<2>::NR : ElLayout<3>::NR;
+    const int ndd = c->dim == 2 ? ElLayout<2>::ND : ElLayout<3>::ND;
     int rc;
-    if ((rc = ensure(c, c->ws, es * (2 * c->dim + 2) * N)) ||
-        (rc = ensure(c, c->wc_el, es * (size_t)(c->dim + 1) * c->npe * E)) || (rc = ensure(c, c->wc_dt, 64)))
+    wc_release_graphs(c);
+    if ((rc = ensure(c, c->ws, sizeof(double) * (2 * c->dim + 2) * N)) ||
+        (rc = ensure(c, c->wc_el, rs * (size_t)nr * E)) || (rc = ensure(c, c->wc_eld, sizeof(double) * ndd * E)) ||
+        (rc = ensure(c, c->wc_nodal, rs * 2 * N)) || (rc = ensure(c, c->wc_dt, 64)))
         return rc;
-    PFG_CUDA(c, cudaMemsetAsync(c->ws.p, 0, es * (2 * c->dim + 2) * N, c->stream));
+    PFG_CUDA(c, cudaMemsetAsync(c->ws.p, 0, sizeof(double) * (2 * c->dim + 2) * N, c->stream));
     double h[4] = {c->prm.max_dt, c->host_time, 0.0, 0.0};
     PFG_CUDA(c, cudaMemcpyAsync(c->wc_dt.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -462,32 +599,14 @@ int wc_alloc(pfg_ctx* c) {
 
 int wc_set_states(pfg_ctx* c, const double* h) {
     const size_t n = (size_t)(2 * c->dim + 2) * c->N;
-    if (!fp32(c)) {
-        PFG_CUDA(c, cudaMemcpyAsync(c->ws.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    } else {
-        int rc = ensure(c, c->stage, sizeof(double) * n);
-        if (rc) return rc;
-        PFG_CUDA(c, cudaMemcpyAsync(c->stage.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-        k_convert_in<float><<<std::min(c->max_grid, div_up((long long)n, BLOCK)), BLOCK, 0, c->stream>>>(
-            n, ptr<double>(c->stage), ptr<float>(c->ws));
-        PFG_CHECK_LAUNCH(c);
-    }
+    PFG_CUDA(c, cudaMemcpyAsync(c->ws.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PFG_OK;
 }
 
 int wc_get_states(pfg_ctx* c, double* h) {
     const size_t n = (size_t)(2 * c->dim + 2) * c->N;
-    if (!fp32(c)) {
-        PFG_CUDA(c, cudaMemcpyAsync(h, c->ws.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-    } else {
-        int rc = ensure(c, c->stage, sizeof(double) * n);
-        if (rc) return rc;
-        k_convert_out<float><<<std::min(c->max_grid, div_up((long long)n, BLOCK)), BLOCK, 0, c->stream>>>(
-            n, ptr<float>(c->ws), ptr<double>(c->stage));
-        PFG_CHECK_LAUNCH(c);
-        PFG_CUDA(c, cudaMemcpyAsync(h, c->stage.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-    }
+    PFG_CUDA(c, cudaMemcpyAsync(h, c->ws.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PFG_OK;
 }
@@ -498,14 +617,18 @@ int wc_enqueue(pfg_ctx* c, double dt, int nsteps) {
         k_set_value<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt) + T_DT, dt);
         PFG_CHECK_LAUNCH(c);
     }
-    const WcConst k = make_const(c);
-    for (int i = 0; i < nsteps; ++i) {
-        int rc;
-        if (c->dim == 2)
-            rc = fp32(c) ? launch_step<2, float>(c, adapt, k) : launch_step<2, double>(c, adapt, k);
-        else
-            rc = fp32(c) ? launch_step<3, float>(c, adapt, k) : launch_step<3, double>(c, adapt, k);
+    if (c->prof) {
+        // phase timers need events between kernels: launch directly
+        const WcConst k = make_const(c);
+        for (int i = 0; i < nsteps; ++i) {
+            int rc = launch_any(c, adapt, k);
+            if (rc) return rc;
+        }
+    } else {
+        cudaGraphExec_t ex;
+        int rc = step_graph(c, adapt, &ex);
         if (rc) return rc;
+        for (int i = 0; i < nsteps; ++i) PFG_CUDA(c, cudaGraphLaunch(ex, c->stream));
     }
     c->wc_pending += nsteps;
     return PFG_OK;
@@ -535,9 +658,9 @@ int wc_next_dt(pfg_ctx* c, double* dt) {
     const WcConst k = make_const(c);
     int rc;
     if (c->dim == 2)
-        rc = fp32(c) ? dt_only<2, float>(c, k) : dt_only<2, double>(c, k);
+        rc = mixed(c) ? dt_only<2, float>(c, k) : dt_only<2, double>(c, k);
     else
-        rc = fp32(c) ? dt_only<3, float>(c, k) : dt_only<3, double>(c, k);
+        rc = mixed(c) ? dt_only<3, float>(c, k) : dt_only<3, double>(c, k);
     if (rc) return rc;
     PFG_CUDA(c, cudaMemcpyAsync(dt, c->wc_dt.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -551,11 +674,11 @@ int wc_mass(pfg_ctx* c, double* out) {
     const GaussConst g = gauss_const(c->dim);
     const int grid = std::max(1, std::min(c->max_grid, div_up(std::max(c->E, 1), BLOCK)));
     if (c->dim == 2)
-        k_wc_mass<2><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos), c->ws.p,
-                                                    fp32(c), g.refSize, red, ticket, res);
+        k_wc_mass<2><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos),
+                                                    ptr<double>(c->ws), g.refSize, red, ticket, res);
     else
-        k_wc_mass<3><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos), c->ws.p,
-                                                    fp32(c), g.refSize, red, ticket, res);
+        k_wc_mass<3><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos),
+                                                    ptr<double>(c->ws), g.refSize, red, ticket, res);
     PFG_CHECK_LAUNCH(c);
     PFG_CUDA(c, cudaMemcpyAsync(c->h_scalars, res, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
