@@ -7,8 +7,11 @@ lattice jittered +-0.1h (seeded), Delaunay + alpha shape (alpha = 1.2): ~82k nod
 triangles; Tait-Murnaghan EOS (rho* = 1000, K0 = 2.2e7 Pa, K0' = 7), CDS_dpdt with Meduri
 stabilisation, CFL security coefficient 0.3, adaptive dt.  One "step" is one explicit time step
 of the whole mesh (SolverWCompNewton::solveOneTimeStep without the host remesh) followed by
-the CFL dt update (computeNextDT).  The state is FP32 by default ("FP32 state with FP64 mass
-sums"), --precision fp64 runs the plain FP64 form.
+the CFL dt update (computeNextDT).  By default the mixed form runs: FP32 arithmetic only, with
+positions, velocities and pressures kept as double-float (two-FP32) pairs and FP64 mass sums
+(GB300 issues FP64 at 1/64 of the FP32 rate, so a plain FP32 state would lose ~1e-6 accuracy
+over the 2000 steps while FP64 arithmetic would bind on the FP64 pipe); --precision fp64 runs
+the plain FP64 form.
 
 Timing: W warm-up steps, then K steps, each timed with CUDA events on the library's own
 stream, with a 256 MB write between steps to flush L2 (the state is ~7 MB and would otherwise

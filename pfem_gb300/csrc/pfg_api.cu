@@ -372,6 +372,7 @@ PFG_API int pfg_get_positions(pfg_ctx* c, double* pos) {
     if (rc) return rc;
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
     if (!pos) return fail(c, PFG_ERR_INVALID, "null positions");
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT && (rc = wc_sync_positions(c))) return rc;
     PFG_CUDA(c, cudaMemcpyAsync(pos, c->pos.p, sizeof(double) * c->dim * c->N, cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PFG_OK;
@@ -411,6 +412,7 @@ PFG_API int pfg_set_dirichlet(pfg_ctx* c, int32_t n, const int32_t* nodes, const
     c->bytes_in_use -= tmp.cap;
     release(tmp);
     if (e != cudaSuccess) return cuda_fail(c, e, "pfg_set_dirichlet");
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT) return wc_dirichlet_changed(c);
     return PFG_OK;
 }
 
@@ -471,11 +473,7 @@ PFG_API int pfg_set_time(pfg_ctx* c, double time, double next_dt) {
     if (rc) return rc;
     if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
-    double h[2] = {next_dt, time};
-    PFG_CUDA(c, cudaMemcpyAsync(c->wc_dt.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
-    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
-    c->host_time = time;
-    return PFG_OK;
+    return wc_set_time(c, time, next_dt);
 }
 
 PFG_API int pfg_volume(pfg_ctx* c, double* v) {
@@ -483,6 +481,7 @@ PFG_API int pfg_volume(pfg_ctx* c, double* v) {
     if (rc) return rc;
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
     if (!v) return fail(c, PFG_ERR_INVALID, "null output");
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT && (rc = wc_sync_positions(c))) return rc;
     return volume(c, v);
 }
 
@@ -500,6 +499,7 @@ PFG_API int pfg_tip(pfg_ctx* c, int32_t coord, int32_t want_max, double* v) {
     if (rc) return rc;
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
     if (!v || coord < 0 || coord >= c->dim) return fail(c, PFG_ERR_INVALID, "bad coordinate");
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT && (rc = wc_sync_positions(c))) return rc;
     return tip(c, coord, want_max, v);
 }
 

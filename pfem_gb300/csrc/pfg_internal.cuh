@@ -184,5 +184,19 @@ int wc_enqueue(pfg_ctx* c, double dt, int nsteps);
 int wc_sync(pfg_ctx* c, pfg_step_status* st);
 int wc_next_dt(pfg_ctx* c, double* dt);
 int wc_mass(pfg_ctx* c, double* out);
+int wc_set_time(pfg_ctx* c, double time, double next_dt);
+int wc_dirichlet_changed(pfg_ctx* c);
+int wc_sync_positions(pfg_ctx* c);
+// mixed form (pfg_wc_mixed.cu)
+size_t wcm_state_bytes(pfg_ctx* c);
+size_t wcm_elem_bytes(pfg_ctx* c);
+int wcm_launch_step(pfg_ctx* c, bool adapt);
+int wcm_positions_in(pfg_ctx* c);
+int wcm_positions_out(pfg_ctx* c);
+int wcm_set_states(pfg_ctx* c, const double* h);
+int wcm_get_states(pfg_ctx* c, double* h);
+int wcm_state_to_stage(pfg_ctx* c);
+int wcm_vbc_refresh(pfg_ctx* c);
+int wcm_next_dt(pfg_ctx* c);
 
 }  // namespace pfg

@@ -479,12 +479,23 @@ __global__ void k_wc_mass(int E, int N, const int* __restrict__ conn, const doub
     grid_sum_last<BLOCK>(acc, partials, ticket, sh, out);
 }
 
-__global__ void k_set_value(double* p, double v) { *p = v; }
+// dt in both precisions: the plain step reads the double, the mixed step the float copy
+__global__ void k_set_dt(double* tdt, double v) {
+    tdt[T_DT] = v;
+    reinterpret_cast<float*>(tdt + 4)[0] = (float)v;
+}
+
+__global__ void k_set_time(double* tdt, double t, double v) {
+    tdt[T_DT] = v;
+    tdt[T_TIME] = t;
+    reinterpret_cast<float*>(tdt + 4)[0] = (float)v;
+}
 
 bool mixed(pfg_ctx* c) { return c->prm.precision == PFG_PREC_MIXED; }
 
-template <int DIM, class R>
+template <int DIM>
 int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
+    using R = double;
     const int N = c->N, E = c->E;
     double* s = ptr<double>(c->ws);
     R* elr = ptr<R>(c->wc_el);
@@ -527,13 +538,15 @@ int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
     return PFG_OK;
 }
 
-int launch_any(pfg_ctx* c, bool adapt, const WcConst& k) {
-    if (c->dim == 2) return mixed(c) ? launch_step<2, float>(c, adapt, k) : launch_step<2, double>(c, adapt, k);
-    return mixed(c) ? launch_step<3, float>(c, adapt, k) : launch_step<3, double>(c, adapt, k);
+int launch_any(pfg_ctx* c, bool adapt) {
+    if (mixed(c)) return wcm_launch_step(c, adapt);
+    const WcConst k = make_const(c);
+    return c->dim == 2 ? launch_step<2>(c, adapt, k) : launch_step<3>(c, adapt, k);
 }
 
-template <int DIM, class R>
+template <int DIM>
 int dt_only(pfg_ctx* c, const WcConst& k) {
+    using R = double;
     const int E = c->E, N = c->N;
     if (E == 0) return fail(c, PFG_ERR_STATE, "no elements");
     k_wc_nodal<R><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, DIM, ptr<double>(c->ws), k, ptr<R>(c->wc_nodal));
@@ -548,10 +561,9 @@ int dt_only(pfg_ctx* c, const WcConst& k) {
 int step_graph(pfg_ctx* c, bool adapt, cudaGraphExec_t* out) {
     cudaGraphExec_t& ex = c->wc_graph[adapt ? 1 : 0];
     if (!ex) {
-        const WcConst k = make_const(c);
         cudaGraph_t g = nullptr;
         PFG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = launch_any(c, adapt, k);
+        int rc = launch_any(c, adapt);
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
@@ -579,25 +591,61 @@ void wc_release_graphs(pfg_ctx* c) {
         }
 }
 
+// Buffers.  Plain form: ws = FP64 states (2d+2)N, wc_el/wc_eld = element partials, wc_nodal =
+// FP64 CFL quantities.  Mixed form: ws = double-float state, wc_el = FP32 element records,
+// wc_nodal = FP32 CFL quantities, wc_eld = FP32 copy of the Dirichlet velocities.
 int wc_alloc(pfg_ctx* c) {
-    const size_t rs = mixed(c) ? sizeof(float) : sizeof(double);
     const size_t N = c->N, E = std::max(c->E, 1);
-    const int nr = c->dim == 2 ? ElLayout<2>::NR : ElLayout<3>::NR;
-    const int ndd = c->dim == 2 ? ElLayout<2>::ND : ElLayout<3>::ND;
     int rc;
     wc_release_graphs(c);
-    if ((rc = ensure(c, c->ws, sizeof(double) * (2 * c->dim + 2) * N)) ||
-        (rc = ensure(c, c->wc_el, rs * (size_t)nr * E)) || (rc = ensure(c, c->wc_eld, sizeof(double) * ndd * E)) ||
-        (rc = ensure(c, c->wc_nodal, rs * 2 * N)) || (rc = ensure(c, c->wc_dt, 64)))
-        return rc;
-    PFG_CUDA(c, cudaMemsetAsync(c->ws.p, 0, sizeof(double) * (2 * c->dim + 2) * N, c->stream));
-    double h[4] = {c->prm.max_dt, c->host_time, 0.0, 0.0};
-    PFG_CUDA(c, cudaMemcpyAsync(c->wc_dt.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    if (mixed(c)) {
+        if ((rc = ensure(c, c->ws, wcm_state_bytes(c))) || (rc = ensure(c, c->wc_el, wcm_elem_bytes(c))) ||
+            (rc = ensure(c, c->wc_eld, sizeof(float) * c->dim * N)) ||
+            (rc = ensure(c, c->wc_nodal, sizeof(float) * 2 * N)) || (rc = ensure(c, c->wc_dt, 64)))
+            return rc;
+        PFG_CUDA(c, cudaMemsetAsync(c->ws.p, 0, wcm_state_bytes(c), c->stream));
+        if ((rc = wcm_positions_in(c)) || (rc = wcm_vbc_refresh(c))) return rc;
+    } else {
+        const int nr = c->dim == 2 ? ElLayout<2>::NR : ElLayout<3>::NR;
+        const int ndd = c->dim == 2 ? ElLayout<2>::ND : ElLayout<3>::ND;
+        if ((rc = ensure(c, c->ws, sizeof(double) * (2 * c->dim + 2) * N)) ||
+            (rc = ensure(c, c->wc_el, sizeof(double) * (size_t)nr * E)) ||
+            (rc = ensure(c, c->wc_eld, sizeof(double) * ndd * E)) ||
+            (rc = ensure(c, c->wc_nodal, sizeof(double) * 2 * N)) || (rc = ensure(c, c->wc_dt, 64)))
+            return rc;
+        PFG_CUDA(c, cudaMemsetAsync(c->ws.p, 0, sizeof(double) * (2 * c->dim + 2) * N, c->stream));
+    }
+    PFG_CUDA(c, cudaMemsetAsync(c->wc_dt.p, 0, 64, c->stream));
+    k_set_time<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), c->host_time, c->prm.max_dt);
+    PFG_CHECK_LAUNCH(c);
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PFG_OK;
 }
 
+int wc_set_time(pfg_ctx* c, double time, double next_dt) {
+    k_set_time<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), time, next_dt);
+    PFG_CHECK_LAUNCH(c);
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->host_time = time;
+    return PFG_OK;
+}
+
+int wc_dirichlet_changed(pfg_ctx* c) {
+    if (!mixed(c)) return PFG_OK;
+    int rc = wcm_vbc_refresh(c);
+    if (rc) return rc;
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+// Make ctx->pos current (the mixed form keeps positions as double-float pairs).
+int wc_sync_positions(pfg_ctx* c) {
+    if (!mixed(c)) return PFG_OK;
+    return wcm_positions_out(c);
+}
+
 int wc_set_states(pfg_ctx* c, const double* h) {
+    if (mixed(c)) return wcm_set_states(c, h);
     const size_t n = (size_t)(2 * c->dim + 2) * c->N;
     PFG_CUDA(c, cudaMemcpyAsync(c->ws.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -605,6 +653,7 @@ int wc_set_states(pfg_ctx* c, const double* h) {
 }
 
 int wc_get_states(pfg_ctx* c, double* h) {
+    if (mixed(c)) return wcm_get_states(c, h);
     const size_t n = (size_t)(2 * c->dim + 2) * c->N;
     PFG_CUDA(c, cudaMemcpyAsync(h, c->ws.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -614,14 +663,13 @@ int wc_get_states(pfg_ctx* c, double* h) {
 int wc_enqueue(pfg_ctx* c, double dt, int nsteps) {
     const bool adapt = !(dt > 0);
     if (!adapt) {
-        k_set_value<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt) + T_DT, dt);
+        k_set_dt<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), dt);
         PFG_CHECK_LAUNCH(c);
     }
     if (c->prof) {
         // phase timers need events between kernels: launch directly
-        const WcConst k = make_const(c);
         for (int i = 0; i < nsteps; ++i) {
-            int rc = launch_any(c, adapt, k);
+            int rc = launch_any(c, adapt);
             if (rc) return rc;
         }
     } else {
@@ -655,12 +703,13 @@ int wc_steps(pfg_ctx* c, double dt, int nsteps, pfg_step_status* st) {
 }
 
 int wc_next_dt(pfg_ctx* c, double* dt) {
-    const WcConst k = make_const(c);
     int rc;
-    if (c->dim == 2)
-        rc = mixed(c) ? dt_only<2, float>(c, k) : dt_only<2, double>(c, k);
-    else
-        rc = mixed(c) ? dt_only<3, float>(c, k) : dt_only<3, double>(c, k);
+    if (mixed(c)) {
+        rc = wcm_next_dt(c);
+    } else {
+        const WcConst k = make_const(c);
+        rc = c->dim == 2 ? dt_only<2>(c, k) : dt_only<3>(c, k);
+    }
     if (rc) return rc;
     PFG_CUDA(c, cudaMemcpyAsync(dt, c->wc_dt.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -673,12 +722,22 @@ int wc_mass(pfg_ctx* c, double* out) {
     unsigned* ticket = reinterpret_cast<unsigned*>(red + c->max_grid * 4 + 48);
     const GaussConst g = gauss_const(c->dim);
     const int grid = std::max(1, std::min(c->max_grid, div_up(std::max(c->E, 1), BLOCK)));
+    const double* s = ptr<double>(c->ws);
+    int rc;
+    if (mixed(c)) {
+        // FP64 sum over an FP64 image of the state
+        const size_t n = (size_t)(2 * c->dim + 2) * c->N;
+        if ((rc = ensure(c, c->stage, sizeof(double) * n)) || (rc = wcm_state_to_stage(c)) ||
+            (rc = wcm_positions_out(c)))
+            return rc;
+        s = ptr<double>(c->stage);
+    }
     if (c->dim == 2)
-        k_wc_mass<2><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos),
-                                                    ptr<double>(c->ws), g.refSize, red, ticket, res);
+        k_wc_mass<2><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos), s, g.refSize,
+                                                    red, ticket, res);
     else
-        k_wc_mass<3><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos),
-                                                    ptr<double>(c->ws), g.refSize, red, ticket, res);
+        k_wc_mass<3><<<grid, BLOCK, 0, c->stream>>>(c->E, c->N, ptr<int>(c->conn), ptr<double>(c->pos), s, g.refSize,
+                                                    red, ticket, res);
     PFG_CHECK_LAUNCH(c);
     PFG_CUDA(c, cudaMemcpyAsync(c->h_scalars, res, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
