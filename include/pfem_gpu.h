@@ -170,6 +170,23 @@ PFG_API int pfg_get_stream(pfg_ctx* ctx, void** stream);
 
 /* CFL time step of the current WC state (SolverWCompNewton::computeNextDT). */
 PFG_API int pfg_next_dt(pfg_ctx* ctx, double* dt);
+/* CFL time step computed without allocating any device memory.  This entry point has no
+ * counterpart in the reference; it serves callers that may not call cudaMalloc when they need
+ * a time step (a host application whose pool allocator owns all device memory, a time loop
+ * running under another component's stream capture, a plugin that only receives device
+ * pointers).  Same result as pfg_next_dt on an FP64 weakly compressible context, computed from
+ * caller-owned device arrays: d_conn ((dim+1) x E int32), d_pos (dim x N), d_states
+ * ((2 dim + 2) x N, [v, p, rho, a]); the step goes to the device double *d_dt.  Uses
+ * params->dim, K0, K0p, mu, security_coeff, max_dt.  Work is enqueued on `stream`
+ * (cudaStream_t, NULL = default stream); the caller synchronises.  Scratch is one static device
+ * array for at most 1,048,576 nodes (16 MiB, held by every device that loads the library until
+ * exit); larger meshes return PFG_ERR_INVALID.  All calls share that array, so calls that
+ * overlap on the GPU race.  The first call on a device looks up the array's address and should
+ * come before any stream capture. */
+PFG_API int pfg_wc_next_dt_noalloc(const pfg_params* params, int32_t n_nodes, int32_t n_elems,
+                                   const int32_t* d_conn, const double* d_pos, const double* d_states,
+                                   double* d_dt, void* stream);
+
 /* Device-side time-step seed for pfg_wc_step(dt <= 0) (Solver::m_initialDT). */
 PFG_API int pfg_set_time(pfg_ctx* ctx, double time, double next_dt);
 

@@ -34,7 +34,7 @@ EXPORTED = (
     "pfg_wc_step", "pfg_next_dt", "pfg_set_time", "pfg_volume", "pfg_mass", "pfg_tip", "pfg_pspg_assemble",
     "pfg_get_csr", "pfg_get_geometry", "pfg_linear_solve", "pfg_version", "pfg_set_profiling",
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
-    "pfg_get_stream",
+    "pfg_get_stream", "pfg_wc_next_dt_noalloc",
 )
 NUM_PHASES = 12
 
@@ -104,6 +104,7 @@ def load(path=LIB_PATH):
         "pfg_wc_step_async": ([vp, C.c_double, C.c_int32], C.c_int),
         "pfg_synchronize": ([vp, C.POINTER(StepStatus)], C.c_int),
         "pfg_get_stream": ([vp, C.POINTER(vp)], C.c_int),
+        "pfg_wc_next_dt_noalloc": ([C.POINTER(Params), C.c_int32, C.c_int32, vp, vp, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
