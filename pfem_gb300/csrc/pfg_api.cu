@@ -284,7 +284,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->nbr_ptr, &c->nbr, &c->pair_node, &c->row_ptr, &c->col, &c->val, &c->val32,
                     &c->diag_pos, &c->rhs, &c->edata, &c->edata32, &c->q, &c->q_prev, &c->q_iter_prev,
                     &c->vbc, &c->kv, &c->kv32, &c->binv, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
-                    &c->stage, &c->wc_eld, &c->wc_nodal};
+                    &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot};
     wc_release_graphs(c);
     for (DBuf* b : bufs) release(*b);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);

@@ -66,6 +66,7 @@ struct pfg_ctx {
     pfg::DBuf pos, pos_save, flags, conn;
     // node -> element incidence (ascending element per node)
     pfg::DBuf ne_ptr, ne_elem, ne_loc;
+    pfg::DBuf inc_slot;    // (e, local i) -> position of that incidence in the node-major lists
     // node adjacency (sorted, includes the node) and the node-pair list
     pfg::DBuf nbr_ptr, nbr, pair_node;
     int P = 0;
@@ -88,6 +89,7 @@ struct pfg_ctx {
     pfg::DBuf wc_dt;       // [dt_next, time, dt_min_bits]
     pfg::DBuf stage;       // FP64 staging for host<->device precision conversion
     int wc_pending = 0;    // steps enqueued since the last synchronize
+    int wc_cur = 0;        // mixed form: current half of the ping-pong v/p state
     double host_time = 0.0;
     // host mirrors for validation
     std::vector<uint8_t> h_flags;

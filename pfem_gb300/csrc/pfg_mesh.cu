@@ -105,6 +105,16 @@ __global__ void k_sort_incidence(int N, const int* __restrict__ ne_ptr, int* __r
     flags[n] = f;
 }
 
+// Inverse of the sorted incidence lists: slot[e*npe + i] = position q of (e, i) in ne_elem,
+// so an element kernel can write its contribution for local node i straight into the node's
+// contiguous segment.
+__global__ void k_incidence_slots(long long inc, int npe, const int* __restrict__ ne_elem,
+                                  const uint8_t* __restrict__ ne_loc, int* __restrict__ slot) {
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= inc) return;
+    slot[(size_t)ne_elem[q] * npe + ne_loc[q]] = (int)q;
+}
+
 // Sorted, de-duplicated neighbour list of node n (n included) in `list`; returns its size or
 // -1 on overflow of MAX_NBR.
 __device__ int gather_neighbours(int n, int npe, int E, const int* __restrict__ conn, const int* __restrict__ ne_ptr,
@@ -283,6 +293,12 @@ int build_topology(pfg_ctx* c) {
     k_sort_incidence<<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
                                                                 ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags));
     PFG_CHECK_LAUNCH(c);
+    TRY(ensure(c, c->inc_slot, sizeof(int) * std::max<long long>(inc, 1)));
+    if (inc > 0) {
+        k_incidence_slots<<<div_up(inc, BLOCK), BLOCK, 0, c->stream>>>(inc, npe, ptr<int>(c->ne_elem),
+                                                                       ptr<uint8_t>(c->ne_loc), ptr<int>(c->inc_slot));
+        PFG_CHECK_LAUNCH(c);
+    }
 
     // adjacency
     TRY(ensure(c, deg, sizeof(int) * (size_t)N));

@@ -599,7 +599,9 @@ int wc_alloc(pfg_ctx* c) {
     int rc;
     wc_release_graphs(c);
     if (mixed(c)) {
-        if ((rc = ensure(c, c->ws, wcm_state_bytes(c))) || (rc = ensure(c, c->wc_el, wcm_elem_bytes(c))) ||
+        c->wc_cur = 0;
+        const size_t elb = std::max(wcm_elem_bytes(c), (size_t)(4096 + 64) * sizeof(float));
+        if ((rc = ensure(c, c->ws, wcm_state_bytes(c))) || (rc = ensure(c, c->wc_el, elb)) ||
             (rc = ensure(c, c->wc_eld, sizeof(float) * c->dim * N)) ||
             (rc = ensure(c, c->wc_nodal, sizeof(float) * 2 * N)) || (rc = ensure(c, c->wc_dt, 64)))
             return rc;
@@ -667,7 +669,7 @@ int wc_enqueue(pfg_ctx* c, double dt, int nsteps) {
         PFG_CHECK_LAUNCH(c);
     }
     if (c->prof) {
-        // phase timers need events between kernels: launch directly
+        // phase timers need events between kernels: launch each phase as its own kernel
         for (int i = 0; i < nsteps; ++i) {
             int rc = launch_any(c, adapt);
             if (rc) return rc;

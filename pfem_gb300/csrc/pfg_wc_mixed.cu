@@ -97,30 +97,37 @@ __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, f
     fast_two_sum(p, e, ph, pl);
 }
 
-// State layout (floats): XH[d][N] XL[d][N] VH[d][N] VL[d][N] PH[N] PL[N] RD[N] AX[d][N]
+// State layout (floats), shared with the fused form (pfg_wc_fused.cu):
+//   XH[d][N] XL[d][N] | VH0 VL0 VH1 VL1 [d][N] | PH0 PL0 PH1 PL1 [N] | RD[N] | AX[d][N]
+// v and p have two halves; `cur` selects the current one (the fused kernel ping-pongs).
 struct St {
     float *xh, *xl, *vh, *vl, *ph, *pl, *rd, *ax;
 };
-__host__ __device__ inline St state_ptrs(float* base, int dim, int N) {
+__host__ __device__ inline St state_ptrs(float* base, int dim, int N, int cur) {
     St s;
     s.xh = base;
     s.xl = base + (size_t)dim * N;
-    s.vh = base + (size_t)2 * dim * N;
-    s.vl = base + (size_t)3 * dim * N;
-    s.ph = base + (size_t)4 * dim * N;
+    s.vh = base + (size_t)(2 + 2 * cur) * dim * N;
+    s.vl = base + (size_t)(3 + 2 * cur) * dim * N;
+    float* pb = base + (size_t)6 * dim * N;
+    s.ph = pb + (size_t)2 * cur * N;
     s.pl = s.ph + N;
-    s.rd = s.pl + N;
+    s.rd = pb + (size_t)4 * N;
     s.ax = s.rd + N;
     return s;
 }
-inline size_t state_floats(int dim, int N) { return (size_t)(5 * dim + 3) * N; }
+inline size_t state_floats(int dim, int N) { return (size_t)(7 * dim + 5) * N; }
 
-// Element record (floats): ML[NPE] CONT[NPE] MLR[NPE] FS[d][NPE] WH[d][NPE] WL[d][NPE]
+// Element -> node exchange, incidence-major: the contribution of element e to its local node i
+// goes to slot q = inc_slot[e*(dim+1)+i], the position of (e, i) in node-major incidence order,
+// so each node sums one contiguous segment.  Fields are planes of Q = E (dim+1) floats:
+//   continuity: [ML | CONT]            momentum: [MLR | FS_f (dim) | WH_f (dim) | WL_f (dim)]
+// (the continuity planes are consumed before the momentum planes are written).
 template <int DIM>
-struct Rec {
-    static constexpr int NPE = DIM + 1;
-    static constexpr int ML = 0, CONT = NPE, MLR = 2 * NPE, FS = 3 * NPE, WH = FS + DIM * NPE, WL = WH + DIM * NPE;
-    static constexpr int SIZE = WL + DIM * NPE;
+struct Planes {
+    static constexpr int ML = 0, CONT = 1;
+    static constexpr int MLR = 0, FS = 1, WH = 1 + DIM, WL = 1 + 2 * DIM;
+    static constexpr int COUNT = 1 + 3 * DIM;
 };
 
 // Jacobian from double-float coordinates: Jh exact differences of hi parts, Jl of lo parts.
@@ -228,8 +235,9 @@ __global__ void k_m_predict(int N, const uint8_t* __restrict__ flags, St st, dou
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* __restrict__ conn, St st,
                                                        const double* __restrict__ tdt, WcmConst k,
-                                                       float* __restrict__ el) {
-    using L = Rec<DIM>;
+                                                       const int* __restrict__ slot, long long Q,
+                                                       float* __restrict__ cb) {
+    using L = Planes<DIM>;
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -255,9 +263,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* 
         for (int f = 0; f < DIM; ++f) adiv += (Gh[f][j] + Gl[f][j]) * st.vh[(size_t)f * N + nd[j]];
     }
     adiv *= k.refSize;  // |e| div v
-    float* out = el + (size_t)e * L::SIZE;
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
+        const long long q = __ldg(slot + (size_t)e * NPE + i);
         float mp = 0, mdp = 0;
 #pragma unroll
         for (int j = 0; j < NPE; ++j) {
@@ -267,24 +275,21 @@ __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* 
         const float swn = k.K0 * k.s[i] + k.K0p * mp;
         float cont = -dt * swn * adiv;
         if (k.meduri) cont += ae * mdp;
-        out[L::ML + i] = ae * k.s[i];
-        out[L::CONT + i] = cont;
+        cb[L::ML * Q + q] = ae * k.s[i];
+        cb[L::CONT * Q + q] = cont;
     }
 }
 
 template <int DIM>
-__global__ void k_m_cont_node(int N, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
-                              const uint8_t* __restrict__ ne_loc, const uint8_t* __restrict__ flags,
-                              const float* __restrict__ el, WcmConst k, St st) {
-    using L = Rec<DIM>;
+__global__ void k_m_cont_node(int N, const int* __restrict__ ne_ptr, const uint8_t* __restrict__ flags,
+                              const float* __restrict__ cb, long long Q, WcmConst k, St st) {
+    using L = Planes<DIM>;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     float m = 0, f0 = 0;
     for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        const float* rec = el + (size_t)ne_elem[q] * L::SIZE;
-        const int i = ne_loc[q];
-        m += rec[L::ML + i];
-        f0 += rec[L::CONT + i];
+        m += cb[L::ML * Q + q];
+        f0 += cb[L::CONT * Q + q];
     }
     if (flags[n] & F_FREE) {
         st.ph[n] = 0.0f;
@@ -302,8 +307,9 @@ __global__ void k_m_cont_node(int N, const int* __restrict__ ne_ptr, const int* 
 
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* __restrict__ conn, St st, WcmConst k,
-                                                      float* __restrict__ el) {
-    using L = Rec<DIM>;
+                                                      const int* __restrict__ slot, long long Q,
+                                                      float* __restrict__ cb) {
+    using L = Planes<DIM>;
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -345,9 +351,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
 #pragma unroll
     for (int a = 0; a < DIM; ++a) divA += Lg[a][a];
     const float kf = k.mu_sum / ae;
-    float* out = el + (size_t)e * L::SIZE;
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
+        const long long q = __ldg(slot + (size_t)e * NPE + i);
         float mr = 0, dp = 0;
 #pragma unroll
         for (int j = 0; j < NPE; ++j) {
@@ -355,7 +361,7 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
             dp += k.s[j] * ((ph[j] - ph[i]) + (pl[j] - pl[i]));
         }
         const float mlr = ae * mr;
-        out[L::MLR + i] = mlr;
+        cb[L::MLR * Q + q] = mlr;
         float gg[NPE];
 #pragma unroll
         for (int j = 0; j < NPE; ++j) {
@@ -372,20 +378,18 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
 #pragma unroll
             for (int f2 = 0; f2 < DIM; ++f2) kv += A[f2][i] * Lg[f2][f1];
             kv -= (2.0f / 3.0f) * A[f1][i] * divA;
-            out[L::FS + f1 * NPE + i] = -kf * kv + A[f1][i] * dp + mlr * k.g[f1];
-            out[L::WH + f1 * NPE + i] = Gh[f1][i];
-            out[L::WL + f1 * NPE + i] = Gl[f1][i];
+            cb[(L::FS + f1) * Q + q] = -kf * kv + A[f1][i] * dp + mlr * k.g[f1];
+            cb[(L::WH + f1) * Q + q] = Gh[f1][i];
+            cb[(L::WL + f1) * Q + q] = Gl[f1][i];
         }
     }
 }
 
 template <int DIM>
-__global__ void k_m_mom_node(int N, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
-                             const uint8_t* __restrict__ ne_loc, const uint8_t* __restrict__ flags,
-                             const float* __restrict__ el, const double* __restrict__ vbc,
+__global__ void k_m_mom_node(int N, const int* __restrict__ ne_ptr, const uint8_t* __restrict__ flags,
+                             const float* __restrict__ cb, long long Q, const double* __restrict__ vbc,
                              const double* __restrict__ tdt, WcmConst k, St st, float* __restrict__ nodal) {
-    using L = Rec<DIM>;
-    constexpr int NPE = DIM + 1;
+    using L = Planes<DIM>;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     const float dt = *dtf_ptr(const_cast<double*>(tdt));
@@ -393,13 +397,11 @@ __global__ void k_m_mom_node(int N, const int* __restrict__ ne_ptr, const int* _
 #pragma unroll
     for (int f = 0; f < DIM; ++f) F[f] = Wh[f] = Wl[f] = 0;
     for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        const float* rec = el + (size_t)ne_elem[q] * L::SIZE;
-        const int i = ne_loc[q];
-        m += rec[L::MLR + i];
+        m += cb[L::MLR * Q + q];
 #pragma unroll
         for (int f = 0; f < DIM; ++f) {
-            F[f] += rec[L::FS + f * NPE + i];
-            df_add(Wh[f], Wl[f], rec[L::WH + f * NPE + i], rec[L::WL + f * NPE + i]);
+            F[f] += cb[(L::FS + f) * Q + q];
+            df_add(Wh[f], Wl[f], cb[(L::WH + f) * Q + q], cb[(L::WL + f) * Q + q]);
         }
     }
     const float pS = st.ph[n] * k.S * k.refSize;
@@ -585,13 +587,15 @@ __global__ void k_m_vbc(int n, const double* __restrict__ vbc, float* __restrict
     if (i < n) out[i] = (float)vbc[i];
 }
 
-St st_of(pfg_ctx* c) { return state_ptrs(ptr<float>(c->ws), c->dim, c->N); }
+St st_of(pfg_ctx* c) { return state_ptrs(ptr<float>(c->ws), c->dim, c->N, c->wc_cur); }
 
 template <int DIM>
 int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
     const int N = c->N, E = c->E;
     St st = st_of(c);
-    float* el = ptr<float>(c->wc_el);
+    float* cb = ptr<float>(c->wc_el);
+    const int* slot = ptr<int>(c->inc_slot);
+    const long long Q = (long long)E * (DIM + 1);
     float* nodal = ptr<float>(c->wc_nodal);
     double* tdt = ptr<double>(c->wc_dt);
     const double* vbcf = reinterpret_cast<const double*>(ptr<float>(c->wc_eld));  // FP32 Dirichlet values
@@ -601,21 +605,19 @@ int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
     prof_end(c, PH_WC_PREDICT);
     if (E > 0) {
         prof_begin(c, PH_WC_CONT_ELEM);
-        k_m_cont_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, tdt, k, el);
+        k_m_cont_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, tdt, k, slot, Q, cb);
         prof_end(c, PH_WC_CONT_ELEM);
     }
     prof_begin(c, PH_WC_CONT_NODE);
-    k_m_cont_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
-                                                    ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags), el, k, st);
+    k_m_cont_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<uint8_t>(c->flags), cb, Q, k, st);
     prof_end(c, PH_WC_CONT_NODE);
     if (E > 0) {
         prof_begin(c, PH_WC_MOM_ELEM);
-        k_m_mom_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, k, el);
+        k_m_mom_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, k, slot, Q, cb);
         prof_end(c, PH_WC_MOM_ELEM);
     }
     prof_begin(c, PH_WC_MOM_NODE);
-    k_m_mom_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
-                                                   ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags), el, vbcf, tdt,
+    k_m_mom_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<uint8_t>(c->flags), cb, Q, vbcf, tdt,
                                                    k, st, adapt ? nodal : nullptr);
     prof_end(c, PH_WC_MOM_NODE);
     if (adapt && E > 0) {
@@ -634,7 +636,8 @@ int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
 size_t wcm_state_bytes(pfg_ctx* c) { return sizeof(float) * state_floats(c->dim, c->N); }
 
 size_t wcm_elem_bytes(pfg_ctx* c) {
-    return sizeof(float) * (size_t)(c->dim == 2 ? Rec<2>::SIZE : Rec<3>::SIZE) * std::max(c->E, 1);
+    const int planes = c->dim == 2 ? Planes<2>::COUNT : Planes<3>::COUNT;
+    return sizeof(float) * (size_t)planes * (c->dim + 1) * std::max(c->E, 1);
 }
 
 int wcm_launch_step(pfg_ctx* c, bool adapt) {
