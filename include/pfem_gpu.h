@@ -88,8 +88,8 @@ typedef struct pfg_params {
     int32_t picard_max_iter;   /* maxIter                                                  */
     int32_t residual;          /* pfg_residual                                             */
     double picard_min_res;     /* minRes                                                   */
-    int32_t krylov_max_iter;   /* per linear solve                                         */
-    int32_t pad0;
+    int32_t krylov_max_iter;   /* per linear solve (mixed: per correction solve)           */
+    int32_t refine_max_iter;   /* mixed: refinement sweeps per linear solve (0 = 30)       */
     double krylov_rel_tol;     /* stop when ||r|| <= max(rel_tol*||b||, abs_tol)           */
     double krylov_abs_tol;
     /* weakly compressible (ContEq + MomEq): */
@@ -100,6 +100,9 @@ typedef struct pfg_params {
     int32_t pad1;
     /* resources: */
     size_t hbm_budget_bytes;   /* 0 = no limit                                             */
+    /* mixed precision, incompressible: */
+    double inner_rel_tol;      /* FP32 correction solve stops at this fraction of its
+                                  starting residual (0 = 1e-4)                             */
 } pfg_params;
 
 typedef struct pfg_step_status {
@@ -150,8 +153,23 @@ PFG_API int pfg_set_dirichlet(pfg_ctx* ctx, int32_t n, const int32_t* nodes, con
 /* One incompressible PSPG time step: MomContEqIncompNewton::solve + PicardAlgo::solve
  * (MomContEquation.inl:287-309 [.inl offsets], PicardAlgo.cpp:31-95,
  * MomContEquationPSPG.inl:261-373).  On non-convergence the positions and states are
- * restored and status->converged = 0. */
+ * restored and status->converged = 0.
+ * precision = PFG_PREC_MIXED: FP32 assembly and FP32 correction solves, with every residual
+ * (refinement and Picard) evaluated in FP64 from the element formulas; the linear solves stop
+ * on the same FP64 residual test as the plain form. */
 PFG_API int pfg_picard_step(pfg_ctx* ctx, double dt, pfg_step_status* status);
+
+/* Batches (mixed precision, incompressible): the uploaded mesh is the union of n_inst
+ * independent meshes stored back to back, instance i owning nodes
+ * [node_offsets[i], node_offsets[i+1]) and only elements among them.  rho[i], mu[i] are the
+ * instance's fluid parameters.  No reference counterpart: the reference runs one Problem per
+ * process; this replaces n_inst independent SolverIncompNewton objects. */
+PFG_API int pfg_set_instances(pfg_ctx* ctx, int32_t n_inst, const int32_t* node_offsets, const double* rho,
+                              const double* mu);
+/* One Picard time step of every instance at once (instance i with time step dt[i]); each
+ * instance converges, fails and restores on its own, exactly as pfg_picard_step would
+ * alone.  status[i] receives instance i's result. */
+PFG_API int pfg_picard_step_batch(pfg_ctx* ctx, const double* dt, pfg_step_status* status);
 
 /* nsteps weakly compressible CDS_dpdt steps (WCompNewton/Solver.cpp:236-276 without the
  * remesh).  dt > 0 uses that fixed step for every step; dt <= 0 uses the device-side CFL step

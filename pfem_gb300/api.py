@@ -34,7 +34,7 @@ EXPORTED = (
     "pfg_wc_step", "pfg_next_dt", "pfg_set_time", "pfg_volume", "pfg_mass", "pfg_tip", "pfg_pspg_assemble",
     "pfg_get_csr", "pfg_get_geometry", "pfg_linear_solve", "pfg_version", "pfg_set_profiling",
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
-    "pfg_get_stream", "pfg_wc_next_dt_noalloc",
+    "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch",
 )
 NUM_PHASES = 12
 
@@ -44,11 +44,12 @@ class Params(C.Structure):
         ("dim", C.c_int32), ("kind", C.c_int32), ("precision", C.c_int32), ("linear_solver", C.c_int32),
         ("gravity", C.c_double * 3), ("mu", C.c_double),
         ("rho", C.c_double), ("picard_max_iter", C.c_int32), ("residual", C.c_int32),
-        ("picard_min_res", C.c_double), ("krylov_max_iter", C.c_int32), ("pad0", C.c_int32),
+        ("picard_min_res", C.c_double), ("krylov_max_iter", C.c_int32), ("refine_max_iter", C.c_int32),
         ("krylov_rel_tol", C.c_double), ("krylov_abs_tol", C.c_double),
         ("K0", C.c_double), ("K0p", C.c_double), ("rho_star", C.c_double), ("security_coeff", C.c_double),
         ("max_dt", C.c_double), ("meduri", C.c_int32), ("pad1", C.c_int32),
         ("hbm_budget_bytes", C.c_size_t),
+        ("inner_rel_tol", C.c_double),
     ]
 
 
@@ -105,6 +106,8 @@ def load(path=LIB_PATH):
         "pfg_synchronize": ([vp, C.POINTER(StepStatus)], C.c_int),
         "pfg_get_stream": ([vp, C.POINTER(vp)], C.c_int),
         "pfg_wc_next_dt_noalloc": ([C.POINTER(Params), C.c_int32, C.c_int32, vp, vp, vp, vp, vp], C.c_int),
+        "pfg_set_instances": ([vp, C.c_int32, ip, dp, dp], C.c_int),
+        "pfg_picard_step_batch": ([vp, dp, C.POINTER(StepStatus)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -116,6 +119,10 @@ def load(path=LIB_PATH):
 
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32)) if a is not None else None
 
 
 def default_params(kind, dim):
@@ -201,6 +208,23 @@ class Context:
         st = StepStatus()
         self._check(self.L.pfg_picard_step(self.h, float(dt), C.byref(st)), "pfg_picard_step")
         return st
+
+    def set_instances(self, node_offsets, rho, mu):
+        """Declare the uploaded mesh a union of independent instances (mixed precision)."""
+        off = np.ascontiguousarray(node_offsets, np.int32)
+        n = len(off) - 1
+        rho = np.ascontiguousarray(np.broadcast_to(np.asarray(rho, float), (n,)))
+        mu = np.ascontiguousarray(np.broadcast_to(np.asarray(mu, float), (n,)))
+        self._check(self.L.pfg_set_instances(self.h, n, _ip(off), _dp(rho), _dp(mu)), "pfg_set_instances")
+        self.n_inst = n
+
+    def picard_step_batch(self, dt):
+        """One Picard step of every instance; returns one StepStatus per instance."""
+        n = getattr(self, "n_inst", 1)
+        dts = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, float), (n,)))
+        st = (StepStatus * n)()
+        self._check(self.L.pfg_picard_step_batch(self.h, _dp(dts), st), "pfg_picard_step_batch")
+        return list(st)
 
     def wc_step(self, dt, nsteps=1):
         st = StepStatus()

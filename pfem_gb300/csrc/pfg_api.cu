@@ -233,6 +233,8 @@ PFG_API int pfg_default_params(int32_t kind, int32_t dim, pfg_params* p) {
     p->krylov_max_iter = 5000;
     p->krylov_rel_tol = 1e-14;
     p->krylov_abs_tol = 1e-10;
+    p->refine_max_iter = 30;
+    p->inner_rel_tol = 1e-4;
     p->K0 = 2.2e7;
     p->K0p = 7.0;
     p->rho_star = 1000.0;
@@ -284,7 +286,8 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->nbr_ptr, &c->nbr, &c->pair_node, &c->row_ptr, &c->col, &c->val, &c->val32,
                     &c->diag_pos, &c->rhs, &c->edata, &c->edata32, &c->q, &c->q_prev, &c->q_iter_prev,
                     &c->vbc, &c->kv, &c->kv32, &c->binv, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
-                    &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot};
+                    &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot, &c->binv32, &c->node_inst,
+                    &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt};
     wc_release_graphs(c);
     for (DBuf* b : bufs) release(*b);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -333,6 +336,7 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
     if ((rc = build_topology(c))) return rc;
     if (c->prm.kind == PFG_KIND_INCOMP_PSPG) {
         if ((rc = pspg_alloc(c)) || (rc = krylov_alloc(c))) return rc;
+        if (c->prm.precision == PFG_PREC_MIXED && (rc = mx_alloc(c))) return rc;
     } else {
         if ((rc = wc_alloc(c))) return rc;
     }
@@ -422,7 +426,55 @@ PFG_API int pfg_picard_step(pfg_ctx* c, double dt, pfg_step_status* st) {
     if (c->prm.kind != PFG_KIND_INCOMP_PSPG) return fail(c, PFG_ERR_STATE, "context is not incompressible");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
     if (!(dt > 0) || !st) return fail(c, PFG_ERR_INVALID, "pfg_picard_step: dt must be > 0 and status non-null");
+    if (c->prm.precision == PFG_PREC_MIXED) {
+        if (c->n_inst != 1) return fail(c, PFG_ERR_STATE, "context holds %d instances: use pfg_picard_step_batch", c->n_inst);
+        return mx_picard_step(c, &dt, st);
+    }
     return picard_step(c, dt, st);
+}
+
+PFG_API int pfg_set_instances(pfg_ctx* c, int32_t n_inst, const int32_t* node_offsets, const double* rho,
+                              const double* mu) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG || c->prm.precision != PFG_PREC_MIXED)
+        return fail(c, PFG_ERR_STATE, "instances need an incompressible context in mixed precision");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (n_inst <= 0 || !node_offsets || !rho || !mu) return fail(c, PFG_ERR_INVALID, "pfg_set_instances: bad arguments");
+    if (node_offsets[0] != 0 || node_offsets[n_inst] != c->N)
+        return fail(c, PFG_ERR_INVALID, "node offsets must start at 0 and end at the node count %d", c->N);
+    for (int i = 0; i < n_inst; ++i) {
+        if (node_offsets[i + 1] < node_offsets[i]) return fail(c, PFG_ERR_INVALID, "node offsets must not decrease");
+        if (!(rho[i] > 0) || !(mu[i] >= 0)) return fail(c, PFG_ERR_INVALID, "instance %d: rho must be > 0, mu >= 0", i);
+    }
+    // every element must stay inside one instance
+    std::vector<int> conn((size_t)c->npe * c->E);
+    if (c->E) {
+        PFG_CUDA(c, cudaMemcpyAsync(conn.data(), c->conn.p, sizeof(int) * conn.size(), cudaMemcpyDeviceToHost, c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    auto inst_of = [&](int n) {
+        return (int)(std::upper_bound(node_offsets, node_offsets + n_inst + 1, n) - node_offsets) - 1;
+    };
+    for (int e = 0; e < c->E; ++e) {
+        const int i0 = inst_of(conn[e]);
+        for (int k = 1; k < c->npe; ++k)
+            if (inst_of(conn[(size_t)k * c->E + e]) != i0)
+                return fail(c, PFG_ERR_INVALID, "element %d joins nodes of two instances", e);
+    }
+    return mx_set_instances(c, n_inst, node_offsets, rho, mu);
+}
+
+PFG_API int pfg_picard_step_batch(pfg_ctx* c, const double* dt, pfg_step_status* st) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG || c->prm.precision != PFG_PREC_MIXED)
+        return fail(c, PFG_ERR_STATE, "batched steps need an incompressible context in mixed precision");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!dt || !st) return fail(c, PFG_ERR_INVALID, "pfg_picard_step_batch: null arguments");
+    for (int i = 0; i < c->n_inst; ++i)
+        if (!(dt[i] > 0)) return fail(c, PFG_ERR_INVALID, "instance %d: dt must be > 0", i);
+    return mx_picard_step(c, dt, st);
 }
 
 PFG_API int pfg_wc_step(pfg_ctx* c, double dt, int32_t nsteps, pfg_step_status* st) {

@@ -107,6 +107,12 @@ struct pfg_ctx {
     // WC: FP64 element partials, per-node CFL quantities, captured step graphs [fixed, adaptive]
     pfg::DBuf wc_eld, wc_nodal;
     cudaGraphExec_t wc_graph[2] = {nullptr, nullptr};
+    // mixed-precision PSPG: FP32 block inverses, instance tables (segments of nodes,
+    // per-instance ints / doubles / FP32 Krylov scalars), reduction partials, counters
+    pfg::DBuf binv32, node_inst, mx_seg, mx_ii, mx_id, mx_sc, mx_part, mx_cnt;
+    int n_inst = 0, n_seg = 0;
+    std::vector<int> h_mx_ii;
+    std::vector<double> h_mx_id;
 };
 
 namespace pfg {
@@ -175,6 +181,11 @@ int krylov_alloc(pfg_ctx* c);
 // Solve A x = b (x in/out, device).  Returns iterations in *iters and ||b - A x|| in *res.
 int bicgstab(pfg_ctx* c, double* d_x, int* iters, double* res);
 int spmv_residual_norm(pfg_ctx* c, const double* d_x, double* res);
+
+// ---- mixed-precision PSPG (pfg_pspg_mixed.cu) -----------------------------------------
+int mx_alloc(pfg_ctx* c);
+int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* rho, const double* mu);
+int mx_picard_step(pfg_ctx* c, const double* dts, pfg_step_status* st);
 
 // ---- WC (pfg_wc.cu) -------------------------------------------------------------------
 int wc_alloc(pfg_ctx* c);

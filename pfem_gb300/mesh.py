@@ -292,3 +292,35 @@ def wc_initial_states(mesh, rho_star=1000.0, K0=2.2e7, K0p=7.0, g=9.81, column=(
     s[d * N:(d + 1) * N] = p
     s[(d + 1) * N:(d + 2) * N] = rho
     return s
+
+
+def concat_meshes(meshes):
+    """Union of independent meshes in one numbering, instance i owning nodes
+    [offsets[i], offsets[i+1]) and the elements among them (the layout pfg_set_instances
+    takes).  Returns (mesh, offsets)."""
+    dim = meshes[0].dim
+    offs = np.zeros(len(meshes) + 1, np.int64)
+    offs[1:] = np.cumsum([m.n_nodes for m in meshes])
+    pos = np.concatenate([m.pos for m in meshes], axis=1)
+    flags = np.concatenate([m.flags for m in meshes])
+    conn = np.concatenate([m.conn + o for m, o in zip(meshes, offs[:-1])], axis=1).astype(np.int32)
+    return HostMesh(dim, np.ascontiguousarray(pos), flags, np.ascontiguousarray(conn),
+                    hchar=meshes[0].hchar, alpha=meshes[0].alpha), offs.astype(np.int32)
+
+
+def concat_states(states, meshes):
+    """Field-major per-instance state vectors -> one field-major vector of the union."""
+    nf = len(states[0]) // meshes[0].n_nodes
+    return np.concatenate([np.concatenate([s[f * m.n_nodes:(f + 1) * m.n_nodes] for s, m in zip(states, meshes)])
+                           for f in range(nf)])
+
+
+def split_states(q, meshes):
+    """Inverse of concat_states."""
+    N = sum(m.n_nodes for m in meshes)
+    nf = len(q) // N
+    out, o = [], 0
+    for m in meshes:
+        out.append(np.concatenate([q[f * N + o:f * N + o + m.n_nodes] for f in range(nf)]))
+        o += m.n_nodes
+    return out

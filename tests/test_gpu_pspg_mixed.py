@@ -1,0 +1,129 @@
+"""Mixed-precision PSPG (FP32 assembly and FP32 correction solves, FP64 matrix-free
+refinement residual) and batched instances, against the FP64 oracle, through the C ABI.
+
+Tolerances: a Picard step within 1e-8 relative per field of the oracle, because the
+refinement stops on the same FP64 residual test as the plain form
+(||b - A x|| <= max(1e-14 ||b||, 1e-10)); Picard iteration counts equal to the oracle's;
+positions within 1e-12.  Batches: every instance bitwise equal to the same instance run
+alone (its reductions run over the same node segments in the same order).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pfem_gb300 import api
+from pfem_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+
+
+def make_ctx(mesh, **kw):
+    p = api.default_params(api.KIND_INCOMP_PSPG, mesh.dim)
+    p.precision = api.PREC_MIXED
+    for k, v in kw.items():
+        setattr(p, k, v)
+    ctx = api.Context(p)
+    ctx.upload_mesh(mesh)
+    return ctx
+
+
+def gravity(d):
+    return (0.0, -9.81) if d == 2 else (0.0, 0.0, -9.81)
+
+
+def field_errs(q, qo, d, N):
+    return [np.linalg.norm(q[f * N:(f + 1) * N] - qo[f * N:(f + 1) * N]) /
+            max(np.linalg.norm(qo[f * N:(f + 1) * N]), 1e-30) for f in range(d + 1)]
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_mixed_picard_matches_oracle(gpu_lib, which, c1_mesh, small3d_mesh):
+    mesh = c1_mesh if which == "c1" else small3d_mesh
+    d, N = mesh.dim, mesh.n_nodes
+    column = (1.0, 2.0) if d == 2 else (0.2, 0.3, 0.3)
+    q0 = M.incomp_initial_states(mesh, column=column)
+    ctx = make_ctx(mesh)
+    ctx.set_states(q0)
+    om = O.OracleMesh(mesh)
+    qo = q0.copy()
+    for step in range(3):
+        st = ctx.picard_step(1e-3)
+        qo, res = O.pspg_picard_step(om, qo, 1e-3, g=gravity(d))
+        assert st.converged == 1 and res.converged
+        assert st.picard_iterations == res.iterations
+        assert st.krylov_iterations > 0
+        errs = field_errs(ctx.get_states(), qo, d, N)
+        assert max(errs) < 1e-8, (step, errs)
+        assert np.abs(ctx.get_positions() - om.positions).max() < 1e-12
+    assert ctx.volume() == pytest.approx(om.volume(), rel=1e-13)
+
+
+def test_mixed_failure_restores_state(gpu_lib, c1_mesh):
+    q0 = M.incomp_initial_states(c1_mesh)
+    ctx = make_ctx(c1_mesh, picard_max_iter=0, picard_min_res=1e-30)
+    ctx.set_states(q0)
+    x0 = ctx.get_positions()
+    st = ctx.picard_step(1e-3)
+    assert st.converged == 0 and st.picard_iterations == 1
+    assert np.array_equal(ctx.get_positions(), x0)
+    assert np.array_equal(ctx.get_states(), q0)
+
+
+def _instances():
+    specs = [(0.1, (1.0, 2.0), 1e-3), (0.08, (0.8, 1.5), 1e-2), (0.12, (1.2, 1.8), 5e-2)]
+    meshes, states, mus = [], [], []
+    for i, (h, col, mu) in enumerate(specs):
+        m = M.dam_break_2d(h, column=col, seed=20261203 + i)
+        meshes.append(m)
+        states.append(M.incomp_initial_states(m, column=col))
+        mus.append(mu)
+    return meshes, states, mus
+
+
+def test_batch_equals_instances_alone(gpu_lib):
+    meshes, states, mus = _instances()
+    U, off = M.concat_meshes(meshes)
+    ctx = make_ctx(U)
+    ctx.set_instances(off, 1000.0, mus)
+    ctx.set_states(M.concat_states(states, meshes))
+    dts = [1e-3, 2e-3, 1e-3]
+    sts = [ctx.picard_step_batch(dts) for _ in range(2)]
+    qb = M.split_states(ctx.get_states(), meshes)
+    xb = ctx.get_positions()
+    for i, m in enumerate(meshes):
+        solo = make_ctx(m, mu=mus[i])
+        solo.set_states(states[i])
+        for k in range(2):
+            s = solo.picard_step(dts[i])
+            b = sts[k][i]
+            assert (s.converged, s.picard_iterations, s.krylov_iterations) == \
+                   (b.converged, b.picard_iterations, b.krylov_iterations)
+            assert s.residual == b.residual
+        assert np.array_equal(solo.get_states(), qb[i])
+        assert np.array_equal(solo.get_positions(), xb[:, off[i]:off[i + 1]])
+
+
+def test_batch_instance_matches_oracle(gpu_lib):
+    meshes, states, mus = _instances()
+    U, off = M.concat_meshes(meshes)
+    ctx = make_ctx(U)
+    ctx.set_instances(off, 1000.0, mus)
+    ctx.set_states(M.concat_states(states, meshes))
+    st = ctx.picard_step_batch(1e-3)
+    qb = M.split_states(ctx.get_states(), meshes)
+    for i, m in enumerate(meshes):
+        om = O.OracleMesh(m)
+        qo, res = O.pspg_picard_step(om, states[i], 1e-3, mu=mus[i])
+        assert st[i].converged == 1 and res.converged
+        assert st[i].picard_iterations == res.iterations
+        assert max(field_errs(qb[i], qo, 2, m.n_nodes)) < 1e-8
+
+
+def test_batch_rejects_cross_instance_elements(gpu_lib):
+    meshes, _, _ = _instances()
+    U, off = M.concat_meshes(meshes)
+    ctx = make_ctx(U)
+    bad = off.copy()
+    bad[1] = (off[1] + off[2]) // 2
+    with pytest.raises(api.PfgError, match="INVALID"):
+        ctx.set_instances(bad, 1000.0, 1e-3)
