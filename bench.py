@@ -50,6 +50,10 @@ def parse_args():
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["wc-c2", "incomp-c1", "incomp-c3", "batch-c4"], default="wc-c2",
+                    help="wc-c2 (default): the headline WC dam break; incomp-c1 / incomp-c3: PSPG Picard "
+                         "steps on the 2D / 3D dam break; batch-c4: 256 independent 2D instances")
+    ap.add_argument("--instances", type=int, default=256, help="batch-c4: number of instances")
     return ap.parse_args()
 
 
@@ -391,8 +395,404 @@ def run_gpu(args):
     return 0
 
 
+# ------------------------------------------------------------------------------------------------
+# Incompressible PSPG workloads: C1 (2D), C3 (3D) single meshes and C4 (batched 2D instances)
+# ------------------------------------------------------------------------------------------------
+
+INCOMP = {
+    "incomp-c1": dict(dt=1e-3, column=(1.0, 2.0), max_steps=200, max_warmup=5,
+                      metric="time-steps/s (2D incompressible dam break, PSPG Picard step)", unit="steps/s",
+                      name="2D incompressible dam break (C1), h = 0.05"),
+    "incomp-c3": dict(dt=5e-4, column=(0.5, 0.5, 1.0), max_steps=100, max_warmup=3,
+                      metric="time-steps/s (3D incompressible dam break, PSPG Picard step)", unit="steps/s",
+                      name="3D incompressible dam break (C3), h = 0.01"),
+    "batch-c4": dict(dt=1e-3, max_steps=20, max_warmup=3,
+                     metric="instance-steps/s (independent 2D incompressible dam breaks, batched Picard step)",
+                     unit="instance-steps/s", name="batched 2D incompressible dam breaks (C4)"),
+}
+
+
+def incomp_params(api, dim, precision, workload, mu=1e-3):
+    p = api.default_params(api.KIND_INCOMP_PSPG, dim)
+    p.precision = precision
+    p.mu = mu
+    if workload == "incomp-c3":  # C3: linear solves to relative residual 1e-8
+        p.krylov_rel_tol = 1e-8
+        p.krylov_abs_tol = 0.0
+    return p
+
+
+def pattern_nnz(mesh):
+    """Non-zeros of the PSPG pattern: identity rows for free nodes and bound-node velocities,
+    deg(n)(d+1) entries in every other row (deg counts the node itself)."""
+    import numpy as np
+    import scipy.sparse as sp
+
+    d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
+    Cm = sp.csr_matrix((np.ones(E * (d + 1)), (np.repeat(np.arange(E), d + 1), mesh.conn.T.ravel())), shape=(E, N))
+    deg = np.diff((Cm.T @ Cm).tocsr().indptr)
+    free = mesh.is_free()
+    bound = (mesh.flags & 1) != 0
+    per = np.where(free, d + 1, np.where(bound, d + deg * (d + 1), (d + 1) * deg * (d + 1)))
+    return int(per.sum())
+
+
+def spmv_bytes(nnz, R, s):
+    """One SpMV: values + column indices, row pointers, input and output vectors."""
+    return nnz * (s + 4) + (R + 1) * 4 + 2 * R * s
+
+
+def asm_bytes(d, N, E, R, nnz, s):
+    """One assembly: connectivity, FP64 positions, current and previous velocities, flags, the
+    CSR structure, the values and the right-hand side written once."""
+    return E * (d + 1) * 4 + N * (d * 8 + 2 * d * s + 1) + (R + 1) * 4 + nnz * 4 + nnz * s + R * s
+
+
+def field_errors(a, b, nf, N):
+    import numpy as np
+
+    return [float(np.linalg.norm(a[f * N:(f + 1) * N] - b[f * N:(f + 1) * N]) /
+                  max(np.linalg.norm(b[f * N:(f + 1) * N]), 1e-300)) for f in range(nf)]
+
+
+def _phase_roofline(phases, pb_spmv, pb_asm, peak):
+    spmv_ms, spmv_n = phases.get("Krylov SpMV", (0.0, 0))
+    asm_ms = phases.get("PSPG element prep", (0.0, 0))[0] + phases.get("PSPG matrix", (0.0, 0))[0]
+    asm_n = max(phases.get("PSPG matrix", (0.0, 0))[1], 1)
+    spmv_us = 1e3 * spmv_ms / max(spmv_n, 1)
+    asm_us = 1e3 * asm_ms / asm_n
+    out = {
+        "bound": "hbm", "kernel": "Krylov SpMV", "achieved": pb_spmv / (spmv_us / 1e6) / 1e9 if spmv_n else None,
+        "peak": peak, "unit": "GB/s", "algorithmic_bytes": pb_spmv, "avg_launch_us": spmv_us, "traffic": None,
+    }
+    out["frac"] = out["achieved"] / peak if out["achieved"] else None
+    out["assembly"] = {"achieved": pb_asm / (asm_us / 1e6) / 1e9 if asm_us else None, "avg_us": asm_us,
+                       "algorithmic_bytes": pb_asm}
+    if out["assembly"]["achieved"]:
+        out["assembly"]["frac"] = out["assembly"]["achieved"] / peak
+    return out
+
+
+def run_gpu_incomp(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    from pfem_gb300 import api, build
+    from pfem_gb300 import mesh as M
+    from pfem_gb300 import workloads as WL
+
+    build.build()
+    if args.workload == "batch-c4":
+        return run_gpu_batch(args)
+    cfg = INCOMP[args.workload]
+    mesh = WL.c1() if args.workload == "incomp-c1" else WL.c3()
+    d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
+    R = (d + 1) * N
+    nnz = pattern_nnz(mesh)
+    q0 = M.incomp_initial_states(mesh, column=cfg["column"])
+    dt = cfg["dt"]
+    K = max(1, min(args.steps, cfg["max_steps"]))
+    Wm = max(3, min(args.warmup, cfg["max_warmup"]))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+
+    def make(precision):
+        ctx = api.Context(incomp_params(api, d, precision, args.workload))
+        ctx.upload_mesh(mesh)
+        ctx.set_states(q0)
+        return ctx
+
+    def run(precision, clocks=None):
+        ctx = make(precision)
+        ext = torch.cuda.ExternalStream(ctx.stream)
+        for _ in range(Wm):
+            ctx.picard_step(dt)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        stats = {"converged": 0, "picard_iterations": 0, "krylov_iterations": 0}
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        with torch.cuda.stream(ext):
+            for k in range(K):
+                flush.fill_(k & 0xFF)
+                ev[k][0].record(ext)
+                st = ctx.picard_step(dt)
+                ev[k][1].record(ext)
+                stats["converged"] += st.converged
+                stats["picard_iterations"] += st.picard_iterations
+                stats["krylov_iterations"] += st.krylov_iterations
+        torch.cuda.synchronize()
+        clk = clocks.stop() if clocks else None
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        return ctx, ms, stats, clk
+
+    prec = api.PREC_MIXED if args.precision == "fp32" else api.PREC_FP64
+    clocks = ClockSampler(local)
+    ctx, total_ms, stats, clk = run(prec, clocks)
+    q_fast, x_fast = ctx.get_states(), ctx.get_positions()
+    other = api.PREC_FP64 if prec == api.PREC_MIXED else api.PREC_MIXED
+    ctx_o, ms_o, stats_o, _ = run(other)
+    q_o, x_o = ctx_o.get_states(), ctx_o.get_positions()
+    acc_vs_fp64 = None
+    if prec == api.PREC_MIXED:
+        acc_vs_fp64 = dict(zip(["v" + "xyz"[i] for i in range(d)] + ["p"], field_errors(q_fast, q_o, d + 1, N)))
+        acc_vs_fp64["x"] = float(np.abs(x_fast - x_o).max() / np.abs(x_o).max())
+        acc_vs_fp64["steps"] = Wm + K
+    ctx_o.close()
+
+    # per-phase times (library event timers, direct launches) on a few more steps
+    Kp = min(K, 3)
+    ctx.set_profiling(True)
+    ctx.reset_phase_times()
+    for _ in range(Kp):
+        ctx.picard_step(dt)
+    phases = ctx.phase_times()
+    ctx.set_profiling(False)
+    s = 4 if prec == api.PREC_MIXED else 8
+    peak, peak_kind = hbm_peak()
+    roof = _phase_roofline(phases, spmv_bytes(nnz, R, s), asm_bytes(d, N, E, R, nnz, s), peak)
+    roof["peak_kind"] = peak_kind
+
+    # end to end through the C ABI with host buffers
+    h_in = torch.empty(R, dtype=torch.float64, pin_memory=True).numpy()
+    h_out = torch.empty(R, dtype=torch.float64, pin_memory=True).numpy()
+    h_in[:] = ctx.get_states()
+    Ke = min(K, 20)
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        ctx.set_states(h_in)
+        ctx.picard_step(dt)
+        ctx.get_states(out=h_out)
+        h_in, h_out = h_out, h_in
+    e2e_s = time.perf_counter() - t0
+
+    cpu = None
+    acc_vs_oracle = None
+    if rank == 0 and not args.no_cpu_baseline and args.workload == "incomp-c1":
+        from oracle import oracle as O
+
+        O.build()
+        om = O.OracleMesh(mesh)
+        qo = q0.copy()
+        g = (0.0, -9.81)
+        t0 = time.perf_counter()
+        n_cpu = 0
+        for k in range(Wm + K):
+            qo, res = O.pspg_picard_step(om, qo, dt, g=g)
+            n_cpu += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": n_cpu / el, "unit": cfg["unit"], "cores": O.num_threads(), "kind": "port",
+               "sample": f"{n_cpu} C1 Picard steps of the FP64 C++/OpenMP oracle with SciPy SuperLU/COLAMD "
+                         f"({el:.1f} s)"}
+        acc_vs_oracle = dict(zip(["vx", "vy", "p"], field_errors(q_fast, qo, 3, N)))
+        acc_vs_oracle["x"] = float(np.abs(x_fast - om.positions).max() / np.abs(om.positions).max())
+
+    value = K / (total_ms / 1e3)
+    if rank == 0:
+        out = {
+            "metric": cfg["metric"], "value": value, "unit": cfg["unit"], "n_gpus": world, "steps": K, "warmup": Wm,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32" if prec == api.PREC_MIXED else "f64",
+            "data": "synthetic (seeded jittered lattice, no .msh shipped by the reference)",
+            "config": {"workload": cfg["name"], "nodes": N, "elements": E, "unknowns": R, "nnz": nnz, "dt": dt,
+                       "precision": "mixed (FP32 assembly + FP32 BiCGSTAB, FP64 refinement residual)"
+                       if prec == api.PREC_MIXED else "plain FP64",
+                       "linear_tolerance": "||r|| <= max(1e-14 ||b||, 1e-10)" if args.workload == "incomp-c1"
+                       else "||r|| <= 1e-8 ||b||",
+                       "l2": "flushed between timed steps (256 MB write)", "remesh": "excluded (host side)",
+                       "parallelism": "replicas only"},
+            "dof_per_s": value * R,
+            "step_stats": stats,
+            "other_precision": {"precision": "fp64" if prec == api.PREC_MIXED else "mixed",
+                                "value": K / (ms_o / 1e3), "step_stats": stats_o},
+            "e2e": {"value": Ke / e2e_s, "unit": cfg["unit"], "h2d_bytes_per_step": int(h_in.nbytes),
+                    "d2h_bytes_per_step": int(h_out.nbytes)},
+            "roofline": roof,
+            "phases_ms_per_step": {k: v[0] / Kp for k, v in phases.items()},
+            "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": int(round(sum(v[1] for k, v in phases.items() if k != "Krylov SpMV") / Kp * K)),
+            "err_vs_fp64_gpu": acc_vs_fp64, "err_vs_oracle": acc_vs_oracle,
+        }
+        print(json.dumps(out))
+    return 0
+
+
+def run_gpu_batch(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    from pfem_gb300 import api
+    from pfem_gb300 import mesh as M
+    from pfem_gb300 import workloads as WL
+
+    cfg = INCOMP["batch-c4"]
+    t0 = time.perf_counter()
+    insts = WL.c4(args.instances)
+    mesh_s = time.perf_counter() - t0
+    meshes = [i.mesh for i in insts]
+    U, off = M.concat_meshes(meshes)
+    mus = np.array([i.mu for i in insts])
+    q0 = M.concat_states([i.q0 for i in insts], meshes)
+    Ntot = U.n_nodes
+    R = 3 * Ntot
+    nnz = sum(pattern_nnz(m) for m in meshes)
+    dt = cfg["dt"]
+    K = max(1, min(args.steps, cfg["max_steps"]))
+    Wm = max(3, min(args.warmup, cfg["max_warmup"]))
+    n = len(insts)
+
+    ctx = api.Context(incomp_params(api, 2, api.PREC_MIXED, "batch-c4"))
+    ctx.upload_mesh(U)
+    ctx.set_instances(off, 1000.0, mus)
+    ctx.set_states(q0)
+    ext = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(Wm):
+        ctx.picard_step_batch(dt)
+    clocks = ClockSampler(local)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    conv = 0
+    pic = 0
+    kry = 0
+    torch.cuda.synchronize()
+    clocks.start()
+    with torch.cuda.stream(ext):
+        for k in range(K):
+            ev[k][0].record(ext)
+            sts = ctx.picard_step_batch(dt)
+            ev[k][1].record(ext)
+            conv += sum(s.converged for s in sts)
+            pic += sum(s.picard_iterations for s in sts)
+            kry = max(kry, max(s.krylov_iterations for s in sts))
+            fp64_inst = sum(s.fp64_solves for s in sts)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    qb = M.split_states(ctx.get_states(), meshes)
+
+    # plain FP64 drop-in, one context per instance, on a sample spread over the size range
+    order = np.argsort([m.n_nodes for m in meshes])
+    sample = sorted(set(order[np.linspace(0, n - 1, min(n, 16)).astype(int)].tolist()))
+    plain_ms, plain_dof_steps = 0.0, 0
+    errs = []
+    for i in sample:
+        m = meshes[i]
+        c = api.Context(incomp_params(api, 2, api.PREC_FP64, "batch-c4", mu=float(mus[i])))
+        c.upload_mesh(m)
+        c.set_states(insts[i].q0)
+        for _ in range(Wm):
+            c.picard_step(dt)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cext = torch.cuda.ExternalStream(c.stream)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(cext):
+            e0.record(cext)
+            for _ in range(K):
+                c.picard_step(dt)
+            e1.record(cext)
+        torch.cuda.synchronize()
+        plain_ms += e0.elapsed_time(e1)
+        plain_dof_steps += 3 * m.n_nodes * K
+        errs.append(max(field_errors(qb[i], c.get_states(), 3, m.n_nodes)))
+        c.close()
+    sample_dof = sum(3 * meshes[i].n_nodes for i in sample)
+    plain_dof_per_s = plain_dof_steps / (plain_ms / 1e3)
+
+    # phase times of one batched step
+    ctx.set_profiling(True)
+    ctx.reset_phase_times()
+    ctx.picard_step_batch(dt)
+    phases = ctx.phase_times()
+    ctx.set_profiling(False)
+    peak, peak_kind = hbm_peak()
+    roof = _phase_roofline(phases, spmv_bytes(nnz, R, 4), asm_bytes(2, Ntot, U.n_elems, R, nnz, 4), peak)
+    roof["peak_kind"] = peak_kind
+
+    value = n * K / (total_ms / 1e3)
+    dof_per_s = R * K / (total_ms / 1e3)
+    if rank == 0:
+        out = {
+            "metric": cfg["metric"], "value": value, "unit": cfg["unit"], "n_gpus": world, "steps": K, "warmup": Wm,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32", "data": "synthetic (seeded jittered lattices, per-instance seeds)",
+            "config": {"workload": cfg["name"], "instances": n, "nodes": Ntot, "elements": int(U.n_elems),
+                       "unknowns": R, "nnz": nnz, "dt": dt, "host_meshing_s": mesh_s,
+                       "precision": "mixed (FP32 assembly + FP32 BiCGSTAB, FP64 refinement residual)",
+                       "l2": "working set > L2 (129 MB)", "parallelism": "one batched launch sequence"},
+            "dof_per_s": dof_per_s,
+            "step_stats": {"converged_instance_steps": conv, "of": n * K, "picard_iterations": pic,
+                           "max_krylov_iterations_per_instance_step": kry,
+                           "instances_with_fp64_correction_solves": fp64_inst},
+            "plain_fp64_sample": {"instances": len(sample), "dof": sample_dof, "dof_per_s": plain_dof_per_s,
+                                  "speedup_dof_per_s": dof_per_s / plain_dof_per_s,
+                                  "max_rel_err_vs_plain": max(errs) if errs else None},
+            "roofline": roof, "phases_ms_per_step": {k: v[0] for k, v in phases.items()},
+            "cpu_baseline": None, "clocks": clk,
+            "e2e": None,
+            "gpu_launches": int(round(sum(v[1] for k, v in phases.items() if k != "Krylov SpMV") * K)),
+        }
+        print(json.dumps(out))
+    return 0
+
+
+def run_reference_incomp(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    cfg = INCOMP[args.workload]
+    from oracle import oracle as O
+    from pfem_gb300 import mesh as M
+    from pfem_gb300 import workloads as WL
+
+    O.build()
+    if args.workload == "batch-c4":
+        insts = WL.c4(args.instances)
+        t0 = time.perf_counter()
+        dof, inst_steps = 0, 0
+        for inst in insts:
+            om = O.OracleMesh(inst.mesh)
+            O.pspg_picard_step(om, inst.q0, cfg["dt"], mu=inst.mu)
+            dof += 3 * inst.mesh.n_nodes
+            inst_steps += 1
+            if time.perf_counter() - t0 > 120:
+                break
+        el = time.perf_counter() - t0
+        v = inst_steps / el
+        sample = f"one Picard step of each of the first {inst_steps} instances ({el:.1f} s), {dof / el:.3g} DOF/s"
+    else:
+        mesh = WL.c1() if args.workload == "incomp-c1" else WL.c3()
+        q = M.incomp_initial_states(mesh, column=cfg["column"])
+        om = O.OracleMesh(mesh)
+        g = (0.0, -9.81) if mesh.dim == 2 else (0.0, 0.0, -9.81)
+        t0 = time.perf_counter()
+        n_done = 0
+        while n_done < min(args.steps, cfg["max_steps"]):
+            q, _ = O.pspg_picard_step(om, q, cfg["dt"], g=g)
+            n_done += 1
+            if time.perf_counter() - t0 > 120:
+                break
+        el = time.perf_counter() - t0
+        v = n_done / el
+        sample = f"{n_done} Picard steps ({el:.1f} s)"
+    out = {"impl": "reference", "metric": cfg["metric"], "value": v, "unit": cfg["unit"], "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice)",
+           "config": {"workload": cfg["name"]},
+           "cpu_baseline": {"value": v, "unit": cfg["unit"], "cores": O.num_threads(), "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": cfg["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "gpu_launches": 0}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.workload != "wc-c2":
+        if args.impl == "reference":
+            return run_reference_incomp(args)
+        return run_gpu_incomp(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -102,7 +102,7 @@ typedef struct pfg_params {
     size_t hbm_budget_bytes;   /* 0 = no limit                                             */
     /* mixed precision, incompressible: */
     double inner_rel_tol;      /* FP32 correction solve stops at this fraction of its
-                                  starting residual (0 = 1e-4)                             */
+                                  starting residual (0 = 1e-3)                             */
 } pfg_params;
 
 typedef struct pfg_step_status {
@@ -113,6 +113,9 @@ typedef struct pfg_step_status {
     double residual;           /* last Picard residual                                     */
     double dt;                 /* time step used by the last step                          */
     double time;               /* device-side simulated time after the call                */
+    int32_t fp64_solves;       /* mixed incompressible: 1 when the correction solves ran in
+                                  FP64 (FP32 ones stopped contracting for this mesh)       */
+    int32_t pad0;
 } pfg_step_status;
 
 typedef struct pfg_ctx pfg_ctx;
@@ -238,8 +241,9 @@ PFG_API int pfg_linear_solve(pfg_ctx* ctx, double* x, int32_t* iterations, doubl
  *   0 WC predict            1 WC continuity/element   2 WC continuity/node
  *   3 WC momentum/element   4 WC momentum/node        5 WC time step
  *   6 PSPG element prep     7 PSPG right-hand side    8 PSPG matrix (node pairs)
- *   9 Krylov iteration     10 Picard residual        11 position update        */
-#define PFG_NUM_PHASES 12
+ *   9 Krylov iteration     10 Picard residual        11 position update
+ *  12 Krylov SpMV (the two products of an iteration, also inside phase 9)          */
+#define PFG_NUM_PHASES 13
 PFG_API int pfg_set_profiling(pfg_ctx* ctx, int32_t enable);
 /* Accumulated milliseconds and launch counts per phase since the last reset. */
 PFG_API int pfg_get_phase_times(pfg_ctx* ctx, double* ms, int64_t* launches);

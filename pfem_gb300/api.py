@@ -36,7 +36,7 @@ EXPORTED = (
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch",
 )
-NUM_PHASES = 12
+NUM_PHASES = 13
 
 
 class Params(C.Structure):
@@ -55,7 +55,8 @@ class Params(C.Structure):
 
 class StepStatus(C.Structure):
     _fields_ = [("converged", C.c_int32), ("picard_iterations", C.c_int32), ("krylov_iterations", C.c_int32),
-                ("steps_done", C.c_int32), ("residual", C.c_double), ("dt", C.c_double), ("time", C.c_double)]
+                ("steps_done", C.c_int32), ("residual", C.c_double), ("dt", C.c_double), ("time", C.c_double),
+                ("fp64_solves", C.c_int32), ("pad0", C.c_int32)]
 
 
 class PfgError(RuntimeError):

@@ -109,8 +109,9 @@ struct pfg_ctx {
     cudaGraphExec_t wc_graph[2] = {nullptr, nullptr};
     // mixed-precision PSPG: FP32 block inverses, instance tables (segments of nodes,
     // per-instance ints / doubles / FP32 Krylov scalars), reduction partials, counters
-    pfg::DBuf binv32, node_inst, mx_seg, mx_ii, mx_id, mx_sc, mx_part, mx_cnt;
+    pfg::DBuf binv32, node_inst, mx_seg, mx_ii, mx_id, mx_sc, mx_part, mx_cnt, mx_scale;
     int n_inst = 0, n_seg = 0;
+    cudaGraphExec_t mx_graph[2] = {nullptr, nullptr};  // one chunk of BiCGSTAB iterations [FP32, FP64]
     std::vector<int> h_mx_ii;
     std::vector<double> h_mx_id;
 };
@@ -149,7 +150,8 @@ enum Phase : int {
     PH_PSPG_PAIRS,
     PH_KRYLOV_ITER,
     PH_RESIDUAL,
-    PH_POSITIONS
+    PH_POSITIONS,
+    PH_KRYLOV_SPMV
 };
 void prof_begin(pfg_ctx* c, int phase);
 void prof_end(pfg_ctx* c, int phase);
@@ -186,6 +188,7 @@ int spmv_residual_norm(pfg_ctx* c, const double* d_x, double* res);
 int mx_alloc(pfg_ctx* c);
 int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* rho, const double* mu);
 int mx_picard_step(pfg_ctx* c, const double* dts, pfg_step_status* st);
+void mx_release_graph(pfg_ctx* c);
 
 // ---- WC (pfg_wc.cu) -------------------------------------------------------------------
 int wc_alloc(pfg_ctx* c);

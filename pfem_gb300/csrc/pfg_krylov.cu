@@ -423,9 +423,13 @@ int bicgstab_g(pfg_ctx* c, double* d_x, int* iters, double* res) {
         for (int k = 0; k < n; ++k) {
             prof_begin(c, PH_KRYLOV_ITER);
             k_update_p<DIM><<<grid_node, BLOCK, 0, c->stream>>>(N, V, ld, binv, kp.sc);
+            prof_begin(c, PH_KRYLOV_SPMV);
             k_spmv_alpha<G><<<grid_rows, BLOCK, 0, c->stream>>>(R, rp, col, val, V, ld, kp);
+            prof_end(c, PH_KRYLOV_SPMV);
             k_update_s<DIM><<<grid_node, BLOCK, 0, c->stream>>>(N, V, ld, binv, kp.sc);
+            prof_begin(c, PH_KRYLOV_SPMV);
             k_spmv_omega<G><<<grid_rows, BLOCK, 0, c->stream>>>(R, rp, col, val, V, ld, kp);
+            prof_end(c, PH_KRYLOV_SPMV);
             k_update_x<<<grid_vec, BLOCK, 0, c->stream>>>(R, d_x, V, ld, kp);
             prof_end(c, PH_KRYLOV_ITER);
         }

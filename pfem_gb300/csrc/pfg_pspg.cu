@@ -10,17 +10,7 @@
 // written exactly once, without atomics, and its element contributions are summed in the
 // same order as Eigen's setFromTriplets sums the reference's triplets (element order).
 //
-// Element matrices use closed forms of the reference's Gauss-point products
-// (MatricesBuilder.inl:216-386), with the sums over Gauss points taken from the same tables:
-//   M_ij  = rho |e| sum_g w_g N_i N_j                     (getM, factor rho)
-//   K     = mu |e| [d_f1f2 gradN_i.gradN_j + dN_i/dx_f2 dN_j/dx_f1]   (B^T Ddev B, Ddev=diag(2..,1..))
-//   D_ij,f = |e| s_i dN_j/dx_f,  s_i = sum_g w_g N_i      (getD, factor 1, m = [1..1,0..])
-//   C_ij,f = |e| dN_i/dx_f s_j                            (getC)
-//   L_ij  = |e| (sum_g w_g / rho) gradN_i.gradN_j         (getL, factor 1/rho)
-//   F_i,f = rho |e| g_f s_i,  H_i = |e| sum_g w_g gradN_i.g  (getF, getH)
-// and the element system of m_buildAbPSPG (MomContEquationPSPG.inl:30-53):
-//   [ M/dt (x) I + K      -D^T   ] [v]   [ F + M/dt v_prev         ]
-//   [ tau/dt C + D       tau L   ] [p] = [ tau H + tau/dt C v_prev ]
+// Element formulas: pfg_pspg_common.cuh.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,16 +19,11 @@
 
 #include "pfg_device.cuh"
 #include "pfg_internal.cuh"
+#include "pfg_pspg_common.cuh"
 
 namespace pfg {
 
 namespace {
-
-// Element data layout (structure of arrays, stride E): [detJ, tau, gradN[f][i] (f-major)]
-template <int DIM>
-constexpr int ed_count() {
-    return 2 + DIM * (DIM + 1);
-}
 
 // m_computeTauPSPG (MomContEquationPSPG.inl:237-259) and the geometry recompute of
 // Mesh::updateNodesPositionFromSave (Mesh.cpp:1258-1264), one thread per element.
@@ -78,13 +63,8 @@ __global__ void k_elem_prep(int E, int N, const int* __restrict__ conn, const do
 }
 
 struct PspgConst {
-    double rho, dt, refSize;
-    double mu_sum;    // sum_g mu w_g          (getK factor)
-    double l_sum;     // sum_g (1/rho) w_g     (getL factor)
-    double h_sum;     // sum_g w_g             (getH factor 1)
-    double MM[4][4];  // sum_g w N_i N_j
-    double s[4];      // sum_g w N_i
-    double g[3];
+    PspgCoef c;
+    PspgTables t;
 };
 
 // Matrix values, one thread per node pair (n, m).
@@ -113,69 +93,8 @@ __global__ void __launch_bounds__(BLOCK) k_pspg_pairs(int P, int N, int E, const
         return;
     }
     double acc[NPE][NPE];
-#pragma unroll
-    for (int a = 0; a < NPE; ++a)
-#pragma unroll
-        for (int b = 0; b < NPE; ++b) acc[a][b] = 0;
-    const double inv_dt = 1 / k.dt;
-    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        const int e = ne_elem[q];
-        int j = -1;
-#pragma unroll
-        for (int jj = 0; jj < NPE; ++jj)
-            if (__ldg(conn + (size_t)jj * E + e) == m) j = jj;
-        if (j < 0) continue;
-        const int i = ne_loc[q];
-        const double detJ = ed[e];
-        const double tau = ed[(size_t)E + e];
-        const double ae = detJ * k.refSize;
-        double gi[DIM], gj[DIM];
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) {
-            gi[f] = ed[(size_t)(2 + f * NPE + i) * E + e];
-            gj[f] = ed[(size_t)(2 + f * NPE + j) * E + e];
-        }
-        double dot = 0;
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) dot += gi[f] * gj[f];
-        const double mij = inv_dt * (k.rho * k.MM[i][j] * ae);
-        const double kf = ae * k.mu_sum;
-#pragma unroll
-        for (int f1 = 0; f1 < DIM; ++f1) {
-#pragma unroll
-            for (int f2 = 0; f2 < DIM; ++f2) {
-                const double kv = kf * ((f1 == f2 ? dot : 0.0) + gi[f2] * gj[f1]);
-                acc[f1][f2] += (f1 == f2 ? mij : 0.0) + kv;
-            }
-            acc[f1][DIM] += -(ae * k.s[j] * gi[f1]);
-        }
-        const double ctau = tau * inv_dt;
-#pragma unroll
-        for (int f2 = 0; f2 < DIM; ++f2) acc[DIM][f2] += ctau * (ae * gi[f2] * k.s[j]) + ae * k.s[i] * gj[f2];
-        acc[DIM][DIM] += tau * (ae * k.l_sum * dot);
-    }
-    const bool bound = fn & F_BOUND;
-    const bool mdir = apply_bc && (flags[m] & F_BOUND) && (flags[m] & F_DIRICHLET);
-#pragma unroll
-    for (int f1 = 0; f1 <= DIM; ++f1) {
-        const int r = n + f1 * N;
-        const int rp = row_ptr[r];
-        if (f1 < DIM && bound) {  // identity velocity rows of bound nodes (:119-126)
-            if (m == n) val[rp] = 1.0;
-            continue;
-        }
-#pragma unroll
-        for (int f2 = 0; f2 <= DIM; ++f2) {
-            double a = acc[f1][f2];
-            // Dirichlet column elimination (:216-229): value moved to the RHS, entry kept at 0
-            if (mdir && f2 < DIM && !(m == n && f1 == f2)) {
-                const double vb = vbc[(size_t)f2 * N + m];
-                if (vb != 0.0) atomicAdd(rhs + r, -a * vb);
-                a = 0.0;
-            }
-            val[rp + f2 * deg + rank] = a;
-        }
-    }
+    pspg_pair_block<DIM>(n, m, E, ne_ptr, ne_elem, ne_loc, conn, ed, k.c, k.t, acc);
+    pspg_write_block<DIM>(n, m, N, deg, rank, fn, flags[m], row_ptr, acc, apply_bc != 0, vbc, rhs, val, nullptr);
 }
 
 // Right-hand side and node boundary conditions, one thread per node (doublet scatter
@@ -186,63 +105,11 @@ __global__ void k_pspg_rhs(int N, int E, const int* __restrict__ ne_ptr, const i
                            const double* __restrict__ ed, const uint8_t* __restrict__ flags,
                            const double* __restrict__ q_prev, const double* __restrict__ vbc,
                            double* __restrict__ rhs, int apply_bc, PspgConst k) {
-    constexpr int NPE = DIM + 1;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
-    double bv[DIM];
-#pragma unroll
-    for (int f = 0; f < DIM; ++f) bv[f] = 0;
-    double bp = 0;
-    const double inv_dt = 1 / k.dt;
-    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        const int e = ne_elem[q];
-        const int i = ne_loc[q];
-        int nd[NPE];
-        load_nodes<DIM>(conn, E, e, nd);
-        const double detJ = ed[e];
-        const double tau = ed[(size_t)E + e];
-        const double ae = detJ * k.refSize;
-        double gi[DIM];
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) gi[f] = ed[(size_t)(2 + f * NPE + i) * E + e];
-        double vp[DIM][NPE];
-#pragma unroll
-        for (int f = 0; f < DIM; ++f)
-#pragma unroll
-            for (int j = 0; j < NPE; ++j) vp[f][j] = q_prev[(size_t)f * N + nd[j]];
-        // momentum rows: F + (M/dt) v_prev
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) {
-            double mv = 0;
-#pragma unroll
-            for (int j = 0; j < NPE; ++j) mv += inv_dt * (k.rho * k.MM[i][j] * ae) * vp[f][j];
-            const double F = ae * (k.rho * k.s[i] * k.g[f]);
-            bv[f] += F + mv;
-        }
-        // continuity row: tau H + (tau/dt) C v_prev
-        double gdot = 0;
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) gdot += gi[f] * k.g[f];
-        const double H = tau * (ae * k.h_sum * gdot);
-        double cv = 0;
-#pragma unroll
-        for (int f = 0; f < DIM; ++f)
-#pragma unroll
-            for (int j = 0; j < NPE; ++j) cv += (ae * gi[f] * k.s[j]) * vp[f][j];
-        bp += H + (tau * inv_dt) * cv;
-    }
-    const uint8_t fl = flags[n];
-    if (apply_bc) {
-        if (fl & F_FREE) {
-            bp = 0;
-            if (!(fl & F_BOUND))
-#pragma unroll
-                for (int f = 0; f < DIM; ++f) bv[f] = q_prev[(size_t)f * N + n] + k.dt * k.g[f];
-        }
-        if ((fl & F_BOUND) && (fl & F_DIRICHLET))
-#pragma unroll
-            for (int f = 0; f < DIM; ++f) bv[f] = vbc[(size_t)f * N + n];
-    }
+    double bv[DIM], bp;
+    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, apply_bc != 0, k.c, k.t, bv,
+                       bp);
 #pragma unroll
     for (int f = 0; f < DIM; ++f) rhs[(size_t)f * N + n] = bv[f];
     rhs[(size_t)DIM * N + n] = bp;
@@ -313,22 +180,22 @@ __global__ void k_tip(int N, const uint8_t* __restrict__ flags, const double* __
 PspgConst make_const(pfg_ctx* c, double dt) {
     const GaussConst g = gauss_const(c->dim);
     PspgConst k{};
-    k.rho = c->prm.rho;
-    k.dt = dt;
-    k.refSize = g.refSize;
-    k.mu_sum = 0;
-    k.l_sum = 0;
-    k.h_sum = 0;
+    k.c.rho = c->prm.rho;
+    k.c.dt = dt;
+    k.c.refSize = g.refSize;
+    k.c.mu_sum = 0;
+    k.c.l_sum = 0;
+    k.c.h_sum = 0;
     for (int q = 0; q < g.n; ++q) {
-        k.mu_sum += c->prm.mu * g.w[q];
-        k.l_sum += (1 / c->prm.rho) * g.w[q];
-        k.h_sum += 1.0 * g.w[q];
+        k.c.mu_sum += c->prm.mu * g.w[q];
+        k.c.l_sum += (1 / c->prm.rho) * g.w[q];
+        k.c.h_sum += 1.0 * g.w[q];
     }
     for (int i = 0; i < 4; ++i) {
-        k.s[i] = g.s[i];
-        for (int j = 0; j < 4; ++j) k.MM[i][j] = g.MM[i][j];
+        k.t.s[i] = g.s[i];
+        for (int j = 0; j < 4; ++j) k.t.MM[i][j] = g.MM[i][j];
     }
-    for (int f = 0; f < 3; ++f) k.g[f] = c->prm.gravity[f];
+    for (int f = 0; f < 3; ++f) k.t.g[f] = c->prm.gravity[f];
     return k;
 }
 

@@ -1,15 +1,17 @@
-// Mixed-precision incompressible PSPG step: FP32 assembly and FP32 Krylov iterations, FP64
-// geometry and an FP64 matrix-free residual that drives iterative refinement.
+// Mixed-precision incompressible PSPG step: FP32 Krylov iterations steered by FP64 iterative
+// refinement.
 //
 // The reference solves A(q) q = b(q) with a direct FP64 LU at every Picard iteration
-// (MomContEquationPSPG.inl:281-291).  Here the matrix is assembled in FP32 (the FP32 copy
-// only steers the correction solves), and every residual r = b - A x is evaluated in FP64
-// straight from the element formulas (no FP64 matrix is stored).  One linear solve is
-//     x <- x + BiCGSTAB_fp32(A32, r)   until ||r|| <= max(rel_tol ||b||, abs_tol),
+// (MomContEquationPSPG.inl:281-291).  Here A and b are assembled once per Picard iteration in
+// FP64 (same gather and element order as the FP64 path) together with an FP32 rounding of A,
+// and one linear solve is
+//     x <- x + BiCGSTAB_fp32(A32, r),  r = b - A x in FP64,  until ||r|| <= max(rel_tol ||b||, abs_tol),
 // the classic mixed-precision iterative refinement: its fixed point is the FP64 system's
-// solution, so the Picard iterates agree with the FP64 path to the refinement tolerance.
-// The residual evaluated right after the Picard re-assembly is, at the same time, the
-// Picard "Ax_f" residual (:366-371) and the first refinement residual of the next solve.
+// solution, so the Picard iterates agree with the FP64 path to the refinement tolerance.  (An
+// FP32-assembled matrix alone is not enough: rounding the C1 system to FP32 already moves its
+// solution by ~7e-7 relative, and FP32 element arithmetic by ~7e-6.)  The residual evaluated
+// right after a re-assembly is, at the same time, the Picard "Ax_f" residual (:366-371) and
+// the first refinement residual of the next solve.
 //
 // Everything runs over "instances": independent meshes stored back to back in one node /
 // element numbering (one instance for a single mesh).  Node-wise kernels run on segments of
@@ -26,40 +28,41 @@
 
 #include "pfg_device.cuh"
 #include "pfg_internal.cuh"
+#include "pfg_pspg_common.cuh"
 
 namespace pfg {
 
 namespace {
 
-constexpr int NB = 128;          // nodes per segment (= threads of the node kernels)
+constexpr int NB = 64;           // nodes per segment (= threads of the node kernels)
 constexpr int SPMV_BLOCK = 256;  // threads of the segment SpMV kernels
 
 // per-instance int fields
-enum : int { I_B0 = 0, I_B1, I_N0, I_N1, I_ACTIVE, I_STATUS, I_IT, I_KIT, I_TICKET, I_COUNT = 12 };
+// I_MODE: precision of the correction solves (0 FP32, 1 FP64); I_ROLL: undo the last sweep
+enum : int { I_B0 = 0, I_B1, I_N0, I_N1, I_ACTIVE, I_STATUS, I_IT, I_KIT, I_TICKET, I_MODE, I_ROLL, I_COUNT = 12 };
 // per-instance double fields
-enum : int { D_RHO = 0, D_MU, D_DT, D_RR, D_BB, D_RES, D_RES_FIRST, D_PAD, D_COUNT = 8 };
-// per-instance FP32 Krylov scalars
+enum : int { D_RHO = 0, D_MU, D_DT, D_RR, D_BB, D_RES, D_PAD0, D_PAD1, D_COUNT = 8 };
+// per-instance Krylov scalars (one FP32 and one FP64 set)
 enum : int { M_RHO = 0, M_RHO_OLD, M_ALPHA, M_OMEGA, M_RR, M_TOL2, M_DONE, M_ITERS, M_COUNT = 8 };
 // FP32 Krylov vectors
 enum : int { W_R = 0, W_RHAT, W_P, W_V, W_S, W_T, W_PHAT, W_SHAT, W_COUNT };
 // device counters
-enum : int { C_NEED = 0, C_ACTIVE = 1 };
+enum : int { C_NEED = 0, C_ACTIVE = 1, C_NEED64 = 2, C_ROLLBACK = 3 };
 
 struct Mx {
     const int* seg;   // [3 * n_seg]: instance, first node, end node
     int* ii;          // [I_COUNT * n_inst]
     double* id;       // [D_COUNT * n_inst]
     float* sc;        // [M_COUNT * n_inst]
-    double* part;     // [2 * n_seg]
+    double* sc64;     // [M_COUNT * n_inst]
+    double* part;     // [4 * n_seg]
     int* cnt;         // [4]
     const int* node_inst;
 };
 
 struct MxConst {
     double refSize, sumw;
-    double MM[4][4];
-    double s[4];
-    double g[3];
+    PspgTables t;
     double rtol, atol, eta, min_res;
     int max_iter;
 };
@@ -70,6 +73,7 @@ Mx mx_ptrs(pfg_ctx* c) {
     m.ii = ptr<int>(c->mx_ii);
     m.id = ptr<double>(c->mx_id);
     m.sc = ptr<float>(c->mx_sc);
+    m.sc64 = reinterpret_cast<double*>(ptr<char>(c->mx_sc) + 256 * (((size_t)c->n_inst * M_COUNT * sizeof(float) + 255) / 256));
     m.part = ptr<double>(c->mx_part);
     m.cnt = ptr<int>(c->mx_cnt);
     m.node_inst = ptr<int>(c->node_inst);
@@ -82,13 +86,13 @@ MxConst mx_const(pfg_ctx* c) {
     k.refSize = g.refSize;
     k.sumw = g.sumw;
     for (int i = 0; i < 4; ++i) {
-        k.s[i] = g.s[i];
-        for (int j = 0; j < 4; ++j) k.MM[i][j] = g.MM[i][j];
+        k.t.s[i] = g.s[i];
+        for (int j = 0; j < 4; ++j) k.t.MM[i][j] = g.MM[i][j];
     }
-    for (int f = 0; f < 3; ++f) k.g[f] = c->prm.gravity[f];
+    for (int f = 0; f < 3; ++f) k.t.g[f] = c->prm.gravity[f];
     k.rtol = c->prm.krylov_rel_tol;
     k.atol = c->prm.krylov_abs_tol;
-    k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-4;
+    k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-3;
     k.min_res = c->prm.picard_min_res;
     k.max_iter = c->prm.picard_max_iter;
     return k;
@@ -121,14 +125,24 @@ __device__ __forceinline__ bool inst_reduce(T (&v)[NV], int b, int b0, int b1, T
     return true;
 }
 
-// ---- element kernels ----------------------------------------------------------------------
+// ---- assembly (FP64 values, FP32 copy) -----------------------------------------------------
 
-// Geometry (FP64, Element.cpp:15-135) and tau (MomContEquationPSPG.inl:237-259) per element;
-// FP64 copy for the residual, FP32 copy [|e|, tau, gradN] for the FP32 assembly.
+__device__ __forceinline__ PspgCoef inst_coef_d(const double* id, double sumw, double refSize) {
+    PspgCoef k;
+    k.rho = id[D_RHO];
+    k.dt = id[D_DT];
+    k.refSize = refSize;
+    k.mu_sum = id[D_MU] * sumw;
+    k.l_sum = sumw / id[D_RHO];
+    k.h_sum = sumw;
+    return k;
+}
+
+// Geometry (Element.cpp:15-135) and tau (MomContEquationPSPG.inl:237-259) of the elements of
+// active instances: [detJ, tau, gradN] in FP64 (structure of arrays, stride E).
 template <int DIM>
 __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
-                          const double* __restrict__ q_iter, Mx m, double refSize, double* __restrict__ ed,
-                          float* __restrict__ ed32) {
+                          const double* __restrict__ q_iter, Mx m, double refSize, double* __restrict__ ed) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -158,26 +172,41 @@ __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const doub
     const double tau = 1 / sqrt(a * a + b * b + 9 * c * c);
     ed[e] = g.detJ;
     ed[(size_t)E + e] = tau;
-    ed32[e] = (float)(g.detJ * refSize);
-    ed32[(size_t)E + e] = (float)tau;
 #pragma unroll
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
-        for (int i = 0; i <= DIM; ++i) {
-            ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
-            ed32[(size_t)(2 + f * (DIM + 1) + i) * E + e] = (float)G[f][i];
-        }
+        for (int i = 0; i <= DIM; ++i) ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
 }
 
-// FP32 matrix values, one thread per node pair (same gather and pattern as the FP64 path).
-// Dirichlet columns are zeroed; their right-hand-side share lives in the FP64 residual.
+// Right-hand side of the nodes of active instances (element doublets + node BCs).
+template <int DIM>
+__global__ void k_mx_rhs(int N, int E, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
+                         const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
+                         const double* __restrict__ ed, const uint8_t* __restrict__ flags,
+                         const double* __restrict__ q_prev, const double* __restrict__ vbc, Mx m, MxConst k,
+                         double* __restrict__ rhs) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const int inst = m.node_inst[n];
+    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    const PspgCoef cf = inst_coef_d(m.id + inst * D_COUNT, k.sumw, k.refSize);
+    double bv[DIM], bp;
+    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, true, cf, k.t, bv, bp);
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) rhs[(size_t)f * N + n] = bv[f];
+    rhs[(size_t)DIM * N + n] = bp;
+}
+
+// FP64 matrix values of active instances, one thread per node pair: the same gather, element
+// order and Dirichlet elimination as the FP64 path.
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const int* __restrict__ pair_node,
                                                     const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
                                                     const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
                                                     const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
-                                                    const float* __restrict__ ed, const uint8_t* __restrict__ flags,
-                                                    const int* __restrict__ row_ptr, float* __restrict__ val, Mx m,
+                                                    const double* __restrict__ ed, const uint8_t* __restrict__ flags,
+                                                    const int* __restrict__ row_ptr, double* __restrict__ val,
+                                                    const double* __restrict__ vbc, double* __restrict__ rhs, Mx m,
                                                     MxConst k) {
     constexpr int NPE = DIM + 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -192,83 +221,73 @@ __global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const i
     const uint8_t fn = flags[n];
     if (fn & F_FREE) {
 #pragma unroll
-        for (int f = 0; f <= DIM; ++f) val[row_ptr[n + f * N]] = 1.0f;
+        for (int f = 0; f <= DIM; ++f) val[row_ptr[n + f * N]] = 1.0;
         return;
     }
-    const float rho = (float)m.id[inst * D_COUNT + D_RHO];
-    const float mu_sum = (float)(m.id[inst * D_COUNT + D_MU] * k.sumw);
-    const float l_sum = (float)(k.sumw / m.id[inst * D_COUNT + D_RHO]);
-    const float inv_dt = (float)(1.0 / m.id[inst * D_COUNT + D_DT]);
-    float acc[NPE][NPE];
+    const PspgCoef cf = inst_coef_d(m.id + inst * D_COUNT, k.sumw, k.refSize);
+    double acc[NPE][NPE];
+    pspg_pair_block<DIM>(n, mm, E, ne_ptr, ne_elem, ne_loc, conn, ed, cf, k.t, acc);
+    pspg_write_block<DIM>(n, mm, N, deg, rank, fn, flags[mm], row_ptr, acc, true, vbc, rhs, val, nullptr);
+}
+
+// ---- FP32 system: symmetric diagonal scaling ----------------------------------------------
+//
+// The correction solves run on S A S with S = diag(|a_rr|^-1/2).  Unscaled, a PSPG residual
+// has pressure rows some four orders of magnitude below its velocity rows, so FP32 dot
+// products drop the pressure part and the correction solves stall on fine meshes; scaled,
+// every row has a unit diagonal.  The FP64 residual and the solution stay unscaled.
+
+template <int DIM>
+__global__ void k_mx_rowscale(int N, const int* __restrict__ diag, const double* __restrict__ val, Mx m,
+                              double* __restrict__ scale) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
 #pragma unroll
-    for (int a = 0; a < NPE; ++a)
-#pragma unroll
-        for (int b = 0; b < NPE; ++b) acc[a][b] = 0;
-    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        const int e = ne_elem[q];
-        int j = -1;
-#pragma unroll
-        for (int jj = 0; jj < NPE; ++jj)
-            if (__ldg(conn + (size_t)jj * E + e) == mm) j = jj;
-        if (j < 0) continue;
-        const int i = ne_loc[q];
-        const float ae = ed[e];
-        const float tau = ed[(size_t)E + e];
-        float gi[DIM], gj[DIM];
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) {
-            gi[f] = ed[(size_t)(2 + f * NPE + i) * E + e];
-            gj[f] = ed[(size_t)(2 + f * NPE + j) * E + e];
-        }
-        float dot = 0;
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) dot += gi[f] * gj[f];
-        const float mij = inv_dt * (rho * (float)k.MM[i][j] * ae);
-        const float kf = ae * mu_sum;
-        const float si = (float)k.s[i], sj = (float)k.s[j];
-#pragma unroll
-        for (int f1 = 0; f1 < DIM; ++f1) {
-#pragma unroll
-            for (int f2 = 0; f2 < DIM; ++f2) {
-                const float kv = kf * ((f1 == f2 ? dot : 0.0f) + gi[f2] * gj[f1]);
-                acc[f1][f2] += (f1 == f2 ? mij : 0.0f) + kv;
-            }
-            acc[f1][DIM] += -(ae * sj * gi[f1]);
-        }
-        const float ctau = tau * inv_dt;
-#pragma unroll
-        for (int f2 = 0; f2 < DIM; ++f2) acc[DIM][f2] += ctau * (ae * gi[f2] * sj) + ae * si * gj[f2];
-        acc[DIM][DIM] += tau * (ae * l_sum * dot);
-    }
-    const bool bound = fn & F_BOUND;
-    const bool mdir = (flags[mm] & F_BOUND) && (flags[mm] & F_DIRICHLET);
-#pragma unroll
-    for (int f1 = 0; f1 <= DIM; ++f1) {
-        const int r = n + f1 * N;
-        const int rp = row_ptr[r];
-        if (f1 < DIM && bound) {
-            if (mm == n) val[rp] = 1.0f;
-            continue;
-        }
-#pragma unroll
-        for (int f2 = 0; f2 <= DIM; ++f2) {
-            float a = acc[f1][f2];
-            if (mdir && f2 < DIM && !(mm == n && f1 == f2)) a = 0.0f;
-            val[rp + f2 * deg + rank] = a;
-        }
+    for (int f = 0; f <= DIM; ++f) {
+        const int r = n + f * N;
+        const double d = fabs(val[diag[r]]);
+        scale[r] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
     }
 }
 
-// ---- node-block Jacobi preconditioner (FP32) ----------------------------------------------
+// val32 = FP32(s_r a_rc s_c) over the rows of a segment's nodes
+template <int G, int DIM>
+__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_scale_vals(Mx m, int N, const int* __restrict__ rp,
+                                                              const int* __restrict__ col,
+                                                              const double* __restrict__ val,
+                                                              const double* __restrict__ scale,
+                                                              float* __restrict__ val32) {
+    const int blk = blockIdx.x;
+    if (!m.ii[m.seg[3 * blk] * I_COUNT + I_ACTIVE]) return;
+    const int n0 = m.seg[3 * blk + 1], cnt = m.seg[3 * blk + 2] - n0;
+    const int rows = cnt * (DIM + 1);
+    const int lane = threadIdx.x % G;
+    for (int t0 = 0; t0 < rows; t0 += SPMV_BLOCK / G) {
+        const int t = t0 + threadIdx.x / G;
+        if (t >= rows) continue;
+        const int f = t / cnt;
+        const int r = f * N + n0 + (t - f * cnt);
+        const double sr = scale[r];
+        for (int kk = rp[r] + lane; kk < rp[r + 1]; kk += G) val32[kk] = (float)(sr * val[kk] * scale[col[kk]]);
+    }
+}
 
+// ---- node-block Jacobi preconditioner --------------------------------------------------------
+
+// Inverse of each node's (dim+1)x(dim+1) diagonal block, computed in FP64: stored as is for
+// the FP64 correction solves and, for the scaled system S A S, in FP32.  The pressure entry of a PSPG block is a small stabilisation term next to the
+// divergence couplings, so the block's Schur complement cancels heavily: inverted in FP32 the
+// preconditioner loses its pressure part on fine meshes and BiCGSTAB breaks down.
 template <int DIM>
-__global__ void k_mx_binv(int N, const int* __restrict__ rp, const float* __restrict__ val,
-                          const int* __restrict__ diag, float* __restrict__ binv, Mx m) {
+__global__ void k_mx_binv(int N, const int* __restrict__ rp, const double* __restrict__ val,
+                          const int* __restrict__ diag, const double* __restrict__ scale, float* __restrict__ binv,
+                          double* __restrict__ binv64, Mx m) {
     constexpr int B = DIM + 1;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
-    float a[B][2 * B];
+    double a[B][2 * B];
 #pragma unroll
     for (int f1 = 0; f1 < B; ++f1) {
         const int r = n + f1 * N;
@@ -277,7 +296,7 @@ __global__ void k_mx_binv(int N, const int* __restrict__ rp, const float* __rest
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2) {
             a[f1][f2] = 0;
-            a[f1][B + f2] = (f1 == f2) ? 1.0f : 0.0f;
+            a[f1][B + f2] = (f1 == f2) ? 1.0 : 0.0;
         }
         if (len == 1) {
             a[f1][f1] = val[dp];
@@ -288,36 +307,39 @@ __global__ void k_mx_binv(int N, const int* __restrict__ rp, const float* __rest
             for (int f2 = 0; f2 < B; ++f2) a[f1][f2] = val[b0 + f2 * deg + self];
         }
     }
-    float dg[B];
+    double sn[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) sn[f] = scale[n + f * N];
+    double dg[B];
 #pragma unroll
     for (int f = 0; f < B; ++f) dg[f] = a[f][f];
     bool ok = true;
 #pragma unroll
     for (int kk = 0; kk < B; ++kk) {
         int piv = kk;
-        float best = fabsf(a[kk][kk]);
+        double best = fabs(a[kk][kk]);
 #pragma unroll
         for (int i = kk + 1; i < B; ++i)
-            if (fabsf(a[i][kk]) > best) {
-                best = fabsf(a[i][kk]);
+            if (fabs(a[i][kk]) > best) {
+                best = fabs(a[i][kk]);
                 piv = i;
             }
-        if (best == 0.0f) ok = false;
+        if (best == 0.0) ok = false;
         if (piv != kk) {
 #pragma unroll
             for (int j = 0; j < 2 * B; ++j) {
-                const float t = a[kk][j];
+                const double t = a[kk][j];
                 a[kk][j] = a[piv][j];
                 a[piv][j] = t;
             }
         }
-        const float inv = ok ? 1.0f / a[kk][kk] : 0.0f;
+        const double inv = ok ? 1.0 / a[kk][kk] : 0.0;
 #pragma unroll
         for (int j = 0; j < 2 * B; ++j) a[kk][j] *= inv;
 #pragma unroll
         for (int i = 0; i < B; ++i) {
             if (i == kk) continue;
-            const float f = a[i][kk];
+            const double f = a[i][kk];
 #pragma unroll
             for (int j = 0; j < 2 * B; ++j) a[i][j] -= f * a[kk][j];
         }
@@ -326,195 +348,101 @@ __global__ void k_mx_binv(int N, const int* __restrict__ rp, const float* __rest
     for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2) {
-            float v = a[f1][B + f2];
-            if (!ok) v = (f1 == f2) ? (dg[f1] != 0.0f ? 1.0f / dg[f1] : 1.0f) : 0.0f;
-            binv[(size_t)(f1 * B + f2) * N + n] = v;
+            double v = a[f1][B + f2];
+            if (!ok) v = (f1 == f2) ? (dg[f1] != 0.0 ? 1.0 / dg[f1] : 1.0) : 0.0;
+            // (S B S)^-1 = S^-1 B^-1 S^-1
+            binv64[(size_t)(f1 * B + f2) * N + n] = v;
+            binv[(size_t)(f1 * B + f2) * N + n] = (float)(v / (sn[f1] * sn[f2]));
         }
 }
 
-template <int DIM>
-__device__ __forceinline__ void block_apply32(int n, int N, const float* __restrict__ binv, const float (&y)[DIM + 1],
-                                              float* __restrict__ z) {
-    constexpr int B = DIM + 1;
+// ---- FP64 residual -------------------------------------------------------------------------
+
+// Row r of the FP64 matrix times x over G lanes (valid on lane 0 of the group).
+template <int G>
+__device__ __forceinline__ double row_dot64(int r, bool act, const int* __restrict__ rp, const int* __restrict__ col,
+                                            const double* __restrict__ val, const double* __restrict__ x, int lane) {
+    const int b = act ? rp[r] : 0, e = act ? rp[r + 1] : 0;
+    double s = 0;
+    for (int kk = b + lane; kk < e; kk += G) s += val[kk] * x[col[kk]];
 #pragma unroll
-    for (int f1 = 0; f1 < B; ++f1) {
-        float s = 0;
-#pragma unroll
-        for (int f2 = 0; f2 < B; ++f2) s += binv[(size_t)(f1 * B + f2) * N + n] * y[f2];
-        z[(size_t)f1 * N + n] = s;
-    }
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+    return s;
 }
 
-// ---- FP64 matrix-free residual ----------------------------------------------------------------
+// r = b - A x over the rows of the segment's nodes with the FP64 matrix (the refinement
+// residual; right after a re-assembly it is also the Picard "Ax_f" residual, :366-371).
+// Seeds the instance's next correction solve (rhat = r, p = v = 0): FP32 on the scaled system
+// (r32 = S r) or, for an instance in FP64 mode, FP64 on A.  `kind`:
+//   RES_SWEEP   after a correction sweep: an FP32 sweep that did not shrink ||r|| tenfold moves
+//               the instance to FP64 mode (and, if ||r|| grew, asks the host to undo it);
+//   RES_PICARD  after a re-assembly: decides the instance's Picard iteration count,
+//               convergence and failure (PicardAlgo.cpp:48-90);
+//   RES_START   first residual of a step, or after an undo.
+enum : int { RES_SWEEP = 0, RES_PICARD = 1, RES_START = 2 };
 
-// r = b - A x for the nodes of one segment, A and b being the PSPG system of
-// m_buildAbPSPG + m_applyBCPSPG (MomContEquationPSPG.inl:6-235) at the element data `ed`
-// (geometry and tau of the current Picard iterate).  Dirichlet velocity entries of x are
-// replaced by their prescribed values, which reproduces the column elimination of
-// :216-229 exactly; identity rows (free nodes, bound-node velocities) give r = b - x.
-// Also seeds the FP32 correction solve: r32 = rhat = r, p = v = 0.  With `check`, the
-// residual is the Picard residual: the instance's iteration count, convergence and failure
-// are decided here (PicardAlgo.cpp:48-90).
-template <int DIM>
-__global__ void __launch_bounds__(NB) k_mx_resid(Mx m, int N, int E, const int* __restrict__ ne_ptr,
-                                                 const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
-                                                 const int* __restrict__ conn, const double* __restrict__ ed,
-                                                 const uint8_t* __restrict__ flags, const double* __restrict__ x,
-                                                 const double* __restrict__ qprev, const double* __restrict__ vbc,
-                                                 MxConst k, float* __restrict__ W, size_t ld, int check) {
-    constexpr int NPE = DIM + 1;
+template <int G, int DIM>
+__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_resid(Mx m, int N, const int* __restrict__ rp,
+                                                         const int* __restrict__ col, const double* __restrict__ val,
+                                                         const double* __restrict__ b, const double* __restrict__ x,
+                                                         const double* __restrict__ scale, MxConst k,
+                                                         float* __restrict__ W, double* __restrict__ W64, size_t ld,
+                                                         int kind) {
     __shared__ double sh[32];
-    const int b = blockIdx.x;
-    const int inst = m.seg[3 * b];
+    const int blk = blockIdx.x;
+    const int inst = m.seg[3 * blk];
     int* ii = m.ii + inst * I_COUNT;
     if (!ii[I_ACTIVE]) return;
-    const int n = m.seg[3 * b + 1] + threadIdx.x;
-    const bool valid = n < m.seg[3 * b + 2];
-    double* idd = m.id + inst * D_COUNT;
-    const double rho = idd[D_RHO], mu = idd[D_MU], dt = idd[D_DT];
-    const double inv_dt = 1 / dt;
-    double rr = 0, bb = 0;
-    if (valid) {
-        const uint8_t fl = flags[n];
-        const bool bound = fl & F_BOUND, isfree = fl & F_FREE;
-        const bool dir = bound && (fl & F_DIRICHLET);
-        double bv[DIM], av[DIM], bp = 0, ap = 0;
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) bv[f] = av[f] = 0;
-        const double kfs = mu * k.sumw, lfs = k.sumw / rho;
-        for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-            const int e = ne_elem[q];
-            const int i = ne_loc[q];
-            int nd[NPE];
-            load_nodes<DIM>(conn, E, e, nd);
-            const double ae = ed[e] * k.refSize;
-            const double tau = ed[(size_t)E + e];
-            double G[DIM][NPE], X[DIM][NPE], VP[DIM][NPE], Pj[NPE];
-#pragma unroll
-            for (int j = 0; j < NPE; ++j) {
-                const int nj = nd[j];
-                const uint8_t fj = flags[nj];
-                const bool dj = (fj & F_BOUND) && (fj & F_DIRICHLET);
-#pragma unroll
-                for (int f = 0; f < DIM; ++f) {
-                    G[f][j] = ed[(size_t)(2 + f * NPE + j) * E + e];
-                    X[f][j] = dj ? vbc[(size_t)f * N + nj] : x[(size_t)f * N + nj];
-                    VP[f][j] = qprev[(size_t)f * N + nj];
-                }
-                Pj[j] = x[(size_t)DIM * N + nj];
-            }
-            double dot[NPE];
-#pragma unroll
-            for (int j = 0; j < NPE; ++j) {
-                double t = 0;
-#pragma unroll
-                for (int f = 0; f < DIM; ++f) t += G[f][i] * G[f][j];
-                dot[j] = t;
-            }
-            double sP = 0, lP = 0;
-#pragma unroll
-            for (int j = 0; j < NPE; ++j) {
-                sP += k.s[j] * Pj[j];
-                lP += dot[j] * Pj[j];
-            }
-            // momentum rows (assembled only for nodes that are not bound, :68)
-#pragma unroll
-            for (int f = 0; f < DIM; ++f) {
-                double mvp = 0;
-#pragma unroll
-                for (int j = 0; j < NPE; ++j) mvp += (rho * k.MM[i][j] * ae * inv_dt) * VP[f][j];
-                bv[f] += ae * (rho * k.s[i] * k.g[f]) + mvp;
-            }
-            if (!bound) {
-                double Lg[DIM][DIM];  // Lg[a][c] = sum_j dN_j/dx_c X_a,j
-#pragma unroll
-                for (int a = 0; a < DIM; ++a)
-#pragma unroll
-                    for (int c2 = 0; c2 < DIM; ++c2) {
-                        double t = 0;
-#pragma unroll
-                        for (int j = 0; j < NPE; ++j) t += G[c2][j] * X[a][j];
-                        Lg[a][c2] = t;
-                    }
-                const double kf = ae * kfs;
-#pragma unroll
-                for (int f = 0; f < DIM; ++f) {
-                    double mx = 0, kx = 0;
-#pragma unroll
-                    for (int j = 0; j < NPE; ++j) {
-                        mx += (rho * k.MM[i][j] * ae * inv_dt) * X[f][j];
-                        kx += dot[j] * X[f][j];
-                    }
-#pragma unroll
-                    for (int f2 = 0; f2 < DIM; ++f2) kx += G[f2][i] * Lg[f2][f];
-                    av[f] += mx + kf * kx - ae * G[f][i] * sP;
-                }
-            }
-            // continuity row
-            double gdot = 0, cvp = 0, cx = 0, dv = 0;
-#pragma unroll
-            for (int f = 0; f < DIM; ++f) {
-                gdot += G[f][i] * k.g[f];
-                double sv = 0, sx = 0;
-#pragma unroll
-                for (int j = 0; j < NPE; ++j) {
-                    sv += k.s[j] * VP[f][j];
-                    sx += k.s[j] * X[f][j];
-                    dv += G[f][j] * X[f][j];
-                }
-                cvp += G[f][i] * sv;
-                cx += G[f][i] * sx;
-            }
-            const double ctau = tau * inv_dt;
-            bp += tau * (ae * k.sumw * gdot) + ctau * ae * cvp;
-            ap += ctau * ae * cx + ae * k.s[i] * dv + tau * ae * lfs * lP;
+    const bool fp64 = ii[I_MODE] != 0;
+    const int n0 = m.seg[3 * blk + 1], cnt = m.seg[3 * blk + 2] - n0;
+    const int rows = cnt * (DIM + 1);
+    const int lane = threadIdx.x % G;
+    double rr = 0, bb = 0, rs = 0;
+    for (int t0 = 0; t0 < rows; t0 += SPMV_BLOCK / G) {
+        const int t = t0 + threadIdx.x / G;
+        const bool act = t < rows;
+        int r = 0;
+        if (act) {
+            const int f = t / cnt;
+            r = f * N + n0 + (t - f * cnt);
         }
-        double r[DIM + 1], bn[DIM + 1];
-        if (isfree) {  // identity rows; b from :190-204 and :211-214
-#pragma unroll
-            for (int f = 0; f < DIM; ++f) {
-                bn[f] = bound ? bv[f] : qprev[(size_t)f * N + n] + dt * k.g[f];
-                if (dir) bn[f] = vbc[(size_t)f * N + n];
-                r[f] = bn[f] - x[(size_t)f * N + n];
+        const double ax = row_dot64<G>(r, act, rp, col, val, x, lane);
+        if (act && lane == 0) {
+            const double bv = b[r];
+            const double rv = bv - ax;
+            if (fp64) {
+                W64[W_R * ld + r] = rv;
+                W64[W_RHAT * ld + r] = rv;
+                W64[W_P * ld + r] = 0.0;
+                W64[W_V * ld + r] = 0.0;
+                rs += rv * rv;
+            } else {
+                const double sv = scale[r] * rv;
+                const float r32 = (float)sv;
+                W[W_R * ld + r] = r32;
+                W[W_RHAT * ld + r] = r32;
+                W[W_P * ld + r] = 0.0f;
+                W[W_V * ld + r] = 0.0f;
+                rs += sv * sv;
             }
-            bn[DIM] = 0;
-            r[DIM] = -x[(size_t)DIM * N + n];
-        } else {
-#pragma unroll
-            for (int f = 0; f < DIM; ++f) {
-                if (bound) {
-                    bn[f] = dir ? vbc[(size_t)f * N + n] : bv[f];
-                    r[f] = bn[f] - x[(size_t)f * N + n];
-                } else {
-                    bn[f] = bv[f];
-                    r[f] = bv[f] - av[f];
-                }
-            }
-            bn[DIM] = bp;
-            r[DIM] = bp - ap;
-        }
-#pragma unroll
-        for (int f = 0; f <= DIM; ++f) {
-            const size_t row = (size_t)f * N + n;
-            const float r32 = (float)r[f];
-            W[W_R * ld + row] = r32;
-            W[W_RHAT * ld + row] = r32;
-            W[W_P * ld + row] = 0.0f;
-            W[W_V * ld + row] = 0.0f;
-            rr += r[f] * r[f];
-            bb += bn[f] * bn[f];
+            rr += rv * rv;
+            bb += bv * bv;
         }
     }
-    double v[2] = {rr, bb};
-    if (!inst_reduce<NB, 2, double>(v, b, ii[I_B0], ii[I_B1], m.part, reinterpret_cast<unsigned*>(ii + I_TICKET), sh))
+    double v[3] = {rr, bb, rs};
+    if (!inst_reduce<SPMV_BLOCK, 3, double>(v, blk, ii[I_B0], ii[I_B1], m.part,
+                                            reinterpret_cast<unsigned*>(ii + I_TICKET), sh))
         return;
     if (threadIdx.x != 0) return;
+    double* idd = m.id + inst * D_COUNT;
     rr = v[0];
     bb = v[1];
+    rs = v[2];
+    const double rr_prev = idd[D_RR];
     idd[D_RR] = rr;
     idd[D_BB] = bb;
     bool active = true;
-    if (check) {
+    if (kind == RES_PICARD) {
         const double res = sqrt(rr);
         idd[D_RES] = res;
         const int it = ++ii[I_IT];
@@ -528,28 +456,70 @@ __global__ void __launch_bounds__(NB) k_mx_resid(Mx m, int N, int E, const int* 
         if (!active) ii[I_ACTIVE] = 0;
     }
     const double tol = fmax(k.rtol * sqrt(bb), k.atol);
-    const bool need = active && rr > tol * tol;
+    bool need = active && rr > tol * tol;
+    if (kind == RES_SWEEP && !fp64 && need && !(rr <= 0.01 * rr_prev)) {
+        ii[I_MODE] = 1;
+        if (!(rr <= rr_prev)) {  // grew or not finite: undo the sweep, residual recomputed after
+            ii[I_ROLL] = 1;
+            idd[D_RR] = rr_prev;
+            atomicAdd(m.cnt + C_ROLLBACK, 1);
+            need = false;
+        }
+    }
     float* sc = m.sc + inst * M_COUNT;
-    sc[M_RHO] = (float)rr;
+    double* sc64 = m.sc64 + inst * M_COUNT;
+    const bool need32 = need && ii[I_MODE] == 0 && !fp64;
+    const bool need64 = need && fp64;
+    sc[M_RHO] = (float)rs;
     sc[M_RHO_OLD] = 1.0f;
     sc[M_ALPHA] = 1.0f;
     sc[M_OMEGA] = 1.0f;
-    sc[M_RR] = (float)rr;
-    sc[M_TOL2] = (float)(k.eta * k.eta * rr);
+    sc[M_RR] = (float)rs;
+    sc[M_TOL2] = (float)(k.eta * k.eta * rs);
     sc[M_ITERS] = 0.0f;
-    sc[M_DONE] = need ? 0.0f : 1.0f;
-    if (need) atomicAdd(m.cnt + C_NEED, 1);
+    sc[M_DONE] = need32 ? 0.0f : 1.0f;
+    sc64[M_RHO] = rs;
+    sc64[M_RHO_OLD] = 1.0;
+    sc64[M_ALPHA] = 1.0;
+    sc64[M_OMEGA] = 1.0;
+    sc64[M_RR] = rs;
+    sc64[M_TOL2] = k.eta * k.eta * rs;
+    sc64[M_ITERS] = 0.0;
+    sc64[M_DONE] = need64 ? 0.0 : 1.0;
+    if (need32) atomicAdd(m.cnt + C_NEED, 1);
+    if (need64) atomicAdd(m.cnt + C_NEED64, 1);
+    // an instance just moved to FP64 mode without undo: its next sweep must start from an
+    // FP64 seed, which the host obtains by re-evaluating the residual
+    if (need && !fp64 && ii[I_MODE] == 1) atomicAdd(m.cnt + C_ROLLBACK, 1);
     if (active) atomicAdd(m.cnt + C_ACTIVE, 1);
 }
 
-// ---- FP32 BiCGSTAB on segments --------------------------------------------------------------
+// ---- BiCGSTAB correction solves on segments (FP32 on S A S, or FP64 on A) --------------------
+//
+// One kernel set, instantiated for T = float (the scaled FP32 system, the mixed form's default)
+// and T = double (the unscaled FP64 system, taken by an instance whose FP32 correction solves
+// stop contracting).  Each precision has its own vectors, block inverses and per-instance
+// scalars; an instance runs in exactly one of them, the other set's kernels skip it.
 
-// Row r of A32 times y over G lanes (valid on lane 0 of the group).
-template <int G>
-__device__ __forceinline__ float row_dot32(int r, bool act, const int* __restrict__ rp, const int* __restrict__ col,
-                                           const float* __restrict__ val, const float* __restrict__ y, int lane) {
+template <class T, int DIM>
+__device__ __forceinline__ void block_apply_t(int n, int N, const T* __restrict__ binv, const T (&y)[DIM + 1],
+                                              T* __restrict__ z) {
+    constexpr int B = DIM + 1;
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        T s = 0;
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) s += binv[(size_t)(f1 * B + f2) * N + n] * y[f2];
+        z[(size_t)f1 * N + n] = s;
+    }
+}
+
+// Row r of the matrix times y over G lanes (valid on lane 0 of the group).
+template <class T, int G>
+__device__ __forceinline__ T row_dot_t(int r, bool act, const int* __restrict__ rp, const int* __restrict__ col,
+                                       const T* __restrict__ val, const T* __restrict__ y, int lane) {
     const int b = act ? rp[r] : 0, e = act ? rp[r + 1] : 0;
-    float s = 0;
+    T s = 0;
     for (int kk = b + lane; kk < e; kk += G) s += val[kk] * __ldg(y + col[kk]);
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
@@ -557,63 +527,63 @@ __device__ __forceinline__ float row_dot32(int r, bool act, const int* __restric
 }
 
 // p = r + beta (p - omega v); phat = Binv p
-template <int DIM>
-__global__ void __launch_bounds__(NB) k_mx_up_p(Mx m, int N, float* __restrict__ W, size_t ld,
-                                                const float* __restrict__ binv) {
+template <class T, int DIM>
+__global__ void __launch_bounds__(NB) k_mx_up_p(Mx m, T* __restrict__ scb, int N, T* __restrict__ W, size_t ld,
+                                                const T* __restrict__ binv) {
     const int b = blockIdx.x;
-    const float* sc = m.sc + m.seg[3 * b] * M_COUNT;
-    if (sc[M_DONE] != 0.0f) return;
+    const T* sc = scb + m.seg[3 * b] * M_COUNT;
+    if (sc[M_DONE] != 0) return;
     const int n = m.seg[3 * b + 1] + threadIdx.x;
     if (n >= m.seg[3 * b + 2]) return;
-    const float beta = (sc[M_RHO] / sc[M_RHO_OLD]) * (sc[M_ALPHA] / sc[M_OMEGA]);
-    const float om = sc[M_OMEGA];
-    float p[DIM + 1];
+    const T beta = (sc[M_RHO] / sc[M_RHO_OLD]) * (sc[M_ALPHA] / sc[M_OMEGA]);
+    const T om = sc[M_OMEGA];
+    T p[DIM + 1];
 #pragma unroll
     for (int f = 0; f <= DIM; ++f) {
         const size_t r = (size_t)f * N + n;
         p[f] = W[W_R * ld + r] + beta * (W[W_P * ld + r] - om * W[W_V * ld + r]);
         W[W_P * ld + r] = p[f];
     }
-    block_apply32<DIM>(n, N, binv, p, W + W_PHAT * ld);
+    block_apply_t<T, DIM>(n, N, binv, p, W + W_PHAT * ld);
 }
 
 // s = r - alpha v; shat = Binv s
-template <int DIM>
-__global__ void __launch_bounds__(NB) k_mx_up_s(Mx m, int N, float* __restrict__ W, size_t ld,
-                                                const float* __restrict__ binv) {
+template <class T, int DIM>
+__global__ void __launch_bounds__(NB) k_mx_up_s(Mx m, T* __restrict__ scb, int N, T* __restrict__ W, size_t ld,
+                                                const T* __restrict__ binv) {
     const int b = blockIdx.x;
-    const float* sc = m.sc + m.seg[3 * b] * M_COUNT;
-    if (sc[M_DONE] != 0.0f) return;
+    const T* sc = scb + m.seg[3 * b] * M_COUNT;
+    if (sc[M_DONE] != 0) return;
     const int n = m.seg[3 * b + 1] + threadIdx.x;
     if (n >= m.seg[3 * b + 2]) return;
-    const float al = sc[M_ALPHA];
-    float s[DIM + 1];
+    const T al = sc[M_ALPHA];
+    T s[DIM + 1];
 #pragma unroll
     for (int f = 0; f <= DIM; ++f) {
         const size_t r = (size_t)f * N + n;
         s[f] = W[W_R * ld + r] - al * W[W_V * ld + r];
         W[W_S * ld + r] = s[f];
     }
-    block_apply32<DIM>(n, N, binv, s, W + W_SHAT * ld);
+    block_apply_t<T, DIM>(n, N, binv, s, W + W_SHAT * ld);
 }
 
-// out = A32 in over the rows of the segment's nodes (all fields); dots for alpha or omega.
-// mode 0: v = A phat, alpha = rho / (rhat . v).  mode 1: t = A shat, omega = (t.s)/(t.t).
-template <int G, int DIM, int MODE>
-__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, int N, const int* __restrict__ rp,
-                                                        const int* __restrict__ col, const float* __restrict__ val,
-                                                        float* __restrict__ W, size_t ld) {
+// out = A in over the rows of the segment's nodes (all fields); dots for alpha or omega.
+// MODE 0: v = A phat, alpha = rho / (rhat . v).  MODE 1: t = A shat, omega = (t.s)/(t.t).
+template <class T, int G, int DIM, int MODE>
+__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, T* __restrict__ scb, int cnt_slot, int N,
+                                                        const int* __restrict__ rp, const int* __restrict__ col,
+                                                        const T* __restrict__ val, T* __restrict__ W, size_t ld) {
     __shared__ double sh[32];
     const int b = blockIdx.x;
     const int inst = m.seg[3 * b];
-    float* sc = m.sc + inst * M_COUNT;
-    if (sc[M_DONE] != 0.0f) return;
+    T* sc = scb + inst * M_COUNT;
+    if (sc[M_DONE] != 0) return;
     const int n0 = m.seg[3 * b + 1], cnt = m.seg[3 * b + 2] - n0;
     const int rows = cnt * (DIM + 1);
     const int lane = threadIdx.x % G;
-    const float* in = W + (MODE == 0 ? W_PHAT : W_SHAT) * ld;
-    float* out = W + (MODE == 0 ? W_V : W_T) * ld;
-    float d0 = 0, d1 = 0;
+    const T* in = W + (MODE == 0 ? W_PHAT : W_SHAT) * ld;
+    T* out = W + (MODE == 0 ? W_V : W_T) * ld;
+    T d0 = 0, d1 = 0;
     for (int t0 = 0; t0 < rows; t0 += SPMV_BLOCK / G) {
         const int t = t0 + threadIdx.x / G;
         const bool act = t < rows;
@@ -622,7 +592,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, int N, const int* 
             const int f = t / cnt;
             r = f * N + n0 + (t - f * cnt);
         }
-        const float y = row_dot32<G>(r, act, rp, col, val, in, lane);
+        const T y = row_dot_t<T, G>(r, act, rp, col, val, in, lane);
         if (act && lane == 0) {
             out[r] = y;
             if (MODE == 0) {
@@ -634,68 +604,88 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, int N, const int* 
         }
     }
     const int* ii = m.ii + inst * I_COUNT;
-    float v[2] = {d0, d1};
-    if (!inst_reduce<SPMV_BLOCK, 2, float>(v, b, ii[I_B0], ii[I_B1], reinterpret_cast<float*>(m.part),
-                                           reinterpret_cast<unsigned*>(m.ii + inst * I_COUNT + I_TICKET), sh))
+    T v[2] = {d0, d1};
+    if (!inst_reduce<SPMV_BLOCK, 2, T>(v, b, ii[I_B0], ii[I_B1], reinterpret_cast<T*>(m.part),
+                                       reinterpret_cast<unsigned*>(m.ii + inst * I_COUNT + I_TICKET), sh))
         return;
     if (threadIdx.x != 0) return;
     if (MODE == 0) {
-        if (v[0] == 0.0f || !isfinite(v[0])) {
-            sc[M_DONE] = 2.0f;
-            atomicSub(m.cnt + C_NEED, 1);
+        const T al = sc[M_RHO] / v[0];
+        if (v[0] == 0 || !isfinite(v[0]) || !isfinite(al)) {  // breakdown: end this correction solve
+            sc[M_DONE] = 2;
+            atomicSub(m.cnt + cnt_slot, 1);
         } else {
-            sc[M_ALPHA] = sc[M_RHO] / v[0];
+            sc[M_ALPHA] = al;
         }
     } else {
-        sc[M_OMEGA] = (v[1] == 0.0f || !isfinite(v[1])) ? 0.0f : v[0] / v[1];
+        // omega = 0 ends the solve after the half step x += alpha phat (see k_mx_up_x)
+        const T om = (v[1] == 0 || !isfinite(v[1])) ? T(0) : v[0] / v[1];
+        sc[M_OMEGA] = isfinite(om) ? om : T(0);
     }
 }
 
-// x += alpha phat + omega shat (FP64 solution); r = s - omega t; rho = rhat.r; rr = r.r
-template <int DIM>
-__global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, int N, double* __restrict__ x, float* __restrict__ W,
-                                                size_t ld) {
+// x += S (alpha phat + omega shat) (FP64 solution; S = I for the unscaled FP64 system);
+// r = s - omega t; rho = rhat.r; rr = r.r
+template <class T, int DIM>
+__global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, T* __restrict__ scb, int cnt_slot, int N, double* __restrict__ x,
+                                                const double* __restrict__ scale, T* __restrict__ W, size_t ld) {
     __shared__ double sh[32];
     const int b = blockIdx.x;
     const int inst = m.seg[3 * b];
-    float* sc = m.sc + inst * M_COUNT;
-    if (sc[M_DONE] != 0.0f) return;
+    T* sc = scb + inst * M_COUNT;
+    if (sc[M_DONE] != 0) return;
     const int n = m.seg[3 * b + 1] + threadIdx.x;
-    const float al = sc[M_ALPHA], om = sc[M_OMEGA];
-    float rh = 0, rr = 0;
+    const T al = sc[M_ALPHA], om = sc[M_OMEGA];
+    T rh = 0, rr = 0;
     if (n < m.seg[3 * b + 2]) {
 #pragma unroll
         for (int f = 0; f <= DIM; ++f) {
             const size_t r = (size_t)f * N + n;
-            x[r] += (double)(al * W[W_PHAT * ld + r]) + (double)(om * W[W_SHAT * ld + r]);
-            const float rv = W[W_S * ld + r] - om * W[W_T * ld + r];
+            const double dx = (double)(al * W[W_PHAT * ld + r]) + (double)(om * W[W_SHAT * ld + r]);
+            x[r] += scale ? scale[r] * dx : dx;
+            const T rv = W[W_S * ld + r] - om * W[W_T * ld + r];
             W[W_R * ld + r] = rv;
             rh += W[W_RHAT * ld + r] * rv;
             rr += rv * rv;
         }
     }
     int* ii = m.ii + inst * I_COUNT;
-    float v[2] = {rh, rr};
-    if (!inst_reduce<NB, 2, float>(v, b, ii[I_B0], ii[I_B1], reinterpret_cast<float*>(m.part),
-                                   reinterpret_cast<unsigned*>(ii + I_TICKET), sh))
+    T v[2] = {rh, rr};
+    if (!inst_reduce<NB, 2, T>(v, b, ii[I_B0], ii[I_B1], reinterpret_cast<T*>(m.part),
+                               reinterpret_cast<unsigned*>(ii + I_TICKET), sh))
         return;
     if (threadIdx.x != 0) return;
     sc[M_RHO_OLD] = sc[M_RHO];
     sc[M_RHO] = v[0];
     sc[M_RR] = v[1];
-    sc[M_ITERS] += 1.0f;
+    sc[M_ITERS] += 1;
     ii[I_KIT] += 1;
-    float done = 0.0f;
+    T done = 0;
     if (!isfinite(v[1]))
-        done = 2.0f;
+        done = 2;
     else if (v[1] <= sc[M_TOL2])
-        done = 1.0f;
-    else if (v[0] == 0.0f || om == 0.0f)
-        done = 2.0f;
-    if (done != 0.0f) {
+        done = 1;
+    else if (v[0] == 0 || om == 0)
+        done = 2;
+    if (done != 0) {
         sc[M_DONE] = done;
-        atomicSub(m.cnt + C_NEED, 1);
+        atomicSub(m.cnt + cnt_slot, 1);
     }
+}
+
+// x = x_save for instances whose last FP32 correction sweep made the residual grow
+template <int DIM>
+__global__ void k_mx_rollback(int N, const double* __restrict__ xs, Mx m, double* __restrict__ x) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    if (!m.ii[m.node_inst[n] * I_COUNT + I_ROLL]) return;
+#pragma unroll
+    for (int f = 0; f <= DIM; ++f) x[(size_t)f * N + n] = xs[(size_t)f * N + n];
+}
+
+__global__ void k_mx_clear_roll(int n_inst, Mx m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_inst) m.ii[i * I_COUNT + I_ROLL] = 0;
 }
 
 // ---- node updates ---------------------------------------------------------------------------
@@ -734,12 +724,18 @@ __global__ void k_mx_restore(int N, const double* __restrict__ save, const doubl
 // instance's arithmetic does not depend on the other instances it is batched with.
 int lanes(pfg_ctx* c) { return c->dim == 2 ? 8 : 16; }
 
-int read_counters(pfg_ctx* c, int* need, int* active) {
+struct Counters {
+    int need32, active, need64, redo;
+};
+
+int read_counters(pfg_ctx* c, Counters* k) {
     PFG_CUDA(c, cudaMemcpyAsync(c->h_scalars, c->mx_cnt.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     const int* h = reinterpret_cast<const int*>(c->h_scalars);
-    *need = h[C_NEED];
-    *active = h[C_ACTIVE];
+    k->need32 = h[C_NEED];
+    k->active = h[C_ACTIVE];
+    k->need64 = h[C_NEED64];
+    k->redo = h[C_ROLLBACK];
     return PFG_OK;
 }
 
@@ -750,79 +746,143 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     if (E > 0) {
         prof_begin(c, PH_PSPG_ELEM);
         k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), q_iter,
-                                                                  m, k.refSize, ptr<double>(c->edata),
-                                                                  ptr<float>(c->edata32));
+                                                                  m, k.refSize, ptr<double>(c->edata));
         prof_end(c, PH_PSPG_ELEM);
         PFG_CHECK_LAUNCH(c);
     }
+    prof_begin(c, PH_PSPG_RHS);
+    k_mx_rhs<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
+        N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
+        ptr<double>(c->edata), ptr<uint8_t>(c->flags), ptr<double>(c->q_prev), ptr<double>(c->vbc), m, k,
+        ptr<double>(c->rhs));
+    prof_end(c, PH_PSPG_RHS);
+    PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);
     k_mx_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
         c->P, N, E, ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(c->ne_ptr),
-        ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<float>(c->edata32),
-        ptr<uint8_t>(c->flags), ptr<int>(c->row_ptr), ptr<float>(c->val32), m, k);
-    k_mx_binv<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->row_ptr), ptr<float>(c->val32),
-                                                              ptr<int>(c->diag_pos), ptr<float>(c->binv32), m);
+        ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<double>(c->edata),
+        ptr<uint8_t>(c->flags), ptr<int>(c->row_ptr), ptr<double>(c->val), ptr<double>(c->vbc), ptr<double>(c->rhs),
+        m, k);
+    constexpr int G = DIM == 2 ? 8 : 16;
+    double* scale = ptr<double>(c->mx_scale);
+    k_mx_rowscale<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->diag_pos), ptr<double>(c->val), m,
+                                                                  scale);
+    k_mx_scale_vals<G, DIM><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, N, ptr<int>(c->row_ptr), ptr<int>(c->col),
+                                                                    ptr<double>(c->val), scale, ptr<float>(c->val32));
+    k_mx_binv<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->row_ptr), ptr<double>(c->val),
+                                                              ptr<int>(c->diag_pos), scale, ptr<float>(c->binv32),
+                                                              ptr<double>(c->binv), m);
     prof_end(c, PH_PSPG_PAIRS);
     PFG_CHECK_LAUNCH(c);
     return PFG_OK;
 }
 
 template <int DIM>
-int mx_residual(pfg_ctx* c, const MxConst& k, int check, int* need, int* active) {
+int mx_residual(pfg_ctx* c, const MxConst& k, int kind, Counters* cnt) {
     Mx m = mx_ptrs(c);
+    constexpr int G = DIM == 2 ? 8 : 16;
     PFG_CUDA(c, cudaMemsetAsync(c->mx_cnt.p, 0, 4 * sizeof(int), c->stream));
     prof_begin(c, PH_RESIDUAL);
-    k_mx_resid<DIM><<<c->n_seg, NB, 0, c->stream>>>(
-        m, c->N, c->E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
-        ptr<double>(c->edata), ptr<uint8_t>(c->flags), ptr<double>(c->q), ptr<double>(c->q_prev),
-        ptr<double>(c->vbc), k, ptr<float>(c->kv32), (size_t)c->R, check);
+    k_mx_resid<G, DIM><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(
+        m, c->N, ptr<int>(c->row_ptr), ptr<int>(c->col), ptr<double>(c->val), ptr<double>(c->rhs), ptr<double>(c->q),
+        ptr<double>(c->mx_scale), k, ptr<float>(c->kv32), ptr<double>(c->kv), (size_t)c->R, kind);
     prof_end(c, PH_RESIDUAL);
     PFG_CHECK_LAUNCH(c);
-    return read_counters(c, need, active);
+    return read_counters(c, cnt);
 }
 
-// Correction solves of every instance that needs one, until all are done or the iteration
-// cap is reached.  x (the FP64 iterate) is updated in place.
-template <int G, int DIM>
-int mx_inner(pfg_ctx* c, int* need) {
+// Correction solves in precision T of every instance that needs one, until all are done or
+// the iteration cap is reached.  x (the FP64 iterate) is updated in place.
+template <class T, int DIM>
+int mx_inner(pfg_ctx* c, Counters* cnt) {
+    constexpr bool F32 = sizeof(T) == 4;
+    constexpr int G = DIM == 2 ? 8 : 16;
     Mx m = mx_ptrs(c);
     const int N = c->N;
     const size_t ld = (size_t)c->R;
-    float* W = ptr<float>(c->kv32);
-    const float* binv = ptr<float>(c->binv32);
+    T* W = F32 ? reinterpret_cast<T*>(c->kv32.p) : reinterpret_cast<T*>(c->kv.p);
+    const T* binv = F32 ? reinterpret_cast<const T*>(c->binv32.p) : reinterpret_cast<const T*>(c->binv.p);
+    const T* val = F32 ? reinterpret_cast<const T*>(c->val32.p) : reinterpret_cast<const T*>(c->val.p);
+    T* scb = F32 ? reinterpret_cast<T*>(m.sc) : reinterpret_cast<T*>(m.sc64);
+    const int slot = F32 ? C_NEED : C_NEED64;
+    const double* scale = F32 ? ptr<double>(c->mx_scale) : nullptr;
     const int* rp = ptr<int>(c->row_ptr);
     const int* col = ptr<int>(c->col);
-    const float* val = ptr<float>(c->val32);
     double* x = ptr<double>(c->q);
+    cudaGraphExec_t& graph = c->mx_graph[F32 ? 0 : 1];
     const int max_it = std::max(1, c->prm.krylov_max_iter);
     const int chunk = 8;
     int done_it = 0;
-    int active = 0;
+    auto iteration = [&]() {
+        prof_begin(c, PH_KRYLOV_ITER);
+        k_mx_up_p<T, DIM><<<c->n_seg, NB, 0, c->stream>>>(m, scb, N, W, ld, binv);
+        prof_begin(c, PH_KRYLOV_SPMV);
+        k_mx_spmv<T, G, DIM, 0><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, scb, slot, N, rp, col, val, W, ld);
+        prof_end(c, PH_KRYLOV_SPMV);
+        k_mx_up_s<T, DIM><<<c->n_seg, NB, 0, c->stream>>>(m, scb, N, W, ld, binv);
+        prof_begin(c, PH_KRYLOV_SPMV);
+        k_mx_spmv<T, G, DIM, 1><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, scb, slot, N, rp, col, val, W, ld);
+        prof_end(c, PH_KRYLOV_SPMV);
+        k_mx_up_x<T, DIM><<<c->n_seg, NB, 0, c->stream>>>(m, scb, slot, N, x, scale, W, ld);
+        prof_end(c, PH_KRYLOV_ITER);
+    };
+    int polls = 0;
+    int* need = F32 ? &cnt->need32 : &cnt->need64;
     while (*need > 0 && done_it < max_it) {
-        const int n = std::min(chunk, max_it - done_it);
-        for (int it = 0; it < n; ++it) {
-            prof_begin(c, PH_KRYLOV_ITER);
-            k_mx_up_p<DIM><<<c->n_seg, NB, 0, c->stream>>>(m, N, W, ld, binv);
-            k_mx_spmv<G, DIM, 0><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, N, rp, col, val, W, ld);
-            k_mx_up_s<DIM><<<c->n_seg, NB, 0, c->stream>>>(m, N, W, ld, binv);
-            k_mx_spmv<G, DIM, 1><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, N, rp, col, val, W, ld);
-            k_mx_up_x<DIM><<<c->n_seg, NB, 0, c->stream>>>(m, N, x, W, ld);
-            prof_end(c, PH_KRYLOV_ITER);
+        // chunks between two polls of the running-solve counter: 1, 1, 2, 2, 4, 4, ... graph
+        // launches (finished instances skip the extra iterations in every kernel)
+        const int reps = std::min(1 << (polls / 2), 4);
+        const int n = std::min(chunk * reps, max_it - done_it);
+        ++polls;
+        if (n == chunk * reps && !c->prof) {
+            // a chunk of iterations replayed from one CUDA graph (captured once per instance set)
+            if (!graph) {
+                cudaGraph_t g = nullptr;
+                PFG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                for (int it = 0; it < chunk; ++it) iteration();
+                cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+                if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+                e = cudaGraphInstantiate(&graph, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    graph = nullptr;
+                    return cuda_fail(c, e, "cudaGraphInstantiate");
+                }
+            }
+            for (int r = 0; r < reps; ++r) PFG_CUDA(c, cudaGraphLaunch(graph, c->stream));
+        } else {
+            for (int it = 0; it < n; ++it) iteration();
         }
         PFG_CHECK_LAUNCH(c);
         done_it += n;
-        int rc = read_counters(c, need, &active);
+        int rc = read_counters(c, cnt);
         if (rc) return rc;
     }
     return PFG_OK;
 }
 
+// One linear solve of every active instance by iterative refinement: correction sweeps in
+// each instance's precision, FP64 residual after each; an FP32 sweep that made things worse
+// is undone and the instance continues in FP64.
 template <int DIM>
-int mx_inner_dim(pfg_ctx* c, int* need) {
-    switch (lanes(c)) {
-        case 8: return mx_inner<8, DIM>(c, need);
-        default: return mx_inner<16, DIM>(c, need);
+int mx_refine(pfg_ctx* c, const MxConst& k, Counters* cnt) {
+    const int max_ref = c->prm.refine_max_iter > 0 ? c->prm.refine_max_iter : 30;
+    int rc;
+    for (int sweep = 0; sweep < max_ref && (cnt->need32 > 0 || cnt->need64 > 0); ++sweep) {
+        PFG_CUDA(c, cudaMemcpyAsync(c->q_iter_prev.p, c->q.p, sizeof(double) * c->R, cudaMemcpyDeviceToDevice,
+                                    c->stream));
+        if (cnt->need32 > 0 && (rc = mx_inner<float, DIM>(c, cnt))) return rc;
+        if (cnt->need64 > 0 && (rc = mx_inner<double, DIM>(c, cnt))) return rc;
+        if ((rc = mx_residual<DIM>(c, k, RES_SWEEP, cnt))) return rc;
+        if (cnt->redo > 0) {
+            k_mx_rollback<DIM><<<div_up(c->N, BLOCK), BLOCK, 0, c->stream>>>(c->N, ptr<double>(c->q_iter_prev),
+                                                                            mx_ptrs(c), ptr<double>(c->q));
+            k_mx_clear_roll<<<div_up(c->n_inst, BLOCK), BLOCK, 0, c->stream>>>(c->n_inst, mx_ptrs(c));
+            PFG_CHECK_LAUNCH(c);
+            if ((rc = mx_residual<DIM>(c, k, RES_START, cnt))) return rc;
+        }
     }
+    return PFG_OK;
 }
 
 template <int DIM>
@@ -830,7 +890,8 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
     const int K = c->n_inst;
     const size_t R = c->R;
     int rc;
-    // per-instance tables: counters reset, dt of this step, all instances active
+    // per-instance tables: counters reset, dt of this step, all instances active (the
+    // correction-solve precision of each instance carries over from its previous steps)
     std::vector<int>& hi = c->h_mx_ii;
     std::vector<double>& hd = c->h_mx_id;
     for (int i = 0; i < K; ++i) {
@@ -840,32 +901,29 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
         r[I_IT] = 0;
         r[I_KIT] = 0;
         r[I_TICKET] = 0;
+        r[I_ROLL] = 0;
         hd[(size_t)i * D_COUNT + D_DT] = dts[i];
     }
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_ii.p, hi.data(), sizeof(int) * hi.size(), cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_id.p, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, c->stream));
-    // prepare: save the node list, qPrev = states, build A32 at the current geometry
+    // prepare: save the node list, qPrev = states, build A and b at the current geometry
     PFG_CUDA(c, cudaMemcpyAsync(c->pos_save.p, c->pos.p, sizeof(double) * c->dim * c->N, cudaMemcpyDeviceToDevice,
                                 c->stream));
     PFG_CUDA(c, cudaMemcpyAsync(c->q_prev.p, c->q.p, sizeof(double) * R, cudaMemcpyDeviceToDevice, c->stream));
     const MxConst k = mx_const(c);
     if ((rc = mx_assemble<DIM>(c, ptr<double>(c->q_prev), k))) return rc;
-    int need = 0, active = 0;
-    if ((rc = mx_residual<DIM>(c, k, 0, &need, &active))) return rc;
-    const int max_ref = c->prm.refine_max_iter > 0 ? c->prm.refine_max_iter : 30;
+    Counters cnt{};
+    if ((rc = mx_residual<DIM>(c, k, RES_START, &cnt))) return rc;
     while (true) {
-        // linear solve of every active instance: refinement sweeps
-        for (int sweep = 0; sweep < max_ref && need > 0; ++sweep) {
-            if ((rc = mx_inner_dim<DIM>(c, &need))) return rc;
-            if ((rc = mx_residual<DIM>(c, k, 0, &need, &active))) return rc;
-        }
+        if ((rc = mx_refine<DIM>(c, k, &cnt))) return rc;
         // Picard update: positions, re-assembly, residual check
         k_mx_positions<DIM><<<div_up(c->N, BLOCK), BLOCK, 0, c->stream>>>(
             c->N, ptr<uint8_t>(c->flags), ptr<double>(c->pos_save), ptr<double>(c->q), mx_ptrs(c), ptr<double>(c->pos));
         PFG_CHECK_LAUNCH(c);
         if ((rc = mx_assemble<DIM>(c, ptr<double>(c->q), k))) return rc;
-        if ((rc = mx_residual<DIM>(c, k, 1, &need, &active))) return rc;
-        if (active == 0) break;
+        if ((rc = mx_residual<DIM>(c, k, RES_PICARD, &cnt))) return rc;
+        if (cnt.active == 0) break;
+        if (cnt.redo > 0 && (rc = mx_residual<DIM>(c, k, RES_START, &cnt))) return rc;
     }
     k_mx_restore<DIM><<<div_up(c->N, BLOCK), BLOCK, 0, c->stream>>>(
         c->N, ptr<double>(c->pos_save), ptr<double>(c->q_prev), mx_ptrs(c), ptr<double>(c->pos), ptr<double>(c->q));
@@ -882,6 +940,7 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
         s.krylov_iterations = r[I_KIT];
         s.residual = hd[(size_t)i * D_COUNT + D_RES];
         s.dt = dts[i];
+        s.fp64_solves = r[I_MODE];
     }
     return PFG_OK;
 }
@@ -889,12 +948,10 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
 }  // namespace
 
 int mx_alloc(pfg_ctx* c) {
-    const size_t R = std::max(c->R, 1), N = std::max(c->N, 1), E = std::max(c->E, 1);
-    const int ned = 2 + c->dim * (c->dim + 1);
+    const size_t R = std::max(c->R, 1), N = std::max(c->N, 1);
     int rc;
     if ((rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max<int64_t>(c->nnz, 1))) ||
-        (rc = ensure(c, c->edata32, sizeof(float) * ned * E)) ||
-        (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) ||
+        (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) || (rc = ensure(c, c->mx_scale, sizeof(double) * R)) ||
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))
         return rc;
@@ -904,8 +961,17 @@ int mx_alloc(pfg_ctx* c) {
     return mx_set_instances(c, 1, off, &rho, &mu);
 }
 
+void mx_release_graph(pfg_ctx* c) {
+    for (auto& g : c->mx_graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
 int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* rho, const double* mu) {
     const int N = c->N;
+    mx_release_graph(c);
     // segments of at most NB nodes inside each instance
     std::vector<int> seg;
     std::vector<int> node_inst(N);
@@ -940,8 +1006,9 @@ int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* 
     if ((rc = ensure(c, c->mx_seg, sizeof(int) * seg.size())) ||
         (rc = ensure(c, c->mx_ii, sizeof(int) * c->h_mx_ii.size())) ||
         (rc = ensure(c, c->mx_id, sizeof(double) * c->h_mx_id.size())) ||
-        (rc = ensure(c, c->mx_sc, sizeof(float) * (size_t)n_inst * M_COUNT)) ||
-        (rc = ensure(c, c->mx_part, sizeof(double) * 2 * (size_t)c->n_seg)))
+        (rc = ensure(c, c->mx_sc, 256 * (((size_t)n_inst * M_COUNT * sizeof(float) + 255) / 256) +
+                                      sizeof(double) * (size_t)n_inst * M_COUNT)) ||
+        (rc = ensure(c, c->mx_part, sizeof(double) * 4 * (size_t)c->n_seg)))
         return rc;
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_seg.p, seg.data(), sizeof(int) * seg.size(), cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaMemcpyAsync(c->node_inst.p, node_inst.data(), sizeof(int) * (size_t)N, cudaMemcpyHostToDevice,

@@ -178,7 +178,15 @@ def alpha_shape(pos, flags, hchar, alpha=1.2, delete_flying_nodes=False):
 
     dim = pos.shape[0]
     P = np.ascontiguousarray(pos.T)
-    tri = Delaunay(P)
+    if dim == 3:
+        # The unjittered wall lattice is full of co-spherical point sets, on which Qhull's
+        # merging is an order of magnitude slower.  Triangulating a copy moved by 1e-6 h
+        # (seeded) breaks the ties, as CGAL's symbolic perturbation does; all geometry below
+        # uses the true positions, so flat wall simplices still drop out.
+        jig = np.random.default_rng(7).uniform(-1.0, 1.0, P.shape) * (1e-6 * hchar)
+        tri = Delaunay(P + jig)
+    else:
+        tri = Delaunay(P)
     simp = tri.simplices.astype(np.int64)
     nbr = tri.neighbors.astype(np.int64)
     vol = _signed_measure(P, simp)

@@ -127,3 +127,28 @@ def test_batch_rejects_cross_instance_elements(gpu_lib):
     bad[1] = (off[1] + off[2]) // 2
     with pytest.raises(api.PfgError, match="INVALID"):
         ctx.set_instances(bad, 1000.0, 1e-3)
+
+
+def test_fp64_fallback_on_hard_instance(gpu_lib):
+    """A 25k-node instance whose FP32 correction solves stop contracting: the step still
+    converges (the solves continue in FP64) and matches the FP64 path."""
+    from pfem_gb300 import workloads as W
+
+    inst = W.c4_instance(0)
+    m = inst.mesh
+    res = {}
+    for prec in (api.PREC_MIXED, api.PREC_FP64):
+        p = api.default_params(api.KIND_INCOMP_PSPG, 2)
+        p.precision = prec
+        p.mu = inst.mu
+        ctx = api.Context(p)
+        ctx.upload_mesh(m)
+        ctx.set_states(inst.q0)
+        st = ctx.picard_step(1e-3)
+        assert st.converged == 1
+        res[prec] = (st, ctx.get_states())
+        ctx.close()
+    st_m, q_m = res[api.PREC_MIXED]
+    assert st_m.fp64_solves == 1
+    assert st_m.picard_iterations == res[api.PREC_FP64][0].picard_iterations
+    assert max(field_errs(q_m, res[api.PREC_FP64][1], 2, m.n_nodes)) < 1e-6
