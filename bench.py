@@ -50,10 +50,14 @@ def parse_args():
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["wc-c2", "incomp-c1", "incomp-c3", "batch-c4"], default="wc-c2",
+    ap.add_argument("--workload", choices=["wc-c2", "incomp-c1", "incomp-c3", "batch-c4", "serve-c5"],
+                    default="wc-c2",
                     help="wc-c2 (default): the headline WC dam break; incomp-c1 / incomp-c3: PSPG Picard "
-                         "steps on the 2D / 3D dam break; batch-c4: 256 independent 2D instances")
+                         "steps on the 2D / 3D dam break; batch-c4: 256 independent 2D instances; "
+                         "serve-c5: a Poisson stream of requests served under an HBM budget")
     ap.add_argument("--instances", type=int, default=256, help="batch-c4: number of instances")
+    ap.add_argument("--requests", type=int, default=24, help="serve-c5: number of requests")
+    ap.add_argument("--rate", type=float, default=1.5, help="serve-c5: mean arrivals per second")
     return ap.parse_args()
 
 
@@ -423,18 +427,9 @@ def incomp_params(api, dim, precision, workload, mu=1e-3):
 
 
 def pattern_nnz(mesh):
-    """Non-zeros of the PSPG pattern: identity rows for free nodes and bound-node velocities,
-    deg(n)(d+1) entries in every other row (deg counts the node itself)."""
-    import numpy as np
-    import scipy.sparse as sp
+    from pfem_gb300 import mesh as M
 
-    d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
-    Cm = sp.csr_matrix((np.ones(E * (d + 1)), (np.repeat(np.arange(E), d + 1), mesh.conn.T.ravel())), shape=(E, N))
-    deg = np.diff((Cm.T @ Cm).tocsr().indptr)
-    free = mesh.is_free()
-    bound = (mesh.flags & 1) != 0
-    per = np.where(free, d + 1, np.where(bound, d + deg * (d + 1), (d + 1) * deg * (d + 1)))
-    return int(per.sum())
+    return M.pspg_nnz(mesh)
 
 
 def spmv_bytes(nnz, R, s):
@@ -486,6 +481,8 @@ def run_gpu_incomp(args):
     build.build()
     if args.workload == "batch-c4":
         return run_gpu_batch(args)
+    if args.workload == "serve-c5":
+        return run_gpu_serve(args)
     cfg = INCOMP[args.workload]
     mesh = WL.c1() if args.workload == "incomp-c1" else WL.c3()
     d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
@@ -736,17 +733,135 @@ def run_gpu_batch(args):
     return 0
 
 
+def c5_requests(n, rate, seed=20261203):
+    """The served mix: Poisson arrivals at `rate`; 80% 2D dam breaks (1k-20k fluid nodes,
+    column aspect 0.5-2), 20% 3D (10k-50k fluid nodes; the 200k upper end is cut to keep a
+    bench run within minutes); weakly compressible or incompressible at even odds; mu
+    log-uniform in [1e-3, 1e-1]; WC requests 50-500 explicit steps, incompressible ones 10-50
+    Picard steps in 2D and 5-20 in 3D."""
+    import math
+
+    import numpy as np
+    from pfem_gb300 import api
+    from pfem_gb300 import mesh as M
+    from pfem_gb300 import serve as SV
+
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        is3d = rng.random() < 0.2
+        wc = rng.random() < 0.5
+        mu = math.exp(rng.uniform(math.log(1e-3), math.log(1e-1)))
+        if is3d:
+            nf = math.exp(rng.uniform(math.log(1e4), math.log(5e4)))
+            col = (0.5, 0.5, 1.0)
+            h = (0.25 / nf) ** (1 / 3)
+            m = M.dam_break_3d(h, seed=seed + i)
+            steps = int(rng.integers(50, 501)) if wc else int(rng.integers(5, 21))
+        else:
+            nf = math.exp(rng.uniform(math.log(1e3), math.log(2e4)))
+            a = rng.uniform(0.5, 2.0)
+            col = (math.sqrt(2 / a), math.sqrt(2 * a))
+            h = math.sqrt(2.0 / nf)
+            m = M.dam_break_2d(h, column=col, seed=seed + i)
+            steps = int(rng.integers(50, 501)) if wc else int(rng.integers(10, 51))
+        kind = api.KIND_WC_CDS_DPDT if wc else api.KIND_INCOMP_PSPG
+        st = M.wc_initial_states(m, column=col) if wc else M.incomp_initial_states(m, column=col)
+        out.append(SV.Request(kind, m, st, steps, dt=5e-4 if is3d else 1e-3, mu=mu, arrival=t, rid=i))
+    return out
+
+
+def run_gpu_serve(args):
+    import numpy as np
+    import torch
+    from pfem_gb300 import serve as SV
+
+    world, rank, local = dist_env()
+    t0 = time.perf_counter()
+    reqs = c5_requests(args.requests, args.rate)
+    mesh_s = time.perf_counter() - t0
+    free, total = torch.cuda.mem_get_info()
+    budget = int(0.5 * free)
+    srv = SV.Server(hbm_budget_bytes=budget, max_active=8)
+    clocks = ClockSampler(local)
+    clocks.start()
+    out = srv.run(reqs, realtime=True)
+    clk = clocks.stop()
+    m = SV.metrics(out, srv.makespan)
+    # the same two requests alone: results must not depend on the mix
+    same = True
+    for r in [x for x in out if x.error is None][:2]:
+        alone = SV.Server(hbm_budget_bytes=budget, max_active=1).run(
+            [c5_requests(args.requests, args.rate)[r.rid]], realtime=False)[0]
+        same &= bool(np.array_equal(alone.result, r.result))
+    h2d = sum(r.states.nbytes + r.mesh.pos.nbytes + r.mesh.conn.nbytes + r.mesh.flags.nbytes for r in out)
+    d2h = sum(r.states.nbytes + r.mesh.pos.nbytes for r in out)
+    steps = sum(r.steps for r in out if r.error is None)
+    if rank == 0:
+        res = {
+            "metric": "aggregate time-steps/s of a served request mix (C5), with p50/p99 request latency",
+            "value": m["steps_per_s"], "unit": "steps/s", "n_gpus": world, "steps": steps, "warmup": 0,
+            "ms_per_step": 1e3 * srv.makespan / max(steps, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "mixed", "data": "synthetic (seeded dam breaks, Poisson arrivals)",
+            "config": {"workload": "served mix (C5)", "requests": args.requests, "rate_per_s": args.rate,
+                       "hbm_budget_bytes": budget, "slots": 8, "host_meshing_s": mesh_s,
+                       "kinds": {"wc": sum(r.kind == 1 for r in out), "incomp": sum(r.kind == 0 for r in out)},
+                       "dims": {"2d": sum(r.mesh.dim == 2 for r in out), "3d": sum(r.mesh.dim == 3 for r in out)}},
+            "latency_p50_s": m["latency_p50_s"], "latency_p99_s": m["latency_p99_s"],
+            "queue_wait_p50_s": m["queue_wait_p50_s"], "queue_wait_p99_s": m["queue_wait_p99_s"],
+            "dof_per_s": m["dof_per_s"], "completed": m["completed"], "failed": m["failed"],
+            "errors": [r.error for r in out if r.error][:3],
+            "peak_active": srv.peak_active, "peak_estimated_bytes": srv.peak_bytes,
+            "alone_equals_mix": same,
+            "e2e": {"value": m["steps_per_s"], "unit": "steps/s", "h2d_bytes_per_step": int(h2d / max(steps, 1)),
+                    "d2h_bytes_per_step": int(d2h / max(steps, 1))},
+            "roofline": None, "cpu_baseline": None, "clocks": clk, "gpu_launches": None,
+        }
+        print(json.dumps(res))
+    return 0
+
+
 def run_reference_incomp(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
-    cfg = INCOMP[args.workload]
     from oracle import oracle as O
     from pfem_gb300 import mesh as M
     from pfem_gb300 import workloads as WL
 
     O.build()
-    if args.workload == "batch-c4":
+    if args.workload == "serve-c5":
+        cfg = {"metric": "aggregate time-steps/s of a served request mix (C5), with p50/p99 request latency",
+               "unit": "steps/s", "name": "served mix (C5)"}
+        t0 = time.perf_counter()
+        n_steps, n_req = 0, 0
+        for r in c5_requests(args.requests, args.rate):
+            om = O.OracleMesh(r.mesh)
+            s = r.states.copy()
+            if r.kind == 1:
+                p = O.wc_params(mu=r.mu, g=(0.0, -9.81) if r.mesh.dim == 2 else (0.0, 0.0, -9.81))
+                dt = O.wc_next_dt(om, p, s)
+                for _ in range(r.steps):
+                    O.wc_step(om, p, dt, s)
+                    dt = O.wc_next_dt(om, p, s)
+                    n_steps += 1
+            else:
+                g = (0.0, -9.81) if r.mesh.dim == 2 else (0.0, 0.0, -9.81)
+                for _ in range(r.steps):
+                    s, _ = O.pspg_picard_step(om, s, r.dt, mu=r.mu, g=g)
+                    n_steps += 1
+            n_req += 1
+            if time.perf_counter() - t0 > 120:
+                break
+        el = time.perf_counter() - t0
+        v = n_steps / el
+        sample = f"the first {n_req} requests run one after another ({n_steps} steps, {el:.1f} s)"
+    else:
+        cfg = INCOMP[args.workload]
+    if args.workload == "serve-c5":
+        pass
+    elif args.workload == "batch-c4":
         insts = WL.c4(args.instances)
         t0 = time.perf_counter()
         dof, inst_steps = 0, 0

@@ -167,6 +167,10 @@ PFG_API int pfg_picard_step(pfg_ctx* ctx, double dt, pfg_step_status* status);
  * [node_offsets[i], node_offsets[i+1]) and only elements among them.  rho[i], mu[i] are the
  * instance's fluid parameters.  No reference counterpart: the reference runs one Problem per
  * process; this replaces n_inst independent SolverIncompNewton objects. */
+/* Device memory currently held by the context, in bytes (for admission control by callers
+ * that run several contexts under one HBM budget). */
+PFG_API int pfg_device_bytes(const pfg_ctx* ctx, size_t* bytes);
+
 PFG_API int pfg_set_instances(pfg_ctx* ctx, int32_t n_inst, const int32_t* node_offsets, const double* rho,
                               const double* mu);
 /* One Picard time step of every instance at once (instance i with time step dt[i]); each

@@ -34,7 +34,7 @@ EXPORTED = (
     "pfg_wc_step", "pfg_next_dt", "pfg_set_time", "pfg_volume", "pfg_mass", "pfg_tip", "pfg_pspg_assemble",
     "pfg_get_csr", "pfg_get_geometry", "pfg_linear_solve", "pfg_version", "pfg_set_profiling",
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
-    "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch",
+    "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
 )
 NUM_PHASES = 13
 
@@ -109,6 +109,7 @@ def load(path=LIB_PATH):
         "pfg_wc_next_dt_noalloc": ([C.POINTER(Params), C.c_int32, C.c_int32, vp, vp, vp, vp, vp], C.c_int),
         "pfg_set_instances": ([vp, C.c_int32, ip, dp, dp], C.c_int),
         "pfg_picard_step_batch": ([vp, dp, C.POINTER(StepStatus)], C.c_int),
+        "pfg_device_bytes": ([vp, C.POINTER(C.c_size_t)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -209,6 +210,12 @@ class Context:
         st = StepStatus()
         self._check(self.L.pfg_picard_step(self.h, float(dt), C.byref(st)), "pfg_picard_step")
         return st
+
+    def device_bytes(self):
+        """Device memory held by this context."""
+        b = C.c_size_t()
+        self._check(self.L.pfg_device_bytes(self.h, C.byref(b)), "pfg_device_bytes")
+        return b.value
 
     def set_instances(self, node_offsets, rho, mu):
         """Declare the uploaded mesh a union of independent instances (mixed precision)."""

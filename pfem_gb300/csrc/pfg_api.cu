@@ -434,6 +434,12 @@ PFG_API int pfg_picard_step(pfg_ctx* c, double dt, pfg_step_status* st) {
     return picard_step(c, dt, st);
 }
 
+PFG_API int pfg_device_bytes(const pfg_ctx* c, size_t* bytes) {
+    if (!c || !bytes) return PFG_ERR_INVALID;
+    *bytes = c->bytes_in_use;
+    return PFG_OK;
+}
+
 PFG_API int pfg_set_instances(pfg_ctx* c, int32_t n_inst, const int32_t* node_offsets, const double* rho,
                               const double* mu) {
     int rc = check_ctx(c);

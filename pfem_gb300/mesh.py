@@ -332,3 +332,17 @@ def split_states(q, meshes):
         out.append(np.concatenate([q[f * N + o:f * N + o + m.n_nodes] for f in range(nf)]))
         o += m.n_nodes
     return out
+
+
+def pspg_nnz(mesh):
+    """Non-zeros of the PSPG matrix pattern: identity rows for free nodes and bound-node
+    velocities, deg(n)(d+1) entries in every other row (deg counts the node itself)."""
+    import scipy.sparse as sp
+
+    d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
+    inc = sp.csr_matrix((np.ones(E * (d + 1)), (np.repeat(np.arange(E), d + 1), mesh.conn.T.ravel())), shape=(E, N))
+    deg = np.diff((inc.T @ inc).tocsr().indptr)
+    free = mesh.is_free()
+    bound = (mesh.flags & BOUND) != 0
+    per = np.where(free, d + 1, np.where(bound, d + deg * (d + 1), (d + 1) * deg * (d + 1)))
+    return int(per.sum())

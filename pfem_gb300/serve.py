@@ -1,0 +1,174 @@
+"""Serving many simulations on one GPU: continuous admission under an HBM budget.
+
+Each admitted request gets its own library context: its mesh and fields stay resident on the
+device for its whole life, its kernels run on the context's own CUDA stream, and a worker
+thread drives its time loop.  Every library call runs without the Python interpreter lock, so
+the device interleaves the work of all admitted requests.  Admission is first come, first
+served under two limits, a number of slots and an HBM budget: a request's device footprint is
+estimated from its mesh before admission, and when a request finishes its context (and
+memory) is released and the next waiting requests are admitted at once.  Contexts never share
+device data, so a request's result is the same alone and in any mix.
+
+No reference counterpart: the reference runs one Problem per process.
+"""
+from __future__ import annotations
+
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api
+from . import mesh as M
+
+
+@dataclass
+class Request:
+    kind: int                       # api.KIND_INCOMP_PSPG or api.KIND_WC_CDS_DPDT
+    mesh: M.HostMesh
+    states: np.ndarray
+    steps: int
+    dt: float = 1e-3                # incompressible time step (WC steps use their CFL step)
+    precision: int = api.PREC_MIXED
+    mu: float = 1e-3
+    arrival: float = 0.0            # seconds after the start of the run
+    rid: int = -1
+    # filled in by the server
+    t_admit: float | None = None
+    t_done: float | None = None
+    result: np.ndarray | None = None
+    positions: np.ndarray | None = None
+    converged_steps: int = 0
+    device_bytes: int = 0
+    estimate_bytes: int = 0
+    error: str | None = None
+
+    @property
+    def dof(self):
+        return (self.mesh.dim + 1) * self.mesh.n_nodes
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+def estimate_device_bytes(kind, precision, mesh) -> int:
+    """Upper estimate of a context's device memory for `mesh`, from the library's buffers:
+    mesh and topology (positions, flags, connectivity, incidence lists, adjacency, CSR
+    structure), then the incompressible system (FP64 values, right-hand side, element data,
+    three state vectors, FP64 Krylov vectors and block inverses; FP32 copies in mixed form) or
+    the WC state and element->node planes."""
+    d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
+    R = (d + 1) * N
+    npe = d + 1
+    nnz = M.pspg_nnz(mesh)
+    P = nnz // (npe * npe) + N
+    b = 3 * d * N * 8 + N + npe * E * (4 + 4 + 1 + 4) + (N + 1) * 8 + 2 * P * 4 + (R + 1) * 4 + nnz * 4 + R * 4
+    if kind == api.KIND_INCOMP_PSPG:
+        b += nnz * 8 + R * 8 + (2 + d * npe) * E * 8 + 3 * R * 8 + 12 * R * 8 + npe * npe * N * 8
+        if precision == api.PREC_MIXED:
+            b += nnz * 4 + 8 * R * 4 + npe * npe * N * 4 + R * 8 + N * 4
+    else:
+        b += (2 * d + 2) * N * 8 * 3 + (7 * d + 5) * N * 4 + (1 + 3 * d) * npe * E * 4 + npe * E * 8 * (2 + d) \
+             + 4 * N * 8
+    return int(1.25 * b) + (4 << 20)
+
+
+class Server:
+    """Runs requests with at most `max_active` at a time and their estimated device memory
+    summed below `hbm_budget_bytes`."""
+
+    def __init__(self, hbm_budget_bytes: int, max_active: int = 8):
+        self.budget = int(hbm_budget_bytes)
+        self.max_active = int(max_active)
+        self._lock = threading.Condition()
+        self._active = 0
+        self._used = 0
+        self.peak_active = 0
+        self.peak_bytes = 0
+
+    # -- one request ----------------------------------------------------------------------
+    def _run_one(self, req: Request, t0: float):
+        try:
+            p = api.default_params(req.kind, req.mesh.dim)
+            p.precision = req.precision
+            p.mu = req.mu
+            p.hbm_budget_bytes = req.estimate_bytes
+            ctx = api.Context(p)
+            try:
+                ctx.upload_mesh(req.mesh)
+                ctx.set_states(req.states)
+                if req.kind == api.KIND_WC_CDS_DPDT:
+                    ctx.set_time(0.0, ctx.next_dt())
+                    ctx.wc_step(0.0, req.steps)
+                    req.converged_steps = req.steps
+                else:
+                    for _ in range(req.steps):
+                        st = ctx.picard_step(req.dt)
+                        req.converged_steps += st.converged
+                req.result = ctx.get_states()
+                req.positions = ctx.get_positions()
+                req.device_bytes = ctx.device_bytes()
+            finally:
+                ctx.close()
+        except Exception as e:  # reported with the request; the server keeps serving
+            req.error = str(e)
+        req.t_done = time.perf_counter() - t0
+        with self._lock:
+            self._active -= 1
+            self._used -= req.estimate_bytes
+            self._lock.notify_all()
+
+    # -- the request loop -----------------------------------------------------------------
+    def run(self, requests, realtime=True):
+        """Serve `requests` (arrival times in seconds from now when `realtime`, else all at
+        once, in list order).  Returns the requests with their timings and results."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        for i, r in enumerate(reqs):
+            if r.rid < 0:
+                r.rid = i
+            r.estimate_bytes = estimate_device_bytes(r.kind, r.precision, r.mesh)
+            if r.estimate_bytes > self.budget:
+                r.error = f"needs ~{r.estimate_bytes} bytes, over the {self.budget}-byte budget"
+        t0 = time.perf_counter()
+        threads = []
+        for r in reqs:
+            if r.error:
+                continue
+            if realtime:
+                wait = r.arrival - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
+            else:
+                r.arrival = time.perf_counter() - t0
+            with self._lock:
+                while self._active >= self.max_active or self._used + r.estimate_bytes > self.budget:
+                    self._lock.wait()
+                self._active += 1
+                self._used += r.estimate_bytes
+                self.peak_active = max(self.peak_active, self._active)
+                self.peak_bytes = max(self.peak_bytes, self._used)
+            r.t_admit = time.perf_counter() - t0
+            th = threading.Thread(target=self._run_one, args=(r, t0), daemon=True)
+            th.start()
+            threads.append(th)
+        for th in threads:
+            th.join()
+        self.makespan = time.perf_counter() - t0
+        return reqs
+
+
+def metrics(reqs, makespan):
+    """Latency percentiles (arrival to result), queueing delay and aggregate throughput."""
+    done = [r for r in reqs if r.error is None and r.t_done is not None]
+    lat = np.array([r.latency for r in done]) if done else np.zeros(1)
+    wait = np.array([r.t_admit - r.arrival for r in done]) if done else np.zeros(1)
+    steps = sum(r.steps for r in done)
+    dof_steps = sum(r.dof * r.steps for r in done)
+    return {
+        "requests": len(reqs), "completed": len(done), "failed": len(reqs) - len(done),
+        "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+        "queue_wait_p50_s": float(np.percentile(wait, 50)), "queue_wait_p99_s": float(np.percentile(wait, 99)),
+        "makespan_s": makespan, "steps_per_s": steps / makespan, "dof_per_s": dof_steps / makespan,
+    }
