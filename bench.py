@@ -162,20 +162,20 @@ def step_bytes(d, N, E):
 
 
 def wc_phase_bytes_mixed(d, N, E):
-    """Algorithmic bytes per launch of each kernel of the mixed form: double-float x, v, p
-    (8 bytes a component), FP32 rho - rho* and a; FP32 element->node contributions written once
-    by the element kernels (incidence-major planes, int32 slot map) and read once by the node
-    kernels; int32 connectivity and incidence offsets, one flag byte per node."""
+    """Algorithmic bytes per launch of each of the four kernels of the mixed form: double-float
+    x, v, p (8 bytes a component), FP32 rho - rho* and a; element->node records (2 floats for
+    continuity, 2+3d useful floats for momentum) written once by the element kernels (int32
+    slot map) and read once by the node kernels; int32 connectivity and incidence offsets, one
+    flag byte per node.  The prediction (x, v, a read; x, v written) is counted in the
+    continuity kernels, the CFL reduction in the momentum node kernel."""
     inc = E * (d + 1)
     npe = d + 1
+    state_in = N * (8 * d + 8 * d + 4 * d + 8)          # x, v, a, p
     return {
-        "WC predict": N * (2 * 8 * d + 4 * d + 2 * 8 * d + 1),                  # v, a, x in; v, x out
-        "WC continuity element": E * npe * 4 + N * (8 * d + 4 * d + 8) + inc * 4 + 2 * inc * 4,
-        "WC continuity node": 2 * inc * 4 + (N + 1) * 4 + N + N * 8 + N * (8 + 4),
-        "WC momentum element": E * npe * 4 + N * (8 * d + 4 * d + 8 + 4) + inc * 4 + (1 + 3 * d) * inc * 4,
-        "WC momentum node": (1 + 3 * d) * inc * 4 + (N + 1) * 4 + N + N * (8 + 4 + 8 * d) + N * 4 * d * 2
-                            + N * (4 * d + 8 * d) + 2 * N * 4,
-        "WC time step": E * npe * 4 + N * 4 * d + 2 * N * 4,
+        "WC continuity element": E * npe * 4 + N + state_in + inc * 4 + 2 * inc * 4,
+        "WC continuity node": 2 * inc * 4 + (N + 1) * 4 + N + state_in + N * (16 * d + 8 + 4),
+        "WC momentum element": E * npe * 4 + N * (8 * d + 4 * d + 8 + 4) + inc * 4 + (2 + 3 * d) * inc * 4,
+        "WC momentum node": (2 + 3 * d) * inc * 4 + (N + 1) * 4 + N + N * (4 + 4 + 8 * d) + N * (4 * d + 8 * d),
     }
 
 

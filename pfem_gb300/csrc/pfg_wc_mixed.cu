@@ -119,15 +119,17 @@ __host__ __device__ inline St state_ptrs(float* base, int dim, int N, int cur) {
 inline size_t state_floats(int dim, int N) { return (size_t)(7 * dim + 5) * N; }
 
 // Element -> node exchange, incidence-major: the contribution of element e to its local node i
-// goes to slot q = inc_slot[e*(dim+1)+i], the position of (e, i) in node-major incidence order,
-// so each node sums one contiguous segment.  Fields are planes of Q = E (dim+1) floats:
-//   continuity: [ML | CONT]            momentum: [MLR | FS_f (dim) | WH_f (dim) | WL_f (dim)]
-// (the continuity planes are consumed before the momentum planes are written).
+// goes to record q = inc_slot[e*(dim+1)+i], the position of (e, i) in node-major incidence
+// order, so each node reads one contiguous run of records.  Records are padded to whole float4s
+// and written with vector stores:
+//   continuity: [ML, CONT]                                                  (float2)
+//   momentum:   [MLR, FS_f (dim), WH_f (dim), WL_f (dim), HE, pad]          (2 / 3 float4)
+// (the continuity records are consumed before the momentum records are written).  HE is the
+// element's CFL length 2 Rin, from which each node takes the minimum over its elements.
 template <int DIM>
-struct Planes {
-    static constexpr int ML = 0, CONT = 1;
-    static constexpr int MLR = 0, FS = 1, WH = 1 + DIM, WL = 1 + 2 * DIM;
-    static constexpr int COUNT = 1 + 3 * DIM;
+struct Rec {
+    static constexpr int MLR = 0, FS = 1, WH = 1 + DIM, WL = 1 + 2 * DIM, HE = 1 + 3 * DIM;
+    static constexpr int MOM = (HE + 1 + 3) / 4 * 4;   // floats per momentum record (8 / 12)
 };
 
 // Jacobian from double-float coordinates: Jh exact differences of hi parts, Jl of lo parts.
@@ -209,47 +211,79 @@ __device__ __forceinline__ float det_f(const float (&J)[DIM][DIM]) {
     }
 }
 
+// Half-step velocity and position update of one node (the start of
+// m_solveWCompNewtonNoT, WCompNewton/Solver.cpp:249-254): v += dt/2 a; x += dt v unless fixed.
+// Evaluated where the values are first needed (continuity element kernel, for each element's
+// nodes) and stored by the continuity node kernel; both evaluate the same operations.
 template <int DIM>
-__global__ void k_m_predict(int N, const uint8_t* __restrict__ flags, St st, double* __restrict__ tdt) {
-    const float dt = *dtf_ptr(tdt);
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n == 0) tdt[T_TIME] += (double)dt;  // Problem::updateTime
-    if (n >= N) return;
-    const bool fixed = flags[n] & F_FIXED;
+__device__ __forceinline__ void predict_node(const St& st, int N, int n, bool fixed, float dt, float (&xh)[DIM],
+                                             float (&xl)[DIM], float (&vh)[DIM], float (&vl)[DIM]) {
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         const size_t k = (size_t)d * N + n;
-        float vh = st.vh[k], vl = st.vl[k];
-        df_add(vh, vl, 0.5f * dt * st.ax[k], 0.0f);
-        st.vh[k] = vh;
-        st.vl[k] = vl;
-        if (!fixed) {
-            float xh = st.xh[k], xl = st.xl[k];
-            df_add(xh, xl, dt * vh, dt * vl);
-            st.xh[k] = xh;
-            st.xl[k] = xl;
-        }
+        vh[d] = st.vh[k];
+        vl[d] = st.vl[k];
+        df_add(vh[d], vl[d], 0.5f * dt * st.ax[k], 0.0f);
+        xh[d] = st.xh[k];
+        xl[d] = st.xl[k];
+        if (!fixed) df_add(xh[d], xl[d], dt * vh[d], dt * vl[d]);
     }
 }
 
+// Element size and CFL length h_e = 2 Rin from the Jacobian (Element::getRin, Element.cpp:226-294)
 template <int DIM>
-__global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* __restrict__ conn, St st,
+__device__ __forceinline__ float cfl_length(const float (&J)[DIM][DIM], float size) {
+    if constexpr (DIM == 2) {
+        const float e01 = sqrtf(J[0][0] * J[0][0] + J[1][0] * J[1][0]);
+        const float e02 = sqrtf(J[0][1] * J[0][1] + J[1][1] * J[1][1]);
+        const float dx = J[0][1] - J[0][0], dy = J[1][1] - J[1][0];
+        const float e12 = sqrtf(dx * dx + dy * dy);
+        return 2.0f * (size / ((e01 + e12 + e02) * 0.5f));
+    } else {  // face areas from edge cross products
+        float u[4][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            u[1][a] = J[a][0];
+            u[2][a] = J[a][1];
+            u[3][a] = J[a][2];
+            u[0][a] = 0.0f;
+        }
+        auto nrm = [&](int a0, int a1, int a2) {
+            const float ux = u[a1][0] - u[a0][0], uy = u[a1][1] - u[a0][1], uz = u[a1][2] - u[a0][2];
+            const float wx = u[a2][0] - u[a0][0], wy = u[a2][1] - u[a0][1], wz = u[a2][2] - u[a0][2];
+            const float cx = uy * wz - uz * wy, cy = uz * wx - ux * wz, cz = ux * wy - uy * wx;
+            return sqrtf(cx * cx + cy * cy + cz * cz);
+        };
+        const float sum = nrm(0, 1, 2) + nrm(0, 3, 2) + nrm(0, 1, 3) + nrm(3, 1, 2);
+        return 2.0f * (6.0f * size / sum);
+    }
+}
+
+// Continuity element kernel (m_buildSystemdpdt, ContEquation.inl:353-413) on the predicted
+// positions and velocities, computed here from the state of the previous step.
+template <int DIM>
+__global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* __restrict__ conn,
+                                                       const uint8_t* __restrict__ flags, St st,
                                                        const double* __restrict__ tdt, WcmConst k,
-                                                       const int* __restrict__ slot, long long Q,
-                                                       float* __restrict__ cb) {
-    using L = Planes<DIM>;
+                                                       const int* __restrict__ slot, float* __restrict__ cb) {
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     const float dt = *dtf_ptr(const_cast<double*>(tdt));
     int nd[NPE];
     load_nodes<DIM>(conn, E, e, nd);
+    float xh[NPE][DIM], xl[NPE][DIM], vh[NPE][DIM], vl[NPE][DIM];
+#pragma unroll
+    for (int j = 0; j < NPE; ++j) predict_node<DIM>(st, N, nd[j], flags[nd[j]] & F_FIXED, dt, xh[j], xl[j], vh[j], vl[j]);
     float Jh[DIM][DIM], Jl[DIM][DIM], J[DIM][DIM];
-    jac_df<DIM>(st, N, nd, Jh, Jl);
 #pragma unroll
     for (int r = 0; r < DIM; ++r)
 #pragma unroll
-        for (int c = 0; c < DIM; ++c) J[r][c] = Jh[r][c] + Jl[r][c];
+        for (int c = 0; c < DIM; ++c) {
+            Jh[r][c] = __fsub_rn(xh[c + 1][r], xh[0][r]);
+            Jl[r][c] = __fsub_rn(xl[c + 1][r], xl[0][r]);
+            J[r][c] = Jh[r][c] + Jl[r][c];
+        }
     const float ae = det_f<DIM>(J) * k.refSize;
     float Gh[DIM][NPE], Gl[DIM][NPE];
     adj_df<DIM>(Jh, Jl, Gh, Gl);
@@ -260,12 +294,12 @@ __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* 
         ph[j] = st.ph[nd[j]];
         pl[j] = st.pl[nd[j]];
 #pragma unroll
-        for (int f = 0; f < DIM; ++f) adiv += (Gh[f][j] + Gl[f][j]) * st.vh[(size_t)f * N + nd[j]];
+        for (int f = 0; f < DIM; ++f) adiv += (Gh[f][j] + Gl[f][j]) * vh[j][f];
     }
     adiv *= k.refSize;  // |e| div v
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
-        const long long q = __ldg(slot + (size_t)e * NPE + i);
+        const int q = __ldg(slot + (size_t)e * NPE + i);
         float mp = 0, mdp = 0;
 #pragma unroll
         for (int j = 0; j < NPE; ++j) {
@@ -275,23 +309,40 @@ __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* 
         const float swn = k.K0 * k.s[i] + k.K0p * mp;
         float cont = -dt * swn * adiv;
         if (k.meduri) cont += ae * mdp;
-        cb[L::ML * Q + q] = ae * k.s[i];
-        cb[L::CONT * Q + q] = cont;
+        reinterpret_cast<float2*>(cb)[q] = make_float2(ae * k.s[i], cont);
     }
 }
 
+// Continuity node kernel: stores the node's predicted position and velocity, sums its
+// continuity records (ContEquation.inl:396-409), applies the free-node BC and Tait EOS.
 template <int DIM>
 __global__ void k_m_cont_node(int N, const int* __restrict__ ne_ptr, const uint8_t* __restrict__ flags,
-                              const float* __restrict__ cb, long long Q, WcmConst k, St st) {
-    using L = Planes<DIM>;
+                              const float* __restrict__ cb, WcmConst k, St st, double* __restrict__ tdt) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const float dt = *dtf_ptr(tdt);
+    if (n == 0) tdt[T_TIME] += (double)dt;  // Problem::updateTime
     if (n >= N) return;
-    float m = 0, f0 = 0;
-    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        m += cb[L::ML * Q + q];
-        f0 += cb[L::CONT * Q + q];
+    const uint8_t fl = flags[n];
+    {
+        float xh[DIM], xl[DIM], vh[DIM], vl[DIM];
+        predict_node<DIM>(st, N, n, fl & F_FIXED, dt, xh, xl, vh, vl);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            const size_t kk = (size_t)d * N + n;
+            st.vh[kk] = vh[d];
+            st.vl[kk] = vl[d];
+            st.xh[kk] = xh[d];
+            st.xl[kk] = xl[d];
+        }
     }
-    if (flags[n] & F_FREE) {
+    float m = 0, f0 = 0;
+    const float2* r2 = reinterpret_cast<const float2*>(cb);
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const float2 c2 = r2[q];
+        m += c2.x;
+        f0 += c2.y;
+    }
+    if (fl & F_FREE) {
         st.ph[n] = 0.0f;
         st.pl[n] = 0.0f;
         st.rd[n] = 0.0f;
@@ -305,11 +356,11 @@ __global__ void k_m_cont_node(int N, const int* __restrict__ ne_ptr, const uint8
     st.rd[n] = k.rho_star * expm1f(log1pf(k.kk * ph) * k.ikp);
 }
 
+// Momentum element kernel (MomEquation.inl:229-302) and the element's CFL length.
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* __restrict__ conn, St st, WcmConst k,
-                                                      const int* __restrict__ slot, long long Q,
-                                                      float* __restrict__ cb) {
-    using L = Planes<DIM>;
+                                                      const int* __restrict__ slot, float* __restrict__ cb) {
+    using L = Rec<DIM>;
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -321,7 +372,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
     for (int r = 0; r < DIM; ++r)
 #pragma unroll
         for (int c = 0; c < DIM; ++c) J[r][c] = Jh[r][c] + Jl[r][c];
-    const float ae = det_f<DIM>(J) * k.refSize;
+    const float det = det_f<DIM>(J);
+    const float ae = det * k.refSize;
+    const float he = cfl_length<DIM>(J, ae);
     float Gh[DIM][NPE], Gl[DIM][NPE], A[DIM][NPE];
     adj_df<DIM>(Jh, Jl, Gh, Gl);
 #pragma unroll
@@ -353,7 +406,10 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
     const float kf = k.mu_sum / ae;
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
-        const long long q = __ldg(slot + (size_t)e * NPE + i);
+        const int q = __ldg(slot + (size_t)e * NPE + i);
+        float rec[L::MOM];
+#pragma unroll
+        for (int r = 0; r < L::MOM; ++r) rec[r] = 0.0f;
         float mr = 0, dp = 0;
 #pragma unroll
         for (int j = 0; j < NPE; ++j) {
@@ -361,7 +417,7 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
             dp += k.s[j] * ((ph[j] - ph[i]) + (pl[j] - pl[i]));
         }
         const float mlr = ae * mr;
-        cb[L::MLR * Q + q] = mlr;
+        rec[L::MLR] = mlr;
         float gg[NPE];
 #pragma unroll
         for (int j = 0; j < NPE; ++j) {
@@ -378,67 +434,136 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
 #pragma unroll
             for (int f2 = 0; f2 < DIM; ++f2) kv += A[f2][i] * Lg[f2][f1];
             kv -= (2.0f / 3.0f) * A[f1][i] * divA;
-            cb[(L::FS + f1) * Q + q] = -kf * kv + A[f1][i] * dp + mlr * k.g[f1];
-            cb[(L::WH + f1) * Q + q] = Gh[f1][i];
-            cb[(L::WL + f1) * Q + q] = Gl[f1][i];
+            rec[L::FS + f1] = -kf * kv + A[f1][i] * dp + mlr * k.g[f1];
+            rec[L::WH + f1] = Gh[f1][i];
+            rec[L::WL + f1] = Gl[f1][i];
         }
+        rec[L::HE] = he;
+        float4* dst = reinterpret_cast<float4*>(cb + (size_t)q * L::MOM);
+#pragma unroll
+        for (int v = 0; v < L::MOM / 4; ++v) dst[v] = make_float4(rec[4 * v], rec[4 * v + 1], rec[4 * v + 2], rec[4 * v + 3]);
     }
 }
 
+// Momentum node kernel (MomEquation.inl:201-226,279-374): sums the node's records, applies the
+// BCs, updates acceleration and velocity.  With `partials`, also the CFL time step of the next
+// step (computeNextDT, WCompNewton/Solver.cpp:192-234): the reference's minimum over elements
+// of sc^2 h_e^2 / max_{nodes of e} max(|u|^2, c^2, 4 alpha^2 / h_e^2) equals the minimum over
+// nodes of the same expression at the node's smallest incident h_e (it grows with h_e), and in
+// FP32 the two orders give the same bits (every operation is monotone).
 template <int DIM>
-__global__ void k_m_mom_node(int N, const int* __restrict__ ne_ptr, const uint8_t* __restrict__ flags,
-                             const float* __restrict__ cb, long long Q, const double* __restrict__ vbc,
-                             const double* __restrict__ tdt, WcmConst k, St st, float* __restrict__ nodal) {
-    using L = Planes<DIM>;
+__global__ void __launch_bounds__(BLOCK) k_m_mom_node(int N, const int* __restrict__ ne_ptr,
+                                                      const uint8_t* __restrict__ flags, const float* __restrict__ cb,
+                                                      const double* __restrict__ vbc, double* __restrict__ tdt,
+                                                      WcmConst k, St st, float* __restrict__ partials) {
+    using L = Rec<DIM>;
+    __shared__ float sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    const float dt = *dtf_ptr(const_cast<double*>(tdt));
-    float m = 0, F[DIM], Wh[DIM], Wl[DIM];
+    const float dt = *dtf_ptr(tdt);
+    float best = 3.0e38f;
+    if (n < N) {
+        float m = 0, F[DIM], Wh[DIM], Wl[DIM];
+        float hmin = 3.0e38f;
 #pragma unroll
-    for (int f = 0; f < DIM; ++f) F[f] = Wh[f] = Wl[f] = 0;
-    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        m += cb[L::MLR * Q + q];
+        for (int f = 0; f < DIM; ++f) F[f] = Wh[f] = Wl[f] = 0;
+        const int q0 = ne_ptr[n], q1 = ne_ptr[n + 1];
+        for (int q = q0; q < q1; ++q) {
+            float rec[L::MOM];
+            const float4* src = reinterpret_cast<const float4*>(cb + (size_t)q * L::MOM);
+#pragma unroll
+            for (int v = 0; v < L::MOM / 4; ++v) {
+                const float4 t = src[v];
+                rec[4 * v] = t.x;
+                rec[4 * v + 1] = t.y;
+                rec[4 * v + 2] = t.z;
+                rec[4 * v + 3] = t.w;
+            }
+            m += rec[L::MLR];
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) {
+                F[f] += rec[L::FS + f];
+                df_add(Wh[f], Wl[f], rec[L::WH + f], rec[L::WL + f]);
+            }
+            hmin = fminf(hmin, rec[L::HE]);
+        }
+        const float pS = st.ph[n] * k.S * k.refSize;
+#pragma unroll
+        for (int f = 0; f < DIM; ++f) F[f] += pS * (Wh[f] + Wl[f]);
+        float inv = 1.0f / m;
+        const uint8_t fl = flags[n];
+        if ((fl & F_FREE) && !(fl & F_BOUND)) {
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) F[f] = k.g[f];
+            inv = 1.0f;
+        } else if ((fl & F_BOUND) && (fl & F_DIRICHLET)) {
+            // Dirichlet values are host-provided FP64; read as float pairs written at set time
+            const float* vb = reinterpret_cast<const float*>(vbc);
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) F[f] = vb[(size_t)f * N + n];
+            inv = 1.0f;
+        }
+        float u2 = 0;
 #pragma unroll
         for (int f = 0; f < DIM; ++f) {
-            F[f] += cb[(L::FS + f) * Q + q];
-            df_add(Wh[f], Wl[f], cb[(L::WH + f) * Q + q], cb[(L::WL + f) * Q + q]);
+            const size_t kk = (size_t)f * N + n;
+            const float a = inv * F[f];
+            st.ax[kk] = a;
+            float vh = st.vh[kk], vl = st.vl[kk];
+            df_add(vh, vl, 0.5f * dt * a, 0.0f);
+            st.vh[kk] = vh;
+            st.vl[kk] = vl;
+            u2 += vh * vh;
+        }
+        if (partials && q1 > q0) {
+            const float rho = k.rho_star + st.rd[n];
+            const float m1 = fmaxf(u2, (k.K0 + k.K0p * st.ph[n]) / rho);
+            const float m2 = k.mu / rho;
+            const float maxSq = fmaxf(m1, 4.0f * m2 * m2 / (hmin * hmin));
+            best = k.sc * k.sc * hmin * hmin / maxSq;
         }
     }
-    const float pS = st.ph[n] * k.S * k.refSize;
+    if (!partials) return;
+    // grid minimum: block minimum, then the last block to finish reduces the block minima
 #pragma unroll
-    for (int f = 0; f < DIM; ++f) F[f] += pS * (Wh[f] + Wl[f]);
-    float inv = 1.0f / m;
-    const uint8_t fl = flags[n];
-    if ((fl & F_FREE) && !(fl & F_BOUND)) {
+    for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_down_sync(0xffffffffu, best, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = best;
+    __syncthreads();
+    if (wid == 0) {
+        best = lane < BLOCK / 32 ? sh[lane] : 3.0e38f;
 #pragma unroll
-        for (int f = 0; f < DIM; ++f) F[f] = k.g[f];
-        inv = 1.0f;
-    } else if ((fl & F_BOUND) && (fl & F_DIRICHLET)) {
-        // Dirichlet values are host-provided FP64; read as float pairs written at set time
-        const float* vb = reinterpret_cast<const float*>(vbc);
-#pragma unroll
-        for (int f = 0; f < DIM; ++f) F[f] = vb[(size_t)f * N + n];
-        inv = 1.0f;
+        for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_down_sync(0xffffffffu, best, o));
     }
-    float u2 = 0;
-#pragma unroll
-    for (int f = 0; f < DIM; ++f) {
-        const size_t kk = (size_t)f * N + n;
-        const float a = inv * F[f];
-        st.ax[kk] = a;
-        float vh = st.vh[kk], vl = st.vl[kk];
-        df_add(vh, vl, 0.5f * dt * a, 0.0f);
-        st.vh[kk] = vh;
-        st.vl[kk] = vl;
-        u2 += vh * vh;
+    __shared__ bool last;
+    unsigned* ticket = reinterpret_cast<unsigned*>(tdt + T_TICKET);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = best;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
-    if (nodal) {
-        const float rho = k.rho_star + st.rd[n];
-        nodal[n] = fmaxf(u2, (k.K0 + k.K0p * st.ph[n]) / rho);
-        nodal[(size_t)N + n] = k.mu / rho;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    float mn = 3.0e38f;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += BLOCK) mn = fminf(mn, __ldcg(partials + i));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, o));
+    __syncthreads();
+    if (lane == 0) sh[wid] = mn;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = 3.0e38f;
+        for (int w = 0; w < BLOCK / 32; ++w) r = fminf(r, sh[w]);
+        const float dtn = fminf(sqrtf(r), k.max_dt);
+        *dtf_ptr(tdt) = dtn;
+        tdt[T_DT] = (double)dtn;
+        tdt[T_MIN] = (double)r;
+        *ticket = 0u;
     }
 }
 
+// CFL time step of the current state, element by element (used once per state upload; the
+// step computes it inside k_m_mom_node).
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_dt(int E, int N, const int* __restrict__ conn, St st,
                                                 const float* __restrict__ nodal, WcmConst k,
@@ -454,32 +579,7 @@ __global__ void __launch_bounds__(BLOCK) k_m_dt(int E, int N, const int* __restr
         for (int r = 0; r < DIM; ++r)
 #pragma unroll
             for (int c = 0; c < DIM; ++c) J[r][c] = Jh[r][c] + Jl[r][c];
-        const float size = det_f<DIM>(J) * k.refSize;
-        float he;
-        if constexpr (DIM == 2) {  // Element::getRin 2D (Element.cpp:228-241)
-            const float e01 = sqrtf(J[0][0] * J[0][0] + J[1][0] * J[1][0]);
-            const float e02 = sqrtf(J[0][1] * J[0][1] + J[1][1] * J[1][1]);
-            const float dx = J[0][1] - J[0][0], dy = J[1][1] - J[1][0];
-            const float e12 = sqrtf(dx * dx + dy * dy);
-            he = 2.0f * (size / ((e01 + e12 + e02) * 0.5f));
-        } else {  // Element::getRin 3D (Element.cpp:242-293): face normals from edge vectors
-            float u[4][3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                u[1][a] = J[a][0];
-                u[2][a] = J[a][1];
-                u[3][a] = J[a][2];
-                u[0][a] = 0.0f;
-            }
-            auto nrm = [&](int a0, int a1, int a2) {
-                const float ux = u[a1][0] - u[a0][0], uy = u[a1][1] - u[a0][1], uz = u[a1][2] - u[a0][2];
-                const float wx = u[a2][0] - u[a0][0], wy = u[a2][1] - u[a0][1], wz = u[a2][2] - u[a0][2];
-                const float cx = uy * wz - uz * wy, cy = uz * wx - ux * wz, cz = ux * wy - uy * wx;
-                return sqrtf(cx * cx + cy * cy + cz * cz);
-            };
-            const float sum = nrm(0, 1, 2) + nrm(0, 3, 2) + nrm(0, 1, 3) + nrm(3, 1, 2);
-            he = 2.0f * (6.0f * size / sum);
-        }
+        const float he = cfl_length<DIM>(J, det_f<DIM>(J) * k.refSize);
         float m1 = 0, m2 = 0;
 #pragma unroll
         for (int a = 0; a <= DIM; ++a) {
@@ -595,38 +695,29 @@ int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
     St st = st_of(c);
     float* cb = ptr<float>(c->wc_el);
     const int* slot = ptr<int>(c->inc_slot);
-    const long long Q = (long long)E * (DIM + 1);
-    float* nodal = ptr<float>(c->wc_nodal);
+    // block minima of the CFL reduction go to the per-node CFL scratch (unused during a step)
+    float* partials = ptr<float>(c->wc_nodal);
     double* tdt = ptr<double>(c->wc_dt);
     const double* vbcf = reinterpret_cast<const double*>(ptr<float>(c->wc_eld));  // FP32 Dirichlet values
     const int gn = div_up(N, BLOCK), ge = std::max(1, div_up(E, BLOCK));
-    prof_begin(c, PH_WC_PREDICT);
-    k_m_predict<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<uint8_t>(c->flags), st, tdt);
-    prof_end(c, PH_WC_PREDICT);
+    const uint8_t* flags = ptr<uint8_t>(c->flags);
     if (E > 0) {
         prof_begin(c, PH_WC_CONT_ELEM);
-        k_m_cont_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, tdt, k, slot, Q, cb);
+        k_m_cont_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), flags, st, tdt, k, slot, cb);
         prof_end(c, PH_WC_CONT_ELEM);
     }
     prof_begin(c, PH_WC_CONT_NODE);
-    k_m_cont_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<uint8_t>(c->flags), cb, Q, k, st);
+    k_m_cont_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), flags, cb, k, st, tdt);
     prof_end(c, PH_WC_CONT_NODE);
     if (E > 0) {
         prof_begin(c, PH_WC_MOM_ELEM);
-        k_m_mom_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, k, slot, Q, cb);
+        k_m_mom_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, k, slot, cb);
         prof_end(c, PH_WC_MOM_ELEM);
     }
     prof_begin(c, PH_WC_MOM_NODE);
-    k_m_mom_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<uint8_t>(c->flags), cb, Q, vbcf, tdt,
-                                                   k, st, adapt ? nodal : nullptr);
+    k_m_mom_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), flags, cb, vbcf, tdt, k, st,
+                                                   adapt && E > 0 ? partials : nullptr);
     prof_end(c, PH_WC_MOM_NODE);
-    if (adapt && E > 0) {
-        const int grid = std::min(c->max_grid, ge);
-        prof_begin(c, PH_WC_DT);
-        k_m_dt<DIM><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, nodal, k,
-                                                   reinterpret_cast<float*>(ptr<double>(c->red)), tdt);
-        prof_end(c, PH_WC_DT);
-    }
     PFG_CHECK_LAUNCH(c);
     return PFG_OK;
 }
@@ -636,8 +727,8 @@ int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
 size_t wcm_state_bytes(pfg_ctx* c) { return sizeof(float) * state_floats(c->dim, c->N); }
 
 size_t wcm_elem_bytes(pfg_ctx* c) {
-    const int planes = c->dim == 2 ? Planes<2>::COUNT : Planes<3>::COUNT;
-    return sizeof(float) * (size_t)planes * (c->dim + 1) * std::max(c->E, 1);
+    const int rec = c->dim == 2 ? Rec<2>::MOM : Rec<3>::MOM;
+    return sizeof(float) * (size_t)rec * (c->dim + 1) * std::max(c->E, 1);
 }
 
 int wcm_launch_step(pfg_ctx* c, bool adapt) {
