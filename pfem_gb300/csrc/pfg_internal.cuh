@@ -109,7 +109,7 @@ struct pfg_ctx {
     cudaGraphExec_t wc_graph[2] = {nullptr, nullptr};
     // mixed-precision PSPG: FP32 block inverses, instance tables (segments of nodes,
     // per-instance ints / doubles / FP32 Krylov scalars), reduction partials, counters
-    pfg::DBuf binv32, node_inst, mx_seg, mx_ii, mx_id, mx_sc, mx_part, mx_cnt, mx_scale;
+    pfg::DBuf binv32, node_inst, mx_seg, mx_ii, mx_id, mx_sc, mx_part, mx_cnt, mx_scale, mx_list;
     int n_inst = 0, n_seg = 0;
     cudaGraphExec_t mx_graph[2] = {nullptr, nullptr};  // one chunk of BiCGSTAB iterations [FP32, FP64]
     std::vector<int> h_mx_ii;

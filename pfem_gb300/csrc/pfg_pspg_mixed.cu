@@ -528,9 +528,10 @@ __device__ __forceinline__ T row_dot_t(int r, bool act, const int* __restrict__ 
 
 // p = r + beta (p - omega v); phat = Binv p
 template <class T, int DIM>
-__global__ void __launch_bounds__(NB) k_mx_up_p(Mx m, T* __restrict__ scb, int N, T* __restrict__ W, size_t ld,
+__global__ void __launch_bounds__(NB) k_mx_up_p(Mx m, const int* __restrict__ list, T* __restrict__ scb, int N,
+                                                T* __restrict__ W, size_t ld,
                                                 const T* __restrict__ binv) {
-    const int b = blockIdx.x;
+    const int b = list ? list[blockIdx.x] : blockIdx.x;  // segment
     const T* sc = scb + m.seg[3 * b] * M_COUNT;
     if (sc[M_DONE] != 0) return;
     const int n = m.seg[3 * b + 1] + threadIdx.x;
@@ -549,9 +550,10 @@ __global__ void __launch_bounds__(NB) k_mx_up_p(Mx m, T* __restrict__ scb, int N
 
 // s = r - alpha v; shat = Binv s
 template <class T, int DIM>
-__global__ void __launch_bounds__(NB) k_mx_up_s(Mx m, T* __restrict__ scb, int N, T* __restrict__ W, size_t ld,
+__global__ void __launch_bounds__(NB) k_mx_up_s(Mx m, const int* __restrict__ list, T* __restrict__ scb, int N,
+                                                T* __restrict__ W, size_t ld,
                                                 const T* __restrict__ binv) {
-    const int b = blockIdx.x;
+    const int b = list ? list[blockIdx.x] : blockIdx.x;  // segment
     const T* sc = scb + m.seg[3 * b] * M_COUNT;
     if (sc[M_DONE] != 0) return;
     const int n = m.seg[3 * b + 1] + threadIdx.x;
@@ -570,11 +572,12 @@ __global__ void __launch_bounds__(NB) k_mx_up_s(Mx m, T* __restrict__ scb, int N
 // out = A in over the rows of the segment's nodes (all fields); dots for alpha or omega.
 // MODE 0: v = A phat, alpha = rho / (rhat . v).  MODE 1: t = A shat, omega = (t.s)/(t.t).
 template <class T, int G, int DIM, int MODE>
-__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, T* __restrict__ scb, int cnt_slot, int N,
+__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, const int* __restrict__ list, T* __restrict__ scb,
+                                                        int cnt_slot, int N,
                                                         const int* __restrict__ rp, const int* __restrict__ col,
                                                         const T* __restrict__ val, T* __restrict__ W, size_t ld) {
     __shared__ double sh[32];
-    const int b = blockIdx.x;
+    const int b = list ? list[blockIdx.x] : blockIdx.x;  // segment
     const int inst = m.seg[3 * b];
     T* sc = scb + inst * M_COUNT;
     if (sc[M_DONE] != 0) return;
@@ -627,10 +630,11 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, T* __restrict__ sc
 // x += S (alpha phat + omega shat) (FP64 solution; S = I for the unscaled FP64 system);
 // r = s - omega t; rho = rhat.r; rr = r.r
 template <class T, int DIM>
-__global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, T* __restrict__ scb, int cnt_slot, int N, double* __restrict__ x,
+__global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, const int* __restrict__ list, T* __restrict__ scb, int cnt_slot,
+                                                int N, double* __restrict__ x,
                                                 const double* __restrict__ scale, T* __restrict__ W, size_t ld) {
     __shared__ double sh[32];
-    const int b = blockIdx.x;
+    const int b = list ? list[blockIdx.x] : blockIdx.x;  // segment
     const int inst = m.seg[3 * b];
     T* sc = scb + inst * M_COUNT;
     if (sc[M_DONE] != 0) return;
@@ -791,55 +795,82 @@ int mx_residual(pfg_ctx* c, const MxConst& k, int kind, Counters* cnt) {
     return read_counters(c, cnt);
 }
 
-// Correction solves in precision T of every instance that needs one, until all are done or
-// the iteration cap is reached.  x (the FP64 iterate) is updated in place.
+// The five kernels of one BiCGSTAB iteration in precision T, over `grid` segments (all of them,
+// or the compacted list of segments whose instance is still iterating).
+template <class T, int DIM>
+struct KSet {
+    Mx m;
+    const int* list;
+    T* scb;
+    int slot, N;
+    size_t ld;
+    T* W;
+    const T* binv;
+    const T* val;
+    const double* scale;
+    const int* rp;
+    const int* col;
+    double* x;
+
+    void iterate(pfg_ctx* c, int grid) const {
+        constexpr int G = DIM == 2 ? 8 : 16;
+        prof_begin(c, PH_KRYLOV_ITER);
+        k_mx_up_p<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
+        prof_begin(c, PH_KRYLOV_SPMV);
+        k_mx_spmv<T, G, DIM, 0><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, col, val, W, ld);
+        prof_end(c, PH_KRYLOV_SPMV);
+        k_mx_up_s<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
+        prof_begin(c, PH_KRYLOV_SPMV);
+        k_mx_spmv<T, G, DIM, 1><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, col, val, W, ld);
+        prof_end(c, PH_KRYLOV_SPMV);
+        k_mx_up_x<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, slot, N, x, scale, W, ld);
+        prof_end(c, PH_KRYLOV_ITER);
+    }
+};
+
+template <class T, int DIM>
+KSet<T, DIM> kset(pfg_ctx* c, const int* list) {
+    constexpr bool F32 = sizeof(T) == 4;
+    KSet<T, DIM> k;
+    k.m = mx_ptrs(c);
+    k.list = list;
+    k.scb = F32 ? reinterpret_cast<T*>(k.m.sc) : reinterpret_cast<T*>(k.m.sc64);
+    k.slot = F32 ? C_NEED : C_NEED64;
+    k.N = c->N;
+    k.ld = (size_t)c->R;
+    k.W = F32 ? reinterpret_cast<T*>(c->kv32.p) : reinterpret_cast<T*>(c->kv.p);
+    k.binv = F32 ? reinterpret_cast<const T*>(c->binv32.p) : reinterpret_cast<const T*>(c->binv.p);
+    k.val = F32 ? reinterpret_cast<const T*>(c->val32.p) : reinterpret_cast<const T*>(c->val.p);
+    k.scale = F32 ? ptr<double>(c->mx_scale) : nullptr;
+    k.rp = ptr<int>(c->row_ptr);
+    k.col = ptr<int>(c->col);
+    k.x = ptr<double>(c->q);
+    return k;
+}
+
+// Correction solves in precision T of a single mesh, until done or the iteration cap is
+// reached: chunks of 8 iterations replayed from a CUDA graph, the running-solve counter polled
+// after 1, 1, 2, 2, 4, 4, ... chunks (a finished solve skips the extra iterations in every
+// kernel).  x (the FP64 iterate) is updated in place.
 template <class T, int DIM>
 int mx_inner(pfg_ctx* c, Counters* cnt) {
     constexpr bool F32 = sizeof(T) == 4;
-    constexpr int G = DIM == 2 ? 8 : 16;
-    Mx m = mx_ptrs(c);
-    const int N = c->N;
-    const size_t ld = (size_t)c->R;
-    T* W = F32 ? reinterpret_cast<T*>(c->kv32.p) : reinterpret_cast<T*>(c->kv.p);
-    const T* binv = F32 ? reinterpret_cast<const T*>(c->binv32.p) : reinterpret_cast<const T*>(c->binv.p);
-    const T* val = F32 ? reinterpret_cast<const T*>(c->val32.p) : reinterpret_cast<const T*>(c->val.p);
-    T* scb = F32 ? reinterpret_cast<T*>(m.sc) : reinterpret_cast<T*>(m.sc64);
-    const int slot = F32 ? C_NEED : C_NEED64;
-    const double* scale = F32 ? ptr<double>(c->mx_scale) : nullptr;
-    const int* rp = ptr<int>(c->row_ptr);
-    const int* col = ptr<int>(c->col);
-    double* x = ptr<double>(c->q);
+    const KSet<T, DIM> ks = kset<T, DIM>(c, nullptr);
     cudaGraphExec_t& graph = c->mx_graph[F32 ? 0 : 1];
     const int max_it = std::max(1, c->prm.krylov_max_iter);
     const int chunk = 8;
     int done_it = 0;
-    auto iteration = [&]() {
-        prof_begin(c, PH_KRYLOV_ITER);
-        k_mx_up_p<T, DIM><<<c->n_seg, NB, 0, c->stream>>>(m, scb, N, W, ld, binv);
-        prof_begin(c, PH_KRYLOV_SPMV);
-        k_mx_spmv<T, G, DIM, 0><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, scb, slot, N, rp, col, val, W, ld);
-        prof_end(c, PH_KRYLOV_SPMV);
-        k_mx_up_s<T, DIM><<<c->n_seg, NB, 0, c->stream>>>(m, scb, N, W, ld, binv);
-        prof_begin(c, PH_KRYLOV_SPMV);
-        k_mx_spmv<T, G, DIM, 1><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, scb, slot, N, rp, col, val, W, ld);
-        prof_end(c, PH_KRYLOV_SPMV);
-        k_mx_up_x<T, DIM><<<c->n_seg, NB, 0, c->stream>>>(m, scb, slot, N, x, scale, W, ld);
-        prof_end(c, PH_KRYLOV_ITER);
-    };
     int polls = 0;
     int* need = F32 ? &cnt->need32 : &cnt->need64;
     while (*need > 0 && done_it < max_it) {
-        // chunks between two polls of the running-solve counter: 1, 1, 2, 2, 4, 4, ... graph
-        // launches (finished instances skip the extra iterations in every kernel)
         const int reps = std::min(1 << (polls / 2), 4);
         const int n = std::min(chunk * reps, max_it - done_it);
         ++polls;
         if (n == chunk * reps && !c->prof) {
-            // a chunk of iterations replayed from one CUDA graph (captured once per instance set)
             if (!graph) {
                 cudaGraph_t g = nullptr;
                 PFG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-                for (int it = 0; it < chunk; ++it) iteration();
+                for (int it = 0; it < chunk; ++it) ks.iterate(c, c->n_seg);
                 cudaError_t e = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
                 e = cudaGraphInstantiate(&graph, g, 0);
@@ -851,7 +882,7 @@ int mx_inner(pfg_ctx* c, Counters* cnt) {
             }
             for (int r = 0; r < reps; ++r) PFG_CUDA(c, cudaGraphLaunch(graph, c->stream));
         } else {
-            for (int it = 0; it < n; ++it) iteration();
+            for (int it = 0; it < n; ++it) ks.iterate(c, c->n_seg);
         }
         PFG_CHECK_LAUNCH(c);
         done_it += n;
@@ -859,6 +890,68 @@ int mx_inner(pfg_ctx* c, Counters* cnt) {
         if (rc) return rc;
     }
     return PFG_OK;
+}
+
+// Correction solves of a batch: FP32 and FP64 instances iterate in the same loop, and after
+// every chunk of 8 iterations the kernels are relaunched over the compacted list of segments
+// whose instance is still iterating (finished instances cost nothing afterwards).
+template <int DIM>
+int mx_inner_batch(pfg_ctx* c, Counters* cnt) {
+    const int K = c->n_inst;
+    int* d_list32 = ptr<int>(c->mx_list);
+    int* d_list64 = d_list32 + c->n_seg;
+    const KSet<float, DIM> k32 = kset<float, DIM>(c, d_list32);
+    const KSet<double, DIM> k64 = kset<double, DIM>(c, d_list64);
+    std::vector<float> done32((size_t)K * M_COUNT);
+    std::vector<double> done64((size_t)K * M_COUNT);
+    std::vector<int> l32, l64;
+    l32.reserve(c->n_seg);
+    l64.reserve(c->n_seg);
+    const std::vector<int>& hi = c->h_mx_ii;
+    auto rebuild = [&]() -> int {
+        const Mx m = mx_ptrs(c);
+        PFG_CUDA(c, cudaMemcpyAsync(done32.data(), m.sc, sizeof(float) * done32.size(), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        PFG_CUDA(c, cudaMemcpyAsync(done64.data(), m.sc64, sizeof(double) * done64.size(), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        std::vector<int> n32, n64;
+        n32.reserve(c->n_seg);
+        n64.reserve(c->n_seg);
+        for (int i = 0; i < K; ++i) {
+            const int b0 = hi[(size_t)i * I_COUNT + I_B0], b1 = hi[(size_t)i * I_COUNT + I_B1];
+            if (done32[(size_t)i * M_COUNT + M_DONE] == 0.0f)
+                for (int b = b0; b < b1; ++b) n32.push_back(b);
+            if (done64[(size_t)i * M_COUNT + M_DONE] == 0.0)
+                for (int b = b0; b < b1; ++b) n64.push_back(b);
+        }
+        if (n32 != l32 && !n32.empty())
+            PFG_CUDA(c, cudaMemcpyAsync(d_list32, n32.data(), sizeof(int) * n32.size(), cudaMemcpyHostToDevice,
+                                        c->stream));
+        if (n64 != l64 && !n64.empty())
+            PFG_CUDA(c, cudaMemcpyAsync(d_list64, n64.data(), sizeof(int) * n64.size(), cudaMemcpyHostToDevice,
+                                        c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        l32.swap(n32);
+        l64.swap(n64);
+        return PFG_OK;
+    };
+    int rc;
+    if ((rc = rebuild())) return rc;
+    const int max_it = std::max(1, c->prm.krylov_max_iter);
+    const int chunk = 8;
+    int done_it = 0;
+    while ((!l32.empty() || !l64.empty()) && done_it < max_it) {
+        const int n = std::min(chunk, max_it - done_it);
+        for (int it = 0; it < n; ++it) {
+            if (!l32.empty()) k32.iterate(c, (int)l32.size());
+            if (!l64.empty()) k64.iterate(c, (int)l64.size());
+        }
+        PFG_CHECK_LAUNCH(c);
+        done_it += n;
+        if ((rc = rebuild())) return rc;
+    }
+    return read_counters(c, cnt);
 }
 
 // One linear solve of every active instance by iterative refinement: correction sweeps in
@@ -871,8 +964,12 @@ int mx_refine(pfg_ctx* c, const MxConst& k, Counters* cnt) {
     for (int sweep = 0; sweep < max_ref && (cnt->need32 > 0 || cnt->need64 > 0); ++sweep) {
         PFG_CUDA(c, cudaMemcpyAsync(c->q_iter_prev.p, c->q.p, sizeof(double) * c->R, cudaMemcpyDeviceToDevice,
                                     c->stream));
-        if (cnt->need32 > 0 && (rc = mx_inner<float, DIM>(c, cnt))) return rc;
-        if (cnt->need64 > 0 && (rc = mx_inner<double, DIM>(c, cnt))) return rc;
+        if (c->n_inst > 1) {
+            if ((rc = mx_inner_batch<DIM>(c, cnt))) return rc;
+        } else {
+            if (cnt->need32 > 0 && (rc = mx_inner<float, DIM>(c, cnt))) return rc;
+            if (cnt->need64 > 0 && (rc = mx_inner<double, DIM>(c, cnt))) return rc;
+        }
         if ((rc = mx_residual<DIM>(c, k, RES_SWEEP, cnt))) return rc;
         if (cnt->redo > 0) {
             k_mx_rollback<DIM><<<div_up(c->N, BLOCK), BLOCK, 0, c->stream>>>(c->N, ptr<double>(c->q_iter_prev),
@@ -1008,7 +1105,8 @@ int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* 
         (rc = ensure(c, c->mx_id, sizeof(double) * c->h_mx_id.size())) ||
         (rc = ensure(c, c->mx_sc, 256 * (((size_t)n_inst * M_COUNT * sizeof(float) + 255) / 256) +
                                       sizeof(double) * (size_t)n_inst * M_COUNT)) ||
-        (rc = ensure(c, c->mx_part, sizeof(double) * 4 * (size_t)c->n_seg)))
+        (rc = ensure(c, c->mx_part, sizeof(double) * 4 * (size_t)c->n_seg)) ||
+        (rc = ensure(c, c->mx_list, sizeof(int) * 2 * (size_t)c->n_seg)))
         return rc;
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_seg.p, seg.data(), sizeof(int) * seg.size(), cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaMemcpyAsync(c->node_inst.p, node_inst.data(), sizeof(int) * (size_t)N, cudaMemcpyHostToDevice,
