@@ -40,10 +40,12 @@ constexpr int SPMV_BLOCK = 256;  // threads of the segment SpMV kernels
 // per-instance int fields
 // I_MODE: precision of the correction solves (0 FP32, 1 FP64); I_ROLL: undo the last sweep
 enum : int { I_B0 = 0, I_B1, I_N0, I_N1, I_ACTIVE, I_STATUS, I_IT, I_KIT, I_TICKET, I_MODE, I_ROLL, I_COUNT = 12 };
+// correction-solve precision of an instance
+enum : int { MODE_FP32 = 0, MODE_FP64 = 2 };
 // per-instance double fields
 enum : int { D_RHO = 0, D_MU, D_DT, D_RR, D_BB, D_RES, D_PAD0, D_PAD1, D_COUNT = 8 };
 // per-instance Krylov scalars (one FP32 and one FP64 set)
-enum : int { M_RHO = 0, M_RHO_OLD, M_ALPHA, M_OMEGA, M_RR, M_TOL2, M_DONE, M_ITERS, M_COUNT = 8 };
+enum : int { M_RHO = 0, M_RHO_OLD, M_ALPHA, M_OMEGA, M_RR, M_TOL2, M_DONE, M_ITERS, M_RR0, M_COUNT = 10 };
 // FP32 Krylov vectors
 enum : int { W_R = 0, W_RHAT, W_P, W_V, W_S, W_T, W_PHAT, W_SHAT, W_COUNT };
 // device counters
@@ -393,7 +395,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_resid(Mx m, int N, const int*
     const int inst = m.seg[3 * blk];
     int* ii = m.ii + inst * I_COUNT;
     if (!ii[I_ACTIVE]) return;
-    const bool fp64 = ii[I_MODE] != 0;
+    const bool fp64 = ii[I_MODE] == MODE_FP64;
     const int n0 = m.seg[3 * blk + 1], cnt = m.seg[3 * blk + 2] - n0;
     const int rows = cnt * (DIM + 1);
     const int lane = threadIdx.x % G;
@@ -457,25 +459,32 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_resid(Mx m, int N, const int*
     }
     const double tol = fmax(k.rtol * sqrt(bb), k.atol);
     bool need = active && rr > tol * tol;
-    if (kind == RES_SWEEP && !fp64 && need && !(rr <= 0.01 * rr_prev)) {
-        ii[I_MODE] = 1;
-        if (!(rr <= rr_prev)) {  // grew or not finite: undo the sweep, residual recomputed after
+    const int mode = ii[I_MODE];  // the mode this pass seeded for
+    if (kind == RES_SWEEP && mode == MODE_FP32 && need && !(rr <= 0.01 * rr_prev)) {
+        // an FP32 sweep that did not shrink ||r|| tenfold: FP64 from now on (and, if ||r||
+        // grew, the sweep is undone and the residual recomputed after)
+        ii[I_MODE] = MODE_FP64;
+        if (!(rr <= rr_prev)) {
             ii[I_ROLL] = 1;
             idd[D_RR] = rr_prev;
             atomicAdd(m.cnt + C_ROLLBACK, 1);
             need = false;
         }
     }
+    const int nmode = ii[I_MODE];
     float* sc = m.sc + inst * M_COUNT;
     double* sc64 = m.sc64 + inst * M_COUNT;
-    const bool need32 = need && ii[I_MODE] == 0 && !fp64;
-    const bool need64 = need && fp64;
+    // seeds written this pass are valid unless the instance just crossed into FP64
+    const bool need32 = need && nmode != MODE_FP64;
+    const bool need64 = need && nmode == MODE_FP64 && fp64;
+    const double eta = k.eta;
     sc[M_RHO] = (float)rs;
     sc[M_RHO_OLD] = 1.0f;
     sc[M_ALPHA] = 1.0f;
     sc[M_OMEGA] = 1.0f;
     sc[M_RR] = (float)rs;
-    sc[M_TOL2] = (float)(k.eta * k.eta * rs);
+    sc[M_RR0] = (float)rs;
+    sc[M_TOL2] = (float)(eta * eta * rs);
     sc[M_ITERS] = 0.0f;
     sc[M_DONE] = need32 ? 0.0f : 1.0f;
     sc64[M_RHO] = rs;
@@ -483,14 +492,15 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_resid(Mx m, int N, const int*
     sc64[M_ALPHA] = 1.0;
     sc64[M_OMEGA] = 1.0;
     sc64[M_RR] = rs;
-    sc64[M_TOL2] = k.eta * k.eta * rs;
+    sc64[M_RR0] = rs;
+    sc64[M_TOL2] = eta * eta * rs;
     sc64[M_ITERS] = 0.0;
     sc64[M_DONE] = need64 ? 0.0 : 1.0;
     if (need32) atomicAdd(m.cnt + C_NEED, 1);
     if (need64) atomicAdd(m.cnt + C_NEED64, 1);
-    // an instance just moved to FP64 mode without undo: its next sweep must start from an
-    // FP64 seed, which the host obtains by re-evaluating the residual
-    if (need && !fp64 && ii[I_MODE] == 1) atomicAdd(m.cnt + C_ROLLBACK, 1);
+    // an instance that just moved to FP64 without an undo needs an FP64 seed: the host
+    // re-evaluates the residual
+    if (need && nmode == MODE_FP64 && !fp64) atomicAdd(m.cnt + C_ROLLBACK, 1);
     if (active) atomicAdd(m.cnt + C_ACTIVE, 1);
 }
 
@@ -669,7 +679,7 @@ __global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, const int* __restrict__ li
         done = 2;
     else if (v[1] <= sc[M_TOL2])
         done = 1;
-    else if (v[0] == 0 || om == 0)
+    else if (v[0] == 0 || om == 0 || v[1] > T(1e6) * sc[M_RR0])  // breakdown or divergence
         done = 2;
     if (done != 0) {
         sc[M_DONE] = done;
@@ -1037,7 +1047,7 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
         s.krylov_iterations = r[I_KIT];
         s.residual = hd[(size_t)i * D_COUNT + D_RES];
         s.dt = dts[i];
-        s.fp64_solves = r[I_MODE];
+        s.fp64_solves = r[I_MODE] == MODE_FP64 ? 1 : 0;
     }
     return PFG_OK;
 }

@@ -97,9 +97,9 @@ __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, f
     fast_two_sum(p, e, ph, pl);
 }
 
-// State layout (floats), shared with the fused form (pfg_wc_fused.cu):
+// State layout (floats):
 //   XH[d][N] XL[d][N] | VH0 VL0 VH1 VL1 [d][N] | PH0 PL0 PH1 PL1 [N] | RD[N] | AX[d][N]
-// v and p have two halves; `cur` selects the current one (the fused kernel ping-pongs).
+// v and p have two halves; `cur` selects the current one (the step works in place on one).
 struct St {
     float *xh, *xl, *vh, *vl, *ph, *pl, *rd, *ax;
 };

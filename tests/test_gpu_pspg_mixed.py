@@ -129,9 +129,9 @@ def test_batch_rejects_cross_instance_elements(gpu_lib):
         ctx.set_instances(bad, 1000.0, 1e-3)
 
 
-def test_fp64_fallback_on_hard_instance(gpu_lib):
-    """A 25k-node instance whose FP32 correction solves stop contracting: the step still
-    converges (the solves continue in FP64) and matches the FP64 path."""
+def test_hard_instance_converges(gpu_lib):
+    """A 25k-node instance on which FP32 correction solves to 1e-3 diverge: the step still
+    converges (looser FP32 solves, FP64 if those fail too) and matches the FP64 path."""
     from pfem_gb300 import workloads as W
 
     inst = W.c4_instance(0)
@@ -149,6 +149,5 @@ def test_fp64_fallback_on_hard_instance(gpu_lib):
         res[prec] = (st, ctx.get_states())
         ctx.close()
     st_m, q_m = res[api.PREC_MIXED]
-    assert st_m.fp64_solves == 1
     assert st_m.picard_iterations == res[api.PREC_FP64][0].picard_iterations
     assert max(field_errs(q_m, res[api.PREC_FP64][1], 2, m.n_nodes)) < 1e-6
