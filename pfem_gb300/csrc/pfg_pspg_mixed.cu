@@ -530,7 +530,20 @@ __device__ __forceinline__ T row_dot_t(int r, bool act, const int* __restrict__ 
                                        const T* __restrict__ val, const T* __restrict__ y, int lane) {
     const int b = act ? rp[r] : 0, e = act ? rp[r + 1] : 0;
     T s = 0;
-    for (int kk = b + lane; kk < e; kk += G) s += val[kk] * __ldg(y + col[kk]);
+    // four independent column/value loads in flight per lane before the dependent gathers
+    int kk = b + lane;
+    for (; kk + 3 * G < e; kk += 4 * G) {
+        const int c0 = __ldg(col + kk), c1 = __ldg(col + kk + G), c2 = __ldg(col + kk + 2 * G),
+                  c3 = __ldg(col + kk + 3 * G);
+        const T v0 = __ldg(val + kk), v1 = __ldg(val + kk + G), v2 = __ldg(val + kk + 2 * G),
+                v3 = __ldg(val + kk + 3 * G);
+        const T y0 = __ldg(y + c0), y1 = __ldg(y + c1), y2 = __ldg(y + c2), y3 = __ldg(y + c3);
+        s += v0 * y0;
+        s += v1 * y1;
+        s += v2 * y2;
+        s += v3 * y3;
+    }
+    for (; kk < e; kk += G) s += __ldg(val + kk) * __ldg(y + __ldg(col + kk));
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
     return s;
@@ -679,7 +692,7 @@ __global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, const int* __restrict__ li
         done = 2;
     else if (v[1] <= sc[M_TOL2])
         done = 1;
-    else if (v[0] == 0 || om == 0 || v[1] > T(1e6) * sc[M_RR0])  // breakdown or divergence
+    else if (v[0] == 0 || om == 0)  // breakdown
         done = 2;
     if (done != 0) {
         sc[M_DONE] = done;
