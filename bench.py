@@ -385,7 +385,8 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(h_out.nbytes)},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "algorithmic_bytes": dom_bytes, "avg_launch_us": dom_us},
+                         "traffic": NCU_TRAFFIC.get(("wc-c2", args.precision, dom_name)),
+                         "algorithmic_bytes": dom_bytes, "avg_launch_us": dom_us},
             "phases_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in phases.items()},
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -448,6 +449,17 @@ def field_errors(a, b, nf, N):
 
     return [float(np.linalg.norm(a[f * N:(f + 1) * N] - b[f * N:(f + 1) * N]) /
                   max(np.linalg.norm(b[f * N:(f + 1) * N]), 1e-300)) for f in range(nf)]
+
+
+# DRAM bytes (read + write) of one launch of a kernel, from one ncu capture of the same
+# workload (profiles/wc_mixed_c2_kernels.md, profiles/pspg_c3_kernels.md; cold caches).
+NCU_TRAFFIC = {
+    ("wc-c2", "fp32", "WC momentum node"): 17.7664e6,
+    ("wc-c2", "fp32", "WC momentum element"): 6.7676e6,
+    ("wc-c2", "fp32", "WC continuity element"): 7.8026e6,
+    ("wc-c2", "fp32", "WC continuity node"): 8.1851e6,
+    ("incomp-c3", "fp32", "Krylov SpMV"): 560.4e6,
+}
 
 
 def _phase_roofline(phases, pb_spmv, pb_asm, peak):
@@ -550,6 +562,7 @@ def run_gpu_incomp(args):
     peak, peak_kind = hbm_peak()
     roof = _phase_roofline(phases, spmv_bytes(nnz, R, s), asm_bytes(d, N, E, R, nnz, s), peak)
     roof["peak_kind"] = peak_kind
+    roof["traffic"] = NCU_TRAFFIC.get((args.workload, args.precision, "Krylov SpMV"))
 
     # end to end through the C ABI with host buffers
     h_in = torch.empty(R, dtype=torch.float64, pin_memory=True).numpy()
