@@ -62,3 +62,20 @@ def test_wc_solver_remeshes_on_schedule(gpu_lib):
     m0 = masses[0][1]
     assert all(abs(mm - m0) / m0 < 0.05 for _, mm in masses)
     sol.close()
+
+
+def test_extractors_write_gmsh_and_csv(gpu_lib, tmp_path):
+    from pfem_gb300 import output as OUT
+
+    mesh = M.dam_break_2d(0.1)
+    sol = S.SolverIncompNewtonGPU(mesh, M.incomp_initial_states(mesh), remesh_params=PRM)
+    gm = OUT.GmshExtractor(str(tmp_path / "results.msh"), 2e-3, what=("p", "ke", "u", "v"))
+    mass = OUT.CsvExtractor(str(tmp_path / "mass.txt"), 1e-3, "mass")
+    tip = OUT.CsvExtractor(str(tmp_path / "tip.txt"), 1e-3, "minmax", coordinate=0, min_max="max")
+    S.Problem(sol, max_time=1.0, extractors=[gm, mass, tip]).simulate(max_steps=4)
+    assert len(gm.written) >= 2
+    rows = [list(map(float, l.split(","))) for l in open(tmp_path / "mass.txt")]
+    assert len(rows) >= 3 and all(r[1] > 0 for r in rows)
+    tips = [list(map(float, l.split(","))) for l in open(tmp_path / "tip.txt")]
+    assert all(0.9 < t[1] < 4.0 for t in tips)
+    sol.close()
