@@ -594,38 +594,78 @@ __global__ void __launch_bounds__(NB) k_mx_up_s(Mx m, const int* __restrict__ li
 
 // out = A in over the rows of the segment's nodes (all fields); dots for alpha or omega.
 // MODE 0: v = A phat, alpha = rho / (rhat . v).  MODE 1: t = A shat, omega = (t.s)/(t.t).
+// Node-row SpMV: the d+1 rows of node n share n's neighbour list, and column (m, f2) of row
+// (n, f1) sits at row_ptr(n, f1) + f2 deg(n) + rank(m); so a group of GN lanes walks n's
+// neighbours once (one index and d+1 input values per neighbour) and accumulates all d+1
+// rows, reading each matrix value once and no per-value column index.  Identity rows (free
+// nodes, bound-node velocities) hold their diagonal only.
 template <class T, int G, int DIM, int MODE>
 __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, const int* __restrict__ list, T* __restrict__ scb,
                                                         int cnt_slot, int N,
-                                                        const int* __restrict__ rp, const int* __restrict__ col,
+                                                        const int* __restrict__ rp, const int* __restrict__ nbr_ptr,
+                                                        const int* __restrict__ nbr,
                                                         const T* __restrict__ val, T* __restrict__ W, size_t ld) {
+    constexpr int B = DIM + 1;
+    constexpr int GN = DIM == 2 ? 4 : 8;  // lanes per node (mean valence ~7 / ~15)
     __shared__ double sh[32];
     const int b = list ? list[blockIdx.x] : blockIdx.x;  // segment
     const int inst = m.seg[3 * b];
     T* sc = scb + inst * M_COUNT;
     if (sc[M_DONE] != 0) return;
     const int n0 = m.seg[3 * b + 1], cnt = m.seg[3 * b + 2] - n0;
-    const int rows = cnt * (DIM + 1);
-    const int lane = threadIdx.x % G;
+    const int lane = threadIdx.x % GN;
     const T* in = W + (MODE == 0 ? W_PHAT : W_SHAT) * ld;
     T* out = W + (MODE == 0 ? W_V : W_T) * ld;
     T d0 = 0, d1 = 0;
-    for (int t0 = 0; t0 < rows; t0 += SPMV_BLOCK / G) {
-        const int t = t0 + threadIdx.x / G;
-        const bool act = t < rows;
-        int r = 0;
-        if (act) {
-            const int f = t / cnt;
-            r = f * N + n0 + (t - f * cnt);
+    for (int off = 0; off < cnt; off += SPMV_BLOCK / GN) {
+        const int ln = off + threadIdx.x / GN;
+        const bool act = ln < cnt;
+        const int n = n0 + (act ? ln : 0);
+        T y[B];
+        int rowp[B];
+        bool full[B];
+#pragma unroll
+        for (int f = 0; f < B; ++f) {
+            y[f] = 0;
+            rowp[f] = act ? rp[n + f * N] : 0;
+            full[f] = act && (rp[n + f * N + 1] - rowp[f] > 1);
         }
-        const T y = row_dot_t<T, G>(r, act, rp, col, val, in, lane);
+        const int b0 = act ? nbr_ptr[n] : 0;
+        const int deg = act ? nbr_ptr[n + 1] - b0 : 0;
+        for (int k = lane; k < deg; k += GN) {
+            const int mn = __ldg(nbr + b0 + k);
+            T xm[B];
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(in + (size_t)f2 * N + mn);
+#pragma unroll
+            for (int f1 = 0; f1 < B; ++f1) {
+                if (!full[f1]) continue;
+                T acc = 0;
+#pragma unroll
+                for (int f2 = 0; f2 < B; ++f2) acc += __ldg(val + rowp[f1] + f2 * deg + k) * xm[f2];
+                y[f1] += acc;
+            }
+        }
         if (act && lane == 0) {
-            out[r] = y;
-            if (MODE == 0) {
-                d0 += W[W_RHAT * ld + r] * y;
-            } else {
-                d0 += y * W[W_S * ld + r];
-                d1 += y * y;
+#pragma unroll
+            for (int f1 = 0; f1 < B; ++f1)
+                if (!full[f1]) y[f1] = val[rowp[f1]] * in[(size_t)f1 * N + n];
+        }
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int o = GN / 2; o > 0; o >>= 1) y[f1] += __shfl_xor_sync(0xffffffffu, y[f1], o, GN);
+        if (act && lane == 0) {
+#pragma unroll
+            for (int f1 = 0; f1 < B; ++f1) {
+                const size_t r = (size_t)f1 * N + n;
+                out[r] = y[f1];
+                if (MODE == 0) {
+                    d0 += W[W_RHAT * ld + r] * y[f1];
+                } else {
+                    d0 += y[f1] * W[W_S * ld + r];
+                    d1 += y[f1] * y[f1];
+                }
             }
         }
     }
@@ -833,6 +873,8 @@ struct KSet {
     const double* scale;
     const int* rp;
     const int* col;
+    const int* nptr;
+    const int* nbr;
     double* x;
 
     void iterate(pfg_ctx* c, int grid) const {
@@ -840,11 +882,11 @@ struct KSet {
         prof_begin(c, PH_KRYLOV_ITER);
         k_mx_up_p<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
         prof_begin(c, PH_KRYLOV_SPMV);
-        k_mx_spmv<T, G, DIM, 0><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, col, val, W, ld);
+        k_mx_spmv<T, G, DIM, 0><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr, val, W, ld);
         prof_end(c, PH_KRYLOV_SPMV);
         k_mx_up_s<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
         prof_begin(c, PH_KRYLOV_SPMV);
-        k_mx_spmv<T, G, DIM, 1><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, col, val, W, ld);
+        k_mx_spmv<T, G, DIM, 1><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr, val, W, ld);
         prof_end(c, PH_KRYLOV_SPMV);
         k_mx_up_x<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, slot, N, x, scale, W, ld);
         prof_end(c, PH_KRYLOV_ITER);
@@ -867,6 +909,8 @@ KSet<T, DIM> kset(pfg_ctx* c, const int* list) {
     k.scale = F32 ? ptr<double>(c->mx_scale) : nullptr;
     k.rp = ptr<int>(c->row_ptr);
     k.col = ptr<int>(c->col);
+    k.nptr = ptr<int>(c->nbr_ptr);
+    k.nbr = ptr<int>(c->nbr);
     k.x = ptr<double>(c->q);
     return k;
 }
