@@ -103,6 +103,11 @@ typedef struct pfg_params {
     /* mixed precision, incompressible: */
     double inner_rel_tol;      /* FP32 correction solve stops at this fraction of its
                                   starting residual (0 = 1e-3)                             */
+    /* both kinds: */
+    double gamma;              /* surface tension coefficient (MomContEq / MomEq "gamma");
+                                  >= 1e-15 adds the facet term of m_applyBCPSPG
+                                  (MomContEquationPSPG.inl:155-187) / MomEq::m_applyBC
+                                  (MomEquation.inl:311-335) and needs pfg_upload_facets    */
 } pfg_params;
 
 typedef struct pfg_step_status {
@@ -139,6 +144,14 @@ PFG_API const char* pfg_last_error(const pfg_ctx* ctx);   /* never NULL */
 PFG_API int pfg_upload_mesh(pfg_ctx* ctx, int32_t n_nodes, const double* pos, const uint8_t* flags,
                             int32_t n_elems, const int32_t* conn);
 
+/* The boundary facets of the uploaded mesh (Mesh::m_facetsList, built by the alpha shape in
+ * Mesh2D.cpp:199-244 / Mesh3D.cpp:232-282): facets[k*F + f] (k < dim) are the nodes of facet
+ * f and facet_elm[f] the element it belongs to (Facet::m_elementIndex).  Needed, after every
+ * pfg_upload_mesh, when params.gamma >= 1e-15: the surface tension term is evaluated on the
+ * facets that touch the free surface (PFG_NODE_FREE_SURFACE).  Every facet node must be a node
+ * of its element. */
+PFG_API int pfg_upload_facets(pfg_ctx* ctx, int32_t n_facets, const int32_t* facets, const int32_t* facet_elm);
+
 /* Node states, field-major.  Incompressible: (dim+1)*N values [v_0..v_{d-1}, p]
  * (getQFromNodesStates / setNodesStatesfromQ, StatesFromToQ.hpp:9-34).
  * WC: (2*dim+2)*N values [v, p, rho, a] (WCompNewton/Problem.cpp:18). */
@@ -162,15 +175,15 @@ PFG_API int pfg_set_dirichlet(pfg_ctx* ctx, int32_t n, const int32_t* nodes, con
  * on the same FP64 residual test as the plain form. */
 PFG_API int pfg_picard_step(pfg_ctx* ctx, double dt, pfg_step_status* status);
 
-/* Batches (mixed precision, incompressible): the uploaded mesh is the union of n_inst
- * independent meshes stored back to back, instance i owning nodes
- * [node_offsets[i], node_offsets[i+1]) and only elements among them.  rho[i], mu[i] are the
- * instance's fluid parameters.  No reference counterpart: the reference runs one Problem per
- * process; this replaces n_inst independent SolverIncompNewton objects. */
 /* Device memory currently held by the context, in bytes (for admission control by callers
  * that run several contexts under one HBM budget). */
 PFG_API int pfg_device_bytes(const pfg_ctx* ctx, size_t* bytes);
 
+/* Batches (mixed precision, incompressible): the uploaded mesh is the union of n_inst
+ * independent meshes stored back to back, instance i owning nodes
+ * [node_offsets[i], node_offsets[i+1]) and only elements among them.  rho[i], mu[i] are the
+ * instance's fluid parameters (gamma is shared).  No reference counterpart: the reference runs
+ * one Problem per process; this replaces n_inst independent SolverIncompNewton objects. */
 PFG_API int pfg_set_instances(pfg_ctx* ctx, int32_t n_inst, const int32_t* node_offsets, const double* rho,
                               const double* mu);
 /* One Picard time step of every instance at once (instance i with time step dt[i]); each

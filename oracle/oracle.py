@@ -44,12 +44,14 @@ def build(force=False):
 
 
 class PspgParams(C.Structure):
-    _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double), ("g", C.c_double * 3)]
+    _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double), ("g", C.c_double * 3),
+                ("gamma", C.c_double)]
 
 
 class WcParams(C.Structure):
     _fields_ = [("K0", C.c_double), ("K0p", C.c_double), ("rhoStar", C.c_double), ("mu", C.c_double),
-                ("g", C.c_double * 3), ("meduri", C.c_int), ("sc", C.c_double), ("maxDT", C.c_double)]
+                ("g", C.c_double * 3), ("meduri", C.c_int), ("sc", C.c_double), ("maxDT", C.c_double),
+                ("gamma", C.c_double)]
 
 
 _lib = None
@@ -64,6 +66,9 @@ def lib():
         L.orc_create.restype = vp
         L.orc_create.argtypes = [C.c_int, C.c_int, dp, u8p, C.c_int, ip]
         L.orc_destroy.argtypes = [vp]
+        L.orc_set_facets.restype = C.c_int
+        L.orc_set_facets.argtypes = [vp, C.c_int, ip, ip]
+        L.orc_surface_tension.argtypes = [vp, C.c_double, C.c_int, dp]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_num_threads.argtypes = [C.c_int]
         for name in ("orc_get_positions", "orc_set_positions", "orc_update_positions_from_save",
@@ -119,6 +124,21 @@ class OracleMesh:
                                   self._flags.ctypes.data_as(C.POINTER(C.c_uint8)), self.E, _ip(self._conn))
         if not self.h:
             raise ValueError("oracle: invalid mesh")
+        facets = getattr(mesh, "facets", None)
+        if facets is not None and facets.shape[1]:
+            self.set_facets(facets, mesh.facet_elm)
+
+    def set_facets(self, facets, facet_elm):
+        self._facets = np.ascontiguousarray(facets, dtype=np.int32)
+        self._facet_elm = np.ascontiguousarray(facet_elm, dtype=np.int32)
+        if lib().orc_set_facets(self.h, self._facet_elm.size, _ip(self._facets), _ip(self._facet_elm)):
+            raise ValueError("oracle: invalid facets")
+
+    def surface_tension(self, gamma, any_node=True):
+        """Surface tension forces alone (dim, N) at the current positions."""
+        out = np.empty((self.dim, self.N))
+        lib().orc_surface_tension(self.h, float(gamma), int(any_node), _dp(out))
+        return out
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
@@ -164,9 +184,9 @@ class OracleMesh:
         return lib().orc_tip(self.h, coord, int(want_max))
 
 
-def pspg_params(rho, mu, dt, g):
+def pspg_params(rho, mu, dt, g, gamma=0.0):
     p = PspgParams()
-    p.rho, p.mu, p.dt = rho, mu, dt
+    p.rho, p.mu, p.dt, p.gamma = rho, mu, dt, gamma
     for i, x in enumerate(g):
         p.g[i] = x
     return p
@@ -183,14 +203,14 @@ def pspg_element(om, e, rho, mu, dt, g, q_iter, q_prev):
     return Ae, be
 
 
-def pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc=None, apply_bc=True):
+def pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc=None, apply_bc=True, gamma=0.0):
     """A (scipy CSC, Eigen's storage order) and b of m_buildAbPSPG (+ m_applyBCPSPG)."""
     import scipy.sparse as sp
 
     R = (om.dim + 1) * om.N
     if vbc is None:
         vbc = np.zeros(om.dim * om.N)
-    p = pspg_params(rho, mu, dt, g)
+    p = pspg_params(rho, mu, dt, g, gamma)
     q_iter = np.ascontiguousarray(q_iter, float)
     q_prev = np.ascontiguousarray(q_prev, float)
     vbc = np.ascontiguousarray(vbc, float)
@@ -216,7 +236,7 @@ def _tick(times, key, t0):
 
 
 def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=None, max_iter=10,
-                     min_res=1e-6, times=None):
+                     min_res=1e-6, times=None, gamma=0.0):
     """One `MomContEqIncompNewton::solve` with PSPG (Picard, residual "Ax_f").
 
     Mutates the oracle mesh positions.  Returns (q, PicardResult); on failure the positions
@@ -233,7 +253,7 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
     om.save()
     _tick(times, "Save/restore nodelist", t0)
     t0 = time.perf_counter()
-    A, b = pspg_assemble(om, rho, mu, dt, g, q_prev, q_prev, vbc)
+    A, b = pspg_assemble(om, rho, mu, dt, g, q_prev, q_prev, vbc, gamma=gamma)
     _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
     q_iter = np.zeros_like(q_prev)
     r = float("inf")
@@ -260,7 +280,7 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
         om.update_from_save(q_iter * dt)
         _tick(times, "Update solutions", t0)
         t0 = time.perf_counter()
-        A, b = pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc)
+        A, b = pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc, gamma=gamma)
         _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
         # residual closure, "Ax_f" (:366-371)
         t0 = time.perf_counter()
@@ -277,7 +297,8 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
     return q_iter, res
 
 
-def wc_params(K0=2.2e7, K0p=7.0, rho_star=1000.0, mu=1e-3, g=(0.0, -9.81), meduri=True, sc=0.3, max_dt=1e-3):
+def wc_params(K0=2.2e7, K0p=7.0, rho_star=1000.0, mu=1e-3, g=(0.0, -9.81), meduri=True, sc=0.3, max_dt=1e-3,
+              gamma=0.0):
     p = WcParams()
     p.K0, p.K0p, p.rhoStar, p.mu = K0, K0p, rho_star, mu
     gg = tuple(g) + (0.0,) * (3 - len(g))
@@ -286,6 +307,7 @@ def wc_params(K0=2.2e7, K0p=7.0, rho_star=1000.0, mu=1e-3, g=(0.0, -9.81), medur
     p.meduri = int(meduri)
     p.sc = sc
     p.maxDT = max_dt
+    p.gamma = gamma
     return p
 
 

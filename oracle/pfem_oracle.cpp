@@ -115,6 +115,7 @@ struct ElemGeom {
 struct PspgParams {
     double rho, mu, dt;
     double g[3];
+    double gamma;      // surface tension coefficient (MomContEq "gamma")
 };
 
 struct WcParams {
@@ -123,6 +124,7 @@ struct WcParams {
     int meduri;        // ContEq stabilization "Meduri" (1) or "None" (0)
     double sc;         // securityCoeff
     double maxDT;
+    double gamma;      // surface tension coefficient (MomEq "gamma")
 };
 
 }  // namespace
@@ -135,6 +137,10 @@ struct OrcMesh {
     std::vector<int32_t> conn;
     std::vector<ElemGeom> geom;
     GaussTable gt;
+    // facets of the alpha shape (Mesh::m_facetsList): dim nodes each (facets[k*F + f]) and the
+    // element each belongs to (Facet::m_elementIndex)
+    int F = 0;
+    std::vector<int32_t> facets, facetElm;
     // assembled PSPG system, Eigen column-major (CSC) storage
     std::vector<int32_t> colptr, rowidx;
     std::vector<double> vals, b;
@@ -357,6 +363,128 @@ Mat ddevWC(int dim) {  // WCompNewton/MomEquation.inl:63-83
     return D;
 }
 
+// ---------------------------------------------------------------------------------------
+// Surface tension on the facets
+// ---------------------------------------------------------------------------------------
+// Facet::computeJ / computeDetJ (srcs/mesh/Facet.cpp:15-77) and Facet::computeNormal
+// (:130-210).  The normal's orientation (flipped away from the out node) is not restated:
+// only n n^T enters the surface tension term.
+void facetGeometry(const OrcMesh& m, int f, double& detJ, double n[3]) {
+    const int a = m.facets[f], b = m.facets[(size_t)m.F + f];
+    n[0] = n[1] = n[2] = 0;
+    if (m.dim == 2) {
+        const double J00 = (m.x(b, 0) - m.x(a, 0)) / 2, J10 = (m.x(b, 1) - m.x(a, 1)) / 2;
+        detJ = std::sqrt(J00 * J00 + J10 * J10);
+        n[0] = m.x(b, 1) - m.x(a, 1);
+        n[1] = m.x(a, 0) - m.x(b, 0);
+        const double norm = std::sqrt(n[0] * n[0] + n[1] * n[1]);
+        n[0] /= norm;
+        n[1] /= norm;
+    } else {
+        const int c = m.facets[2 * (size_t)m.F + f];
+        double u[3], w[3];
+        for (int d = 0; d < 3; ++d) {
+            u[d] = m.x(b, d) - m.x(a, d);
+            w[d] = m.x(c, d) - m.x(a, d);
+        }
+        const double g0 = u[1] * w[2] - w[1] * u[2], g1 = u[2] * w[0] - w[2] * u[0], g2 = u[0] * w[1] - w[0] * u[1];
+        detJ = std::sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+        n[0] = u[1] * w[2] - u[2] * w[1];
+        n[1] = u[2] * w[0] - u[0] * w[2];
+        n[2] = u[0] * w[1] - u[1] * w[0];
+        const double norm = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int d = 0; d < 3; ++d) n[d] /= norm;
+    }
+}
+
+// MatrixBuilder::getP, MatricesBuilder.inl:166-190: the tangential projector I - n n^T in
+// Voigt order (2D: 11, 22, 12; 3D: 11, 22, 33, 12, 13, 23).
+Mat getP(int dim, const double n[3]) {
+    if (dim == 2) {
+        Mat P(3, 1);
+        P(0, 0) = 1 - n[0] * n[0];
+        P(1, 0) = 1 - n[1] * n[1];
+        P(2, 0) = -n[0] * n[1];
+        return P;
+    }
+    Mat P(6, 1);
+    P(0, 0) = 1 - n[0] * n[0];
+    P(1, 0) = 1 - n[1] * n[1];
+    P(2, 0) = 1 - n[2] * n[2];
+    P(3, 0) = -n[0] * n[1];
+    P(4, 0) = -n[0] * n[2];
+    P(5, 0) = -n[1] * n[2];
+    return P;
+}
+
+// MatrixBuilder::getT, MatricesBuilder.inl:192-214 (entry by entry).
+Mat getT(int dim, const Mat& Pm) {
+    auto P = [&](int i) { return Pm(i, 0); };
+    if (dim == 2) {
+        Mat T(3, 3);
+        T(0, 0) = P(0) * P(0); T(0, 1) = P(2) * P(2); T(0, 2) = 2 * P(0) * P(2);
+        T(1, 0) = T(0, 1);     T(1, 1) = P(1) * P(1); T(1, 2) = 2 * P(2) * P(1);
+        T(2, 0) = P(0) * P(2); T(2, 1) = P(2) * P(1); T(2, 2) = P(0) * P(1) + P(2) * P(2);
+        return T;
+    }
+    Mat T(6, 6);
+    T(0, 0) = P(0) * P(0); T(0, 1) = P(3) * P(3); T(0, 2) = P(4) * P(4);
+    T(0, 3) = 2 * P(0) * P(3); T(0, 5) = 2 * P(4) * P(3); T(0, 4) = 2 * P(0) * P(4);
+    T(1, 0) = T(0, 1); T(1, 1) = P(1) * P(1); T(1, 2) = P(5) * P(5);
+    T(1, 3) = 2 * P(3) * P(1); T(1, 5) = 2 * P(5) * P(1); T(1, 4) = 2 * P(3) * P(5);
+    T(2, 0) = T(0, 2); T(2, 1) = T(1, 2); T(2, 2) = P(2) * P(2);
+    T(2, 3) = 2 * P(5) * P(4); T(2, 5) = 2 * P(5) * P(2); T(2, 4) = 2 * P(2) * P(4);
+    T(3, 0) = P(0) * P(3); T(3, 1) = P(3) * P(1); T(3, 2) = P(4) * P(5);
+    T(3, 3) = P(0) * P(1) + P(3) * P(3); T(3, 5) = P(4) * P(1) + P(5) * P(3); T(3, 4) = P(4) * P(3) + P(0) * P(5);
+    T(5, 0) = P(3) * P(4); T(5, 1) = P(5) * P(1); T(5, 2) = P(5) * P(2);
+    T(5, 3) = P(4) * P(1) + P(5) * P(3); T(5, 5) = P(1) * P(2) + P(5) * P(5); T(5, 4) = P(5) * P(4) + P(3) * P(2);
+    T(4, 0) = P(0) * P(4); T(4, 1) = P(3) * P(5); T(4, 2) = P(2) * P(4);
+    T(4, 3) = P(4) * P(3) + P(0) * P(5); T(4, 5) = P(5) * P(4) + P(3) * P(2); T(4, 4) = P(2) * P(0) + P(4) * P(4);
+    return T;
+}
+
+// MatrixBuilder::getFST, MatricesBuilder.inl:388-402, with the constant factor gamma of
+// setFSTcomputeFactor (IncompNewton/MomContEquation.inl:208-213, WCompNewton/MomEquation.inl:
+// 141-146).  Three facet Gauss points (nGPLD = 3, MomContEquation.inl:17,22), weights of
+// Mesh::getGaussWeight (Mesh.cpp:416-450), reference sizes of Mesh::getRefElementSize
+// (Mesh.cpp:472-484).  FST[i + d*npe] is the force on velocity component d of element node i.
+void getFST(const OrcMesh& m, int f, double gamma, double* FST) {
+    const int dim = m.dim, npe = m.npe;
+    const double w2[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0}, w3[3] = {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0};
+    const double* w = dim == 2 ? w2 : w3;
+    const double refLD = dim == 2 ? 2.0 : 0.5;
+    const ElemGeom& geo = m.geom[m.facetElm[f]];
+    Mat B = getB(dim, getGradN(dim, geo));
+    double detJ, n[3];
+    facetGeometry(m, f, detJ, n);
+    Mat P = getP(dim, n);
+    Mat T = getT(dim, P);
+    Mat BtTP = mul(mul(transpose(B), T), P);
+    for (int r = 0; r < dim * npe; ++r) FST[r] = 0;
+    for (int g = 0; g < 3; ++g)
+        for (int r = 0; r < dim * npe; ++r) FST[r] -= gamma * BtTP(r, 0) * w[g];
+    for (int r = 0; r < dim * npe; ++r) FST[r] *= detJ * refLD;
+}
+
+// The facet loops of m_applyBCPSPG (MomContEquationPSPG.inl:155-187; a facet counts when any
+// of its nodes is on the free surface) and MomEqWCompNewton::m_applyBC (MomEquation.inl:
+// 311-335; Facet::isOnFreeSurface, Facet.cpp:249-255: all of its nodes), adding each facet's
+// FST to the velocity rows target[node + d*N] in facet order.
+void addSurfaceTension(const OrcMesh& m, double gamma, bool anyNode, double* target) {
+    if (gamma < 1e-15) return;
+    const int dim = m.dim, npe = m.npe, N = m.N;
+    double FST[12];
+    for (int f = 0; f < m.F; ++f) {
+        int cnt = 0;
+        for (int k = 0; k < dim; ++k) cnt += (m.flags[m.facets[(size_t)k * m.F + f]] & FREE_SURFACE) ? 1 : 0;
+        if (anyNode ? cnt == 0 : cnt < dim) continue;
+        getFST(m, f, gamma, FST);
+        const int e = m.facetElm[f];
+        for (int i = 0; i < npe; ++i)
+            for (int d = 0; d < dim; ++d) target[m.node(e, i) + (size_t)d * N] += FST[i + d * npe];
+    }
+}
+
 // MomContEqIncompNewton::m_computeTauPSPG, MomContEquationPSPG.inl:237-259
 double computeTau(const OrcMesh& m, int e, const ElemGeom& geo, const PspgParams& p, const double* q) {
     const double h = std::sqrt(m.gt.refSize * geo.detJ / M_PI);
@@ -466,6 +594,33 @@ OrcMesh* orc_create(int dim, int N, const double* pos, const uint8_t* flags, int
 
 void orc_destroy(OrcMesh* m) { delete m; }
 
+// The facet list the alpha shape leaves behind (Mesh2D.cpp:199-244, Mesh3D.cpp:232-282):
+// facets[k*F + f] (k < dim) and the element of each facet.  Returns 0, or -1 on bad input.
+int orc_set_facets(OrcMesh* m, int F, const int32_t* facets, const int32_t* facetElm) {
+    if (F < 0) return -1;
+    for (int f = 0; f < F; ++f) {
+        const int e = facetElm[f];
+        if (e < 0 || e >= m->E) return -1;
+        for (int k = 0; k < m->dim; ++k) {
+            const int v = facets[(size_t)k * F + f];
+            bool in = false;
+            for (int i = 0; i < m->npe; ++i) in |= m->node(e, i) == v;
+            if (!in) return -1;
+        }
+    }
+    m->F = F;
+    m->facets.assign(facets, facets + (size_t)m->dim * F);
+    m->facetElm.assign(facetElm, facetElm + F);
+    return 0;
+}
+
+// The surface tension forces alone (dim x N, field-major), with the PSPG facet rule
+// (any_node != 0) or the WC one, at the current positions.
+void orc_surface_tension(const OrcMesh* m, double gamma, int any_node, double* out) {
+    std::fill(out, out + (size_t)m->dim * m->N, 0.0);
+    addSurfaceTension(*m, gamma, any_node != 0, out);
+}
+
 int orc_num_threads() {
 #ifdef _OPENMP
     return omp_get_max_threads();
@@ -543,7 +698,7 @@ void orc_pspg_element(const OrcMesh* m, int e, const PspgParams* p, const double
 }
 
 // m_buildAbPSPG (MomContEquationPSPG.inl:6-146) followed, when apply_bc != 0, by
-// m_applyBCPSPG (:148-235, gamma = 0 so no surface tension).  vbc holds the Dirichlet
+// m_applyBCPSPG (:148-235; surface tension when p->gamma >= 1e-15).  vbc holds the Dirichlet
 // velocity of every node (dim x N field-major; read only at Dirichlet nodes), standing in
 // for the Lua BoundaryV(pos, t + dt) call.  Returns nnz of the compressed matrix.
 int orc_pspg_assemble(OrcMesh* m, const PspgParams* p, const double* qIter, const double* qPrev, const double* vbc,
@@ -624,6 +779,8 @@ int orc_pspg_assemble(OrcMesh* m, const PspgParams* p, const double* qIter, cons
     for (const auto& d : indexb) m->b[d.first] += d.second;
 
     if (apply_bc) {
+        // m_applyBCPSPG facet loop (:155-187)
+        addSurfaceTension(*m, p->gamma, true, m->b.data());
         // m_applyBCPSPG node loop (:189-232)
         for (int n = 0; n < N; ++n) {
             if (m->isFree[n]) {
@@ -770,7 +927,8 @@ void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const doub
                 F[n + (size_t)d * N] += FT[(size_t)e * dim * npe + i + d * npe];
             }
     for (size_t k = 0; k < invMv.size(); ++k) invMv[k] = 1 / invMv[k];
-    // m_applyBC (:305-374), gamma = 0
+    // m_applyBC (:305-374): facet loop (:311-335), then the node loop
+    addSurfaceTension(*m, p->gamma, false, F.data());
     for (int n = 0; n < N; ++n) {
         if (m->isFree[n] && !m->bound(n)) {
             for (int d = 0; d < dim; ++d) {

@@ -35,6 +35,7 @@ EXPORTED = (
     "pfg_get_csr", "pfg_get_geometry", "pfg_linear_solve", "pfg_version", "pfg_set_profiling",
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
+    "pfg_upload_facets",
 )
 NUM_PHASES = 13
 
@@ -50,6 +51,7 @@ class Params(C.Structure):
         ("max_dt", C.c_double), ("meduri", C.c_int32), ("pad1", C.c_int32),
         ("hbm_budget_bytes", C.c_size_t),
         ("inner_rel_tol", C.c_double),
+        ("gamma", C.c_double),
     ]
 
 
@@ -82,6 +84,7 @@ def load(path=LIB_PATH):
         "pfg_destroy": ([vp], C.c_int),
         "pfg_last_error": ([vp], C.c_char_p),
         "pfg_upload_mesh": ([vp, C.c_int32, dp, u8p, C.c_int32, ip], C.c_int),
+        "pfg_upload_facets": ([vp, C.c_int32, ip, ip], C.c_int),
         "pfg_set_states": ([vp, dp], C.c_int),
         "pfg_get_states": ([vp, dp], C.c_int),
         "pfg_get_positions": ([vp, dp], C.c_int),
@@ -177,6 +180,16 @@ class Context:
                                            conn.shape[1], conn.ctypes.data_as(C.POINTER(C.c_int32))),
                     "pfg_upload_mesh")
         self.N, self.E = pos.shape[1], conn.shape[1]
+        facets = getattr(mesh, "facets", None)
+        if facets is not None and facets.shape[1]:
+            self.upload_facets(facets, mesh.facet_elm)
+
+    def upload_facets(self, facets, facet_elm):
+        """The mesh's boundary facets (dim x F nodes) and the element of each."""
+        facets = np.ascontiguousarray(facets, np.int32)
+        facet_elm = np.ascontiguousarray(facet_elm, np.int32)
+        self._check(self.L.pfg_upload_facets(self.h, facet_elm.size, _ip(facets), _ip(facet_elm)),
+                    "pfg_upload_facets")
 
     def set_states(self, s):
         s = np.ascontiguousarray(s, np.float64)

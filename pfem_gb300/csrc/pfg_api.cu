@@ -172,6 +172,13 @@ int check_ctx(pfg_ctx* c) {
     return PFG_OK;
 }
 
+// Surface tension needs the facets of the current mesh.
+int check_facets(pfg_ctx* c) {
+    if (c->prm.gamma >= 1e-15 && !c->has_facets)
+        return fail(c, PFG_ERR_STATE, "gamma > 0: call pfg_upload_facets after pfg_upload_mesh");
+    return PFG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -288,7 +295,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->vbc, &c->kv, &c->kv32, &c->binv, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
                     &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot, &c->binv32, &c->node_inst,
                     &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt, &c->mx_scale,
-                    &c->mx_list};
+                    &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force};
     wc_release_graphs(c);
     mx_release_graph(c);
     for (DBuf* b : bufs) release(*b);
@@ -330,6 +337,10 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
         (rc = ensure(c, c->vbc, sizeof(double) * dim * N)))
         return rc;
     c->h_flags.assign(flags, flags + N);
+    c->h_conn.assign(conn, conn + (size_t)npe * E);
+    c->has_facets = false;
+    c->F = 0;
+    c->n_fst_nodes = 0;
     PFG_CUDA(c, cudaMemcpyAsync(c->pos.p, pos, sizeof(double) * dim * N, cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaMemcpyAsync(c->pos_save.p, pos, sizeof(double) * dim * N, cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaMemcpyAsync(c->flags.p, flags, N, cudaMemcpyHostToDevice, c->stream));
@@ -344,6 +355,71 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
     }
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     c->has_mesh = true;
+    return PFG_OK;
+}
+
+PFG_API int pfg_upload_facets(pfg_ctx* c, int32_t n_facets, const int32_t* facets, const int32_t* facet_elm) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (n_facets < 0 || n_facets >= (1 << 29) || (n_facets > 0 && (!facets || !facet_elm)))
+        return fail(c, PFG_ERR_INVALID, "pfg_upload_facets: invalid count or null pointers");
+    const int dim = c->dim, npe = c->npe, N = c->N, E = c->E, F = n_facets;
+    // the facet rule of the kind: any node on the free surface (m_applyBCPSPG,
+    // MomContEquationPSPG.inl:163-174) or all of them (Facet::isOnFreeSurface, Facet.cpp:249-255)
+    const bool any_node = c->prm.kind == PFG_KIND_INCOMP_PSPG;
+    std::vector<uint8_t> use(F, 0);
+    std::vector<int> cnt((size_t)N + 1, 0);
+    for (int f = 0; f < F; ++f) {
+        const int e = facet_elm[f];
+        if (e < 0 || e >= E) return fail(c, PFG_ERR_INVALID, "facet %d: element %d out of range", f, e);
+        int on_fs = 0;
+        for (int k = 0; k < dim; ++k) {
+            const int v = facets[(size_t)k * F + f];
+            bool in = false;
+            for (int i = 0; i < npe; ++i) in |= c->h_conn[(size_t)i * E + e] == v;
+            if (!in) return fail(c, PFG_ERR_INVALID, "facet %d: node %d is not a node of element %d", f, v, e);
+            on_fs += (c->h_flags[v] & F_FREE_SURFACE) ? 1 : 0;
+        }
+        use[f] = any_node ? on_fs > 0 : on_fs == dim;
+        if (use[f])
+            for (int i = 0; i < npe; ++i) cnt[c->h_conn[(size_t)i * E + e]]++;
+    }
+    // listed nodes (ascending) with their entries in ascending facet order (the order the
+    // reference adds them)
+    std::vector<int> nodes, nf_ptr(1, 0), slot((size_t)N, -1);
+    for (int n = 0; n < N; ++n)
+        if (cnt[n]) {
+            slot[n] = nf_ptr.back();
+            nodes.push_back(n);
+            nf_ptr.push_back(nf_ptr.back() + cnt[n]);
+        }
+    std::vector<int> nf_ent(std::max(nf_ptr.back(), 1));
+    for (int f = 0; f < F; ++f)
+        if (use[f])
+            for (int i = 0; i < npe; ++i) nf_ent[slot[c->h_conn[(size_t)i * E + facet_elm[f]]]++] = f * 4 + i;
+    const size_t nf = std::max<size_t>((size_t)F, 1), nn = std::max<size_t>(nodes.size(), 1);
+    if ((rc = ensure(c, c->fc_nodes, sizeof(int) * dim * nf)) || (rc = ensure(c, c->fc_elem, sizeof(int) * nf)) ||
+        (rc = ensure(c, c->nf_nodes, sizeof(int) * nn)) || (rc = ensure(c, c->nf_ptr, sizeof(int) * (nn + 1))) ||
+        (rc = ensure(c, c->nf_ent, sizeof(int) * nf_ent.size())) ||
+        (rc = ensure(c, c->fst_force, sizeof(double) * dim * (size_t)N)))
+        return rc;
+    if (F) {
+        PFG_CUDA(c, cudaMemcpyAsync(c->fc_nodes.p, facets, sizeof(int) * dim * (size_t)F, cudaMemcpyHostToDevice, c->stream));
+        PFG_CUDA(c, cudaMemcpyAsync(c->fc_elem.p, facet_elm, sizeof(int) * (size_t)F, cudaMemcpyHostToDevice, c->stream));
+    }
+    if (!nodes.empty())
+        PFG_CUDA(c, cudaMemcpyAsync(c->nf_nodes.p, nodes.data(), sizeof(int) * nodes.size(), cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->nf_ptr.p, nf_ptr.data(), sizeof(int) * nf_ptr.size(), cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->nf_ent.p, nf_ent.data(), sizeof(int) * nf_ent.size(), cudaMemcpyHostToDevice, c->stream));
+    // nodes outside the list keep a zero force
+    PFG_CUDA(c, cudaMemsetAsync(c->fst_force.p, 0, sizeof(double) * dim * (size_t)N, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->F = F;
+    c->n_fst_nodes = (int)nodes.size();
+    c->has_facets = true;
+    // captured WC step graphs hold the previous facet arguments
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT) wc_release_graphs(c);
     return PFG_OK;
 }
 
@@ -427,6 +503,7 @@ PFG_API int pfg_picard_step(pfg_ctx* c, double dt, pfg_step_status* st) {
     if (rc) return rc;
     if (c->prm.kind != PFG_KIND_INCOMP_PSPG) return fail(c, PFG_ERR_STATE, "context is not incompressible");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if ((rc = check_facets(c))) return rc;
     if (!(dt > 0) || !st) return fail(c, PFG_ERR_INVALID, "pfg_picard_step: dt must be > 0 and status non-null");
     if (c->prm.precision == PFG_PREC_MIXED) {
         if (c->n_inst != 1) return fail(c, PFG_ERR_STATE, "context holds %d instances: use pfg_picard_step_batch", c->n_inst);
@@ -479,6 +556,7 @@ PFG_API int pfg_picard_step_batch(pfg_ctx* c, const double* dt, pfg_step_status*
     if (c->prm.kind != PFG_KIND_INCOMP_PSPG || c->prm.precision != PFG_PREC_MIXED)
         return fail(c, PFG_ERR_STATE, "batched steps need an incompressible context in mixed precision");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if ((rc = check_facets(c))) return rc;
     if (!dt || !st) return fail(c, PFG_ERR_INVALID, "pfg_picard_step_batch: null arguments");
     for (int i = 0; i < c->n_inst; ++i)
         if (!(dt[i] > 0)) return fail(c, PFG_ERR_INVALID, "instance %d: dt must be > 0", i);
@@ -490,6 +568,7 @@ PFG_API int pfg_wc_step(pfg_ctx* c, double dt, int32_t nsteps, pfg_step_status* 
     if (rc) return rc;
     if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if ((rc = check_facets(c))) return rc;
     if (nsteps < 0 || !st) return fail(c, PFG_ERR_INVALID, "pfg_wc_step: bad arguments");
     return wc_steps(c, dt, nsteps, st);
 }
@@ -499,6 +578,7 @@ PFG_API int pfg_wc_step_async(pfg_ctx* c, double dt, int32_t nsteps) {
     if (rc) return rc;
     if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if ((rc = check_facets(c))) return rc;
     if (nsteps < 0) return fail(c, PFG_ERR_INVALID, "pfg_wc_step_async: nsteps < 0");
     return wc_enqueue(c, dt, nsteps);
 }
@@ -568,6 +648,7 @@ PFG_API int pfg_pspg_assemble(pfg_ctx* c, double dt, const double* q_iter, const
     if (rc) return rc;
     if (c->prm.kind != PFG_KIND_INCOMP_PSPG) return fail(c, PFG_ERR_STATE, "context is not incompressible");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if ((rc = check_facets(c))) return rc;
     if (!(dt > 0)) return fail(c, PFG_ERR_INVALID, "dt must be > 0");
     double* kv = ptr<double>(c->kv);
     const size_t R = c->R;

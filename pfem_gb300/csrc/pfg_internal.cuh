@@ -114,6 +114,14 @@ struct pfg_ctx {
     cudaGraphExec_t mx_graph[2] = {nullptr, nullptr};  // one chunk of BiCGSTAB iterations [FP32, FP64]
     std::vector<int> h_mx_ii;
     std::vector<double> h_mx_id;
+    // surface tension: facets (dim x F nodes, element of each), the nodes their elements touch
+    // with each one's (facet, local node of the facet's element) entries, and the force array
+    // (dim x N, FP64 or FP32 by the kind's precision)
+    pfg::DBuf fc_nodes, fc_elem, nf_nodes, nf_ptr, nf_ent, fst_force;
+    int F = 0;
+    int n_fst_nodes = 0;
+    bool has_facets = false;
+    std::vector<int32_t> h_conn;
 };
 
 namespace pfg {

@@ -104,12 +104,12 @@ __global__ void k_pspg_rhs(int N, int E, const int* __restrict__ ne_ptr, const i
                            const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
                            const double* __restrict__ ed, const uint8_t* __restrict__ flags,
                            const double* __restrict__ q_prev, const double* __restrict__ vbc,
-                           double* __restrict__ rhs, int apply_bc, PspgConst k) {
+                           double* __restrict__ rhs, int apply_bc, PspgConst k, const double* __restrict__ fst) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     double bv[DIM], bp;
-    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, apply_bc != 0, k.c, k.t, bv,
-                       bp);
+    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, apply_bc != 0, k.c, k.t, fst,
+                       bv, bp);
 #pragma unroll
     for (int f = 0; f < DIM; ++f) rhs[(size_t)f * N + n] = bv[f];
     rhs[(size_t)DIM * N + n] = bp;
@@ -213,10 +213,14 @@ int assemble_dim(pfg_ctx* c, double dt, const double* d_qiter, const double* d_q
     }
     const PspgConst k = make_const(c, dt);
     prof_begin(c, PH_PSPG_RHS);
+    const FstArgs fa = fst_args(c);
+    if (fa.nodes && apply_bc)
+        k_fst<DIM, double><<<div_up(fa.n_nodes, BLOCK), BLOCK, 0, c->stream>>>(
+            fa, E, ptr<int>(c->conn), PosF64{ptr<double>(c->pos), N}, N, ptr<double>(c->fst_force));
     k_pspg_rhs<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
         N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
         ptr<double>(c->edata), ptr<uint8_t>(c->flags), d_qprev, ptr<double>(c->vbc), ptr<double>(c->rhs),
-        apply_bc ? 1 : 0, k);
+        apply_bc ? 1 : 0, k, fst_force<double>(c));
     prof_end(c, PH_PSPG_RHS);
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "pfg_device.cuh"
+#include "pfg_fst.cuh"
 
 namespace pfg {
 
@@ -92,14 +93,16 @@ __device__ __forceinline__ void pspg_pair_block(int n, int m, int E, const int* 
 }
 
 // Right-hand side of node n (doublet scatter :93-97,:140-144 in element order) followed by
-// the node boundary conditions of m_applyBCPSPG (:189-232).
+// m_applyBCPSPG: the surface tension of the node's free-surface facets (:155-187, facet
+// order) and the node boundary conditions (:189-232).
 template <int DIM>
 __device__ __forceinline__ void pspg_node_rhs(int n, int N, int E, const int* __restrict__ ne_ptr,
                                               const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
                                               const int* __restrict__ conn, const double* __restrict__ ed,
                                               uint8_t fl, const double* __restrict__ q_prev,
                                               const double* __restrict__ vbc, bool apply_bc, const PspgCoef& k,
-                                              const PspgTables& t, double (&bv)[DIM], double& bp) {
+                                              const PspgTables& t, const double* __restrict__ fst,
+                                              double (&bv)[DIM], double& bp) {
     constexpr int NPE = DIM + 1;
 #pragma unroll
     for (int f = 0; f < DIM; ++f) bv[f] = 0;
@@ -143,6 +146,9 @@ __device__ __forceinline__ void pspg_node_rhs(int n, int N, int E, const int* __
         bp += H + (tau * inv_dt) * cv;
     }
     if (apply_bc) {
+        if (fst)
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) bv[f] += fst[(size_t)f * N + n];
         if (fl & F_FREE) {
             bp = 0;
             if (!(fl & F_BOUND))

@@ -186,14 +186,14 @@ __global__ void k_mx_rhs(int N, int E, const int* __restrict__ ne_ptr, const int
                          const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
                          const double* __restrict__ ed, const uint8_t* __restrict__ flags,
                          const double* __restrict__ q_prev, const double* __restrict__ vbc, Mx m, MxConst k,
-                         double* __restrict__ rhs) {
+                         double* __restrict__ rhs, const double* __restrict__ fst) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     const int inst = m.node_inst[n];
     if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
     const PspgCoef cf = inst_coef_d(m.id + inst * D_COUNT, k.sumw, k.refSize);
     double bv[DIM], bp;
-    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, true, cf, k.t, bv, bp);
+    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, true, cf, k.t, fst, bv, bp);
 #pragma unroll
     for (int f = 0; f < DIM; ++f) rhs[(size_t)f * N + n] = bv[f];
     rhs[(size_t)DIM * N + n] = bp;
@@ -818,10 +818,14 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
         PFG_CHECK_LAUNCH(c);
     }
     prof_begin(c, PH_PSPG_RHS);
+    const FstArgs fa = fst_args(c);
+    if (fa.nodes)
+        k_fst<DIM, double><<<div_up(fa.n_nodes, BLOCK), BLOCK, 0, c->stream>>>(
+            fa, E, ptr<int>(c->conn), PosF64{ptr<double>(c->pos), N}, N, ptr<double>(c->fst_force));
     k_mx_rhs<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
         N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
         ptr<double>(c->edata), ptr<uint8_t>(c->flags), ptr<double>(c->q_prev), ptr<double>(c->vbc), m, k,
-        ptr<double>(c->rhs));
+        ptr<double>(c->rhs), fst_force<double>(c));
     prof_end(c, PH_PSPG_RHS);
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);

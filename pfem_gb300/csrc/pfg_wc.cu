@@ -30,6 +30,7 @@
 #include <cstring>
 
 #include "pfg_device.cuh"
+#include "pfg_fst.cuh"
 #include "pfg_internal.cuh"
 
 namespace pfg {
@@ -319,14 +320,15 @@ __global__ void __launch_bounds__(BLOCK) k_wc_mom_elem(int E, int N, const int* 
     }
 }
 
-// a = F / M with the momentum BCs (MomEquation.inl:341-372); v = v1/2 + dt/2 a.  Also the
-// per-node quantities of computeNextDT: max(u^2, c^2) and mu/rho.
+// a = F / M with the surface tension of the node's free-surface facets (MomEquation.inl:
+// 311-335) and the momentum BCs (:341-372); v = v1/2 + dt/2 a.  Also the per-node quantities
+// of computeNextDT: max(u^2, c^2) and mu/rho.
 template <int DIM, class R>
 __global__ void k_wc_mom_node(int N, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
                               const uint8_t* __restrict__ ne_loc, const uint8_t* __restrict__ flags,
                               const R* __restrict__ elr, const double* __restrict__ eld,
                               const double* __restrict__ vbc, const double* __restrict__ tdt, WcConst k,
-                              double* __restrict__ s, R* __restrict__ nodal) {
+                              double* __restrict__ s, R* __restrict__ nodal, const double* __restrict__ fst) {
     using L = ElLayout<DIM>;
     constexpr int NPE = DIM + 1;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -349,6 +351,9 @@ __global__ void k_wc_mom_node(int N, const int* __restrict__ ne_ptr, const int* 
     const double pS = s[(size_t)DIM * N + n] * k.S;
 #pragma unroll
     for (int f = 0; f < DIM; ++f) F[f] += pS * W[f];
+    if (fst)
+#pragma unroll
+        for (int f = 0; f < DIM; ++f) F[f] += fst[(size_t)f * N + n];
     double inv = 1 / m;
     const uint8_t fl = flags[n];
     if ((fl & F_FREE) && !(fl & F_BOUND)) {  // free fall (MomEquation.inl:347-354)
@@ -523,9 +528,14 @@ int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
         prof_end(c, PH_WC_MOM_ELEM);
     }
     prof_begin(c, PH_WC_MOM_NODE);
+    const FstArgs fa = fst_args(c);
+    if (fa.nodes)
+        k_fst<DIM, double><<<div_up(fa.n_nodes, BLOCK), BLOCK, 0, c->stream>>>(
+            fa, E, ptr<int>(c->conn), PosF64{ptr<double>(c->pos), N}, N, ptr<double>(c->fst_force));
     k_wc_mom_node<DIM, R><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
                                                        ptr<uint8_t>(c->ne_loc), ptr<uint8_t>(c->flags), elr, eld,
-                                                       ptr<double>(c->vbc), tdt, k, s, adapt ? nodal : nullptr);
+                                                       ptr<double>(c->vbc), tdt, k, s, adapt ? nodal : nullptr,
+                                                       fst_force<double>(c));
     prof_end(c, PH_WC_MOM_NODE);
     if (adapt && E > 0) {
         const int grid = std::min(c->max_grid, ge);

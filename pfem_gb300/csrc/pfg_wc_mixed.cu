@@ -22,6 +22,7 @@
 #include <cstring>
 
 #include "pfg_device.cuh"
+#include "pfg_fst.cuh"
 #include "pfg_internal.cuh"
 
 namespace pfg {
@@ -117,6 +118,16 @@ __host__ __device__ inline St state_ptrs(float* base, int dim, int N, int cur) {
     return s;
 }
 inline size_t state_floats(int dim, int N) { return (size_t)(7 * dim + 5) * N; }
+
+// Coordinate differences of double-float positions in FP32 (hi - hi is exact for nearby nodes).
+struct PosDF {
+    const float *xh, *xl;
+    int N;
+    __device__ __forceinline__ float operator()(int a, int b, int d) const {
+        const size_t ia = (size_t)d * N + a, ib = (size_t)d * N + b;
+        return (xh[ia] - xh[ib]) + (xl[ia] - xl[ib]);
+    }
+};
 
 // Element -> node exchange, incidence-major: the contribution of element e to its local node i
 // goes to record q = inc_slot[e*(dim+1)+i], the position of (e, i) in node-major incidence
@@ -445,8 +456,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
     }
 }
 
-// Momentum node kernel (MomEquation.inl:201-226,279-374): sums the node's records, applies the
-// BCs, updates acceleration and velocity.  With `partials`, also the CFL time step of the next
+// Momentum node kernel (MomEquation.inl:201-226,279-374): sums the node's records, adds the
+// surface tension of its free-surface facets (in FP32), applies the BCs, updates acceleration
+// and velocity.  With `partials`, also the CFL time step of the next
 // step (computeNextDT, WCompNewton/Solver.cpp:192-234): the reference's minimum over elements
 // of sc^2 h_e^2 / max_{nodes of e} max(|u|^2, c^2, 4 alpha^2 / h_e^2) equals the minimum over
 // nodes of the same expression at the node's smallest incident h_e (it grows with h_e), and in
@@ -455,7 +467,8 @@ template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_mom_node(int N, const int* __restrict__ ne_ptr,
                                                       const uint8_t* __restrict__ flags, const float* __restrict__ cb,
                                                       const double* __restrict__ vbc, double* __restrict__ tdt,
-                                                      WcmConst k, St st, float* __restrict__ partials) {
+                                                      WcmConst k, St st, float* __restrict__ partials,
+                                                      const float* __restrict__ fst) {
     using L = Rec<DIM>;
     __shared__ float sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -489,6 +502,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_node(int N, const int* __restri
         const float pS = st.ph[n] * k.S * k.refSize;
 #pragma unroll
         for (int f = 0; f < DIM; ++f) F[f] += pS * (Wh[f] + Wl[f]);
+        if (fst)
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) F[f] += fst[(size_t)f * N + n];
         float inv = 1.0f / m;
         const uint8_t fl = flags[n];
         if ((fl & F_FREE) && !(fl & F_BOUND)) {
@@ -715,8 +731,12 @@ int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
         prof_end(c, PH_WC_MOM_ELEM);
     }
     prof_begin(c, PH_WC_MOM_NODE);
+    const FstArgs fa = fst_args(c);
+    if (fa.nodes)
+        k_fst<DIM, float><<<div_up(fa.n_nodes, BLOCK), BLOCK, 0, c->stream>>>(
+            fa, E, ptr<int>(c->conn), PosDF{st.xh, st.xl, N}, N, ptr<float>(c->fst_force));
     k_m_mom_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), flags, cb, vbcf, tdt, k, st,
-                                                   adapt && E > 0 ? partials : nullptr);
+                                                   adapt && E > 0 ? partials : nullptr, fst_force<float>(c));
     prof_end(c, PH_WC_MOM_NODE);
     PFG_CHECK_LAUNCH(c);
     return PFG_OK;

@@ -53,6 +53,13 @@ class Context {
         check(pfg_upload_mesh(ctx_, n, pos.data(), flags.data(), e, conn.data()), "pfg_upload_mesh");
         nodes_ = n;
     }
+    // boundary facets (dim x F nodes) and the element of each; needed after every uploadMesh
+    // when params.gamma > 0 (surface tension)
+    void uploadFacets(const std::vector<int32_t>& facets, const std::vector<int32_t>& facetElm) {
+        if (facets.size() != (size_t)dim() * facetElm.size())
+            throw std::runtime_error("uploadFacets: facets must be dim x F");
+        check(pfg_upload_facets(ctx_, (int32_t)facetElm.size(), facets.data(), facetElm.data()), "pfg_upload_facets");
+    }
     int nodes() const { return nodes_; }
     int statesPerNode() const {
         return params_.kind == PFG_KIND_INCOMP_PSPG ? params_.dim + 1 : 2 * params_.dim + 2;

@@ -272,6 +272,51 @@ def dam_break_3d(h=0.01, alpha=1.2, seed=20261203, column=(0.5, 0.5, 1.0), tank=
     return alpha_shape(pos, flags, h, alpha, delete_flying_nodes=True)
 
 
+def square_nodes_2d(h, side=1.0, jitter=0.1, seed=20261203):
+    """A free square of fluid, no walls: the lattice h * (i, j), 0 <= i, j <= side / h, with the
+    interior nodes jittered like the dam-break column (the boundary stays straight).
+
+    Stands in for the reference's surface tension case `examples/2D/squareToDisk` (unit
+    square, gmsh size 0.025, no boundary conditions; the .msh is not shipped).
+    Returns (pos (2,N), flags (N,))."""
+    n = int(round(side / h))
+    gx, gy = np.meshgrid(side * np.arange(n + 1) / n, side * np.arange(n + 1) / n, indexing="ij")
+    pos = np.stack([gx.ravel(), gy.ravel()])
+    inner = (gx.ravel() > 0) & (gx.ravel() < side) & (gy.ravel() > 0) & (gy.ravel() < side)
+    rng = np.random.default_rng(seed)
+    pos[:, inner] += rng.uniform(-jitter * h, jitter * h, size=(2, int(inner.sum())))
+    return pos.copy(), np.zeros(pos.shape[1], np.uint8)
+
+
+def square_to_disk_2d(h=0.025, alpha=1.2, seed=20261203):
+    pos, flags = square_nodes_2d(h, seed=seed)
+    return alpha_shape(pos, flags, h, alpha)
+
+
+def ball_nodes_3d(R, h):
+    """A free ball of fluid, no walls: the centre plus shells of radius R k / n (n = R / h)
+    with Fibonacci-sphere points at spacing ~h (a 3D surface tension case).
+    Returns (pos (3,N), flags (N,))."""
+    pts = [np.zeros((1, 3))]
+    nr = int(round(R / h))
+    ga = np.pi * (3 - np.sqrt(5))
+    for k in range(1, nr + 1):
+        r = R * k / nr
+        m = max(12, int(round(4.4 * np.pi * r * r / (h * h))))
+        i = np.arange(m) + 0.5
+        z = 1 - 2 * i / m
+        rr = np.sqrt(1 - z * z)
+        th = ga * i + 0.7 * k
+        pts.append(r * np.stack([rr * np.cos(th), rr * np.sin(th), z], 1))
+    pos = np.concatenate(pts).T.copy()
+    return pos, np.zeros(pos.shape[1], np.uint8)
+
+
+def ball_3d(R=0.1, h=0.02, alpha=1.3):
+    pos, flags = ball_nodes_3d(R, h)
+    return alpha_shape(pos, flags, h, alpha)
+
+
 def incomp_initial_states(mesh, rho=1000.0, g=9.81, column=(1.0, 2.0)):
     """Hydrostatic column at rest (`damBreakKoshizukaIncomp.lua:73-81` with the column's
     width and height): q = [v (d fields), p], field-major, length (d+1)*N."""

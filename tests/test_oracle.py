@@ -129,3 +129,54 @@ def test_volume_and_tip(c1_mesh):
     om = O.OracleMesh(c1_mesh)
     assert om.volume() == pytest.approx(2.0, rel=2e-2)
     assert 0.95 < om.tip() < 1.06
+
+
+def _disk(R=0.1, h=0.01):
+    pts = [np.zeros((1, 2))]
+    nr = int(round(R / h))
+    for k in range(1, nr + 1):
+        r = R * k / nr
+        m = max(6, int(round(2 * np.pi * r / h)))
+        a = 0.37 * k + 2 * np.pi * np.arange(m) / m
+        pts.append(r * np.stack([np.cos(a), np.sin(a)], 1))
+    pos = np.concatenate(pts).T.copy()
+    return M.alpha_shape(pos, np.zeros(pos.shape[1], np.uint8), h, 1.2)
+
+
+def test_surface_tension_forces_are_translation_free():
+    """sum_i dN_i/dx = 0 in every element, so each facet's forces sum to zero; every force
+    sits on a node of a free-surface facet's element."""
+    for mesh in (M.square_to_disk_2d(0.05), M.ball_3d(0.1, 0.025)):
+        om = O.OracleMesh(mesh)
+        st = om.surface_tension(1.9)
+        assert np.abs(st).max() > 1e-3
+        assert np.abs(st.sum(axis=1)).max() < 1e-12 * np.abs(st).max()
+        touched = np.zeros(mesh.n_nodes, bool)
+        touched[mesh.conn[:, mesh.facet_elm].ravel()] = True
+        assert np.all(st[:, ~touched] == 0.0)
+        assert np.array_equal(om.surface_tension(0.0), np.zeros_like(st))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_laplace_pressure_of_a_drop(dim):
+    """A drop at rest with no gravity: one PSPG step gives the Laplace pressure jump inside
+    (gamma / R in 2D, 2 gamma / R in 3D) and no motion."""
+    mesh = _disk() if dim == 2 else M.ball_3d(0.1, 0.02)
+    gamma, R = 0.0728, 0.1
+    N = mesh.n_nodes
+    fs = (mesh.flags & M.FREE_SURFACE) != 0
+    om = O.OracleMesh(mesh)
+    q, res = O.pspg_picard_step(om, np.zeros((dim + 1) * N), 1e-3, g=(0.0,) * dim, gamma=gamma)
+    assert res.converged
+    p = q[dim * N:]
+    expect = (dim - 1) * gamma / R
+    assert abs(p[~fs].mean() / expect - 1) < (5e-3 if dim == 2 else 2e-2)
+    assert np.abs(q[:dim * N]).max() < (1e-9 if dim == 2 else 1e-3)
+
+
+def test_invalid_facets_rejected(c1_mesh):
+    om = O.OracleMesh(c1_mesh)
+    bad = c1_mesh.facet_elm.copy()
+    bad[0] = c1_mesh.n_elems
+    with pytest.raises(ValueError):
+        om.set_facets(c1_mesh.facets, bad)
