@@ -71,6 +71,12 @@ typedef enum {
 } pfg_linsolve;
 
 typedef enum {
+    PFG_PC_BLOCK_JACOBI = 0,   /* node-block Jacobi                                         */
+    PFG_PC_MULTIGRID = 1       /* node-aggregation multigrid V-cycle (mixed precision only;
+                                  the FP64 form uses node-block Jacobi)                     */
+} pfg_preconditioner;
+
+typedef enum {
     PFG_RES_AX_F = 0,          /* ||A q - b||_2            MomContEquationPSPG.inl:366-371 */
     PFG_RES_U = 1,             /* relative velocity change                        :319-342 */
     PFG_RES_U_P = 2            /* max(rel. velocity change, rel. pressure change) :343-364 */
@@ -108,6 +114,9 @@ typedef struct pfg_params {
                                   >= 1e-15 adds the facet term of m_applyBCPSPG
                                   (MomContEquationPSPG.inl:155-187) / MomEq::m_applyBC
                                   (MomEquation.inl:311-335) and needs pfg_upload_facets    */
+    /* mixed precision, incompressible: */
+    int32_t preconditioner;    /* pfg_preconditioner of the FP32 correction solves         */
+    int32_t pad2;
 } pfg_params;
 
 typedef struct pfg_step_status {
@@ -259,8 +268,10 @@ PFG_API int pfg_linear_solve(pfg_ctx* ctx, double* x, int32_t* iterations, doubl
  *   3 WC momentum/element   4 WC momentum/node        5 WC time step
  *   6 PSPG element prep     7 PSPG right-hand side    8 PSPG matrix (node pairs)
  *   9 Krylov iteration     10 Picard residual        11 position update
- *  12 Krylov SpMV (the two products of an iteration, also inside phase 9)          */
-#define PFG_NUM_PHASES 13
+ *  12 Krylov SpMV (the two products of an iteration, also inside phase 9)
+ *  13 Multigrid cycle (the preconditioner applies of an iteration, also inside phase 9)
+ *  14 Multigrid setup (coarse values and block inverses after each assembly)        */
+#define PFG_NUM_PHASES 15
 PFG_API int pfg_set_profiling(pfg_ctx* ctx, int32_t enable);
 /* Accumulated milliseconds and launch counts per phase since the last reset. */
 PFG_API int pfg_get_phase_times(pfg_ctx* ctx, double* ms, int64_t* launches);

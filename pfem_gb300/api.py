@@ -23,6 +23,8 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 LINSOLVE_BICGSTAB = 0
 LINSOLVE_LU = 1
+PC_BLOCK_JACOBI = 0
+PC_MULTIGRID = 1
 RES_AX_F = 0
 
 NODE_BOUND, NODE_FREE_SURFACE, NODE_FIXED, NODE_DIRICHLET, NODE_FREE = 1, 2, 4, 8, 16
@@ -37,7 +39,7 @@ EXPORTED = (
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
     "pfg_upload_facets",
 )
-NUM_PHASES = 13
+NUM_PHASES = 15
 
 
 class Params(C.Structure):
@@ -52,6 +54,7 @@ class Params(C.Structure):
         ("hbm_budget_bytes", C.c_size_t),
         ("inner_rel_tol", C.c_double),
         ("gamma", C.c_double),
+        ("preconditioner", C.c_int32), ("pad2", C.c_int32),
     ]
 
 

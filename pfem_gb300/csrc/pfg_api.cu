@@ -189,7 +189,7 @@ PFG_API const char* pfg_phase_name(int32_t phase) {
     static const char* names[PFG_NUM_PHASES] = {
         "WC predict", "WC continuity element", "WC continuity node", "WC momentum element", "WC momentum node",
         "WC time step", "PSPG element prep", "PSPG right-hand side", "PSPG matrix", "Krylov iteration",
-        "Picard residual", "Position update", "Krylov SpMV"};
+        "Picard residual", "Position update", "Krylov SpMV", "Multigrid cycle", "Multigrid setup"};
     return (phase >= 0 && phase < PFG_NUM_PHASES) ? names[phase] : "";
 }
 
@@ -242,6 +242,7 @@ PFG_API int pfg_default_params(int32_t kind, int32_t dim, pfg_params* p) {
     p->krylov_abs_tol = 1e-10;
     p->refine_max_iter = 30;
     p->inner_rel_tol = 1e-3;
+    p->preconditioner = PFG_PC_MULTIGRID;
     p->K0 = 2.2e7;
     p->K0p = 7.0;
     p->rho_star = 1000.0;
@@ -295,8 +296,10 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->vbc, &c->kv, &c->kv32, &c->binv, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
                     &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot, &c->binv32, &c->node_inst,
                     &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt, &c->mx_scale,
-                    &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force};
+                    &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force,
+                    &c->mg_x0, &c->mg_r0};
     wc_release_graphs(c);
+    mg_release(c);
     mx_release_graph(c);
     for (DBuf* b : bufs) release(*b);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);

@@ -47,6 +47,18 @@ struct DBuf {
 
 struct Reducer;  // fwd
 
+// One coarse level of the node-aggregation multigrid (pfg_mg.cu): block CSR with (d+1)^2
+// FP32 blocks and node-major (d+1)-vectors.
+struct MgLevel {
+    int n = 0, nnzb = 0;
+    DBuf agg;              // finer-level node -> aggregate (this level's node), -1 = none
+    DBuf mem_ptr, mem;     // members of each aggregate, ascending
+    DBuf bptr, bcol, bdiag;
+    DBuf gptr, glist;      // Galerkin gather list of each block (finer-level block ids)
+    DBuf val, binv;        // blocks, diagonal-block inverses
+    DBuf x, xb, b, r;      // cycle vectors
+};
+
 }  // namespace pfg
 
 struct pfg_ctx {
@@ -122,6 +134,11 @@ struct pfg_ctx {
     int n_fst_nodes = 0;
     bool has_facets = false;
     std::vector<int32_t> h_conn;
+    // multigrid preconditioner of the mixed correction solves: coarse levels (n_mg in use) and
+    // the level-0 cycle vectors
+    std::vector<pfg::MgLevel> mg;
+    int n_mg = 0;
+    pfg::DBuf mg_x0, mg_r0;
 };
 
 namespace pfg {
@@ -159,7 +176,9 @@ enum Phase : int {
     PH_KRYLOV_ITER,
     PH_RESIDUAL,
     PH_POSITIONS,
-    PH_KRYLOV_SPMV
+    PH_KRYLOV_SPMV,
+    PH_MG_CYCLE,
+    PH_MG_SETUP
 };
 void prof_begin(pfg_ctx* c, int phase);
 void prof_end(pfg_ctx* c, int phase);
@@ -197,6 +216,12 @@ int mx_alloc(pfg_ctx* c);
 int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* rho, const double* mu);
 int mx_picard_step(pfg_ctx* c, const double* dts, pfg_step_status* st);
 void mx_release_graph(pfg_ctx* c);
+
+// ---- multigrid preconditioner (pfg_mg.cu) ---------------------------------------------
+int mg_setup(pfg_ctx* c);
+int mg_numeric(pfg_ctx* c);
+void mg_apply(pfg_ctx* c, const float* b, float* out);
+void mg_release(pfg_ctx* c);
 
 // ---- WC (pfg_wc.cu) -------------------------------------------------------------------
 int wc_alloc(pfg_ctx* c);

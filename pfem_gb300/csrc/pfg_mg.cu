@@ -1,0 +1,665 @@
+// Node-aggregation multigrid: the preconditioner of the FP32 correction solves of the mixed
+// incompressible form.
+//
+// The reference solves each Picard system with a sparse LU (MomContEquation.hpp:11).  On the
+// GPU the solve is Krylov, and with the node-block Jacobi preconditioner its iteration count
+// grows with the mesh (the pressure block is a discrete Laplacian): hundreds of iterations on
+// 3D meshes, thousands on fine 2D columns.  One V-cycle of this multigrid replaces the block
+// Jacobi apply and makes the count nearly mesh independent.
+//
+// Hierarchy (built on the host once per mesh upload, from the node adjacency only):
+//   * level 0 is the assembled system (field-major CSR, FP32 scaled values S A S);
+//   * each coarser level aggregates the nodes of the finer one: greedy, in node order, a node
+//     whose neighbours are all unaggregated starts an aggregate with them; every node left
+//     joins the aggregate of its first aggregated neighbour.  Nodes without neighbours (free
+//     nodes) take no part: only the smoother acts on them.  Aggregates follow the adjacency,
+//     so they never join two instances of a batch;
+//   * prolongation is piecewise constant per aggregate and per field (P = aggregate indicator
+//     (x) I_{d+1}), so the Galerkin operator P^T A P sums the (d+1)^2 blocks of the fine node
+//     pairs (i, j) into the block of (agg i, agg j): a fixed gather list per coarse block,
+//     summed in ascending fine-block order (deterministic, no atomics);
+//   * coarsening stops when a level is block diagonal (every connected component, i.e. every
+//     instance, is one aggregate): its block inverse is the exact coarse solve.
+// Coarse levels are stored as block CSR with node-major (d+1)-vectors.
+//
+// Cycle: V(1,1) with damped node-block Jacobi (omega = 0.7 in 2D, 0.5 in 3D) on every level; the block
+// inverses are computed in FP64 from the FP32 blocks (the PSPG block's Schur complement cancels
+// heavily) and stored in FP32.  The values are refreshed after every assembly (one gather pass
+// over the FP32 matrix plus the coarse levels).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "pfg_device.cuh"
+#include "pfg_internal.cuh"
+
+namespace pfg {
+
+namespace {
+
+// Damping of the block-Jacobi smoother, by block size (d+1): the 3D blocks need more damping
+// (at 0.6 the smoother already amplifies some modes of a 3D PSPG system).
+__host__ __device__ constexpr float mg_omega(int B) { return B == 3 ? 0.7f : 0.5f; }
+
+// ---- level 0 (field-major CSR) ---------------------------------------------------------------
+
+// y = (A x) over the d+1 rows of node n, by GN lanes walking n's neighbour list (all lanes hold
+// the result).  Column (m, f2) of row (n, f1) sits at rp(n, f1) + f2 deg(n) + rank(m); identity
+// rows hold their diagonal only.
+template <int DIM, int GN>
+__device__ __forceinline__ void row0_product(int n, bool act, int N, const int* __restrict__ rp,
+                                             const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                                             const float* __restrict__ val, const float* __restrict__ x, int lane,
+                                             float (&y)[DIM + 1]) {
+    constexpr int B = DIM + 1;
+    int rowp[B];
+    bool full[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        y[f] = 0;
+        rowp[f] = act ? rp[n + f * N] : 0;
+        full[f] = act && (rp[n + f * N + 1] - rowp[f] > 1);
+    }
+    const int b0 = act ? nbr_ptr[n] : 0;
+    const int deg = act ? nbr_ptr[n + 1] - b0 : 0;
+    for (int k = lane; k < deg; k += GN) {
+        const int mn = __ldg(nbr + b0 + k);
+        float xm[B];
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(x + (size_t)f2 * N + mn);
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1) {
+            if (!full[f1]) continue;
+            float acc = 0;
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) acc += __ldg(val + rowp[f1] + f2 * deg + k) * xm[f2];
+            y[f1] += acc;
+        }
+    }
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+#pragma unroll
+        for (int o = GN / 2; o > 0; o >>= 1) y[f1] += __shfl_xor_sync(0xffffffffu, y[f1], o, GN);
+        if (act && !full[f1]) y[f1] = val[rowp[f1]] * x[(size_t)f1 * N + n];
+    }
+}
+
+// x = omega Binv b (pre-smoothing from a zero guess); x = Binv b, the exact solve, for a node
+// without neighbours
+template <int DIM>
+__global__ void k_mg0_smooth0(int N, const int* __restrict__ nbr_ptr, const float* __restrict__ binv,
+                              const float* __restrict__ b, float* __restrict__ x) {
+    constexpr int B = DIM + 1;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const float w = nbr_ptr[n + 1] - nbr_ptr[n] == 1 ? 1.0f : mg_omega(DIM + 1);
+    float v[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) v[f] = b[(size_t)f * N + n];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        float s = 0;
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) s += binv[(size_t)(f1 * B + f2) * N + n] * v[f2];
+        x[(size_t)f1 * N + n] = w * s;
+    }
+}
+
+// POST = 0: r = b - A x.  POST = 1: out = x + omega Binv (b - A x), or out = x for a node
+// without neighbours (already solved exactly).
+template <int DIM, int POST>
+__global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict__ rp, const int* __restrict__ nbr_ptr,
+                                                   const int* __restrict__ nbr, const float* __restrict__ val,
+                                                   const float* __restrict__ binv, const float* __restrict__ b,
+                                                   const float* __restrict__ x, float* __restrict__ out) {
+    constexpr int B = DIM + 1;
+    constexpr int GN = DIM == 2 ? 4 : 8;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = t / GN, lane = t % GN;
+    const bool act = n < N;
+    float y[B];
+    row0_product<DIM, GN>(act ? n : 0, act, N, rp, nbr_ptr, nbr, val, x, lane, y);
+    if (!act || lane != 0) return;
+    float r[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) r[f] = b[(size_t)f * N + n] - y[f];
+    if (POST == 0) {
+#pragma unroll
+        for (int f = 0; f < B; ++f) out[(size_t)f * N + n] = r[f];
+    } else if (nbr_ptr[n + 1] - nbr_ptr[n] == 1) {
+#pragma unroll
+        for (int f = 0; f < B; ++f) out[(size_t)f * N + n] = x[(size_t)f * N + n];
+    } else {
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1) {
+            float s = 0;
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) s += binv[(size_t)(f1 * B + f2) * N + n] * r[f2];
+            out[(size_t)f1 * N + n] = x[(size_t)f1 * N + n] + mg_omega(B) * s;
+        }
+    }
+}
+
+// bc[I] = sum over the members n of aggregate I of r[n] (level 0: field-major r)
+template <int DIM>
+__global__ void k_mg0_restrict(int nc, const int* __restrict__ mem_ptr, const int* __restrict__ mem, int N,
+                               const float* __restrict__ r, float* __restrict__ bc) {
+    constexpr int B = DIM + 1;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= nc) return;
+    float s[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) s[f] = 0;
+    for (int q = mem_ptr[I]; q < mem_ptr[I + 1]; ++q) {
+        const int n = mem[q];
+#pragma unroll
+        for (int f = 0; f < B; ++f) s[f] += r[(size_t)f * N + n];
+    }
+#pragma unroll
+    for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
+}
+
+// x[n] += xc[agg n] (level 0: field-major x)
+template <int DIM>
+__global__ void k_mg0_prolong(int N, const int* __restrict__ agg, const float* __restrict__ xc,
+                              float* __restrict__ x) {
+    constexpr int B = DIM + 1;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const int I = agg[n];
+    if (I < 0) return;
+#pragma unroll
+    for (int f = 0; f < B; ++f) x[(size_t)f * N + n] += xc[(size_t)I * B + f];
+}
+
+// ---- coarse levels (block CSR, node-major vectors) --------------------------------------------
+
+// x = omega Binv b; x = Binv b for a block row without off-diagonal blocks
+template <int B>
+__global__ void k_mgb_smooth0(int n, const int* __restrict__ bptr, const float* __restrict__ binv,
+                              const float* __restrict__ b, float* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float w = bptr[i + 1] - bptr[i] == 1 ? 1.0f : mg_omega(B);
+    float v[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) v[f] = b[(size_t)i * B + f];
+    const float* bi = binv + (size_t)i * B * B;
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        float s = 0;
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) s += bi[f1 * B + f2] * v[f2];
+        x[(size_t)i * B + f1] = w * s;
+    }
+}
+
+// POST = 0: r = b - A x.  POST = 1: out = x + omega Binv (b - A x), or out = x for a block row
+// without off-diagonal blocks (solved exactly).  GN lanes per block row.
+template <int B, int GN, int POST>
+__global__ void __launch_bounds__(256) k_mgb_resid(int n, const int* __restrict__ bptr, const int* __restrict__ bcol,
+                                                   const float* __restrict__ val, const float* __restrict__ binv,
+                                                   const float* __restrict__ b, const float* __restrict__ x,
+                                                   float* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / GN, lane = t % GN;
+    const bool act = i < n;
+    float y[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) y[f] = 0;
+    const int k0 = act ? bptr[i] : 0, k1 = act ? bptr[i + 1] : 0;
+    for (int k = k0 + lane; k < k1; k += GN) {
+        const int j = __ldg(bcol + k);
+        float xj[B];
+#pragma unroll
+        for (int f = 0; f < B; ++f) xj[f] = __ldg(x + (size_t)j * B + f);
+        const float* a = val + (size_t)k * B * B;
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) y[f1] += __ldg(a + f1 * B + f2) * xj[f2];
+    }
+#pragma unroll
+    for (int f = 0; f < B; ++f)
+#pragma unroll
+        for (int o = GN / 2; o > 0; o >>= 1) y[f] += __shfl_xor_sync(0xffffffffu, y[f], o, GN);
+    if (!act || lane != 0) return;
+    float r[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) r[f] = b[(size_t)i * B + f] - y[f];
+    if (POST == 0) {
+#pragma unroll
+        for (int f = 0; f < B; ++f) out[(size_t)i * B + f] = r[f];
+    } else if (k1 - k0 == 1) {
+#pragma unroll
+        for (int f = 0; f < B; ++f) out[(size_t)i * B + f] = x[(size_t)i * B + f];
+    } else {
+        const float* bi = binv + (size_t)i * B * B;
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1) {
+            float s = 0;
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) s += bi[f1 * B + f2] * r[f2];
+            out[(size_t)i * B + f1] = x[(size_t)i * B + f1] + mg_omega(B) * s;
+        }
+    }
+}
+
+template <int B>
+__global__ void k_mgb_restrict(int nc, const int* __restrict__ mem_ptr, const int* __restrict__ mem,
+                               const float* __restrict__ r, float* __restrict__ bc) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= nc) return;
+    float s[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) s[f] = 0;
+    for (int q = mem_ptr[I]; q < mem_ptr[I + 1]; ++q) {
+        const int i = mem[q];
+#pragma unroll
+        for (int f = 0; f < B; ++f) s[f] += r[(size_t)i * B + f];
+    }
+#pragma unroll
+    for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
+}
+
+template <int B>
+__global__ void k_mgb_prolong(int n, const int* __restrict__ agg, const float* __restrict__ xc,
+                              float* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int I = agg[i];
+    if (I < 0) return;
+#pragma unroll
+    for (int f = 0; f < B; ++f) x[(size_t)i * B + f] += xc[(size_t)I * B + f];
+}
+
+// ---- numeric setup ------------------------------------------------------------------------------
+
+// Level-1 blocks from the level-0 matrix: thread (k, f1, f2) sums entry (f1, f2) of the fine
+// node-pair blocks in coarse block k's list.
+template <int DIM>
+__global__ void k_mg_galerkin0(int nnzb, const int* __restrict__ gptr, const int* __restrict__ glist,
+                               const int* __restrict__ pair_node, const int* __restrict__ nbr_ptr,
+                               const int* __restrict__ nbr, const int* __restrict__ rp, int N,
+                               const float* __restrict__ val, float* __restrict__ cval) {
+    constexpr int B = DIM + 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nnzb * B * B) return;
+    const int k = (int)(t / (B * B)), e = (int)(t % (B * B));
+    const int f1 = e / B, f2 = e % B;
+    float s = 0;
+    for (int q = gptr[k]; q < gptr[k + 1]; ++q) {
+        const int p = glist[q];
+        const int i = pair_node[p];
+        const int b0 = nbr_ptr[i];
+        const int deg = nbr_ptr[i + 1] - b0, rank = p - b0;
+        const int r = i + f1 * N;
+        const int rp0 = rp[r];
+        if (rp[r + 1] - rp0 > 1)
+            s += val[rp0 + f2 * deg + rank];
+        else if (f1 == f2 && nbr[p] == i)
+            s += val[rp0];
+    }
+    cval[t] = s;
+}
+
+template <int B>
+__global__ void k_mg_galerkin(int nnzb, const int* __restrict__ gptr, const int* __restrict__ glist,
+                              const float* __restrict__ fval, float* __restrict__ cval) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nnzb * B * B) return;
+    const int k = (int)(t / (B * B)), e = (int)(t % (B * B));
+    float s = 0;
+    for (int q = gptr[k]; q < gptr[k + 1]; ++q) s += fval[(size_t)glist[q] * B * B + e];
+    cval[t] = s;
+}
+
+// Inverse of each diagonal block, Gauss-Jordan with partial pivoting in FP64, stored in FP32.
+// A singular block falls back to the inverse of its diagonal.
+template <int B>
+__global__ void k_mg_binv(int n, const int* __restrict__ bdiag, const float* __restrict__ val,
+                          float* __restrict__ binv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* blk = val + (size_t)bdiag[i] * B * B;
+    double a[B][2 * B], dg[B];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) {
+            a[f1][f2] = blk[f1 * B + f2];
+            a[f1][B + f2] = f1 == f2 ? 1.0 : 0.0;
+        }
+        dg[f1] = a[f1][f1];
+    }
+    bool ok = true;
+#pragma unroll
+    for (int kk = 0; kk < B; ++kk) {
+        int piv = kk;
+        double best = fabs(a[kk][kk]);
+#pragma unroll
+        for (int r = kk + 1; r < B; ++r)
+            if (fabs(a[r][kk]) > best) {
+                best = fabs(a[r][kk]);
+                piv = r;
+            }
+        if (best == 0.0) ok = false;
+        if (piv != kk) {
+#pragma unroll
+            for (int j = 0; j < 2 * B; ++j) {
+                const double tmp = a[kk][j];
+                a[kk][j] = a[piv][j];
+                a[piv][j] = tmp;
+            }
+        }
+        const double inv = ok ? 1.0 / a[kk][kk] : 0.0;
+#pragma unroll
+        for (int j = 0; j < 2 * B; ++j) a[kk][j] *= inv;
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+            if (r == kk) continue;
+            const double f = a[r][kk];
+#pragma unroll
+            for (int j = 0; j < 2 * B; ++j) a[r][j] -= f * a[kk][j];
+        }
+    }
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) {
+            double v = a[f1][B + f2];
+            if (!ok) v = f1 == f2 ? (dg[f1] != 0.0 ? 1.0 / dg[f1] : 1.0) : 0.0;
+            binv[(size_t)i * B * B + f1 * B + f2] = (float)v;
+        }
+}
+
+// ---- host: hierarchy ------------------------------------------------------------------------------
+
+// Greedy aggregation of a graph given as CSR adjacency without self loops.  agg[i] = aggregate
+// of node i or -1 (no neighbours).  Returns the number of aggregates.
+int aggregate(int n, const std::vector<int>& aptr, const std::vector<int>& aidx, std::vector<int>& agg) {
+    constexpr int UNSEEN = -1, LONE = -2;
+    agg.assign(n, UNSEEN);
+    int na = 0;
+    for (int i = 0; i < n; ++i) {
+        if (agg[i] != UNSEEN) continue;
+        const int b = aptr[i], e = aptr[i + 1];
+        if (b == e) {
+            agg[i] = LONE;
+            continue;
+        }
+        bool fresh = true;
+        for (int k = b; k < e && fresh; ++k) fresh = agg[aidx[k]] == UNSEEN;
+        if (!fresh) continue;
+        agg[i] = na;
+        for (int k = b; k < e; ++k) agg[aidx[k]] = na;
+        ++na;
+    }
+    for (int i = 0; i < n; ++i) {
+        if (agg[i] != UNSEEN) continue;
+        int to = -1;
+        for (int k = aptr[i]; k < aptr[i + 1] && to < 0; ++k)
+            if (agg[aidx[k]] >= 0) to = agg[aidx[k]];
+        agg[i] = to >= 0 ? to : na++;
+    }
+    for (int i = 0; i < n; ++i)
+        if (agg[i] == LONE) agg[i] = -1;
+    return na;
+}
+
+template <class T>
+int upload(pfg_ctx* c, DBuf& buf, const std::vector<T>& h) {
+    int rc = ensure(c, buf, sizeof(T) * std::max<size_t>(h.size(), 1));
+    if (rc) return rc;
+    if (!h.empty()) PFG_CUDA(c, cudaMemcpyAsync(buf.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, c->stream));
+    return PFG_OK;
+}
+
+}  // namespace
+
+void mg_release(pfg_ctx* c) {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (MgLevel& l : c->mg) {
+        DBuf* bufs[] = {&l.agg, &l.mem_ptr, &l.mem, &l.bptr, &l.bcol, &l.bdiag, &l.gptr,
+                        &l.glist, &l.val, &l.binv, &l.x, &l.xb, &l.b, &l.r};
+        for (DBuf* b : bufs) {
+            c->bytes_in_use -= std::min(c->bytes_in_use, b->cap);
+            release(*b);
+        }
+    }
+    c->mg.clear();
+    c->n_mg = 0;
+}
+
+// Builds the coarse levels of the current mesh (host aggregation, device patterns and lists).
+// Device buffers of earlier meshes are reused (grow-only).
+int mg_setup(pfg_ctx* c) {
+    c->n_mg = 0;
+    const int N = c->N, B = c->dim + 1;
+    int rc;
+    if ((rc = ensure(c, c->mg_x0, sizeof(float) * (size_t)B * N)) ||
+        (rc = ensure(c, c->mg_r0, sizeof(float) * (size_t)B * N)))
+        return rc;
+    // level-0 graph: the node adjacency without self (device lists, sorted)
+    std::vector<int> ptr0(N + 1), idx0(c->P);
+    PFG_CUDA(c, cudaMemcpyAsync(ptr0.data(), c->nbr_ptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(idx0.data(), c->nbr.p, sizeof(int) * (size_t)c->P, cudaMemcpyDeviceToHost, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    // fine level description: block rows (with self) and block columns
+    std::vector<int> fptr = ptr0, fcol = idx0;
+    int fn = N;
+    for (int lev = 1; lev <= 16; ++lev) {
+        // adjacency without self
+        std::vector<int> aptr(fn + 1, 0), aidx;
+        aidx.reserve(fcol.size());
+        for (int i = 0; i < fn; ++i) {
+            for (int k = fptr[i]; k < fptr[i + 1]; ++k)
+                if (fcol[k] != i) aidx.push_back(fcol[k]);
+            aptr[i + 1] = (int)aidx.size();
+        }
+        if (aidx.empty()) break;  // the finer level is block diagonal: it is the coarsest
+        std::vector<int> agg;
+        const int nc = aggregate(fn, aptr, aidx, agg);
+        if (nc >= fn) break;
+        // members
+        std::vector<int> mptr(nc + 1, 0), mem;
+        for (int i = 0; i < fn; ++i)
+            if (agg[i] >= 0) mptr[agg[i] + 1]++;
+        for (int I = 0; I < nc; ++I) mptr[I + 1] += mptr[I];
+        mem.resize(mptr[nc]);
+        {
+            std::vector<int> fill(mptr.begin(), mptr.end() - 1);
+            for (int i = 0; i < fn; ++i)
+                if (agg[i] >= 0) mem[fill[agg[i]]++] = i;
+        }
+        // coarse block pattern: aggregates adjacent through any member pair, with self
+        std::vector<int> cptr(nc + 1, 0), ccol;
+        {
+            std::vector<int> tmp;
+            for (int I = 0; I < nc; ++I) {
+                tmp.clear();
+                tmp.push_back(I);
+                for (int q = mptr[I]; q < mptr[I + 1]; ++q) {
+                    const int i = mem[q];
+                    for (int k = fptr[i]; k < fptr[i + 1]; ++k) {
+                        const int J = agg[fcol[k]];
+                        if (J >= 0) tmp.push_back(J);
+                    }
+                }
+                std::sort(tmp.begin(), tmp.end());
+                tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+                ccol.insert(ccol.end(), tmp.begin(), tmp.end());
+                cptr[I + 1] = (int)ccol.size();
+            }
+        }
+        const int nnzb = (int)ccol.size();
+        std::vector<int> cdiag(nc);
+        for (int I = 0; I < nc; ++I)
+            cdiag[I] = (int)(std::lower_bound(ccol.begin() + cptr[I], ccol.begin() + cptr[I + 1], I) - ccol.begin());
+        // Galerkin gather lists: fine block k (row i, column fcol[k]) -> coarse block
+        std::vector<int> target(fcol.size(), -1), gptr(nnzb + 1, 0), glist;
+        for (int i = 0; i < fn; ++i) {
+            const int I = agg[i];
+            if (I < 0) continue;
+            for (int k = fptr[i]; k < fptr[i + 1]; ++k) {
+                const int J = agg[fcol[k]];
+                if (J < 0) continue;
+                const int kc = (int)(std::lower_bound(ccol.begin() + cptr[I], ccol.begin() + cptr[I + 1], J) - ccol.begin());
+                target[k] = kc;
+                gptr[kc + 1]++;
+            }
+        }
+        for (int k = 0; k < nnzb; ++k) gptr[k + 1] += gptr[k];
+        glist.resize(gptr[nnzb]);
+        {
+            std::vector<int> fill(gptr.begin(), gptr.end() - 1);
+            for (size_t k = 0; k < target.size(); ++k)
+                if (target[k] >= 0) glist[fill[target[k]]++] = (int)k;
+        }
+        if ((int)c->mg.size() < lev) c->mg.emplace_back();
+        MgLevel& L = c->mg[lev - 1];
+        L.n = nc;
+        L.nnzb = nnzb;
+        c->n_mg = lev;
+        if ((rc = upload(c, L.agg, agg)) || (rc = upload(c, L.mem_ptr, mptr)) || (rc = upload(c, L.mem, mem)) ||
+            (rc = upload(c, L.bptr, cptr)) || (rc = upload(c, L.bcol, ccol)) || (rc = upload(c, L.bdiag, cdiag)) ||
+            (rc = upload(c, L.gptr, gptr)) || (rc = upload(c, L.glist, glist)) ||
+            (rc = ensure(c, L.val, sizeof(float) * (size_t)std::max(nnzb, 1) * B * B)) ||
+            (rc = ensure(c, L.binv, sizeof(float) * (size_t)nc * B * B)) ||
+            (rc = ensure(c, L.x, sizeof(float) * (size_t)nc * B)) || (rc = ensure(c, L.xb, sizeof(float) * (size_t)nc * B)) ||
+            (rc = ensure(c, L.b, sizeof(float) * (size_t)nc * B)) || (rc = ensure(c, L.r, sizeof(float) * (size_t)nc * B)))
+            return rc;
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+        fptr.swap(cptr);
+        fcol.swap(ccol);
+        fn = nc;
+    }
+    return PFG_OK;
+}
+
+// Coarse values and block inverses of every level from the current FP32 level-0 matrix.
+int mg_numeric(pfg_ctx* c) {
+    const int N = c->N;
+    for (int l = 0; l < c->n_mg; ++l) {
+        MgLevel& L = c->mg[l];
+        const long long nt = (long long)L.nnzb * (c->dim + 1) * (c->dim + 1);
+        const int grid = div_up(nt, BLOCK);
+        if (l == 0) {
+            if (c->dim == 2)
+                k_mg_galerkin0<2><<<grid, BLOCK, 0, c->stream>>>(L.nnzb, ptr<int>(L.gptr), ptr<int>(L.glist),
+                                                                 ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr),
+                                                                 ptr<int>(c->nbr), ptr<int>(c->row_ptr), N,
+                                                                 ptr<float>(c->val32), ptr<float>(L.val));
+            else
+                k_mg_galerkin0<3><<<grid, BLOCK, 0, c->stream>>>(L.nnzb, ptr<int>(L.gptr), ptr<int>(L.glist),
+                                                                 ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr),
+                                                                 ptr<int>(c->nbr), ptr<int>(c->row_ptr), N,
+                                                                 ptr<float>(c->val32), ptr<float>(L.val));
+        } else {
+            const float* fv = ptr<float>(c->mg[l - 1].val);
+            if (c->dim == 2)
+                k_mg_galerkin<3><<<grid, BLOCK, 0, c->stream>>>(L.nnzb, ptr<int>(L.gptr), ptr<int>(L.glist), fv,
+                                                                ptr<float>(L.val));
+            else
+                k_mg_galerkin<4><<<grid, BLOCK, 0, c->stream>>>(L.nnzb, ptr<int>(L.gptr), ptr<int>(L.glist), fv,
+                                                                ptr<float>(L.val));
+        }
+        if (c->dim == 2)
+            k_mg_binv<3><<<div_up(L.n, BLOCK), BLOCK, 0, c->stream>>>(L.n, ptr<int>(L.bdiag), ptr<float>(L.val),
+                                                                      ptr<float>(L.binv));
+        else
+            k_mg_binv<4><<<div_up(L.n, BLOCK), BLOCK, 0, c->stream>>>(L.n, ptr<int>(L.bdiag), ptr<float>(L.val),
+                                                                      ptr<float>(L.binv));
+    }
+    PFG_CHECK_LAUNCH(c);
+    return PFG_OK;
+}
+
+namespace {
+
+template <int DIM>
+void vcycle(pfg_ctx* c, const float* b0, float* out0) {
+    constexpr int B = DIM + 1;
+    constexpr int GN0 = DIM == 2 ? 4 : 8;
+    constexpr int GNB = 4;
+    const int N = c->N;
+    cudaStream_t s = c->stream;
+    const float* binv0 = ptr<float>(c->binv32);
+    float* x0 = ptr<float>(c->mg_x0);
+    float* r0 = ptr<float>(c->mg_r0);
+    const int* rp = ptr<int>(c->row_ptr);
+    const int* nptr = ptr<int>(c->nbr_ptr);
+    const int* nbr = ptr<int>(c->nbr);
+    const float* v0 = ptr<float>(c->val32);
+    const int L = c->n_mg;
+    const int g0 = div_up(N, BLOCK), g0l = div_up((long long)N * GN0, 256);
+    if (L == 0) {  // no coarse level: two damped block-Jacobi sweeps
+        k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
+        k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, rp, nptr, nbr, v0, binv0, b0, x0, out0);
+        return;
+    }
+    // down
+    k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
+    k_mg0_resid<DIM, 0><<<g0l, 256, 0, s>>>(N, rp, nptr, nbr, v0, binv0, b0, x0, r0);
+    {
+        MgLevel& L1 = c->mg[0];
+        k_mg0_restrict<DIM><<<div_up(L1.n, BLOCK), BLOCK, 0, s>>>(L1.n, ptr<int>(L1.mem_ptr), ptr<int>(L1.mem), N, r0,
+                                                                  ptr<float>(L1.b));
+    }
+    for (int l = 0; l + 1 < L; ++l) {
+        MgLevel& A = c->mg[l];
+        MgLevel& C = c->mg[l + 1];
+        const int gl = div_up((long long)A.n * GNB, 256);
+        k_mgb_smooth0<B><<<div_up(A.n, BLOCK), BLOCK, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<float>(A.binv), ptr<float>(A.b),
+                                                              ptr<float>(A.x));
+        k_mgb_resid<B, GNB, 0><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
+                                                  ptr<float>(A.binv), ptr<float>(A.b), ptr<float>(A.x), ptr<float>(A.r));
+        k_mgb_restrict<B><<<div_up(C.n, BLOCK), BLOCK, 0, s>>>(C.n, ptr<int>(C.mem_ptr), ptr<int>(C.mem),
+                                                               ptr<float>(A.r), ptr<float>(C.b));
+    }
+    // coarsest: exact block solve when block diagonal, else four damped sweeps
+    {
+        MgLevel& Z = c->mg[L - 1];
+        if (Z.nnzb == Z.n) {
+            k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
+                                                                  ptr<float>(Z.b), ptr<float>(Z.xb));
+        } else {
+            const int gl = div_up((long long)Z.n * GNB, 256);
+            k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
+                                                                  ptr<float>(Z.b), ptr<float>(Z.x));
+            for (int sweep = 0; sweep < 4; ++sweep) {
+                float* from = ptr<float>(sweep % 2 == 0 ? Z.x : Z.xb);
+                float* to = ptr<float>(sweep % 2 == 0 ? Z.xb : Z.x);
+                k_mgb_resid<B, GNB, 1><<<gl, 256, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<int>(Z.bcol), ptr<float>(Z.val),
+                                                          ptr<float>(Z.binv), ptr<float>(Z.b), from, to);
+            }
+            // four sweeps end in Z.x: copy the result slot
+            cudaMemcpyAsync(Z.xb.p, Z.x.p, sizeof(float) * (size_t)Z.n * B, cudaMemcpyDeviceToDevice, s);
+        }
+    }
+    // up
+    for (int l = L - 2; l >= 0; --l) {
+        MgLevel& A = c->mg[l];
+        MgLevel& C = c->mg[l + 1];
+        const int gl = div_up((long long)A.n * GNB, 256);
+        k_mgb_prolong<B><<<div_up(A.n, BLOCK), BLOCK, 0, s>>>(A.n, ptr<int>(C.agg), ptr<float>(C.xb), ptr<float>(A.x));
+        k_mgb_resid<B, GNB, 1><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
+                                                  ptr<float>(A.binv), ptr<float>(A.b), ptr<float>(A.x), ptr<float>(A.xb));
+    }
+    k_mg0_prolong<DIM><<<g0, BLOCK, 0, s>>>(N, ptr<int>(c->mg[0].agg), ptr<float>(c->mg[0].xb), x0);
+    k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, rp, nptr, nbr, v0, binv0, b0, x0, out0);
+}
+
+}  // namespace
+
+// out = M^-1 b for the FP32 scaled system (one V-cycle), both field-major R-vectors.
+void mg_apply(pfg_ctx* c, const float* b, float* out) {
+    if (c->dim == 2)
+        vcycle<2>(c, b, out);
+    else
+        vcycle<3>(c, b, out);
+}
+
+}  // namespace pfg

@@ -845,6 +845,12 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
                                                               ptr<double>(c->binv), m);
     prof_end(c, PH_PSPG_PAIRS);
     PFG_CHECK_LAUNCH(c);
+    if (c->n_mg > 0) {
+        prof_begin(c, PH_MG_SETUP);
+        int rc = mg_numeric(c);
+        prof_end(c, PH_MG_SETUP);
+        if (rc) return rc;
+    }
     return PFG_OK;
 }
 
@@ -885,10 +891,22 @@ struct KSet {
         constexpr int G = DIM == 2 ? 8 : 16;
         prof_begin(c, PH_KRYLOV_ITER);
         k_mx_up_p<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
+        if constexpr (sizeof(T) == 4)
+            if (c->n_mg > 0) {
+                prof_begin(c, PH_MG_CYCLE);
+                mg_apply(c, W + W_P * ld, W + W_PHAT * ld);
+                prof_end(c, PH_MG_CYCLE);
+            }
         prof_begin(c, PH_KRYLOV_SPMV);
         k_mx_spmv<T, G, DIM, 0><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr, val, W, ld);
         prof_end(c, PH_KRYLOV_SPMV);
         k_mx_up_s<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
+        if constexpr (sizeof(T) == 4)
+            if (c->n_mg > 0) {
+                prof_begin(c, PH_MG_CYCLE);
+                mg_apply(c, W + W_S * ld, W + W_SHAT * ld);
+                prof_end(c, PH_MG_CYCLE);
+            }
         prof_begin(c, PH_KRYLOV_SPMV);
         k_mx_spmv<T, G, DIM, 1><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr, val, W, ld);
         prof_end(c, PH_KRYLOV_SPMV);
@@ -1123,6 +1141,8 @@ int mx_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))
         return rc;
+    c->n_mg = 0;
+    if (c->prm.preconditioner == PFG_PC_MULTIGRID && (rc = mg_setup(c))) return rc;
     // one instance covering the whole mesh until pfg_set_instances says otherwise
     const int off[2] = {0, c->N};
     const double rho = c->prm.rho, mu = c->prm.mu;

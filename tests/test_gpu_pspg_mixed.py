@@ -151,3 +151,26 @@ def test_hard_instance_converges(gpu_lib):
     st_m, q_m = res[api.PREC_MIXED]
     assert st_m.picard_iterations == res[api.PREC_FP64][0].picard_iterations
     assert max(field_errs(q_m, res[api.PREC_FP64][1], 2, m.n_nodes)) < 1e-6
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_multigrid_matches_block_jacobi(gpu_lib, which, c1_mesh, small3d_mesh):
+    """Both preconditioners stop on the same FP64 residual test, so a step agrees to the
+    tolerance; the multigrid V-cycle needs several times fewer Krylov iterations."""
+    mesh = c1_mesh if which == "c1" else small3d_mesh
+    d, N = mesh.dim, mesh.n_nodes
+    column = (1.0, 2.0) if d == 2 else (0.2, 0.3, 0.3)
+    q0 = M.incomp_initial_states(mesh, column=column)
+    out = {}
+    for pc in (api.PC_BLOCK_JACOBI, api.PC_MULTIGRID):
+        ctx = make_ctx(mesh, preconditioner=pc)
+        ctx.set_states(q0)
+        kit = 0
+        for _ in range(3):
+            st = ctx.picard_step(1e-3)
+            assert st.converged == 1
+            kit += st.krylov_iterations
+        out[pc] = (ctx.get_states(), kit)
+    (qj, kj), (qm, km) = out[api.PC_BLOCK_JACOBI], out[api.PC_MULTIGRID]
+    assert max(field_errs(qm, qj, d, N)) < 1e-8
+    assert km * 1.5 < kj, (km, kj)
