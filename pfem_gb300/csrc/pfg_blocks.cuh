@@ -1,0 +1,57 @@
+// FP32 node-pair block products shared by the mixed incompressible Krylov solver
+// (pfg_pspg_mixed.cu) and the multigrid preconditioner (pfg_mg.cu).  Header-only device code.
+//
+// Layout: the scaled FP32 system is stored as one (d+1)x(d+1) block per node pair p = (n, m)
+// of the adjacency, p = nbr_ptr[n] + rank of m in n's sorted neighbour list, row-major inside
+// the block (k_mx_scale_bsr).
+#pragma once
+
+#include "pfg_device.cuh"
+
+namespace pfg {
+
+// Lanes per node of the node-row products (mean valence ~7 in 2D, ~15 in 3D) and the threads
+// of a segment kernel: one pass over the segment's NB nodes.
+template <int DIM>
+constexpr int node_lanes() {
+    return DIM == 2 ? 4 : 8;
+}
+
+// FP32 block row of node n times x over GN lanes: sum over n's neighbours m of blk(n,m) x_m,
+// with the blocks of the node-pair layout (k_mx_scale_bsr); 3D blocks are read as 4 float4.
+template <int DIM, int GN>
+__device__ __forceinline__ void block_row_f32(int n, bool act, int N, const int* __restrict__ nbr_ptr,
+                                              const int* __restrict__ nbr, const float* __restrict__ blk,
+                                              const float* __restrict__ x, int lane, float (&y)[DIM + 1]) {
+    constexpr int B = DIM + 1;
+#pragma unroll
+    for (int f = 0; f < B; ++f) y[f] = 0;
+    const int b0 = act ? nbr_ptr[n] : 0;
+    const int b1 = act ? nbr_ptr[n + 1] : 0;
+    for (int p = b0 + lane; p < b1; p += GN) {
+        const int mn = __ldg(nbr + p);
+        float xm[B];
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(x + (size_t)f2 * N + mn);
+        if constexpr (B == 4) {
+            const float4* a4 = reinterpret_cast<const float4*>(blk + (size_t)p * 16);
+#pragma unroll
+            for (int f1 = 0; f1 < 4; ++f1) {
+                const float4 a = __ldg(a4 + f1);
+                y[f1] += a.x * xm[0] + a.y * xm[1] + a.z * xm[2] + a.w * xm[3];
+            }
+        } else {
+            const float* a = blk + (size_t)p * B * B;
+#pragma unroll
+            for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+                for (int f2 = 0; f2 < B; ++f2) y[f1] += __ldg(a + f1 * B + f2) * xm[f2];
+        }
+    }
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int o = GN / 2; o > 0; o >>= 1) y[f1] += __shfl_xor_sync(0xffffffffu, y[f1], o, GN);
+}
+
+}  // namespace pfg

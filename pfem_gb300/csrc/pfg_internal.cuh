@@ -139,6 +139,7 @@ struct pfg_ctx {
     std::vector<pfg::MgLevel> mg;
     int n_mg = 0;
     pfg::DBuf mg_x0, mg_r0;
+    pfg::DBuf mg_in64;     // FP64 correction solves: FP32 scaled input and output of the cycle
 };
 
 namespace pfg {

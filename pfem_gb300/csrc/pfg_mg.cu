@@ -8,7 +8,7 @@
 // Jacobi apply and makes the count nearly mesh independent.
 //
 // Hierarchy (built on the host once per mesh upload, from the node adjacency only):
-//   * level 0 is the assembled system (field-major CSR, FP32 scaled values S A S);
+//   * level 0 is the assembled system: the FP32 scaled values S A S in node-pair blocks;
 //   * each coarser level aggregates the nodes of the finer one: greedy, in node order, a node
 //     whose neighbours are all unaggregated starts an aggregate with them; every node left
 //     joins the aggregate of its first aggregated neighbour.  Nodes without neighbours (free
@@ -32,6 +32,7 @@
 #include <cstring>
 #include <vector>
 
+#include "pfg_blocks.cuh"
 #include "pfg_device.cuh"
 #include "pfg_internal.cuh"
 
@@ -44,47 +45,6 @@ namespace {
 __host__ __device__ constexpr float mg_omega(int B) { return B == 3 ? 0.7f : 0.5f; }
 
 // ---- level 0 (field-major CSR) ---------------------------------------------------------------
-
-// y = (A x) over the d+1 rows of node n, by GN lanes walking n's neighbour list (all lanes hold
-// the result).  Column (m, f2) of row (n, f1) sits at rp(n, f1) + f2 deg(n) + rank(m); identity
-// rows hold their diagonal only.
-template <int DIM, int GN>
-__device__ __forceinline__ void row0_product(int n, bool act, int N, const int* __restrict__ rp,
-                                             const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
-                                             const float* __restrict__ val, const float* __restrict__ x, int lane,
-                                             float (&y)[DIM + 1]) {
-    constexpr int B = DIM + 1;
-    int rowp[B];
-    bool full[B];
-#pragma unroll
-    for (int f = 0; f < B; ++f) {
-        y[f] = 0;
-        rowp[f] = act ? rp[n + f * N] : 0;
-        full[f] = act && (rp[n + f * N + 1] - rowp[f] > 1);
-    }
-    const int b0 = act ? nbr_ptr[n] : 0;
-    const int deg = act ? nbr_ptr[n + 1] - b0 : 0;
-    for (int k = lane; k < deg; k += GN) {
-        const int mn = __ldg(nbr + b0 + k);
-        float xm[B];
-#pragma unroll
-        for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(x + (size_t)f2 * N + mn);
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1) {
-            if (!full[f1]) continue;
-            float acc = 0;
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) acc += __ldg(val + rowp[f1] + f2 * deg + k) * xm[f2];
-            y[f1] += acc;
-        }
-    }
-#pragma unroll
-    for (int f1 = 0; f1 < B; ++f1) {
-#pragma unroll
-        for (int o = GN / 2; o > 0; o >>= 1) y[f1] += __shfl_xor_sync(0xffffffffu, y[f1], o, GN);
-        if (act && !full[f1]) y[f1] = val[rowp[f1]] * x[(size_t)f1 * N + n];
-    }
-}
 
 // x = omega Binv b (pre-smoothing from a zero guess); x = Binv b, the exact solve, for a node
 // without neighbours
@@ -110,17 +70,17 @@ __global__ void k_mg0_smooth0(int N, const int* __restrict__ nbr_ptr, const floa
 // POST = 0: r = b - A x.  POST = 1: out = x + omega Binv (b - A x), or out = x for a node
 // without neighbours (already solved exactly).
 template <int DIM, int POST>
-__global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict__ rp, const int* __restrict__ nbr_ptr,
-                                                   const int* __restrict__ nbr, const float* __restrict__ val,
+__global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict__ nbr_ptr,
+                                                   const int* __restrict__ nbr, const float* __restrict__ blk,
                                                    const float* __restrict__ binv, const float* __restrict__ b,
                                                    const float* __restrict__ x, float* __restrict__ out) {
     constexpr int B = DIM + 1;
-    constexpr int GN = DIM == 2 ? 4 : 8;
+    constexpr int GN = node_lanes<DIM>();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = t / GN, lane = t % GN;
     const bool act = n < N;
     float y[B];
-    row0_product<DIM, GN>(act ? n : 0, act, N, rp, nbr_ptr, nbr, val, x, lane, y);
+    block_row_f32<DIM, GN>(act ? n : 0, act, N, nbr_ptr, nbr, blk, x, lane, y);
     if (!act || lane != 0) return;
     float r[B];
 #pragma unroll
@@ -276,34 +236,6 @@ __global__ void k_mgb_prolong(int n, const int* __restrict__ agg, const float* _
 }
 
 // ---- numeric setup ------------------------------------------------------------------------------
-
-// Level-1 blocks from the level-0 matrix: thread (k, f1, f2) sums entry (f1, f2) of the fine
-// node-pair blocks in coarse block k's list.
-template <int DIM>
-__global__ void k_mg_galerkin0(int nnzb, const int* __restrict__ gptr, const int* __restrict__ glist,
-                               const int* __restrict__ pair_node, const int* __restrict__ nbr_ptr,
-                               const int* __restrict__ nbr, const int* __restrict__ rp, int N,
-                               const float* __restrict__ val, float* __restrict__ cval) {
-    constexpr int B = DIM + 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)nnzb * B * B) return;
-    const int k = (int)(t / (B * B)), e = (int)(t % (B * B));
-    const int f1 = e / B, f2 = e % B;
-    float s = 0;
-    for (int q = gptr[k]; q < gptr[k + 1]; ++q) {
-        const int p = glist[q];
-        const int i = pair_node[p];
-        const int b0 = nbr_ptr[i];
-        const int deg = nbr_ptr[i + 1] - b0, rank = p - b0;
-        const int r = i + f1 * N;
-        const int rp0 = rp[r];
-        if (rp[r + 1] - rp0 > 1)
-            s += val[rp0 + f2 * deg + rank];
-        else if (f1 == f2 && nbr[p] == i)
-            s += val[rp0];
-    }
-    cval[t] = s;
-}
 
 template <int B>
 __global__ void k_mg_galerkin(int nnzb, const int* __restrict__ gptr, const int* __restrict__ glist,
@@ -541,24 +473,13 @@ int mg_setup(pfg_ctx* c) {
 
 // Coarse values and block inverses of every level from the current FP32 level-0 matrix.
 int mg_numeric(pfg_ctx* c) {
-    const int N = c->N;
     for (int l = 0; l < c->n_mg; ++l) {
         MgLevel& L = c->mg[l];
         const long long nt = (long long)L.nnzb * (c->dim + 1) * (c->dim + 1);
         const int grid = div_up(nt, BLOCK);
-        if (l == 0) {
-            if (c->dim == 2)
-                k_mg_galerkin0<2><<<grid, BLOCK, 0, c->stream>>>(L.nnzb, ptr<int>(L.gptr), ptr<int>(L.glist),
-                                                                 ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr),
-                                                                 ptr<int>(c->nbr), ptr<int>(c->row_ptr), N,
-                                                                 ptr<float>(c->val32), ptr<float>(L.val));
-            else
-                k_mg_galerkin0<3><<<grid, BLOCK, 0, c->stream>>>(L.nnzb, ptr<int>(L.gptr), ptr<int>(L.glist),
-                                                                 ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr),
-                                                                 ptr<int>(c->nbr), ptr<int>(c->row_ptr), N,
-                                                                 ptr<float>(c->val32), ptr<float>(L.val));
-        } else {
-            const float* fv = ptr<float>(c->mg[l - 1].val);
+        {
+            // level-0 blocks are the node-pair blocks of the FP32 system; glist holds pair ids
+            const float* fv = l == 0 ? ptr<float>(c->val32) : ptr<float>(c->mg[l - 1].val);
             if (c->dim == 2)
                 k_mg_galerkin<3><<<grid, BLOCK, 0, c->stream>>>(L.nnzb, ptr<int>(L.gptr), ptr<int>(L.glist), fv,
                                                                 ptr<float>(L.val));
@@ -582,14 +503,13 @@ namespace {
 template <int DIM>
 void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     constexpr int B = DIM + 1;
-    constexpr int GN0 = DIM == 2 ? 4 : 8;
+    constexpr int GN0 = node_lanes<DIM>();
     constexpr int GNB = 4;
     const int N = c->N;
     cudaStream_t s = c->stream;
     const float* binv0 = ptr<float>(c->binv32);
     float* x0 = ptr<float>(c->mg_x0);
     float* r0 = ptr<float>(c->mg_r0);
-    const int* rp = ptr<int>(c->row_ptr);
     const int* nptr = ptr<int>(c->nbr_ptr);
     const int* nbr = ptr<int>(c->nbr);
     const float* v0 = ptr<float>(c->val32);
@@ -597,12 +517,12 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     const int g0 = div_up(N, BLOCK), g0l = div_up((long long)N * GN0, 256);
     if (L == 0) {  // no coarse level: two damped block-Jacobi sweeps
         k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
-        k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, rp, nptr, nbr, v0, binv0, b0, x0, out0);
+        k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, out0);
         return;
     }
     // down
     k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
-    k_mg0_resid<DIM, 0><<<g0l, 256, 0, s>>>(N, rp, nptr, nbr, v0, binv0, b0, x0, r0);
+    k_mg0_resid<DIM, 0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, r0);
     {
         MgLevel& L1 = c->mg[0];
         k_mg0_restrict<DIM><<<div_up(L1.n, BLOCK), BLOCK, 0, s>>>(L1.n, ptr<int>(L1.mem_ptr), ptr<int>(L1.mem), N, r0,
@@ -649,7 +569,7 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
                                                   ptr<float>(A.binv), ptr<float>(A.b), ptr<float>(A.x), ptr<float>(A.xb));
     }
     k_mg0_prolong<DIM><<<g0, BLOCK, 0, s>>>(N, ptr<int>(c->mg[0].agg), ptr<float>(c->mg[0].xb), x0);
-    k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, rp, nptr, nbr, v0, binv0, b0, x0, out0);
+    k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, out0);
 }
 
 }  // namespace

@@ -28,6 +28,7 @@
 
 #include "pfg_device.cuh"
 #include "pfg_internal.cuh"
+#include "pfg_blocks.cuh"
 #include "pfg_pspg_common.cuh"
 
 namespace pfg {
@@ -253,26 +254,43 @@ __global__ void k_mx_rowscale(int N, const int* __restrict__ diag, const double*
     }
 }
 
-// val32 = FP32(s_r a_rc s_c) over the rows of a segment's nodes
-template <int G, int DIM>
-__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_scale_vals(Mx m, int N, const int* __restrict__ rp,
-                                                              const int* __restrict__ col,
-                                                              const double* __restrict__ val,
-                                                              const double* __restrict__ scale,
-                                                              float* __restrict__ val32) {
-    const int blk = blockIdx.x;
-    if (!m.ii[m.seg[3 * blk] * I_COUNT + I_ACTIVE]) return;
-    const int n0 = m.seg[3 * blk + 1], cnt = m.seg[3 * blk + 2] - n0;
-    const int rows = cnt * (DIM + 1);
-    const int lane = threadIdx.x % G;
-    for (int t0 = 0; t0 < rows; t0 += SPMV_BLOCK / G) {
-        const int t = t0 + threadIdx.x / G;
-        if (t >= rows) continue;
-        const int f = t / cnt;
-        const int r = f * N + n0 + (t - f * cnt);
+// The FP32 scaled system S A S in node-pair blocks: blk[p][f1][f2] = FP32(s_(n,f1) a s_(m,f2))
+// for the pair p = (n, m) of the adjacency (p = nbr_ptr[n] + rank of m), one thread per pair.
+// Identity rows keep their (scaled) diagonal and zeros elsewhere.  One contiguous (d+1)^2 block
+// per neighbour lets the FP32 products load it with vector loads and no per-value index.
+template <int DIM>
+__global__ void k_mx_scale_bsr(int P, int N, const int* __restrict__ pair_node, const int* __restrict__ nbr_ptr,
+                               const int* __restrict__ nbr, const int* __restrict__ rp,
+                               const double* __restrict__ val, const double* __restrict__ scale, Mx m,
+                               float* __restrict__ blk) {
+    constexpr int B = DIM + 1;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int n = pair_node[p];
+    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
+    const int mm = nbr[p];
+    const int b0 = nbr_ptr[n];
+    const int deg = nbr_ptr[n + 1] - b0, rank = p - b0;
+    float out[B * B];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        const int r = n + f1 * N;
+        const int r0 = rp[r];
         const double sr = scale[r];
-        for (int kk = rp[r] + lane; kk < rp[r + 1]; kk += G) val32[kk] = (float)(sr * val[kk] * scale[col[kk]]);
+        const bool full = rp[r + 1] - r0 > 1;
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) {
+            double a = 0.0;
+            if (full)
+                a = sr * val[r0 + f2 * deg + rank] * scale[mm + f2 * N];
+            else if (f1 == f2 && mm == n)
+                a = sr * val[r0] * sr;
+            out[f1 * B + f2] = (float)a;
+        }
     }
+    float* dst = blk + (size_t)p * B * B;
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) dst[e] = out[e];
 }
 
 // ---- node-block Jacobi preconditioner --------------------------------------------------------
@@ -592,21 +610,63 @@ __global__ void __launch_bounds__(NB) k_mx_up_s(Mx m, const int* __restrict__ li
     block_apply_t<T, DIM>(n, N, binv, s, W + W_SHAT * ld);
 }
 
+// FP64 row products of node n (field-major CSR: column (m, f2) of row (n, f1) at
+// row_ptr(n, f1) + f2 deg(n) + rank(m); identity rows hold their diagonal only).
+template <int DIM, int GN>
+__device__ __forceinline__ void node_rows_f64(int n, bool act, int N, const int* __restrict__ rp,
+                                              const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                                              const double* __restrict__ val, const double* __restrict__ x,
+                                              int lane, double (&y)[DIM + 1]) {
+    constexpr int B = DIM + 1;
+    int rowp[B];
+    bool full[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        y[f] = 0;
+        rowp[f] = act ? rp[n + f * N] : 0;
+        full[f] = act && (rp[n + f * N + 1] - rowp[f] > 1);
+    }
+    const int b0 = act ? nbr_ptr[n] : 0;
+    const int deg = act ? nbr_ptr[n + 1] - b0 : 0;
+    for (int k = lane; k < deg; k += GN) {
+        const int mn = __ldg(nbr + b0 + k);
+        double xm[B];
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(x + (size_t)f2 * N + mn);
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1) {
+            if (!full[f1]) continue;
+            double acc = 0;
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) acc += __ldg(val + rowp[f1] + f2 * deg + k) * xm[f2];
+            y[f1] += acc;
+        }
+    }
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+#pragma unroll
+        for (int o = GN / 2; o > 0; o >>= 1) y[f1] += __shfl_xor_sync(0xffffffffu, y[f1], o, GN);
+        if (act && !full[f1]) y[f1] = val[rowp[f1]] * x[(size_t)f1 * N + n];
+    }
+}
+
 // out = A in over the rows of the segment's nodes (all fields); dots for alpha or omega.
 // MODE 0: v = A phat, alpha = rho / (rhat . v).  MODE 1: t = A shat, omega = (t.s)/(t.t).
-// Node-row SpMV: the d+1 rows of node n share n's neighbour list, and column (m, f2) of row
-// (n, f1) sits at row_ptr(n, f1) + f2 deg(n) + rank(m); so a group of GN lanes walks n's
-// neighbours once (one index and d+1 input values per neighbour) and accumulates all d+1
-// rows, reading each matrix value once and no per-value column index.  Identity rows (free
-// nodes, bound-node velocities) hold their diagonal only.
-template <class T, int G, int DIM, int MODE>
-__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, const int* __restrict__ list, T* __restrict__ scb,
-                                                        int cnt_slot, int N,
-                                                        const int* __restrict__ rp, const int* __restrict__ nbr_ptr,
-                                                        const int* __restrict__ nbr,
-                                                        const T* __restrict__ val, T* __restrict__ W, size_t ld) {
+// Node-row product: the d+1 rows of node n share n's neighbour list, so a group of GN lanes
+// walks n's neighbours once (one index and d+1 input values per neighbour) and accumulates
+// all d+1 rows.  One pass: NB x GN threads per segment.  FP32 reads the node-pair blocks of
+// the scaled system, FP64 the field-major CSR of A.
+template <class T, int DIM, int MODE>
+__global__ void __launch_bounds__(NB * node_lanes<DIM>()) k_mx_spmv(Mx m, const int* __restrict__ list,
+                                                                  T* __restrict__ scb, int cnt_slot, int N,
+                                                                  const int* __restrict__ rp,
+                                                                  const int* __restrict__ nbr_ptr,
+                                                                  const int* __restrict__ nbr,
+                                                                  const T* __restrict__ val, T* __restrict__ W,
+                                                                  size_t ld) {
     constexpr int B = DIM + 1;
-    constexpr int GN = DIM == 2 ? 4 : 8;  // lanes per node (mean valence ~7 / ~15)
+    constexpr int GN = node_lanes<DIM>();
+    constexpr int NT = NB * GN;
     __shared__ double sh[32];
     const int b = list ? list[blockIdx.x] : blockIdx.x;  // segment
     const int inst = m.seg[3 * b];
@@ -617,61 +677,30 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_spmv(Mx m, const int* __restr
     const T* in = W + (MODE == 0 ? W_PHAT : W_SHAT) * ld;
     T* out = W + (MODE == 0 ? W_V : W_T) * ld;
     T d0 = 0, d1 = 0;
-    for (int off = 0; off < cnt; off += SPMV_BLOCK / GN) {
-        const int ln = off + threadIdx.x / GN;
-        const bool act = ln < cnt;
-        const int n = n0 + (act ? ln : 0);
-        T y[B];
-        int rowp[B];
-        bool full[B];
+    const int ln = threadIdx.x / GN;
+    const bool act = ln < cnt;
+    const int n = n0 + (act ? ln : 0);
+    T y[B];
+    if constexpr (sizeof(T) == 4)
+        block_row_f32<DIM, GN>(n, act, N, nbr_ptr, nbr, val, in, lane, y);
+    else
+        node_rows_f64<DIM, GN>(n, act, N, rp, nbr_ptr, nbr, val, in, lane, y);
+    if (act && lane == 0) {
 #pragma unroll
-        for (int f = 0; f < B; ++f) {
-            y[f] = 0;
-            rowp[f] = act ? rp[n + f * N] : 0;
-            full[f] = act && (rp[n + f * N + 1] - rowp[f] > 1);
-        }
-        const int b0 = act ? nbr_ptr[n] : 0;
-        const int deg = act ? nbr_ptr[n + 1] - b0 : 0;
-        for (int k = lane; k < deg; k += GN) {
-            const int mn = __ldg(nbr + b0 + k);
-            T xm[B];
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(in + (size_t)f2 * N + mn);
-#pragma unroll
-            for (int f1 = 0; f1 < B; ++f1) {
-                if (!full[f1]) continue;
-                T acc = 0;
-#pragma unroll
-                for (int f2 = 0; f2 < B; ++f2) acc += __ldg(val + rowp[f1] + f2 * deg + k) * xm[f2];
-                y[f1] += acc;
-            }
-        }
-        if (act && lane == 0) {
-#pragma unroll
-            for (int f1 = 0; f1 < B; ++f1)
-                if (!full[f1]) y[f1] = val[rowp[f1]] * in[(size_t)f1 * N + n];
-        }
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1)
-#pragma unroll
-            for (int o = GN / 2; o > 0; o >>= 1) y[f1] += __shfl_xor_sync(0xffffffffu, y[f1], o, GN);
-        if (act && lane == 0) {
-#pragma unroll
-            for (int f1 = 0; f1 < B; ++f1) {
-                const size_t r = (size_t)f1 * N + n;
-                out[r] = y[f1];
-                if (MODE == 0) {
-                    d0 += W[W_RHAT * ld + r] * y[f1];
-                } else {
-                    d0 += y[f1] * W[W_S * ld + r];
-                    d1 += y[f1] * y[f1];
-                }
+        for (int f1 = 0; f1 < B; ++f1) {
+            const size_t r = (size_t)f1 * N + n;
+            out[r] = y[f1];
+            if (MODE == 0) {
+                d0 += W[W_RHAT * ld + r] * y[f1];
+            } else {
+                d0 += y[f1] * W[W_S * ld + r];
+                d1 += y[f1] * y[f1];
             }
         }
     }
     const int* ii = m.ii + inst * I_COUNT;
     T v[2] = {d0, d1};
-    if (!inst_reduce<SPMV_BLOCK, 2, T>(v, b, ii[I_B0], ii[I_B1], reinterpret_cast<T*>(m.part),
+    if (!inst_reduce<NT, 2, T>(v, b, ii[I_B0], ii[I_B1], reinterpret_cast<T*>(m.part),
                                        reinterpret_cast<unsigned*>(m.ii + inst * I_COUNT + I_TICKET), sh))
         return;
     if (threadIdx.x != 0) return;
@@ -787,10 +816,6 @@ __global__ void k_mx_restore(int N, const double* __restrict__ save, const doubl
 
 // ---- host side ---------------------------------------------------------------------------------
 
-// Lanes per SpMV row from the dimension alone (mean row length ~21 in 2D, ~60 in 3D), so an
-// instance's arithmetic does not depend on the other instances it is batched with.
-int lanes(pfg_ctx* c) { return c->dim == 2 ? 8 : 16; }
-
 struct Counters {
     int need32, active, need64, redo;
 };
@@ -834,12 +859,13 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
         ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<double>(c->edata),
         ptr<uint8_t>(c->flags), ptr<int>(c->row_ptr), ptr<double>(c->val), ptr<double>(c->vbc), ptr<double>(c->rhs),
         m, k);
-    constexpr int G = DIM == 2 ? 8 : 16;
     double* scale = ptr<double>(c->mx_scale);
     k_mx_rowscale<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->diag_pos), ptr<double>(c->val), m,
                                                                   scale);
-    k_mx_scale_vals<G, DIM><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(m, N, ptr<int>(c->row_ptr), ptr<int>(c->col),
-                                                                    ptr<double>(c->val), scale, ptr<float>(c->val32));
+    k_mx_scale_bsr<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(c->P, N, ptr<int>(c->pair_node),
+                                                                      ptr<int>(c->nbr_ptr), ptr<int>(c->nbr),
+                                                                      ptr<int>(c->row_ptr), ptr<double>(c->val), scale,
+                                                                      m, ptr<float>(c->val32));
     k_mx_binv<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->row_ptr), ptr<double>(c->val),
                                                               ptr<int>(c->diag_pos), scale, ptr<float>(c->binv32),
                                                               ptr<double>(c->binv), m);
@@ -868,8 +894,41 @@ int mx_residual(pfg_ctx* c, const MxConst& k, int kind, Counters* cnt) {
     return read_counters(c, cnt);
 }
 
+// FP64 correction solves preconditioned by the FP32 multigrid of the scaled system:
+// M^-1 v = S (S A S)^-1_MG (S v).  k_mx_to_mg writes FP32(S v), k_mx_from_mg v_hat = S out.
+template <int DIM>
+__global__ void __launch_bounds__(NB) k_mx_to_mg(Mx m, const int* __restrict__ list, const double* __restrict__ scb,
+                                                 int N, const double* __restrict__ v, const double* __restrict__ scale,
+                                                 float* __restrict__ out) {
+    const int b = list ? list[blockIdx.x] : blockIdx.x;
+    if (scb[m.seg[3 * b] * M_COUNT + M_DONE] != 0) return;
+    const int n = m.seg[3 * b + 1] + threadIdx.x;
+    if (n >= m.seg[3 * b + 2]) return;
+#pragma unroll
+    for (int f = 0; f <= DIM; ++f) {
+        const size_t r = (size_t)f * N + n;
+        out[r] = (float)(scale[r] * v[r]);
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(NB) k_mx_from_mg(Mx m, const int* __restrict__ list, const double* __restrict__ scb,
+                                                   int N, const float* __restrict__ in, const double* __restrict__ scale,
+                                                   double* __restrict__ vhat) {
+    const int b = list ? list[blockIdx.x] : blockIdx.x;
+    if (scb[m.seg[3 * b] * M_COUNT + M_DONE] != 0) return;
+    const int n = m.seg[3 * b + 1] + threadIdx.x;
+    if (n >= m.seg[3 * b + 2]) return;
+#pragma unroll
+    for (int f = 0; f <= DIM; ++f) {
+        const size_t r = (size_t)f * N + n;
+        vhat[r] = scale[r] * (double)in[r];
+    }
+}
+
 // The five kernels of one BiCGSTAB iteration in precision T, over `grid` segments (all of them,
-// or the compacted list of segments whose instance is still iterating).
+// or the compacted list of segments whose instance is still iterating).  With the multigrid
+// on, its V-cycle replaces the node-block Jacobi apply in both precisions.
 template <class T, int DIM>
 struct KSet {
     Mx m;
@@ -887,33 +946,81 @@ struct KSet {
     const int* nbr;
     double* x;
 
-    void iterate(pfg_ctx* c, int grid) const {
-        constexpr int G = DIM == 2 ? 8 : 16;
-        prof_begin(c, PH_KRYLOV_ITER);
-        k_mx_up_p<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
-        if constexpr (sizeof(T) == 4)
-            if (c->n_mg > 0) {
-                prof_begin(c, PH_MG_CYCLE);
-                mg_apply(c, W + W_P * ld, W + W_PHAT * ld);
-                prof_end(c, PH_MG_CYCLE);
-            }
-        prof_begin(c, PH_KRYLOV_SPMV);
-        k_mx_spmv<T, G, DIM, 0><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr, val, W, ld);
-        prof_end(c, PH_KRYLOV_SPMV);
-        k_mx_up_s<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv);
-        if constexpr (sizeof(T) == 4)
-            if (c->n_mg > 0) {
-                prof_begin(c, PH_MG_CYCLE);
-                mg_apply(c, W + W_S * ld, W + W_SHAT * ld);
-                prof_end(c, PH_MG_CYCLE);
-            }
-        prof_begin(c, PH_KRYLOV_SPMV);
-        k_mx_spmv<T, G, DIM, 1><<<grid, SPMV_BLOCK, 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr, val, W, ld);
-        prof_end(c, PH_KRYLOV_SPMV);
+    // vhat = M^-1 v by the multigrid (the block-Jacobi vhat of the update kernel is overwritten)
+    void precondition(pfg_ctx* c, int grid, T* v, T* vhat) const {
+        if (c->n_mg == 0) return;
+        prof_begin(c, PH_MG_CYCLE);
+        if constexpr (sizeof(T) == 4) {
+            mg_apply(c, v, vhat);
+        } else {
+            float* in = ptr<float>(c->mg_in64);
+            float* out = in + ld;
+            const double* sc = ptr<double>(c->mx_scale);
+            k_mx_to_mg<DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, v, sc, in);
+            mg_apply(c, in, out);
+            k_mx_from_mg<DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, out, sc, vhat);
+        }
+        prof_end(c, PH_MG_CYCLE);
+    }
+
+    void up_p(pfg_ctx* c, int grid) const { k_mx_up_p<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv); }
+    void up_s(pfg_ctx* c, int grid) const { k_mx_up_s<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, N, W, ld, binv); }
+    void up_x(pfg_ctx* c, int grid) const {
         k_mx_up_x<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, slot, N, x, scale, W, ld);
+    }
+    template <int MODE>
+    void spmv(pfg_ctx* c, int grid) const {
+        prof_begin(c, PH_KRYLOV_SPMV);
+        k_mx_spmv<T, DIM, MODE><<<grid, NB * node_lanes<DIM>(), 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr,
+                                                                              val, W, ld);
+        prof_end(c, PH_KRYLOV_SPMV);
+    }
+
+    void iterate(pfg_ctx* c, int grid) const {
+        prof_begin(c, PH_KRYLOV_ITER);
+        up_p(c, grid);
+        precondition(c, grid, W + W_P * ld, W + W_PHAT * ld);
+        spmv<0>(c, grid);
+        up_s(c, grid);
+        precondition(c, grid, W + W_S * ld, W + W_SHAT * ld);
+        spmv<1>(c, grid);
+        up_x(c, grid);
         prof_end(c, PH_KRYLOV_ITER);
     }
 };
+
+// One BiCGSTAB iteration of a batch whose instances iterate in both precisions (na segments
+// in FP32, nb in FP64).  With the multigrid on, one V-cycle serves both: the FP64 instances'
+// scaled vectors are written into their (unused) rows of the FP32 workspace, so the cycle over
+// all nodes preconditions every instance at once.
+template <int DIM>
+void iterate_batch(pfg_ctx* c, const KSet<float, DIM>& a, int na, const KSet<double, DIM>& b, int nb) {
+    auto shared_cycle = [&](int src, int dst) {
+        if (c->n_mg == 0) return;
+        prof_begin(c, PH_MG_CYCLE);
+        const double* sc = ptr<double>(c->mx_scale);
+        float* in = a.W + src * a.ld;
+        float* out = a.W + dst * a.ld;
+        if (nb) k_mx_to_mg<DIM><<<nb, NB, 0, c->stream>>>(b.m, b.list, b.scb, b.N, b.W + src * b.ld, sc, in);
+        mg_apply(c, in, out);
+        if (nb) k_mx_from_mg<DIM><<<nb, NB, 0, c->stream>>>(b.m, b.list, b.scb, b.N, out, sc, b.W + dst * b.ld);
+        prof_end(c, PH_MG_CYCLE);
+    };
+    prof_begin(c, PH_KRYLOV_ITER);
+    if (na) a.up_p(c, na);
+    if (nb) b.up_p(c, nb);
+    shared_cycle(W_P, W_PHAT);
+    if (na) a.template spmv<0>(c, na);
+    if (nb) b.template spmv<0>(c, nb);
+    if (na) a.up_s(c, na);
+    if (nb) b.up_s(c, nb);
+    shared_cycle(W_S, W_SHAT);
+    if (na) a.template spmv<1>(c, na);
+    if (nb) b.template spmv<1>(c, nb);
+    if (na) a.up_x(c, na);
+    if (nb) b.up_x(c, nb);
+    prof_end(c, PH_KRYLOV_ITER);
+}
 
 template <class T, int DIM>
 KSet<T, DIM> kset(pfg_ctx* c, const int* list) {
@@ -1032,10 +1139,7 @@ int mx_inner_batch(pfg_ctx* c, Counters* cnt) {
     int done_it = 0;
     while ((!l32.empty() || !l64.empty()) && done_it < max_it) {
         const int n = std::min(chunk, max_it - done_it);
-        for (int it = 0; it < n; ++it) {
-            if (!l32.empty()) k32.iterate(c, (int)l32.size());
-            if (!l64.empty()) k64.iterate(c, (int)l64.size());
-        }
+        for (int it = 0; it < n; ++it) iterate_batch<DIM>(c, k32, (int)l32.size(), k64, (int)l64.size());
         PFG_CHECK_LAUNCH(c);
         done_it += n;
         if ((rc = rebuild())) return rc;
@@ -1136,13 +1240,17 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
 int mx_alloc(pfg_ctx* c) {
     const size_t R = std::max(c->R, 1), N = std::max(c->N, 1);
     int rc;
-    if ((rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max<int64_t>(c->nnz, 1))) ||
+    if ((rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))) ||
         (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) || (rc = ensure(c, c->mx_scale, sizeof(double) * R)) ||
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))
         return rc;
     c->n_mg = 0;
-    if (c->prm.preconditioner == PFG_PC_MULTIGRID && (rc = mg_setup(c))) return rc;
+    if (c->prm.preconditioner == PFG_PC_MULTIGRID) {
+        if ((rc = mg_setup(c)) || (rc = ensure(c, c->mg_in64, sizeof(float) * 2 * R))) return rc;
+        // the cycle runs over every node: keep the rows of instances not in FP64 mode finite
+        PFG_CUDA(c, cudaMemsetAsync(c->mg_in64.p, 0, sizeof(float) * 2 * R, c->stream));
+    }
     // one instance covering the whole mesh until pfg_set_instances says otherwise
     const int off[2] = {0, c->N};
     const double rho = c->prm.rho, mu = c->prm.mu;
