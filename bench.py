@@ -56,6 +56,8 @@ def parse_args():
                          "steps on the 2D / 3D dam break; batch-c4: 256 independent 2D instances; "
                          "serve-c5: a Poisson stream of requests served under an HBM budget")
     ap.add_argument("--instances", type=int, default=256, help="batch-c4: number of instances")
+    ap.add_argument("--h", type=float, default=None,
+                    help="incomp-c1 / incomp-c3: node spacing (default 0.05 / 0.01); smaller cases for profiling")
     ap.add_argument("--requests", type=int, default=24, help="serve-c5: number of requests")
     ap.add_argument("--rate", type=float, default=1.5, help="serve-c5: mean arrivals per second")
     return ap.parse_args()
@@ -480,6 +482,22 @@ def _phase_roofline(phases, pb_spmv, pb_asm, peak):
     return out
 
 
+def incomp_cfg(args):
+    cfg = INCOMP[args.workload]
+    if args.h is not None and args.workload in ("incomp-c1", "incomp-c3"):
+        cfg = dict(cfg, name=cfg["name"].rsplit("h = ", 1)[0] + f"h = {args.h:g}")
+    return cfg
+
+
+def incomp_mesh(args):
+    from pfem_gb300 import mesh as M
+    from pfem_gb300 import workloads as WL
+
+    if args.h is not None:
+        return M.dam_break_2d(args.h) if args.workload == "incomp-c1" else M.dam_break_3d(args.h)
+    return WL.c1() if args.workload == "incomp-c1" else WL.c3()
+
+
 def run_gpu_incomp(args):
     import numpy as np
     import torch
@@ -495,8 +513,8 @@ def run_gpu_incomp(args):
         return run_gpu_batch(args)
     if args.workload == "serve-c5":
         return run_gpu_serve(args)
-    cfg = INCOMP[args.workload]
-    mesh = WL.c1() if args.workload == "incomp-c1" else WL.c3()
+    cfg = incomp_cfg(args)
+    mesh = incomp_mesh(args)
     d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
     R = (d + 1) * N
     nnz = pattern_nnz(mesh)
@@ -871,7 +889,7 @@ def run_reference_incomp(args):
         v = n_steps / el
         sample = f"the first {n_req} requests run one after another ({n_steps} steps, {el:.1f} s)"
     else:
-        cfg = INCOMP[args.workload]
+        cfg = incomp_cfg(args)
     if args.workload == "serve-c5":
         pass
     elif args.workload == "batch-c4":
@@ -889,7 +907,7 @@ def run_reference_incomp(args):
         v = inst_steps / el
         sample = f"one Picard step of each of the first {inst_steps} instances ({el:.1f} s), {dof / el:.3g} DOF/s"
     else:
-        mesh = WL.c1() if args.workload == "incomp-c1" else WL.c3()
+        mesh = incomp_mesh(args)
         q = M.incomp_initial_states(mesh, column=cfg["column"])
         om = O.OracleMesh(mesh)
         g = (0.0, -9.81) if mesh.dim == 2 else (0.0, 0.0, -9.81)

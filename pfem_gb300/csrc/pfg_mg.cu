@@ -102,23 +102,35 @@ __global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict_
     }
 }
 
-// bc[I] = sum over the members n of aggregate I of r[n] (level 0: field-major r)
+// Lanes per aggregate of the restrictions: aggregates hold ~7 (2D) to ~20 (3D) members, and a
+// single thread summing them is a chain of dependent loads.
+constexpr int RL = 8;
+
+// bc[I] = sum over the members n of aggregate I of r[n] (level 0: field-major r); RL lanes per
+// aggregate, strided over the members, then a fixed shuffle tree.
 template <int DIM>
 __global__ void k_mg0_restrict(int nc, const int* __restrict__ mem_ptr, const int* __restrict__ mem, int N,
                                const float* __restrict__ r, float* __restrict__ bc) {
     constexpr int B = DIM + 1;
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= nc) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = t / RL, lane = t % RL;
+    const bool act = I < nc;
     float s[B];
 #pragma unroll
     for (int f = 0; f < B; ++f) s[f] = 0;
-    for (int q = mem_ptr[I]; q < mem_ptr[I + 1]; ++q) {
+    const int q1 = act ? mem_ptr[I + 1] : 0;
+    for (int q = (act ? mem_ptr[I] : 0) + lane; q < q1; q += RL) {
         const int n = mem[q];
 #pragma unroll
         for (int f = 0; f < B; ++f) s[f] += r[(size_t)f * N + n];
     }
 #pragma unroll
-    for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
+    for (int f = 0; f < B; ++f)
+#pragma unroll
+        for (int o = RL / 2; o > 0; o >>= 1) s[f] += __shfl_xor_sync(0xffffffffu, s[f], o, RL);
+    if (act && lane == 0)
+#pragma unroll
+        for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
 }
 
 // x[n] += xc[agg n] (level 0: field-major x)
@@ -135,13 +147,13 @@ __global__ void k_mg0_prolong(int N, const int* __restrict__ agg, const float* _
 }
 
 // ---- coarse levels (block CSR, node-major vectors) --------------------------------------------
+// Row operations as device functions, used by the one-level kernels and by the single-block
+// kernel that runs the small coarse levels (k_mg_tail).
 
-// x = omega Binv b; x = Binv b for a block row without off-diagonal blocks
+// x_i = w Binv_i b_i; w = 1 (exact) for a block row without off-diagonal blocks
 template <int B>
-__global__ void k_mgb_smooth0(int n, const int* __restrict__ bptr, const float* __restrict__ binv,
-                              const float* __restrict__ b, float* __restrict__ x) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void smooth0_row(int i, const int* __restrict__ bptr, const float* __restrict__ binv,
+                                            const float* __restrict__ b, float* __restrict__ x) {
     const float w = bptr[i + 1] - bptr[i] == 1 ? 1.0f : mg_omega(B);
     float v[B];
 #pragma unroll
@@ -156,30 +168,28 @@ __global__ void k_mgb_smooth0(int n, const int* __restrict__ bptr, const float* 
     }
 }
 
-// POST = 0: r = b - A x.  POST = 1: out = x + omega Binv (b - A x), or out = x for a block row
-// without off-diagonal blocks (solved exactly).  GN lanes per block row.
+// Block row i over GN lanes (all lanes of the group call it with the same i and act).
+// POST = 0: r_i = b_i - (A x)_i.  POST = 1: out_i = x_i + omega Binv_i (b - A x)_i, or x_i for a
+// block row without off-diagonal blocks (solved exactly).
 template <int B, int GN, int POST>
-__global__ void __launch_bounds__(256) k_mgb_resid(int n, const int* __restrict__ bptr, const int* __restrict__ bcol,
-                                                   const float* __restrict__ val, const float* __restrict__ binv,
-                                                   const float* __restrict__ b, const float* __restrict__ x,
-                                                   float* __restrict__ out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = t / GN, lane = t % GN;
-    const bool act = i < n;
+__device__ __forceinline__ void resid_row(int i, bool act, int lane, const int* __restrict__ bptr,
+                                          const int* __restrict__ bcol, const float* __restrict__ val,
+                                          const float* __restrict__ binv, const float* __restrict__ b,
+                                          const float* __restrict__ x, float* __restrict__ out) {
     float y[B];
 #pragma unroll
     for (int f = 0; f < B; ++f) y[f] = 0;
     const int k0 = act ? bptr[i] : 0, k1 = act ? bptr[i + 1] : 0;
     for (int k = k0 + lane; k < k1; k += GN) {
-        const int j = __ldg(bcol + k);
+        const int j = bcol[k];
         float xj[B];
 #pragma unroll
-        for (int f = 0; f < B; ++f) xj[f] = __ldg(x + (size_t)j * B + f);
+        for (int f = 0; f < B; ++f) xj[f] = x[(size_t)j * B + f];
         const float* a = val + (size_t)k * B * B;
 #pragma unroll
         for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) y[f1] += __ldg(a + f1 * B + f2) * xj[f2];
+            for (int f2 = 0; f2 < B; ++f2) y[f1] += a[f1 * B + f2] * xj[f2];
     }
 #pragma unroll
     for (int f = 0; f < B; ++f)
@@ -207,32 +217,143 @@ __global__ void __launch_bounds__(256) k_mgb_resid(int n, const int* __restrict_
     }
 }
 
+// bc_I = sum of r over aggregate I's members, RL lanes (same I and act on all lanes)
 template <int B>
-__global__ void k_mgb_restrict(int nc, const int* __restrict__ mem_ptr, const int* __restrict__ mem,
-                               const float* __restrict__ r, float* __restrict__ bc) {
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= nc) return;
+__device__ __forceinline__ void restrict_row(int I, bool act, int lane, const int* __restrict__ mem_ptr,
+                                             const int* __restrict__ mem, const float* __restrict__ r,
+                                             float* __restrict__ bc) {
     float s[B];
 #pragma unroll
     for (int f = 0; f < B; ++f) s[f] = 0;
-    for (int q = mem_ptr[I]; q < mem_ptr[I + 1]; ++q) {
+    const int q1 = act ? mem_ptr[I + 1] : 0;
+    for (int q = (act ? mem_ptr[I] : 0) + lane; q < q1; q += RL) {
         const int i = mem[q];
 #pragma unroll
         for (int f = 0; f < B; ++f) s[f] += r[(size_t)i * B + f];
     }
 #pragma unroll
-    for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
+    for (int f = 0; f < B; ++f)
+#pragma unroll
+        for (int o = RL / 2; o > 0; o >>= 1) s[f] += __shfl_xor_sync(0xffffffffu, s[f], o, RL);
+    if (act && lane == 0)
+#pragma unroll
+        for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
+}
+
+template <int B>
+__device__ __forceinline__ void prolong_row(int i, const int* __restrict__ agg, const float* __restrict__ xc,
+                                            float* __restrict__ x) {
+    const int I = agg[i];
+    if (I < 0) return;
+#pragma unroll
+    for (int f = 0; f < B; ++f) x[(size_t)i * B + f] += xc[(size_t)I * B + f];
+}
+
+template <int B>
+__global__ void k_mgb_smooth0(int n, const int* __restrict__ bptr, const float* __restrict__ binv,
+                              const float* __restrict__ b, float* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) smooth0_row<B>(i, bptr, binv, b, x);
+}
+
+template <int B, int GN, int POST>
+__global__ void __launch_bounds__(256) k_mgb_resid(int n, const int* __restrict__ bptr, const int* __restrict__ bcol,
+                                                   const float* __restrict__ val, const float* __restrict__ binv,
+                                                   const float* __restrict__ b, const float* __restrict__ x,
+                                                   float* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / GN;
+    resid_row<B, GN, POST>(i < n ? i : 0, i < n, t % GN, bptr, bcol, val, binv, b, x, out);
+}
+
+template <int B>
+__global__ void k_mgb_restrict(int nc, const int* __restrict__ mem_ptr, const int* __restrict__ mem,
+                               const float* __restrict__ r, float* __restrict__ bc) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = t / RL;
+    restrict_row<B>(I < nc ? I : 0, I < nc, t % RL, mem_ptr, mem, r, bc);
 }
 
 template <int B>
 __global__ void k_mgb_prolong(int n, const int* __restrict__ agg, const float* __restrict__ xc,
                               float* __restrict__ x) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int I = agg[i];
-    if (I < 0) return;
-#pragma unroll
-    for (int f = 0; f < B; ++f) x[(size_t)i * B + f] += xc[(size_t)I * B + f];
+    if (i < n) prolong_row<B>(i, agg, xc, x);
+}
+
+// The small coarse levels (each at most TAIL_MAX nodes) in one thread block: down sweeps,
+// coarsest solve and up sweeps with a block barrier between the phases, instead of five
+// launches per level whose run time is launch latency.
+constexpr int TAIL_MAX = 2048;
+constexpr int TAIL_LEVELS = 12;
+constexpr int TAIL_THREADS = 1024;
+
+struct TailLevel {
+    int n;
+    const int *bptr, *bcol;
+    const float *val, *binv;
+    float *b, *x, *xb, *r;
+    const int* agg;                // node -> aggregate of the next tail level
+    const int *mem_ptr, *mem;      // members of the next tail level's aggregates
+};
+
+struct TailArgs {
+    int T;
+    int exact_last;
+    TailLevel lv[TAIL_LEVELS];
+};
+
+template <int B>
+__global__ void __launch_bounds__(TAIL_THREADS) k_mg_tail(TailArgs a) {
+    constexpr int GN = 4;
+    const int tid = threadIdx.x;
+    for (int t = 0; t + 1 < a.T; ++t) {
+        const TailLevel& L = a.lv[t];
+        const TailLevel& C = a.lv[t + 1];
+        for (int i = tid; i < L.n; i += TAIL_THREADS) smooth0_row<B>(i, L.bptr, L.binv, L.b, L.x);
+        __syncthreads();
+        for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
+            const int i = base + tid / GN;
+            resid_row<B, GN, 0>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.binv, L.b, L.x, L.r);
+        }
+        __syncthreads();
+        for (int base = 0; base < C.n; base += TAIL_THREADS / RL) {
+            const int I = base + tid / RL;
+            restrict_row<B>(I < C.n ? I : 0, I < C.n, tid % RL, L.mem_ptr, L.mem, L.r, C.b);
+        }
+        __syncthreads();
+    }
+    {
+        const TailLevel& Z = a.lv[a.T - 1];
+        if (a.exact_last) {
+            for (int i = tid; i < Z.n; i += TAIL_THREADS) smooth0_row<B>(i, Z.bptr, Z.binv, Z.b, Z.xb);
+        } else {  // four damped sweeps, ping-pong x -> xb -> x ...; the result goes to xb
+            for (int i = tid; i < Z.n; i += TAIL_THREADS) smooth0_row<B>(i, Z.bptr, Z.binv, Z.b, Z.x);
+            for (int sweep = 0; sweep < 4; ++sweep) {
+                __syncthreads();
+                const float* from = sweep % 2 == 0 ? Z.x : Z.xb;
+                float* to = sweep % 2 == 0 ? Z.xb : Z.x;
+                for (int base = 0; base < Z.n; base += TAIL_THREADS / GN) {
+                    const int i = base + tid / GN;
+                    resid_row<B, GN, 1>(i < Z.n ? i : 0, i < Z.n, tid % GN, Z.bptr, Z.bcol, Z.val, Z.binv, Z.b, from, to);
+                }
+            }
+            __syncthreads();
+            for (int i = tid; i < Z.n * B; i += TAIL_THREADS) Z.xb[i] = Z.x[i];
+        }
+    }
+    __syncthreads();
+    for (int t = a.T - 2; t >= 0; --t) {
+        const TailLevel& L = a.lv[t];
+        const TailLevel& C = a.lv[t + 1];
+        for (int i = tid; i < L.n; i += TAIL_THREADS) prolong_row<B>(i, L.agg, C.xb, L.x);
+        __syncthreads();
+        for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
+            const int i = base + tid / GN;
+            resid_row<B, GN, 1>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.binv, L.b, L.x, L.xb);
+        }
+        __syncthreads();
+    }
 }
 
 // ---- numeric setup ------------------------------------------------------------------------------
@@ -520,15 +641,19 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
         k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, out0);
         return;
     }
+    // levels lt.. are small enough for the single-block tail
+    int lt = L;
+    while (lt > 0 && c->mg[lt - 1].n <= TAIL_MAX && L - (lt - 1) <= TAIL_LEVELS) --lt;
     // down
     k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
     k_mg0_resid<DIM, 0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, r0);
     {
         MgLevel& L1 = c->mg[0];
-        k_mg0_restrict<DIM><<<div_up(L1.n, BLOCK), BLOCK, 0, s>>>(L1.n, ptr<int>(L1.mem_ptr), ptr<int>(L1.mem), N, r0,
-                                                                  ptr<float>(L1.b));
+        k_mg0_restrict<DIM><<<div_up((long long)L1.n * RL, BLOCK), BLOCK, 0, s>>>(
+            L1.n, ptr<int>(L1.mem_ptr), ptr<int>(L1.mem), N, r0, ptr<float>(L1.b));
     }
-    for (int l = 0; l + 1 < L; ++l) {
+    const int ldown = lt < L ? lt : L - 1;  // levels below this one are handled below
+    for (int l = 0; l < ldown; ++l) {
         MgLevel& A = c->mg[l];
         MgLevel& C = c->mg[l + 1];
         const int gl = div_up((long long)A.n * GNB, 256);
@@ -536,31 +661,52 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
                                                               ptr<float>(A.x));
         k_mgb_resid<B, GNB, 0><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
                                                   ptr<float>(A.binv), ptr<float>(A.b), ptr<float>(A.x), ptr<float>(A.r));
-        k_mgb_restrict<B><<<div_up(C.n, BLOCK), BLOCK, 0, s>>>(C.n, ptr<int>(C.mem_ptr), ptr<int>(C.mem),
-                                                               ptr<float>(A.r), ptr<float>(C.b));
+        k_mgb_restrict<B><<<div_up((long long)C.n * RL, BLOCK), BLOCK, 0, s>>>(C.n, ptr<int>(C.mem_ptr), ptr<int>(C.mem),
+                                                                               ptr<float>(A.r), ptr<float>(C.b));
     }
-    // coarsest: exact block solve when block diagonal, else four damped sweeps
-    {
-        MgLevel& Z = c->mg[L - 1];
-        if (Z.nnzb == Z.n) {
-            k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
-                                                                  ptr<float>(Z.b), ptr<float>(Z.xb));
-        } else {
-            const int gl = div_up((long long)Z.n * GNB, 256);
-            k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
-                                                                  ptr<float>(Z.b), ptr<float>(Z.x));
-            for (int sweep = 0; sweep < 4; ++sweep) {
-                float* from = ptr<float>(sweep % 2 == 0 ? Z.x : Z.xb);
-                float* to = ptr<float>(sweep % 2 == 0 ? Z.xb : Z.x);
-                k_mgb_resid<B, GNB, 1><<<gl, 256, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<int>(Z.bcol), ptr<float>(Z.val),
-                                                          ptr<float>(Z.binv), ptr<float>(Z.b), from, to);
+    MgLevel& Z = c->mg[L - 1];
+    if (lt < L) {
+        TailArgs ta{};
+        ta.T = L - lt;
+        ta.exact_last = Z.nnzb == Z.n;
+        for (int t = 0; t < ta.T; ++t) {
+            MgLevel& A = c->mg[lt + t];
+            TailLevel& tl = ta.lv[t];
+            tl.n = A.n;
+            tl.bptr = ptr<int>(A.bptr);
+            tl.bcol = ptr<int>(A.bcol);
+            tl.val = ptr<float>(A.val);
+            tl.binv = ptr<float>(A.binv);
+            tl.b = ptr<float>(A.b);
+            tl.x = ptr<float>(A.x);
+            tl.xb = ptr<float>(A.xb);
+            tl.r = ptr<float>(A.r);
+            if (t + 1 < ta.T) {
+                MgLevel& C = c->mg[lt + t + 1];
+                tl.agg = ptr<int>(C.agg);
+                tl.mem_ptr = ptr<int>(C.mem_ptr);
+                tl.mem = ptr<int>(C.mem);
             }
-            // four sweeps end in Z.x: copy the result slot
-            cudaMemcpyAsync(Z.xb.p, Z.x.p, sizeof(float) * (size_t)Z.n * B, cudaMemcpyDeviceToDevice, s);
         }
+        k_mg_tail<B><<<1, TAIL_THREADS, 0, s>>>(ta);
+    } else if (Z.nnzb == Z.n) {  // coarsest: exact block solve when block diagonal
+        k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
+                                                              ptr<float>(Z.b), ptr<float>(Z.xb));
+    } else {  // else four damped sweeps
+        const int gl = div_up((long long)Z.n * GNB, 256);
+        k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
+                                                              ptr<float>(Z.b), ptr<float>(Z.x));
+        for (int sweep = 0; sweep < 4; ++sweep) {
+            float* from = ptr<float>(sweep % 2 == 0 ? Z.x : Z.xb);
+            float* to = ptr<float>(sweep % 2 == 0 ? Z.xb : Z.x);
+            k_mgb_resid<B, GNB, 1><<<gl, 256, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<int>(Z.bcol), ptr<float>(Z.val),
+                                                      ptr<float>(Z.binv), ptr<float>(Z.b), from, to);
+        }
+        // four sweeps end in Z.x: copy the result slot
+        cudaMemcpyAsync(Z.xb.p, Z.x.p, sizeof(float) * (size_t)Z.n * B, cudaMemcpyDeviceToDevice, s);
     }
     // up
-    for (int l = L - 2; l >= 0; --l) {
+    for (int l = ldown - 1; l >= 0; --l) {
         MgLevel& A = c->mg[l];
         MgLevel& C = c->mg[l + 1];
         const int gl = div_up((long long)A.n * GNB, 256);
