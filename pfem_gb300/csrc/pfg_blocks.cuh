@@ -1,9 +1,10 @@
-// FP32 node-pair block products shared by the mixed incompressible Krylov solver
-// (pfg_pspg_mixed.cu) and the multigrid preconditioner (pfg_mg.cu).  Header-only device code.
+// Node-pair block products shared by the mixed incompressible Krylov solver (pfg_pspg_mixed.cu)
+// and the multigrid preconditioner (pfg_mg.cu).  Header-only device code.
 //
-// Layout: the scaled FP32 system is stored as one (d+1)x(d+1) block per node pair p = (n, m)
-// of the adjacency, p = nbr_ptr[n] + rank of m in n's sorted neighbour list, row-major inside
-// the block (k_mx_scale_bsr).
+// Layout: the scaled system is stored as one (d+1)x(d+1) block per node pair p = (n, m) of the
+// adjacency, p = nbr_ptr[n] + rank of m in n's sorted neighbour list, row-major inside the block
+// (k_mx_scale_bsr): in FP32 for the Krylov products and, for the multigrid's level-0 sweeps, a
+// bfloat16 copy (FP32 range, 8-bit significand; accumulation stays FP32).
 #pragma once
 
 #include "pfg_device.cuh"
@@ -46,6 +47,49 @@ __device__ __forceinline__ void block_row_f32(int n, bool act, int N, const int*
             for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
                 for (int f2 = 0; f2 < B; ++f2) y[f1] += __ldg(a + f1 * B + f2) * xm[f2];
+        }
+    }
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int o = GN / 2; o > 0; o >>= 1) y[f1] += __shfl_xor_sync(0xffffffffu, y[f1], o, GN);
+}
+
+// bfloat16 (stored as its 16 bits) -> FP32: the upper half of an FP32 bit pattern
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+// The same block-row product with the bfloat16 copy of the blocks: 3D blocks are 32 bytes, read
+// as two 16-byte loads.
+template <int DIM, int GN>
+__device__ __forceinline__ void block_row_bf16(int n, bool act, int N, const int* __restrict__ nbr_ptr,
+                                               const int* __restrict__ nbr, const uint16_t* __restrict__ blk,
+                                               const float* __restrict__ x, int lane, float (&y)[DIM + 1]) {
+    constexpr int B = DIM + 1;
+#pragma unroll
+    for (int f = 0; f < B; ++f) y[f] = 0;
+    const int b0 = act ? nbr_ptr[n] : 0;
+    const int b1 = act ? nbr_ptr[n + 1] : 0;
+    for (int p = b0 + lane; p < b1; p += GN) {
+        const int mn = __ldg(nbr + p);
+        float xm[B];
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(x + (size_t)f2 * N + mn);
+        if constexpr (B == 4) {
+            const uint4* a4 = reinterpret_cast<const uint4*>(blk + (size_t)p * 16);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint4 w = __ldg(a4 + h);  // rows 2h and 2h + 1
+                y[2 * h] += bf16_lo(w.x) * xm[0] + bf16_hi(w.x) * xm[1] + bf16_lo(w.y) * xm[2] + bf16_hi(w.y) * xm[3];
+                y[2 * h + 1] +=
+                    bf16_lo(w.z) * xm[0] + bf16_hi(w.z) * xm[1] + bf16_lo(w.w) * xm[2] + bf16_hi(w.w) * xm[3];
+            }
+        } else {
+            const uint16_t* a = blk + (size_t)p * B * B;
+#pragma unroll
+            for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+                for (int f2 = 0; f2 < B; ++f2) y[f1] += bf16_lo(__ldg(a + f1 * B + f2)) * xm[f2];
         }
     }
 #pragma unroll

@@ -140,6 +140,7 @@ struct pfg_ctx {
     int n_mg = 0;
     pfg::DBuf mg_x0, mg_r0;
     pfg::DBuf mg_in64;     // FP64 correction solves: FP32 scaled input and output of the cycle
+    pfg::DBuf val16;       // bfloat16 copy of the node-pair blocks (level-0 multigrid sweeps)
 };
 
 namespace pfg {

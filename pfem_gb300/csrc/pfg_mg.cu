@@ -8,7 +8,9 @@
 // Jacobi apply and makes the count nearly mesh independent.
 //
 // Hierarchy (built on the host once per mesh upload, from the node adjacency only):
-//   * level 0 is the assembled system: the FP32 scaled values S A S in node-pair blocks;
+//   * level 0 is the assembled system: the scaled values S A S in node-pair blocks, read by the
+//     sweeps from a bfloat16 copy (half the bytes of FP32; a smoother needs no more digits,
+//     and the Krylov products keep the FP32 blocks);
 //   * each coarser level aggregates the nodes of the finer one: greedy, in node order, a node
 //     whose neighbours are all unaggregated starts an aggregate with them; every node left
 //     joins the aggregate of its first aggregated neighbour.  Nodes without neighbours (free
@@ -71,7 +73,7 @@ __global__ void k_mg0_smooth0(int N, const int* __restrict__ nbr_ptr, const floa
 // without neighbours (already solved exactly).
 template <int DIM, int POST>
 __global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict__ nbr_ptr,
-                                                   const int* __restrict__ nbr, const float* __restrict__ blk,
+                                                   const int* __restrict__ nbr, const uint16_t* __restrict__ blk,
                                                    const float* __restrict__ binv, const float* __restrict__ b,
                                                    const float* __restrict__ x, float* __restrict__ out) {
     constexpr int B = DIM + 1;
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict_
     const int n = t / GN, lane = t % GN;
     const bool act = n < N;
     float y[B];
-    block_row_f32<DIM, GN>(act ? n : 0, act, N, nbr_ptr, nbr, blk, x, lane, y);
+    block_row_bf16<DIM, GN>(act ? n : 0, act, N, nbr_ptr, nbr, blk, x, lane, y);
     if (!act || lane != 0) return;
     float r[B];
 #pragma unroll
@@ -633,7 +635,7 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     float* r0 = ptr<float>(c->mg_r0);
     const int* nptr = ptr<int>(c->nbr_ptr);
     const int* nbr = ptr<int>(c->nbr);
-    const float* v0 = ptr<float>(c->val32);
+    const uint16_t* v0 = ptr<uint16_t>(c->val16);  // level-0 sweeps read the bfloat16 blocks
     const int L = c->n_mg;
     const int g0 = div_up(N, BLOCK), g0l = div_up((long long)N * GN0, 256);
     if (L == 0) {  // no coarse level: two damped block-Jacobi sweeps

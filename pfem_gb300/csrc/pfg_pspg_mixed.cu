@@ -19,6 +19,7 @@
 // instance, deterministically, by the last segment of that instance to finish.  Instances
 // carry their own rho, mu, dt, Picard counters and Krylov scalars; converged or failed
 // instances drop out of the launches while the others keep iterating.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -262,7 +263,7 @@ template <int DIM>
 __global__ void k_mx_scale_bsr(int P, int N, const int* __restrict__ pair_node, const int* __restrict__ nbr_ptr,
                                const int* __restrict__ nbr, const int* __restrict__ rp,
                                const double* __restrict__ val, const double* __restrict__ scale, Mx m,
-                               float* __restrict__ blk) {
+                               float* __restrict__ blk, uint16_t* __restrict__ blk16) {
     constexpr int B = DIM + 1;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
@@ -291,6 +292,11 @@ __global__ void k_mx_scale_bsr(int P, int N, const int* __restrict__ pair_node, 
     float* dst = blk + (size_t)p * B * B;
 #pragma unroll
     for (int e = 0; e < B * B; ++e) dst[e] = out[e];
+    if (blk16) {
+        uint16_t* d16 = blk16 + (size_t)p * B * B;
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) d16[e] = __bfloat16_as_ushort(__float2bfloat16_rn(out[e]));
+    }
 }
 
 // ---- node-block Jacobi preconditioner --------------------------------------------------------
@@ -865,7 +871,8 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     k_mx_scale_bsr<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(c->P, N, ptr<int>(c->pair_node),
                                                                       ptr<int>(c->nbr_ptr), ptr<int>(c->nbr),
                                                                       ptr<int>(c->row_ptr), ptr<double>(c->val), scale,
-                                                                      m, ptr<float>(c->val32));
+                                                                      m, ptr<float>(c->val32),
+                                                                      c->n_mg > 0 ? ptr<uint16_t>(c->val16) : nullptr);
     k_mx_binv<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->row_ptr), ptr<double>(c->val),
                                                               ptr<int>(c->diag_pos), scale, ptr<float>(c->binv32),
                                                               ptr<double>(c->binv), m);
@@ -1247,7 +1254,9 @@ int mx_alloc(pfg_ctx* c) {
         return rc;
     c->n_mg = 0;
     if (c->prm.preconditioner == PFG_PC_MULTIGRID) {
-        if ((rc = mg_setup(c)) || (rc = ensure(c, c->mg_in64, sizeof(float) * 2 * R))) return rc;
+        if ((rc = mg_setup(c)) || (rc = ensure(c, c->mg_in64, sizeof(float) * 2 * R)) ||
+            (rc = ensure(c, c->val16, sizeof(uint16_t) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))))
+            return rc;
         // the cycle runs over every node: keep the rows of instances not in FP64 mode finite
         PFG_CUDA(c, cudaMemsetAsync(c->mg_in64.p, 0, sizeof(float) * 2 * R, c->stream));
     }
