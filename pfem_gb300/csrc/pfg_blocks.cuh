@@ -4,7 +4,14 @@
 // Layout: the scaled system is stored as one (d+1)x(d+1) block per node pair p = (n, m) of the
 // adjacency, p = nbr_ptr[n] + rank of m in n's sorted neighbour list, row-major inside the block
 // (k_mx_scale_bsr): in FP32 for the Krylov products and, for the multigrid's level-0 sweeps, a
-// bfloat16 copy (FP32 range, 8-bit significand; accumulation stays FP32).
+// bfloat16 copy (FP32 range, 8-bit significand; accumulation stays FP32) whose rows are padded
+// to four values (bf16_stride), so every row is one 8-byte load.
+
+// bfloat16 values per block of the copy: B rows of 4 (3D: the 4x4 block itself)
+template <int B>
+constexpr int bf16_stride() {
+    return B * 4;
+}
 #pragma once
 
 #include "pfg_device.cuh"
@@ -60,7 +67,7 @@ __device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w 
 __device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
 
 // The same block-row product with the bfloat16 copy of the blocks: 3D blocks are 32 bytes, read
-// as two 16-byte loads.
+// as two 16-byte loads; 2D blocks are three padded rows of 8 bytes.
 template <int DIM, int GN>
 __device__ __forceinline__ void block_row_bf16(int n, bool act, int N, const int* __restrict__ nbr_ptr,
                                                const int* __restrict__ nbr, const uint16_t* __restrict__ blk,
@@ -85,11 +92,12 @@ __device__ __forceinline__ void block_row_bf16(int n, bool act, int N, const int
                     bf16_lo(w.z) * xm[0] + bf16_hi(w.z) * xm[1] + bf16_lo(w.w) * xm[2] + bf16_hi(w.w) * xm[3];
             }
         } else {
-            const uint16_t* a = blk + (size_t)p * B * B;
+            const uint2* a2 = reinterpret_cast<const uint2*>(blk + (size_t)p * bf16_stride<B>());
 #pragma unroll
-            for (int f1 = 0; f1 < B; ++f1)
-#pragma unroll
-                for (int f2 = 0; f2 < B; ++f2) y[f1] += bf16_lo(__ldg(a + f1 * B + f2)) * xm[f2];
+            for (int f1 = 0; f1 < B; ++f1) {
+                const uint2 w = __ldg(a2 + f1);  // row f1: (a0, a1 | a2, pad)
+                y[f1] += bf16_lo(w.x) * xm[0] + bf16_hi(w.x) * xm[1] + bf16_lo(w.y) * xm[2];
+            }
         }
     }
 #pragma unroll

@@ -293,9 +293,12 @@ __global__ void k_mx_scale_bsr(int P, int N, const int* __restrict__ pair_node, 
 #pragma unroll
     for (int e = 0; e < B * B; ++e) dst[e] = out[e];
     if (blk16) {
-        uint16_t* d16 = blk16 + (size_t)p * B * B;
+        uint16_t* d16 = blk16 + (size_t)p * bf16_stride<B>();
 #pragma unroll
-        for (int e = 0; e < B * B; ++e) d16[e] = __bfloat16_as_ushort(__float2bfloat16_rn(out[e]));
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < 4; ++f2)
+                d16[f1 * 4 + f2] = f2 < B ? __bfloat16_as_ushort(__float2bfloat16_rn(out[f1 * B + f2])) : (uint16_t)0;
     }
 }
 
@@ -1255,7 +1258,7 @@ int mx_alloc(pfg_ctx* c) {
     c->n_mg = 0;
     if (c->prm.preconditioner == PFG_PC_MULTIGRID) {
         if ((rc = mg_setup(c)) || (rc = ensure(c, c->mg_in64, sizeof(float) * 2 * R)) ||
-            (rc = ensure(c, c->val16, sizeof(uint16_t) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))))
+            (rc = ensure(c, c->val16, sizeof(uint16_t) * (size_t)std::max(c->P, 1) * (c->dim + 1) * 4)))
             return rc;
         // the cycle runs over every node: keep the rows of instances not in FP64 mode finite
         PFG_CUDA(c, cudaMemsetAsync(c->mg_in64.p, 0, sizeof(float) * 2 * R, c->stream));
