@@ -283,10 +283,12 @@ __global__ void k_mgb_prolong(int n, const int* __restrict__ agg, const float* _
     if (i < n) prolong_row<B>(i, agg, xc, x);
 }
 
-// The small coarse levels (each at most TAIL_MAX nodes) in one thread block: down sweeps,
-// coarsest solve and up sweeps with a block barrier between the phases, instead of five
-// launches per level whose run time is launch latency.
+// The small coarse levels (at most TAIL_MAX nodes and TAIL_BYTES of blocks each) in one thread
+// block: down sweeps, coarsest solve and up sweeps with a block barrier between the phases,
+// instead of five launches per level whose run time is launch latency.  Larger levels stay
+// with the whole GPU: one block streams only a few hundred GB/s.
 constexpr int TAIL_MAX = 2048;
+constexpr size_t TAIL_BYTES = 256 << 10;
 constexpr int TAIL_LEVELS = 12;
 constexpr int TAIL_THREADS = 1024;
 
@@ -645,7 +647,9 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     }
     // levels lt.. are small enough for the single-block tail
     int lt = L;
-    while (lt > 0 && c->mg[lt - 1].n <= TAIL_MAX && L - (lt - 1) <= TAIL_LEVELS) --lt;
+    while (lt > 0 && c->mg[lt - 1].n <= TAIL_MAX && (size_t)c->mg[lt - 1].nnzb * B * B * sizeof(float) <= TAIL_BYTES &&
+           L - (lt - 1) <= TAIL_LEVELS)
+        --lt;
     // down
     k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
     k_mg0_resid<DIM, 0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, r0);
