@@ -297,7 +297,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot, &c->binv32, &c->node_inst,
                     &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt, &c->mx_scale,
                     &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force,
-                    &c->mg_x0, &c->mg_r0, &c->mg_in64, &c->val16};
+                    &c->mg_x0, &c->mg_in64, &c->val16};
     wc_release_graphs(c);
     mg_release(c);
     mx_release_graph(c);

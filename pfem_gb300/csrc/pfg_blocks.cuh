@@ -67,11 +67,13 @@ __device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w 
 __device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
 
 // The same block-row product with the bfloat16 copy of the blocks: 3D blocks are 32 bytes, read
-// as two 16-byte loads; 2D blocks are three padded rows of 8 bytes.
-template <int DIM, int GN>
-__device__ __forceinline__ void block_row_bf16(int n, bool act, int N, const int* __restrict__ nbr_ptr,
+// as two 16-byte loads; 2D blocks are three padded rows of 8 bytes.  The iterate comes from a
+// functor, xf.load(m, v) filling v with the d+1 values at node m, so a multigrid sweep can read
+// a prolonged coarse correction directly.
+template <int DIM, int GN, class XF>
+__device__ __forceinline__ void block_row_bf16(int n, bool act, const int* __restrict__ nbr_ptr,
                                                const int* __restrict__ nbr, const uint16_t* __restrict__ blk,
-                                               const float* __restrict__ x, int lane, float (&y)[DIM + 1]) {
+                                               const XF& xf, int lane, float (&y)[DIM + 1]) {
     constexpr int B = DIM + 1;
 #pragma unroll
     for (int f = 0; f < B; ++f) y[f] = 0;
@@ -80,8 +82,7 @@ __device__ __forceinline__ void block_row_bf16(int n, bool act, int N, const int
     for (int p = b0 + lane; p < b1; p += GN) {
         const int mn = __ldg(nbr + p);
         float xm[B];
-#pragma unroll
-        for (int f2 = 0; f2 < B; ++f2) xm[f2] = __ldg(x + (size_t)f2 * N + mn);
+        xf.load(mn, xm);
         if constexpr (B == 4) {
             const uint4* a4 = reinterpret_cast<const uint4*>(blk + (size_t)p * 16);
 #pragma unroll

@@ -56,7 +56,7 @@ struct MgLevel {
     DBuf bptr, bcol, bdiag;
     DBuf gptr, glist;      // Galerkin gather list of each block (finer-level block ids)
     DBuf val, binv;        // blocks, diagonal-block inverses
-    DBuf x, xb, b, r;      // cycle vectors
+    DBuf x, xb, b;         // cycle vectors
 };
 
 }  // namespace pfg
@@ -138,7 +138,7 @@ struct pfg_ctx {
     // the level-0 cycle vectors
     std::vector<pfg::MgLevel> mg;
     int n_mg = 0;
-    pfg::DBuf mg_x0, mg_r0;
+    pfg::DBuf mg_x0;
     pfg::DBuf mg_in64;     // FP64 correction solves: FP32 scaled input and output of the cycle
     pfg::DBuf val16;       // bfloat16 copy of the node-pair blocks (level-0 multigrid sweeps)
 };

@@ -24,7 +24,8 @@
 //     instance, is one aggregate): its block inverse is the exact coarse solve.
 // Coarse levels are stored as block CSR with node-major (d+1)-vectors.
 //
-// Cycle: V(1,1) with damped node-block Jacobi (omega = 0.7 in 2D, 0.5 in 3D) on every level; the block
+// Cycle: V(0,2) in 2D, V(1,1) in 3D, with damped node-block Jacobi (omega = 0.7 in 2D, 0.5 in
+// 3D) on every level; the block
 // inverses are computed in FP64 from the FP32 blocks (the PSPG block's Schur complement cancels
 // heavily) and stored in FP32.  The values are refreshed after every assembly (one gather pass
 // over the FP32 matrix plus the coarse levels).
@@ -48,15 +49,67 @@ __host__ __device__ constexpr float mg_omega(int B) { return B == 3 ? 0.7f : 0.5
 
 // ---- level 0 (field-major CSR) ---------------------------------------------------------------
 
-// x = omega Binv b (pre-smoothing from a zero guess); x = Binv b, the exact solve, for a node
-// without neighbours
+// Iterate readers for the sweeps.  X0/XB: the current iterate (level 0 field-major, coarse
+// levels node-major).  P0/PB: the prolonged coarse correction P xc, the iterate right after the
+// coarse-grid correction (the cycle has no pre-smoothing, so the iterate is zero before it).
+template <int B>
+struct X0 {
+    const float* x;
+    int N;
+    __device__ __forceinline__ void load(int m, float (&v)[B]) const {
+#pragma unroll
+        for (int f = 0; f < B; ++f) v[f] = __ldg(x + (size_t)f * N + m);
+    }
+};
+template <int B>
+struct XB {
+    const float* x;
+    __device__ __forceinline__ void load(int m, float (&v)[B]) const {
+#pragma unroll
+        for (int f = 0; f < B; ++f) v[f] = x[(size_t)m * B + f];
+    }
+};
+template <int B>
+struct PC {
+    const int* agg;
+    const float* xc;
+    __device__ __forceinline__ void load(int m, float (&v)[B]) const {
+        const int I = agg[m];
+#pragma unroll
+        for (int f = 0; f < B; ++f) v[f] = I >= 0 ? xc[(size_t)I * B + f] : 0.0f;
+    }
+};
+
+// x + P xc: the pre-smoothed iterate plus the prolonged coarse correction (V(1,1) cycles)
+template <int B, bool FIELD_MAJOR>
+struct XPC {
+    const float* x;
+    int N;
+    const int* agg;
+    const float* xc;
+    __device__ __forceinline__ void load(int m, float (&v)[B]) const {
+        const int I = agg[m];
+#pragma unroll
+        for (int f = 0; f < B; ++f) {
+            const float xv = FIELD_MAJOR ? __ldg(x + (size_t)f * N + m) : x[(size_t)m * B + f];
+            v[f] = I >= 0 ? xv + xc[(size_t)I * B + f] : xv;
+        }
+    }
+};
+
+// Lanes per aggregate of the restrictions: aggregates hold ~7 (2D) to ~20 (3D) members, and a
+// single thread summing them is a chain of dependent loads.
+constexpr int RL = 8;
+
+// x = omega Binv b, the first sweep from a zero iterate (V(1,1) cycles); x = Binv b, the exact
+// solve, for a node without neighbours
 template <int DIM>
 __global__ void k_mg0_smooth0(int N, const int* __restrict__ nbr_ptr, const float* __restrict__ binv,
                               const float* __restrict__ b, float* __restrict__ x) {
     constexpr int B = DIM + 1;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
-    const float w = nbr_ptr[n + 1] - nbr_ptr[n] == 1 ? 1.0f : mg_omega(DIM + 1);
+    const float w = nbr_ptr[n + 1] - nbr_ptr[n] == 1 ? 1.0f : mg_omega(B);
     float v[B];
 #pragma unroll
     for (int f = 0; f < B; ++f) v[f] = b[(size_t)f * N + n];
@@ -69,44 +122,53 @@ __global__ void k_mg0_smooth0(int N, const int* __restrict__ nbr_ptr, const floa
     }
 }
 
-// POST = 0: r = b - A x.  POST = 1: out = x + omega Binv (b - A x), or out = x for a node
-// without neighbours (already solved exactly).
-template <int DIM, int POST>
-__global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict__ nbr_ptr,
-                                                   const int* __restrict__ nbr, const uint16_t* __restrict__ blk,
-                                                   const float* __restrict__ binv, const float* __restrict__ b,
-                                                   const float* __restrict__ x, float* __restrict__ out) {
+// r = b - A x at level 0 (V(1,1) cycles), x read through xf
+template <int DIM, class XF>
+__global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                                                   const uint16_t* __restrict__ blk, const float* __restrict__ b, XF xf,
+                                                   float* __restrict__ r) {
     constexpr int B = DIM + 1;
     constexpr int GN = node_lanes<DIM>();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = t / GN, lane = t % GN;
     const bool act = n < N;
     float y[B];
-    block_row_bf16<DIM, GN>(act ? n : 0, act, N, nbr_ptr, nbr, blk, x, lane, y);
+    block_row_bf16<DIM, GN>(act ? n : 0, act, nbr_ptr, nbr, blk, xf, lane, y);
     if (!act || lane != 0) return;
-    float r[B];
 #pragma unroll
-    for (int f = 0; f < B; ++f) r[f] = b[(size_t)f * N + n] - y[f];
-    if (POST == 0) {
-#pragma unroll
-        for (int f = 0; f < B; ++f) out[(size_t)f * N + n] = r[f];
-    } else if (nbr_ptr[n + 1] - nbr_ptr[n] == 1) {
-#pragma unroll
-        for (int f = 0; f < B; ++f) out[(size_t)f * N + n] = x[(size_t)f * N + n];
-    } else {
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1) {
-            float s = 0;
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) s += binv[(size_t)(f1 * B + f2) * N + n] * r[f2];
-            out[(size_t)f1 * N + n] = x[(size_t)f1 * N + n] + mg_omega(B) * s;
-        }
-    }
+    for (int f = 0; f < B; ++f) r[(size_t)f * N + n] = b[(size_t)f * N + n] - y[f];
 }
 
-// Lanes per aggregate of the restrictions: aggregates hold ~7 (2D) to ~20 (3D) members, and a
-// single thread summing them is a chain of dependent loads.
-constexpr int RL = 8;
+// One smoothing sweep at level 0, node n over GN lanes: out_n = x_n + omega Binv_n (b - A x)_n,
+// the iterate x read through xf.  A node without neighbours is solved exactly: out_n = Binv_n b_n.
+template <int DIM, class XF>
+__global__ void __launch_bounds__(256) k_mg0_post(int N, const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                                                  const uint16_t* __restrict__ blk, const float* __restrict__ binv,
+                                                  const float* __restrict__ b, XF xf, float* __restrict__ out) {
+    constexpr int B = DIM + 1;
+    constexpr int GN = node_lanes<DIM>();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = t / GN, lane = t % GN;
+    const bool act = n < N;
+    float y[B];
+    block_row_bf16<DIM, GN>(act ? n : 0, act, nbr_ptr, nbr, blk, xf, lane, y);
+    if (!act || lane != 0) return;
+    const bool lone = nbr_ptr[n + 1] - nbr_ptr[n] == 1;
+    float xn[B], r[B];
+    xf.load(n, xn);
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        const float bv = b[(size_t)f * N + n];
+        r[f] = lone ? bv : bv - y[f];
+    }
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        float s = 0;
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) s += binv[(size_t)(f1 * B + f2) * N + n] * r[f2];
+        out[(size_t)f1 * N + n] = lone ? s : xn[f1] + mg_omega(B) * s;
+    }
+}
 
 // bc[I] = sum over the members n of aggregate I of r[n] (level 0: field-major r); RL lanes per
 // aggregate, strided over the members, then a fixed shuffle tree.
@@ -135,24 +197,82 @@ __global__ void k_mg0_restrict(int nc, const int* __restrict__ mem_ptr, const in
         for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
 }
 
-// x[n] += xc[agg n] (level 0: field-major x)
-template <int DIM>
-__global__ void k_mg0_prolong(int N, const int* __restrict__ agg, const float* __restrict__ xc,
-                              float* __restrict__ x) {
-    constexpr int B = DIM + 1;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    const int I = agg[n];
-    if (I < 0) return;
-#pragma unroll
-    for (int f = 0; f < B; ++f) x[(size_t)f * N + n] += xc[(size_t)I * B + f];
-}
-
 // ---- coarse levels (block CSR, node-major vectors) --------------------------------------------
 // Row operations as device functions, used by the one-level kernels and by the single-block
 // kernel that runs the small coarse levels (k_mg_tail).
 
-// x_i = w Binv_i b_i; w = 1 (exact) for a block row without off-diagonal blocks
+// One sweep on block row i over GN lanes (all lanes of the group call it with the same i and
+// act): out_i = x_i + omega Binv_i (b - A x)_i; a row without off-diagonal blocks is solved
+// exactly (out_i = Binv_i b_i).
+template <int B, int GN, class XF>
+__device__ __forceinline__ void post_row(int i, bool act, int lane, const int* __restrict__ bptr,
+                                         const int* __restrict__ bcol, const float* __restrict__ val,
+                                         const float* __restrict__ binv, const float* __restrict__ b, const XF& xf,
+                                         float* __restrict__ out) {
+    float y[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) y[f] = 0;
+    const int k0 = act ? bptr[i] : 0, k1 = act ? bptr[i + 1] : 0;
+    for (int k = k0 + lane; k < k1; k += GN) {
+        float xj[B];
+        xf.load(bcol[k], xj);
+        const float* a = val + (size_t)k * B * B;
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) y[f1] += a[f1 * B + f2] * xj[f2];
+    }
+#pragma unroll
+    for (int f = 0; f < B; ++f)
+#pragma unroll
+        for (int o = GN / 2; o > 0; o >>= 1) y[f] += __shfl_xor_sync(0xffffffffu, y[f], o, GN);
+    if (!act || lane != 0) return;
+    const bool lone = k1 - k0 == 1;
+    float xi[B], r[B];
+    xf.load(i, xi);
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        const float bv = b[(size_t)i * B + f];
+        r[f] = lone ? bv : bv - y[f];
+    }
+    const float* bi = binv + (size_t)i * B * B;
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        float s = 0;
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) s += bi[f1 * B + f2] * r[f2];
+        out[(size_t)i * B + f1] = lone ? s : xi[f1] + mg_omega(B) * s;
+    }
+}
+
+// r_i = b_i - (A x)_i over GN lanes (V(1,1) cycles)
+template <int B, int GN, class XF>
+__device__ __forceinline__ void resid_row(int i, bool act, int lane, const int* __restrict__ bptr,
+                                          const int* __restrict__ bcol, const float* __restrict__ val,
+                                          const float* __restrict__ b, const XF& xf, float* __restrict__ r) {
+    float y[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) y[f] = 0;
+    const int k0 = act ? bptr[i] : 0, k1 = act ? bptr[i + 1] : 0;
+    for (int k = k0 + lane; k < k1; k += GN) {
+        float xj[B];
+        xf.load(bcol[k], xj);
+        const float* a = val + (size_t)k * B * B;
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) y[f1] += a[f1 * B + f2] * xj[f2];
+    }
+#pragma unroll
+    for (int f = 0; f < B; ++f)
+#pragma unroll
+        for (int o = GN / 2; o > 0; o >>= 1) y[f] += __shfl_xor_sync(0xffffffffu, y[f], o, GN);
+    if (!act || lane != 0) return;
+#pragma unroll
+    for (int f = 0; f < B; ++f) r[(size_t)i * B + f] = b[(size_t)i * B + f] - y[f];
+}
+
+// x_i = omega Binv_i b_i, the first sweep from zero (exact for a row without off-diagonal blocks)
 template <int B>
 __device__ __forceinline__ void smooth0_row(int i, const int* __restrict__ bptr, const float* __restrict__ binv,
                                             const float* __restrict__ b, float* __restrict__ x) {
@@ -167,55 +287,6 @@ __device__ __forceinline__ void smooth0_row(int i, const int* __restrict__ bptr,
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2) s += bi[f1 * B + f2] * v[f2];
         x[(size_t)i * B + f1] = w * s;
-    }
-}
-
-// Block row i over GN lanes (all lanes of the group call it with the same i and act).
-// POST = 0: r_i = b_i - (A x)_i.  POST = 1: out_i = x_i + omega Binv_i (b - A x)_i, or x_i for a
-// block row without off-diagonal blocks (solved exactly).
-template <int B, int GN, int POST>
-__device__ __forceinline__ void resid_row(int i, bool act, int lane, const int* __restrict__ bptr,
-                                          const int* __restrict__ bcol, const float* __restrict__ val,
-                                          const float* __restrict__ binv, const float* __restrict__ b,
-                                          const float* __restrict__ x, float* __restrict__ out) {
-    float y[B];
-#pragma unroll
-    for (int f = 0; f < B; ++f) y[f] = 0;
-    const int k0 = act ? bptr[i] : 0, k1 = act ? bptr[i + 1] : 0;
-    for (int k = k0 + lane; k < k1; k += GN) {
-        const int j = bcol[k];
-        float xj[B];
-#pragma unroll
-        for (int f = 0; f < B; ++f) xj[f] = x[(size_t)j * B + f];
-        const float* a = val + (size_t)k * B * B;
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1)
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) y[f1] += a[f1 * B + f2] * xj[f2];
-    }
-#pragma unroll
-    for (int f = 0; f < B; ++f)
-#pragma unroll
-        for (int o = GN / 2; o > 0; o >>= 1) y[f] += __shfl_xor_sync(0xffffffffu, y[f], o, GN);
-    if (!act || lane != 0) return;
-    float r[B];
-#pragma unroll
-    for (int f = 0; f < B; ++f) r[f] = b[(size_t)i * B + f] - y[f];
-    if (POST == 0) {
-#pragma unroll
-        for (int f = 0; f < B; ++f) out[(size_t)i * B + f] = r[f];
-    } else if (k1 - k0 == 1) {
-#pragma unroll
-        for (int f = 0; f < B; ++f) out[(size_t)i * B + f] = x[(size_t)i * B + f];
-    } else {
-        const float* bi = binv + (size_t)i * B * B;
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1) {
-            float s = 0;
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) s += bi[f1 * B + f2] * r[f2];
-            out[(size_t)i * B + f1] = x[(size_t)i * B + f1] + mg_omega(B) * s;
-        }
     }
 }
 
@@ -242,13 +313,31 @@ __device__ __forceinline__ void restrict_row(int I, bool act, int lane, const in
         for (int f = 0; f < B; ++f) bc[(size_t)I * B + f] = s[f];
 }
 
+// x_i = Binv_i b_i (the coarsest level, block diagonal)
 template <int B>
-__device__ __forceinline__ void prolong_row(int i, const int* __restrict__ agg, const float* __restrict__ xc,
-                                            float* __restrict__ x) {
-    const int I = agg[i];
-    if (I < 0) return;
+__device__ __forceinline__ void solve_row(int i, const float* __restrict__ binv, const float* __restrict__ b,
+                                          float* __restrict__ x) {
+    float v[B];
 #pragma unroll
-    for (int f = 0; f < B; ++f) x[(size_t)i * B + f] += xc[(size_t)I * B + f];
+    for (int f = 0; f < B; ++f) v[f] = b[(size_t)i * B + f];
+    const float* bi = binv + (size_t)i * B * B;
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        float s = 0;
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) s += bi[f1 * B + f2] * v[f2];
+        x[(size_t)i * B + f1] = s;
+    }
+}
+
+template <int B, class XF>
+__global__ void __launch_bounds__(256) k_mgb_post(int n, const int* __restrict__ bptr, const int* __restrict__ bcol,
+                                                  const float* __restrict__ val, const float* __restrict__ binv,
+                                                  const float* __restrict__ b, XF xf, float* __restrict__ out) {
+    constexpr int GN = 4;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / GN;
+    post_row<B, GN>(i < n ? i : 0, i < n, t % GN, bptr, bcol, val, binv, b, xf, out);
 }
 
 template <int B>
@@ -258,14 +347,14 @@ __global__ void k_mgb_smooth0(int n, const int* __restrict__ bptr, const float* 
     if (i < n) smooth0_row<B>(i, bptr, binv, b, x);
 }
 
-template <int B, int GN, int POST>
+template <int B, class XF>
 __global__ void __launch_bounds__(256) k_mgb_resid(int n, const int* __restrict__ bptr, const int* __restrict__ bcol,
-                                                   const float* __restrict__ val, const float* __restrict__ binv,
-                                                   const float* __restrict__ b, const float* __restrict__ x,
-                                                   float* __restrict__ out) {
+                                                   const float* __restrict__ val, const float* __restrict__ b, XF xf,
+                                                   float* __restrict__ r) {
+    constexpr int GN = 4;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / GN;
-    resid_row<B, GN, POST>(i < n ? i : 0, i < n, t % GN, bptr, bcol, val, binv, b, x, out);
+    resid_row<B, GN>(i < n ? i : 0, i < n, t % GN, bptr, bcol, val, b, xf, r);
 }
 
 template <int B>
@@ -277,16 +366,17 @@ __global__ void k_mgb_restrict(int nc, const int* __restrict__ mem_ptr, const in
 }
 
 template <int B>
-__global__ void k_mgb_prolong(int n, const int* __restrict__ agg, const float* __restrict__ xc,
-                              float* __restrict__ x) {
+__global__ void k_mgb_solve(int n, const float* __restrict__ binv, const float* __restrict__ b,
+                            float* __restrict__ x) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) prolong_row<B>(i, agg, xc, x);
+    if (i < n) solve_row<B>(i, binv, b, x);
 }
 
 // The small coarse levels (at most TAIL_MAX nodes and TAIL_BYTES of blocks each) in one thread
-// block: down sweeps, coarsest solve and up sweeps with a block barrier between the phases,
-// instead of five launches per level whose run time is launch latency.  Larger levels stay
-// with the whole GPU: one block streams only a few hundred GB/s.
+// block: restrictions, coarsest solve and the two sweeps of every level on the way up, with a
+// block barrier between the phases, instead of three launches per level whose run time is
+// launch latency.  Larger levels stay with the whole GPU: one block streams only a few hundred
+// GB/s.
 constexpr int TAIL_MAX = 2048;
 constexpr size_t TAIL_BYTES = 256 << 10;
 constexpr int TAIL_LEVELS = 12;
@@ -296,7 +386,7 @@ struct TailLevel {
     int n;
     const int *bptr, *bcol;
     const float *val, *binv;
-    float *b, *x, *xb, *r;
+    float *b, *x, *xb;
     const int* agg;                // node -> aggregate of the next tail level
     const int *mem_ptr, *mem;      // members of the next tail level's aggregates
 };
@@ -307,54 +397,77 @@ struct TailArgs {
     TailLevel lv[TAIL_LEVELS];
 };
 
+// Cycle shape by block size: V(0,2) in 2D, V(1,1) in 3D (measured on the GPU: V(0,2) took
+// C4 from 294 to 328 instance-steps/s and C1 from 75 to 92 steps/s, but raised C3's Krylov
+// iterations by 13% and cost it 5%).
+template <int B>
+constexpr bool pre_smooth() {
+    return B == 4;
+}
+
 template <int B>
 __global__ void __launch_bounds__(TAIL_THREADS) k_mg_tail(TailArgs a) {
     constexpr int GN = 4;
+    constexpr bool PRE = pre_smooth<B>();
     const int tid = threadIdx.x;
     for (int t = 0; t + 1 < a.T; ++t) {
         const TailLevel& L = a.lv[t];
         const TailLevel& C = a.lv[t + 1];
-        for (int i = tid; i < L.n; i += TAIL_THREADS) smooth0_row<B>(i, L.bptr, L.binv, L.b, L.x);
-        __syncthreads();
-        for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
-            const int i = base + tid / GN;
-            resid_row<B, GN, 0>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.binv, L.b, L.x, L.r);
+        if (PRE) {  // x = omega Binv b; r = b - A x into xb (free until the way up)
+            for (int i = tid; i < L.n; i += TAIL_THREADS) smooth0_row<B>(i, L.bptr, L.binv, L.b, L.x);
+            __syncthreads();
+            for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
+                const int i = base + tid / GN;
+                resid_row<B, GN>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.b, XB<B>{L.x}, L.xb);
+            }
+            __syncthreads();
         }
-        __syncthreads();
         for (int base = 0; base < C.n; base += TAIL_THREADS / RL) {
             const int I = base + tid / RL;
-            restrict_row<B>(I < C.n ? I : 0, I < C.n, tid % RL, L.mem_ptr, L.mem, L.r, C.b);
+            restrict_row<B>(I < C.n ? I : 0, I < C.n, tid % RL, L.mem_ptr, L.mem, PRE ? L.xb : L.b, C.b);
         }
         __syncthreads();
     }
     {
         const TailLevel& Z = a.lv[a.T - 1];
         if (a.exact_last) {
-            for (int i = tid; i < Z.n; i += TAIL_THREADS) smooth0_row<B>(i, Z.bptr, Z.binv, Z.b, Z.xb);
-        } else {  // four damped sweeps, ping-pong x -> xb -> x ...; the result goes to xb
-            for (int i = tid; i < Z.n; i += TAIL_THREADS) smooth0_row<B>(i, Z.bptr, Z.binv, Z.b, Z.x);
+            for (int i = tid; i < Z.n; i += TAIL_THREADS) solve_row<B>(i, Z.binv, Z.b, Z.xb);
+        } else {  // four sweeps from zero, ping-pong xb -> x -> xb ...; the result goes to xb
+            for (int i = tid; i < Z.n * B; i += TAIL_THREADS) Z.xb[i] = 0.0f;
             for (int sweep = 0; sweep < 4; ++sweep) {
                 __syncthreads();
-                const float* from = sweep % 2 == 0 ? Z.x : Z.xb;
-                float* to = sweep % 2 == 0 ? Z.xb : Z.x;
+                const float* from = sweep % 2 == 0 ? Z.xb : Z.x;
+                float* to = sweep % 2 == 0 ? Z.x : Z.xb;
                 for (int base = 0; base < Z.n; base += TAIL_THREADS / GN) {
                     const int i = base + tid / GN;
-                    resid_row<B, GN, 1>(i < Z.n ? i : 0, i < Z.n, tid % GN, Z.bptr, Z.bcol, Z.val, Z.binv, Z.b, from, to);
+                    post_row<B, GN>(i < Z.n ? i : 0, i < Z.n, tid % GN, Z.bptr, Z.bcol, Z.val, Z.binv, Z.b,
+                                    XB<B>{from}, to);
                 }
             }
-            __syncthreads();
-            for (int i = tid; i < Z.n * B; i += TAIL_THREADS) Z.xb[i] = Z.x[i];
         }
     }
     __syncthreads();
     for (int t = a.T - 2; t >= 0; --t) {
         const TailLevel& L = a.lv[t];
         const TailLevel& C = a.lv[t + 1];
-        for (int i = tid; i < L.n; i += TAIL_THREADS) prolong_row<B>(i, L.agg, C.xb, L.x);
-        __syncthreads();
-        for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
-            const int i = base + tid / GN;
-            resid_row<B, GN, 1>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.binv, L.b, L.x, L.xb);
+        if (PRE) {
+            for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
+                const int i = base + tid / GN;
+                post_row<B, GN>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.binv, L.b,
+                                XPC<B, false>{L.x, 0, L.agg, C.xb}, L.xb);
+            }
+        } else {
+            for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
+                const int i = base + tid / GN;
+                post_row<B, GN>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.binv, L.b,
+                                PC<B>{L.agg, C.xb}, L.x);
+            }
+            __syncthreads();
+            for (int base = 0; base < L.n; base += TAIL_THREADS / GN) {
+                const int i = base + tid / GN;
+                post_row<B, GN>(i < L.n ? i : 0, i < L.n, tid % GN, L.bptr, L.bcol, L.val, L.binv, L.b,
+                                XB<B>{L.x}, L.xb);
+            }
         }
         __syncthreads();
     }
@@ -480,7 +593,7 @@ void mg_release(pfg_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (MgLevel& l : c->mg) {
         DBuf* bufs[] = {&l.agg, &l.mem_ptr, &l.mem, &l.bptr, &l.bcol, &l.bdiag, &l.gptr,
-                        &l.glist, &l.val, &l.binv, &l.x, &l.xb, &l.b, &l.r};
+                        &l.glist, &l.val, &l.binv, &l.x, &l.xb, &l.b};
         for (DBuf* b : bufs) {
             c->bytes_in_use -= std::min(c->bytes_in_use, b->cap);
             release(*b);
@@ -496,9 +609,7 @@ int mg_setup(pfg_ctx* c) {
     c->n_mg = 0;
     const int N = c->N, B = c->dim + 1;
     int rc;
-    if ((rc = ensure(c, c->mg_x0, sizeof(float) * (size_t)B * N)) ||
-        (rc = ensure(c, c->mg_r0, sizeof(float) * (size_t)B * N)))
-        return rc;
+    if ((rc = ensure(c, c->mg_x0, sizeof(float) * (size_t)B * N))) return rc;
     // level-0 graph: the node adjacency without self (device lists, sorted)
     std::vector<int> ptr0(N + 1), idx0(c->P);
     PFG_CUDA(c, cudaMemcpyAsync(ptr0.data(), c->nbr_ptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, c->stream));
@@ -586,7 +697,7 @@ int mg_setup(pfg_ctx* c) {
             (rc = ensure(c, L.val, sizeof(float) * (size_t)std::max(nnzb, 1) * B * B)) ||
             (rc = ensure(c, L.binv, sizeof(float) * (size_t)nc * B * B)) ||
             (rc = ensure(c, L.x, sizeof(float) * (size_t)nc * B)) || (rc = ensure(c, L.xb, sizeof(float) * (size_t)nc * B)) ||
-            (rc = ensure(c, L.b, sizeof(float) * (size_t)nc * B)) || (rc = ensure(c, L.r, sizeof(float) * (size_t)nc * B)))
+            (rc = ensure(c, L.b, sizeof(float) * (size_t)nc * B)))
             return rc;
         PFG_CUDA(c, cudaStreamSynchronize(c->stream));  // host vectors go out of scope
         fptr.swap(cptr);
@@ -625,6 +736,11 @@ int mg_numeric(pfg_ctx* c) {
 
 namespace {
 
+// One cycle.  V(0,2) (2D): restrict the right-hand side down to the coarsest level, solve it
+// exactly, and on the way up apply at every level the prolonged correction followed by two
+// damped block-Jacobi sweeps (the first reads the prolonged correction directly).  V(1,1)
+// (3D): one sweep from zero and the residual on the way down, the prolonged correction and one
+// sweep on the way up.  Both read the level's matrix twice per level.
 template <int DIM>
 void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     constexpr int B = DIM + 1;
@@ -634,41 +750,43 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     cudaStream_t s = c->stream;
     const float* binv0 = ptr<float>(c->binv32);
     float* x0 = ptr<float>(c->mg_x0);
-    float* r0 = ptr<float>(c->mg_r0);
     const int* nptr = ptr<int>(c->nbr_ptr);
     const int* nbr = ptr<int>(c->nbr);
     const uint16_t* v0 = ptr<uint16_t>(c->val16);  // level-0 sweeps read the bfloat16 blocks
     const int L = c->n_mg;
-    const int g0 = div_up(N, BLOCK), g0l = div_up((long long)N * GN0, 256);
-    if (L == 0) {  // no coarse level: two damped block-Jacobi sweeps
-        k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
-        k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, out0);
-        return;
-    }
+    const int g0l = div_up((long long)N * GN0, 256);
     // levels lt.. are small enough for the single-block tail
     int lt = L;
     while (lt > 0 && c->mg[lt - 1].n <= TAIL_MAX && (size_t)c->mg[lt - 1].nnzb * B * B * sizeof(float) <= TAIL_BYTES &&
            L - (lt - 1) <= TAIL_LEVELS)
         --lt;
-    // down
-    k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
-    k_mg0_resid<DIM, 0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, r0);
+    constexpr bool PRE = pre_smooth<B>();
+    const int g0 = div_up(N, BLOCK);
+    // down: restrict the right-hand side (V(0,2)) or the residual of one sweep (V(1,1), kept in
+    // out0 / xb until the way up)
     {
         MgLevel& L1 = c->mg[0];
+        if (PRE) {
+            k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
+            k_mg0_resid<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, b0, X0<B>{x0, N}, out0);
+        }
         k_mg0_restrict<DIM><<<div_up((long long)L1.n * RL, BLOCK), BLOCK, 0, s>>>(
-            L1.n, ptr<int>(L1.mem_ptr), ptr<int>(L1.mem), N, r0, ptr<float>(L1.b));
+            L1.n, ptr<int>(L1.mem_ptr), ptr<int>(L1.mem), N, PRE ? out0 : b0, ptr<float>(L1.b));
     }
     const int ldown = lt < L ? lt : L - 1;  // levels below this one are handled below
     for (int l = 0; l < ldown; ++l) {
         MgLevel& A = c->mg[l];
         MgLevel& C = c->mg[l + 1];
-        const int gl = div_up((long long)A.n * GNB, 256);
-        k_mgb_smooth0<B><<<div_up(A.n, BLOCK), BLOCK, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<float>(A.binv), ptr<float>(A.b),
-                                                              ptr<float>(A.x));
-        k_mgb_resid<B, GNB, 0><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
-                                                  ptr<float>(A.binv), ptr<float>(A.b), ptr<float>(A.x), ptr<float>(A.r));
+        if (PRE) {
+            k_mgb_smooth0<B><<<div_up(A.n, BLOCK), BLOCK, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<float>(A.binv),
+                                                                  ptr<float>(A.b), ptr<float>(A.x));
+            k_mgb_resid<B><<<div_up((long long)A.n * GNB, 256), 256, 0, s>>>(
+                A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val), ptr<float>(A.b), XB<B>{ptr<float>(A.x)},
+                ptr<float>(A.xb));
+        }
         k_mgb_restrict<B><<<div_up((long long)C.n * RL, BLOCK), BLOCK, 0, s>>>(C.n, ptr<int>(C.mem_ptr), ptr<int>(C.mem),
-                                                                               ptr<float>(A.r), ptr<float>(C.b));
+                                                                               ptr<float>(PRE ? A.xb : A.b),
+                                                                               ptr<float>(C.b));
     }
     MgLevel& Z = c->mg[L - 1];
     if (lt < L) {
@@ -686,7 +804,6 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
             tl.b = ptr<float>(A.b);
             tl.x = ptr<float>(A.x);
             tl.xb = ptr<float>(A.xb);
-            tl.r = ptr<float>(A.r);
             if (t + 1 < ta.T) {
                 MgLevel& C = c->mg[lt + t + 1];
                 tl.agg = ptr<int>(C.agg);
@@ -696,32 +813,44 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
         }
         k_mg_tail<B><<<1, TAIL_THREADS, 0, s>>>(ta);
     } else if (Z.nnzb == Z.n) {  // coarsest: exact block solve when block diagonal
-        k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
-                                                              ptr<float>(Z.b), ptr<float>(Z.xb));
-    } else {  // else four damped sweeps
+        k_mgb_solve<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<float>(Z.binv), ptr<float>(Z.b), ptr<float>(Z.xb));
+    } else {  // else four sweeps from zero, ending in xb
         const int gl = div_up((long long)Z.n * GNB, 256);
-        k_mgb_smooth0<B><<<div_up(Z.n, BLOCK), BLOCK, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<float>(Z.binv),
-                                                              ptr<float>(Z.b), ptr<float>(Z.x));
+        cudaMemsetAsync(Z.xb.p, 0, sizeof(float) * (size_t)Z.n * B, s);
         for (int sweep = 0; sweep < 4; ++sweep) {
-            float* from = ptr<float>(sweep % 2 == 0 ? Z.x : Z.xb);
-            float* to = ptr<float>(sweep % 2 == 0 ? Z.xb : Z.x);
-            k_mgb_resid<B, GNB, 1><<<gl, 256, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<int>(Z.bcol), ptr<float>(Z.val),
-                                                      ptr<float>(Z.binv), ptr<float>(Z.b), from, to);
+            const float* from = ptr<float>(sweep % 2 == 0 ? Z.xb : Z.x);
+            float* to = ptr<float>(sweep % 2 == 0 ? Z.x : Z.xb);
+            k_mgb_post<B><<<gl, 256, 0, s>>>(Z.n, ptr<int>(Z.bptr), ptr<int>(Z.bcol), ptr<float>(Z.val), ptr<float>(Z.binv),
+                                             ptr<float>(Z.b), XB<B>{from}, to);
         }
-        // four sweeps end in Z.x: copy the result slot
-        cudaMemcpyAsync(Z.xb.p, Z.x.p, sizeof(float) * (size_t)Z.n * B, cudaMemcpyDeviceToDevice, s);
     }
-    // up
+    // up: prolonged correction and the sweeps of every level
     for (int l = ldown - 1; l >= 0; --l) {
         MgLevel& A = c->mg[l];
         MgLevel& C = c->mg[l + 1];
         const int gl = div_up((long long)A.n * GNB, 256);
-        k_mgb_prolong<B><<<div_up(A.n, BLOCK), BLOCK, 0, s>>>(A.n, ptr<int>(C.agg), ptr<float>(C.xb), ptr<float>(A.x));
-        k_mgb_resid<B, GNB, 1><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
-                                                  ptr<float>(A.binv), ptr<float>(A.b), ptr<float>(A.x), ptr<float>(A.xb));
+        if (PRE) {
+            k_mgb_post<B><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
+                                             ptr<float>(A.binv), ptr<float>(A.b),
+                                             XPC<B, false>{ptr<float>(A.x), 0, ptr<int>(C.agg), ptr<float>(C.xb)},
+                                             ptr<float>(A.xb));
+        } else {
+            k_mgb_post<B><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
+                                             ptr<float>(A.binv), ptr<float>(A.b), PC<B>{ptr<int>(C.agg), ptr<float>(C.xb)},
+                                             ptr<float>(A.x));
+            k_mgb_post<B><<<gl, 256, 0, s>>>(A.n, ptr<int>(A.bptr), ptr<int>(A.bcol), ptr<float>(A.val),
+                                             ptr<float>(A.binv), ptr<float>(A.b), XB<B>{ptr<float>(A.x)},
+                                             ptr<float>(A.xb));
+        }
     }
-    k_mg0_prolong<DIM><<<g0, BLOCK, 0, s>>>(N, ptr<int>(c->mg[0].agg), ptr<float>(c->mg[0].xb), x0);
-    k_mg0_resid<DIM, 1><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, x0, out0);
+    const int* agg0 = ptr<int>(c->mg[0].agg);
+    const float* xc0 = ptr<float>(c->mg[0].xb);
+    if (PRE) {
+        k_mg0_post<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, XPC<B, true>{x0, N, agg0, xc0}, out0);
+    } else {
+        k_mg0_post<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, PC<B>{agg0, xc0}, x0);
+        k_mg0_post<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, X0<B>{x0, N}, out0);
+    }
 }
 
 }  // namespace
