@@ -167,6 +167,10 @@ PFG_API int pfg_upload_facets(pfg_ctx* ctx, int32_t n_facets, const int32_t* fac
 PFG_API int pfg_set_states(pfg_ctx* ctx, const double* states);
 PFG_API int pfg_get_states(pfg_ctx* ctx, double* states);
 PFG_API int pfg_get_positions(pfg_ctx* ctx, double* pos);          /* dim*N */
+/* Replace the node positions (dim*N) and keep the connectivity and the states, as
+ * Mesh::restoreNodesList does with a saved node list (Mesh.cpp:1019-1053), or for a host that
+ * moves nodes without remeshing. */
+PFG_API int pfg_set_positions(pfg_ctx* ctx, const double* pos);
 PFG_API int pfg_get_flags(pfg_ctx* ctx, uint8_t* flags);           /* N, PFG_NODE_FREE set */
 
 /* Dirichlet velocities V_bc(pos, t + dt) of n Dirichlet nodes, values[d*n + i] (field-major

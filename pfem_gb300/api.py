@@ -37,7 +37,7 @@ EXPORTED = (
     "pfg_get_csr", "pfg_get_geometry", "pfg_linear_solve", "pfg_version", "pfg_set_profiling",
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
-    "pfg_upload_facets",
+    "pfg_upload_facets", "pfg_set_positions",
 )
 NUM_PHASES = 15
 
@@ -90,6 +90,7 @@ def load(path=LIB_PATH):
         "pfg_upload_facets": ([vp, C.c_int32, ip, ip], C.c_int),
         "pfg_set_states": ([vp, dp], C.c_int),
         "pfg_get_states": ([vp, dp], C.c_int),
+        "pfg_set_positions": ([vp, dp], C.c_int),
         "pfg_get_positions": ([vp, dp], C.c_int),
         "pfg_get_flags": ([vp, u8p], C.c_int),
         "pfg_set_dirichlet": ([vp, C.c_int32, ip, dp], C.c_int),
@@ -210,6 +211,12 @@ class Context:
         out = np.empty((self.dim, self.N))
         self._check(self.L.pfg_get_positions(self.h, _dp(out)), "pfg_get_positions")
         return out
+
+    def set_positions(self, pos):
+        """Replace the node positions (dim, N), keeping connectivity and states."""
+        pos = np.ascontiguousarray(pos, np.float64)
+        assert pos.size == self.dim * self.N
+        self._check(self.L.pfg_set_positions(self.h, _dp(pos)), "pfg_set_positions")
 
     def get_flags(self):
         out = np.empty(self.N, np.uint8)

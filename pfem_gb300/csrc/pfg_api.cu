@@ -463,6 +463,20 @@ PFG_API int pfg_get_positions(pfg_ctx* c, double* pos) {
     return PFG_OK;
 }
 
+PFG_API int pfg_set_positions(pfg_ctx* c, const double* pos) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (!pos) return fail(c, PFG_ERR_INVALID, "null positions");
+    const size_t bytes = sizeof(double) * c->dim * c->N;
+    PFG_CUDA(c, cudaMemcpyAsync(c->pos.p, pos, bytes, cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->pos_save.p, pos, bytes, cudaMemcpyHostToDevice, c->stream));
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT && c->prm.precision == PFG_PREC_MIXED && (rc = wcm_positions_in(c)))
+        return rc;
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
 PFG_API int pfg_get_flags(pfg_ctx* c, uint8_t* flags) {
     int rc = check_ctx(c);
     if (rc) return rc;

@@ -174,3 +174,21 @@ def test_multigrid_matches_block_jacobi(gpu_lib, which, c1_mesh, small3d_mesh):
     (qj, kj), (qm, km) = out[api.PC_BLOCK_JACOBI], out[api.PC_MULTIGRID]
     assert max(field_errs(qm, qj, d, N)) < 1e-8
     assert km * 1.5 < kj, (km, kj)
+
+
+def test_set_positions_restores_a_step(gpu_lib, c1_mesh):
+    """pfg_set_positions + pfg_set_states put a context back to a saved node list: the same
+    step then gives the same bits."""
+    mesh = c1_mesh
+    ctx = make_ctx(mesh)
+    ctx.set_states(M.incomp_initial_states(mesh))
+    ctx.picard_step(1e-3)
+    x0, q0 = ctx.get_positions(), ctx.get_states()
+    ctx.picard_step(1e-3)
+    x1, q1 = ctx.get_positions(), ctx.get_states()
+    ctx.set_positions(x0)
+    ctx.set_states(q0)
+    assert np.array_equal(ctx.get_positions(), x0)
+    ctx.picard_step(1e-3)
+    assert np.array_equal(ctx.get_positions(), x1)
+    assert np.array_equal(ctx.get_states(), q1)
