@@ -2,7 +2,9 @@
 
 Each admitted request gets its own library context: its mesh and fields stay resident on the
 device for its whole life, its kernels run on the context's own CUDA stream, and a worker
-thread drives its time loop.  Every library call runs without the Python interpreter lock, so
+thread drives its time loop.  Incompressible requests run the reference's loop: the host
+remeshes after every accepted step (in the request's thread, while the other requests keep
+the GPU busy) and a failed step is retried with half the time step.  Every library call runs without the Python interpreter lock, so
 the device interleaves the work of all admitted requests.  Admission is first come, first
 served under two limits, a number of slots and an HBM budget: a request's device footprint is
 estimated from its mesh before admission, and when a request finishes its context (and
@@ -21,6 +23,8 @@ import numpy as np
 
 from . import api
 from . import mesh as M
+from . import remesh as RM
+from . import solver as SO
 
 
 @dataclass
@@ -32,6 +36,7 @@ class Request:
     dt: float = 1e-3                # incompressible time step (WC steps use their CFL step)
     precision: int = api.PREC_MIXED
     mu: float = 1e-3
+    remesh: bool = True             # incompressible: remesh after every accepted step
     arrival: float = 0.0            # seconds after the start of the run
     rid: int = -1
     # filled in by the server
@@ -69,6 +74,8 @@ def estimate_device_bytes(kind, precision, mesh) -> int:
         b += nnz * 8 + R * 8 + (2 + d * npe) * E * 8 + 3 * R * 8 + 12 * R * 8 + npe * npe * N * 8
         if precision == api.PREC_MIXED:
             b += nnz * 4 + 8 * R * 4 + npe * npe * N * 4 + R * 8 + N * 4
+            # multigrid: bfloat16 blocks, coarse levels (< half the FP32 blocks), cycle vectors
+            b += nnz * 3 + nnz * 2 + 3 * R * 4
     else:
         b += (2 * d + 2) * N * 8 * 3 + (7 * d + 5) * N * 4 + (1 + 3 * d) * npe * E * 4 + npe * E * 8 * (2 + d) \
              + 4 * N * 8
@@ -95,23 +102,26 @@ class Server:
             p.precision = req.precision
             p.mu = req.mu
             p.hbm_budget_bytes = req.estimate_bytes
-            ctx = api.Context(p)
-            try:
-                ctx.upload_mesh(req.mesh)
-                ctx.set_states(req.states)
-                if req.kind == api.KIND_WC_CDS_DPDT:
-                    ctx.set_time(0.0, ctx.next_dt())
-                    ctx.wc_step(0.0, req.steps)
-                    req.converged_steps = req.steps
-                else:
-                    for _ in range(req.steps):
-                        st = ctx.picard_step(req.dt)
-                        req.converged_steps += st.converged
-                req.result = ctx.get_states()
-                req.positions = ctx.get_positions()
-                req.device_bytes = ctx.device_bytes()
-            finally:
-                ctx.close()
+            if req.kind == api.KIND_INCOMP_PSPG and req.remesh:
+                self._run_incomp(req, p)
+            else:
+                ctx = api.Context(p)
+                try:
+                    ctx.upload_mesh(req.mesh)
+                    ctx.set_states(req.states)
+                    if req.kind == api.KIND_WC_CDS_DPDT:
+                        ctx.set_time(0.0, ctx.next_dt())
+                        ctx.wc_step(0.0, req.steps)
+                        req.converged_steps = req.steps
+                    else:
+                        for _ in range(req.steps):
+                            st = ctx.picard_step(req.dt)
+                            req.converged_steps += st.converged
+                    req.result = ctx.get_states()
+                    req.positions = ctx.get_positions()
+                    req.device_bytes = ctx.device_bytes()
+                finally:
+                    ctx.close()
         except Exception as e:  # reported with the request; the server keeps serving
             req.error = str(e)
         req.t_done = time.perf_counter() - t0
@@ -119,6 +129,33 @@ class Server:
             self._active -= 1
             self._used -= req.estimate_bytes
             self._lock.notify_all()
+
+    @staticmethod
+    def _run_incomp(req: Request, p):
+        """`steps` accepted steps of the reference's loop (`IncompNewton/Solver.cpp:216-247`):
+        remesh after each accepted step, dt halved after a failed one (at most 4 x steps tries)."""
+        m = req.mesh
+        lo, hi = m.pos.min(axis=1), m.pos.max(axis=1)
+        pad = 0.1 * (hi - lo)
+        box = tuple(lo - pad) + tuple(hi + pad)
+        box = box[:2 * m.dim - 1] + (1e30,)  # open at the top: nodes leave only sideways or below
+        prm = RM.RemeshParams(hchar=m.hchar, alpha=m.alpha, bounding_box=box)
+        sol = SO.SolverIncompNewtonGPU(m, req.states, params=p, remesh_params=prm, precision=req.precision,
+                                       initial_dt=req.dt, max_dt=req.dt)
+        try:
+            tries = 0
+            while sol.steps < req.steps and tries < 4 * req.steps:
+                sol.solve_one_time_step()
+                sol.compute_next_dt()
+                tries += 1
+            req.converged_steps = sol.steps
+            req.result = sol.states()
+            req.positions = sol.positions()
+            req.device_bytes = sol.ctx.device_bytes()
+            if sol.steps < req.steps:
+                req.error = f"{sol.steps} of {req.steps} steps converged in {tries} tries"
+        finally:
+            sol.close()
 
     # -- the request loop -----------------------------------------------------------------
     def run(self, requests, realtime=True):
@@ -129,6 +166,8 @@ class Server:
             if r.rid < 0:
                 r.rid = i
             r.estimate_bytes = estimate_device_bytes(r.kind, r.precision, r.mesh)
+            if r.kind == api.KIND_INCOMP_PSPG and r.remesh:  # remeshing may add nodes
+                r.estimate_bytes = int(1.5 * r.estimate_bytes)
             if r.estimate_bytes > self.budget:
                 r.error = f"needs ~{r.estimate_bytes} bytes, over the {self.budget}-byte budget"
         t0 = time.perf_counter()
@@ -164,8 +203,8 @@ def metrics(reqs, makespan):
     done = [r for r in reqs if r.error is None and r.t_done is not None]
     lat = np.array([r.latency for r in done]) if done else np.zeros(1)
     wait = np.array([r.t_admit - r.arrival for r in done]) if done else np.zeros(1)
-    steps = sum(r.steps for r in done)
-    dof_steps = sum(r.dof * r.steps for r in done)
+    steps = sum(r.converged_steps for r in done)
+    dof_steps = sum(r.dof * r.converged_steps for r in done)
     return {
         "requests": len(reqs), "completed": len(done), "failed": len(reqs) - len(done),
         "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
