@@ -49,7 +49,8 @@ enum : int { D_RHO = 0, D_MU, D_DT, D_RR, D_BB, D_RES, D_PAD0, D_PAD1, D_COUNT =
 // per-instance Krylov scalars (one FP32 and one FP64 set)
 enum : int { M_RHO = 0, M_RHO_OLD, M_ALPHA, M_OMEGA, M_RR, M_TOL2, M_DONE, M_ITERS, M_RR0, M_COUNT = 10 };
 // FP32 Krylov vectors
-enum : int { W_R = 0, W_RHAT, W_P, W_V, W_S, W_T, W_PHAT, W_SHAT, W_COUNT };
+// W_Z: the FP32 correction of an FP32 solve, added to the FP64 iterate once per sweep
+enum : int { W_R = 0, W_RHAT, W_P, W_V, W_S, W_T, W_PHAT, W_SHAT, W_Z, W_COUNT };
 // device counters
 enum : int { C_NEED = 0, C_ACTIVE = 1, C_NEED64 = 2, C_ROLLBACK = 3 };
 
@@ -102,13 +103,37 @@ MxConst mx_const(pfg_ctx* c) {
     return k;
 }
 
+// Block sum in the solve's own precision (FP32 sums for the FP32 solves keep the FP64 pipe,
+// 1/64 of the FP32 rate on GB300, out of the Krylov kernels).  sh: 32 values of scratch.
+template <int NT, class T>
+__device__ __forceinline__ T block_sum_t(T v, double* shd) {
+    if constexpr (sizeof(T) == 8) {
+        return block_sum<NT>(v, shd);
+    } else {
+        float* sh = reinterpret_cast<float*>(shd);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) sh[wid] = v;
+        __syncthreads();
+        v = 0;
+        if (wid == 0) {
+            v = lane < NT / 32 ? sh[lane] : 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        }
+        __syncthreads();
+        return v;
+    }
+}
+
 // Per-instance deterministic reduction of NV values: each segment block writes its partials,
 // the last block of the instance to arrive sums the partials of the instance's blocks in
 // block order.  Returns true in the last block (totals valid in thread 0).
 template <int NT, int NV, class T>
 __device__ __forceinline__ bool inst_reduce(T (&v)[NV], int b, int b0, int b1, T* part, unsigned* ticket, double* sh) {
 #pragma unroll
-    for (int i = 0; i < NV; ++i) v[i] = (T)block_sum<NT>((double)v[i], sh);
+    for (int i = 0; i < NV; ++i) v[i] = block_sum_t<NT, T>(v[i], sh);
     __shared__ bool last;
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -123,7 +148,7 @@ __device__ __forceinline__ bool inst_reduce(T (&v)[NV], int b, int b0, int b1, T
     for (int i = 0; i < NV; ++i) {
         T s = 0;
         for (int k = b0 + threadIdx.x; k < b1; k += NT) s += __ldcg(part + (size_t)k * NV + i);
-        v[i] = (T)block_sum<NT>((double)s, sh);
+        v[i] = block_sum_t<NT, T>(s, sh);
     }
     if (threadIdx.x == 0) *ticket = 0u;
     return true;
@@ -728,8 +753,8 @@ __global__ void __launch_bounds__(NB * node_lanes<DIM>()) k_mx_spmv(Mx m, const 
     }
 }
 
-// x += S (alpha phat + omega shat) (FP64 solution; S = I for the unscaled FP64 system);
-// r = s - omega t; rho = rhat.r; rr = r.r
+// FP32: z += alpha phat + omega shat (the correction, added to x as S z after the solve);
+// FP64: x += alpha phat + omega shat.  r = s - omega t; rho = rhat.r; rr = r.r
 template <class T, int DIM>
 __global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, const int* __restrict__ list, T* __restrict__ scb, int cnt_slot,
                                                 int N, double* __restrict__ x,
@@ -746,8 +771,10 @@ __global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, const int* __restrict__ li
 #pragma unroll
         for (int f = 0; f <= DIM; ++f) {
             const size_t r = (size_t)f * N + n;
-            const double dx = (double)(al * W[W_PHAT * ld + r]) + (double)(om * W[W_SHAT * ld + r]);
-            x[r] += scale ? scale[r] * dx : dx;
+            if constexpr (sizeof(T) == 4)
+                W[W_Z * ld + r] += al * W[W_PHAT * ld + r] + om * W[W_SHAT * ld + r];
+            else
+                x[r] += al * W[W_PHAT * ld + r] + om * W[W_SHAT * ld + r];
             const T rv = W[W_S * ld + r] - om * W[W_T * ld + r];
             W[W_R * ld + r] = rv;
             rh += W[W_RHAT * ld + r] * rv;
@@ -775,6 +802,23 @@ __global__ void __launch_bounds__(NB) k_mx_up_x(Mx m, const int* __restrict__ li
     if (done != 0) {
         sc[M_DONE] = done;
         atomicSub(m.cnt + cnt_slot, 1);
+    }
+}
+
+// x += S z and z = 0 over every node: the FP32 solves' corrections (z stays 0 for instances
+// solving in FP64)
+template <int DIM>
+__global__ void k_mx_apply_z(int N, const double* __restrict__ scale, float* __restrict__ z, double* __restrict__ x) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+#pragma unroll
+    for (int f = 0; f <= DIM; ++f) {
+        const size_t r = (size_t)f * N + n;
+        const float zv = z[r];
+        if (zv != 0.0f) {
+            x[r] += scale[r] * (double)zv;
+            z[r] = 0.0f;
+        }
     }
 }
 
@@ -1173,6 +1217,9 @@ int mx_refine(pfg_ctx* c, const MxConst& k, Counters* cnt) {
             if (cnt->need32 > 0 && (rc = mx_inner<float, DIM>(c, cnt))) return rc;
             if (cnt->need64 > 0 && (rc = mx_inner<double, DIM>(c, cnt))) return rc;
         }
+        k_mx_apply_z<DIM><<<div_up(c->N, BLOCK), BLOCK, 0, c->stream>>>(
+            c->N, ptr<double>(c->mx_scale), ptr<float>(c->kv32) + (size_t)W_Z * c->R, ptr<double>(c->q));
+        PFG_CHECK_LAUNCH(c);
         if ((rc = mx_residual<DIM>(c, k, RES_SWEEP, cnt))) return rc;
         if (cnt->redo > 0) {
             k_mx_rollback<DIM><<<div_up(c->N, BLOCK), BLOCK, 0, c->stream>>>(c->N, ptr<double>(c->q_iter_prev),
@@ -1255,6 +1302,7 @@ int mx_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))
         return rc;
+    PFG_CUDA(c, cudaMemsetAsync(ptr<float>(c->kv32) + (size_t)W_Z * R, 0, sizeof(float) * R, c->stream));
     c->n_mg = 0;
     if (c->prm.preconditioner == PFG_PC_MULTIGRID) {
         if ((rc = mg_setup(c)) || (rc = ensure(c, c->mg_in64, sizeof(float) * 2 * R)) ||

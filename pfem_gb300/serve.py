@@ -82,6 +82,13 @@ def estimate_device_bytes(kind, precision, mesh) -> int:
     return int(1.25 * b) + (4 << 20)
 
 
+def admission_bytes(req: Request) -> int:
+    """What admission reserves for a request: its estimate, with half again for an
+    incompressible request that remeshes (the remesh may add nodes)."""
+    b = estimate_device_bytes(req.kind, req.precision, req.mesh)
+    return int(1.5 * b) if req.kind == api.KIND_INCOMP_PSPG and req.remesh else b
+
+
 class Server:
     """Runs requests with at most `max_active` at a time and their estimated device memory
     summed below `hbm_budget_bytes`."""
@@ -165,9 +172,7 @@ class Server:
         for i, r in enumerate(reqs):
             if r.rid < 0:
                 r.rid = i
-            r.estimate_bytes = estimate_device_bytes(r.kind, r.precision, r.mesh)
-            if r.kind == api.KIND_INCOMP_PSPG and r.remesh:  # remeshing may add nodes
-                r.estimate_bytes = int(1.5 * r.estimate_bytes)
+            r.estimate_bytes = admission_bytes(r)
             if r.estimate_bytes > self.budget:
                 r.error = f"needs ~{r.estimate_bytes} bytes, over the {self.budget}-byte budget"
         t0 = time.perf_counter()

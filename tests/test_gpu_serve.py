@@ -51,7 +51,7 @@ def test_results_same_alone_and_in_mix(gpu_lib):
 
 def test_admission_respects_budget(gpu_lib):
     reqs = _requests()
-    est = max(SV.estimate_device_bytes(r.kind, r.precision, r.mesh) for r in reqs)
+    est = max(SV.admission_bytes(r) for r in reqs)
     srv = SV.Server(hbm_budget_bytes=int(1.2 * est), max_active=8)
     out = srv.run(reqs, realtime=False)
     assert all(r.error is None for r in out)
