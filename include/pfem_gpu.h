@@ -108,7 +108,8 @@ typedef struct pfg_params {
     size_t hbm_budget_bytes;   /* 0 = no limit                                             */
     /* mixed precision, incompressible: */
     double inner_rel_tol;      /* FP32 correction solve stops at this fraction of its
-                                  starting residual (0 = 1e-3)                             */
+                                  starting residual (0 = 1e-4; defaults: 1e-3 in 2D,
+                                  1e-4 in 3D)                                              */
     /* both kinds: */
     double gamma;              /* surface tension coefficient (MomContEq / MomEq "gamma");
                                   >= 1e-15 adds the facet term of m_applyBCPSPG

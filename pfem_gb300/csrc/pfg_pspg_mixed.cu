@@ -97,7 +97,7 @@ MxConst mx_const(pfg_ctx* c) {
     for (int f = 0; f < 3; ++f) k.t.g[f] = c->prm.gravity[f];
     k.rtol = c->prm.krylov_rel_tol;
     k.atol = c->prm.krylov_abs_tol;
-    k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-3;
+    k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-4;
     k.min_res = c->prm.picard_min_res;
     k.max_iter = c->prm.picard_max_iter;
     return k;
