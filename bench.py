@@ -460,7 +460,8 @@ NCU_TRAFFIC = {
     ("wc-c2", "fp32", "WC momentum element"): 6.7676e6,
     ("wc-c2", "fp32", "WC continuity element"): 7.8026e6,
     ("wc-c2", "fp32", "WC continuity node"): 8.1851e6,
-    ("incomp-c3", "fp32", "Krylov SpMV"): 560.4e6,
+    # scaled from the h = 0.012 capture by nnz (189.4 MB x 66.96 / 39.16): node-pair blocks
+    ("incomp-c3", "fp32", "Krylov SpMV"): 323.9e6,
 }
 
 
