@@ -118,6 +118,11 @@ typedef struct pfg_params {
     /* mixed precision, incompressible: */
     int32_t preconditioner;    /* pfg_preconditioner of the FP32 correction solves         */
     int32_t pad2;
+    /* incompressible, Bingham fluid (problem "Bingham", MomContEquation.inl:54-58,102-121):
+       tau0 > 0 makes the viscosity mu + tau0 (1 - exp(-m_reg gd)) / gd per element, gd the
+       strain-rate norm of the Picard iterate                                             */
+    double tau0;               /* yield stress (0 = Newtonian)                             */
+    double m_reg;              /* regularisation parameter mReg                            */
 } pfg_params;
 
 typedef struct pfg_step_status {

@@ -45,7 +45,7 @@ def build(force=False):
 
 class PspgParams(C.Structure):
     _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double), ("g", C.c_double * 3),
-                ("gamma", C.c_double)]
+                ("gamma", C.c_double), ("tau0", C.c_double), ("mReg", C.c_double)]
 
 
 class WcParams(C.Structure):
@@ -184,33 +184,33 @@ class OracleMesh:
         return lib().orc_tip(self.h, coord, int(want_max))
 
 
-def pspg_params(rho, mu, dt, g, gamma=0.0):
+def pspg_params(rho, mu, dt, g, gamma=0.0, tau0=0.0, m_reg=0.0):
     p = PspgParams()
-    p.rho, p.mu, p.dt, p.gamma = rho, mu, dt, gamma
+    p.rho, p.mu, p.dt, p.gamma, p.tau0, p.mReg = rho, mu, dt, gamma, tau0, m_reg
     for i, x in enumerate(g):
         p.g[i] = x
     return p
 
 
-def pspg_element(om, e, rho, mu, dt, g, q_iter, q_prev):
+def pspg_element(om, e, rho, mu, dt, g, q_iter, q_prev, tau0=0.0, m_reg=0.0):
     npe = om.dim + 1
     nt = (om.dim + 1) * npe
     Ae = np.empty((nt, nt))
     be = np.empty(nt)
-    p = pspg_params(rho, mu, dt, g)
+    p = pspg_params(rho, mu, dt, g, tau0=tau0, m_reg=m_reg)
     lib().orc_pspg_element(om.h, e, C.byref(p), _dp(np.ascontiguousarray(q_iter, float)),
                            _dp(np.ascontiguousarray(q_prev, float)), _dp(Ae), _dp(be))
     return Ae, be
 
 
-def pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc=None, apply_bc=True, gamma=0.0):
+def pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc=None, apply_bc=True, gamma=0.0, tau0=0.0, m_reg=0.0):
     """A (scipy CSC, Eigen's storage order) and b of m_buildAbPSPG (+ m_applyBCPSPG)."""
     import scipy.sparse as sp
 
     R = (om.dim + 1) * om.N
     if vbc is None:
         vbc = np.zeros(om.dim * om.N)
-    p = pspg_params(rho, mu, dt, g, gamma)
+    p = pspg_params(rho, mu, dt, g, gamma, tau0, m_reg)
     q_iter = np.ascontiguousarray(q_iter, float)
     q_prev = np.ascontiguousarray(q_prev, float)
     vbc = np.ascontiguousarray(vbc, float)
@@ -236,7 +236,7 @@ def _tick(times, key, t0):
 
 
 def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=None, max_iter=10,
-                     min_res=1e-6, times=None, gamma=0.0):
+                     min_res=1e-6, times=None, gamma=0.0, tau0=0.0, m_reg=0.0):
     """One `MomContEqIncompNewton::solve` with PSPG (Picard, residual "Ax_f").
 
     Mutates the oracle mesh positions.  Returns (q, PicardResult); on failure the positions
@@ -253,7 +253,7 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
     om.save()
     _tick(times, "Save/restore nodelist", t0)
     t0 = time.perf_counter()
-    A, b = pspg_assemble(om, rho, mu, dt, g, q_prev, q_prev, vbc, gamma=gamma)
+    A, b = pspg_assemble(om, rho, mu, dt, g, q_prev, q_prev, vbc, gamma=gamma, tau0=tau0, m_reg=m_reg)
     _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
     q_iter = np.zeros_like(q_prev)
     r = float("inf")
@@ -280,7 +280,7 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
         om.update_from_save(q_iter * dt)
         _tick(times, "Update solutions", t0)
         t0 = time.perf_counter()
-        A, b = pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc, gamma=gamma)
+        A, b = pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc, gamma=gamma, tau0=tau0, m_reg=m_reg)
         _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
         # residual closure, "Ax_f" (:366-371)
         t0 = time.perf_counter()

@@ -116,6 +116,8 @@ struct PspgParams {
     double rho, mu, dt;
     double g[3];
     double gamma;      // surface tension coefficient (MomContEq "gamma")
+    double tau0;       // Bingham yield stress (problem "Bingham"; 0 = Newtonian)
+    double mReg;       // Bingham regularisation parameter
 };
 
 struct WcParams {
@@ -516,8 +518,27 @@ void pspgElement(const OrcMesh& m, int e, const PspgParams& p, const double* qIt
     Mat Ms = getM(m, geo, [&](int) { return p.rho; });
     for (int i = 0; i < npe; ++i)
         for (int j = 0; j < npe; ++j) Ms(i, j) *= (1 / dt);
+    // K factor (setKcomputeFactor, MomContEquation.inl:102-131): mu, or for a Bingham fluid
+    // mu + tau0 (1 - exp(-mReg gd)) / gd with gd = sqrt(V^T B^T ddev B V) of the iterate
+    double mue = p.mu;
+    if (p.tau0 > 0) {
+        Mat dd = ddevIncomp(dim);
+        const int nv = dim * npe;
+        double V[12];
+        for (int f = 0; f < dim; ++f)
+            for (int k = 0; k < npe; ++k) V[f * npe + k] = qIter[(size_t)f * m.N + m.node(e, k)];
+        double gd2 = 0;
+        for (int r = 0; r < B.r; ++r) {
+            double eps = 0;
+            for (int c = 0; c < nv; ++c) eps += B(r, c) * V[c];
+            gd2 += eps * dd(r, r) * eps;
+        }
+        const double gd = std::sqrt(gd2);
+        const double muEq = gd < 1e-15 ? p.tau0 * p.mReg : p.tau0 * (1 - std::exp(-p.mReg * gd)) / gd;
+        mue = p.mu + muEq;
+    }
     double sumW = 0;
-    for (int g = 0; g < m.gt.n; ++g) sumW += p.mu * m.gt.w[g];
+    for (int g = 0; g < m.gt.n; ++g) sumW += mue * m.gt.w[g];
     Mat K = getK(m, geo, sumW, B, ddevIncomp(dim));
     Mat D = getD(m, geo, [](int) { return 1.0; }, B);
     Mat C = getC(m, geo, 1.0, G);

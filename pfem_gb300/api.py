@@ -55,6 +55,7 @@ class Params(C.Structure):
         ("inner_rel_tol", C.c_double),
         ("gamma", C.c_double),
         ("preconditioner", C.c_int32), ("pad2", C.c_int32),
+        ("tau0", C.c_double), ("m_reg", C.c_double),
     ]
 
 

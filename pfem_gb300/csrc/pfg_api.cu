@@ -261,6 +261,8 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     if (params->kind != PFG_KIND_INCOMP_PSPG && params->kind != PFG_KIND_WC_CDS_DPDT) return PFG_ERR_INVALID;
     if (params->precision != PFG_PREC_FP64 && params->precision != PFG_PREC_MIXED) return PFG_ERR_INVALID;
     if (params->linear_solver != PFG_LINSOLVE_BICGSTAB) return PFG_ERR_UNSUPPORTED;
+    if (params->tau0 < 0 || (params->tau0 > 0 && !(params->m_reg > 0))) return PFG_ERR_INVALID;
+    if (params->tau0 > 0 && params->kind != PFG_KIND_INCOMP_PSPG) return PFG_ERR_UNSUPPORTED;  // Bingham: PSPG only
     pfg_ctx* c = new (std::nothrow) pfg_ctx();
     if (!c) return PFG_ERR_NOMEM;
     c->prm = *params;

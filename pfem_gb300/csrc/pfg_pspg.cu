@@ -30,7 +30,7 @@ namespace {
 template <int DIM>
 __global__ void k_elem_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
                             const double* __restrict__ q_iter, double rho, double mu, double dt, double refSize,
-                            double* __restrict__ ed) {
+                            ViscArgs va, double* __restrict__ ed) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -60,6 +60,7 @@ __global__ void k_elem_prep(int E, int N, const int* __restrict__ conn, const do
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
         for (int i = 0; i <= DIM; ++i) ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
+    ed[(size_t)ed_ksum<DIM>() * E + e] = k_sum<DIM>(va, mu, G, q_iter, N, nd);
 }
 
 struct PspgConst {
@@ -207,7 +208,7 @@ int assemble_dim(pfg_ctx* c, double dt, const double* d_qiter, const double* d_q
         prof_begin(c, PH_PSPG_ELEM);
         k_elem_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
                                                                     d_qiter, c->prm.rho, c->prm.mu, dt, g.refSize,
-                                                                    ptr<double>(c->edata));
+                                                                    visc_args(c), ptr<double>(c->edata));
         prof_end(c, PH_PSPG_ELEM);
         PFG_CHECK_LAUNCH(c);
     }

@@ -33,10 +33,76 @@ struct PspgTables {
     double g[3];
 };
 
-// Element data layout (structure of arrays, stride E): [detJ, tau, gradN[f][i] (f-major)]
+// Element data layout (structure of arrays, stride E):
+//   [detJ, tau, gradN[f][i] (f-major), ksum]
+// ksum = sum_g mu_e w_g, the viscous factor of getK (MatricesBuilder.inl:276-290)
 template <int DIM>
 constexpr int ed_count() {
+    return 3 + DIM * (DIM + 1);
+}
+template <int DIM>
+constexpr int ed_ksum() {
     return 2 + DIM * (DIM + 1);
+}
+
+// The viscosity law of the K factor (setKcomputeFactor, MomContEquation.inl:102-131): mu, or
+// for a Bingham fluid (problem "Bingham", tau0 > 0) mu + tau0 (1 - exp(-mReg gd)) / gd (tau0 mReg
+// when gd < 1e-15), gd = sqrt(V^T B^T ddev B V) of the element's iterate velocities, ddev =
+// diag(2, 2, 1) in 2D and diag(2, 2, 2, 1, 1, 1) in 3D (:73-94).  Summed over the Gauss points
+// like the reference's factor.
+struct ViscArgs {
+    double w[4];
+    int ng;
+    double tau0, mreg;
+};
+
+inline ViscArgs visc_args(const pfg_ctx* c) {
+    const GaussConst g = gauss_const(c->dim);
+    ViscArgs v{};
+    v.ng = g.n;
+    for (int i = 0; i < g.n; ++i) v.w[i] = g.w[i];
+    v.tau0 = c->prm.tau0;
+    v.mreg = c->prm.m_reg;
+    return v;
+}
+
+template <int DIM>
+__device__ __forceinline__ double k_sum(const ViscArgs& va, double mu, const double (&G)[DIM][DIM + 1],
+                                        const double* __restrict__ q, int N, const int (&nd)[DIM + 1]) {
+    double mue = mu;
+    if (va.tau0 > 0) {
+        double v[DIM][DIM + 1];
+#pragma unroll
+        for (int f = 0; f < DIM; ++f)
+#pragma unroll
+            for (int i = 0; i <= DIM; ++i) v[f][i] = q[(size_t)f * N + nd[i]];
+        // strain rates (getB, MatricesBuilder.inl:129-164): normal d v_f / d x_f and engineering shears
+        double e[DIM][DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) {
+                double s = 0;
+#pragma unroll
+                for (int i = 0; i <= DIM; ++i) s += G[b][i] * v[a][i];
+                e[a][b] = s;  // d v_a / d x_b
+            }
+        double gd2 = 0;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) gd2 += 2 * e[a][a] * e[a][a];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = a + 1; b < DIM; ++b) {
+                const double sh = e[a][b] + e[b][a];
+                gd2 += sh * sh;
+            }
+        const double gd = sqrt(gd2);
+        mue = mu + (gd < 1e-15 ? va.tau0 * va.mreg : va.tau0 * (1 - exp(-va.mreg * gd)) / gd);
+    }
+    double s = 0;
+    for (int g = 0; g < va.ng; ++g) s += mue * va.w[g];
+    return s;
 }
 
 // Block (n, m) of the assembled matrix before boundary conditions: the sum, in ascending
@@ -75,7 +141,7 @@ __device__ __forceinline__ void pspg_pair_block(int n, int m, int E, const int* 
 #pragma unroll
         for (int f = 0; f < DIM; ++f) dot += gi[f] * gj[f];
         const double mij = inv_dt * (k.rho * t.MM[i][j] * ae);
-        const double kf = ae * k.mu_sum;
+        const double kf = ae * ed[(size_t)ed_ksum<DIM>() * E + e];
 #pragma unroll
         for (int f1 = 0; f1 < DIM; ++f1) {
 #pragma unroll

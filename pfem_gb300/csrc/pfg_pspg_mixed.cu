@@ -171,7 +171,8 @@ __device__ __forceinline__ PspgCoef inst_coef_d(const double* id, double sumw, d
 // active instances: [detJ, tau, gradN] in FP64 (structure of arrays, stride E).
 template <int DIM>
 __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
-                          const double* __restrict__ q_iter, Mx m, double refSize, double* __restrict__ ed) {
+                          const double* __restrict__ q_iter, Mx m, double refSize, ViscArgs va,
+                          double* __restrict__ ed) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -205,6 +206,7 @@ __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const doub
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
         for (int i = 0; i <= DIM; ++i) ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
+    ed[(size_t)ed_ksum<DIM>() * E + e] = k_sum<DIM>(va, mu, G, q_iter, N, nd);
 }
 
 // Right-hand side of the nodes of active instances (element doublets + node BCs).
@@ -891,7 +893,7 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     if (E > 0) {
         prof_begin(c, PH_PSPG_ELEM);
         k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), q_iter,
-                                                                  m, k.refSize, ptr<double>(c->edata));
+                                                                  m, k.refSize, visc_args(c), ptr<double>(c->edata));
         prof_end(c, PH_PSPG_ELEM);
         PFG_CHECK_LAUNCH(c);
     }

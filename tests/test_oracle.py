@@ -180,3 +180,23 @@ def test_invalid_facets_rejected(c1_mesh):
     bad[0] = c1_mesh.n_elems
     with pytest.raises(ValueError):
         om.set_facets(c1_mesh.facets, bad)
+
+
+def test_bingham_viscosity_in_simple_shear():
+    """KAT: u = s y on one triangle is a simple shear with gd = s, so the viscous block of the
+    Bingham element is (mu + tau0 (1 - exp(-mReg s)) / s) / mu times the Newtonian one."""
+    X = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0]])  # nodes x coordinates
+    mesh = _single_element_mesh(X)
+    om = O.OracleMesh(mesh)
+    N = mesh.n_nodes
+    s = 0.37
+    q = np.zeros(3 * N)
+    q[:N] = s * X[:, 1]
+    mu, tau0, mreg, dt = 2.0, 5.0, 40.0, 1e-3
+    args = (1000.0, mu, dt, (0.0, -9.81))
+    A_n, _ = O.pspg_element(om, 0, *args, q, q)
+    A_b, _ = O.pspg_element(om, 0, *args, q, q, tau0=tau0, m_reg=mreg)
+    A_m, _ = O.pspg_element(om, 0, 1000.0, 0.0, dt, (0.0, -9.81), q, q)  # mass part only (mu = 0)
+    K_n, K_b = (A_n - A_m)[:6, :6], (A_b - A_m)[:6, :6]
+    mue = mu + tau0 * (1 - np.exp(-mreg * s)) / s
+    assert np.allclose(K_b, K_n * (mue / mu), rtol=1e-12, atol=1e-12 * np.abs(K_b).max())
