@@ -286,6 +286,10 @@ PFG_API int pfg_set_profiling(pfg_ctx* ctx, int32_t enable);
 /* Accumulated milliseconds and launch counts per phase since the last reset. */
 PFG_API int pfg_get_phase_times(pfg_ctx* ctx, double* ms, int64_t* launches);
 PFG_API int pfg_reset_phase_times(pfg_ctx* ctx);
+/* Node pairs ((d+1)^2 blocks) read by the timed Krylov SpMV launches (phase 12) since the last
+ * reset: the algorithmic work of those launches in a batch whose converged instances drop out
+ * of the products (mixed precision; the plain FP64 form reports 0). */
+PFG_API int pfg_get_spmv_pairs(pfg_ctx* ctx, int64_t* pairs);
 PFG_API const char* pfg_phase_name(int32_t phase);
 
 /* Library version string. */

@@ -45,7 +45,17 @@ def build(force=False):
 
 class PspgParams(C.Structure):
     _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double), ("g", C.c_double * 3),
-                ("gamma", C.c_double), ("tau0", C.c_double), ("mReg", C.c_double)]
+                ("gamma", C.c_double), ("tau0", C.c_double), ("mReg", C.c_double),
+                ("alpha", C.c_double), ("Tr", C.c_double), ("T", C.POINTER(C.c_double))]
+
+
+class HeatParams(C.Structure):
+    _fields_ = [("rho", C.c_double), ("cv", C.c_double), ("k", C.c_double), ("h", C.c_double),
+                ("Tinf", C.c_double), ("epsRad", C.c_double), ("fsFlags", C.c_int32), ("pad", C.c_int32)]
+
+
+# heat boundary-condition flags (per node, and for the free-surface tag)
+HT_T, HT_Q, HT_QH, HT_QR = 1, 2, 4, 8
 
 
 class WcParams(C.Structure):
@@ -82,6 +92,9 @@ def lib():
         L.orc_pspg_assemble.restype = C.c_int
         L.orc_pspg_assemble.argtypes = [vp, C.POINTER(PspgParams), dp, dp, dp, C.c_int]
         L.orc_pspg_get.argtypes = [vp, ip, ip, dp, dp]
+        L.orc_heat_assemble.restype = C.c_int
+        L.orc_heat_assemble.argtypes = [vp, C.POINTER(HeatParams), C.c_double, dp, u8p, dp, dp]
+        L.orc_facet_gauss_positions.argtypes = [vp, dp]
         L.orc_wc_step.argtypes = [vp, C.POINTER(WcParams), C.c_double, dp, dp]
         L.orc_wc_next_dt.restype = C.c_double
         L.orc_wc_next_dt.argtypes = [vp, C.POINTER(WcParams), dp]
@@ -184,11 +197,16 @@ class OracleMesh:
         return lib().orc_tip(self.h, coord, int(want_max))
 
 
-def pspg_params(rho, mu, dt, g, gamma=0.0, tau0=0.0, m_reg=0.0):
+def pspg_params(rho, mu, dt, g, gamma=0.0, tau0=0.0, m_reg=0.0, boussinesq=None):
+    """boussinesq: None, or (alpha, Tr, T) with T the node temperatures (kept alive on p)."""
     p = PspgParams()
     p.rho, p.mu, p.dt, p.gamma, p.tau0, p.mReg = rho, mu, dt, gamma, tau0, m_reg
     for i, x in enumerate(g):
         p.g[i] = x
+    if boussinesq is not None:
+        alpha, Tr, T = boussinesq
+        p._T = np.ascontiguousarray(T, dtype=np.float64)
+        p.alpha, p.Tr, p.T = alpha, Tr, _dp(p._T)
     return p
 
 
@@ -203,14 +221,15 @@ def pspg_element(om, e, rho, mu, dt, g, q_iter, q_prev, tau0=0.0, m_reg=0.0):
     return Ae, be
 
 
-def pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc=None, apply_bc=True, gamma=0.0, tau0=0.0, m_reg=0.0):
+def pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc=None, apply_bc=True, gamma=0.0, tau0=0.0, m_reg=0.0,
+                  boussinesq=None):
     """A (scipy CSC, Eigen's storage order) and b of m_buildAbPSPG (+ m_applyBCPSPG)."""
     import scipy.sparse as sp
 
     R = (om.dim + 1) * om.N
     if vbc is None:
         vbc = np.zeros(om.dim * om.N)
-    p = pspg_params(rho, mu, dt, g, gamma, tau0, m_reg)
+    p = pspg_params(rho, mu, dt, g, gamma, tau0, m_reg, boussinesq)
     q_iter = np.ascontiguousarray(q_iter, float)
     q_prev = np.ascontiguousarray(q_prev, float)
     vbc = np.ascontiguousarray(vbc, float)
@@ -236,7 +255,7 @@ def _tick(times, key, t0):
 
 
 def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=None, max_iter=10,
-                     min_res=1e-6, times=None, gamma=0.0, tau0=0.0, m_reg=0.0):
+                     min_res=1e-6, times=None, gamma=0.0, tau0=0.0, m_reg=0.0, boussinesq=None):
     """One `MomContEqIncompNewton::solve` with PSPG (Picard, residual "Ax_f").
 
     Mutates the oracle mesh positions.  Returns (q, PicardResult); on failure the positions
@@ -253,7 +272,8 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
     om.save()
     _tick(times, "Save/restore nodelist", t0)
     t0 = time.perf_counter()
-    A, b = pspg_assemble(om, rho, mu, dt, g, q_prev, q_prev, vbc, gamma=gamma, tau0=tau0, m_reg=m_reg)
+    A, b = pspg_assemble(om, rho, mu, dt, g, q_prev, q_prev, vbc, gamma=gamma, tau0=tau0, m_reg=m_reg,
+                         boussinesq=boussinesq)
     _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
     q_iter = np.zeros_like(q_prev)
     r = float("inf")
@@ -280,7 +300,8 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
         om.update_from_save(q_iter * dt)
         _tick(times, "Update solutions", t0)
         t0 = time.perf_counter()
-        A, b = pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc, gamma=gamma, tau0=tau0, m_reg=m_reg)
+        A, b = pspg_assemble(om, rho, mu, dt, g, q_iter, q_prev, vbc, gamma=gamma, tau0=tau0, m_reg=m_reg,
+                             boussinesq=boussinesq)
         _tick(times, "Compute triplets+Assemble matrix+Apply boundary conditions", t0)
         # residual closure, "Ax_f" (:366-371)
         t0 = time.perf_counter()
@@ -295,6 +316,49 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
     res.converged = True
     res.iterations = it
     return q_iter, res
+
+
+def heat_params(rho, cv, k, h=0.0, t_inf=0.0, eps_rad=0.0, fs_flags=0):
+    p = HeatParams()
+    p.rho, p.cv, p.k, p.h, p.Tinf, p.epsRad, p.fsFlags = rho, cv, k, h, t_inf, eps_rad, int(fs_flags)
+    return p
+
+
+def heat_assemble(om, params, dt, t_prev, flags, t_bc=None, q_gp=None):
+    """A (scipy CSC) and b of HeatEqIncompNewton::m_buildAb + m_applyBC from T_prev."""
+    import scipy.sparse as sp
+
+    N = om.N
+    t_prev = np.ascontiguousarray(t_prev, float)
+    flags = np.ascontiguousarray(flags, np.uint8)
+    t_bc = np.ascontiguousarray(np.zeros(N) if t_bc is None else t_bc, float)
+    qp = None if q_gp is None else np.ascontiguousarray(q_gp, float)
+    nnz = lib().orc_heat_assemble(om.h, C.byref(params), float(dt), _dp(t_prev),
+                                  flags.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(t_bc),
+                                  None if qp is None else _dp(qp))
+    colptr = np.empty(N + 1, np.int32)
+    rowidx = np.empty(nnz, np.int32)
+    vals = np.empty(nnz)
+    b = np.empty(N)
+    lib().orc_pspg_get(om.h, _ip(colptr), _ip(rowidx), _dp(vals), _dp(b))
+    return sp.csc_matrix((vals, rowidx, colptr), shape=(N, N)), b
+
+
+def heat_step(om, params, dt, t_prev, flags, t_bc=None, q_gp=None):
+    """`HeatEqIncompNewton::solve` without phase change: one Picard pass (runOnlyOnce,
+    HeatEquation.inl:195-196), the linear solve by SuperLU/COLAMD as in pspg_picard_step."""
+    from scipy.sparse.linalg import splu
+
+    A, b = heat_assemble(om, params, dt, t_prev, flags, t_bc, q_gp)
+    return splu(A, permc_spec="COLAMD").solve(b)
+
+
+def facet_gauss_positions(om):
+    """Facet::getPosFromGP at the heat Gauss points: (F, 3, dim)."""
+    F = om._facet_elm.size
+    out = np.empty((F, 3, om.dim))
+    lib().orc_facet_gauss_positions(om.h, _dp(out))
+    return out
 
 
 def wc_params(K0=2.2e7, K0p=7.0, rho_star=1000.0, mu=1e-3, g=(0.0, -9.81), meduri=True, sc=0.3, max_dt=1e-3,

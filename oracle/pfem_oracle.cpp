@@ -118,7 +118,21 @@ struct PspgParams {
     double gamma;      // surface tension coefficient (MomContEq "gamma")
     double tau0;       // Bingham yield stress (problem "Bingham"; 0 = Newtonian)
     double mReg;       // Bingham regularisation parameter
+    // problem "Boussinesq" (MomContEquation.inl:34-37,164-171,193-199): body-force factor
+    // rho (1 - alpha (T - Tr)) and PSPG gravity factor 1 - alpha (T - Tr) at each Gauss point,
+    // T interpolated from the node temperatures (null: not Boussinesq)
+    double alpha, Tr;
+    const double* T;
 };
+
+// HeatEqIncompNewton material (HeatEquation.inl:27-32) and the heat boundary-condition flags
+struct HeatParams {
+    double rho, cv, k;
+    double h, Tinf, epsRad;
+    int32_t fsFlags;   // flags of the free-surface tag (-2): HT_Q / HT_QH / HT_QR
+    int32_t pad;
+};
+constexpr uint8_t HT_T = 1, HT_Q = 2, HT_QH = 4, HT_QR = 8;
 
 struct WcParams {
     double K0, K0p, rhoStar, mu;
@@ -334,14 +348,16 @@ void getF(const OrcMesh& m, const ElemGeom& geo, F factor, const double* vec, do
 }
 
 // getH = |e| sum_g f w gradN^T vec, MatricesBuilder.inl:372-386
-void getH(const OrcMesh& m, const ElemGeom& geo, double factor, const Mat& G, const double* vec, double* out) {
+template <class F>
+void getH(const OrcMesh& m, const ElemGeom& geo, F factor, const Mat& G, const double* vec, double* out) {
     const int npe = m.npe, dim = m.dim;
     for (int i = 0; i < npe; ++i) out[i] = 0;
     for (int g = 0; g < m.gt.n; ++g) {
+        const double f = factor(g);
         for (int i = 0; i < npe; ++i) {
             double s = 0;
             for (int r = 0; r < dim; ++r) s += G(r, i) * vec[r];
-            out[i] += factor * s * m.gt.w[g];
+            out[i] += f * s * m.gt.w[g];
         }
     }
     double s = geo.detJ * m.gt.refSize;
@@ -548,8 +564,16 @@ void pspgElement(const OrcMesh& m, int e, const PspgParams& p, const double* qIt
     for (int g = 0; g < m.gt.n; ++g) lsum += (1 / p.rho) * m.gt.w[g];
     Mat L = getL(m, geo, lsum, G);
     double Fe[12], He[4];
-    getF(m, geo, [&](int) { return p.rho; }, p.g, Fe);
-    getH(m, geo, 1.0, G, p.g, He);
+    if (p.T) {
+        double Te[4];
+        for (int k = 0; k < npe; ++k) Te[k] = p.T[m.node(e, k)];
+        auto boussinesq = [&](int g) { return 1 - p.alpha * (nDot(m.gt, g, Te, npe) - p.Tr); };
+        getF(m, geo, [&](int g) { return p.rho * boussinesq(g); }, p.g, Fe);
+        getH(m, geo, boussinesq, G, p.g, He);
+    } else {
+        getF(m, geo, [&](int) { return p.rho; }, p.g, Fe);
+        getH(m, geo, [](int) { return 1.0; }, G, p.g, He);
+    }
     for (int i = 0; i < npe; ++i) He[i] *= tau;
 
     const int nv = dim * npe, nt = (dim + 1) * npe;
@@ -589,6 +613,106 @@ struct Triplet {
     int32_t row, col;
     double val;
 };
+
+// Eigen's SparseMatrix::setFromTriplets: duplicates are summed in triplet order, storage is
+// column-major with sorted row indices.  A stable sort by (col, row) keeps triplet order
+// inside each duplicate group, then the group is summed left to right.
+void setFromTriplets(OrcMesh& m, const std::vector<Triplet>& indexA, int R) {
+    std::vector<uint32_t> order(indexA.size());
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        const Triplet &ta = indexA[a], &tb = indexA[b];
+        return ta.col != tb.col ? ta.col < tb.col : ta.row < tb.row;
+    });
+    m.colptr.assign(R + 1, 0);
+    m.rowidx.clear();
+    m.vals.clear();
+    m.rowidx.reserve(indexA.size() / 3);
+    m.vals.reserve(indexA.size() / 3);
+    for (size_t k = 0; k < order.size();) {
+        const Triplet& t = indexA[order[k]];
+        double s = t.val;
+        size_t k2 = k + 1;
+        while (k2 < order.size() && indexA[order[k2]].col == t.col && indexA[order[k2]].row == t.row)
+            s += indexA[order[k2++]].val;
+        m.rowidx.push_back(t.row);
+        m.vals.push_back(s);
+        m.colptr[t.col + 1]++;
+        k = k2;
+    }
+    for (int c = 0; c < R; ++c) m.colptr[c + 1] += m.colptr[c];
+}
+
+// ---------------------------------------------------------------------------------------
+// Heat equation (HeatEqIncompNewton), srcs/simulation/physics/IncompNewton/HeatEquation.inl
+// ---------------------------------------------------------------------------------------
+// Facet Gauss rule (nGPLD = 3, HeatEquation.inl:13-22): Mesh::getGaussPoints/getGaussWeight/
+// getShapeFunctions/getRefElementSize of dimension d-1 (Mesh.cpp:342-530).
+struct FacetGauss {
+    double xi[3][2];
+    double w[3];
+    double sf[3][3];
+    double ref;
+};
+
+FacetGauss facetGauss(int dim) {
+    FacetGauss t{};
+    if (dim == 2) {
+        const double x[3] = {-std::sqrt(3.0 / 5.0), 0.0, std::sqrt(3.0 / 5.0)};
+        const double w[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
+        for (int g = 0; g < 3; ++g) {
+            t.xi[g][0] = x[g];
+            t.w[g] = w[g];
+            t.sf[g][0] = (1 - x[g]) / 2;
+            t.sf[g][1] = (1 + x[g]) / 2;
+        }
+        t.ref = 2.0;
+    } else {
+        const double p[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}, {2.0 / 3.0, 1.0 / 6.0}};
+        for (int g = 0; g < 3; ++g) {
+            t.xi[g][0] = p[g][0];
+            t.xi[g][1] = p[g][1];
+            t.w[g] = 1.0 / 3.0;
+            t.sf[g][0] = 1 - p[g][0] - p[g][1];
+            t.sf[g][1] = p[g][0];
+            t.sf[g][2] = p[g][1];
+        }
+        t.ref = 0.5;
+    }
+    return t;
+}
+
+// Facet::computeNormal (Facet.cpp:130-210): the normal of facetGeometry turned away from the
+// element's node that is not on the facet (Facet::getOutNode).
+void orientedNormal(const OrcMesh& m, int f, double n[3]) {
+    double detJ;
+    facetGeometry(m, f, detJ, n);
+    const int e = m.facetElm[f], a = m.facets[f];
+    int out = -1;
+    for (int k = 0; k < m.npe; ++k) {
+        const int v = m.node(e, k);
+        bool on = false;
+        for (int i = 0; i < m.dim; ++i) on |= m.facets[(size_t)i * m.F + f] == v;
+        if (!on) out = v;
+    }
+    double dot = 0;
+    for (int d = 0; d < m.dim; ++d) dot += n[d] * (m.x(out, d) - m.x(a, d));
+    if (dot > 0)
+        for (int d = 0; d < m.dim; ++d) n[d] = -n[d];
+}
+
+// Element matrices of HeatEqIncompNewton::m_buildAb (HeatEquation.inl:240-246): Me with the
+// factor cv rho (:54-59) and Le = dt getL with the factor k (:70-74).
+void heatElement(const OrcMesh& m, int e, const HeatParams& p, double dt, Mat& Me, Mat& Le) {
+    const ElemGeom& geo = m.geom[e];
+    Mat G = getGradN(m.dim, geo);
+    Me = getM(m, geo, [&](int) { return p.cv * p.rho; });
+    double ksum = 0;
+    for (int g = 0; g < m.gt.n; ++g) ksum += p.k * m.gt.w[g];
+    Le = getL(m, geo, ksum, G);
+    for (int i = 0; i < Le.r; ++i)
+        for (int j = 0; j < Le.c; ++j) Le(i, j) = dt * Le(i, j);
+}
 
 }  // namespace
 
@@ -770,32 +894,8 @@ int orc_pspg_assemble(OrcMesh* m, const PspgParams* p, const double* qIter, cons
         if (m->bound(n) || m->isFree[n])
             for (int d = 0; d < dim; ++d) indexA.push_back(Triplet{n + d * N, n + d * N, 1.0});
     }
-    // setFromTriplets (:136): duplicates are summed in triplet order, storage is
-    // column-major with sorted row indices.  A stable sort by (col, row) keeps triplet order
-    // inside each duplicate group, then the group is summed left to right.
-    std::vector<uint32_t> order(indexA.size());
-    std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
-        const Triplet &ta = indexA[a], &tb = indexA[b];
-        return ta.col != tb.col ? ta.col < tb.col : ta.row < tb.row;
-    });
-    m->colptr.assign(R + 1, 0);
-    m->rowidx.clear();
-    m->vals.clear();
-    m->rowidx.reserve(indexA.size() / 3);
-    m->vals.reserve(indexA.size() / 3);
-    for (size_t k = 0; k < order.size();) {
-        const Triplet& t = indexA[order[k]];
-        double s = t.val;
-        size_t k2 = k + 1;
-        while (k2 < order.size() && indexA[order[k2]].col == t.col && indexA[order[k2]].row == t.row)
-            s += indexA[order[k2++]].val;
-        m->rowidx.push_back(t.row);
-        m->vals.push_back(s);
-        m->colptr[t.col + 1]++;
-        k = k2;
-    }
-    for (int c = 0; c < R; ++c) m->colptr[c + 1] += m->colptr[c];
+    // setFromTriplets (:136)
+    setFromTriplets(*m, indexA, R);
     // RHS scatter in doublet order (:140-144)
     for (const auto& d : indexb) m->b[d.first] += d.second;
 
@@ -824,6 +924,132 @@ int orc_pspg_assemble(OrcMesh* m, const PspgParams* p, const double* qIter, cons
         }
     }
     return (int)m->vals.size();
+}
+
+// HeatEqIncompNewton::m_buildAb (HeatEquation.inl:226-305) and m_applyBC (:307-394) for one
+// Picard pass from T_prev.  hf[n]: HT_T (Dirichlet T = Tbc[n]), HT_Q / HT_QH / HT_QR (flux,
+// convection, radiation on the facets whose nodes all carry the flag; a free-surface facet
+// uses p->fsFlags).  qgp[(f*3 + g)*dim + d]: the prescribed flux vector at Gauss point g of
+// facet f (the "Q" BC function; read only for HT_Q facets, may be null otherwise).  The
+// system is left in colptr/rowidx/vals/b (orc_pspg_get).  Returns nnz.
+int orc_heat_assemble(OrcMesh* m, const HeatParams* p, double dt, const double* Tprev, const uint8_t* hf,
+                      const double* Tbc, const double* qgp) {
+    const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    const size_t tripletPerElm = (size_t)dim * npe * npe + (size_t)dim * npe * dim * npe + 3 * (size_t)npe * dim * npe +
+                                 (size_t)npe * npe;
+    // default-constructed triplets (0, 0, 0.0) stay in the unassigned slots (:232-233)
+    std::vector<Triplet> indexA(tripletPerElm * E, Triplet{0, 0, 0.0});
+    // doubletPerElm slots per element, of which the first npe*E are written (:236,:283); the
+    // rest stay (0, 0.0)
+    std::vector<std::pair<int32_t, double>> indexb((size_t)(2 * dim * npe + 2 * npe) * E, {0, 0.0});
+    m->b.assign(N, 0.0);
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        Mat Me, Le;
+        heatElement(*m, e, *p, dt, Me, Le);
+        double th[4];
+        for (int k = 0; k < npe; ++k) th[k] = Tprev[m->node(e, k)];
+        size_t countA = 0;
+        for (int i = 0; i < npe; ++i) {
+            const int ni = m->node(e, i);
+            for (int j = 0; j < npe; ++j) {
+                if (!(hf[ni] & HT_T)) {
+                    if (!m->isFree[ni]) indexA[tripletPerElm * e + countA] = Triplet{ni, m->node(e, j), Me(i, j)};
+                    countA++;
+                    if (!m->isFree[ni]) indexA[tripletPerElm * e + countA] = Triplet{ni, m->node(e, j), Le(i, j)};
+                    countA++;
+                }
+            }
+            double s = 0;
+            for (int j = 0; j < npe; ++j) s += Me(i, j) * th[j];
+            indexb[(size_t)npe * e + i] = {ni, s};
+        }
+    }
+    for (int n = 0; n < N; ++n)
+        if ((hf[n] & HT_T) || m->isFree[n]) indexA.push_back(Triplet{n, n, 1.0});
+    setFromTriplets(*m, indexA, N);
+    for (const auto& d : indexb) m->b[d.first] += d.second;
+
+    // facet loop (:315-375)
+    const FacetGauss fg = facetGauss(dim);
+    constexpr double sigma = 5.670374419e-8;
+    for (int f = 0; f < m->F; ++f) {
+        int nd[3];
+        bool fs = true;
+        for (int k = 0; k < dim; ++k) {
+            nd[k] = m->facets[(size_t)k * m->F + f];
+            fs = fs && (m->flags[nd[k]] & FREE_SURFACE);
+        }
+        bool bq = true, bqh = true, bqr = true;
+        for (int k = 0; k < dim; ++k) {
+            const int fl = fs ? p->fsFlags : hf[nd[k]];
+            bq = bq && (fl & HT_Q);
+            bqh = bqh && (fl & HT_QH);
+            bqr = bqr && (fl & HT_QR);
+        }
+        if (!bq && !bqh && !bqr) continue;
+        double detJ, nrm[3];
+        facetGeometry(*m, f, detJ, nrm);
+        double tf[3];
+        for (int k = 0; k < dim; ++k) tf[k] = Tprev[nd[k]];
+        if (bq) {  // getQN, MatricesBuilder.inl:246-272
+            orientedNormal(*m, f, nrm);
+            double qn[3] = {0, 0, 0};
+            for (int g = 0; g < 3; ++g) {
+                double qdn = 0;
+                for (int d = 0; d < dim; ++d) qdn += qgp[((size_t)f * 3 + g) * dim + d] * nrm[d];
+                const double fact = qdn * fg.w[g];
+                for (int k = 0; k < dim; ++k) qn[k] += fact * fg.sf[g][k];
+            }
+            for (int k = 0; k < dim; ++k) m->b[nd[k]] -= dt * (qn[k] * fg.ref * detJ);
+        }
+        for (int pass = 0; pass < 2; ++pass) {  // getSGamma, MatricesBuilder.inl:357-370 (:82-94)
+            if (!(pass == 0 ? bqh : bqr)) continue;
+            double sg[3] = {0, 0, 0};
+            for (int g = 0; g < 3; ++g) {
+                double T = 0;
+                for (int k = 0; k < dim; ++k) T += fg.sf[g][k] * tf[k];
+                const double fac = pass == 0 ? p->h * (T - p->Tinf)
+                                             : sigma * p->epsRad * (T * T * T * T - p->Tinf * p->Tinf * p->Tinf * p->Tinf);
+                for (int k = 0; k < dim; ++k) sg[k] += fac * fg.sf[g][k] * fg.w[g];
+            }
+            for (int k = 0; k < dim; ++k) m->b[nd[k]] -= dt * (sg[k] * (detJ * fg.ref));
+        }
+    }
+    // node loop (:377-393)
+    for (int n = 0; n < N; ++n) {
+        if (m->isFree[n] && !(hf[n] & HT_T)) {
+            m->b[n] = Tprev[n];
+        } else if (hf[n] & HT_T) {
+            const double r = Tbc[n];
+            m->b[n] = r;
+            for (int k = m->colptr[n]; k < m->colptr[n + 1]; ++k) {
+                if (m->rowidx[k] == n) continue;
+                m->b[m->rowidx[k]] -= m->vals[k] * r;
+                m->vals[k] = 0;
+            }
+        }
+    }
+    return (int)m->vals.size();
+}
+
+// Facet::getPosFromGP (Facet.cpp:227-237) at the three heat Gauss points of every facet:
+// out[(f*3 + g)*dim + d].  In 2D the facet Jacobian is half the edge (Facet.cpp:31-32) and the
+// Gauss points lie in [-1, 1], so the positions are those of the reference, centred on node 0.
+void orc_facet_gauss_positions(const OrcMesh* m, double* out) {
+    const int dim = m->dim;
+    const FacetGauss fg = facetGauss(dim);
+    for (int f = 0; f < m->F; ++f) {
+        const int a = m->facets[f], b = m->facets[(size_t)m->F + f];
+        const int c = dim == 3 ? m->facets[2 * (size_t)m->F + f] : a;
+        for (int g = 0; g < 3; ++g)
+            for (int d = 0; d < dim; ++d) {
+                double J0 = m->x(b, d) - m->x(a, d), J1 = 0;
+                if (dim == 2) J0 /= 2;
+                else J1 = m->x(c, d) - m->x(a, d);
+                out[((size_t)f * 3 + g) * dim + d] = J0 * fg.xi[g][0] + J1 * fg.xi[g][1] + m->x(a, d);
+            }
+    }
 }
 
 void orc_pspg_get(const OrcMesh* m, int32_t* colptr, int32_t* rowidx, double* vals, double* b) {

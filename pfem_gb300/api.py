@@ -37,7 +37,7 @@ EXPORTED = (
     "pfg_get_csr", "pfg_get_geometry", "pfg_linear_solve", "pfg_version", "pfg_set_profiling",
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
-    "pfg_upload_facets", "pfg_set_positions",
+    "pfg_upload_facets", "pfg_set_positions", "pfg_get_spmv_pairs",
 )
 NUM_PHASES = 15
 
@@ -110,6 +110,7 @@ def load(path=LIB_PATH):
         "pfg_set_profiling": ([vp, C.c_int32], C.c_int),
         "pfg_get_phase_times": ([vp, dp, i64p], C.c_int),
         "pfg_reset_phase_times": ([vp], C.c_int),
+        "pfg_get_spmv_pairs": ([vp, i64p], C.c_int),
         "pfg_phase_name": ([C.c_int32], C.c_char_p),
         "pfg_wc_step_async": ([vp, C.c_double, C.c_int32], C.c_int),
         "pfg_synchronize": ([vp, C.POINTER(StepStatus)], C.c_int),
@@ -337,6 +338,12 @@ class Context:
         self._check(self.L.pfg_get_phase_times(self.h, _dp(ms), n.ctypes.data_as(C.POINTER(C.c_int64))),
                     "pfg_get_phase_times")
         return {self.L.pfg_phase_name(i).decode(): (float(ms[i]), int(n[i])) for i in range(NUM_PHASES) if n[i]}
+
+    def spmv_pairs(self):
+        """Node pairs read by the timed Krylov SpMV launches since the last reset."""
+        v = C.c_int64()
+        self._check(self.L.pfg_get_spmv_pairs(self.h, C.byref(v)), "pfg_get_spmv_pairs")
+        return int(v.value)
 
     def linear_solve(self, x0):
         x = np.ascontiguousarray(x0, np.float64).copy()

@@ -212,6 +212,15 @@ PFG_API int pfg_get_phase_times(pfg_ctx* c, double* ms, int64_t* launches) {
     return PFG_OK;
 }
 
+PFG_API int pfg_get_spmv_pairs(pfg_ctx* c, int64_t* pairs) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!pairs) return fail(c, PFG_ERR_INVALID, "null pointer");
+    if ((rc = prof_flush(c))) return rc;
+    *pairs = c->spmv_pairs;
+    return PFG_OK;
+}
+
 PFG_API int pfg_reset_phase_times(pfg_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
@@ -220,6 +229,7 @@ PFG_API int pfg_reset_phase_times(pfg_ctx* c) {
         c->phase_ms[i] = 0;
         c->phase_n[i] = 0;
     }
+    c->spmv_pairs = 0;
     return PFG_OK;
 }
 
@@ -295,7 +305,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DBuf* bufs[] = {&c->pos, &c->pos_save, &c->flags, &c->conn, &c->ne_ptr, &c->ne_elem, &c->ne_loc,
                     &c->nbr_ptr, &c->nbr, &c->pair_node, &c->row_ptr, &c->col, &c->val, &c->val32,
-                    &c->diag_pos, &c->rhs, &c->edata, &c->edata32, &c->q, &c->q_prev, &c->q_iter_prev,
+                    &c->diag_pos, &c->rhs, &c->edata, &c->edata_df, &c->q, &c->q_prev, &c->q_iter_prev,
                     &c->vbc, &c->kv, &c->kv32, &c->binv, &c->red, &c->err_word, &c->ws, &c->wc_el, &c->wc_dt,
                     &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot, &c->binv32, &c->node_inst,
                     &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt, &c->mx_scale,

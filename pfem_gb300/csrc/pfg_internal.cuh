@@ -86,7 +86,7 @@ struct pfg_ctx {
     pfg::DBuf row_ptr, col, val, val32, diag_pos, rhs;
     int64_t nnz = 0;
     // element data: detJ, tau, gradN (SoA)
-    pfg::DBuf edata, edata32;
+    pfg::DBuf edata, edata_df;  // element data: FP64, and its double-float copy (mixed form)
     // incompressible states
     pfg::DBuf q, q_prev, q_iter_prev, vbc;
     // Krylov workspace
@@ -116,6 +116,9 @@ struct pfg_ctx {
     std::vector<int> marks;  // (phase, ev_start, ev_stop) triples
     double phase_ms[PFG_NUM_PHASES] = {};
     long long phase_n[PFG_NUM_PHASES] = {};
+    long long spmv_pairs = 0;             // node pairs read by the timed Krylov SpMV launches
+    long long spmv_list_pairs = 0;        // node pairs of the instances the next launch covers
+    std::vector<long long> h_inst_pairs;  // node pairs per instance
     // WC: FP64 element partials, per-node CFL quantities, captured step graphs [fixed, adaptive]
     pfg::DBuf wc_eld, wc_nodal;
     cudaGraphExec_t wc_graph[2] = {nullptr, nullptr};

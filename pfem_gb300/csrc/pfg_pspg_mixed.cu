@@ -30,6 +30,7 @@
 #include "pfg_device.cuh"
 #include "pfg_internal.cuh"
 #include "pfg_blocks.cuh"
+#include "pfg_df.cuh"
 #include "pfg_pspg_common.cuh"
 
 namespace pfg {
@@ -68,6 +69,7 @@ struct Mx {
 struct MxConst {
     double refSize, sumw;
     PspgTables t;
+    DF mm_df[4][4], s_df[4], ref_df;  // double-float copies of the tables and refSize
     double rtol, atol, eta, min_res;
     int max_iter;
 };
@@ -95,6 +97,12 @@ MxConst mx_const(pfg_ctx* c) {
         for (int j = 0; j < 4; ++j) k.t.MM[i][j] = g.MM[i][j];
     }
     for (int f = 0; f < 3; ++f) k.t.g[f] = c->prm.gravity[f];
+    auto split = [](double d) { const float h = (float)d; return DF{h, (float)(d - (double)h)}; };
+    for (int i = 0; i < 4; ++i) {
+        k.s_df[i] = split(g.s[i]);
+        for (int j = 0; j < 4; ++j) k.mm_df[i][j] = split(g.MM[i][j]);
+    }
+    k.ref_df = split(g.refSize);
     k.rtol = c->prm.krylov_rel_tol;
     k.atol = c->prm.krylov_abs_tol;
     k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-4;
@@ -172,7 +180,7 @@ __device__ __forceinline__ PspgCoef inst_coef_d(const double* id, double sumw, d
 template <int DIM>
 __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
                           const double* __restrict__ q_iter, Mx m, double refSize, ViscArgs va,
-                          double* __restrict__ ed) {
+                          double* __restrict__ ed, DF* __restrict__ edf) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -207,6 +215,9 @@ __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const doub
 #pragma unroll
         for (int i = 0; i <= DIM; ++i) ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
     ed[(size_t)ed_ksum<DIM>() * E + e] = k_sum<DIM>(va, mu, G, q_iter, N, nd);
+    // double-float copy for the pair assembly (FP64 conversions once per element, not per pair)
+#pragma unroll
+    for (int v = 0; v < ed_count<DIM>(); ++v) edf[(size_t)v * E + e] = df_from(ed[(size_t)v * E + e]);
 }
 
 // Right-hand side of the nodes of active instances (element doublets + node BCs).
@@ -228,18 +239,86 @@ __global__ void k_mx_rhs(int N, int E, const int* __restrict__ ne_ptr, const int
     rhs[(size_t)DIM * N + n] = bp;
 }
 
+// Block (n, m) like pspg_pair_block (same gather, element order and expressions), evaluated in
+// double-float on the FP32 pipe from the double-float element data; returned in FP64.  On
+// GB300 the FP64 evaluation is bound by the FP64 pipe (87% busy, 1/64 of the FP32 rate);
+// double-float carries ~48 bits, so the values agree with the FP64 evaluation to ~1e-14 of
+// the row scale.
+struct PairDF {
+    DF rho, inv_dt, refSize, l_sum;
+};
+
+template <int DIM>
+__device__ __forceinline__ void pspg_pair_block_df(int n, int m, int E, const int* __restrict__ ne_ptr,
+                                                   const int* __restrict__ ne_elem,
+                                                   const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
+                                                   const DF* __restrict__ edf, const PairDF& k,
+                                                   const DF (&MM)[4][4], const DF (&S)[4],
+                                                   double (&out)[DIM + 1][DIM + 1]) {
+    constexpr int NPE = DIM + 1;
+    DF acc[NPE][NPE];
+#pragma unroll
+    for (int a = 0; a < NPE; ++a)
+#pragma unroll
+        for (int b = 0; b < NPE; ++b) acc[a][b] = DF{0.0f, 0.0f};
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const int e = ne_elem[q];
+        int j = -1;
+#pragma unroll
+        for (int jj = 0; jj < NPE; ++jj)
+            if (__ldg(conn + (size_t)jj * E + e) == m) j = jj;
+        if (j < 0) continue;
+        const int i = ne_loc[q];
+        const DF detJ = edf[e];
+        const DF tau = edf[(size_t)E + e];
+        const DF ae = df_mul(detJ, k.refSize);
+        DF gi[DIM], gj[DIM];
+#pragma unroll
+        for (int f = 0; f < DIM; ++f) {
+            gi[f] = edf[(size_t)(2 + f * NPE + i) * E + e];
+            gj[f] = edf[(size_t)(2 + f * NPE + j) * E + e];
+        }
+        DF dot = df_mul(gi[0], gj[0]);
+#pragma unroll
+        for (int f = 1; f < DIM; ++f) dot = df_add(dot, df_mul(gi[f], gj[f]));
+        const DF mij = df_mul(k.inv_dt, df_mul(df_mul(k.rho, MM[i][j]), ae));
+        const DF kf = df_mul(ae, edf[(size_t)ed_ksum<DIM>() * E + e]);
+#pragma unroll
+        for (int f1 = 0; f1 < DIM; ++f1) {
+#pragma unroll
+            for (int f2 = 0; f2 < DIM; ++f2) {
+                const DF g2 = df_mul(gi[f2], gj[f1]);
+                const DF kv = df_mul(kf, f1 == f2 ? df_add(dot, g2) : g2);
+                acc[f1][f2] = df_add(acc[f1][f2], f1 == f2 ? df_add(mij, kv) : kv);
+            }
+            acc[f1][DIM] = df_add(acc[f1][DIM], df_neg(df_mul(df_mul(ae, S[j]), gi[f1])));
+        }
+        const DF ctau = df_mul(tau, k.inv_dt);
+#pragma unroll
+        for (int f2 = 0; f2 < DIM; ++f2) {
+            const DF c1 = df_mul(ctau, df_mul(df_mul(ae, gi[f2]), S[j]));
+            const DF c2 = df_mul(df_mul(ae, S[i]), gj[f2]);
+            acc[DIM][f2] = df_add(acc[DIM][f2], df_add(c1, c2));
+        }
+        acc[DIM][DIM] = df_add(acc[DIM][DIM], df_mul(tau, df_mul(df_mul(ae, k.l_sum), dot)));
+    }
+#pragma unroll
+    for (int a = 0; a < NPE; ++a)
+#pragma unroll
+        for (int b = 0; b < NPE; ++b) out[a][b] = df_to(acc[a][b]);
+}
+
 // FP64 matrix values of active instances, one thread per node pair: the same gather, element
-// order and Dirichlet elimination as the FP64 path.
+// order and Dirichlet elimination as the FP64 path, the block evaluated in double-float.
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const int* __restrict__ pair_node,
                                                     const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
                                                     const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
                                                     const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
-                                                    const double* __restrict__ ed, const uint8_t* __restrict__ flags,
+                                                    const DF* __restrict__ edf, const uint8_t* __restrict__ flags,
                                                     const int* __restrict__ row_ptr, double* __restrict__ val,
                                                     const double* __restrict__ vbc, double* __restrict__ rhs, Mx m,
                                                     MxConst k) {
-    constexpr int NPE = DIM + 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P) return;
     const int n = pair_node[t];
@@ -255,9 +334,16 @@ __global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const i
         for (int f = 0; f <= DIM; ++f) val[row_ptr[n + f * N]] = 1.0;
         return;
     }
-    const PspgCoef cf = inst_coef_d(m.id + inst * D_COUNT, k.sumw, k.refSize);
-    double acc[NPE][NPE];
-    pspg_pair_block<DIM>(n, mm, E, ne_ptr, ne_elem, ne_loc, conn, ed, cf, k.t, acc);
+    PairDF kd;
+    {
+        const double* id = m.id + inst * D_COUNT;
+        kd.rho = df_from(id[D_RHO]);
+        kd.inv_dt = df_from(1 / id[D_DT]);
+        kd.refSize = k.ref_df;
+        kd.l_sum = df_from(k.sumw / id[D_RHO]);
+    }
+    double acc[DIM + 1][DIM + 1];
+    pspg_pair_block_df<DIM>(n, mm, E, ne_ptr, ne_elem, ne_loc, conn, edf, kd, k.mm_df, k.s_df, acc);
     pspg_write_block<DIM>(n, mm, N, deg, rank, fn, flags[mm], row_ptr, acc, true, vbc, rhs, val, nullptr);
 }
 
@@ -893,7 +979,8 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     if (E > 0) {
         prof_begin(c, PH_PSPG_ELEM);
         k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), q_iter,
-                                                                  m, k.refSize, visc_args(c), ptr<double>(c->edata));
+                                                                  m, k.refSize, visc_args(c), ptr<double>(c->edata),
+                                                                  ptr<DF>(c->edata_df));
         prof_end(c, PH_PSPG_ELEM);
         PFG_CHECK_LAUNCH(c);
     }
@@ -911,7 +998,7 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     prof_begin(c, PH_PSPG_PAIRS);
     k_mx_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
         c->P, N, E, ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(c->ne_ptr),
-        ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<double>(c->edata),
+        ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<DF>(c->edata_df),
         ptr<uint8_t>(c->flags), ptr<int>(c->row_ptr), ptr<double>(c->val), ptr<double>(c->vbc), ptr<double>(c->rhs),
         m, k);
     double* scale = ptr<double>(c->mx_scale);
@@ -1024,12 +1111,18 @@ struct KSet {
     void up_x(pfg_ctx* c, int grid) const {
         k_mx_up_x<T, DIM><<<grid, NB, 0, c->stream>>>(m, list, scb, slot, N, x, scale, W, ld);
     }
+    // The FP32 products are the timed "Krylov SpMV" phase (with the node pairs they read); the
+    // FP64 fallback's stay in the iteration phase only.
     template <int MODE>
     void spmv(pfg_ctx* c, int grid) const {
-        prof_begin(c, PH_KRYLOV_SPMV);
+        constexpr bool F32 = sizeof(T) == 4;
+        if (F32) {
+            prof_begin(c, PH_KRYLOV_SPMV);
+            if (c->prof) c->spmv_pairs += c->spmv_list_pairs;
+        }
         k_mx_spmv<T, DIM, MODE><<<grid, NB * node_lanes<DIM>(), 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr,
                                                                               val, W, ld);
-        prof_end(c, PH_KRYLOV_SPMV);
+        if (F32) prof_end(c, PH_KRYLOV_SPMV);
     }
 
     void iterate(pfg_ctx* c, int grid) const {
@@ -1170,10 +1263,13 @@ int mx_inner_batch(pfg_ctx* c, Counters* cnt) {
         std::vector<int> n32, n64;
         n32.reserve(c->n_seg);
         n64.reserve(c->n_seg);
+        c->spmv_list_pairs = 0;
         for (int i = 0; i < K; ++i) {
             const int b0 = hi[(size_t)i * I_COUNT + I_B0], b1 = hi[(size_t)i * I_COUNT + I_B1];
-            if (done32[(size_t)i * M_COUNT + M_DONE] == 0.0f)
+            if (done32[(size_t)i * M_COUNT + M_DONE] == 0.0f) {
                 for (int b = b0; b < b1; ++b) n32.push_back(b);
+                c->spmv_list_pairs += c->h_inst_pairs[i];
+            }
             if (done64[(size_t)i * M_COUNT + M_DONE] == 0.0)
                 for (int b = b0; b < b1; ++b) n64.push_back(b);
         }
@@ -1297,9 +1393,10 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
 }  // namespace
 
 int mx_alloc(pfg_ctx* c) {
-    const size_t R = std::max(c->R, 1), N = std::max(c->N, 1);
+    const size_t R = std::max(c->R, 1), N = std::max(c->N, 1), E = std::max(c->E, 1);
+    const int ned = c->dim == 2 ? ed_count<2>() : ed_count<3>();
     int rc;
-    if ((rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))) ||
+    if ((rc = ensure(c, c->edata_df, sizeof(DF) * ned * E)) || (rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))) ||
         (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) || (rc = ensure(c, c->mx_scale, sizeof(double) * R)) ||
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))
@@ -1377,7 +1474,13 @@ int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* 
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_id.p, c->h_mx_id.data(), sizeof(double) * c->h_mx_id.size(),
                                 cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaMemsetAsync(c->mx_sc.p, 0, sizeof(float) * (size_t)n_inst * M_COUNT, c->stream));
+    // node pairs per instance (the work of its SpMV rows, for the phase counters)
+    std::vector<int> nptr((size_t)N + 1);
+    PFG_CUDA(c, cudaMemcpyAsync(nptr.data(), c->nbr_ptr.p, sizeof(int) * nptr.size(), cudaMemcpyDeviceToHost,
+                                c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->h_inst_pairs.assign(n_inst, 0);
+    for (int i = 0; i < n_inst; ++i) c->h_inst_pairs[i] = (long long)nptr[node_off[i + 1]] - nptr[node_off[i]];
     return PFG_OK;
 }
 
