@@ -123,7 +123,33 @@ typedef struct pfg_params {
        strain-rate norm of the Picard iterate                                             */
     double tau0;               /* yield stress (0 = Newtonian)                             */
     double m_reg;              /* regularisation parameter mReg                            */
+    /* incompressible, heat equation (HeatEqIncompNewton, IncompNewton/HeatEquation.inl:27-32;
+       problems "Conduction" and "Boussinesq"); used by pfg_heat_step:                      */
+    double heat_k;             /* thermal conductivity k                                   */
+    double heat_cv;            /* specific heat cv (the heat mass factor is cv rho)        */
+    double heat_h;             /* convection coefficient h of the Qh facets                */
+    double heat_t_inf;         /* ambient temperature Tinf of the Qh / Qr facets           */
+    double heat_eps_rad;       /* emissivity epsRad of the Qr facets                       */
+    int32_t heat_fs_flags;     /* pfg_heat_flag bits of the free-surface tag: PFG_HEAT_Q,
+                                  PFG_HEAT_QH, PFG_HEAT_QR (FreeSurfaceQ / Qh / Qr)        */
+    int32_t boussinesq;        /* 1: problem "Boussinesq" (MomContEquation.inl:164-199): the
+                                  PSPG body force uses rho (1 - alpha (T - Tr)) and the
+                                  pressure-row gravity term 1 - alpha (T - Tr) at each
+                                  Gauss point, T the node temperatures                     */
+    double alpha_t;            /* thermal expansion coefficient alpha                      */
+    double t_ref;              /* reference temperature Tr                                 */
 } pfg_params;
+
+/* Heat boundary-condition flags per node (the reference's tag flags of HeatEq's BC table,
+ * IncompNewton/Solver.cpp:132-170): T Dirichlet, Q prescribed flux, Qh convection, Qr
+ * radiation.  A facet takes a flux term when all its nodes carry the flag; a free-surface
+ * facet uses pfg_params.heat_fs_flags instead (HeatEquation.inl:319-335). */
+typedef enum pfg_heat_flag {
+    PFG_HEAT_T = 1,
+    PFG_HEAT_Q = 2,
+    PFG_HEAT_QH = 4,
+    PFG_HEAT_QR = 8
+} pfg_heat_flag;
 
 typedef struct pfg_step_status {
     int32_t converged;         /* 1 = step accepted (reference: solveOneTimeStep() true)   */
@@ -286,6 +312,29 @@ PFG_API int pfg_set_profiling(pfg_ctx* ctx, int32_t enable);
 /* Accumulated milliseconds and launch counts per phase since the last reset. */
 PFG_API int pfg_get_phase_times(pfg_ctx* ctx, double* ms, int64_t* launches);
 PFG_API int pfg_reset_phase_times(pfg_ctx* ctx);
+/* ---- Heat equation and Boussinesq coupling (incompressible contexts) --------------------
+ * The temperature is one value per node (the reference's state dim+1 of a Boussinesq problem,
+ * state 0 of a Conduction problem), kept on the device next to the flow states.  Node
+ * temperatures are reset to zero by pfg_upload_mesh. */
+PFG_API int pfg_set_temperature(pfg_ctx* ctx, const double* T);   /* N values */
+PFG_API int pfg_get_temperature(pfg_ctx* ctx, double* T);
+/* Heat boundary conditions: flags[n] (pfg_heat_flag bits) and the Dirichlet temperature
+ * t_dirichlet[n] of PFG_HEAT_T nodes (the "T" BC function evaluated by the caller at the
+ * node position and time t + dt, HeatEquation.inl:384-389).  Needs the facets of the mesh
+ * (pfg_upload_facets) when any node or heat_fs_flags has a flux flag.  Replaces the BC
+ * evaluation of HeatEqIncompNewton::m_applyBC (:307-394). */
+PFG_API int pfg_heat_set_bc(pfg_ctx* ctx, const uint8_t* flags, const double* t_dirichlet);
+/* Prescribed heat flux vectors at the three Gauss points of every facet: q_gp[(f*3 + g)*dim
+ * + d] (the "Q" BC function at Facet::getPosFromGP, time t + dt; MatricesBuilder.inl:
+ * 246-272).  Read for the facets that take the Q term; NULL clears it. */
+PFG_API int pfg_heat_set_flux(pfg_ctx* ctx, const double* q_gp);
+/* One HeatEqIncompNewton::solve without phase change (one Picard pass, HeatEquation.inl:
+ * 195-196, 216-224): assembles (cv rho M + dt k L) T = cv rho M T_prev + boundary terms at
+ * the current positions, solves it (FP64 conjugate gradients, Jacobi preconditioner, to the
+ * Krylov tolerances of the params) and replaces the node temperatures.  On failure the
+ * temperatures are unchanged.  st->krylov_iterations and st->residual report the solve. */
+PFG_API int pfg_heat_step(pfg_ctx* ctx, double dt, pfg_step_status* st);
+
 /* Node pairs ((d+1)^2 blocks) read by the timed Krylov SpMV launches (phase 12) since the last
  * reset: the algorithmic work of those launches in a batch whose converged instances drop out
  * of the products (mixed precision; the plain FP64 form reports 0). */

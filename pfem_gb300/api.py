@@ -37,7 +37,8 @@ EXPORTED = (
     "pfg_get_csr", "pfg_get_geometry", "pfg_linear_solve", "pfg_version", "pfg_set_profiling",
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
-    "pfg_upload_facets", "pfg_set_positions", "pfg_get_spmv_pairs",
+    "pfg_upload_facets", "pfg_set_positions", "pfg_get_spmv_pairs", "pfg_set_temperature",
+    "pfg_get_temperature", "pfg_heat_set_bc", "pfg_heat_set_flux", "pfg_heat_step",
 )
 NUM_PHASES = 15
 
@@ -56,7 +57,14 @@ class Params(C.Structure):
         ("gamma", C.c_double),
         ("preconditioner", C.c_int32), ("pad2", C.c_int32),
         ("tau0", C.c_double), ("m_reg", C.c_double),
+        ("heat_k", C.c_double), ("heat_cv", C.c_double), ("heat_h", C.c_double), ("heat_t_inf", C.c_double),
+        ("heat_eps_rad", C.c_double), ("heat_fs_flags", C.c_int32), ("boussinesq", C.c_int32),
+        ("alpha_t", C.c_double), ("t_ref", C.c_double),
     ]
+
+
+# heat boundary-condition flags (pfg_heat_flag)
+HEAT_T, HEAT_Q, HEAT_QH, HEAT_QR = 1, 2, 4, 8
 
 
 class StepStatus(C.Structure):
@@ -111,6 +119,11 @@ def load(path=LIB_PATH):
         "pfg_get_phase_times": ([vp, dp, i64p], C.c_int),
         "pfg_reset_phase_times": ([vp], C.c_int),
         "pfg_get_spmv_pairs": ([vp, i64p], C.c_int),
+        "pfg_set_temperature": ([vp, dp], C.c_int),
+        "pfg_get_temperature": ([vp, dp], C.c_int),
+        "pfg_heat_set_bc": ([vp, u8p, dp], C.c_int),
+        "pfg_heat_set_flux": ([vp, dp], C.c_int),
+        "pfg_heat_step": ([vp, C.c_double, C.POINTER(StepStatus)], C.c_int),
         "pfg_phase_name": ([C.c_int32], C.c_char_p),
         "pfg_wc_step_async": ([vp, C.c_double, C.c_int32], C.c_int),
         "pfg_synchronize": ([vp, C.POINTER(StepStatus)], C.c_int),
@@ -230,6 +243,44 @@ class Context:
         values = np.ascontiguousarray(values, np.float64)
         self._check(self.L.pfg_set_dirichlet(self.h, nodes.size, nodes.ctypes.data_as(C.POINTER(C.c_int32)),
                                              _dp(values)), "pfg_set_dirichlet")
+
+    # ---- heat equation (incompressible contexts) ----
+    def set_temperature(self, T):
+        T = np.ascontiguousarray(T, np.float64)
+        assert T.size == self.N
+        self._check(self.L.pfg_set_temperature(self.h, _dp(T)), "pfg_set_temperature")
+
+    def get_temperature(self, out=None):
+        if out is None:
+            out = np.empty(self.N)
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.N
+        self._check(self.L.pfg_get_temperature(self.h, _dp(out)), "pfg_get_temperature")
+        return out
+
+    def heat_set_bc(self, flags, t_dirichlet=None):
+        """Per-node heat BC flags (HEAT_T / HEAT_Q / HEAT_QH / HEAT_QR) and Dirichlet temperatures."""
+        flags = np.ascontiguousarray(flags, np.uint8)
+        assert flags.size == self.N
+        tp = None
+        if t_dirichlet is not None:
+            self._tbc = np.ascontiguousarray(t_dirichlet, np.float64)
+            assert self._tbc.size == self.N
+            tp = _dp(self._tbc)
+        self._check(self.L.pfg_heat_set_bc(self.h, flags.ctypes.data_as(C.POINTER(C.c_uint8)), tp),
+                    "pfg_heat_set_bc")
+
+    def heat_set_flux(self, q_gp):
+        """Flux vectors at the three Gauss points of every facet, (F, 3, dim), or None."""
+        if q_gp is None:
+            self._check(self.L.pfg_heat_set_flux(self.h, None), "pfg_heat_set_flux")
+            return
+        q = np.ascontiguousarray(q_gp, np.float64)
+        self._check(self.L.pfg_heat_set_flux(self.h, _dp(q)), "pfg_heat_set_flux")
+
+    def heat_step(self, dt):
+        st = StepStatus()
+        self._check(self.L.pfg_heat_step(self.h, float(dt), C.byref(st)), "pfg_heat_step")
+        return st
 
     def picard_step(self, dt):
         st = StepStatus()

@@ -273,6 +273,10 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     if (params->linear_solver != PFG_LINSOLVE_BICGSTAB) return PFG_ERR_UNSUPPORTED;
     if (params->tau0 < 0 || (params->tau0 > 0 && !(params->m_reg > 0))) return PFG_ERR_INVALID;
     if (params->tau0 > 0 && params->kind != PFG_KIND_INCOMP_PSPG) return PFG_ERR_UNSUPPORTED;  // Bingham: PSPG only
+    // Boussinesq coupling and the heat equation: incompressible (PSPG) contexts only
+    if (params->boussinesq && params->kind != PFG_KIND_INCOMP_PSPG) return PFG_ERR_UNSUPPORTED;
+    if (params->boussinesq != 0 && params->boussinesq != 1) return PFG_ERR_INVALID;
+    if (params->heat_fs_flags & ~(PFG_HEAT_Q | PFG_HEAT_QH | PFG_HEAT_QR)) return PFG_ERR_INVALID;
     pfg_ctx* c = new (std::nothrow) pfg_ctx();
     if (!c) return PFG_ERR_NOMEM;
     c->prm = *params;
@@ -310,7 +314,8 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->stage, &c->wc_eld, &c->wc_nodal, &c->inc_slot, &c->binv32, &c->node_inst,
                     &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt, &c->mx_scale,
                     &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force,
-                    &c->mg_x0, &c->mg_in64, &c->val16};
+                    &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
+                    &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q};
     wc_release_graphs(c);
     mg_release(c);
     mx_release_graph(c);
@@ -355,6 +360,8 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
     c->h_flags.assign(flags, flags + N);
     c->h_conn.assign(conn, conn + (size_t)npe * E);
     c->has_facets = false;
+    c->h_facets.clear();
+    c->h_facet_elm.clear();
     c->F = 0;
     c->n_fst_nodes = 0;
     PFG_CUDA(c, cudaMemcpyAsync(c->pos.p, pos, sizeof(double) * dim * N, cudaMemcpyHostToDevice, c->stream));
@@ -365,6 +372,10 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
     if ((rc = build_topology(c))) return rc;
     if (c->prm.kind == PFG_KIND_INCOMP_PSPG) {
         if ((rc = pspg_alloc(c)) || (rc = krylov_alloc(c))) return rc;
+        // heat buffers: allocated with the mesh for Boussinesq contexts (the assembly reads the
+        // temperatures), else on first use of the heat API
+        c->heat_ready = false;
+        if (c->prm.boussinesq && (rc = heat_alloc(c))) return rc;
         if (c->prm.precision == PFG_PREC_MIXED && (rc = mx_alloc(c))) return rc;
     } else {
         if ((rc = wc_alloc(c))) return rc;
@@ -434,9 +445,100 @@ PFG_API int pfg_upload_facets(pfg_ctx* c, int32_t n_facets, const int32_t* facet
     c->F = F;
     c->n_fst_nodes = (int)nodes.size();
     c->has_facets = true;
+    c->h_facets.assign(facets, facets + (size_t)dim * F);
+    c->h_facet_elm.assign(facet_elm, facet_elm + F);
+    c->has_heat_q = false;  // flux vectors are per facet: a new facet list needs new ones
     // captured WC step graphs hold the previous facet arguments
     if (c->prm.kind == PFG_KIND_WC_CDS_DPDT) wc_release_graphs(c);
     return PFG_OK;
+}
+
+// ---- heat equation -----------------------------------------------------------------------
+
+namespace {
+int check_heat(pfg_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG)
+        return fail(c, PFG_ERR_UNSUPPORTED, "the heat equation needs an incompressible (PSPG) context");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    return c->heat_ready ? PFG_OK : heat_alloc(c);
+}
+}  // namespace
+
+PFG_API int pfg_set_temperature(pfg_ctx* c, const double* T) {
+    int rc = check_heat(c);
+    if (rc) return rc;
+    if (!T) return fail(c, PFG_ERR_INVALID, "null temperatures");
+    PFG_CUDA(c, cudaMemcpyAsync(c->heat_t.p, T, sizeof(double) * c->N, cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+PFG_API int pfg_get_temperature(pfg_ctx* c, double* T) {
+    int rc = check_heat(c);
+    if (rc) return rc;
+    if (!T) return fail(c, PFG_ERR_INVALID, "null temperatures");
+    PFG_CUDA(c, cudaMemcpyAsync(T, c->heat_t.p, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+PFG_API int pfg_heat_set_bc(pfg_ctx* c, const uint8_t* flags, const double* t_dirichlet) {
+    int rc = check_heat(c);
+    if (rc) return rc;
+    if (!flags) return fail(c, PFG_ERR_INVALID, "null heat flags");
+    const int N = c->N;
+    bool any_t = false;
+    for (int n = 0; n < N; ++n) {
+        if (flags[n] & ~(PFG_HEAT_T | PFG_HEAT_Q | PFG_HEAT_QH | PFG_HEAT_QR))
+            return fail(c, PFG_ERR_INVALID, "node %d: unknown heat flag bits 0x%x", n, flags[n]);
+        // the reference rejects a boundary with both a T and a flux condition (Solver.cpp:160-162)
+        if ((flags[n] & PFG_HEAT_T) && (flags[n] & (PFG_HEAT_Q | PFG_HEAT_QH | PFG_HEAT_QR)))
+            return fail(c, PFG_ERR_INVALID, "node %d: both a T and a flux heat condition", n);
+        any_t |= (flags[n] & PFG_HEAT_T) != 0;
+    }
+    if (any_t && !t_dirichlet) return fail(c, PFG_ERR_INVALID, "Dirichlet heat nodes need t_dirichlet");
+    c->h_heat_flags.assign(flags, flags + N);
+    PFG_CUDA(c, cudaMemcpyAsync(c->heat_flags.p, flags, N, cudaMemcpyHostToDevice, c->stream));
+    if (t_dirichlet)
+        PFG_CUDA(c, cudaMemcpyAsync(c->heat_tbc.p, t_dirichlet, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->has_heat_bc = true;
+    return PFG_OK;
+}
+
+PFG_API int pfg_heat_set_flux(pfg_ctx* c, const double* q_gp) {
+    int rc = check_heat(c);
+    if (rc) return rc;
+    if (!q_gp) {
+        c->has_heat_q = false;
+        return PFG_OK;
+    }
+    if (!c->has_facets) return fail(c, PFG_ERR_STATE, "pfg_heat_set_flux: call pfg_upload_facets first");
+    const size_t n = (size_t)std::max(c->F, 1) * 3 * c->dim;
+    if ((rc = ensure(c, c->heat_q, sizeof(double) * n))) return rc;
+    if (c->F)
+        PFG_CUDA(c, cudaMemcpyAsync(c->heat_q.p, q_gp, sizeof(double) * (size_t)c->F * 3 * c->dim,
+                                    cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->has_heat_q = true;
+    return PFG_OK;
+}
+
+PFG_API int pfg_heat_step(pfg_ctx* c, double dt, pfg_step_status* st) {
+    int rc = check_heat(c);
+    if (rc) return rc;
+    if (!st) return fail(c, PFG_ERR_INVALID, "null status");
+    if (!(dt > 0)) return fail(c, PFG_ERR_INVALID, "dt must be > 0");
+    if (!(c->prm.heat_cv * c->prm.rho > 0) || !(c->prm.heat_k >= 0))
+        return fail(c, PFG_ERR_INVALID, "heat: needs cv rho > 0 and k >= 0");
+    bool flux = (c->prm.heat_fs_flags & (PFG_HEAT_Q | PFG_HEAT_QH | PFG_HEAT_QR)) != 0;
+    for (uint8_t f : c->h_heat_flags) flux |= (f & (PFG_HEAT_Q | PFG_HEAT_QH | PFG_HEAT_QR)) != 0;
+    if (flux && !c->has_facets) return fail(c, PFG_ERR_STATE, "heat flux conditions need pfg_upload_facets");
+    std::memset(st, 0, sizeof(*st));
+    if ((rc = heat_build_facets(c))) return rc;
+    return heat_step(c, dt, st);
 }
 
 PFG_API int pfg_set_states(pfg_ctx* c, const double* states) {

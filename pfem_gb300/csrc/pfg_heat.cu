@@ -1,0 +1,576 @@
+// Heat equation of the incompressible solver (HeatEqIncompNewton, IncompNewton/HeatEquation.inl)
+// on the device: assembly over the node pairs, boundary terms gathered at the nodes, and an FP64
+// conjugate-gradient solve.
+//
+// One pass of HeatEqIncompNewton::solve without phase change (runOnlyOnce, :195-196):
+//   (cv rho M + dt k L) T = cv rho M T_prev - dt (QN + SGamma_h + SGamma_r)     (:226-305, :307-375)
+// with identity rows for free nodes and Dirichlet nodes, the Dirichlet columns moved to the
+// right-hand side (:377-393).  M and L are MatrixBuilder::getM / getL (MatricesBuilder.inl:216-229,
+// 308-321) with the factors cv rho and k (HeatEquation.inl:54-74).
+//
+// Layout: the scalar system reuses the node adjacency of the flow system (nbr_ptr / nbr, sorted,
+// diagonal included) as its CSR pattern, values in node-pair order, so row n's entry for its
+// neighbour of rank r sits at nbr_ptr[n] + r.  Each value is gathered by one thread from the
+// elements the two nodes share, in ascending element order with M before L inside an element:
+// the order in which Eigen's setFromTriplets sums the reference's triplets (:248-270, :295).
+// The boundary facets a node belongs to are listed per node in ascending facet order (the
+// reference's facet loop order), so the right-hand side needs no atomics either.
+//
+// The reference factorises the system with SparseLU; here it is SPD (M and L symmetric, the
+// Dirichlet elimination symmetric, identity rows decoupled), so Jacobi-preconditioned CG in FP64
+// solves it to the Krylov tolerances of the context (the system is mass dominated: a few dozen
+// iterations).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "pfg_device.cuh"
+#include "pfg_internal.cuh"
+
+namespace pfg {
+
+namespace {
+
+constexpr uint8_t HT_T = PFG_HEAT_T, HT_Q = PFG_HEAT_Q, HT_QH = PFG_HEAT_QH, HT_QR = PFG_HEAT_QR;
+
+struct HeatConst {
+    double MM[4][4];  // sum_g w_g N_i N_j
+    double mfac;      // cv rho (the M factor, :54-59)
+    double lsum;      // sum_g k w_g (the L factor summed over the Gauss points, :70-74)
+    double refSize;   // reference element size
+    double dt;
+    // facet terms
+    double h, tinf, eps_rad;
+    double fw[3], fsf[3][3], fxi[3][2];  // facet Gauss rule: weights, shape functions, points
+    double fref;                         // refSize(dim - 1)
+};
+
+HeatConst heat_const(pfg_ctx* c, double dt) {
+    const GaussConst g = gauss_const(c->dim);
+    HeatConst k{};
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) k.MM[i][j] = g.MM[i][j];
+    k.mfac = c->prm.heat_cv * c->prm.rho;
+    k.lsum = 0;
+    for (int q = 0; q < g.n; ++q) k.lsum += c->prm.heat_k * g.w[q];
+    k.refSize = g.refSize;
+    k.dt = dt;
+    k.h = c->prm.heat_h;
+    k.tinf = c->prm.heat_t_inf;
+    k.eps_rad = c->prm.heat_eps_rad;
+    // three-point facet rule (nGPLD = 3, HeatEquation.inl:13-22; Mesh.cpp:342-530)
+    if (c->dim == 2) {
+        const double x[3] = {-std::sqrt(3.0 / 5.0), 0.0, std::sqrt(3.0 / 5.0)};
+        const double w[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
+        for (int q = 0; q < 3; ++q) {
+            k.fxi[q][0] = x[q];
+            k.fw[q] = w[q];
+            k.fsf[q][0] = (1 - x[q]) / 2;
+            k.fsf[q][1] = (1 + x[q]) / 2;
+        }
+        k.fref = 2.0;
+    } else {
+        const double p[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}, {2.0 / 3.0, 1.0 / 6.0}};
+        for (int q = 0; q < 3; ++q) {
+            k.fxi[q][0] = p[q][0];
+            k.fxi[q][1] = p[q][1];
+            k.fw[q] = 1.0 / 3.0;
+            k.fsf[q][0] = 1 - p[q][0] - p[q][1];
+            k.fsf[q][1] = p[q][0];
+            k.fsf[q][2] = p[q][1];
+        }
+        k.fref = 0.5;
+    }
+    return k;
+}
+
+// detJ and shape gradients of every element (slots 0 and 2.. of the flow element data; the
+// flow assembly recomputes them before its own use).
+template <int DIM>
+__global__ void k_heat_geom(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
+                            double* __restrict__ ed) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int nd[DIM + 1];
+    load_nodes<DIM>(conn, E, e, nd);
+    Geom<DIM> g;
+    compute_geom<DIM>(pos, N, nd, g);
+    double G[DIM][DIM + 1];
+    grad_n<DIM>(g, G);
+    ed[e] = g.detJ;
+#pragma unroll
+    for (int f = 0; f < DIM; ++f)
+#pragma unroll
+        for (int i = 0; i <= DIM; ++i) ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
+}
+
+// Value of the pair (n, m), one thread per pair: sum over the shared elements of
+// Me(i,j) = (cv rho MM_ij) |e| and Le(i,j) = dt (|e| k_sum) gradN_i . gradN_j; identity rows for
+// free and Dirichlet nodes (:287-293).
+template <int DIM>
+__global__ void __launch_bounds__(BLOCK) k_heat_pairs(int P, int E, const int* __restrict__ pair_node,
+                                                      const int* __restrict__ nbr, const int* __restrict__ ne_ptr,
+                                                      const int* __restrict__ ne_elem,
+                                                      const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
+                                                      const double* __restrict__ ed,
+                                                      const uint8_t* __restrict__ flags,
+                                                      const uint8_t* __restrict__ hflags, double* __restrict__ val,
+                                                      HeatConst k) {
+    constexpr int NPE = DIM + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P) return;
+    const int n = pair_node[t], m = nbr[t];
+    if ((hflags[n] & HT_T) || (flags[n] & F_FREE)) {
+        val[t] = m == n ? 1.0 : 0.0;
+        return;
+    }
+    double acc = 0;
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const int e = ne_elem[q];
+        int j = -1;
+#pragma unroll
+        for (int jj = 0; jj < NPE; ++jj)
+            if (__ldg(conn + (size_t)jj * E + e) == m) j = jj;
+        if (j < 0) continue;
+        const int i = ne_loc[q];
+        const double ae = ed[e] * k.refSize;
+        double dot = 0;
+#pragma unroll
+        for (int f = 0; f < DIM; ++f)
+            dot += ed[(size_t)(2 + f * NPE + i) * E + e] * ed[(size_t)(2 + f * NPE + j) * E + e];
+        acc += (k.mfac * k.MM[i][j]) * ae;
+        acc += k.dt * ((ae * k.lsum) * dot);
+    }
+    val[t] = acc;
+}
+
+// Facet f's geometry: measure factor detJ (Facet::computeDetJ, Facet.cpp:60-77) and, for the
+// flux term, the unit normal turned away from the element's other node (Facet::computeNormal,
+// :130-210).
+template <int DIM>
+__device__ __forceinline__ double facet_detj(const double* __restrict__ pos, int N, const int (&fn)[DIM]) {
+    if constexpr (DIM == 2) {
+        const double j0 = (pos[fn[1]] - pos[fn[0]]) / 2, j1 = (pos[(size_t)N + fn[1]] - pos[(size_t)N + fn[0]]) / 2;
+        return sqrt(j0 * j0 + j1 * j1);
+    } else {
+        double u[3], w[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            u[d] = pos[(size_t)d * N + fn[1]] - pos[(size_t)d * N + fn[0]];
+            w[d] = pos[(size_t)d * N + fn[2]] - pos[(size_t)d * N + fn[0]];
+        }
+        const double g0 = u[1] * w[2] - w[1] * u[2], g1 = u[2] * w[0] - w[2] * u[0], g2 = u[0] * w[1] - w[0] * u[1];
+        return sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void facet_normal(const double* __restrict__ pos, int N, const int (&fn)[DIM], int out,
+                                             double (&nv)[DIM]) {
+    if constexpr (DIM == 2) {
+        nv[0] = pos[(size_t)N + fn[1]] - pos[(size_t)N + fn[0]];
+        nv[1] = pos[fn[0]] - pos[fn[1]];
+    } else {
+        double u[3], w[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            u[d] = pos[(size_t)d * N + fn[1]] - pos[(size_t)d * N + fn[0]];
+            w[d] = pos[(size_t)d * N + fn[2]] - pos[(size_t)d * N + fn[0]];
+        }
+        nv[0] = u[1] * w[2] - u[2] * w[1];
+        nv[1] = u[2] * w[0] - u[0] * w[2];
+        nv[2] = u[0] * w[1] - u[1] * w[0];
+    }
+    double dot = 0, nn = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        dot += nv[d] * (pos[(size_t)d * N + out] - pos[(size_t)d * N + fn[0]]);
+        nn += nv[d] * nv[d];
+    }
+    const double s = dot > 0 ? -1.0 : 1.0;
+    const double norm = sqrt(nn);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) nv[d] = (s * nv[d]) / norm;
+}
+
+struct HeatFacets {
+    const int* ptr;         // N + 1 offsets into ent
+    const int* ent;         // facet * 4 + facet-local node
+    const uint8_t* fflags;  // HT_Q / HT_QH / HT_QR of each facet
+    const int* fnodes;      // dim x F
+    const int* felem;
+    const double* q;        // (F, 3, dim) flux vectors at the Gauss points, or null
+    int F;
+};
+
+// Right-hand side of node n: element gather of cv rho M T_prev (:240-283), the facet terms in
+// facet order (:315-375), the node conditions (:377-393) and the Dirichlet column elimination
+// of row n in ascending column order (the reference's node loop order), which zeroes the
+// eliminated values.
+template <int DIM>
+__global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __restrict__ ne_ptr,
+                                                    const int* __restrict__ ne_elem,
+                                                    const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
+                                                    const double* __restrict__ ed, const double* __restrict__ pos,
+                                                    const uint8_t* __restrict__ flags,
+                                                    const uint8_t* __restrict__ hflags,
+                                                    const double* __restrict__ t_prev, const double* __restrict__ tbc,
+                                                    const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                                                    double* __restrict__ val, HeatFacets hf, HeatConst k,
+                                                    double* __restrict__ rhs) {
+    constexpr int NPE = DIM + 1;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    double b = 0;
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const int e = ne_elem[q];
+        const int i = ne_loc[q];
+        int nd[NPE];
+        load_nodes<DIM>(conn, E, e, nd);
+        const double ae = ed[e] * k.refSize;
+        double s = 0;
+#pragma unroll
+        for (int j = 0; j < NPE; ++j) s += ((k.mfac * k.MM[i][j]) * ae) * t_prev[nd[j]];
+        b += s;
+    }
+    constexpr double sigma = 5.670374419e-8;  // Stefan-Boltzmann constant (:90)
+    for (int q = hf.ptr[n]; q < hf.ptr[n + 1]; ++q) {
+        const int ent = hf.ent[q];
+        const int f = ent >> 2, kk = ent & 3;
+        const uint8_t ff = hf.fflags[f];
+        int fn[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) fn[d] = hf.fnodes[(size_t)d * hf.F + f];
+        const double detJ = facet_detj<DIM>(pos, N, fn);
+        if (ff & HT_Q) {  // getQN, MatricesBuilder.inl:246-272
+            const int e = hf.felem[f];
+            int out = -1;
+#pragma unroll
+            for (int a = 0; a < NPE; ++a) {
+                const int v = conn[(size_t)a * E + e];
+                bool on = false;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) on |= v == fn[d];
+                if (!on) out = v;
+            }
+            double nv[DIM];
+            facet_normal<DIM>(pos, N, fn, out, nv);
+            double qn = 0;
+#pragma unroll
+            for (int g = 0; g < 3; ++g) {
+                double qdn = 0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) qdn += hf.q[((size_t)f * 3 + g) * DIM + d] * nv[d];
+                qn += (qdn * k.fw[g]) * k.fsf[g][kk];
+            }
+            b -= k.dt * ((qn * k.fref) * detJ);
+        }
+#pragma unroll
+        for (int pass = 0; pass < 2; ++pass) {  // getSGamma, MatricesBuilder.inl:357-370 (:76-94)
+            if (!(ff & (pass == 0 ? HT_QH : HT_QR))) continue;
+            double sg = 0;
+#pragma unroll
+            for (int g = 0; g < 3; ++g) {
+                double T = 0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) T += k.fsf[g][d] * t_prev[fn[d]];
+                const double fac = pass == 0 ? k.h * (T - k.tinf)
+                                             : sigma * k.eps_rad * (T * T * T * T - k.tinf * k.tinf * k.tinf * k.tinf);
+                sg += (fac * k.fsf[g][kk]) * k.fw[g];
+            }
+            b -= k.dt * (sg * (detJ * k.fref));
+        }
+    }
+    const uint8_t h = hflags[n];
+    const bool fr = flags[n] & F_FREE;
+    if (h & HT_T) {
+        b = tbc[n];
+    } else if (fr) {
+        b = t_prev[n];
+    } else {
+        for (int t = nbr_ptr[n]; t < nbr_ptr[n + 1]; ++t) {
+            const int m = nbr[t];
+            if (m != n && (hflags[m] & HT_T)) {
+                b -= val[t] * tbc[m];
+                val[t] = 0.0;
+            }
+        }
+    }
+    rhs[n] = b;
+}
+
+// ---- Jacobi-preconditioned conjugate gradients over the pair-ordered CSR -----------------
+
+enum : int { S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_TOL2, S_DONE, S_ITERS, S_BB, S_COUNT };
+enum : int { V_R = 0, V_Z, V_P, V_Q, V_DIAG, V_COUNT };
+
+struct CgPtrs {
+    double* partials;  // 2 * max_grid
+    double* sc;        // S_COUNT
+    unsigned* ticket;
+};
+
+CgPtrs cg_ptrs(pfg_ctx* c) {
+    double* red = ptr<double>(c->heat_red);
+    CgPtrs k;
+    k.partials = red;
+    k.sc = red + 2 * (size_t)c->max_grid;
+    k.ticket = reinterpret_cast<unsigned*>(k.sc + 32);
+    return k;
+}
+
+template <int NT>
+__device__ __forceinline__ bool grid_sum2(double a, double b, double* partials, unsigned* ticket, double* sh,
+                                          double& ra, double& rb) {
+    a = block_sum<NT>(a, sh);
+    b = block_sum<NT>(b, sh);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = a;
+        partials[gridDim.x + blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double sa = 0, sb = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += NT) {
+        sa += ((volatile double*)partials)[i];
+        sb += ((volatile double*)partials)[gridDim.x + i];
+    }
+    ra = block_sum<NT>(sa, sh);
+    rb = block_sum<NT>(sb, sh);
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+// r = b - A x, z = r / diag, p = z; rz = r.z; tolerance from ||b||.  An exact start still runs
+// one iteration (alpha = 0), which finds ||r|| <= tol.
+__global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict__ rp, const int* __restrict__ col,
+                                                   const double* __restrict__ val, const double* __restrict__ b,
+                                                   const double* __restrict__ x, double* __restrict__ V, size_t ld,
+                                                   CgPtrs k, double rtol, double atol) {
+    __shared__ double sh[32];
+    double rz = 0, bb = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        double ax = 0, d = 1.0;
+        for (int t = rp[n]; t < rp[n + 1]; ++t) {
+            const int m = col[t];
+            ax += val[t] * x[m];
+            if (m == n) d = val[t];
+        }
+        const double r = b[n] - ax;
+        const double z = r / d;
+        V[V_R * ld + n] = r;
+        V[V_Z * ld + n] = z;
+        V[V_P * ld + n] = z;
+        V[V_DIAG * ld + n] = d;
+        rz += r * z;
+        bb += b[n] * b[n];
+    }
+    double s1, s2;
+    if (grid_sum2<BLOCK>(rz, bb, k.partials, k.ticket, sh, s1, s2) && threadIdx.x == 0) {
+        k.sc[S_RZ] = s1;
+        k.sc[S_BB] = s2;
+        const double tol = fmax(rtol * sqrt(s2), atol);
+        k.sc[S_TOL2] = tol * tol;
+        k.sc[S_ITERS] = 0;
+        k.sc[S_DONE] = 0;
+    }
+}
+
+// q = A p, alpha = rz / (p . q)
+__global__ void __launch_bounds__(BLOCK) k_cg_spmv(int N, const int* __restrict__ rp, const int* __restrict__ col,
+                                                   const double* __restrict__ val, double* __restrict__ V, size_t ld,
+                                                   CgPtrs k) {
+    __shared__ double sh[32];
+    if (k.sc[S_DONE] != 0.0) return;
+    const double* p = V + V_P * ld;
+    double pq = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        double s = 0;
+        for (int t = rp[n]; t < rp[n + 1]; ++t) s += val[t] * p[col[t]];
+        V[V_Q * ld + n] = s;
+        pq += p[n] * s;
+    }
+    double a, unused;
+    if (grid_sum2<BLOCK>(pq, 0.0, k.partials, k.ticket, sh, a, unused) && threadIdx.x == 0) {
+        k.sc[S_PQ] = a;
+        k.sc[S_ALPHA] = a != 0.0 ? k.sc[S_RZ] / a : 0.0;
+    }
+}
+
+// x += alpha p, r -= alpha q, z = r / diag; beta = rz_new / rz; done when ||r|| <= tol.
+__global__ void __launch_bounds__(BLOCK) k_cg_update(int N, double* __restrict__ x, double* __restrict__ V, size_t ld,
+                                                     CgPtrs k, int max_it) {
+    __shared__ double sh[32];
+    if (k.sc[S_DONE] != 0.0) return;
+    const double alpha = k.sc[S_ALPHA];
+    double rz = 0, rr = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        x[n] += alpha * V[V_P * ld + n];
+        const double r = V[V_R * ld + n] - alpha * V[V_Q * ld + n];
+        const double z = r / V[V_DIAG * ld + n];
+        V[V_R * ld + n] = r;
+        V[V_Z * ld + n] = z;
+        rz += r * z;
+        rr += r * r;
+    }
+    double s1, s2;
+    if (grid_sum2<BLOCK>(rz, rr, k.partials, k.ticket, sh, s1, s2) && threadIdx.x == 0) {
+        const double it = k.sc[S_ITERS] + 1;
+        k.sc[S_ITERS] = it;
+        k.sc[S_RR] = s2;
+        k.sc[S_BETA] = k.sc[S_RZ] != 0.0 ? s1 / k.sc[S_RZ] : 0.0;
+        k.sc[S_RZ] = s1;
+        if (s2 <= k.sc[S_TOL2]) k.sc[S_DONE] = 1;
+        else if (!(s2 == s2) || k.sc[S_PQ] <= 0.0) k.sc[S_DONE] = 2;  // NaN or loss of definiteness
+        else if (it >= max_it) k.sc[S_DONE] = 3;
+    }
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(BLOCK) k_cg_p(int N, double* __restrict__ V, size_t ld, CgPtrs k) {
+    if (k.sc[S_DONE] != 0.0) return;
+    const double beta = k.sc[S_BETA];
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
+        V[V_P * ld + n] = V[V_Z * ld + n] + beta * V[V_P * ld + n];
+}
+
+template <int DIM>
+int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
+    const int N = c->N, E = c->E;
+    const HeatConst k = heat_const(c, dt);
+    double* T = ptr<double>(c->heat_t);
+    double* V = ptr<double>(c->heat_cg);
+    const size_t ld = (size_t)std::max(N, 1);
+    double* x = V + V_COUNT * ld;
+    if (E > 0) {
+        k_heat_geom<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
+                                                                    ptr<double>(c->edata));
+        PFG_CHECK_LAUNCH(c);
+    }
+    if (c->P > 0)
+        k_heat_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
+            c->P, E, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
+            ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<double>(c->edata), ptr<uint8_t>(c->flags),
+            ptr<uint8_t>(c->heat_flags), ptr<double>(c->heat_val), k);
+    HeatFacets hf;
+    hf.ptr = ptr<int>(c->hf_ptr);
+    hf.ent = ptr<int>(c->hf_ent);
+    hf.fflags = ptr<uint8_t>(c->hf_fflags);
+    hf.fnodes = ptr<int>(c->fc_nodes);
+    hf.felem = ptr<int>(c->fc_elem);
+    hf.q = c->has_heat_q ? ptr<double>(c->heat_q) : nullptr;
+    hf.F = c->F;
+    k_heat_rhs<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
+        N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
+        ptr<double>(c->edata), ptr<double>(c->pos), ptr<uint8_t>(c->flags), ptr<uint8_t>(c->heat_flags), T,
+        ptr<double>(c->heat_tbc), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<double>(c->heat_val), hf, k,
+        ptr<double>(c->heat_rhs));
+    PFG_CHECK_LAUNCH(c);
+    // CG from T_prev (solveWithGuess, :126)
+    PFG_CUDA(c, cudaMemcpyAsync(x, T, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    const CgPtrs kp = cg_ptrs(c);
+    const int grid = std::max(1, std::min(c->max_grid, div_up(N, BLOCK)));
+    const int* rp = ptr<int>(c->nbr_ptr);
+    const int* col = ptr<int>(c->nbr);
+    const double* val = ptr<double>(c->heat_val);
+    k_cg_init<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, ptr<double>(c->heat_rhs), x, V, ld, kp,
+                                             c->prm.krylov_rel_tol, c->prm.krylov_abs_tol);
+    PFG_CHECK_LAUNCH(c);
+    const int max_it = std::max(1, c->prm.krylov_max_iter);
+    double* h = c->h_scalars;
+    int done_it = 0;
+    while (done_it < max_it) {
+        const int n = std::min(8, max_it - done_it);
+        for (int it = 0; it < n; ++it) {
+            k_cg_spmv<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
+            k_cg_update<<<grid, BLOCK, 0, c->stream>>>(N, x, V, ld, kp, max_it);
+            k_cg_p<<<grid, BLOCK, 0, c->stream>>>(N, V, ld, kp);
+        }
+        PFG_CHECK_LAUNCH(c);
+        done_it += n;
+        PFG_CUDA(c, cudaMemcpyAsync(h, kp.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (h[S_DONE] != 0.0) break;
+    }
+    const bool ok = h[S_DONE] == 1.0;
+    st->converged = ok ? 1 : 0;
+    st->picard_iterations = 1;
+    st->krylov_iterations = (int)h[S_ITERS];
+    st->residual = std::sqrt(h[S_RR]);
+    st->dt = dt;
+    if (ok) PFG_CUDA(c, cudaMemcpyAsync(T, x, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PFG_OK;
+}
+
+}  // namespace
+
+int heat_alloc(pfg_ctx* c) {
+    const size_t N = std::max(c->N, 1), P = std::max(c->P, 1);
+    int rc;
+    if ((rc = ensure(c, c->heat_t, sizeof(double) * N)) || (rc = ensure(c, c->heat_flags, N)) ||
+        (rc = ensure(c, c->heat_tbc, sizeof(double) * N)) || (rc = ensure(c, c->heat_val, sizeof(double) * P)) ||
+        (rc = ensure(c, c->heat_rhs, sizeof(double) * N)) ||
+        (rc = ensure(c, c->heat_cg, sizeof(double) * (V_COUNT + 1) * N)) ||
+        (rc = ensure(c, c->heat_red, sizeof(double) * (2 * (size_t)std::max(c->max_grid, 1) + 64))) ||
+        (rc = ensure(c, c->hf_ptr, sizeof(int) * (N + 1))))
+        return rc;
+    PFG_CUDA(c, cudaMemsetAsync(c->heat_t.p, 0, sizeof(double) * N, c->stream));
+    PFG_CUDA(c, cudaMemsetAsync(c->heat_flags.p, 0, N, c->stream));
+    PFG_CUDA(c, cudaMemsetAsync(c->heat_tbc.p, 0, sizeof(double) * N, c->stream));
+    PFG_CUDA(c, cudaMemsetAsync(c->hf_ptr.p, 0, sizeof(int) * (N + 1), c->stream));
+    PFG_CUDA(c, cudaMemsetAsync(c->heat_red.p, 0, sizeof(double) * (2 * (size_t)std::max(c->max_grid, 1) + 64),
+                                c->stream));
+    c->h_heat_flags.assign(c->N, 0);
+    c->has_heat_bc = false;
+    c->has_heat_q = false;
+    c->heat_ready = true;
+    return PFG_OK;
+}
+
+// Per-node lists of the facets that take a heat flux term (all their nodes carry the flag, or
+// the free-surface flags for a facet whose nodes are all on the free surface, HeatEquation.inl:
+// 319-335; Facet::isOnFreeSurface, Facet.cpp:249-255), in ascending facet order.
+int heat_build_facets(pfg_ctx* c) {
+    const int N = c->N, F = c->has_facets ? c->F : 0, dim = c->dim;
+    const int fsf = c->prm.heat_fs_flags & (HT_Q | HT_QH | HT_QR);
+    std::vector<uint8_t> ff((size_t)std::max(F, 1), 0);
+    std::vector<int> cnt((size_t)N + 1, 0);
+    for (int f = 0; f < F; ++f) {
+        bool fs = true;
+        for (int d = 0; d < dim; ++d) fs = fs && (c->h_flags[c->h_facets[(size_t)d * F + f]] & F_FREE_SURFACE);
+        int fl = HT_Q | HT_QH | HT_QR;
+        for (int d = 0; d < dim; ++d) fl &= fs ? fsf : c->h_heat_flags[c->h_facets[(size_t)d * F + f]];
+        ff[f] = (uint8_t)fl;
+        if (fl)
+            for (int d = 0; d < dim; ++d) cnt[c->h_facets[(size_t)d * F + f] + 1]++;
+    }
+    for (int n = 0; n < N; ++n) cnt[n + 1] += cnt[n];
+    std::vector<int> ent((size_t)std::max(cnt[N], 1));
+    std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+    for (int f = 0; f < F; ++f)
+        if (ff[f])
+            for (int d = 0; d < dim; ++d) ent[pos[c->h_facets[(size_t)d * F + f]]++] = f * 4 + d;
+    int rc;
+    if ((rc = ensure(c, c->hf_ent, sizeof(int) * ent.size())) || (rc = ensure(c, c->hf_fflags, ff.size())))
+        return rc;
+    PFG_CUDA(c, cudaMemcpyAsync(c->hf_ptr.p, cnt.data(), sizeof(int) * ((size_t)N + 1), cudaMemcpyHostToDevice,
+                                c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->hf_ent.p, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->hf_fflags.p, ff.data(), ff.size(), cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    bool need_q = false;
+    for (int f = 0; f < F; ++f) need_q |= (ff[f] & HT_Q) != 0;
+    if (need_q && !c->has_heat_q) return fail(c, PFG_ERR_STATE, "heat facets with a Q flag need pfg_heat_set_flux");
+    return PFG_OK;
+}
+
+int heat_step(pfg_ctx* c, double dt, pfg_step_status* st) {
+    return c->dim == 2 ? heat_dim<2>(c, dt, st) : heat_dim<3>(c, dt, st);
+}
+
+}  // namespace pfg

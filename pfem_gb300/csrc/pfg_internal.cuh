@@ -144,6 +144,16 @@ struct pfg_ctx {
     pfg::DBuf mg_x0;
     pfg::DBuf mg_in64;     // FP64 correction solves: FP32 scaled input and output of the cycle
     pfg::DBuf val16;       // bfloat16 copy of the node-pair blocks (level-0 multigrid sweeps)
+    // heat equation: node temperatures, BC flags and Dirichlet values, the scalar system over
+    // the node pairs (values in pair order, right-hand side), CG vectors, reductions, the
+    // per-node lists of heat facets (facet * 4 + facet-local node) with each facet's flux
+    // flags, and the flux vectors at the facet Gauss points
+    pfg::DBuf heat_t, heat_flags, heat_tbc, heat_val, heat_rhs, heat_cg, heat_red;
+    pfg::DBuf hf_ptr, hf_ent, hf_fflags, heat_q;
+    bool heat_ready = false;  // heat buffers allocated (and zeroed) for the current mesh
+    bool has_heat_bc = false, has_heat_q = false;
+    std::vector<uint8_t> h_heat_flags;
+    std::vector<int32_t> h_facets, h_facet_elm;
 };
 
 namespace pfg {
@@ -218,6 +228,10 @@ int spmv_residual_norm(pfg_ctx* c, const double* d_x, double* res);
 
 // ---- mixed-precision PSPG (pfg_pspg_mixed.cu) -----------------------------------------
 int mx_alloc(pfg_ctx* c);
+// ---- heat equation (pfg_heat.cu) ----
+int heat_alloc(pfg_ctx* c);
+int heat_build_facets(pfg_ctx* c);
+int heat_step(pfg_ctx* c, double dt, pfg_step_status* st);
 int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* rho, const double* mu);
 int mx_picard_step(pfg_ctx* c, const double* dts, pfg_step_status* st);
 void mx_release_graph(pfg_ctx* c);

@@ -66,6 +66,7 @@ __global__ void k_elem_prep(int E, int N, const int* __restrict__ conn, const do
 struct PspgConst {
     PspgCoef c;
     PspgTables t;
+    BoussArgs bq;
 };
 
 // Matrix values, one thread per node pair (n, m).
@@ -109,7 +110,7 @@ __global__ void k_pspg_rhs(int N, int E, const int* __restrict__ ne_ptr, const i
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     double bv[DIM], bp;
-    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, apply_bc != 0, k.c, k.t, fst,
+    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, apply_bc != 0, k.c, k.t, fst, k.bq,
                        bv, bp);
 #pragma unroll
     for (int f = 0; f < DIM; ++f) rhs[(size_t)f * N + n] = bv[f];
@@ -197,6 +198,7 @@ PspgConst make_const(pfg_ctx* c, double dt) {
         for (int j = 0; j < 4; ++j) k.t.MM[i][j] = g.MM[i][j];
     }
     for (int f = 0; f < 3; ++f) k.t.g[f] = c->prm.gravity[f];
+    k.bq = boussinesq_args(c);
     return k;
 }
 

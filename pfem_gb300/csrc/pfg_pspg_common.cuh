@@ -27,6 +27,26 @@ struct PspgCoef {
     double h_sum;     // sum_g w_g             (getH factor 1)
 };
 
+// Problem "Boussinesq" (MomContEquation.inl:164-199): the body-force factor rho (1 - alpha (T - Tr))
+// and the PSPG gravity factor 1 - alpha (T - Tr) at each Gauss point, T interpolated from the node
+// temperatures.  Summed over the Gauss points they are, per element node i,
+//   F:  rho [(1 + alpha Tr) s_i - alpha sum_k MM_ik T_k]     H:  (1 + alpha Tr) sum_g w_g - alpha sum_k s_k T_k
+// with s_i = sum_g w_g N_i and MM_ik = sum_g w_g N_i N_k.  T == nullptr: not Boussinesq.
+struct BoussArgs {
+    const double* T;
+    double alpha, Tr;
+};
+
+inline BoussArgs boussinesq_args(pfg_ctx* c) {
+    BoussArgs b{nullptr, 0.0, 0.0};
+    if (c->prm.boussinesq) {
+        b.T = ptr<double>(c->heat_t);
+        b.alpha = c->prm.alpha_t;
+        b.Tr = c->prm.t_ref;
+    }
+    return b;
+}
+
 struct PspgTables {
     double MM[4][4];  // sum_g w N_i N_j
     double s[4];      // sum_g w N_i
@@ -168,7 +188,7 @@ __device__ __forceinline__ void pspg_node_rhs(int n, int N, int E, const int* __
                                               uint8_t fl, const double* __restrict__ q_prev,
                                               const double* __restrict__ vbc, bool apply_bc, const PspgCoef& k,
                                               const PspgTables& t, const double* __restrict__ fst,
-                                              double (&bv)[DIM], double& bp) {
+                                              const BoussArgs& bq, double (&bv)[DIM], double& bp) {
     constexpr int NPE = DIM + 1;
 #pragma unroll
     for (int f = 0; f < DIM; ++f) bv[f] = 0;
@@ -190,20 +210,34 @@ __device__ __forceinline__ void pspg_node_rhs(int n, int N, int E, const int* __
         for (int f = 0; f < DIM; ++f)
 #pragma unroll
             for (int j = 0; j < NPE; ++j) vp[f][j] = q_prev[(size_t)f * N + nd[j]];
+        // Gauss sums of the body-force factor over N_i and of the gravity factor
+        double fs = t.s[i], hs = k.h_sum;
+        if (bq.T) {
+            double mt = 0, st = 0;
+#pragma unroll
+            for (int j = 0; j < NPE; ++j) {
+                const double Tj = bq.T[nd[j]];
+                mt += t.MM[i][j] * Tj;
+                st += t.s[j] * Tj;
+            }
+            const double c0 = 1 + bq.alpha * bq.Tr;
+            fs = c0 * t.s[i] - bq.alpha * mt;
+            hs = c0 * k.h_sum - bq.alpha * st;
+        }
         // momentum rows: F + (M/dt) v_prev
 #pragma unroll
         for (int f = 0; f < DIM; ++f) {
             double mv = 0;
 #pragma unroll
             for (int j = 0; j < NPE; ++j) mv += inv_dt * (k.rho * t.MM[i][j] * ae) * vp[f][j];
-            const double F = ae * (k.rho * t.s[i] * t.g[f]);
+            const double F = ae * (k.rho * fs * t.g[f]);
             bv[f] += F + mv;
         }
         // continuity row: tau H + (tau/dt) C v_prev
         double gdot = 0;
 #pragma unroll
         for (int f = 0; f < DIM; ++f) gdot += gi[f] * t.g[f];
-        const double H = tau * (ae * k.h_sum * gdot);
+        const double H = tau * (ae * hs * gdot);
         double cv = 0;
 #pragma unroll
         for (int f = 0; f < DIM; ++f)

@@ -70,6 +70,7 @@ struct MxConst {
     double refSize, sumw;
     PspgTables t;
     DF mm_df[4][4], s_df[4], ref_df;  // double-float copies of the tables and refSize
+    BoussArgs bq;
     double rtol, atol, eta, min_res;
     int max_iter;
 };
@@ -103,6 +104,7 @@ MxConst mx_const(pfg_ctx* c) {
         for (int j = 0; j < 4; ++j) k.mm_df[i][j] = split(g.MM[i][j]);
     }
     k.ref_df = split(g.refSize);
+    k.bq = boussinesq_args(c);
     k.rtol = c->prm.krylov_rel_tol;
     k.atol = c->prm.krylov_abs_tol;
     k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-4;
@@ -233,7 +235,7 @@ __global__ void k_mx_rhs(int N, int E, const int* __restrict__ ne_ptr, const int
     if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
     const PspgCoef cf = inst_coef_d(m.id + inst * D_COUNT, k.sumw, k.refSize);
     double bv[DIM], bp;
-    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, true, cf, k.t, fst, bv, bp);
+    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, true, cf, k.t, fst, k.bq, bv, bp);
 #pragma unroll
     for (int f = 0; f < DIM; ++f) rhs[(size_t)f * N + n] = bv[f];
     rhs[(size_t)DIM * N + n] = bp;

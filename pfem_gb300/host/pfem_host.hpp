@@ -88,6 +88,27 @@ class Context {
         check(pfg_mass(ctx_, &m), "pfg_mass");
         return m;
     }
+    // heat equation (HeatEqIncompNewton): node temperatures, BCs, one solve
+    void setTemperature(const std::vector<double>& T) {
+        if (T.size() != (size_t)nodes_) throw std::runtime_error("setTemperature: wrong size");
+        check(pfg_set_temperature(ctx_, T.data()), "pfg_set_temperature");
+    }
+    std::vector<double> temperature() const {
+        std::vector<double> T((size_t)nodes_);
+        check(pfg_get_temperature(ctx_, T.data()), "pfg_get_temperature");
+        return T;
+    }
+    void setHeatBC(const std::vector<uint8_t>& flags, const std::vector<double>& tDirichlet) {
+        if (flags.size() != (size_t)nodes_ || (!tDirichlet.empty() && tDirichlet.size() != (size_t)nodes_))
+            throw std::runtime_error("setHeatBC: wrong size");
+        check(pfg_heat_set_bc(ctx_, flags.data(), tDirichlet.empty() ? nullptr : tDirichlet.data()),
+              "pfg_heat_set_bc");
+    }
+    pfg_step_status heatStep(double dt) {
+        pfg_step_status st{};
+        check(pfg_heat_step(ctx_, dt, &st), "pfg_heat_step");
+        return st;
+    }
 
   private:
     pfg_ctx* ctx_ = nullptr;

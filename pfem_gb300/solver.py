@@ -1,6 +1,7 @@
 """Host-side solver classes: the reference's time loop around the GPU per-step solve.
 
-    SolverIncompNewtonGPU   srcs/simulation/physics/IncompNewton/Solver.cpp (PSPG, no temperature)
+    SolverIncompNewtonGPU   srcs/simulation/physics/IncompNewton/Solver.cpp (PSPG; problems
+                            "IncompNewtonNoT", "Bingham", "Boussinesq", "Conduction")
     SolverWCompNewtonGPU    srcs/simulation/physics/WCompNewton/Solver.cpp  (CDS_dpdt, no temperature)
     Problem                 srcs/simulation/Problem.cpp:320-380 (Problem::simulate)
 
@@ -15,6 +16,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import api
+from . import heat as H
 from . import mesh as M
 from . import remesh as RM
 
@@ -71,11 +73,30 @@ class _SolverBase:
 class SolverIncompNewtonGPU(_SolverBase):
     """PSPG Picard step on the GPU with the reference's dt control (`IncompNewton/Solver.cpp:216-247`):
     dt /= coeffDTDecrease after a failed step, dt = min(maxDT, dt * coeffDTincrease) after a
-    successful one (with adaptDT; a failed step without it raises, like the reference)."""
+    successful one (with adaptDT; a failed step without it raises, like the reference).
+
+    `problem` selects the reference's solve function (`Solver.cpp:95-175`): "IncompNewtonNoT"
+    (and "Bingham", through params.tau0) solve the momentum-continuity equation; "Boussinesq"
+    (params.boussinesq = 1) adds the heat equation before or after it (`solve_heat_first`,
+    `m_solveBoussinesq`, :249-284); "Conduction" solves the heat equation alone on a fixed mesh
+    (`m_solveConduction`, :286-296).  Heat problems take the initial node temperatures, a BC
+    callable heat_bc(pos, flags, t) -> (heat flags (N,) uint8, Dirichlet temperatures (N,)) and
+    optionally a flux callable q(x, t) -> (dim,) evaluated at the facet Gauss points; both are
+    evaluated at t + dt before each heat solve, as the reference's m_applyBC does."""
     kind = api.KIND_INCOMP_PSPG
 
     def __init__(self, mesh, states, params=None, remesh_params=None, precision=api.PREC_FP64, dirichlet=None,
-                 initial_dt=1e-3, max_dt=1e-3, adapt_dt=True, coeff_dt_increase=1.5, coeff_dt_decrease=2.0):
+                 initial_dt=1e-3, max_dt=1e-3, adapt_dt=True, coeff_dt_increase=1.5, coeff_dt_decrease=2.0,
+                 problem="IncompNewtonNoT", temperature=None, heat_bc=None, heat_flux=None, solve_heat_first=True):
+        if problem not in ("IncompNewtonNoT", "Bingham", "Boussinesq", "Conduction"):
+            raise ValueError(f"unknown problem {problem!r}")
+        if problem in ("Boussinesq", "Conduction") and temperature is None:
+            raise ValueError(f"problem {problem!r} needs the initial temperatures")
+        self.problem = problem
+        self.heat_bc = heat_bc
+        self.heat_flux = heat_flux
+        self.solve_heat_first = solve_heat_first
+        self._t0 = None if temperature is None else np.asarray(temperature, float)
         super().__init__(mesh, states, params, remesh_params, precision, dirichlet)
         self.dt = initial_dt
         self.max_dt = max_dt
@@ -85,12 +106,64 @@ class SolverIncompNewtonGPU(_SolverBase):
         self.solve_succeeded = True
         self.last_status = None
 
+    def _upload(self, mesh, states, temperature=None):
+        super()._upload(mesh, states)
+        t = temperature if temperature is not None else self._t0
+        if t is not None:
+            self.ctx.set_temperature(t)
+
+    def temperature(self):
+        return self.ctx.get_temperature()
+
+    def remesh(self):
+        """`Mesh::remesh` with the temperature travelling as one more node state."""
+        if self.remesh_params is None:
+            return
+        if self._t0 is None:
+            return super().remesh()
+        cur = self.mesh.copy()
+        cur.pos = self.ctx.get_positions()
+        cur.flags = self.ctx.get_flags() & np.uint8(0x0F)
+        R = (self.mesh.dim + 1) * self.mesh.n_nodes
+        st = np.concatenate([self.ctx.get_states(), self.ctx.get_temperature()])
+        new, st2 = RM.remesh(cur, st, self.remesh_params)
+        R2 = (new.dim + 1) * new.n_nodes
+        assert st2.size == R2 + new.n_nodes and R > 0
+        self._upload(new, st2[:R2], st2[R2:])
+
+    def _heat(self):
+        """`HeatEqIncompNewton::solve` with the BCs evaluated at t + dt on the current positions."""
+        t = self.time + self.dt
+        pos = self.ctx.get_positions()
+        if self.heat_bc is not None:
+            flags, tbc = self.heat_bc(pos, self.mesh.flags, t)
+            self.ctx.heat_set_bc(flags, tbc)
+        if self.heat_flux is not None and self.mesh.facets.shape[1]:
+            self.ctx.heat_set_flux(H.flux_at_gauss_points(pos, self.mesh.facets, self.heat_flux, t))
+        st = self.ctx.heat_step(self.dt)
+        self.last_heat_status = st
+        return bool(st.converged)
+
     def solve_one_time_step(self) -> bool:
-        """`SolverIncompNewton::m_solveIncompNewtonNoT`: Picard solve; on success the time
-        advances and the mesh is rebuilt."""
+        """`SolverIncompNewton::m_solveIncompNewtonNoT` / `m_solveBoussinesq` / `m_solveConduction`:
+        on success the time advances and (but for Conduction) the mesh is rebuilt.  As in the
+        reference, a Boussinesq step whose momentum solve fails keeps the temperatures of its
+        heat solve (the node list is saved after it)."""
+        if self.problem == "Conduction":
+            self.solve_succeeded = self._heat()
+            if self.solve_succeeded:
+                self.time += self.dt
+                self.steps += 1
+            return self.solve_succeeded
+        heat = self.problem == "Boussinesq"
+        if heat and self.solve_heat_first and not self._heat():
+            self.solve_succeeded = False
+            return False
         st = self.ctx.picard_step(self.dt)
         self.last_status = st
         self.solve_succeeded = bool(st.converged)
+        if self.solve_succeeded and heat and not self.solve_heat_first:
+            self.solve_succeeded = self._heat()
         if self.solve_succeeded:
             self.time += self.dt
             self.steps += 1

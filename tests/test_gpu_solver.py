@@ -79,3 +79,65 @@ def test_extractors_write_gmsh_and_csv(gpu_lib, tmp_path):
     tips = [list(map(float, l.split(","))) for l in open(tmp_path / "tip.txt")]
     assert all(0.9 < t[1] < 4.0 for t in tips)
     sol.close()
+
+
+def test_boussinesq_solver_with_remesh_matches_oracle_loop(gpu_lib):
+    """`m_solveBoussinesq` with solveHeatFirst (heat, momentum, remesh carrying T) against the
+    oracle-driven loop; wall nodes held at a hot bottom / cold rest, free-surface convection."""
+    mesh = M.dam_break_2d(0.1)
+    q0 = M.incomp_initial_states(mesh)
+    T0 = np.full(mesh.n_nodes, 650.0)
+    alpha, tr, h, tinf = 69e-6, 650.0, 5.0, 300.0
+
+    def heat_bc(pos, flags, t):
+        bound = (flags & M.BOUND) != 0
+        fl = np.where(bound, api.HEAT_T, 0).astype(np.uint8)
+        return fl, np.where(pos[1] < 0.05, 1000.0, 650.0) * bound
+
+    p = api.default_params(api.KIND_INCOMP_PSPG, 2)
+    p.boussinesq, p.alpha_t, p.t_ref = 1, alpha, tr
+    p.heat_k, p.heat_cv, p.heat_h, p.heat_t_inf, p.heat_fs_flags = 0.6, 4.0, h, tinf, api.HEAT_QH
+    sol = S.SolverIncompNewtonGPU(mesh, q0, params=p, remesh_params=PRM, problem="Boussinesq", temperature=T0,
+                                  heat_bc=heat_bc)
+    S.Problem(sol, max_time=1.0).simulate(max_steps=4)
+    hp = O.heat_params(1000.0, 4.0, 0.6, h=h, t_inf=tinf, fs_flags=O.HT_QH)
+    m, q, T, dt = mesh, q0.copy(), T0.copy(), 1e-3
+    for _ in range(4):
+        om = O.OracleMesh(m)
+        fl, tbc = heat_bc(m.pos, m.flags, 0.0)
+        T = O.heat_step(om, hp, dt, T, fl, tbc)
+        qn, res = O.pspg_picard_step(om, q, dt, boussinesq=(alpha, tr, T))
+        assert res.converged
+        cur = m.copy()
+        cur.pos = om.positions
+        m, st = R.remesh(cur, np.concatenate([qn, T]), PRM)
+        q, T = st[:3 * m.n_nodes], st[3 * m.n_nodes:]
+        dt = min(1e-3, dt * 1.5)
+    assert sol.steps == 4 and sol.mesh.n_nodes == m.n_nodes and np.array_equal(sol.mesh.conn, m.conn)
+    assert np.abs(sol.temperature() - T).max() <= 1e-10 * np.abs(T).max()
+    qg, N = sol.states(), m.n_nodes
+    for f in range(3):
+        a, b = qg[f * N:(f + 1) * N], q[f * N:(f + 1) * N]
+        assert np.linalg.norm(a - b) <= 1e-8 * max(np.linalg.norm(b), 1e-30)
+    sol.close()
+
+
+def test_conduction_solver_keeps_the_mesh(gpu_lib):
+    """`m_solveConduction`: heat only, fixed mesh, time advances by dt per accepted step."""
+    mesh = M.dam_break_2d(0.1)
+    p = api.default_params(api.KIND_INCOMP_PSPG, 2)
+    p.rho, p.heat_k, p.heat_cv = 1.0, 237.0, 1000.0
+    T0 = 10 * np.exp(-((mesh.pos[0] - 0.5) ** 2 + (mesh.pos[1] - 0.5) ** 2) / 0.05)
+    sol = S.SolverIncompNewtonGPU(mesh, M.incomp_initial_states(mesh), params=p, problem="Conduction",
+                                  temperature=T0, initial_dt=0.025, max_dt=0.1)
+    S.Problem(sol, max_time=0.2).simulate(max_steps=10)
+    assert sol.time >= 0.2 - 1e-12 and np.array_equal(sol.positions(), mesh.pos)
+    om = O.OracleMesh(mesh)
+    hp = O.heat_params(1.0, 1000.0, 237.0)
+    T, dt, t = T0.copy(), 0.025, 0.0
+    while t < 0.2:
+        T = O.heat_step(om, hp, dt, T, np.zeros(mesh.n_nodes, np.uint8))
+        t += dt
+        dt = min(0.1, dt * 1.5)
+    assert np.abs(sol.temperature() - T).max() <= 1e-10 * np.abs(T).max()
+    sol.close()

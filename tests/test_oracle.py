@@ -200,3 +200,114 @@ def test_bingham_viscosity_in_simple_shear():
     K_n, K_b = (A_n - A_m)[:6, :6], (A_b - A_m)[:6, :6]
     mue = mu + tau0 * (1 - np.exp(-mreg * s)) / s
     assert np.allclose(K_b, K_n * (mue / mu), rtol=1e-12, atol=1e-12 * np.abs(K_b).max())
+
+
+# ---- heat equation and Boussinesq coupling (HeatEquation.inl, MomContEquation.inl:164-199) ----
+
+def _heat_mesh(dim):
+    return M.dam_break_2d(0.1, column=(1.0, 2.0), seed=5) if dim == 2 else M.dam_break_3d(0.1)
+
+
+def _mass_total(om, t):
+    """1^T M T: the heat content of the consistent mass matrix (cv rho = 1)."""
+    A, _ = O.heat_assemble(om, O.heat_params(1.0, 1.0, 0.0), 1.0, t, np.zeros(om.N, np.uint8))
+    return float(np.ones(om.N) @ (A @ t))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_heat_conserves_energy_without_boundary_terms(dim):
+    m = _heat_mesh(dim)
+    om = O.OracleMesh(m)
+    t0 = 300 + 50 * np.random.default_rng(1).random(m.n_nodes)
+    p = O.heat_params(1000.0, 4.0, 0.6)
+    t1 = O.heat_step(om, p, 0.05, t0, np.zeros(m.n_nodes, np.uint8))
+    # L has zero row sums and is symmetric, so 1^T (M + dt L) = 1^T M: sum(M T) is conserved
+    assert _mass_total(om, t1) == pytest.approx(_mass_total(om, t0), rel=1e-13)
+    assert np.ptp(t1) < np.ptp(t0)  # diffusion flattens the field
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_heat_keeps_a_linear_field_with_matching_dirichlet_walls(dim):
+    m = _heat_mesh(dim)
+    om = O.OracleMesh(m)
+    lin = 300 + 7 * m.pos[0] - 3 * m.pos[dim - 1]
+    fl = np.where(m.flags & M.BOUND, O.HT_T, 0).astype(np.uint8)
+    fl[(m.flags & M.FREE_SURFACE) != 0] = O.HT_T  # the whole boundary prescribed
+    p = O.heat_params(1.0, 1.0, 5.0)
+    t1 = O.heat_step(om, p, 0.1, lin, fl, t_bc=lin)
+    # P1 Laplacian of a linear field vanishes at interior nodes, M T = M T_prev
+    assert np.abs(t1 - lin).max() < 1e-9 * np.abs(lin).max()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_heat_flux_and_convection_energy_balance(dim):
+    m = _heat_mesh(dim)
+    om = O.OracleMesh(m)
+    N = m.n_nodes
+    dt, h, tinf = 0.2, 8.0, 250.0
+    t0 = np.full(N, 300.0)
+    # convection on the free surface: with T uniform, energy change = -dt h (T - Tinf) |free surface|
+    p = O.heat_params(1.0, 1.0, 0.3, h=h, t_inf=tinf, fs_flags=O.HT_QH)
+    A, b = O.heat_assemble(om, p, dt, t0, np.zeros(N, np.uint8))
+    fs_measure = 0.0
+    for f in range(m.facets.shape[1]):
+        nd = m.facets[:, f]
+        if all(m.flags[nd] & M.FREE_SURFACE):
+            X = m.pos[:, nd]
+            fs_measure += (np.linalg.norm(X[:, 1] - X[:, 0]) if dim == 2 else
+                           0.5 * np.linalg.norm(np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0])))
+    assert fs_measure > 0
+    assert b.sum() - _mass_total(om, t0) == pytest.approx(-dt * h * (300.0 - tinf) * fs_measure, rel=1e-12)
+    # a uniform flux q through the wall facets: energy change = -dt sum_f (q . n) |f|, n outward
+    fl = np.where(m.flags & M.BOUND, O.HT_Q, 0).astype(np.uint8)
+    q = np.array([0.7, -1.3, 0.4][:dim])
+    qgp = np.broadcast_to(q, (m.facets.shape[1], 3, dim)).copy()
+    A, b = O.heat_assemble(om, O.heat_params(1.0, 1.0, 0.3), dt, t0, fl, q_gp=qgp)
+    flow = 0.0
+    cen = m.pos.mean(axis=1)
+    for f in range(m.facets.shape[1]):
+        nd = m.facets[:, f]
+        if not all(fl[nd] & O.HT_Q):
+            continue
+        X = m.pos[:, nd]
+        if dim == 2:
+            n = np.array([X[1, 1] - X[1, 0], X[0, 0] - X[0, 1]])
+        else:
+            n = np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]) / 2
+        e = m.facet_elm[f]
+        out = [v for v in m.conn[:, e] if v not in nd][0]
+        if n @ (m.pos[:, out] - X[:, 0]) > 0:
+            n = -n
+        flow += q @ n  # |n| is the facet measure
+    assert flow != 0
+    # the balance is a small difference of two sums of the heat content: round-off of that scale
+    e0 = _mass_total(om, t0)
+    assert b.sum() - e0 == pytest.approx(-dt * flow, abs=1e-13 * e0)
+
+
+def test_heat_gauss_positions_helper_matches_oracle():
+    from pfem_gb300 import heat as H
+
+    for dim in (2, 3):
+        m = _heat_mesh(dim)
+        om = O.OracleMesh(m)
+        assert np.abs(O.facet_gauss_positions(om) - H.facet_gauss_positions(m.pos, m.facets)).max() < 1e-14
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_boussinesq_uniform_temperature_scales_gravity(dim):
+    """A uniform T turns the Boussinesq factors into the constant 1 - alpha (T - Tr): the
+    right-hand side equals the plain one with gravity scaled by it."""
+    m = _heat_mesh(dim)
+    om = O.OracleMesh(m)
+    R = (dim + 1) * m.n_nodes
+    rng = np.random.default_rng(3)
+    q = np.zeros(R)
+    q[:dim * m.n_nodes] = 0.01 * rng.standard_normal(dim * m.n_nodes)
+    alpha, tr, T = 69e-6, 650.0, 900.0
+    fac = 1 - alpha * (T - tr)
+    g = (0.0, -9.81, 0.0) if dim == 2 else (0.0, 0.0, -9.81)
+    _, b1 = O.pspg_assemble(om, 1000.0, 1e-3, 1e-3, g, q, q, boussinesq=(alpha, tr, np.full(m.n_nodes, T)),
+                            apply_bc=False)
+    _, b0 = O.pspg_assemble(om, 1000.0, 1e-3, 1e-3, tuple(fac * x for x in g), q, q, apply_bc=False)
+    assert np.abs(b1 - b0).max() < 1e-12 * np.abs(b0).max()
