@@ -138,6 +138,10 @@ typedef struct pfg_params {
                                   Gauss point, T the node temperatures                     */
     double alpha_t;            /* thermal expansion coefficient alpha                      */
     double t_ref;              /* reference temperature Tr                                 */
+    double dgamma_dt;          /* Boussinesq: surface tension gamma + dgamma_dt (T - Tr) at
+                                  the facet Gauss points (DgammaDT, MomContEquation.inl:
+                                  174-179); the facet term runs when gamma or dgamma_dt is
+                                  >= 1e-15 (MomContEquationPSPG.inl:157-158)              */
 } pfg_params;
 
 /* Heat boundary-condition flags per node (the reference's tag flags of HeatEq's BC table,

@@ -46,7 +46,8 @@ def build(force=False):
 class PspgParams(C.Structure):
     _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double), ("g", C.c_double * 3),
                 ("gamma", C.c_double), ("tau0", C.c_double), ("mReg", C.c_double),
-                ("alpha", C.c_double), ("Tr", C.c_double), ("T", C.POINTER(C.c_double))]
+                ("alpha", C.c_double), ("Tr", C.c_double), ("T", C.POINTER(C.c_double)),
+                ("dgammaDT", C.c_double)]
 
 
 class HeatParams(C.Structure):
@@ -198,15 +199,16 @@ class OracleMesh:
 
 
 def pspg_params(rho, mu, dt, g, gamma=0.0, tau0=0.0, m_reg=0.0, boussinesq=None):
-    """boussinesq: None, or (alpha, Tr, T) with T the node temperatures (kept alive on p)."""
+    """boussinesq: None, or (alpha, Tr, T[, DgammaDT]) with T the node temperatures (kept alive on p)."""
     p = PspgParams()
     p.rho, p.mu, p.dt, p.gamma, p.tau0, p.mReg = rho, mu, dt, gamma, tau0, m_reg
     for i, x in enumerate(g):
         p.g[i] = x
     if boussinesq is not None:
-        alpha, Tr, T = boussinesq
+        alpha, Tr, T = boussinesq[:3]
         p._T = np.ascontiguousarray(T, dtype=np.float64)
         p.alpha, p.Tr, p.T = alpha, Tr, _dp(p._T)
+        p.dgammaDT = boussinesq[3] if len(boussinesq) > 3 else 0.0
     return p
 
 

@@ -123,6 +123,7 @@ struct PspgParams {
     // T interpolated from the node temperatures (null: not Boussinesq)
     double alpha, Tr;
     const double* T;
+    double dgammaDT;   // Boussinesq surface tension gamma + DgammaDT (T - Tr) (:174-179)
 };
 
 // HeatEqIncompNewton material (HeatEquation.inl:27-32) and the heat boundary-condition flags
@@ -381,6 +382,42 @@ Mat ddevWC(int dim) {  // WCompNewton/MomEquation.inl:63-83
     return D;
 }
 
+// Facet Gauss rule (nGPLD = 3, HeatEquation.inl:13-22): Mesh::getGaussPoints/getGaussWeight/
+// getShapeFunctions/getRefElementSize of dimension d-1 (Mesh.cpp:342-530).
+struct FacetGauss {
+    double xi[3][2];
+    double w[3];
+    double sf[3][3];
+    double ref;
+};
+
+FacetGauss facetGauss(int dim) {
+    FacetGauss t{};
+    if (dim == 2) {
+        const double x[3] = {-std::sqrt(3.0 / 5.0), 0.0, std::sqrt(3.0 / 5.0)};
+        const double w[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
+        for (int g = 0; g < 3; ++g) {
+            t.xi[g][0] = x[g];
+            t.w[g] = w[g];
+            t.sf[g][0] = (1 - x[g]) / 2;
+            t.sf[g][1] = (1 + x[g]) / 2;
+        }
+        t.ref = 2.0;
+    } else {
+        const double p[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}, {2.0 / 3.0, 1.0 / 6.0}};
+        for (int g = 0; g < 3; ++g) {
+            t.xi[g][0] = p[g][0];
+            t.xi[g][1] = p[g][1];
+            t.w[g] = 1.0 / 3.0;
+            t.sf[g][0] = 1 - p[g][0] - p[g][1];
+            t.sf[g][1] = p[g][0];
+            t.sf[g][2] = p[g][1];
+        }
+        t.ref = 0.5;
+    }
+    return t;
+}
+
 // ---------------------------------------------------------------------------------------
 // Surface tension on the facets
 // ---------------------------------------------------------------------------------------
@@ -466,11 +503,14 @@ Mat getT(int dim, const Mat& Pm) {
 // 141-146).  Three facet Gauss points (nGPLD = 3, MomContEquation.inl:17,22), weights of
 // Mesh::getGaussWeight (Mesh.cpp:416-450), reference sizes of Mesh::getRefElementSize
 // (Mesh.cpp:472-484).  FST[i + d*npe] is the force on velocity component d of element node i.
-void getFST(const OrcMesh& m, int f, double gamma, double* FST) {
+// With T (problem "Boussinesq") the factor is gamma + dgdt (T_g - Tr) at each facet Gauss point,
+// T_g interpolated from the facet's node temperatures (MomContEquation.inl:174-179).
+void getFST(const OrcMesh& m, int f, double gamma, double* FST, const double* Tn = nullptr, double dgdt = 0,
+            double Tr = 0) {
     const int dim = m.dim, npe = m.npe;
-    const double w2[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0}, w3[3] = {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0};
-    const double* w = dim == 2 ? w2 : w3;
-    const double refLD = dim == 2 ? 2.0 : 0.5;
+    const FacetGauss fg = facetGauss(dim);
+    const double* w = fg.w;
+    const double refLD = fg.ref;
     const ElemGeom& geo = m.geom[m.facetElm[f]];
     Mat B = getB(dim, getGradN(dim, geo));
     double detJ, n[3];
@@ -479,8 +519,15 @@ void getFST(const OrcMesh& m, int f, double gamma, double* FST) {
     Mat T = getT(dim, P);
     Mat BtTP = mul(mul(transpose(B), T), P);
     for (int r = 0; r < dim * npe; ++r) FST[r] = 0;
-    for (int g = 0; g < 3; ++g)
-        for (int r = 0; r < dim * npe; ++r) FST[r] -= gamma * BtTP(r, 0) * w[g];
+    for (int g = 0; g < 3; ++g) {
+        double fac = gamma;
+        if (Tn) {
+            double Tg = 0;
+            for (int k = 0; k < dim; ++k) Tg += fg.sf[g][k] * Tn[m.facets[(size_t)k * m.F + f]];
+            fac = gamma + dgdt * (Tg - Tr);
+        }
+        for (int r = 0; r < dim * npe; ++r) FST[r] -= fac * BtTP(r, 0) * w[g];
+    }
     for (int r = 0; r < dim * npe; ++r) FST[r] *= detJ * refLD;
 }
 
@@ -488,15 +535,16 @@ void getFST(const OrcMesh& m, int f, double gamma, double* FST) {
 // of its nodes is on the free surface) and MomEqWCompNewton::m_applyBC (MomEquation.inl:
 // 311-335; Facet::isOnFreeSurface, Facet.cpp:249-255: all of its nodes), adding each facet's
 // FST to the velocity rows target[node + d*N] in facet order.
-void addSurfaceTension(const OrcMesh& m, double gamma, bool anyNode, double* target) {
-    if (gamma < 1e-15) return;
+void addSurfaceTension(const OrcMesh& m, double gamma, bool anyNode, double* target, const double* T = nullptr,
+                       double dgdt = 0, double Tr = 0) {
+    if (gamma < 1e-15 && !(T && dgdt >= 1e-15)) return;
     const int dim = m.dim, npe = m.npe, N = m.N;
     double FST[12];
     for (int f = 0; f < m.F; ++f) {
         int cnt = 0;
         for (int k = 0; k < dim; ++k) cnt += (m.flags[m.facets[(size_t)k * m.F + f]] & FREE_SURFACE) ? 1 : 0;
         if (anyNode ? cnt == 0 : cnt < dim) continue;
-        getFST(m, f, gamma, FST);
+        getFST(m, f, gamma, FST, T, dgdt, Tr);
         const int e = m.facetElm[f];
         for (int i = 0; i < npe; ++i)
             for (int d = 0; d < dim; ++d) target[m.node(e, i) + (size_t)d * N] += FST[i + d * npe];
@@ -646,42 +694,6 @@ void setFromTriplets(OrcMesh& m, const std::vector<Triplet>& indexA, int R) {
 // ---------------------------------------------------------------------------------------
 // Heat equation (HeatEqIncompNewton), srcs/simulation/physics/IncompNewton/HeatEquation.inl
 // ---------------------------------------------------------------------------------------
-// Facet Gauss rule (nGPLD = 3, HeatEquation.inl:13-22): Mesh::getGaussPoints/getGaussWeight/
-// getShapeFunctions/getRefElementSize of dimension d-1 (Mesh.cpp:342-530).
-struct FacetGauss {
-    double xi[3][2];
-    double w[3];
-    double sf[3][3];
-    double ref;
-};
-
-FacetGauss facetGauss(int dim) {
-    FacetGauss t{};
-    if (dim == 2) {
-        const double x[3] = {-std::sqrt(3.0 / 5.0), 0.0, std::sqrt(3.0 / 5.0)};
-        const double w[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
-        for (int g = 0; g < 3; ++g) {
-            t.xi[g][0] = x[g];
-            t.w[g] = w[g];
-            t.sf[g][0] = (1 - x[g]) / 2;
-            t.sf[g][1] = (1 + x[g]) / 2;
-        }
-        t.ref = 2.0;
-    } else {
-        const double p[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}, {2.0 / 3.0, 1.0 / 6.0}};
-        for (int g = 0; g < 3; ++g) {
-            t.xi[g][0] = p[g][0];
-            t.xi[g][1] = p[g][1];
-            t.w[g] = 1.0 / 3.0;
-            t.sf[g][0] = 1 - p[g][0] - p[g][1];
-            t.sf[g][1] = p[g][0];
-            t.sf[g][2] = p[g][1];
-        }
-        t.ref = 0.5;
-    }
-    return t;
-}
-
 // Facet::computeNormal (Facet.cpp:130-210): the normal of facetGeometry turned away from the
 // element's node that is not on the facet (Facet::getOutNode).
 void orientedNormal(const OrcMesh& m, int f, double n[3]) {
@@ -901,7 +913,7 @@ int orc_pspg_assemble(OrcMesh* m, const PspgParams* p, const double* qIter, cons
 
     if (apply_bc) {
         // m_applyBCPSPG facet loop (:155-187)
-        addSurfaceTension(*m, p->gamma, true, m->b.data());
+        addSurfaceTension(*m, p->gamma, true, m->b.data(), p->T, p->dgammaDT, p->Tr);
         // m_applyBCPSPG node loop (:189-232)
         for (int n = 0; n < N; ++n) {
             if (m->isFree[n]) {

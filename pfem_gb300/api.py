@@ -59,7 +59,7 @@ class Params(C.Structure):
         ("tau0", C.c_double), ("m_reg", C.c_double),
         ("heat_k", C.c_double), ("heat_cv", C.c_double), ("heat_h", C.c_double), ("heat_t_inf", C.c_double),
         ("heat_eps_rad", C.c_double), ("heat_fs_flags", C.c_int32), ("boussinesq", C.c_int32),
-        ("alpha_t", C.c_double), ("t_ref", C.c_double),
+        ("alpha_t", C.c_double), ("t_ref", C.c_double), ("dgamma_dt", C.c_double),
     ]
 
 

@@ -9,6 +9,7 @@
 
 #include "pfg_device.cuh"
 #include "pfg_internal.cuh"
+#include "pfg_fst.cuh"
 
 namespace pfg {
 
@@ -174,8 +175,8 @@ int check_ctx(pfg_ctx* c) {
 
 // Surface tension needs the facets of the current mesh.
 int check_facets(pfg_ctx* c) {
-    if (c->prm.gamma >= 1e-15 && !c->has_facets)
-        return fail(c, PFG_ERR_STATE, "gamma > 0: call pfg_upload_facets after pfg_upload_mesh");
+    if (fst_on(c) && !c->has_facets)
+        return fail(c, PFG_ERR_STATE, "surface tension: call pfg_upload_facets after pfg_upload_mesh");
     return PFG_OK;
 }
 

@@ -33,6 +33,12 @@ struct FstArgs {
     int F, n_nodes;
     double coef;           // gamma * sum_g w_g (3-point facet rule) * refSize(dim - 1)
     float coef32;          // the same, for FP32 kernels
+    // problem "Boussinesq" with DgammaDT: the factor gamma + DgammaDT (T_g - Tr) summed over the
+    // facet Gauss points is sum_g w_g (gamma - DgammaDT Tr) + DgammaDT sum_g w_g T_g, and
+    // sum_g w_g N_k(g) = sum_g w_g / dim for every facet node k of both 3-point rules, so the
+    // facet coefficient is coef + tcoef * (sum of the facet's node temperatures)
+    const double* T;       // node temperatures, or nullptr
+    double tcoef;          // DgammaDT * sum_g w_g / dim * refSize(dim - 1)
 };
 
 // Coordinate differences x_a - x_b of an FP64 position array.
@@ -152,7 +158,13 @@ __device__ __forceinline__ void fst_gather(int j, int E, const FstArgs& fa, cons
             }
         }
         // rows of B^T w for node i (getB, MatricesBuilder.inl:129-164)
-        const T cm = (sizeof(T) == sizeof(float) ? (T)fa.coef32 : (T)fa.coef) * meas;
+        T cf = sizeof(T) == sizeof(float) ? (T)fa.coef32 : (T)fa.coef;
+        if (fa.T) {
+            double ts = fa.T[a] + fa.T[b];
+            if constexpr (DIM == 3) ts += fa.T[fa.fnodes[2 * fa.F + f]];
+            cf = (T)(fa.coef + fa.tcoef * ts);
+        }
+        const T cm = cf * meas;
         if constexpr (DIM == 2) {
             F[0] -= cm * (g[0] * tw[0] + g[1] * tw[2]);
             F[1] -= cm * (g[1] * tw[1] + g[0] * tw[2]);
@@ -178,10 +190,16 @@ __global__ void k_fst(FstArgs fa, int E, const int* __restrict__ conn, Pos dx, i
     for (int d = 0; d < DIM; ++d) out[(size_t)d * N + n] = F[d];
 }
 
-// Kernel argument block of the context (nodes = nullptr when gamma < 1e-15 or no entries).
+// The facet term runs when gamma >= 1e-15, or (Boussinesq) DgammaDT >= 1e-15
+// (MomContEquationPSPG.inl:157-158).
+inline bool fst_on(const pfg_ctx* c) {
+    return c->prm.gamma >= 1e-15 || (c->prm.boussinesq && c->prm.dgamma_dt >= 1e-15);
+}
+
+// Kernel argument block of the context (nodes = nullptr when the term is off or has no entries).
 inline FstArgs fst_args(const pfg_ctx* c) {
     FstArgs a{};
-    if (c->prm.gamma < 1e-15 || c->n_fst_nodes == 0) return a;
+    if (!fst_on(c) || c->n_fst_nodes == 0) return a;
     a.nodes = ptr<int>(c->nf_nodes);
     a.n_nodes = c->n_fst_nodes;
     a.nf_ptr = ptr<int>(c->nf_ptr);
@@ -192,15 +210,21 @@ inline FstArgs fst_args(const pfg_ctx* c) {
     // 3-point facet rules (Mesh::getGaussWeight, Mesh.cpp:416-450), summed in order, and the
     // reference facet sizes (Mesh::getRefElementSize, Mesh.cpp:472-484)
     const double sumw = c->dim == 2 ? 5.0 / 18.0 + 8.0 / 18.0 + 5.0 / 18.0 : 1.0 / 3.0 + 1.0 / 3.0 + 1.0 / 3.0;
-    a.coef = c->prm.gamma * sumw * (c->dim == 2 ? 2.0 : 0.5);
+    const double ref = c->dim == 2 ? 2.0 : 0.5;
+    a.coef = c->prm.gamma * sumw * ref;
     a.coef32 = (float)a.coef;
+    if (c->prm.boussinesq && c->prm.dgamma_dt != 0.0) {
+        a.T = ptr<double>(c->heat_t);
+        a.coef = (c->prm.gamma - c->prm.dgamma_dt * c->prm.t_ref) * sumw * ref;
+        a.tcoef = c->prm.dgamma_dt * sumw / c->dim * ref;
+    }
     return a;
 }
 
 // The force array the node kernels add (nullptr when surface tension is off).
 template <class T>
 inline const T* fst_force(const pfg_ctx* c) {
-    return (c->prm.gamma < 1e-15 || c->n_fst_nodes == 0) ? nullptr : ptr<T>(c->fst_force);
+    return (!fst_on(c) || c->n_fst_nodes == 0) ? nullptr : ptr<T>(c->fst_force);
 }
 
 }  // namespace pfg

@@ -173,3 +173,56 @@ def test_gamma_needs_facets(gpu_lib, square):
         ctx.upload_facets(bad, square.facet_elm)
     ctx.upload_facets(square.facets, square.facet_elm)
     assert ctx.picard_step(2.5e-3).converged == 1
+
+
+def _hot_spot(mesh):
+    x = mesh.pos
+    return 300.0 + 80.0 * np.exp(-((x[0] - 0.3) ** 2 + (x[1] - 0.4) ** 2) / 0.05)
+
+
+DGDT = -1.5e-3  # Boussinesq surface tension slope DgammaDT (gamma + DgammaDT (T - Tr))
+
+
+@pytest.mark.parametrize("which", ["square", "ball"])
+def test_temperature_dependent_surface_tension_rhs(gpu_lib, which, square, ball):
+    """Problem "Boussinesq": gamma + DgammaDT (T_g - Tr) at the facet Gauss points
+    (MomContEquation.inl:174-179), with a non-uniform temperature and no buoyancy (alpha = 0)."""
+    mesh = square if which == "square" else ball
+    d, N = mesh.dim, mesh.n_nodes
+    rng = np.random.default_rng(12)
+    q_iter = rng.uniform(-0.05, 0.05, (d + 1) * N)
+    q_prev = rng.uniform(-0.05, 0.05, (d + 1) * N)
+    T = _hot_spot(mesh)
+    ctx = incomp_ctx(mesh, boussinesq=1, alpha_t=0.0, t_ref=300.0, dgamma_dt=DGDT)
+    ctx.set_temperature(T)
+    ctx.pspg_assemble(2.5e-3, q_iter, q_prev, apply_bc=True)
+    _, _, _, b = ctx.get_csr()
+    om = O.OracleMesh(mesh)
+    A, b_o = O.pspg_assemble(om, 100.0, 1.0, 2.5e-3, (0.0,) * 3, q_iter, q_prev, gamma=GAMMA,
+                             boussinesq=(0.0, 300.0, T, DGDT))
+    _, b1 = O.pspg_assemble(om, 100.0, 1.0, 2.5e-3, (0.0,) * 3, q_iter, q_prev, gamma=GAMMA)
+    assert np.abs(b_o - b1).max() > 1e-3 * np.abs(b1 - O.pspg_assemble(
+        om, 100.0, 1.0, 2.5e-3, (0.0,) * 3, q_iter, q_prev)[1]).max()  # the slope matters here
+    bscale = np.maximum(np.abs(b_o), np.abs(A.tocsr()).max(axis=1).toarray().ravel() * 1e-3)
+    assert (np.abs(b - b_o) / np.maximum(bscale, 1e-300)).max() < 1e-12
+
+
+@pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_MIXED])
+def test_temperature_dependent_surface_tension_picard(gpu_lib, square, precision):
+    mesh = square
+    d, N = mesh.dim, mesh.n_nodes
+    T = _hot_spot(mesh)
+    ctx = incomp_ctx(mesh, precision, boussinesq=1, alpha_t=0.0, t_ref=300.0, dgamma_dt=DGDT)
+    ctx.set_temperature(T)
+    q0 = np.zeros((d + 1) * N)
+    ctx.set_states(q0)
+    om = O.OracleMesh(mesh)
+    qo = q0.copy()
+    for step in range(3):
+        st = ctx.picard_step(2.5e-3)
+        qo, res = O.pspg_picard_step(om, qo, 2.5e-3, rho=100.0, mu=1.0, g=(0.0, 0.0), gamma=GAMMA,
+                                     boussinesq=(0.0, 300.0, T, DGDT))
+        assert st.converged == 1 and res.converged
+        assert st.picard_iterations == res.iterations
+        errs = field_errs(ctx.get_states(), qo, d + 1, N)
+        assert max(errs) < 1e-8, (step, errs)

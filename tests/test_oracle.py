@@ -311,3 +311,18 @@ def test_boussinesq_uniform_temperature_scales_gravity(dim):
                             apply_bc=False)
     _, b0 = O.pspg_assemble(om, 1000.0, 1e-3, 1e-3, tuple(fac * x for x in g), q, q, apply_bc=False)
     assert np.abs(b1 - b0).max() < 1e-12 * np.abs(b0).max()
+
+
+def test_uniform_temperature_surface_tension_equals_shifted_gamma():
+    """With a uniform T the Boussinesq factor gamma + DgammaDT (T - Tr) is a constant."""
+    m = M.square_to_disk_2d(0.05)
+    om = O.OracleMesh(m)
+    N = m.n_nodes
+    q = np.zeros(3 * N)
+    gamma, dgdt, T, tr = 1.9, -2e-3, 420.0, 300.0
+    _, b1 = O.pspg_assemble(om, 100.0, 1.0, 1e-3, (0.0, 0.0, 0.0), q, q, gamma=gamma,
+                            boussinesq=(0.0, tr, np.full(N, T), dgdt), apply_bc=True)
+    _, b0 = O.pspg_assemble(om, 100.0, 1.0, 1e-3, (0.0, 0.0, 0.0), q, q, gamma=gamma + dgdt * (T - tr),
+                            apply_bc=True)
+    assert np.abs(b0).max() > 0
+    assert np.abs(b1 - b0).max() < 1e-13 * np.abs(b0).max()
