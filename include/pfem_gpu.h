@@ -79,7 +79,8 @@ typedef enum {
 typedef enum {
     PFG_RES_AX_F = 0,          /* ||A q - b||_2            MomContEquationPSPG.inl:366-371 */
     PFG_RES_U = 1,             /* relative velocity change                        :319-342 */
-    PFG_RES_U_P = 2            /* max(rel. velocity change, rel. pressure change) :343-364 */
+    PFG_RES_U_P = 2,           /* max(rel. velocity change, rel. pressure change) :343-364 */
+    PFG_RES_T = 3              /* heat: relative temperature change  HeatEquation.inl:153-180 */
 } pfg_residual;
 
 typedef struct pfg_params {
@@ -142,6 +143,17 @@ typedef struct pfg_params {
                                   the facet Gauss points (DgammaDT, MomContEquation.inl:
                                   174-179); the facet term runs when gamma or dgamma_dt is
                                   >= 1e-15 (MomContEquationPSPG.inl:157-158)              */
+    /* heat equation Picard loop (HeatEq maxIter / minRes / residual) and phase change
+       (HeatEquation.inl:36-45, 60-66, 421-425): with heat_phase_change the mass factor is
+       (cv + dfl/dT(T) Lm) rho at the element Gauss points and each heat step iterates       */
+    int32_t heat_max_iter;     /* maxIter                                                  */
+    int32_t heat_residual;     /* PFG_RES_T or PFG_RES_AX_F                                */
+    double heat_min_res;       /* minRes                                                   */
+    int32_t heat_phase_change; /* 1: latent heat (Tm, DT, Lm given)                       */
+    int32_t pad3;
+    double heat_tm;            /* melting temperature Tm                                   */
+    double heat_dt_melt;       /* melting range DT                                         */
+    double heat_lm;            /* latent heat Lm                                           */
 } pfg_params;
 
 /* Heat boundary-condition flags per node (the reference's tag flags of HeatEq's BC table,

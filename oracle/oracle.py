@@ -52,7 +52,8 @@ class PspgParams(C.Structure):
 
 class HeatParams(C.Structure):
     _fields_ = [("rho", C.c_double), ("cv", C.c_double), ("k", C.c_double), ("h", C.c_double),
-                ("Tinf", C.c_double), ("epsRad", C.c_double), ("fsFlags", C.c_int32), ("pad", C.c_int32)]
+                ("Tinf", C.c_double), ("epsRad", C.c_double), ("fsFlags", C.c_int32), ("phaseChange", C.c_int32),
+                ("Tm", C.c_double), ("DT", C.c_double), ("Lm", C.c_double)]
 
 
 # heat boundary-condition flags (per node, and for the free-surface tag)
@@ -94,7 +95,7 @@ def lib():
         L.orc_pspg_assemble.argtypes = [vp, C.POINTER(PspgParams), dp, dp, dp, C.c_int]
         L.orc_pspg_get.argtypes = [vp, ip, ip, dp, dp]
         L.orc_heat_assemble.restype = C.c_int
-        L.orc_heat_assemble.argtypes = [vp, C.POINTER(HeatParams), C.c_double, dp, u8p, dp, dp]
+        L.orc_heat_assemble.argtypes = [vp, C.POINTER(HeatParams), C.c_double, dp, u8p, dp, dp, dp]
         L.orc_facet_gauss_positions.argtypes = [vp, dp]
         L.orc_wc_step.argtypes = [vp, C.POINTER(WcParams), C.c_double, dp, dp]
         L.orc_wc_next_dt.restype = C.c_double
@@ -320,14 +321,19 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
     return q_iter, res
 
 
-def heat_params(rho, cv, k, h=0.0, t_inf=0.0, eps_rad=0.0, fs_flags=0):
+def heat_params(rho, cv, k, h=0.0, t_inf=0.0, eps_rad=0.0, fs_flags=0, phase_change=None):
+    """phase_change: None or (Tm, DT, Lm)."""
     p = HeatParams()
     p.rho, p.cv, p.k, p.h, p.Tinf, p.epsRad, p.fsFlags = rho, cv, k, h, t_inf, eps_rad, int(fs_flags)
+    if phase_change is not None:
+        p.phaseChange = 1
+        p.Tm, p.DT, p.Lm = phase_change
     return p
 
 
-def heat_assemble(om, params, dt, t_prev, flags, t_bc=None, q_gp=None):
-    """A (scipy CSC) and b of HeatEqIncompNewton::m_buildAb + m_applyBC from T_prev."""
+def heat_assemble(om, params, dt, t_prev, flags, t_bc=None, q_gp=None, t_state=None):
+    """A (scipy CSC) and b of HeatEqIncompNewton::m_buildAb + m_applyBC from T_prev, with the
+    node states t_state (default T_prev) in the phase-change factor and the facet terms."""
     import scipy.sparse as sp
 
     N = om.N
@@ -335,9 +341,10 @@ def heat_assemble(om, params, dt, t_prev, flags, t_bc=None, q_gp=None):
     flags = np.ascontiguousarray(flags, np.uint8)
     t_bc = np.ascontiguousarray(np.zeros(N) if t_bc is None else t_bc, float)
     qp = None if q_gp is None else np.ascontiguousarray(q_gp, float)
+    ts = None if t_state is None else np.ascontiguousarray(t_state, float)
     nnz = lib().orc_heat_assemble(om.h, C.byref(params), float(dt), _dp(t_prev),
                                   flags.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(t_bc),
-                                  None if qp is None else _dp(qp))
+                                  None if qp is None else _dp(qp), None if ts is None else _dp(ts))
     colptr = np.empty(N + 1, np.int32)
     rowidx = np.empty(nnz, np.int32)
     vals = np.empty(nnz)
@@ -346,13 +353,45 @@ def heat_assemble(om, params, dt, t_prev, flags, t_bc=None, q_gp=None):
     return sp.csc_matrix((vals, rowidx, colptr), shape=(N, N)), b
 
 
-def heat_step(om, params, dt, t_prev, flags, t_bc=None, q_gp=None):
-    """`HeatEqIncompNewton::solve` without phase change: one Picard pass (runOnlyOnce,
-    HeatEquation.inl:195-196), the linear solve by SuperLU/COLAMD as in pspg_picard_step."""
+def heat_step(om, params, dt, t_prev, flags, t_bc=None, q_gp=None, max_iter=10, min_res=1e-6, residual="T",
+              result=None):
+    """`HeatEqIncompNewton::solve` (HeatEquation.inl:216-224) through `PicardAlgo::solve`
+    (PicardAlgo.cpp:31-95): without phase change one pass (runOnlyOnce, :195-196); with it,
+    Picard iterations that rebuild A and b from the new node temperatures (:131-138) until the
+    residual "T" (relative change over the non-free nodes, :153-180) or "Ax_f" (:182-185) is at
+    most min_res, failing after max_iter + 1 passes.  Linear solves by SuperLU/COLAMD.  Returns
+    the temperatures (t_prev on failure); `result`, a dict, receives converged / iterations."""
     from scipy.sparse.linalg import splu
 
+    t_prev = np.asarray(t_prev, float)
+    free = om.is_free()
     A, b = heat_assemble(om, params, dt, t_prev, flags, t_bc, q_gp)
-    return splu(A, permc_spec="COLAMD").solve(b)
+    t_it_prev = t_prev.copy()
+    res, it = float("inf"), 0
+    ok = True
+    while res > min_res:
+        if it > max_iter:
+            ok = False
+            break
+        t_it = splu(A, permc_spec="COLAMD").solve(b)
+        if params.phaseChange:
+            A, b = heat_assemble(om, params, dt, t_prev, flags, t_bc, q_gp, t_state=t_it)
+        if residual == "T":
+            num = float(np.sum((t_it - t_it_prev)[~free] ** 2))
+            den = float(np.sum(t_it_prev[~free] ** 2))
+            res = float("inf") if den == 0 else np.sqrt(num / den)
+        else:
+            res = float(np.linalg.norm(A @ t_it - b))
+        t_it_prev = t_it
+        if np.isnan(res):
+            ok = False
+            break
+        it += 1
+        if not params.phaseChange:
+            break
+    if result is not None:
+        result.update(converged=ok, iterations=it, residual=res)
+    return t_it if ok else t_prev.copy()
 
 
 def facet_gauss_positions(om):

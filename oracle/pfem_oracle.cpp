@@ -131,8 +131,16 @@ struct HeatParams {
     double rho, cv, k;
     double h, Tinf, epsRad;
     int32_t fsFlags;   // flags of the free-surface tag (-2): HT_Q / HT_QH / HT_QR
-    int32_t pad;
+    int32_t phaseChange;  // latent heat in the M factor (HeatEquation.inl:36-45, 60-66)
+    double Tm, DT, Lm;    // melting temperature, melting range, latent heat
 };
+
+// d fl / dT of the liquid fraction, HeatEqIncompNewton::m_getDflDT (HeatEquation.inl:421-425)
+double dFlDT(const HeatParams& p, double T) {
+    const double d3 = p.DT * p.DT * p.DT;
+    const double in = static_cast<double>(T > p.Tm - p.DT / 2) * static_cast<double>(T < p.Tm + p.DT / 2);
+    return in * (-2 * 3 / d3 * T * T + 6 * 2 * p.Tm / d3 * T + (3 / (2 * p.DT) - 6 * p.Tm * p.Tm / d3));
+}
 constexpr uint8_t HT_T = 1, HT_Q = 2, HT_QH = 4, HT_QR = 8;
 
 struct WcParams {
@@ -714,11 +722,18 @@ void orientedNormal(const OrcMesh& m, int f, double n[3]) {
 }
 
 // Element matrices of HeatEqIncompNewton::m_buildAb (HeatEquation.inl:240-246): Me with the
-// factor cv rho (:54-59) and Le = dt getL with the factor k (:70-74).
-void heatElement(const OrcMesh& m, int e, const HeatParams& p, double dt, Mat& Me, Mat& Le) {
+// factor cv rho (:54-59), with phase change (cv + dfl/dT(T_g) Lm) rho at each Gauss point, T_g
+// from the node states Ts (:60-66), and Le = dt getL with the factor k (:70-74).
+void heatElement(const OrcMesh& m, int e, const HeatParams& p, double dt, const double* Ts, Mat& Me, Mat& Le) {
     const ElemGeom& geo = m.geom[e];
     Mat G = getGradN(m.dim, geo);
-    Me = getM(m, geo, [&](int) { return p.cv * p.rho; });
+    if (p.phaseChange) {
+        double te[4];
+        for (int k = 0; k < m.npe; ++k) te[k] = Ts[m.node(e, k)];
+        Me = getM(m, geo, [&](int g) { return (p.cv + dFlDT(p, nDot(m.gt, g, te, m.npe)) * p.Lm) * p.rho; });
+    } else {
+        Me = getM(m, geo, [&](int) { return p.cv * p.rho; });
+    }
     double ksum = 0;
     for (int g = 0; g < m.gt.n; ++g) ksum += p.k * m.gt.w[g];
     Le = getL(m, geo, ksum, G);
@@ -939,14 +954,16 @@ int orc_pspg_assemble(OrcMesh* m, const PspgParams* p, const double* qIter, cons
 }
 
 // HeatEqIncompNewton::m_buildAb (HeatEquation.inl:226-305) and m_applyBC (:307-394) for one
-// Picard pass from T_prev.  hf[n]: HT_T (Dirichlet T = Tbc[n]), HT_Q / HT_QH / HT_QR (flux,
+// Picard pass from T_prev, with the node states Ts (the M factor with phase change, the facet
+// temperatures of Qh / Qr; null: Ts = T_prev).  hf[n]: HT_T (Dirichlet T = Tbc[n]), HT_Q / HT_QH / HT_QR (flux,
 // convection, radiation on the facets whose nodes all carry the flag; a free-surface facet
 // uses p->fsFlags).  qgp[(f*3 + g)*dim + d]: the prescribed flux vector at Gauss point g of
 // facet f (the "Q" BC function; read only for HT_Q facets, may be null otherwise).  The
 // system is left in colptr/rowidx/vals/b (orc_pspg_get).  Returns nnz.
 int orc_heat_assemble(OrcMesh* m, const HeatParams* p, double dt, const double* Tprev, const uint8_t* hf,
-                      const double* Tbc, const double* qgp) {
+                      const double* Tbc, const double* qgp, const double* Ts) {
     const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    if (!Ts) Ts = Tprev;
     const size_t tripletPerElm = (size_t)dim * npe * npe + (size_t)dim * npe * dim * npe + 3 * (size_t)npe * dim * npe +
                                  (size_t)npe * npe;
     // default-constructed triplets (0, 0, 0.0) stay in the unassigned slots (:232-233)
@@ -958,7 +975,7 @@ int orc_heat_assemble(OrcMesh* m, const HeatParams* p, double dt, const double* 
 #pragma omp parallel for
     for (int e = 0; e < E; ++e) {
         Mat Me, Le;
-        heatElement(*m, e, *p, dt, Me, Le);
+        heatElement(*m, e, *p, dt, Ts, Me, Le);
         double th[4];
         for (int k = 0; k < npe; ++k) th[k] = Tprev[m->node(e, k)];
         size_t countA = 0;
@@ -1003,7 +1020,7 @@ int orc_heat_assemble(OrcMesh* m, const HeatParams* p, double dt, const double* 
         double detJ, nrm[3];
         facetGeometry(*m, f, detJ, nrm);
         double tf[3];
-        for (int k = 0; k < dim; ++k) tf[k] = Tprev[nd[k]];
+        for (int k = 0; k < dim; ++k) tf[k] = Ts[nd[k]];
         if (bq) {  // getQN, MatricesBuilder.inl:246-272
             orientedNormal(*m, f, nrm);
             double qn[3] = {0, 0, 0};

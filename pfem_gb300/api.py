@@ -25,7 +25,7 @@ LINSOLVE_BICGSTAB = 0
 LINSOLVE_LU = 1
 PC_BLOCK_JACOBI = 0
 PC_MULTIGRID = 1
-RES_AX_F = 0
+RES_AX_F, RES_U, RES_U_P, RES_T = 0, 1, 2, 3
 
 NODE_BOUND, NODE_FREE_SURFACE, NODE_FIXED, NODE_DIRICHLET, NODE_FREE = 1, 2, 4, 8, 16
 
@@ -60,6 +60,9 @@ class Params(C.Structure):
         ("heat_k", C.c_double), ("heat_cv", C.c_double), ("heat_h", C.c_double), ("heat_t_inf", C.c_double),
         ("heat_eps_rad", C.c_double), ("heat_fs_flags", C.c_int32), ("boussinesq", C.c_int32),
         ("alpha_t", C.c_double), ("t_ref", C.c_double), ("dgamma_dt", C.c_double),
+        ("heat_max_iter", C.c_int32), ("heat_residual", C.c_int32), ("heat_min_res", C.c_double),
+        ("heat_phase_change", C.c_int32), ("pad3", C.c_int32), ("heat_tm", C.c_double), ("heat_dt_melt", C.c_double),
+        ("heat_lm", C.c_double),
     ]
 
 

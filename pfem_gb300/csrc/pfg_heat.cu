@@ -21,6 +21,7 @@
 // solves it to the Krylov tolerances of the context (the system is mass dominated: a few dozen
 // iterations).
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <vector>
 
@@ -43,7 +44,36 @@ struct HeatConst {
     double h, tinf, eps_rad;
     double fw[3], fsf[3][3], fxi[3][2];  // facet Gauss rule: weights, shape functions, points
     double fref;                         // refSize(dim - 1)
+    // phase change (HeatEquation.inl:36-45, 60-66): M factor (cv + dfl/dT(T_g) Lm) rho at the
+    // element Gauss points, T_g from the node temperatures of the current Picard iterate
+    int phase, ng;
+    double gN[4][4], gw[4];              // element Gauss rule: N_i at point g, weights
+    double cv, rho, tm, dtm, lm;
 };
+
+// d fl / dT of the liquid fraction (HeatEquation.inl:421-425): nonzero inside the melting
+// range (Tm - DT/2, Tm + DT/2), where fl is the cubic smoothstep of (T - Tm) / DT
+__device__ __forceinline__ double dfl_dt(const HeatConst& k, double T) {
+    const double d3 = k.dtm * k.dtm * k.dtm;
+    const double in = static_cast<double>(T > k.tm - k.dtm / 2) * static_cast<double>(T < k.tm + k.dtm / 2);
+    return in * (-2 * 3 / d3 * T * T + 6 * 2 * k.tm / d3 * T + (3 / (2 * k.dtm) - 6 * k.tm * k.tm / d3));
+}
+
+// Element mass entry M_ij / |e|: cv rho MM_ij, or with phase change sum_g (f_g N_i N_j) w_g
+// with f_g from the element's node temperatures ts (getM, MatricesBuilder.inl:216-229).
+template <int DIM>
+__device__ __forceinline__ double heat_m(const HeatConst& k, int i, int j, const double (&ts)[DIM + 1]) {
+    if (!k.phase) return k.mfac * k.MM[i][j];
+    double s = 0;
+    for (int g = 0; g < k.ng; ++g) {
+        double Tg = 0;
+#pragma unroll
+        for (int a = 0; a <= DIM; ++a) Tg += k.gN[g][a] * ts[a];
+        const double f = (k.cv + dfl_dt(k, Tg) * k.lm) * k.rho;
+        s += (f * (k.gN[g][i] * k.gN[g][j])) * k.gw[g];
+    }
+    return s;
+}
 
 HeatConst heat_const(pfg_ctx* c, double dt) {
     const GaussConst g = gauss_const(c->dim);
@@ -51,6 +81,17 @@ HeatConst heat_const(pfg_ctx* c, double dt) {
     for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 4; ++j) k.MM[i][j] = g.MM[i][j];
     k.mfac = c->prm.heat_cv * c->prm.rho;
+    k.phase = c->prm.heat_phase_change != 0;
+    k.ng = g.n;
+    for (int q = 0; q < 4; ++q) {
+        k.gw[q] = g.w[q];
+        for (int i = 0; i < 4; ++i) k.gN[q][i] = g.N[q][i];
+    }
+    k.cv = c->prm.heat_cv;
+    k.rho = c->prm.rho;
+    k.tm = c->prm.heat_tm;
+    k.dtm = c->prm.heat_dt_melt;
+    k.lm = c->prm.heat_lm;
     k.lsum = 0;
     for (int q = 0; q < g.n; ++q) k.lsum += c->prm.heat_k * g.w[q];
     k.refSize = g.refSize;
@@ -115,7 +156,7 @@ __global__ void __launch_bounds__(BLOCK) k_heat_pairs(int P, int E, const int* _
                                                       const double* __restrict__ ed,
                                                       const uint8_t* __restrict__ flags,
                                                       const uint8_t* __restrict__ hflags, double* __restrict__ val,
-                                                      HeatConst k) {
+                                                      const double* __restrict__ ts, HeatConst k) {
     constexpr int NPE = DIM + 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P) return;
@@ -138,7 +179,11 @@ __global__ void __launch_bounds__(BLOCK) k_heat_pairs(int P, int E, const int* _
 #pragma unroll
         for (int f = 0; f < DIM; ++f)
             dot += ed[(size_t)(2 + f * NPE + i) * E + e] * ed[(size_t)(2 + f * NPE + j) * E + e];
-        acc += (k.mfac * k.MM[i][j]) * ae;
+        double te[NPE] = {};
+        if (k.phase)
+#pragma unroll
+            for (int a = 0; a < NPE; ++a) te[a] = ts[__ldg(conn + (size_t)a * E + e)];
+        acc += heat_m<DIM>(k, i, j, te) * ae;
         acc += k.dt * ((ae * k.lsum) * dot);
     }
     val[t] = acc;
@@ -214,7 +259,8 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
                                                     const double* __restrict__ ed, const double* __restrict__ pos,
                                                     const uint8_t* __restrict__ flags,
                                                     const uint8_t* __restrict__ hflags,
-                                                    const double* __restrict__ t_prev, const double* __restrict__ tbc,
+                                                    const double* __restrict__ t_prev, const double* __restrict__ ts,
+                                                    const double* __restrict__ tbc,
                                                     const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
                                                     double* __restrict__ val, HeatFacets hf, HeatConst k,
                                                     double* __restrict__ rhs) {
@@ -228,9 +274,13 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
         int nd[NPE];
         load_nodes<DIM>(conn, E, e, nd);
         const double ae = ed[e] * k.refSize;
+        double te[NPE] = {};
+        if (k.phase)
+#pragma unroll
+            for (int a = 0; a < NPE; ++a) te[a] = ts[nd[a]];
         double s = 0;
 #pragma unroll
-        for (int j = 0; j < NPE; ++j) s += ((k.mfac * k.MM[i][j]) * ae) * t_prev[nd[j]];
+        for (int j = 0; j < NPE; ++j) s += (heat_m<DIM>(k, i, j, te) * ae) * t_prev[nd[j]];
         b += s;
     }
     constexpr double sigma = 5.670374419e-8;  // Stefan-Boltzmann constant (:90)
@@ -273,7 +323,7 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
             for (int g = 0; g < 3; ++g) {
                 double T = 0;
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) T += k.fsf[g][d] * t_prev[fn[d]];
+                for (int d = 0; d < DIM; ++d) T += k.fsf[g][d] * ts[fn[d]];
                 const double fac = pass == 0 ? k.h * (T - k.tinf)
                                              : sigma * k.eps_rad * (T * T * T * T - k.tinf * k.tinf * k.tinf * k.tinf);
                 sg += (fac * k.fsf[g][kk]) * k.fw[g];
@@ -301,7 +351,7 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
 
 // ---- Jacobi-preconditioned conjugate gradients over the pair-ordered CSR -----------------
 
-enum : int { S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_TOL2, S_DONE, S_ITERS, S_BB, S_COUNT };
+enum : int { S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_TOL2, S_DONE, S_ITERS, S_BB, S_NUM, S_DEN, S_COUNT };
 enum : int { V_R = 0, V_Z, V_P, V_Q, V_DIAG, V_COUNT };
 
 struct CgPtrs {
@@ -438,24 +488,45 @@ __global__ void __launch_bounds__(BLOCK) k_cg_p(int N, double* __restrict__ V, s
         V[V_P * ld + n] = V[V_Z * ld + n] + beta * V[V_P * ld + n];
 }
 
+// Squared relative change of the non-free nodes (residual "T", HeatEquation.inl:153-180):
+// sum (x - xp)^2 and sum xp^2 into sc[S_NUM], sc[S_DEN]; or, with b, ||b - A x||^2 into
+// sc[S_NUM] (residual "Ax_f", :182-185).
+__global__ void __launch_bounds__(BLOCK) k_heat_res(int N, const double* __restrict__ x, const double* __restrict__ xp,
+                                                    const uint8_t* __restrict__ flags, const int* __restrict__ rp,
+                                                    const int* __restrict__ col, const double* __restrict__ val,
+                                                    const double* __restrict__ b, CgPtrs k) {
+    __shared__ double sh[32];
+    double num = 0, den = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        if (b) {
+            double ax = 0;
+            for (int t = rp[n]; t < rp[n + 1]; ++t) ax += val[t] * x[col[t]];
+            const double r = b[n] - ax;
+            num += r * r;
+        } else if (!(flags[n] & F_FREE)) {
+            const double d = x[n] - xp[n];
+            num += d * d;
+            den += xp[n] * xp[n];
+        }
+    }
+    double s1, s2;
+    if (grid_sum2<BLOCK>(num, den, k.partials, k.ticket, sh, s1, s2) && threadIdx.x == 0) {
+        k.sc[S_NUM] = s1;
+        k.sc[S_DEN] = s2;
+    }
+}
+
 template <int DIM>
-int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
+void heat_assemble(pfg_ctx* c, const HeatConst& k, const double* tprev, const double* ts) {
     const int N = c->N, E = c->E;
-    const HeatConst k = heat_const(c, dt);
-    double* T = ptr<double>(c->heat_t);
-    double* V = ptr<double>(c->heat_cg);
-    const size_t ld = (size_t)std::max(N, 1);
-    double* x = V + V_COUNT * ld;
-    if (E > 0) {
+    if (E > 0)
         k_heat_geom<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
                                                                     ptr<double>(c->edata));
-        PFG_CHECK_LAUNCH(c);
-    }
     if (c->P > 0)
         k_heat_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
             c->P, E, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
             ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<double>(c->edata), ptr<uint8_t>(c->flags),
-            ptr<uint8_t>(c->heat_flags), ptr<double>(c->heat_val), k);
+            ptr<uint8_t>(c->heat_flags), ptr<double>(c->heat_val), ts, k);
     HeatFacets hf;
     hf.ptr = ptr<int>(c->hf_ptr);
     hf.ent = ptr<int>(c->hf_ent);
@@ -466,12 +537,18 @@ int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
     hf.F = c->F;
     k_heat_rhs<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
         N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
-        ptr<double>(c->edata), ptr<double>(c->pos), ptr<uint8_t>(c->flags), ptr<uint8_t>(c->heat_flags), T,
+        ptr<double>(c->edata), ptr<double>(c->pos), ptr<uint8_t>(c->flags), ptr<uint8_t>(c->heat_flags), tprev, ts,
         ptr<double>(c->heat_tbc), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<double>(c->heat_val), hf, k,
         ptr<double>(c->heat_rhs));
-    PFG_CHECK_LAUNCH(c);
-    // CG from T_prev (solveWithGuess, :126)
-    PFG_CUDA(c, cudaMemcpyAsync(x, T, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+}
+
+// CG solve of the assembled system from x0 = T_prev (solveWithGuess, :126) into x.  Returns
+// the convergence flag; iterations and the last recursive residual accumulate in st.
+int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, bool* ok) {
+    const int N = c->N;
+    double* V = ptr<double>(c->heat_cg);
+    const size_t ld = (size_t)std::max(N, 1);
+    PFG_CUDA(c, cudaMemcpyAsync(x, tprev, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     const CgPtrs kp = cg_ptrs(c);
     const int grid = std::max(1, std::min(c->max_grid, div_up(N, BLOCK)));
     const int* rp = ptr<int>(c->nbr_ptr);
@@ -496,13 +573,74 @@ int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
         PFG_CUDA(c, cudaStreamSynchronize(c->stream));
         if (h[S_DONE] != 0.0) break;
     }
-    const bool ok = h[S_DONE] == 1.0;
-    st->converged = ok ? 1 : 0;
-    st->picard_iterations = 1;
-    st->krylov_iterations = (int)h[S_ITERS];
-    st->residual = std::sqrt(h[S_RR]);
+    *ok = h[S_DONE] == 1.0;
+    st->krylov_iterations += (int)h[S_ITERS];
+    return PFG_OK;
+}
+
+// HeatEqIncompNewton::solve through PicardAlgo::solve (PicardAlgo.cpp:31-95): without phase
+// change one pass (runOnlyOnce); with it, the system is rebuilt from each iterate's temperatures
+// (:131-138) until the residual is at most heat_min_res, failing (temperatures restored) after
+// heat_max_iter + 1 passes or on a NaN residual.
+template <int DIM>
+int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
+    const int N = c->N;
+    const HeatConst k = heat_const(c, dt);
+    double* T = ptr<double>(c->heat_t);  // the node states: the Picard iterate
+    double* V = ptr<double>(c->heat_cg);
+    const size_t ld = (size_t)std::max(N, 1);
+    double* x = V + V_COUNT * ld;
+    double* tprev = x + ld;
+    double* xprev = tprev + ld;
+    PFG_CUDA(c, cudaMemcpyAsync(tprev, T, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(xprev, T, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    heat_assemble<DIM>(c, k, tprev, T);
+    PFG_CHECK_LAUNCH(c);
+    const bool axf = c->prm.heat_residual == PFG_RES_AX_F;
+    const int max_iter = c->prm.heat_max_iter;
+    const CgPtrs kp = cg_ptrs(c);
+    const int grid = std::max(1, std::min(c->max_grid, div_up(N, BLOCK)));
+    double* h = c->h_scalars;
+    double res = INFINITY;
+    int it = 0;
+    bool ok = true;
     st->dt = dt;
-    if (ok) PFG_CUDA(c, cudaMemcpyAsync(T, x, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    while (res > c->prm.heat_min_res) {
+        if (it > max_iter) {
+            ok = false;
+            break;
+        }
+        bool solved = false;
+        int rc = heat_cg(c, tprev, x, st, &solved);
+        if (rc) return rc;
+        if (!solved) {
+            ok = false;
+            break;
+        }
+        PFG_CUDA(c, cudaMemcpyAsync(T, x, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+        if (k.phase) {
+            heat_assemble<DIM>(c, k, tprev, T);
+            PFG_CHECK_LAUNCH(c);
+        }
+        k_heat_res<<<grid, BLOCK, 0, c->stream>>>(N, x, xprev, ptr<uint8_t>(c->flags), ptr<int>(c->nbr_ptr),
+                                                   ptr<int>(c->nbr), ptr<double>(c->heat_val),
+                                                   axf ? ptr<double>(c->heat_rhs) : nullptr, kp);
+        PFG_CHECK_LAUNCH(c);
+        PFG_CUDA(c, cudaMemcpyAsync(xprev, x, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+        PFG_CUDA(c, cudaMemcpyAsync(h, kp.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        res = axf ? std::sqrt(h[S_NUM]) : (h[S_DEN] == 0.0 ? DBL_MAX : std::sqrt(h[S_NUM] / h[S_DEN]));
+        ++it;
+        if (std::isnan(res)) {
+            ok = false;
+            break;
+        }
+        if (!k.phase) break;
+    }
+    st->converged = ok ? 1 : 0;
+    st->picard_iterations = it;
+    st->residual = res;
+    if (!ok) PFG_CUDA(c, cudaMemcpyAsync(T, tprev, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PFG_OK;
 }
@@ -515,7 +653,7 @@ int heat_alloc(pfg_ctx* c) {
     if ((rc = ensure(c, c->heat_t, sizeof(double) * N)) || (rc = ensure(c, c->heat_flags, N)) ||
         (rc = ensure(c, c->heat_tbc, sizeof(double) * N)) || (rc = ensure(c, c->heat_val, sizeof(double) * P)) ||
         (rc = ensure(c, c->heat_rhs, sizeof(double) * N)) ||
-        (rc = ensure(c, c->heat_cg, sizeof(double) * (V_COUNT + 1) * N)) ||
+        (rc = ensure(c, c->heat_cg, sizeof(double) * (V_COUNT + 3) * N)) ||
         (rc = ensure(c, c->heat_red, sizeof(double) * (2 * (size_t)std::max(c->max_grid, 1) + 64))) ||
         (rc = ensure(c, c->hf_ptr, sizeof(int) * (N + 1))))
         return rc;

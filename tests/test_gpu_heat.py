@@ -171,3 +171,53 @@ def test_boussinesq_coupled_steps_match_oracle(gpu_lib, c1_mesh):
         errs = [np.linalg.norm(q[f * N:(f + 1) * N] - qo[f * N:(f + 1) * N]) /
                 max(np.linalg.norm(qo[f * N:(f + 1) * N]), 1e-30) for f in range(d + 1)]
         assert max(errs) < 1e-8, (step, errs)
+
+
+TM, DTM, LM = 933.15, 20.0, 396000.0  # the reference's phase-change example (aluminium)
+
+
+@pytest.mark.parametrize("residual", [api.RES_T, api.RES_AX_F])
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_heat_phase_change_picard_matches_oracle(gpu_lib, which, residual, c1_mesh, small3d_mesh):
+    """HeatEqIncompNewton with phase change: Picard iterations on the latent-heat mass factor
+    (HeatEquation.inl:60-66, 131-138), same iteration counts as the oracle."""
+    mesh = c1_mesh if which == "c1" else small3d_mesh
+    N = mesh.n_nodes
+    kw = dict(heat_h=500.0, heat_t_inf=300.0, heat_fs_flags=api.HEAT_QH)
+    ctx = make_ctx(mesh, rho=2385.0, heat_cv=1080.0, heat_k=94.03, heat_phase_change=1, heat_tm=TM,
+                   heat_dt_melt=DTM, heat_lm=LM, heat_residual=residual, **kw)
+    t0 = np.full(N, TM + 5.0) + 2 * np.sin(3 * mesh.pos[0])
+    ctx.set_temperature(t0)
+    om = O.OracleMesh(mesh)
+    p = O.heat_params(2385.0, 1080.0, 94.03, h=500.0, t_inf=300.0, fs_flags=O.HT_QH, phase_change=(TM, DTM, LM))
+    fl = np.zeros(N, np.uint8)
+    to = t0.copy()
+    for step in range(2):
+        st = ctx.heat_step(1.0)
+        r = {}
+        to = O.heat_step(om, p, 1.0, to, fl, residual="T" if residual == api.RES_T else "Ax_f", result=r)
+        assert st.converged == 1 and r["converged"]
+        assert st.picard_iterations == r["iterations"] and st.picard_iterations >= 2
+        t = ctx.get_temperature()
+        assert np.abs(t - to).max() / np.abs(to).max() < 1e-10, step
+
+
+def test_heat_phase_change_failure_restores(gpu_lib, c1_mesh):
+    """A Picard loop that does not reach minRes in maxIter + 1 passes fails and restores the
+    temperatures, as PicardAlgo::solve does (PicardAlgo.cpp:52-61), like the oracle."""
+    mesh = c1_mesh
+    N = mesh.n_nodes
+    ctx = make_ctx(mesh, rho=2385.0, heat_cv=1080.0, heat_k=94.03, heat_phase_change=1, heat_tm=TM,
+                   heat_dt_melt=DTM, heat_lm=LM, heat_max_iter=1, heat_min_res=1e-14, heat_h=500.0,
+                   heat_t_inf=300.0, heat_fs_flags=api.HEAT_QH)
+    t0 = np.full(N, TM + 5.0) + 2 * np.sin(3 * mesh.pos[0])
+    ctx.set_temperature(t0)
+    st = ctx.heat_step(1.0)
+    om = O.OracleMesh(mesh)
+    r = {}
+    to = O.heat_step(om, O.heat_params(2385.0, 1080.0, 94.03, h=500.0, t_inf=300.0, fs_flags=O.HT_QH,
+                                       phase_change=(TM, DTM, LM)), 1.0, t0, np.zeros(N, np.uint8),
+                     max_iter=1, min_res=1e-14, result=r)
+    assert st.converged == 0 and not r["converged"]
+    assert st.picard_iterations == r["iterations"] == 2
+    assert np.array_equal(ctx.get_temperature(), t0) and np.array_equal(to, t0)

@@ -326,3 +326,30 @@ def test_uniform_temperature_surface_tension_equals_shifted_gamma():
                             apply_bc=True)
     assert np.abs(b0).max() > 0
     assert np.abs(b1 - b0).max() < 1e-13 * np.abs(b0).max()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_heat_phase_change_latent_heat(dim):
+    """Phase change (HeatEquation.inl:60-66): below the melting range the latent term is zero
+    and the Picard loop reproduces the single pass; inside it the latent heat slows the cooling
+    through the free surface (Qh)."""
+    m = _heat_mesh(dim)
+    om = O.OracleMesh(m)
+    N = m.n_nodes
+    fl = np.zeros(N, np.uint8)
+    tm, dtm, lm = 933.15, 20.0, 396000.0
+    kw = dict(h=500.0, t_inf=300.0, fs_flags=O.HT_QH)
+    plain = O.heat_params(2385.0, 1080.0, 94.03, **kw)
+    latent = O.heat_params(2385.0, 1080.0, 94.03, phase_change=(tm, dtm, lm), **kw)
+    # without facet terms (they read the iterate) the rebuilt system equals the first one
+    cold = np.full(N, 500.0) + 2 * np.sin(3 * m.pos[0])
+    r = {}
+    t_pc = O.heat_step(om, O.heat_params(2385.0, 1080.0, 94.03, phase_change=(tm, dtm, lm)), 1.0, cold, fl, result=r)
+    assert r["converged"] and r["iterations"] == 2
+    assert np.abs(t_pc - O.heat_step(om, O.heat_params(2385.0, 1080.0, 94.03), 1.0, cold, fl)).max() < 1e-12 * 500
+    melt = np.full(N, tm + 5.0) + 2 * np.sin(3 * m.pos[0])
+    r = {}
+    t_pc = O.heat_step(om, latent, 1.0, melt, fl, result=r)
+    t_pl = O.heat_step(om, plain, 1.0, melt, fl)
+    assert r["converged"] and r["iterations"] >= 3
+    assert np.abs(t_pc - melt).max() < 0.1 * np.abs(t_pl - melt).max()
