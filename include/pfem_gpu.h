@@ -200,6 +200,13 @@ PFG_API const char* pfg_last_error(const pfg_ctx* ctx);   /* never NULL */
  * Node states are reset to zero; set them with pfg_set_states afterwards. */
 PFG_API int pfg_upload_mesh(pfg_ctx* ctx, int32_t n_nodes, const double* pos, const uint8_t* flags,
                             int32_t n_elems, const int32_t* conn);
+/* pfg_upload_mesh keeping the node states on the device (incompressible contexts): new node j
+ * takes the states (and temperature) of origin[j*width + 0], or the mean of the valid entries
+ * origin[j*width + k] (-1 padded; the centroid node Mesh::addNodes creates takes the mean of its
+ * element's nodes, Mesh.cpp:59-67).  The table comes from the host remesh; the states never
+ * cross to the host.  width <= 4. */
+PFG_API int pfg_upload_mesh_remap(pfg_ctx* ctx, int32_t n_nodes, const double* pos, const uint8_t* flags,
+                                  int32_t n_elems, const int32_t* conn, const int32_t* origin, int32_t width);
 
 /* The boundary facets of the uploaded mesh (Mesh::m_facetsList, built by the alpha shape in
  * Mesh2D.cpp:199-244 / Mesh3D.cpp:232-282): facets[k*F + f] (k < dim) are the nodes of facet

@@ -38,7 +38,7 @@ EXPORTED = (
     "pfg_get_phase_times", "pfg_reset_phase_times", "pfg_phase_name", "pfg_wc_step_async", "pfg_synchronize",
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
     "pfg_upload_facets", "pfg_set_positions", "pfg_get_spmv_pairs", "pfg_set_temperature",
-    "pfg_get_temperature", "pfg_heat_set_bc", "pfg_heat_set_flux", "pfg_heat_step",
+    "pfg_get_temperature", "pfg_heat_set_bc", "pfg_heat_set_flux", "pfg_heat_step", "pfg_upload_mesh_remap",
 )
 NUM_PHASES = 15
 
@@ -123,6 +123,7 @@ def load(path=LIB_PATH):
         "pfg_reset_phase_times": ([vp], C.c_int),
         "pfg_get_spmv_pairs": ([vp, i64p], C.c_int),
         "pfg_set_temperature": ([vp, dp], C.c_int),
+        "pfg_upload_mesh_remap": ([vp, C.c_int32, dp, u8p, C.c_int32, ip, ip, C.c_int32], C.c_int),
         "pfg_get_temperature": ([vp, dp], C.c_int),
         "pfg_heat_set_bc": ([vp, u8p, dp], C.c_int),
         "pfg_heat_set_flux": ([vp, dp], C.c_int),
@@ -201,6 +202,23 @@ class Context:
         self._check(self.L.pfg_upload_mesh(self.h, pos.shape[1], _dp(pos), flags.ctypes.data_as(C.POINTER(C.c_uint8)),
                                            conn.shape[1], conn.ctypes.data_as(C.POINTER(C.c_int32))),
                     "pfg_upload_mesh")
+        self.N, self.E = pos.shape[1], conn.shape[1]
+        facets = getattr(mesh, "facets", None)
+        if facets is not None and facets.shape[1]:
+            self.upload_facets(facets, mesh.facet_elm)
+
+    def upload_mesh_remap(self, mesh, origin):
+        """Upload a remeshed domain keeping the node states (and temperatures) on the device:
+        origin (N_new, w) from `remesh.remesh_map`."""
+        pos = np.ascontiguousarray(mesh.pos, np.float64)
+        flags = np.ascontiguousarray(mesh.flags, np.uint8)
+        conn = np.ascontiguousarray(mesh.conn, np.int32)
+        org = np.ascontiguousarray(origin, np.int32)
+        assert org.ndim == 2 and org.shape[0] == pos.shape[1]
+        self._check(self.L.pfg_upload_mesh_remap(self.h, pos.shape[1], _dp(pos),
+                                                 flags.ctypes.data_as(C.POINTER(C.c_uint8)), conn.shape[1],
+                                                 conn.ctypes.data_as(C.POINTER(C.c_int32)), _ip(org), org.shape[1]),
+                    "pfg_upload_mesh_remap")
         self.N, self.E = pos.shape[1], conn.shape[1]
         facets = getattr(mesh, "facets", None)
         if facets is not None and facets.shape[1]:

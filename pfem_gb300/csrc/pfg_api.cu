@@ -391,6 +391,71 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
     return PFG_OK;
 }
 
+namespace {
+// New node states from the old ones: a copy for one source, the mean in source order for
+// several (the centroid node of Mesh::addNodes, Mesh.cpp:59-67).  One thread per (field, node).
+__global__ void k_remap(int n_new, int nf, int n_old, const double* __restrict__ old, const int* __restrict__ origin,
+                        int width, double* __restrict__ out) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)n_new * nf) return;
+    const int f = (int)(t / n_new), j = (int)(t % n_new);
+    const int* o = origin + (size_t)j * width;
+    double s = old[(size_t)f * n_old + o[0]];
+    int cnt = 1;
+    for (int k = 1; k < width && o[k] >= 0; ++k, ++cnt) s += old[(size_t)f * n_old + o[k]];
+    out[(size_t)f * n_new + j] = cnt > 1 ? s / cnt : s;
+}
+}  // namespace
+
+PFG_API int pfg_upload_mesh_remap(pfg_ctx* c, int32_t n_nodes, const double* pos, const uint8_t* flags,
+                                  int32_t n_elems, const int32_t* conn, const int32_t* origin, int32_t width) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG)
+        return fail(c, PFG_ERR_UNSUPPORTED, "pfg_upload_mesh_remap: incompressible contexts only");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "pfg_upload_mesh_remap: no previous mesh");
+    if (!origin || width < 1 || width > 4 || n_nodes <= 0)
+        return fail(c, PFG_ERR_INVALID, "pfg_upload_mesh_remap: invalid origin table");
+    const int n_old = c->N, nf = c->dim + 1;
+    for (int j = 0; j < n_nodes; ++j)
+        for (int k = 0; k < width; ++k) {
+            const int v = origin[(size_t)j * width + k];
+            if ((k == 0 && (v < 0 || v >= n_old)) || v >= n_old || (k > 0 && v < -1))
+                return fail(c, PFG_ERR_INVALID, "origin of node %d: %d out of range", j, v);
+        }
+    // the old states (and temperatures) survive the upload in a scratch buffer
+    const bool heat = c->heat_ready;
+    const size_t old_n = (size_t)(nf + (heat ? 1 : 0)) * n_old;
+    DBuf keep{}, org{};
+    auto done = [&](int r) {
+        cudaStreamSynchronize(c->stream);
+        c->bytes_in_use -= keep.cap + org.cap;
+        release(keep);
+        release(org);
+        return r;
+    };
+    if ((rc = ensure(c, keep, sizeof(double) * old_n)) ||
+        (rc = ensure(c, org, sizeof(int) * (size_t)n_nodes * width)))
+        return done(rc);
+    if (cudaMemcpyAsync(keep.p, c->q.p, sizeof(double) * nf * n_old, cudaMemcpyDeviceToDevice, c->stream) ||
+        (heat && cudaMemcpyAsync(ptr<double>(keep) + (size_t)nf * n_old, c->heat_t.p, sizeof(double) * n_old,
+                                 cudaMemcpyDeviceToDevice, c->stream)) ||
+        cudaMemcpyAsync(org.p, origin, sizeof(int) * (size_t)n_nodes * width, cudaMemcpyHostToDevice, c->stream))
+        return done(fail(c, PFG_ERR_CUDA, "pfg_upload_mesh_remap: copy failed"));
+    if ((rc = pfg_upload_mesh(c, n_nodes, pos, flags, n_elems, conn))) return done(rc);
+    const long long nt = (long long)n_nodes * nf;
+    k_remap<<<div_up(nt, BLOCK), BLOCK, 0, c->stream>>>(n_nodes, nf, n_old, ptr<double>(keep), ptr<int>(org), width,
+                                                        ptr<double>(c->q));
+    if (heat) {
+        if ((rc = heat_alloc(c))) return done(rc);
+        k_remap<<<div_up(n_nodes, BLOCK), BLOCK, 0, c->stream>>>(n_nodes, 1, n_old, ptr<double>(keep) + (size_t)nf * n_old,
+                                                                 ptr<int>(org), width, ptr<double>(c->heat_t));
+    }
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return done(fail(c, PFG_ERR_CUDA, "pfg_upload_mesh_remap: remap failed"));
+    return done(PFG_OK);
+}
+
 PFG_API int pfg_upload_facets(pfg_ctx* c, int32_t n_facets, const int32_t* facets, const int32_t* facet_elm) {
     int rc = check_ctx(c);
     if (rc) return rc;

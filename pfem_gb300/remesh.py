@@ -169,6 +169,56 @@ def check_bounding_box(pos, bbox, dim):
     return ((pos >= lo) & (pos <= hi)).all(axis=0)
 
 
+def remesh_map(mesh, params: RemeshParams):
+    """One `Mesh::remesh` of `mesh` (positions already moved) without the states: returns the new
+    HostMesh and, per new node, the old nodes its states come from, (n_new, dim + 1) int32 padded
+    with -1: one old node for a node that survived, the element's dim + 1 nodes for a node added
+    at a centroid (their mean, `Mesh.cpp:59-67`).  `pfg_upload_mesh_remap` applies it on the
+    device; `apply_origin` on the host."""
+    d = mesh.dim
+    N = mesh.n_nodes
+    pos = mesh.pos.copy()
+    if params.laplacian_smoothing_boundaries:
+        laplacian_smoothing_boundaries(mesh, pos)
+    ident = np.full((N, d + 1), -1, np.int32)
+    ident[:, 0] = np.arange(N)
+    # add_nodes with the "state" of a node being its own index row
+    pos2, flags, _ = add_nodes(mesh, pos, np.zeros(N), params)
+    n_add = pos2.shape[1] - N
+    origin = ident
+    if n_add:
+        X = pos[:, mesh.conn]
+        J = X[:, 1:, :] - X[:, :1, :]
+        size = np.linalg.det(np.moveaxis(J, 2, 0)) * (0.5 if d == 2 else 1.0 / 6.0)
+        fs = (mesh.flags & M.FREE_SURFACE) != 0
+        grow = size > params.omega * params.hchar ** d
+        if not params.add_on_fs:
+            grow &= ~fs[mesh.conn].any(axis=0)
+        sel = np.nonzero(grow)[0]
+        assert sel.size == n_add
+        origin = np.concatenate([ident, mesh.conn[:, sel].T.astype(np.int32)])
+    keep = np.ones(pos2.shape[1], bool)
+    keep[:N] = remove_nodes(mesh, pos2, flags, params)
+    keep &= check_bounding_box(pos2, params.bounding_box, d)
+    idx = np.nonzero(keep)[0]
+    new = M.alpha_shape(pos2[:, idx], flags[idx], params.hchar, params.alpha,
+                        delete_flying_nodes=params.delete_flying_nodes)
+    return new, np.ascontiguousarray(origin[idx][new.node_origin])
+
+
+def apply_origin(states, origin, n_old):
+    """Field-major states of the new nodes from an origin table of `remesh_map`: a copy for one
+    source, the mean in source order for dim + 1 sources (as numpy's mean in `add_nodes`)."""
+    S = np.asarray(states, float).reshape(-1, n_old)
+    single = origin[:, 1] < 0
+    out = np.empty((S.shape[0], origin.shape[0]))
+    out[:, single] = S[:, origin[single, 0]]
+    multi = ~single
+    if multi.any():
+        out[:, multi] = S[:, origin[multi]].mean(axis=2)
+    return out.ravel()
+
+
 def remesh(mesh, states, params: RemeshParams):
     """One `Mesh::remesh` of `mesh` (positions already moved) carrying the field-major node
     `states` along.  Returns (new HostMesh, new states)."""

@@ -116,20 +116,18 @@ class SolverIncompNewtonGPU(_SolverBase):
         return self.ctx.get_temperature()
 
     def remesh(self):
-        """`Mesh::remesh` with the temperature travelling as one more node state."""
+        """`Mesh::remesh` on the host (positions and flags only); the node states and
+        temperatures are remapped on the device from the new nodes' origins
+        (`pfg_upload_mesh_remap`), so they never cross to the host."""
         if self.remesh_params is None:
             return
-        if self._t0 is None:
-            return super().remesh()
         cur = self.mesh.copy()
         cur.pos = self.ctx.get_positions()
         cur.flags = self.ctx.get_flags() & np.uint8(0x0F)
-        R = (self.mesh.dim + 1) * self.mesh.n_nodes
-        st = np.concatenate([self.ctx.get_states(), self.ctx.get_temperature()])
-        new, st2 = RM.remesh(cur, st, self.remesh_params)
-        R2 = (new.dim + 1) * new.n_nodes
-        assert st2.size == R2 + new.n_nodes and R > 0
-        self._upload(new, st2[:R2], st2[R2:])
+        new, origin = RM.remesh_map(cur, self.remesh_params)
+        self.mesh = new
+        self.ctx.upload_mesh_remap(new, origin)
+        self._apply_dirichlet()
 
     def _heat(self):
         """`HeatEqIncompNewton::solve` with the BCs evaluated at t + dt on the current positions."""
