@@ -50,11 +50,12 @@ def parse_args():
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["wc-c2", "incomp-c1", "incomp-c3", "batch-c4", "serve-c5"],
+    ap.add_argument("--workload", choices=["wc-c2", "incomp-c1", "incomp-c3", "batch-c4", "serve-c5", "heat-c3"],
                     default="wc-c2",
                     help="wc-c2 (default): the headline WC dam break; incomp-c1 / incomp-c3: PSPG Picard "
                          "steps on the 2D / 3D dam break; batch-c4: 256 independent 2D instances; "
-                         "serve-c5: a Poisson stream of requests served under an HBM budget")
+                         "serve-c5: a Poisson stream of requests served under an HBM budget; heat-c3: "
+                         "heat-equation steps (problem Conduction) on the 3D dam-break mesh")
     ap.add_argument("--instances", type=int, default=256, help="batch-c4: number of instances")
     ap.add_argument("--h", type=float, default=None,
                     help="incomp-c1 / incomp-c3: node spacing (default 0.05 / 0.01); smaller cases for profiling")
@@ -435,6 +436,16 @@ def pattern_nnz(mesh):
     return M.pspg_nnz(mesh)
 
 
+def node_pairs(mesh):
+    """Node pairs sharing an element, each node with itself included: the scalar pattern."""
+    import numpy as np
+    import scipy.sparse as sp
+
+    d, N, E = mesh.dim, mesh.n_nodes, mesh.n_elems
+    inc = sp.csr_matrix((np.ones(E * (d + 1)), (np.repeat(np.arange(E), d + 1), mesh.conn.T.ravel())), shape=(E, N))
+    return int((inc.T @ inc).tocsr().nnz)
+
+
 def spmv_bytes(nnz, R, s):
     """One SpMV: values + column indices, row pointers, input and output vectors."""
     return nnz * (s + 4) + (R + 1) * 4 + 2 * R * s
@@ -519,6 +530,8 @@ def run_gpu_incomp(args):
     from pfem_gb300 import workloads as WL
 
     build.build()
+    if args.workload == "heat-c3":
+        return run_gpu_heat(args)
     if args.workload == "batch-c4":
         return run_gpu_batch(args)
     if args.workload == "serve-c5":
@@ -670,6 +683,149 @@ def run_gpu_incomp(args):
             "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": int(round(sum(v[1] for k, v in phases.items() if k != "Krylov SpMV") / Kp * K)),
             "err_vs_fp64_gpu": acc_vs_fp64, "err_vs_oracle": acc_vs_oracle,
+        }
+        print(json.dumps(out))
+    return 0
+
+
+# Heat equation (problem "Conduction", HeatEqIncompNewton) on the C3 mesh with the material,
+# time step and wall temperature of the reference's conduction example (conductionIncomp.lua:
+# rho 1, k 237, cv 1000, initialDT 0.025, walls at T = 10) and a Gaussian initial temperature.
+HEAT = dict(metric="heat steps/s (3D conduction on the dam-break mesh, HeatEqIncompNewton step)", unit="steps/s",
+            name="3D conduction on the C3 mesh (h = 0.01)", dt=0.025, max_steps=100, max_warmup=3,
+            rho=1.0, k=237.0, cv=1000.0, t_wall=10.0, cpu_h=0.03)
+
+
+def heat_setup(mesh):
+    import numpy as np
+    from pfem_gb300 import mesh as M
+
+    bound = (mesh.flags & M.BOUND) != 0
+    flags = np.where(bound, 1, 0).astype(np.uint8)   # PFG_HEAT_T on the walls
+    tbc = np.where(bound, HEAT["t_wall"], 0.0)
+    x = mesh.pos
+    t0 = 10.0 * np.exp(-((x[0] - 0.3) ** 2 + (x[1] - 0.3) ** 2 + (x[2] - 0.2) ** 2) / 0.05)
+    return flags, tbc, t0
+
+
+def heat_oracle_sample(seconds):
+    """Oracle heat steps (C++ assembly, SuperLU) on a coarser mesh of the same domain: the
+    C3 mesh's one LU step does not fit a bounded sample.  Returns (node-steps/s, sample)."""
+    from oracle import oracle as O
+    from pfem_gb300 import mesh as M
+
+    O.build()
+    m = M.dam_break_3d(HEAT["cpu_h"])
+    flags, tbc, t = heat_setup(m)
+    om = O.OracleMesh(m)
+    p = O.heat_params(HEAT["rho"], HEAT["cv"], HEAT["k"])
+    t0 = time.perf_counter()
+    n = 0
+    while n < 1 or (time.perf_counter() - t0 < seconds and n < 50):
+        t = O.heat_step(om, p, HEAT["dt"], t, flags, tbc)
+        n += 1
+    el = time.perf_counter() - t0
+    return m.n_nodes * n / el, (f"{n} oracle heat steps on the same domain at h = {HEAT['cpu_h']} ({m.n_nodes} nodes, "
+                                f"{el:.1f} s), scaled to the C3 mesh by node count (LU cost grows faster: "
+                                f"favours the CPU)"), O.num_threads()
+
+
+def run_gpu_heat(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    from pfem_gb300 import api, build
+    from pfem_gb300 import mesh as M
+    from pfem_gb300 import workloads as WL
+
+    build.build()
+    mesh = WL.c3() if args.h is None else M.dam_break_3d(args.h)
+    N = mesh.n_nodes
+    flags, tbc, t0 = heat_setup(mesh)
+    p = api.default_params(api.KIND_INCOMP_PSPG, 3)
+    p.rho, p.heat_k, p.heat_cv = HEAT["rho"], HEAT["k"], HEAT["cv"]
+    ctx = api.Context(p)
+    ctx.upload_mesh(mesh)
+    ctx.set_temperature(t0)
+    ctx.heat_set_bc(flags, tbc)
+    dt = HEAT["dt"]
+    K = max(1, min(args.steps, HEAT["max_steps"]))
+    Wm = max(3, min(args.warmup, HEAT["max_warmup"]))
+    ext = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MB > 129 MB L2
+    for _ in range(Wm):
+        ctx.heat_step(dt)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = ClockSampler(local)
+    conv, iters = 0, 0
+    torch.cuda.synchronize()
+    clocks.start()
+    with torch.cuda.stream(ext):
+        for k in range(K):
+            flush.fill_(k & 0xFF)
+            ev[k][0].record(ext)
+            st = ctx.heat_step(dt)
+            ev[k][1].record(ext)
+            conv += st.converged
+            iters += st.krylov_iterations
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if conv != K:
+        raise RuntimeError(f"{K - conv} of {K} timed heat steps did not converge")
+
+    # phases on a few more steps: assembly and the CG products
+    Kp = min(K, 5)
+    ctx.set_profiling(True)
+    ctx.reset_phase_times()
+    it_p = 0
+    for _ in range(Kp):
+        it_p += ctx.heat_step(dt).krylov_iterations
+    phases = ctx.phase_times()
+    ctx.set_profiling(False)
+    P = node_pairs(mesh)                            # node pairs (diagonal included)
+    spmv_b = P * (8 + 4) + (N + 1) * 4 + 2 * N * 8   # values + columns, row pointers, p in, Ap out
+    spmv_ms, spmv_n = phases.get("Heat CG SpMV", (0.0, 0))
+    peak, peak_kind = hbm_peak()
+    achieved = spmv_b * it_p / (spmv_ms / 1e3) / 1e9 if spmv_ms else None
+    roof = {"bound": "hbm", "kernel": "Heat CG SpMV", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "traffic": None, "algorithmic_bytes": spmv_b,
+            "avg_launch_us": 1e3 * spmv_ms / max(it_p, 1), "peak_kind": peak_kind,
+            "note": "time of all SpMV launches (including the no-op tail of the last 8-iteration chunk) "
+                    "over the iterations run"}
+
+    # end to end through the C ABI: temperatures in from pinned host memory, out after the step
+    h_t = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    h_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    h_t[:] = ctx.get_temperature()
+    Ke = min(K, 20)
+    t1 = time.perf_counter()
+    for _ in range(Ke):
+        ctx.set_temperature(h_t)
+        ctx.heat_step(dt)
+        ctx.get_temperature(out=h_o)
+    e2e_s = time.perf_counter() - t1
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        nps, sample, cores = heat_oracle_sample(args.cpu_sample_seconds)
+        cpu = {"value": nps / N, "unit": HEAT["unit"], "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        out = {
+            "metric": HEAT["metric"], "value": K / (total_ms / 1e3), "unit": HEAT["unit"], "n_gpus": world,
+            "steps": K, "warmup": Wm, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice)",
+            "config": {"workload": HEAT["name"], "nodes": N, "elements": int(mesh.n_elems), "node_pairs": P,
+                       "dt": dt, "material": "rho 1, k 237, cv 1000 (conduction example)",
+                       "linear_solver": "FP64 Jacobi CG, ||r|| <= max(1e-14 ||b||, 1e-10)",
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas only"},
+            "step_stats": {"converged": conv, "cg_iterations": iters},
+            "roofline": roof, "phases_ms_per_step": {k: v[0] / Kp for k, v in phases.items()},
+            "cpu_baseline": cpu, "clocks": clk,
+            "e2e": {"value": Ke / e2e_s, "unit": HEAT["unit"], "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N},
+            "gpu_launches": int(round(sum(v[1] for v in phases.values()) / Kp * K)),
         }
         print(json.dumps(out))
     return 0
@@ -913,6 +1069,21 @@ def run_reference_incomp(args):
     from pfem_gb300 import workloads as WL
 
     O.build()
+    if args.workload == "heat-c3":
+        from pfem_gb300 import workloads as WL2
+
+        nps, sample, cores = heat_oracle_sample(args.cpu_sample_seconds)
+        n_c3 = WL2.c3().n_nodes
+        v = nps / n_c3
+        out = {"impl": "reference", "metric": HEAT["metric"], "value": v, "unit": HEAT["unit"], "n_gpus": args.gpus,
+               "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice)",
+               "config": {"workload": HEAT["name"]},
+               "cpu_baseline": {"value": v, "unit": HEAT["unit"], "cores": cores, "kind": "port", "sample": sample},
+               "e2e": {"value": v, "unit": HEAT["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "gpu_launches": 0}
+        print(json.dumps(out))
+        return 0
     if args.workload == "serve-c5":
         cfg = {"metric": "aggregate time-steps/s of a served request mix (C5), with p50/p99 request latency",
                "unit": "steps/s", "name": "served mix (C5)"}

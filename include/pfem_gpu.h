@@ -329,8 +329,9 @@ PFG_API int pfg_linear_solve(pfg_ctx* ctx, double* x, int32_t* iterations, doubl
  *   9 Krylov iteration     10 Picard residual        11 position update
  *  12 Krylov SpMV (the two products of an iteration, also inside phase 9)
  *  13 Multigrid cycle (the preconditioner applies of an iteration, also inside phase 9)
- *  14 Multigrid setup (coarse values and block inverses after each assembly)        */
-#define PFG_NUM_PHASES 15
+ *  14 Multigrid setup (coarse values and block inverses after each assembly)
+ *  15 Heat assembly        16 Heat CG SpMV (the product of each conjugate-gradient step) */
+#define PFG_NUM_PHASES 17
 PFG_API int pfg_set_profiling(pfg_ctx* ctx, int32_t enable);
 /* Accumulated milliseconds and launch counts per phase since the last reset. */
 PFG_API int pfg_get_phase_times(pfg_ctx* ctx, double* ms, int64_t* launches);

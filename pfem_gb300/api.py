@@ -40,7 +40,7 @@ EXPORTED = (
     "pfg_upload_facets", "pfg_set_positions", "pfg_get_spmv_pairs", "pfg_set_temperature",
     "pfg_get_temperature", "pfg_heat_set_bc", "pfg_heat_set_flux", "pfg_heat_step", "pfg_upload_mesh_remap",
 )
-NUM_PHASES = 15
+NUM_PHASES = 17
 
 
 class Params(C.Structure):

@@ -190,7 +190,8 @@ PFG_API const char* pfg_phase_name(int32_t phase) {
     static const char* names[PFG_NUM_PHASES] = {
         "WC predict", "WC continuity element", "WC continuity node", "WC momentum element", "WC momentum node",
         "WC time step", "PSPG element prep", "PSPG right-hand side", "PSPG matrix", "Krylov iteration",
-        "Picard residual", "Position update", "Krylov SpMV", "Multigrid cycle", "Multigrid setup"};
+        "Picard residual", "Position update", "Krylov SpMV", "Multigrid cycle", "Multigrid setup",
+        "Heat assembly", "Heat CG SpMV"};
     return (phase >= 0 && phase < PFG_NUM_PHASES) ? names[phase] : "";
 }
 

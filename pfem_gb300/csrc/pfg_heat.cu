@@ -395,12 +395,14 @@ __device__ __forceinline__ bool grid_sum2(double a, double b, double* partials, 
     return true;
 }
 
-// r = b - A x, z = r / diag, p = z; rz = r.z; tolerance from ||b||.  An exact start still runs
-// one iteration (alpha = 0), which finds ||r|| <= tol.
+// r = b - A x, z = r / diag, p = z; rz = r.z; tolerance max(rtol ||b||, atol), capped at
+// max(cap, 2e-16 ||b||) (the heat Picard loop with an absolute "Ax_f" residual needs the linear
+// solve below its minRes, down to the rounding level an LU solve reaches).  An exact start still
+// runs one iteration (alpha = 0), which finds ||r|| <= tol.
 __global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict__ rp, const int* __restrict__ col,
                                                    const double* __restrict__ val, const double* __restrict__ b,
                                                    const double* __restrict__ x, double* __restrict__ V, size_t ld,
-                                                   CgPtrs k, double rtol, double atol) {
+                                                   CgPtrs k, double rtol, double atol, double cap) {
     __shared__ double sh[32];
     double rz = 0, bb = 0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict_
     if (grid_sum2<BLOCK>(rz, bb, k.partials, k.ticket, sh, s1, s2) && threadIdx.x == 0) {
         k.sc[S_RZ] = s1;
         k.sc[S_BB] = s2;
-        const double tol = fmax(rtol * sqrt(s2), atol);
+        const double tol = fmin(fmax(rtol * sqrt(s2), atol), fmax(cap, 2e-16 * sqrt(s2)));
         k.sc[S_TOL2] = tol * tol;
         k.sc[S_ITERS] = 0;
         k.sc[S_DONE] = 0;
@@ -519,6 +521,7 @@ __global__ void __launch_bounds__(BLOCK) k_heat_res(int N, const double* __restr
 template <int DIM>
 void heat_assemble(pfg_ctx* c, const HeatConst& k, const double* tprev, const double* ts) {
     const int N = c->N, E = c->E;
+    prof_begin(c, PH_HEAT_ASSEMBLY);
     if (E > 0)
         k_heat_geom<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
                                                                     ptr<double>(c->edata));
@@ -540,11 +543,12 @@ void heat_assemble(pfg_ctx* c, const HeatConst& k, const double* tprev, const do
         ptr<double>(c->edata), ptr<double>(c->pos), ptr<uint8_t>(c->flags), ptr<uint8_t>(c->heat_flags), tprev, ts,
         ptr<double>(c->heat_tbc), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<double>(c->heat_val), hf, k,
         ptr<double>(c->heat_rhs));
+    prof_end(c, PH_HEAT_ASSEMBLY);
 }
 
 // CG solve of the assembled system from x0 = T_prev (solveWithGuess, :126) into x.  Returns
 // the convergence flag; iterations and the last recursive residual accumulate in st.
-int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, bool* ok) {
+int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, bool* ok, double cap) {
     const int N = c->N;
     double* V = ptr<double>(c->heat_cg);
     const size_t ld = (size_t)std::max(N, 1);
@@ -555,7 +559,7 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
     const int* col = ptr<int>(c->nbr);
     const double* val = ptr<double>(c->heat_val);
     k_cg_init<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, ptr<double>(c->heat_rhs), x, V, ld, kp,
-                                             c->prm.krylov_rel_tol, c->prm.krylov_abs_tol);
+                                             c->prm.krylov_rel_tol, c->prm.krylov_abs_tol, cap);
     PFG_CHECK_LAUNCH(c);
     const int max_it = std::max(1, c->prm.krylov_max_iter);
     double* h = c->h_scalars;
@@ -563,7 +567,9 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
     while (done_it < max_it) {
         const int n = std::min(8, max_it - done_it);
         for (int it = 0; it < n; ++it) {
+            prof_begin(c, PH_HEAT_SPMV);
             k_cg_spmv<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
+            prof_end(c, PH_HEAT_SPMV);
             k_cg_update<<<grid, BLOCK, 0, c->stream>>>(N, x, V, ld, kp, max_it);
             k_cg_p<<<grid, BLOCK, 0, c->stream>>>(N, V, ld, kp);
         }
@@ -611,7 +617,7 @@ int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
             break;
         }
         bool solved = false;
-        int rc = heat_cg(c, tprev, x, st, &solved);
+        int rc = heat_cg(c, tprev, x, st, &solved, axf ? 0.1 * c->prm.heat_min_res : INFINITY);
         if (rc) return rc;
         if (!solved) {
             ok = false;

@@ -193,7 +193,9 @@ enum Phase : int {
     PH_POSITIONS,
     PH_KRYLOV_SPMV,
     PH_MG_CYCLE,
-    PH_MG_SETUP
+    PH_MG_SETUP,
+    PH_HEAT_ASSEMBLY,
+    PH_HEAT_SPMV
 };
 void prof_begin(pfg_ctx* c, int phase);
 void prof_end(pfg_ctx* c, int phase);
