@@ -757,6 +757,9 @@ def run_gpu_heat(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MB > 129 MB L2
     for _ in range(Wm):
         ctx.heat_step(dt)
+    # every timed step starts from the state after the warm-up: consecutive steps would relax
+    # to the steady state, where the CG needs a single iteration
+    t_w = ctx.get_temperature()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     clocks = ClockSampler(local)
     conv, iters = 0, 0
@@ -764,6 +767,7 @@ def run_gpu_heat(args):
     clocks.start()
     with torch.cuda.stream(ext):
         for k in range(K):
+            ctx.set_temperature(t_w)
             flush.fill_(k & 0xFF)
             ev[k][0].record(ext)
             st = ctx.heat_step(dt)
@@ -782,6 +786,7 @@ def run_gpu_heat(args):
     ctx.reset_phase_times()
     it_p = 0
     for _ in range(Kp):
+        ctx.set_temperature(t_w)
         it_p += ctx.heat_step(dt).krylov_iterations
     phases = ctx.phase_times()
     ctx.set_profiling(False)
@@ -799,7 +804,7 @@ def run_gpu_heat(args):
     # end to end through the C ABI: temperatures in from pinned host memory, out after the step
     h_t = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
     h_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
-    h_t[:] = ctx.get_temperature()
+    h_t[:] = t_w
     Ke = min(K, 20)
     t1 = time.perf_counter()
     for _ in range(Ke):

@@ -520,6 +520,7 @@ PFG_API int pfg_upload_facets(pfg_ctx* c, int32_t n_facets, const int32_t* facet
     c->h_facets.assign(facets, facets + (size_t)dim * F);
     c->h_facet_elm.assign(facet_elm, facet_elm + F);
     c->has_heat_q = false;  // flux vectors are per facet: a new facet list needs new ones
+    c->heat_facets_dirty = true;
     // captured WC step graphs hold the previous facet arguments
     if (c->prm.kind == PFG_KIND_WC_CDS_DPDT) wc_release_graphs(c);
     return PFG_OK;
@@ -572,6 +573,7 @@ PFG_API int pfg_heat_set_bc(pfg_ctx* c, const uint8_t* flags, const double* t_di
     }
     if (any_t && !t_dirichlet) return fail(c, PFG_ERR_INVALID, "Dirichlet heat nodes need t_dirichlet");
     c->h_heat_flags.assign(flags, flags + N);
+    c->heat_facets_dirty = true;
     PFG_CUDA(c, cudaMemcpyAsync(c->heat_flags.p, flags, N, cudaMemcpyHostToDevice, c->stream));
     if (t_dirichlet)
         PFG_CUDA(c, cudaMemcpyAsync(c->heat_tbc.p, t_dirichlet, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
@@ -583,6 +585,7 @@ PFG_API int pfg_heat_set_bc(pfg_ctx* c, const uint8_t* flags, const double* t_di
 PFG_API int pfg_heat_set_flux(pfg_ctx* c, const double* q_gp) {
     int rc = check_heat(c);
     if (rc) return rc;
+    c->heat_facets_dirty = true;  // the Q requirement is checked with the lists
     if (!q_gp) {
         c->has_heat_q = false;
         return PFG_OK;

@@ -432,19 +432,34 @@ __global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict_
     }
 }
 
-// q = A p, alpha = rz / (p . q)
+// q = A p, alpha = rz / (p . q).  G lanes per row (4 in 2D, 8 in 3D: about one entry per lane)
+// so a row's values and columns are read by adjacent lanes; the group's sum is a shuffle
+// reduction in a fixed order, so the result does not depend on the launch shape.
+template <int G>
 __global__ void __launch_bounds__(BLOCK) k_cg_spmv(int N, const int* __restrict__ rp, const int* __restrict__ col,
                                                    const double* __restrict__ val, double* __restrict__ V, size_t ld,
                                                    CgPtrs k) {
     __shared__ double sh[32];
     if (k.sc[S_DONE] != 0.0) return;
     const double* p = V + V_P * ld;
+    const int lane = threadIdx.x % G;
+    constexpr int GPW = 32 / G;  // rows per warp and trip
+    const int wglob = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int nwarps = gridDim.x * blockDim.x / 32;
     double pq = 0;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+    // all lanes of a warp share r0, so they run the same trips (the shuffles need the warp)
+    for (int r0 = wglob * GPW; r0 < N; r0 += nwarps * GPW) {
+        const int r = r0 + (threadIdx.x & 31) / G;
+        const bool act = r < N;
+        const int b = act ? rp[r] : 0, e = act ? rp[r + 1] : 0;
         double s = 0;
-        for (int t = rp[n]; t < rp[n + 1]; ++t) s += val[t] * p[col[t]];
-        V[V_Q * ld + n] = s;
-        pq += p[n] * s;
+        for (int t = b + lane; t < e; t += G) s += val[t] * p[col[t]];
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+        if (act && lane == 0) {
+            V[V_Q * ld + r] = s;
+            pq += p[r] * s;
+        }
     }
     double a, unused;
     if (grid_sum2<BLOCK>(pq, 0.0, k.partials, k.ticket, sh, a, unused) && threadIdx.x == 0) {
@@ -555,6 +570,7 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
     PFG_CUDA(c, cudaMemcpyAsync(x, tprev, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     const CgPtrs kp = cg_ptrs(c);
     const int grid = std::max(1, std::min(c->max_grid, div_up(N, BLOCK)));
+    const int grid_rows = std::max(1, std::min(c->max_grid, div_up((long long)N * (c->dim == 2 ? 4 : 8), BLOCK)));
     const int* rp = ptr<int>(c->nbr_ptr);
     const int* col = ptr<int>(c->nbr);
     const double* val = ptr<double>(c->heat_val);
@@ -568,7 +584,10 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
         const int n = std::min(8, max_it - done_it);
         for (int it = 0; it < n; ++it) {
             prof_begin(c, PH_HEAT_SPMV);
-            k_cg_spmv<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
+            if (c->dim == 2)
+                k_cg_spmv<4><<<grid_rows, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
+            else
+                k_cg_spmv<8><<<grid_rows, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
             prof_end(c, PH_HEAT_SPMV);
             k_cg_update<<<grid, BLOCK, 0, c->stream>>>(N, x, V, ld, kp, max_it);
             k_cg_p<<<grid, BLOCK, 0, c->stream>>>(N, V, ld, kp);
@@ -673,6 +692,7 @@ int heat_alloc(pfg_ctx* c) {
     c->has_heat_bc = false;
     c->has_heat_q = false;
     c->heat_ready = true;
+    c->heat_facets_dirty = true;
     return PFG_OK;
 }
 
@@ -680,6 +700,7 @@ int heat_alloc(pfg_ctx* c) {
 // the free-surface flags for a facet whose nodes are all on the free surface, HeatEquation.inl:
 // 319-335; Facet::isOnFreeSurface, Facet.cpp:249-255), in ascending facet order.
 int heat_build_facets(pfg_ctx* c) {
+    if (!c->heat_facets_dirty) return PFG_OK;
     const int N = c->N, F = c->has_facets ? c->F : 0, dim = c->dim;
     const int fsf = c->prm.heat_fs_flags & (HT_Q | HT_QH | HT_QR);
     std::vector<uint8_t> ff((size_t)std::max(F, 1), 0);
@@ -710,6 +731,7 @@ int heat_build_facets(pfg_ctx* c) {
     bool need_q = false;
     for (int f = 0; f < F; ++f) need_q |= (ff[f] & HT_Q) != 0;
     if (need_q && !c->has_heat_q) return fail(c, PFG_ERR_STATE, "heat facets with a Q flag need pfg_heat_set_flux");
+    c->heat_facets_dirty = false;
     return PFG_OK;
 }
 

@@ -152,6 +152,7 @@ struct pfg_ctx {
     pfg::DBuf hf_ptr, hf_ent, hf_fflags, heat_q;
     bool heat_ready = false;  // heat buffers allocated (and zeroed) for the current mesh
     bool has_heat_bc = false, has_heat_q = false;
+    bool heat_facets_dirty = true;  // the per-node heat facet lists need rebuilding
     std::vector<uint8_t> h_heat_flags;
     std::vector<int32_t> h_facets, h_facet_elm;
 };

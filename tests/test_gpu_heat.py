@@ -180,7 +180,9 @@ TM, DTM, LM = 933.15, 20.0, 396000.0  # the reference's phase-change example (al
 @pytest.mark.parametrize("which", ["c1", "3d"])
 def test_heat_phase_change_picard_matches_oracle(gpu_lib, which, residual, c1_mesh, small3d_mesh):
     """HeatEqIncompNewton with phase change: Picard iterations on the latent-heat mass factor
-    (HeatEquation.inl:60-66, 131-138), same iteration counts as the oracle."""
+    (HeatEquation.inl:60-66, 131-138), the same outcome and iteration count as the oracle.  The
+    absolute "Ax_f" residual of this system contracts ~5x per iteration, so in 3D neither side
+    reaches minRes within maxIter: both fail and restore."""
     mesh = c1_mesh if which == "c1" else small3d_mesh
     N = mesh.n_nodes
     kw = dict(heat_h=500.0, heat_t_inf=300.0, heat_fs_flags=api.HEAT_QH)
@@ -196,8 +198,10 @@ def test_heat_phase_change_picard_matches_oracle(gpu_lib, which, residual, c1_me
         st = ctx.heat_step(1.0)
         r = {}
         to = O.heat_step(om, p, 1.0, to, fl, residual="T" if residual == api.RES_T else "Ax_f", result=r)
-        assert st.converged == 1 and r["converged"]
-        assert st.picard_iterations == r["iterations"] and st.picard_iterations >= 2
+        assert st.converged == int(r["converged"]) and st.picard_iterations == r["iterations"]
+        assert st.picard_iterations >= 2
+        if residual == api.RES_T or which == "c1":
+            assert st.converged == 1
         t = ctx.get_temperature()
         assert np.abs(t - to).max() / np.abs(to).max() < 1e-10, step
 
