@@ -432,9 +432,10 @@ __global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict_
     }
 }
 
-// q = A p, alpha = rz / (p . q).  G lanes per row (4 in 2D, 8 in 3D: about one entry per lane)
-// so a row's values and columns are read by adjacent lanes; the group's sum is a shuffle
-// reduction in a fixed order, so the result does not depend on the launch shape.
+// q = A p, alpha = rz / (p . q).  G lanes per row; the group's sum is a shuffle reduction in a
+// fixed order.  Measured on the C3 heat system (ncu, one cold launch): one thread per row
+// 38.5 us, 8 lanes per row 49.3 us (issue bound on the per-row overhead of ~13-entry rows), so
+// the launches use G = 1.
 template <int G>
 __global__ void __launch_bounds__(BLOCK) k_cg_spmv(int N, const int* __restrict__ rp, const int* __restrict__ col,
                                                    const double* __restrict__ val, double* __restrict__ V, size_t ld,
@@ -454,8 +455,10 @@ __global__ void __launch_bounds__(BLOCK) k_cg_spmv(int N, const int* __restrict_
         const int b = act ? rp[r] : 0, e = act ? rp[r + 1] : 0;
         double s = 0;
         for (int t = b + lane; t < e; t += G) s += val[t] * p[col[t]];
+        if constexpr (G > 1) {
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+            for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+        }
         if (act && lane == 0) {
             V[V_Q * ld + r] = s;
             pq += p[r] * s;
@@ -570,7 +573,6 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
     PFG_CUDA(c, cudaMemcpyAsync(x, tprev, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     const CgPtrs kp = cg_ptrs(c);
     const int grid = std::max(1, std::min(c->max_grid, div_up(N, BLOCK)));
-    const int grid_rows = std::max(1, std::min(c->max_grid, div_up((long long)N * (c->dim == 2 ? 4 : 8), BLOCK)));
     const int* rp = ptr<int>(c->nbr_ptr);
     const int* col = ptr<int>(c->nbr);
     const double* val = ptr<double>(c->heat_val);
@@ -584,10 +586,7 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
         const int n = std::min(8, max_it - done_it);
         for (int it = 0; it < n; ++it) {
             prof_begin(c, PH_HEAT_SPMV);
-            if (c->dim == 2)
-                k_cg_spmv<4><<<grid_rows, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
-            else
-                k_cg_spmv<8><<<grid_rows, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
+            k_cg_spmv<1><<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
             prof_end(c, PH_HEAT_SPMV);
             k_cg_update<<<grid, BLOCK, 0, c->stream>>>(N, x, V, ld, kp, max_it);
             k_cg_p<<<grid, BLOCK, 0, c->stream>>>(N, V, ld, kp);
