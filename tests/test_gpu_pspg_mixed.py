@@ -192,3 +192,37 @@ def test_set_positions_restores_a_step(gpu_lib, c1_mesh):
     ctx.picard_step(1e-3)
     assert np.array_equal(ctx.get_positions(), x1)
     assert np.array_equal(ctx.get_states(), q1)
+
+
+def test_c3_full_size_properties(gpu_lib):
+    """The C3 mesh (330k nodes, 1.74M tets) at its own tolerance (relative residual 1e-8):
+    size-independent properties of two Picard steps.  Both forms converge with the same Picard
+    iteration counts, agree to what that tolerance allows, keep the fluid volume (to the PSPG
+    divergence error) and keep the wall nodes fixed."""
+    from pfem_gb300 import workloads as W
+
+    mesh = W.c3()
+    N = mesh.n_nodes
+    q0 = M.incomp_initial_states(mesh, column=(0.5, 0.5, 1.0))
+    bound = (mesh.flags & M.BOUND) != 0
+    out = {}
+    for prec in (api.PREC_MIXED, api.PREC_FP64):
+        p = api.default_params(api.KIND_INCOMP_PSPG, 3)
+        p.precision = prec
+        p.krylov_rel_tol, p.krylov_abs_tol = 1e-8, 0.0
+        ctx = api.Context(p)
+        ctx.upload_mesh(mesh)
+        ctx.set_states(q0)
+        v0 = ctx.volume()
+        its = []
+        for _ in range(2):
+            st = ctx.picard_step(5e-4)
+            assert st.converged == 1
+            its.append(st.picard_iterations)
+        x = ctx.get_positions()
+        assert np.isfinite(x).all() and np.array_equal(x[:, bound], mesh.pos[:, bound])
+        assert abs(ctx.volume() / v0 - 1) < 1e-3, ctx.volume() / v0 - 1
+        out[prec] = (its, ctx.get_states())
+        ctx.close()
+    assert out[api.PREC_MIXED][0] == out[api.PREC_FP64][0]
+    assert max(field_errs(out[api.PREC_MIXED][1], out[api.PREC_FP64][1], 3, N)) < 1e-3
