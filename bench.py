@@ -583,14 +583,14 @@ def run_gpu_incomp(args):
         ms = sum(a.elapsed_time(b) for a, b in ev)
         if stats["converged"] != K:
             raise RuntimeError(f"{K - stats['converged']} of {K} timed steps did not converge")
-        return ctx, ms, stats, clk  # holds the state one step after the warm-up
+        return ctx, ms, stats, clk, (x_w, q_w)  # ctx holds the state one step after the warm-up
 
     prec = api.PREC_MIXED if args.precision == "fp32" else api.PREC_FP64
     clocks = ClockSampler(local)
-    ctx, total_ms, stats, clk = run(prec, clocks)
+    ctx, total_ms, stats, clk, (x_w, q_w) = run(prec, clocks)
     q_fast, x_fast = ctx.get_states(), ctx.get_positions()
     other = api.PREC_FP64 if prec == api.PREC_MIXED else api.PREC_MIXED
-    ctx_o, ms_o, stats_o, _ = run(other)
+    ctx_o, ms_o, stats_o, _, _ = run(other)
     q_o, x_o = ctx_o.get_states(), ctx_o.get_positions()
     acc_vs_fp64 = None
     if prec == api.PREC_MIXED:
@@ -599,9 +599,10 @@ def run_gpu_incomp(args):
         acc_vs_fp64["steps"] = Wm + 1
     ctx_o.close()
 
-    # per-phase times (library event timers, direct launches) on a few more steps
+    # per-phase times (library event timers, direct launches) on a few more steps from the warm
+    # state, as the timed steps
     Kp = min(K, 3)
-    x_s, q_s = ctx.get_positions(), ctx.get_states()
+    x_s, q_s = x_w, q_w
     ctx.set_profiling(True)
     ctx.reset_phase_times()
     for _ in range(Kp):  # from the same state every time, as the timed steps
