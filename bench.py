@@ -647,15 +647,19 @@ def run_gpu_incomp(args):
         g = (0.0, -9.81)
         t0 = time.perf_counter()
         n_cpu = 0
+        q_cmp = x_cmp = None
         for k in range(Wm + K):
             qo, res = O.pspg_picard_step(om, qo, dt, g=g)
             n_cpu += 1
+            if n_cpu == Wm + 1:  # the GPU's q_fast: one step after the warm-up steps
+                q_cmp, x_cmp = qo.copy(), om.positions
         el = time.perf_counter() - t0
         cpu = {"value": n_cpu / el, "unit": cfg["unit"], "cores": O.num_threads(), "kind": "port",
                "sample": f"{n_cpu} C1 Picard steps of the FP64 C++/OpenMP oracle with SciPy SuperLU/COLAMD "
                          f"({el:.1f} s)"}
-        acc_vs_oracle = dict(zip(["vx", "vy", "p"], field_errors(q_fast, qo, 3, N)))
-        acc_vs_oracle["x"] = float(np.abs(x_fast - om.positions).max() / np.abs(om.positions).max())
+        acc_vs_oracle = dict(zip(["vx", "vy", "p"], field_errors(q_fast, q_cmp, 3, N)))
+        acc_vs_oracle["x"] = float(np.abs(x_fast - x_cmp).max() / np.abs(x_cmp).max())
+        acc_vs_oracle["steps"] = Wm + 1
 
     value = K / (total_ms / 1e3)
     if rank == 0:
