@@ -473,6 +473,8 @@ NCU_TRAFFIC = {
     ("wc-c2", "fp32", "WC continuity node"): 8.1851e6,
     # scaled from the h = 0.012 capture by nnz (189.4 MB x 66.96 / 39.16): node-pair blocks
     ("incomp-c3", "fp32", "Krylov SpMV"): 323.9e6,
+    # one cold launch on the C3 heat system (profiles/heat_cg_c3.md): 56.66 MB read + 0.24 MB written
+    ("heat-c3", "fp64", "Heat CG SpMV"): 56.9e6,
 }
 
 
@@ -801,7 +803,8 @@ def run_gpu_heat(args):
     peak, peak_kind = hbm_peak()
     achieved = spmv_b * it_p / (spmv_ms / 1e3) / 1e9 if spmv_ms else None
     roof = {"bound": "hbm", "kernel": "Heat CG SpMV", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak if achieved else None, "traffic": None, "algorithmic_bytes": spmv_b,
+            "frac": achieved / peak if achieved else None, "traffic": NCU_TRAFFIC.get(("heat-c3", "fp64", "Heat CG SpMV")),
+            "algorithmic_bytes": spmv_b,
             "avg_launch_us": 1e3 * spmv_ms / max(it_p, 1), "peak_kind": peak_kind,
             "note": "time of all SpMV launches (including the no-op tail of the last 8-iteration chunk) "
                     "over the iterations run"}
