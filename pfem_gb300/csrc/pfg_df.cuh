@@ -46,18 +46,6 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
     return r;
 }
 
-// Sum with the low parts added without their own error term (Dekker's add): the error is
-// about 2^-44 of max(|a|, |b|) instead of the result, which is enough where accuracy is only
-// needed relative to the magnitude of the operands (matrix entries against their row scale).
-__device__ __forceinline__ DF df_add_fast(DF a, DF b) {
-    float s, e;
-    two_sum_f(a.h, b.h, s, e);
-    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
-    DF r;
-    quick_two_sum_f(s, e, r.h, r.l);
-    return r;
-}
-
 __device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
 
 __device__ __forceinline__ DF df_mul(DF a, DF b) {

@@ -242,8 +242,7 @@ __global__ void k_mx_rhs(int N, int E, const int* __restrict__ ne_ptr, const int
 }
 
 // Block (n, m) like pspg_pair_block (same gather, element order and expressions), evaluated in
-// double-float on the FP32 pipe from the double-float element data; returned in FP64.  The sums
-// use Dekker's add: their error is relative to the operands, i.e. to the row scale.  On
+// double-float on the FP32 pipe from the double-float element data; returned in FP64.  On
 // GB300 the FP64 evaluation is bound by the FP64 pipe (87% busy, 1/64 of the FP32 rate);
 // double-float carries ~48 bits, so the values agree with the FP64 evaluation to ~1e-14 of
 // the row scale.
@@ -283,7 +282,7 @@ __device__ __forceinline__ void pspg_pair_block_df(int n, int m, int E, const in
         }
         DF dot = df_mul(gi[0], gj[0]);
 #pragma unroll
-        for (int f = 1; f < DIM; ++f) dot = df_add_fast(dot, df_mul(gi[f], gj[f]));
+        for (int f = 1; f < DIM; ++f) dot = df_add(dot, df_mul(gi[f], gj[f]));
         const DF mij = df_mul(k.inv_dt, df_mul(df_mul(k.rho, MM[i][j]), ae));
         const DF kf = df_mul(ae, edf[(size_t)ed_ksum<DIM>() * E + e]);
 #pragma unroll
@@ -291,19 +290,19 @@ __device__ __forceinline__ void pspg_pair_block_df(int n, int m, int E, const in
 #pragma unroll
             for (int f2 = 0; f2 < DIM; ++f2) {
                 const DF g2 = df_mul(gi[f2], gj[f1]);
-                const DF kv = df_mul(kf, f1 == f2 ? df_add_fast(dot, g2) : g2);
-                acc[f1][f2] = df_add_fast(acc[f1][f2], f1 == f2 ? df_add_fast(mij, kv) : kv);
+                const DF kv = df_mul(kf, f1 == f2 ? df_add(dot, g2) : g2);
+                acc[f1][f2] = df_add(acc[f1][f2], f1 == f2 ? df_add(mij, kv) : kv);
             }
-            acc[f1][DIM] = df_add_fast(acc[f1][DIM], df_neg(df_mul(df_mul(ae, S[j]), gi[f1])));
+            acc[f1][DIM] = df_add(acc[f1][DIM], df_neg(df_mul(df_mul(ae, S[j]), gi[f1])));
         }
         const DF ctau = df_mul(tau, k.inv_dt);
 #pragma unroll
         for (int f2 = 0; f2 < DIM; ++f2) {
             const DF c1 = df_mul(ctau, df_mul(df_mul(ae, gi[f2]), S[j]));
             const DF c2 = df_mul(df_mul(ae, S[i]), gj[f2]);
-            acc[DIM][f2] = df_add_fast(acc[DIM][f2], df_add_fast(c1, c2));
+            acc[DIM][f2] = df_add(acc[DIM][f2], df_add(c1, c2));
         }
-        acc[DIM][DIM] = df_add_fast(acc[DIM][DIM], df_mul(tau, df_mul(df_mul(ae, k.l_sum), dot)));
+        acc[DIM][DIM] = df_add(acc[DIM][DIM], df_mul(tau, df_mul(df_mul(ae, k.l_sum), dot)));
     }
 #pragma unroll
     for (int a = 0; a < NPE; ++a)
