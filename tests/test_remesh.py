@@ -70,3 +70,31 @@ def test_remesh_carries_states_with_nodes():
         if i is not None:
             assert q2[2 * N2 + j] == q[2 * m.n_nodes + i]
     assert new.n_elems > 0 and not new.is_free()[(new.flags & M.BOUND) == 0].any()
+
+
+def test_remesh_map_reproduces_the_host_remap():
+    """`remesh_map` + `apply_origin` (the table `pfg_upload_mesh_remap` applies on the device)
+    give the host remap's mesh and states bitwise, added centroid nodes included."""
+    mesh = M.dam_break_2d(0.1)
+    rng = np.random.default_rng(7)
+    prm = R.RemeshParams(hchar=0.1, omega=0.7, gamma=0.2, bounding_box=(-0.01, -1.0, 4.01, 100.0))
+    cur = mesh.copy()
+    cur.pos = mesh.pos + 0.02 * rng.standard_normal(mesh.pos.shape) * ((mesh.flags & M.BOUND) == 0)
+    states = rng.standard_normal(4 * mesh.n_nodes)  # three flow fields and a temperature
+    new, st = R.remesh(cur, states, prm)
+    new2, origin = R.remesh_map(cur, prm)
+    assert np.array_equal(new.conn, new2.conn) and np.array_equal(new.pos, new2.pos)
+    assert origin.shape == (new.n_nodes, 3) and (origin[:, 1] >= 0).any()
+    assert np.array_equal(R.apply_origin(states, origin, mesh.n_nodes), st)
+
+
+def test_flux_at_gauss_points_uses_reference_positions():
+    from pfem_gb300 import heat as H
+
+    mesh = M.dam_break_2d(0.1)
+    q = H.flux_at_gauss_points(mesh.pos, mesh.facets, lambda x, t: np.array([x[0] + t, 2 * x[1]]), 0.5)
+    xs = H.facet_gauss_positions(mesh.pos, mesh.facets)
+    assert q.shape == (mesh.facets.shape[1], 3, 2)
+    assert np.allclose(q[..., 0], xs[..., 0] + 0.5) and np.allclose(q[..., 1], 2 * xs[..., 1])
+    # 2D: the middle point sits on the facet's first node (half-edge Jacobian on [-1, 1])
+    assert np.array_equal(xs[:, 1, :], mesh.pos[:, mesh.facets[0]].T)
