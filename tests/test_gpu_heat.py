@@ -225,3 +225,30 @@ def test_heat_phase_change_failure_restores(gpu_lib, c1_mesh):
     assert st.converged == 0 and not r["converged"]
     assert st.picard_iterations == r["iterations"] == 2
     assert np.array_equal(ctx.get_temperature(), t0) and np.array_equal(to, t0)
+
+
+def test_heat_free_nodes(gpu_lib, c1_mesh):
+    """Nodes in no element (flying drops after a remesh): identity rows, T kept, or set when the
+    node is a Dirichlet node (HeatEquation.inl:287-293, 380-389), as in the oracle."""
+    base = c1_mesh
+    m = base.copy()
+    extra = np.array([[3.5, 3.6], [2.5, 2.6]])
+    m.pos = np.concatenate([base.pos, extra], axis=1)
+    m.flags = np.concatenate([base.flags, np.zeros(2, np.uint8)])
+    N = m.n_nodes
+    ctx = make_ctx(m, heat_h=5.0, heat_t_inf=300.0, heat_fs_flags=api.HEAT_QH)
+    t0 = 300.0 + 50.0 * np.sin(2 * m.pos[0])
+    fl = np.zeros(N, np.uint8)
+    fl[N - 1] = api.HEAT_T
+    tbc = np.zeros(N)
+    tbc[N - 1] = 777.0
+    ctx.set_temperature(t0)
+    ctx.heat_set_bc(fl, tbc)
+    st = ctx.heat_step(0.05)
+    om = O.OracleMesh(m)
+    assert om.is_free()[N - 2] and om.is_free()[N - 1]
+    to = O.heat_step(om, O.heat_params(RHO, CV, K, h=5.0, t_inf=300.0, fs_flags=O.HT_QH), 0.05, t0, fl, tbc)
+    t = ctx.get_temperature()
+    assert st.converged == 1
+    assert t[N - 2] == t0[N - 2] and t[N - 1] == 777.0
+    assert np.abs(t - to).max() / np.abs(to).max() < 1e-10
