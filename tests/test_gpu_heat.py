@@ -250,5 +250,6 @@ def test_heat_free_nodes(gpu_lib, c1_mesh):
     to = O.heat_step(om, O.heat_params(RHO, CV, K, h=5.0, t_inf=300.0, fs_flags=O.HT_QH), 0.05, t0, fl, tbc)
     t = ctx.get_temperature()
     assert st.converged == 1
-    assert t[N - 2] == t0[N - 2] and t[N - 1] == 777.0
+    # identity rows: exact in the oracle's LU, to the CG tolerance on the device
+    assert t[N - 2] == pytest.approx(t0[N - 2], rel=1e-12) and t[N - 1] == pytest.approx(777.0, rel=1e-12)
     assert np.abs(t - to).max() / np.abs(to).max() < 1e-10
