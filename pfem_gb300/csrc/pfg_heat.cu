@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
 // ---- Jacobi-preconditioned conjugate gradients over the pair-ordered CSR -----------------
 
 enum : int { S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_TOL2, S_DONE, S_ITERS, S_BB, S_NUM, S_DEN, S_COUNT };
-enum : int { V_R = 0, V_Z, V_P, V_Q, V_DIAG, V_COUNT };
+enum : int { V_R = 0, V_Z, V_P, V_Q, V_DIAG, V_COUNT };  // V_DIAG holds the inverse diagonal
 
 struct CgPtrs {
     double* partials;  // 2 * max_grid
@@ -413,11 +413,12 @@ __global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict_
             if (m == n) d = val[t];
         }
         const double r = b[n] - ax;
-        const double z = r / d;
+        const double dinv = 1.0 / d;  // one FP64 division per row per solve, multiplies after
+        const double z = r * dinv;
         V[V_R * ld + n] = r;
         V[V_Z * ld + n] = z;
         V[V_P * ld + n] = z;
-        V[V_DIAG * ld + n] = d;
+        V[V_DIAG * ld + n] = dinv;
         rz += r * z;
         bb += b[n] * b[n];
     }
@@ -481,7 +482,7 @@ __global__ void __launch_bounds__(BLOCK) k_cg_update(int N, double* __restrict__
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         x[n] += alpha * V[V_P * ld + n];
         const double r = V[V_R * ld + n] - alpha * V[V_Q * ld + n];
-        const double z = r / V[V_DIAG * ld + n];
+        const double z = r * V[V_DIAG * ld + n];  // inverse diagonal
         V[V_R * ld + n] = r;
         V[V_Z * ld + n] = z;
         rz += r * z;
