@@ -351,11 +351,21 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
 
 // ---- Jacobi-preconditioned conjugate gradients over the pair-ordered CSR -----------------
 
-enum : int { S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_TOL2, S_DONE, S_ITERS, S_BB, S_NUM, S_DEN, S_COUNT };
-enum : int { V_R = 0, V_Z, V_P, V_Q, V_DIAG, V_COUNT };  // V_DIAG holds the inverse diagonal
+// ---- Jacobi-preconditioned conjugate gradients, Chronopoulos-Gear form ------------------
+//
+// The classic recurrences rearranged so that one iteration needs one SpMV kernel with one
+// fused reduction (gamma = r.z, delta = w.z with w = A z, and ||r||^2) and one pointwise kernel
+// (Chronopoulos and Gear, J. Comput. Appl. Math. 25, 1989): s = A p is carried by recurrence.
+//   pointwise: p = z + beta p; s = w + beta s; x += alpha p; r -= alpha s; z = r / diag
+//   spmv:      w = A z; gamma, delta, rr; beta = gamma / gamma_old;
+//              alpha = gamma / (delta - beta gamma / alpha_old)
+// Mathematically the same iterates as classic CG; the rounding differs.
+
+enum : int { S_GAMMA = 0, S_ALPHA, S_BETA, S_RR, S_TOL2, S_DONE, S_ITERS, S_BB, S_NUM, S_DEN, S_FIRST, S_COUNT };
+enum : int { V_R = 0, V_Z, V_P, V_S, V_W, V_DIAG, V_COUNT };  // V_DIAG holds the inverse diagonal
 
 struct CgPtrs {
-    double* partials;  // 2 * max_grid
+    double* partials;  // 3 * max_grid
     double* sc;        // S_COUNT
     unsigned* ticket;
 };
@@ -364,9 +374,40 @@ CgPtrs cg_ptrs(pfg_ctx* c) {
     double* red = ptr<double>(c->heat_red);
     CgPtrs k;
     k.partials = red;
-    k.sc = red + 2 * (size_t)c->max_grid;
+    k.sc = red + 3 * (size_t)c->max_grid;
     k.ticket = reinterpret_cast<unsigned*>(k.sc + 32);
     return k;
+}
+
+// Three-value version of grid_sum2.
+template <int NT>
+__device__ __forceinline__ bool grid_sum3(double a, double b, double c, double* partials, unsigned* ticket,
+                                          double* sh, double& ra, double& rb, double& rc) {
+    a = block_sum<NT>(a, sh);
+    b = block_sum<NT>(b, sh);
+    c = block_sum<NT>(c, sh);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = a;
+        partials[gridDim.x + blockIdx.x] = b;
+        partials[2 * gridDim.x + blockIdx.x] = c;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double sa = 0, sb = 0, sc = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += NT) {
+        sa += ((volatile double*)partials)[i];
+        sb += ((volatile double*)partials)[gridDim.x + i];
+        sc += ((volatile double*)partials)[2 * gridDim.x + i];
+    }
+    ra = block_sum<NT>(sa, sh);
+    rb = block_sum<NT>(sb, sh);
+    rc = block_sum<NT>(sc, sh);
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
 }
 
 template <int NT>
@@ -395,16 +436,15 @@ __device__ __forceinline__ bool grid_sum2(double a, double b, double* partials, 
     return true;
 }
 
-// r = b - A x, z = r / diag, p = z; rz = r.z; tolerance max(rtol ||b||, atol), capped at
+// r = b - A x, z = r / diag, p = s = 0; tolerance max(rtol ||b||, atol), capped at
 // max(cap, 2e-16 ||b||) (the heat Picard loop with an absolute "Ax_f" residual needs the linear
-// solve below its minRes, down to the rounding level an LU solve reaches).  An exact start still
-// runs one iteration (alpha = 0), which finds ||r|| <= tol.
+// solve below its minRes, down to the rounding level an LU solve reaches).
 __global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict__ rp, const int* __restrict__ col,
                                                    const double* __restrict__ val, const double* __restrict__ b,
                                                    const double* __restrict__ x, double* __restrict__ V, size_t ld,
                                                    CgPtrs k, double rtol, double atol, double cap) {
     __shared__ double sh[32];
-    double rz = 0, bb = 0;
+    double bb = 0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
         double ax = 0, d = 1.0;
         for (int t = rp[n]; t < rp[n + 1]; ++t) {
@@ -414,99 +454,99 @@ __global__ void __launch_bounds__(BLOCK) k_cg_init(int N, const int* __restrict_
         }
         const double r = b[n] - ax;
         const double dinv = 1.0 / d;  // one FP64 division per row per solve, multiplies after
-        const double z = r * dinv;
         V[V_R * ld + n] = r;
-        V[V_Z * ld + n] = z;
-        V[V_P * ld + n] = z;
+        V[V_Z * ld + n] = r * dinv;
+        V[V_P * ld + n] = 0.0;
+        V[V_S * ld + n] = 0.0;
         V[V_DIAG * ld + n] = dinv;
-        rz += r * z;
         bb += b[n] * b[n];
     }
-    double s1, s2;
-    if (grid_sum2<BLOCK>(rz, bb, k.partials, k.ticket, sh, s1, s2) && threadIdx.x == 0) {
-        k.sc[S_RZ] = s1;
-        k.sc[S_BB] = s2;
-        const double tol = fmin(fmax(rtol * sqrt(s2), atol), fmax(cap, 2e-16 * sqrt(s2)));
+    double s1, unused;
+    if (grid_sum2<BLOCK>(bb, 0.0, k.partials, k.ticket, sh, s1, unused) && threadIdx.x == 0) {
+        k.sc[S_BB] = s1;
+        const double tol = fmin(fmax(rtol * sqrt(s1), atol), fmax(cap, 2e-16 * sqrt(s1)));
         k.sc[S_TOL2] = tol * tol;
         k.sc[S_ITERS] = 0;
         k.sc[S_DONE] = 0;
+        k.sc[S_GAMMA] = 0;
+        k.sc[S_ALPHA] = 1;
+        k.sc[S_BETA] = 0;
+        k.sc[S_FIRST] = 1;
     }
 }
 
-// q = A p, alpha = rz / (p . q).  G lanes per row; the group's sum is a shuffle reduction in a
-// fixed order.  Measured on the C3 heat system (ncu, one cold launch): one thread per row
-// 38.5 us, 8 lanes per row 49.3 us (issue bound on the per-row overhead of ~13-entry rows), so
-// the launches use G = 1.
+// w = A z with gamma = r.z, delta = w.z and ||r||^2 in one reduction; the last block updates
+// the scalars and the convergence state (1 converged, 2 breakdown or NaN, 3 iteration cap).
+// G lanes per row, the group's sum a shuffle reduction in a fixed order.  Measured on the C3
+// heat system (ncu, one cold launch of the earlier p.q SpMV): one thread per row 38.5 us,
+// 8 lanes per row 49.3 us (issue bound on the per-row overhead of ~13-entry rows): G = 1.
 template <int G>
 __global__ void __launch_bounds__(BLOCK) k_cg_spmv(int N, const int* __restrict__ rp, const int* __restrict__ col,
                                                    const double* __restrict__ val, double* __restrict__ V, size_t ld,
-                                                   CgPtrs k) {
+                                                   CgPtrs k, int max_it) {
     __shared__ double sh[32];
     if (k.sc[S_DONE] != 0.0) return;
-    const double* p = V + V_P * ld;
+    const double* z = V + V_Z * ld;
+    const double* r = V + V_R * ld;
     const int lane = threadIdx.x % G;
     constexpr int GPW = 32 / G;  // rows per warp and trip
     const int wglob = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
     const int nwarps = gridDim.x * blockDim.x / 32;
-    double pq = 0;
+    double ga = 0, de = 0, rr = 0;
     // all lanes of a warp share r0, so they run the same trips (the shuffles need the warp)
     for (int r0 = wglob * GPW; r0 < N; r0 += nwarps * GPW) {
-        const int r = r0 + (threadIdx.x & 31) / G;
-        const bool act = r < N;
-        const int b = act ? rp[r] : 0, e = act ? rp[r + 1] : 0;
-        double s = 0;
-        for (int t = b + lane; t < e; t += G) s += val[t] * p[col[t]];
+        const int n = r0 + (threadIdx.x & 31) / G;
+        const bool act = n < N;
+        const int b = act ? rp[n] : 0, e = act ? rp[n + 1] : 0;
+        double w = 0;
+        for (int t = b + lane; t < e; t += G) w += val[t] * z[col[t]];
         if constexpr (G > 1) {
 #pragma unroll
-            for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+            for (int o = G / 2; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o, G);
         }
         if (act && lane == 0) {
-            V[V_Q * ld + r] = s;
-            pq += p[r] * s;
+            V[V_W * ld + n] = w;
+            const double zn = z[n], rn = r[n];
+            ga += rn * zn;
+            de += w * zn;
+            rr += rn * rn;
         }
     }
-    double a, unused;
-    if (grid_sum2<BLOCK>(pq, 0.0, k.partials, k.ticket, sh, a, unused) && threadIdx.x == 0) {
-        k.sc[S_PQ] = a;
-        k.sc[S_ALPHA] = a != 0.0 ? k.sc[S_RZ] / a : 0.0;
-    }
-}
-
-// x += alpha p, r -= alpha q, z = r / diag; beta = rz_new / rz; done when ||r|| <= tol.
-__global__ void __launch_bounds__(BLOCK) k_cg_update(int N, double* __restrict__ x, double* __restrict__ V, size_t ld,
-                                                     CgPtrs k, int max_it) {
-    __shared__ double sh[32];
-    if (k.sc[S_DONE] != 0.0) return;
-    const double alpha = k.sc[S_ALPHA];
-    double rz = 0, rr = 0;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
-        x[n] += alpha * V[V_P * ld + n];
-        const double r = V[V_R * ld + n] - alpha * V[V_Q * ld + n];
-        const double z = r * V[V_DIAG * ld + n];  // inverse diagonal
-        V[V_R * ld + n] = r;
-        V[V_Z * ld + n] = z;
-        rz += r * z;
-        rr += r * r;
-    }
-    double s1, s2;
-    if (grid_sum2<BLOCK>(rz, rr, k.partials, k.ticket, sh, s1, s2) && threadIdx.x == 0) {
-        const double it = k.sc[S_ITERS] + 1;
+    double g, s_de, s_rr;
+    if (!grid_sum3<BLOCK>(ga, de, rr, k.partials, k.ticket, sh, g, s_de, s_rr)) return;
+    if (threadIdx.x == 0) {
+        const bool first = k.sc[S_FIRST] != 0.0;
+        const double it = k.sc[S_ITERS] + (first ? 0.0 : 1.0);
         k.sc[S_ITERS] = it;
-        k.sc[S_RR] = s2;
-        k.sc[S_BETA] = k.sc[S_RZ] != 0.0 ? s1 / k.sc[S_RZ] : 0.0;
-        k.sc[S_RZ] = s1;
-        if (s2 <= k.sc[S_TOL2]) k.sc[S_DONE] = 1;
-        else if (!(s2 == s2) || k.sc[S_PQ] <= 0.0) k.sc[S_DONE] = 2;  // NaN or loss of definiteness
+        k.sc[S_FIRST] = 0;
+        k.sc[S_RR] = s_rr;
+        const double gold = k.sc[S_GAMMA];
+        const double beta = gold != 0.0 ? g / gold : 0.0;
+        const double den = s_de - beta * g / k.sc[S_ALPHA];
+        k.sc[S_BETA] = beta;
+        k.sc[S_ALPHA] = den != 0.0 ? g / den : 0.0;
+        k.sc[S_GAMMA] = g;
+        if (s_rr <= k.sc[S_TOL2]) k.sc[S_DONE] = 1;
+        else if (!(s_rr == s_rr) || !(den > 0.0)) k.sc[S_DONE] = 2;  // NaN or loss of definiteness
         else if (it >= max_it) k.sc[S_DONE] = 3;
     }
 }
 
-// p = z + beta p
-__global__ void __launch_bounds__(BLOCK) k_cg_p(int N, double* __restrict__ V, size_t ld, CgPtrs k) {
+// p = z + beta p; s = w + beta s; x += alpha p; r -= alpha s; z = r / diag
+__global__ void __launch_bounds__(BLOCK) k_cg_update(int N, double* __restrict__ x, double* __restrict__ V, size_t ld,
+                                                     CgPtrs k) {
     if (k.sc[S_DONE] != 0.0) return;
-    const double beta = k.sc[S_BETA];
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
-        V[V_P * ld + n] = V[V_Z * ld + n] + beta * V[V_P * ld + n];
+    const double alpha = k.sc[S_ALPHA], beta = k.sc[S_BETA];
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const double p = V[V_Z * ld + n] + beta * V[V_P * ld + n];
+        const double sv = V[V_W * ld + n] + beta * V[V_S * ld + n];
+        V[V_P * ld + n] = p;
+        V[V_S * ld + n] = sv;
+        x[n] += alpha * p;
+        const double r = V[V_R * ld + n] - alpha * sv;
+        V[V_R * ld + n] = r;
+        V[V_Z * ld + n] = r * V[V_DIAG * ld + n];  // inverse diagonal
+    }
 }
 
 // Squared relative change of the non-free nodes (residual "T", HeatEquation.inl:153-180):
@@ -579,18 +619,21 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
     const double* val = ptr<double>(c->heat_val);
     k_cg_init<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, ptr<double>(c->heat_rhs), x, V, ld, kp,
                                              c->prm.krylov_rel_tol, c->prm.krylov_abs_tol, cap);
-    PFG_CHECK_LAUNCH(c);
     const int max_it = std::max(1, c->prm.krylov_max_iter);
+    // w0 = A z0 with the first scalars (no iteration counted)
+    prof_begin(c, PH_HEAT_SPMV);
+    k_cg_spmv<1><<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp, max_it);
+    prof_end(c, PH_HEAT_SPMV);
+    PFG_CHECK_LAUNCH(c);
     double* h = c->h_scalars;
     int done_it = 0;
     while (done_it < max_it) {
         const int n = std::min(8, max_it - done_it);
         for (int it = 0; it < n; ++it) {
+            k_cg_update<<<grid, BLOCK, 0, c->stream>>>(N, x, V, ld, kp);
             prof_begin(c, PH_HEAT_SPMV);
-            k_cg_spmv<1><<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp);
+            k_cg_spmv<1><<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, V, ld, kp, max_it);
             prof_end(c, PH_HEAT_SPMV);
-            k_cg_update<<<grid, BLOCK, 0, c->stream>>>(N, x, V, ld, kp, max_it);
-            k_cg_p<<<grid, BLOCK, 0, c->stream>>>(N, V, ld, kp);
         }
         PFG_CHECK_LAUNCH(c);
         done_it += n;
@@ -679,14 +722,14 @@ int heat_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->heat_tbc, sizeof(double) * N)) || (rc = ensure(c, c->heat_val, sizeof(double) * P)) ||
         (rc = ensure(c, c->heat_rhs, sizeof(double) * N)) ||
         (rc = ensure(c, c->heat_cg, sizeof(double) * (V_COUNT + 3) * N)) ||
-        (rc = ensure(c, c->heat_red, sizeof(double) * (2 * (size_t)std::max(c->max_grid, 1) + 64))) ||
+        (rc = ensure(c, c->heat_red, sizeof(double) * (3 * (size_t)std::max(c->max_grid, 1) + 64))) ||
         (rc = ensure(c, c->hf_ptr, sizeof(int) * (N + 1))))
         return rc;
     PFG_CUDA(c, cudaMemsetAsync(c->heat_t.p, 0, sizeof(double) * N, c->stream));
     PFG_CUDA(c, cudaMemsetAsync(c->heat_flags.p, 0, N, c->stream));
     PFG_CUDA(c, cudaMemsetAsync(c->heat_tbc.p, 0, sizeof(double) * N, c->stream));
     PFG_CUDA(c, cudaMemsetAsync(c->hf_ptr.p, 0, sizeof(int) * (N + 1), c->stream));
-    PFG_CUDA(c, cudaMemsetAsync(c->heat_red.p, 0, sizeof(double) * (2 * (size_t)std::max(c->max_grid, 1) + 64),
+    PFG_CUDA(c, cudaMemsetAsync(c->heat_red.p, 0, sizeof(double) * (3 * (size_t)std::max(c->max_grid, 1) + 64),
                                 c->stream));
     c->h_heat_flags.assign(c->N, 0);
     c->has_heat_bc = false;
