@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "pfg_device.cuh"
+#include "pfg_df.cuh"
 #include "pfg_internal.cuh"
 
 namespace pfg {
@@ -35,6 +36,8 @@ namespace {
 constexpr uint8_t HT_T = PFG_HEAT_T, HT_Q = PFG_HEAT_Q, HT_QH = PFG_HEAT_QH, HT_QR = PFG_HEAT_QR;
 
 struct HeatConst {
+    DF m_df[4][4];    // cv rho MM_ij in double-float (the pair gather without phase change)
+    DF ldt_df;        // dt * sum_g k w_g in double-float
     double MM[4][4];  // sum_g w_g N_i N_j
     double mfac;      // cv rho (the M factor, :54-59)
     double lsum;      // sum_g k w_g (the L factor summed over the Gauss points, :70-74)
@@ -92,6 +95,10 @@ HeatConst heat_const(pfg_ctx* c, double dt) {
     k.tm = c->prm.heat_tm;
     k.dtm = c->prm.heat_dt_melt;
     k.lm = c->prm.heat_lm;
+    auto split = [](double d) { const float h = (float)d; return DF{h, (float)(d - (double)h)}; };
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) k.m_df[i][j] = split(k.mfac * k.MM[i][j]);
+    k.ldt_df = split(dt * k.lsum);
     k.lsum = 0;
     for (int q = 0; q < g.n; ++q) k.lsum += c->prm.heat_k * g.w[q];
     k.refSize = g.refSize;
@@ -129,7 +136,7 @@ HeatConst heat_const(pfg_ctx* c, double dt) {
 // flow assembly recomputes them before its own use).
 template <int DIM>
 __global__ void k_heat_geom(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
-                            double* __restrict__ ed) {
+                            double refSize, double* __restrict__ ed, DF* __restrict__ edf) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -143,6 +150,12 @@ __global__ void k_heat_geom(int E, int N, const int* __restrict__ conn, const do
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
         for (int i = 0; i <= DIM; ++i) ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
+    // double-float copy for the pair gather: |e| = detJ refSize in slot 0, the gradients after
+    edf[e] = df_from(g.detJ * refSize);
+#pragma unroll
+    for (int f = 0; f < DIM; ++f)
+#pragma unroll
+        for (int i = 0; i <= DIM; ++i) edf[(size_t)(2 + f * (DIM + 1) + i) * E + e] = df_from(G[f][i]);
 }
 
 // Value of the pair (n, m), one thread per pair: sum over the shared elements of
@@ -156,13 +169,37 @@ __global__ void __launch_bounds__(BLOCK) k_heat_pairs(int P, int E, const int* _
                                                       const double* __restrict__ ed,
                                                       const uint8_t* __restrict__ flags,
                                                       const uint8_t* __restrict__ hflags, double* __restrict__ val,
-                                                      const double* __restrict__ ts, HeatConst k) {
+                                                      const double* __restrict__ ts, const DF* __restrict__ edf,
+                                                      HeatConst k) {
     constexpr int NPE = DIM + 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P) return;
     const int n = pair_node[t], m = nbr[t];
     if ((hflags[n] & HT_T) || (flags[n] & F_FREE)) {
         val[t] = m == n ? 1.0 : 0.0;
+        return;
+    }
+    if (!k.phase) {
+        // double-float on the FP32 pipe (GB300's FP64 pipe runs at 1/64 of it; the FP64
+        // gather below kept it 85% busy): |e| cv rho MM_ij + dt k_sum |e| gradN_i . gradN_j
+        DF acc{0.0f, 0.0f};
+        for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+            const int e = ne_elem[q];
+            int j = -1;
+#pragma unroll
+            for (int jj = 0; jj < NPE; ++jj)
+                if (__ldg(conn + (size_t)jj * E + e) == m) j = jj;
+            if (j < 0) continue;
+            const int i = ne_loc[q];
+            const DF ae = edf[e];
+            DF dot = df_mul(edf[(size_t)(2 + i) * E + e], edf[(size_t)(2 + j) * E + e]);
+#pragma unroll
+            for (int f = 1; f < DIM; ++f)
+                dot = df_add(dot, df_mul(edf[(size_t)(2 + f * NPE + i) * E + e], edf[(size_t)(2 + f * NPE + j) * E + e]));
+            acc = df_add(acc, df_mul(k.m_df[i][j], ae));
+            acc = df_add(acc, df_mul(df_mul(k.ldt_df, ae), dot));
+        }
+        val[t] = df_to(acc);
         return;
     }
     double acc = 0;
@@ -583,12 +620,13 @@ void heat_assemble(pfg_ctx* c, const HeatConst& k, const double* tprev, const do
     prof_begin(c, PH_HEAT_ASSEMBLY);
     if (E > 0)
         k_heat_geom<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
-                                                                    ptr<double>(c->edata));
+                                                                    k.refSize, ptr<double>(c->edata),
+                                                                    ptr<DF>(c->edata_df));
     if (c->P > 0)
         k_heat_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
             c->P, E, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
             ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<double>(c->edata), ptr<uint8_t>(c->flags),
-            ptr<uint8_t>(c->heat_flags), ptr<double>(c->heat_val), ts, k);
+            ptr<uint8_t>(c->heat_flags), ptr<double>(c->heat_val), ts, ptr<DF>(c->edata_df), k);
     HeatFacets hf;
     hf.ptr = ptr<int>(c->hf_ptr);
     hf.ent = ptr<int>(c->hf_ent);
@@ -723,7 +761,8 @@ int heat_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->heat_rhs, sizeof(double) * N)) ||
         (rc = ensure(c, c->heat_cg, sizeof(double) * (V_COUNT + 3) * N)) ||
         (rc = ensure(c, c->heat_red, sizeof(double) * (3 * (size_t)std::max(c->max_grid, 1) + 64))) ||
-        (rc = ensure(c, c->hf_ptr, sizeof(int) * (N + 1))))
+        (rc = ensure(c, c->hf_ptr, sizeof(int) * (N + 1))) ||
+        (rc = ensure(c, c->edata_df, sizeof(DF) * (3 + c->dim * (c->dim + 1)) * (size_t)std::max(c->E, 1))))
         return rc;
     PFG_CUDA(c, cudaMemsetAsync(c->heat_t.p, 0, sizeof(double) * N, c->stream));
     PFG_CUDA(c, cudaMemsetAsync(c->heat_flags.p, 0, N, c->stream));
