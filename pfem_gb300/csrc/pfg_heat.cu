@@ -95,10 +95,6 @@ HeatConst heat_const(pfg_ctx* c, double dt) {
     k.tm = c->prm.heat_tm;
     k.dtm = c->prm.heat_dt_melt;
     k.lm = c->prm.heat_lm;
-    auto split = [](double d) { const float h = (float)d; return DF{h, (float)(d - (double)h)}; };
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) k.m_df[i][j] = split(k.mfac * k.MM[i][j]);
-    k.ldt_df = split(dt * k.lsum);
     k.lsum = 0;
     for (int q = 0; q < g.n; ++q) k.lsum += c->prm.heat_k * g.w[q];
     k.refSize = g.refSize;
@@ -129,6 +125,11 @@ HeatConst heat_const(pfg_ctx* c, double dt) {
         }
         k.fref = 0.5;
     }
+    // double-float copies for the pair gather (after mfac, MM and lsum are set)
+    auto split = [](double d) { const float h = (float)d; return DF{h, (float)(d - (double)h)}; };
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) k.m_df[i][j] = split(k.mfac * k.MM[i][j]);
+    k.ldt_df = split(dt * k.lsum);
     return k;
 }
 
