@@ -288,7 +288,13 @@ PFG_API int pfg_next_dt(pfg_ctx* ctx, double* dt);
  * array for at most 1,048,576 nodes (16 MiB, held by every device that loads the library until
  * exit); larger meshes return PFG_ERR_INVALID.  All calls share that array, so calls that
  * overlap on the GPU race.  The first call on a device looks up the array's address and should
- * come before any stream capture. */
+ * come before any stream capture; that address is kept for the life of the process, so do not
+ * call cudaDeviceReset (or otherwise destroy and recreate the device's primary context) between
+ * calls.  The caller owns the validation of d_conn: every index must lie in [0, n_nodes), and
+ * none is checked here (checking would need a device pass of its own).  As in the reference's
+ * loop, where std::min drops a NaN candidate (WCompNewton/Solver.cpp:222), an element with a
+ * NaN state or position is skipped by the minimum, so the step stays finite; a caller that must
+ * detect a non-finite state checks the states themselves (pfg_next_dt behaves the same way). */
 PFG_API int pfg_wc_next_dt_noalloc(const pfg_params* params, int32_t n_nodes, int32_t n_elems,
                                    const int32_t* d_conn, const double* d_pos, const double* d_states,
                                    double* d_dt, void* stream);

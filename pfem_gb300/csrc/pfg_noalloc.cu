@@ -22,7 +22,13 @@
 //   * calls whose kernels overlap on the GPU (different streams, no ordering between them)
 //     race on the shared array: order them on one stream or serialise them;
 //   * the first call on each device looks up the array's device address (cudaGetSymbolAddress
-//     with that device current); make that first call before any stream capture begins.
+//     with that device current); make that first call before any stream capture begins.  The
+//     address is cached per device index for the life of the process: a cudaDeviceReset (or
+//     any teardown of the device's primary context) between calls would leave it stale;
+//   * connectivity indices are trusted: the caller guarantees 0 <= d_conn[k] < n_nodes;
+//   * NaN: fmin/fmax drop a NaN operand, so an element with a NaN state is skipped and the
+//     step stays finite, as std::min skips a NaN candidate in the reference's element loop
+//     (WCompNewton/Solver.cpp:222; its NaN check at :230 therefore never sees one there).
 #include <cuda_runtime.h>
 
 #include <algorithm>

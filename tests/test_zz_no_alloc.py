@@ -28,18 +28,23 @@ def _noalloc_dt(lib, params, mesh, conn, pos, st, out):
     return rc
 
 
-def test_noalloc_dt_matches_context_dt_on_consecutive_calls(gpu_lib):
+@pytest.mark.parametrize("dim", [2, 3])
+def test_noalloc_dt_matches_context_dt_on_consecutive_calls(gpu_lib, dim):
     torch = pytest.importorskip("torch")
     from pfem_gb300 import api
     from pfem_gb300 import mesh as M
 
-    mesh = M.dam_break_2d(0.02)
-    p = api.default_params(api.KIND_WC_CDS_DPDT, 2)
+    if dim == 2:
+        mesh, column = M.dam_break_2d(0.02), (1.0, 2.0)
+    else:
+        mesh, column = M.dam_break_3d(0.05, tank=(0.6, 0.3, 0.5), column=(0.2, 0.3, 0.3)), (0.2, 0.3, 0.3)
+    p = api.default_params(api.KIND_WC_CDS_DPDT, dim)
     ctx = api.Context(p)
     ctx.upload_mesh(mesh)
-    s0 = M.wc_initial_states(mesh)
+    s0 = M.wc_initial_states(mesh, column=column)
     rng = np.random.default_rng(11)
-    s0[:2 * mesh.n_nodes] = rng.uniform(-0.5, 0.5, 2 * mesh.n_nodes)   # velocities matter in the CFL bound
+    # velocities matter in the CFL bound
+    s0[:dim * mesh.n_nodes] = rng.uniform(-0.5, 0.5, dim * mesh.n_nodes)
     ctx.set_states(s0)
     out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
 
