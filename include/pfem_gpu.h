@@ -76,6 +76,12 @@ typedef enum {
                                   the FP64 form uses node-block Jacobi)                     */
 } pfg_preconditioner;
 
+/* Arithmetic of the mixed form's FP32 system (the correction solves' operator). */
+typedef enum {
+    PFG_ASM_FP32 = 0,        /* FP32 element arithmetic and FP32 sums                      */
+    PFG_ASM_DOUBLE_FLOAT = 1 /* double-float element arithmetic, rounded to FP32 once       */
+} pfg_assembly;
+
 typedef enum {
     PFG_RES_AX_F = 0,          /* ||A q - b||_2            MomContEquationPSPG.inl:366-371 */
     PFG_RES_U = 1,             /* relative velocity change                        :319-342 */
@@ -118,7 +124,8 @@ typedef struct pfg_params {
                                   (MomEquation.inl:311-335) and needs pfg_upload_facets    */
     /* mixed precision, incompressible: */
     int32_t preconditioner;    /* pfg_preconditioner of the FP32 correction solves         */
-    int32_t pad2;
+    int32_t assembly;          /* pfg_assembly: arithmetic of the FP32 system's node blocks
+                                  (the refinement residual is double-float either way)    */
     /* incompressible, Bingham fluid (problem "Bingham", MomContEquation.inl:54-58,102-121):
        tau0 > 0 makes the viscosity mu + tau0 (1 - exp(-m_reg gd)) / gd per element, gd the
        strain-rate norm of the Picard iterate                                             */

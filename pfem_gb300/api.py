@@ -25,6 +25,8 @@ LINSOLVE_BICGSTAB = 0
 LINSOLVE_LU = 1
 PC_BLOCK_JACOBI = 0
 PC_MULTIGRID = 1
+ASM_FP32 = 0
+ASM_DOUBLE_FLOAT = 1
 RES_AX_F, RES_U, RES_U_P, RES_T = 0, 1, 2, 3
 
 NODE_BOUND, NODE_FREE_SURFACE, NODE_FIXED, NODE_DIRICHLET, NODE_FREE = 1, 2, 4, 8, 16
@@ -55,7 +57,7 @@ class Params(C.Structure):
         ("hbm_budget_bytes", C.c_size_t),
         ("inner_rel_tol", C.c_double),
         ("gamma", C.c_double),
-        ("preconditioner", C.c_int32), ("pad2", C.c_int32),
+        ("preconditioner", C.c_int32), ("assembly", C.c_int32),
         ("tau0", C.c_double), ("m_reg", C.c_double),
         ("heat_k", C.c_double), ("heat_cv", C.c_double), ("heat_h", C.c_double), ("heat_t_inf", C.c_double),
         ("heat_eps_rad", C.c_double), ("heat_fs_flags", C.c_int32), ("boussinesq", C.c_int32),

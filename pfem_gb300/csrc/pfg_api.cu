@@ -284,6 +284,7 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     if (params->heat_fs_flags & ~(PFG_HEAT_Q | PFG_HEAT_QH | PFG_HEAT_QR)) return PFG_ERR_INVALID;
     if (params->heat_residual != PFG_RES_T && params->heat_residual != PFG_RES_AX_F) return PFG_ERR_INVALID;
     if (params->heat_phase_change && !(params->heat_dt_melt > 0)) return PFG_ERR_INVALID;
+    if (params->assembly != PFG_ASM_FP32 && params->assembly != PFG_ASM_DOUBLE_FLOAT) return PFG_ERR_INVALID;
     pfg_ctx* c = new (std::nothrow) pfg_ctx();
     if (!c) return PFG_ERR_NOMEM;
     c->prm = *params;
@@ -322,7 +323,9 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt, &c->mx_scale,
                     &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force,
                     &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
-                    &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q};
+                    &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
+                    &c->pe_ptr, &c->pe_item, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
+                    &c->mx_rec, &c->mx_gdf, &c->wc_inst};
     wc_release_graphs(c);
     mg_release(c);
     mx_release_graph(c);

@@ -82,11 +82,16 @@ struct pfg_ctx {
     // node adjacency (sorted, includes the node) and the node-pair list
     pfg::DBuf nbr_ptr, nbr, pair_node;
     int P = 0;
+    // mixed PSPG: element list of each off-diagonal node pair (e*16 + i*4 + j, ascending e)
+    pfg::DBuf pe_ptr, pe_item;
     // CSR system
     pfg::DBuf row_ptr, col, val, val32, diag_pos, rhs;
     int64_t nnz = 0;
-    // element data: detJ, tau, gradN (SoA)
-    pfg::DBuf edata, edata_df;  // element data: FP64, and its double-float copy (mixed form)
+    // element data [detJ, tau, gradN, ksum] (structure of arrays): FP64, and in the mixed form
+    // double-float as two FP32 planes (high parts, then low parts).  Both are overwritten by the
+    // heat assembly (k_heat_geom stores the heat layout in them): every reader's own assembly
+    // rewrites them first, so no reader may carry them across a heat step.
+    pfg::DBuf edata, edata_df;
     // incompressible states
     pfg::DBuf q, q_prev, q_iter_prev, vbc;
     // Krylov workspace
@@ -121,14 +126,25 @@ struct pfg_ctx {
     std::vector<long long> h_inst_pairs;  // node pairs per instance
     // WC: FP64 element partials, per-node CFL quantities, captured step graphs [fixed, adaptive]
     pfg::DBuf wc_eld, wc_nodal;
+    // WC mixed form, batched: number of instances (1 = a single mesh) and per-instance
+    // [mu, mu sum_g w_g]; the node -> instance map shares node_inst with the PSPG form
+    int n_wc_inst = 1;
+    pfg::DBuf wc_inst;
     cudaGraphExec_t wc_graph[2] = {nullptr, nullptr};
     // mixed-precision PSPG: FP32 block inverses, instance tables (segments of nodes,
     // per-instance ints / doubles / FP32 Krylov scalars), reduction partials, counters
     pfg::DBuf binv32, node_inst, mx_seg, mx_ii, mx_id, mx_sc, mx_part, mx_cnt, mx_scale, mx_list;
+    // mixed PSPG assembly and residual: FP32 row scales, per-instance FP32 / double-float
+    // coefficients, double-float copies of the iterate (Dirichlet values substituted), of the
+    // previous velocities, of the temperatures and of the positions and iterate velocities (the
+    // element prep's inputs), and the element records of A_e x (one 32-byte record of d+1
+    // double-float values per element node)
+    pfg::DBuf mx_scale32, mx_f32, mx_xdf, mx_vpdf, mx_tdf, mx_rec, mx_gdf;
     int n_inst = 0, n_seg = 0;
     cudaGraphExec_t mx_graph[2] = {nullptr, nullptr};  // one chunk of BiCGSTAB iterations [FP32, FP64]
     std::vector<int> h_mx_ii;
     std::vector<double> h_mx_id;
+    std::vector<float> h_mx_f32;
     // surface tension: facets (dim x F nodes, element of each), the nodes their elements touch
     // with each one's (facet, local node of the facet's element) entries, and the force array
     // (dim x N, FP64 or FP32 by the kind's precision)
@@ -253,6 +269,7 @@ int wc_get_states(pfg_ctx* c, double* h);
 int wc_steps(pfg_ctx* c, double dt, int nsteps, pfg_step_status* st);
 int wc_enqueue(pfg_ctx* c, double dt, int nsteps);
 int wc_sync(pfg_ctx* c, pfg_step_status* st);
+int wc_sync_batch(pfg_ctx* c, pfg_step_status* st);
 int wc_next_dt(pfg_ctx* c, double* dt);
 int wc_mass(pfg_ctx* c, double* out);
 int wc_set_time(pfg_ctx* c, double time, double next_dt);
@@ -269,5 +286,6 @@ int wcm_get_states(pfg_ctx* c, double* h);
 int wcm_state_to_stage(pfg_ctx* c);
 int wcm_vbc_refresh(pfg_ctx* c);
 int wcm_next_dt(pfg_ctx* c);
+int wcm_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* mu);
 
 }  // namespace pfg

@@ -166,6 +166,43 @@ __global__ void k_fill_nbr(int N, int npe, int E, const int* __restrict__ conn, 
     }
 }
 
+// Position of m in n's sorted neighbour list nbr[b0, b1) (m must be there).
+__device__ __forceinline__ int nbr_rank(const int* __restrict__ nbr, int b0, int b1, int m) {
+    int lo = b0, hi = b1 - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (nbr[mid] < m) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo - b0;
+}
+
+// Element lists of the off-diagonal node pairs: pair p = (n, m), m != n, lists every element
+// containing both, ascending, as e * 16 + (local index of n) * 4 + (local index of m).  One
+// thread per node n owns the lists of n's pairs and walks n's sorted incidences, so each list
+// comes out in ascending element order.  FILL = false counts, FILL = true writes.
+template <bool FILL>
+__global__ void k_pair_items(int N, int npe, int E, const int* __restrict__ conn, const int* __restrict__ ne_ptr,
+                             const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
+                             const int* __restrict__ nbr_ptr, const int* __restrict__ nbr, int* __restrict__ cnt,
+                             const int* __restrict__ pe_ptr, int* __restrict__ pe_item) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const int b0 = nbr_ptr[n], b1 = nbr_ptr[n + 1];
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const int e = ne_elem[q];
+        const int i = ne_loc[q];
+        for (int j = 0; j < npe; ++j) {
+            if (j == i) continue;
+            const int p = b0 + nbr_rank(nbr, b0, b1, conn[(size_t)j * E + e]);
+            if (FILL)
+                pe_item[pe_ptr[p] + cnt[p]++] = (e << 4) | (i << 2) | j;
+            else
+                ++cnt[p];
+        }
+    }
+}
+
 __global__ void k_row_len(int N, int dim, const uint8_t* __restrict__ flags, const int* __restrict__ nbr_ptr,
                           int* __restrict__ len) {
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -322,6 +359,31 @@ int build_topology(pfg_ctx* c) {
                                                       ptr<int>(c->ne_elem), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr),
                                                       ptr<int>(c->pair_node));
     PFG_CHECK_LAUNCH(c);
+
+    if (c->prm.kind == PFG_KIND_INCOMP_PSPG && c->prm.precision == PFG_PREC_MIXED) {
+        // element lists of the off-diagonal node pairs (the FP32 pair assembly)
+        if (E >= (1 << 27)) {
+            cleanup();
+            return fail(c, PFG_ERR_UNSUPPORTED, "too many elements for the pair element lists");
+        }
+        TRY(ensure(c, cnt, sizeof(int) * (size_t)std::max(c->P, 1)));
+        TRY(ensure(c, c->pe_ptr, sizeof(int) * ((size_t)c->P + 1)));
+        PFG_CUDA(c, cudaMemsetAsync(cnt.p, 0, sizeof(int) * (size_t)c->P, c->stream));
+        k_pair_items<false><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
+                                                                   ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
+                                                                   ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
+                                                                   nullptr, nullptr);
+        PFG_CHECK_LAUNCH(c);
+        TRY(scan_exclusive(c, ptr<int>(cnt), ptr<int>(c->pe_ptr), c->P, tmp));
+        const long long items = (long long)E * npe * (npe - 1);
+        TRY(ensure(c, c->pe_item, sizeof(int) * (size_t)std::max<long long>(items, 1)));
+        PFG_CUDA(c, cudaMemsetAsync(cnt.p, 0, sizeof(int) * (size_t)c->P, c->stream));
+        k_pair_items<true><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
+                                                                  ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
+                                                                  ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
+                                                                  ptr<int>(c->pe_ptr), ptr<int>(c->pe_item));
+        PFG_CHECK_LAUNCH(c);
+    }
 
     if (c->prm.kind == PFG_KIND_INCOMP_PSPG) {
         const long long R = (long long)(dim + 1) * N;

@@ -263,7 +263,8 @@ __device__ __forceinline__ void pspg_node_rhs(int n, int N, int E, const int* __
 
 // Writes the (n, m) block into the CSR values with the identity rows and the Dirichlet column
 // elimination of m_applyBCPSPG (:108-128, :216-229); the eliminated entries' share of the
-// right-hand side goes to rhs.  val32, when non-null, receives the FP32 rounding of each value.
+// right-hand side goes to rhs (when non-null).  val32, when non-null, receives the FP32 rounding
+// of each value.
 template <int DIM>
 __device__ __forceinline__ void pspg_write_block(int n, int m, int N, int deg, int rank, uint8_t fn, uint8_t fm,
                                                  const int* __restrict__ row_ptr, const double (&acc)[DIM + 1][DIM + 1],
@@ -289,7 +290,7 @@ __device__ __forceinline__ void pspg_write_block(int n, int m, int N, int deg, i
             // Dirichlet column elimination (:216-229): value moved to the RHS, entry kept at 0
             if (mdir && f2 < DIM && !(m == n && f1 == f2)) {
                 const double vb = vbc[(size_t)f2 * N + m];
-                if (vb != 0.0) atomicAdd(rhs + r, -a * vb);
+                if (vb != 0.0 && rhs) atomicAdd(rhs + r, -a * vb);
                 a = 0.0;
             }
             val[rp + f2 * deg + rank] = a;

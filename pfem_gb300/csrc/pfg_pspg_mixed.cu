@@ -42,7 +42,8 @@ constexpr int SPMV_BLOCK = 256;  // threads of the segment SpMV kernels
 
 // per-instance int fields
 // I_MODE: precision of the correction solves (0 FP32, 1 FP64); I_ROLL: undo the last sweep
-enum : int { I_B0 = 0, I_B1, I_N0, I_N1, I_ACTIVE, I_STATUS, I_IT, I_KIT, I_TICKET, I_MODE, I_ROLL, I_COUNT = 12 };
+// I_M64: the FP64 CSR values of the instance are current for this assembly
+enum : int { I_B0 = 0, I_B1, I_N0, I_N1, I_ACTIVE, I_STATUS, I_IT, I_KIT, I_TICKET, I_MODE, I_ROLL, I_M64, I_COUNT = 12 };
 // correction-solve precision of an instance
 enum : int { MODE_FP32 = 0, MODE_FP64 = 2 };
 // per-instance double fields
@@ -69,7 +70,10 @@ struct Mx {
 struct MxConst {
     double refSize, sumw;
     PspgTables t;
-    DF mm_df[4][4], s_df[4], ref_df;  // double-float copies of the tables and refSize
+    // double-float copies of the tables, refSize, sum_g w_g, 1/pi, gravity and the Boussinesq
+    // factors 1 + alpha Tr and alpha; FP32 copies for the FP32 assembly
+    DF mm_df[4][4], s_df[4], ref_df, hsum_df, inv_pi_df, g_df[3], bq_c0, bq_alpha;
+    float mm32[4][4], s32[4], ref32;
     BoussArgs bq;
     double rtol, atol, eta, min_res;
     int max_iter;
@@ -104,7 +108,17 @@ MxConst mx_const(pfg_ctx* c) {
         for (int j = 0; j < 4; ++j) k.mm_df[i][j] = split(g.MM[i][j]);
     }
     k.ref_df = split(g.refSize);
+    k.hsum_df = split(g.sumw);
+    k.inv_pi_df = split(1.0 / M_PI);
+    for (int f = 0; f < 3; ++f) k.g_df[f] = split(c->prm.gravity[f]);
     k.bq = boussinesq_args(c);
+    k.bq_c0 = split(1 + k.bq.alpha * k.bq.Tr);
+    k.bq_alpha = split(k.bq.alpha);
+    for (int i = 0; i < 4; ++i) {
+        k.s32[i] = (float)g.s[i];
+        for (int j = 0; j < 4; ++j) k.mm32[i][j] = (float)g.MM[i][j];
+    }
+    k.ref32 = (float)g.refSize;
     k.rtol = c->prm.krylov_rel_tol;
     k.atol = c->prm.krylov_abs_tol;
     k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-4;
@@ -164,25 +178,52 @@ __device__ __forceinline__ bool inst_reduce(T (&v)[NV], int b, int b0, int b1, T
     return true;
 }
 
-// ---- assembly (FP64 values, FP32 copy) -----------------------------------------------------
+// ---- assembly --------------------------------------------------------------------------------
+//
+// Per Picard iteration (MomContEquationPSPG.inl:6-235 at the current iterate):
+//   k_mx_prep_df element: geometry (Element.cpp:15-135), tau (:237-259) and the K factor in
+//                double-float on the FP32 pipe (k_mx_prep: the same in FP64, for Bingham
+//                fluids), stored as double-float in two FP32 planes (high parts, low parts);
+//   k_mx_vprep   node: double-float copies of the previous velocities (and temperatures);
+//   k_mx_node    node: its own (d+1)^2 block, its right-hand side in double-float, the node
+//                boundary conditions, the row scales, the block inverses, the scaled diagonal
+//                block of the FP32 system and ||b||^2 per instance;
+//   k_mx_asm32   node pair: the off-diagonal blocks of the scaled FP32 system from the pair's
+//                element list.
+// The FP32 system only steers the correction solves; the refinement residual below is
+// evaluated matrix-free in double-float, so it alone decides the solution.  The FP64 CSR
+// values are assembled (k_mx_pairs, double-float) only for instances whose correction solves
+// fell back to FP64.
 
-__device__ __forceinline__ PspgCoef inst_coef_d(const double* id, double sumw, double refSize) {
-    PspgCoef k;
-    k.rho = id[D_RHO];
-    k.dt = id[D_DT];
-    k.refSize = refSize;
-    k.mu_sum = id[D_MU] * sumw;
-    k.l_sum = sumw / id[D_RHO];
-    k.h_sum = sumw;
-    return k;
+// Per-instance coefficients as double-float pairs: rho, 1/dt, sum_g w_g / rho, rho/dt,
+// 4 mu / rho and mu sum_g w_g (the Newtonian K factor).
+enum : int { F_RHO = 0, F_INVDT = 2, F_LSUM = 4, F_CM = 6, F_MU4R = 8, F_KSUM = 10, F_COUNT = 12 };
+
+__device__ __forceinline__ DF inst_df(const float* f32, int inst, int which) {
+    return DF{f32[inst * F_COUNT + which], f32[inst * F_COUNT + which + 1]};
 }
 
+// Element data as double-float planes: value v of element e is h[v E + e] + l[v E + e].
+struct EdPlanes {
+    const float* h;
+    const float* l;
+    int E;
+    __device__ __forceinline__ DF df(int v, int e) const {
+        const size_t o = (size_t)v * E + e;
+        return DF{__ldg(h + o), __ldg(l + o)};
+    }
+    __device__ __forceinline__ float f(int v, int e) const { return __ldg(h + (size_t)v * E + e); }
+};
+
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
+
 // Geometry (Element.cpp:15-135) and tau (MomContEquationPSPG.inl:237-259) of the elements of
-// active instances: [detJ, tau, gradN] in FP64 (structure of arrays, stride E).
+// active instances in FP64, with the Bingham K factor: [detJ, tau, gradN, ksum] stored as
+// double-float planes.
 template <int DIM>
 __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
                           const double* __restrict__ q_iter, Mx m, double refSize, ViscArgs va,
-                          double* __restrict__ ed, DF* __restrict__ edf) {
+                          float* __restrict__ eh, float* __restrict__ el) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -210,253 +251,194 @@ __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const doub
     U /= (DIM + 1);
     const double a = 2 / dt, b = 2 * U / h, c = 4 * mu / (h * h * rho);
     const double tau = 1 / sqrt(a * a + b * b + 9 * c * c);
-    ed[e] = g.detJ;
-    ed[(size_t)E + e] = tau;
+    double v[ed_count<DIM>()];
+    v[0] = g.detJ;
+    v[1] = tau;
 #pragma unroll
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
-        for (int i = 0; i <= DIM; ++i) ed[(size_t)(2 + f * (DIM + 1) + i) * E + e] = G[f][i];
-    ed[(size_t)ed_ksum<DIM>() * E + e] = k_sum<DIM>(va, mu, G, q_iter, N, nd);
-    // double-float copy for the pair assembly (FP64 conversions once per element, not per pair)
+        for (int i = 0; i <= DIM; ++i) v[2 + f * (DIM + 1) + i] = G[f][i];
+    v[ed_ksum<DIM>()] = k_sum<DIM>(va, mu, G, q_iter, N, nd);
 #pragma unroll
-    for (int v = 0; v < ed_count<DIM>(); ++v) edf[(size_t)v * E + e] = df_from(ed[(size_t)v * E + e]);
+    for (int k = 0; k < ed_count<DIM>(); ++k) {
+        const DF d = df_from(v[k]);
+        eh[(size_t)k * E + e] = d.h;
+        el[(size_t)k * E + e] = d.l;
+    }
 }
 
-// Right-hand side of the nodes of active instances (element doublets + node BCs).
+// Double-float copies of the positions and the iterate's velocities (inputs of k_mx_prep_df).
 template <int DIM>
-__global__ void k_mx_rhs(int N, int E, const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
-                         const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
-                         const double* __restrict__ ed, const uint8_t* __restrict__ flags,
-                         const double* __restrict__ q_prev, const double* __restrict__ vbc, Mx m, MxConst k,
-                         double* __restrict__ rhs, const double* __restrict__ fst) {
+__global__ void k_mx_gprep(int N, const double* __restrict__ pos, const double* __restrict__ q_iter, Mx m,
+                           DF* __restrict__ gdf) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
-    const int inst = m.node_inst[n];
-    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
-    const PspgCoef cf = inst_coef_d(m.id + inst * D_COUNT, k.sumw, k.refSize);
-    double bv[DIM], bp;
-    pspg_node_rhs<DIM>(n, N, E, ne_ptr, ne_elem, ne_loc, conn, ed, flags[n], q_prev, vbc, true, cf, k.t, fst, k.bq, bv, bp);
+    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
 #pragma unroll
-    for (int f = 0; f < DIM; ++f) rhs[(size_t)f * N + n] = bv[f];
-    rhs[(size_t)DIM * N + n] = bp;
+    for (int f = 0; f < DIM; ++f) {
+        gdf[(size_t)f * N + n] = df_from(pos[(size_t)f * N + n]);
+        gdf[(size_t)(DIM + f) * N + n] = df_from(q_iter[(size_t)f * N + n]);
+    }
 }
 
-// Block (n, m) like pspg_pair_block (same gather, element order and expressions), evaluated in
-// double-float on the FP32 pipe from the double-float element data; returned in FP64.  On
-// GB300 the FP64 evaluation is bound by the FP64 pipe (87% busy, 1/64 of the FP32 rate);
-// double-float carries ~48 bits, so the values agree with the FP64 evaluation to ~1e-14 of
-// the row scale.
-struct PairDF {
-    DF rho, inv_dt, refSize, l_sum;
-};
-
+// k_mx_prep in double-float on the FP32 pipe for Newtonian fluids (the FP64 element prep is
+// bound by the FP64 pipe, 1/64 of the FP32 rate on GB300): the same quantities from the same
+// closed forms (Element.cpp:15-135, MomContEquationPSPG.inl:237-259), each operation an
+// error-free or double-float one, so the element data agree with the FP64 ones to ~1e-14.
 template <int DIM>
-__device__ __forceinline__ void pspg_pair_block_df(int n, int m, int E, const int* __restrict__ ne_ptr,
-                                                   const int* __restrict__ ne_elem,
-                                                   const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
-                                                   const DF* __restrict__ edf, const PairDF& k,
-                                                   const DF (&MM)[4][4], const DF (&S)[4],
-                                                   double (&out)[DIM + 1][DIM + 1]) {
+__global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const DF* __restrict__ gdf,
+                             const float* __restrict__ f32, Mx m, DF ref_df, DF inv_pi, float* __restrict__ eh,
+                             float* __restrict__ el) {
     constexpr int NPE = DIM + 1;
-    DF acc[NPE][NPE];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int nd[NPE];
+    load_nodes<DIM>(conn, E, e, nd);
+    const int inst = m.node_inst[nd[0]];
+    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    DF X[NPE][DIM];
 #pragma unroll
-    for (int a = 0; a < NPE; ++a)
+    for (int k = 0; k < NPE; ++k)
 #pragma unroll
-        for (int b = 0; b < NPE; ++b) acc[a][b] = DF{0.0f, 0.0f};
-    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-        const int e = ne_elem[q];
-        int j = -1;
+        for (int f = 0; f < DIM; ++f) X[k][f] = gdf[(size_t)f * N + nd[k]];
+    DF J[DIM][DIM];
 #pragma unroll
-        for (int jj = 0; jj < NPE; ++jj)
-            if (__ldg(conn + (size_t)jj * E + e) == m) j = jj;
-        if (j < 0) continue;
-        const int i = ne_loc[q];
-        const DF detJ = edf[e];
-        const DF tau = edf[(size_t)E + e];
-        const DF ae = df_mul(detJ, k.refSize);
-        DF gi[DIM], gj[DIM];
+    for (int r = 0; r < DIM; ++r)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) J[r][c] = df_sub(X[c + 1][r], X[0][r]);
+    DF det, cof[DIM][DIM];  // invJ = cof / det
+    if constexpr (DIM == 2) {
+        det = df_sub(df_mul(J[0][0], J[1][1]), df_mul(J[1][0], J[0][1]));
+        cof[0][0] = J[1][1];
+        cof[0][1] = df_neg(J[0][1]);
+        cof[1][0] = df_neg(J[1][0]);
+        cof[1][1] = J[0][0];
+    } else {
+        det = df_add(df_add(df_mul(df_mul(J[0][0], J[1][1]), J[2][2]), df_mul(df_mul(J[0][1], J[1][2]), J[2][0])),
+                     df_mul(df_mul(J[0][2], J[1][0]), J[2][1]));
+        det = df_sub(det, df_add(df_add(df_mul(df_mul(J[2][0], J[1][1]), J[0][2]),
+                                        df_mul(df_mul(J[2][1], J[1][2]), J[0][0])),
+                                 df_mul(df_mul(J[2][2], J[1][0]), J[0][1])));
+        auto c2 = [&](int a, int b, int c, int d) { return df_sub(df_mul(J[a][b], J[c][d]), df_mul(J[a][d], J[c][b])); };
+        cof[0][0] = c2(1, 1, 2, 2);
+        cof[0][1] = c2(2, 1, 0, 2);
+        cof[0][2] = c2(0, 1, 1, 2);
+        cof[1][0] = c2(2, 0, 1, 2);
+        cof[1][1] = c2(0, 0, 2, 2);
+        cof[1][2] = c2(1, 0, 0, 2);
+        cof[2][0] = c2(1, 0, 2, 1);
+        cof[2][1] = c2(2, 0, 0, 1);
+        cof[2][2] = c2(0, 0, 1, 1);
+    }
+    const DF inv_det = df_div(DF{1.0f, 0.0f}, det);
+    DF G[DIM][NPE];
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) {
+        DF sum{0.0f, 0.0f};
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            G[f][k + 1] = df_mul(cof[k][f], inv_det);
+            sum = df_add(sum, G[f][k + 1]);
+        }
+        G[f][0] = df_neg(sum);
+    }
+    // tau (m_computeTauPSPG): h = sqrt(refSize detJ / pi), U = mean nodal |v| of the iterate
+    const DF h = df_sqrt(df_mul(df_mul(ref_df, det), inv_pi));
+    DF U{0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < NPE; ++k) {
+        DF u2{0.0f, 0.0f};
 #pragma unroll
         for (int f = 0; f < DIM; ++f) {
-            gi[f] = edf[(size_t)(2 + f * NPE + i) * E + e];
-            gj[f] = edf[(size_t)(2 + f * NPE + j) * E + e];
+            const DF v = gdf[(size_t)(DIM + f) * N + nd[k]];
+            u2 = df_add(u2, df_mul(v, v));
         }
-        DF dot = df_mul(gi[0], gj[0]);
+        U = df_add(U, df_sqrt(u2));
+    }
+    U = df_div(U, DF{(float)NPE, 0.0f});
+    const DF inv_dt = inst_df(f32, inst, F_INVDT);
+    const DF a = df_add(inv_dt, inv_dt);
+    const DF b = df_div(df_add(U, U), h);
+    const DF c = df_div(inst_df(f32, inst, F_MU4R), df_mul(h, h));
+    const DF nine{9.0f, 0.0f};
+    const DF tau = df_div(DF{1.0f, 0.0f}, df_sqrt(df_add(df_add(df_mul(a, a), df_mul(b, b)), df_mul(nine, df_mul(c, c)))));
+    auto put = [&](int v, DF d) {
+        eh[(size_t)v * E + e] = d.h;
+        el[(size_t)v * E + e] = d.l;
+    };
+    put(0, det);
+    put(1, tau);
 #pragma unroll
-        for (int f = 1; f < DIM; ++f) dot = df_add(dot, df_mul(gi[f], gj[f]));
-        const DF mij = df_mul(k.inv_dt, df_mul(df_mul(k.rho, MM[i][j]), ae));
-        const DF kf = df_mul(ae, edf[(size_t)ed_ksum<DIM>() * E + e]);
+    for (int f = 0; f < DIM; ++f)
 #pragma unroll
-        for (int f1 = 0; f1 < DIM; ++f1) {
+        for (int i = 0; i < NPE; ++i) put(2 + f * NPE + i, G[f][i]);
+    put(ed_ksum<DIM>(), inst_df(f32, inst, F_KSUM));
+}
+
+// Double-float copies of the previous velocities and (Boussinesq) the temperatures.
+template <int DIM>
+__global__ void k_mx_vprep(int N, const double* __restrict__ q_prev, const double* __restrict__ T, Mx m,
+                           DF* __restrict__ vp, DF* __restrict__ tdf) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
 #pragma unroll
-            for (int f2 = 0; f2 < DIM; ++f2) {
-                const DF g2 = df_mul(gi[f2], gj[f1]);
-                const DF kv = df_mul(kf, f1 == f2 ? df_add(dot, g2) : g2);
-                acc[f1][f2] = df_add(acc[f1][f2], f1 == f2 ? df_add(mij, kv) : kv);
-            }
-            acc[f1][DIM] = df_add(acc[f1][DIM], df_neg(df_mul(df_mul(ae, S[j]), gi[f1])));
-        }
-        const DF ctau = df_mul(tau, k.inv_dt);
+    for (int f = 0; f < DIM; ++f) vp[(size_t)f * N + n] = df_from(q_prev[(size_t)f * N + n]);
+    if (T) tdf[n] = df_from(T[n]);
+}
+
+// One element's share of block (i, j) of the system before boundary conditions, added to acc:
+// the expressions of pspg_pair_block in double-float.
+template <int DIM>
+__device__ __forceinline__ void pair_item_df(const EdPlanes& ed, int e, int i, int j, DF rho, DF inv_dt, DF l_sum,
+                                             const MxConst& k, DF (&acc)[DIM + 1][DIM + 1]) {
+    constexpr int NPE = DIM + 1;
+    const DF detJ = ed.df(0, e);
+    const DF tau = ed.df(1, e);
+    const DF ae = df_mul(detJ, k.ref_df);
+    DF gi[DIM], gj[DIM];
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) {
+        gi[f] = ed.df(2 + f * NPE + i, e);
+        gj[f] = ed.df(2 + f * NPE + j, e);
+    }
+    DF dot = df_mul(gi[0], gj[0]);
+#pragma unroll
+    for (int f = 1; f < DIM; ++f) dot = df_add(dot, df_mul(gi[f], gj[f]));
+    const DF mij = df_mul(inv_dt, df_mul(df_mul(rho, k.mm_df[i][j]), ae));
+    const DF kf = df_mul(ae, ed.df(ed_ksum<DIM>(), e));
+#pragma unroll
+    for (int f1 = 0; f1 < DIM; ++f1) {
 #pragma unroll
         for (int f2 = 0; f2 < DIM; ++f2) {
-            const DF c1 = df_mul(ctau, df_mul(df_mul(ae, gi[f2]), S[j]));
-            const DF c2 = df_mul(df_mul(ae, S[i]), gj[f2]);
-            acc[DIM][f2] = df_add(acc[DIM][f2], df_add(c1, c2));
+            const DF g2 = df_mul(gi[f2], gj[f1]);
+            const DF kv = df_mul(kf, f1 == f2 ? df_add(dot, g2) : g2);
+            acc[f1][f2] = df_add(acc[f1][f2], f1 == f2 ? df_add(mij, kv) : kv);
         }
-        acc[DIM][DIM] = df_add(acc[DIM][DIM], df_mul(tau, df_mul(df_mul(ae, k.l_sum), dot)));
+        acc[f1][DIM] = df_add(acc[f1][DIM], df_neg(df_mul(df_mul(ae, k.s_df[j]), gi[f1])));
     }
+    const DF ctau = df_mul(tau, inv_dt);
 #pragma unroll
-    for (int a = 0; a < NPE; ++a)
-#pragma unroll
-        for (int b = 0; b < NPE; ++b) out[a][b] = df_to(acc[a][b]);
+    for (int f2 = 0; f2 < DIM; ++f2) {
+        const DF c1 = df_mul(ctau, df_mul(df_mul(ae, gi[f2]), k.s_df[j]));
+        const DF c2 = df_mul(df_mul(ae, k.s_df[i]), gj[f2]);
+        acc[DIM][f2] = df_add(acc[DIM][f2], df_add(c1, c2));
+    }
+    acc[DIM][DIM] = df_add(acc[DIM][DIM], df_mul(tau, df_mul(df_mul(ae, l_sum), dot)));
 }
 
-// FP64 matrix values of active instances, one thread per node pair: the same gather, element
-// order and Dirichlet elimination as the FP64 path, the block evaluated in double-float.
-template <int DIM>
-__global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const int* __restrict__ pair_node,
-                                                    const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
-                                                    const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
-                                                    const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
-                                                    const DF* __restrict__ edf, const uint8_t* __restrict__ flags,
-                                                    const int* __restrict__ row_ptr, double* __restrict__ val,
-                                                    const double* __restrict__ vbc, double* __restrict__ rhs, Mx m,
-                                                    MxConst k) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P) return;
-    const int n = pair_node[t];
-    const int inst = m.node_inst[n];
-    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
-    const int b0 = nbr_ptr[n];
-    const int deg = nbr_ptr[n + 1] - b0;
-    const int rank = t - b0;
-    const int mm = nbr[t];
-    const uint8_t fn = flags[n];
-    if (fn & F_FREE) {
-#pragma unroll
-        for (int f = 0; f <= DIM; ++f) val[row_ptr[n + f * N]] = 1.0;
-        return;
-    }
-    PairDF kd;
-    {
-        const double* id = m.id + inst * D_COUNT;
-        kd.rho = df_from(id[D_RHO]);
-        kd.inv_dt = df_from(1 / id[D_DT]);
-        kd.refSize = k.ref_df;
-        kd.l_sum = df_from(k.sumw / id[D_RHO]);
-    }
-    double acc[DIM + 1][DIM + 1];
-    pspg_pair_block_df<DIM>(n, mm, E, ne_ptr, ne_elem, ne_loc, conn, edf, kd, k.mm_df, k.s_df, acc);
-    pspg_write_block<DIM>(n, mm, N, deg, rank, fn, flags[mm], row_ptr, acc, true, vbc, rhs, val, nullptr);
-}
-
-// ---- FP32 system: symmetric diagonal scaling ----------------------------------------------
-//
-// The correction solves run on S A S with S = diag(|a_rr|^-1/2).  Unscaled, a PSPG residual
-// has pressure rows some four orders of magnitude below its velocity rows, so FP32 dot
-// products drop the pressure part and the correction solves stall on fine meshes; scaled,
-// every row has a unit diagonal.  The FP64 residual and the solution stay unscaled.
-
-template <int DIM>
-__global__ void k_mx_rowscale(int N, const int* __restrict__ diag, const double* __restrict__ val, Mx m,
-                              double* __restrict__ scale) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
-#pragma unroll
-    for (int f = 0; f <= DIM; ++f) {
-        const int r = n + f * N;
-        const double d = fabs(val[diag[r]]);
-        scale[r] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
-    }
-}
-
-// The FP32 scaled system S A S in node-pair blocks: blk[p][f1][f2] = FP32(s_(n,f1) a s_(m,f2))
-// for the pair p = (n, m) of the adjacency (p = nbr_ptr[n] + rank of m), one thread per pair.
-// Identity rows keep their (scaled) diagonal and zeros elsewhere.  One contiguous (d+1)^2 block
-// per neighbour lets the FP32 products load it with vector loads and no per-value index.
-template <int DIM>
-__global__ void k_mx_scale_bsr(int P, int N, const int* __restrict__ pair_node, const int* __restrict__ nbr_ptr,
-                               const int* __restrict__ nbr, const int* __restrict__ rp,
-                               const double* __restrict__ val, const double* __restrict__ scale, Mx m,
-                               float* __restrict__ blk, uint16_t* __restrict__ blk16) {
-    constexpr int B = DIM + 1;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    const int n = pair_node[p];
-    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
-    const int mm = nbr[p];
-    const int b0 = nbr_ptr[n];
-    const int deg = nbr_ptr[n + 1] - b0, rank = p - b0;
-    float out[B * B];
-#pragma unroll
-    for (int f1 = 0; f1 < B; ++f1) {
-        const int r = n + f1 * N;
-        const int r0 = rp[r];
-        const double sr = scale[r];
-        const bool full = rp[r + 1] - r0 > 1;
-#pragma unroll
-        for (int f2 = 0; f2 < B; ++f2) {
-            double a = 0.0;
-            if (full)
-                a = sr * val[r0 + f2 * deg + rank] * scale[mm + f2 * N];
-            else if (f1 == f2 && mm == n)
-                a = sr * val[r0] * sr;
-            out[f1 * B + f2] = (float)a;
-        }
-    }
-    float* dst = blk + (size_t)p * B * B;
-#pragma unroll
-    for (int e = 0; e < B * B; ++e) dst[e] = out[e];
-    if (blk16) {
-        uint16_t* d16 = blk16 + (size_t)p * bf16_stride<B>();
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1)
-#pragma unroll
-            for (int f2 = 0; f2 < 4; ++f2)
-                d16[f1 * 4 + f2] = f2 < B ? __bfloat16_as_ushort(__float2bfloat16_rn(out[f1 * B + f2])) : (uint16_t)0;
-    }
-}
-
-// ---- node-block Jacobi preconditioner --------------------------------------------------------
-
-// Inverse of each node's (dim+1)x(dim+1) diagonal block, computed in FP64: stored as is for
-// the FP64 correction solves and, for the scaled system S A S, in FP32.  The pressure entry of a PSPG block is a small stabilisation term next to the
-// divergence couplings, so the block's Schur complement cancels heavily: inverted in FP32 the
-// preconditioner loses its pressure part on fine meshes and BiCGSTAB breaks down.
-template <int DIM>
-__global__ void k_mx_binv(int N, const int* __restrict__ rp, const double* __restrict__ val,
-                          const int* __restrict__ diag, const double* __restrict__ scale, float* __restrict__ binv,
-                          double* __restrict__ binv64, Mx m) {
-    constexpr int B = DIM + 1;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
+// Inverse of a (d+1)x(d+1) block by Gauss-Jordan elimination with partial pivoting in FP64; a
+// singular block falls back to the inverse of its diagonal.
+template <int B>
+__device__ __forceinline__ void block_inverse(const double (&a0)[B][B], double (&inv)[B][B]) {
     double a[B][2 * B];
 #pragma unroll
-    for (int f1 = 0; f1 < B; ++f1) {
-        const int r = n + f1 * N;
-        const int dp = diag[r];
-        const int b0 = rp[r], len = rp[r + 1] - b0;
+    for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2) {
-            a[f1][f2] = 0;
+            a[f1][f2] = a0[f1][f2];
             a[f1][B + f2] = (f1 == f2) ? 1.0 : 0.0;
         }
-        if (len == 1) {
-            a[f1][f1] = val[dp];
-        } else {
-            const int deg = len / B;
-            const int self = dp - b0 - f1 * deg;
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) a[f1][f2] = val[b0 + f2 * deg + self];
-        }
-    }
-    double sn[B];
-#pragma unroll
-    for (int f = 0; f < B; ++f) sn[f] = scale[n + f * N];
-    double dg[B];
-#pragma unroll
-    for (int f = 0; f < B; ++f) dg[f] = a[f][f];
     bool ok = true;
 #pragma unroll
     for (int kk = 0; kk < B; ++kk) {
@@ -469,17 +451,20 @@ __global__ void k_mx_binv(int N, const int* __restrict__ rp, const double* __res
                 piv = i;
             }
         if (best == 0.0) ok = false;
-        if (piv != kk) {
+        // row swap through compile-time indices (keeps the block in registers)
 #pragma unroll
-            for (int j = 0; j < 2 * B; ++j) {
-                const double t = a[kk][j];
-                a[kk][j] = a[piv][j];
-                a[piv][j] = t;
+        for (int i = kk + 1; i < B; ++i)
+            if (i == piv) {
+#pragma unroll
+                for (int j = 0; j < 2 * B; ++j) {
+                    const double t = a[kk][j];
+                    a[kk][j] = a[i][j];
+                    a[i][j] = t;
+                }
             }
-        }
-        const double inv = ok ? 1.0 / a[kk][kk] : 0.0;
+        const double inv_p = ok ? 1.0 / a[kk][kk] : 0.0;
 #pragma unroll
-        for (int j = 0; j < 2 * B; ++j) a[kk][j] *= inv;
+        for (int j = 0; j < 2 * B; ++j) a[kk][j] *= inv_p;
 #pragma unroll
         for (int i = 0; i < B; ++i) {
             if (i == kk) continue;
@@ -491,33 +476,526 @@ __global__ void k_mx_binv(int N, const int* __restrict__ rp, const double* __res
 #pragma unroll
     for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
-        for (int f2 = 0; f2 < B; ++f2) {
-            double v = a[f1][B + f2];
-            if (!ok) v = (f1 == f2) ? (dg[f1] != 0.0 ? 1.0 / dg[f1] : 1.0) : 0.0;
-            // (S B S)^-1 = S^-1 B^-1 S^-1
-            binv64[(size_t)(f1 * B + f2) * N + n] = v;
-            binv[(size_t)(f1 * B + f2) * N + n] = (float)(v / (sn[f1] * sn[f2]));
-        }
+        for (int f2 = 0; f2 < B; ++f2)
+            inv[f1][f2] = ok ? a[f1][B + f2]
+                             : ((f1 == f2) ? (a0[f1][f1] != 0.0 ? 1.0 / a0[f1][f1] : 1.0) : 0.0);
 }
 
-// ---- FP64 residual -------------------------------------------------------------------------
+__device__ __forceinline__ int self_rank(const int* __restrict__ nbr, int b0, int b1, int n) {
+    int lo = b0, hi = b1 - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (nbr[mid] < n) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo - b0;
+}
 
-// Row r of the FP64 matrix times x over G lanes (valid on lane 0 of the group).
-template <int G>
-__device__ __forceinline__ double row_dot64(int r, bool act, const int* __restrict__ rp, const int* __restrict__ col,
-                                            const double* __restrict__ val, const double* __restrict__ x, int lane) {
-    const int b = act ? rp[r] : 0, e = act ? rp[r + 1] : 0;
-    double s = 0;
-    for (int kk = b + lane; kk < e; kk += G) s += val[kk] * x[col[kk]];
+template <int B>
+__device__ __forceinline__ void store_block32(float* __restrict__ blk, uint16_t* __restrict__ blk16, int p,
+                                              const float (&out)[B * B]) {
+    if constexpr (B == 4) {
+        float4* d4 = reinterpret_cast<float4*>(blk + (size_t)p * 16);
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
-    return s;
+        for (int r = 0; r < 4; ++r) d4[r] = make_float4(out[4 * r], out[4 * r + 1], out[4 * r + 2], out[4 * r + 3]);
+    } else {
+        float* dst = blk + (size_t)p * B * B;
+#pragma unroll
+        for (int e = 0; e < B * B; ++e) dst[e] = out[e];
+    }
+    if (blk16) {
+        uint16_t h[B * 4];
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < 4; ++f2)
+                h[f1 * 4 + f2] = f2 < B ? __bfloat16_as_ushort(__float2bfloat16_rn(out[f1 * B + f2])) : (uint16_t)0;
+        uint2* d2 = reinterpret_cast<uint2*>(blk16 + (size_t)p * bf16_stride<B>());
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+            d2[f1] = make_uint2((uint32_t)h[f1 * 4] | ((uint32_t)h[f1 * 4 + 1] << 16),
+                                (uint32_t)h[f1 * 4 + 2] | ((uint32_t)h[f1 * 4 + 3] << 16));
+    }
 }
 
-// r = b - A x over the rows of the segment's nodes with the FP64 matrix (the refinement
-// residual; right after a re-assembly it is also the Picard "Ax_f" residual, :366-371).
-// Seeds the instance's next correction solve (rhat = r, p = v = 0): FP32 on the scaled system
-// (r32 = S r) or, for an instance in FP64 mode, FP64 on A.  `kind`:
+// Node kernel, one block per segment, one thread per node: the node's diagonal block (in the
+// FP32 system's arithmetic: FP32, or double-float with DFA) and right-hand side (double-float)
+// in element order, with the expressions of pspg_pair_block and pspg_node_rhs; then
+// m_applyBCPSPG's node conditions (:189-232; identity rows :108-128, the Dirichlet columns of
+// the node's own block zeroed), the row scales S = |a_rr|^-1/2, the block inverses (FP64, and
+// scaled in FP32), the scaled diagonal block of the FP32 system and ||b||^2 of each instance
+// (the relative tolerance of its linear solves).
+template <int DIM, bool DFA>
+__global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* __restrict__ ne_ptr,
+                                                const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
+                                                const int* __restrict__ conn, EdPlanes ed,
+                                                const uint8_t* __restrict__ flags, const DF* __restrict__ vp,
+                                                const DF* __restrict__ tdf, const double* __restrict__ q_prev,
+                                                const double* __restrict__ vbc, const double* __restrict__ fst,
+                                                const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                                                const float* __restrict__ f32, MxConst k, double* __restrict__ rhs,
+                                                double* __restrict__ scale, float* __restrict__ scale32,
+                                                double* __restrict__ binv64, float* __restrict__ binv32,
+                                                float* __restrict__ blk, uint16_t* __restrict__ blk16) {
+    constexpr int B = DIM + 1, NPE = DIM + 1;
+    __shared__ double sh[32];
+    const int sb = blockIdx.x;
+    const int inst = m.seg[3 * sb];
+    int* ii = m.ii + inst * I_COUNT;
+    if (!ii[I_ACTIVE]) return;
+    const int n = m.seg[3 * sb + 1] + threadIdx.x;
+    const bool act = n < m.seg[3 * sb + 2];
+    double bb = 0;
+    if (act) {
+        if (n == ii[I_N0]) ii[I_M64] = 0;  // the FP64 CSR values (if any) predate this assembly
+        const uint8_t fl = flags[n];
+        const DF rho = inst_df(f32, inst, F_RHO), inv_dt = inst_df(f32, inst, F_INVDT);
+        const DF l_sum = inst_df(f32, inst, F_LSUM);
+        DF A[DFA ? B : 1][DFA ? B : 1], bv[DIM], bp = DF{0.0f, 0.0f};
+        float A32[B][B];
+#pragma unroll
+        for (int a = 0; a < B; ++a)
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                if constexpr (DFA) A[a][b] = DF{0.0f, 0.0f};
+                A32[a][b] = 0.0f;
+            }
+        const float cm32 = f32[inst * F_COUNT + F_CM], ct32 = f32[inst * F_COUNT + F_INVDT];
+        const float l32 = f32[inst * F_COUNT + F_LSUM];
+#pragma unroll
+        for (int f = 0; f < DIM; ++f) bv[f] = DF{0.0f, 0.0f};
+        for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+            const int e = ne_elem[q];
+            const int i = ne_loc[q];
+            int nd[NPE];
+            load_nodes<DIM>(conn, E, e, nd);
+            const DF ae = df_mul(ed.df(0, e), k.ref_df);
+            const DF tau = ed.df(1, e);
+            DF gi[DIM];
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) gi[f] = ed.df(2 + f * NPE + i, e);
+            if constexpr (DFA) {
+                pair_item_df<DIM>(ed, e, i, i, rho, inv_dt, l_sum, k, A);
+            } else {  // pspg_pair_block's (i, i) share in FP32
+                const float a32 = ae.h, t32 = tau.h, kf = a32 * ed.f(ed_ksum<DIM>(), e);
+                float g[DIM], dot = 0.0f;
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) {
+                    g[f] = gi[f].h;
+                    dot += g[f] * g[f];
+                }
+                const float mii = cm32 * k.mm32[i][i] * a32, as = a32 * k.s32[i];
+#pragma unroll
+                for (int f1 = 0; f1 < DIM; ++f1) {
+#pragma unroll
+                    for (int f2 = 0; f2 < DIM; ++f2) A32[f1][f2] += kf * ((f1 == f2 ? dot : 0.0f) + g[f2] * g[f1]);
+                    A32[f1][f1] += mii;
+                    A32[f1][DIM] -= as * g[f1];
+                    A32[DIM][f1] += (t32 * ct32 + 1.0f) * as * g[f1];
+                }
+                A32[DIM][DIM] += t32 * a32 * l32 * dot;
+            }
+            DF fs = k.s_df[i], hs = k.hsum_df;
+            if (tdf) {  // Boussinesq factors (MomContEquation.inl:164-199)
+                DF mt{0.0f, 0.0f}, st{0.0f, 0.0f};
+#pragma unroll
+                for (int j = 0; j < NPE; ++j) {
+                    const DF Tj = tdf[nd[j]];
+                    mt = df_add(mt, df_mul(k.mm_df[i][j], Tj));
+                    st = df_add(st, df_mul(k.s_df[j], Tj));
+                }
+                fs = df_sub(df_mul(k.bq_c0, k.s_df[i]), df_mul(k.bq_alpha, mt));
+                hs = df_sub(df_mul(k.bq_c0, k.hsum_df), df_mul(k.bq_alpha, st));
+            }
+            // momentum rows: F + (M/dt) v_prev; continuity row: tau H + (tau/dt) C v_prev
+            DF mrow[NPE];
+#pragma unroll
+            for (int j = 0; j < NPE; ++j) mrow[j] = df_mul(inv_dt, df_mul(df_mul(rho, k.mm_df[i][j]), ae));
+            DF cv{0.0f, 0.0f}, gdot{0.0f, 0.0f};
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) {
+                DF mv{0.0f, 0.0f};
+                const DF ag = df_mul(ae, gi[f]);
+#pragma unroll
+                for (int j = 0; j < NPE; ++j) {
+                    const DF vj = vp[(size_t)f * N + nd[j]];
+                    mv = df_add(mv, df_mul(mrow[j], vj));
+                    cv = df_add(cv, df_mul(df_mul(ag, k.s_df[j]), vj));
+                }
+                const DF F = df_mul(ae, df_mul(df_mul(rho, fs), k.g_df[f]));
+                bv[f] = df_add(bv[f], df_add(F, mv));
+                gdot = df_add(gdot, df_mul(gi[f], k.g_df[f]));
+            }
+            const DF H = df_mul(tau, df_mul(df_mul(ae, hs), gdot));
+            bp = df_add(bp, df_add(H, df_mul(df_mul(tau, inv_dt), cv)));
+        }
+        // right-hand side with the node conditions (m_applyBCPSPG :186-232)
+        const bool free_n = fl & F_FREE, bound = fl & F_BOUND, dir = bound && (fl & F_DIRICHLET);
+        double b[B];
+#pragma unroll
+        for (int f = 0; f < DIM; ++f) b[f] = df_to(bv[f]) + (fst ? fst[(size_t)f * N + n] : 0.0);
+        b[DIM] = df_to(bp);
+        if (free_n) {
+            b[DIM] = 0.0;
+            if (!bound) {
+                const double dt = m.id[inst * D_COUNT + D_DT];
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) b[f] = q_prev[(size_t)f * N + n] + dt * k.t.g[f];
+            }
+        }
+        if (dir)
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) b[f] = vbc[(size_t)f * N + n];
+#pragma unroll
+        for (int f = 0; f < B; ++f) {
+            rhs[(size_t)f * N + n] = b[f];
+            bb += b[f] * b[f];
+        }
+        // the node's own block with its identity rows and zeroed Dirichlet columns
+        double a[B][B];
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) {
+                double v;
+                if constexpr (DFA) v = df_to(A[f1][f2]);
+                else v = (double)A32[f1][f2];
+                if (free_n || (bound && f1 < DIM)) v = (f1 == f2) ? 1.0 : 0.0;
+                else if (dir && f2 < DIM && f1 != f2) v = 0.0;
+                a[f1][f2] = v;
+            }
+        double s[B];
+#pragma unroll
+        for (int f = 0; f < B; ++f) {
+            const double d = fabs(a[f][f]);
+            s[f] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+            scale[(size_t)f * N + n] = s[f];
+            scale32[(size_t)f * N + n] = (float)s[f];
+        }
+        double inv[B][B];
+        block_inverse<B>(a, inv);
+        float out[B * B];
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) {
+                binv64[(size_t)(f1 * B + f2) * N + n] = inv[f1][f2];
+                // (S A S)^-1 = S^-1 A^-1 S^-1
+                binv32[(size_t)(f1 * B + f2) * N + n] = (float)(inv[f1][f2] / (s[f1] * s[f2]));
+                out[f1 * B + f2] = (float)(s[f1] * a[f1][f2] * s[f2]);
+            }
+        const int b0 = nbr_ptr[n];
+        store_block32<B>(blk, blk16, b0 + self_rank(nbr, b0, nbr_ptr[n + 1], n), out);
+    }
+    double v[1] = {bb};
+    if (!inst_reduce<NB, 1, double>(v, sb, ii[I_B0], ii[I_B1], m.part, reinterpret_cast<unsigned*>(ii + I_TICKET), sh))
+        return;
+    if (threadIdx.x == 0) m.id[inst * D_COUNT + D_BB] = v[0];
+}
+
+// Off-diagonal blocks of the scaled FP32 system, one thread per node pair p = (n, m), m != n:
+// the pair's elements in ascending order (FP32 arithmetic with the element formulas of
+// pspg_pair_block, or with DFA double-float arithmetic rounded once), the identity rows of
+// bound nodes, the zeroed Dirichlet columns (:216-229) and the row / column scales; written as
+// one (d+1)^2 block (and its bfloat16 copy).
+template <int DIM, bool DFA>
+__global__ void __launch_bounds__(BLOCK) k_mx_asm32(int P, int N, const int* __restrict__ pair_node,
+                                                    const int* __restrict__ nbr, const int* __restrict__ pe_ptr,
+                                                    const int* __restrict__ pe_item, EdPlanes ed,
+                                                    const uint8_t* __restrict__ flags,
+                                                    const float* __restrict__ scale32, const float* __restrict__ f32,
+                                                    Mx m, MxConst k, float* __restrict__ blk,
+                                                    uint16_t* __restrict__ blk16) {
+    constexpr int B = DIM + 1, NPE = DIM + 1;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int n = pair_node[p];
+    const int mm = nbr[p];
+    if (mm == n) return;  // diagonal blocks: k_mx_node
+    const int inst = m.node_inst[n];
+    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    const uint8_t fn = flags[n], fm = flags[mm];
+    float a[B][B];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) a[f1][f2] = 0.0f;
+    if (DFA && !(fn & F_FREE)) {
+        const DF rho = inst_df(f32, inst, F_RHO), inv_dt = inst_df(f32, inst, F_INVDT);
+        const DF l_sum = inst_df(f32, inst, F_LSUM);
+        DF acc[B][B];
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) acc[f1][f2] = DF{0.0f, 0.0f};
+        const int k1 = pe_ptr[p + 1];
+        for (int kk = pe_ptr[p]; kk < k1; ++kk) {
+            const int it = __ldg(pe_item + kk);
+            pair_item_df<DIM>(ed, it >> 4, (it >> 2) & 3, it & 3, rho, inv_dt, l_sum, k, acc);
+        }
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) a[f1][f2] = acc[f1][f2].h + acc[f1][f2].l;
+    } else if (!(fn & F_FREE)) {
+        const float cm = f32[inst * F_COUNT + F_CM], inv_dt = f32[inst * F_COUNT + F_INVDT];
+        const float l_sum = f32[inst * F_COUNT + F_LSUM];
+        const int k0 = pe_ptr[p], k1 = pe_ptr[p + 1];
+        // the element data of the next item are loaded before this item's arithmetic (two
+        // items' gathers in flight per thread)
+        struct Item {
+            float ae, tau, ks, gi[DIM], gj[DIM];
+            int i, j;
+        };
+        auto load = [&](int kk, Item& t) {
+            const int it = __ldg(pe_item + kk);
+            const int e = it >> 4;
+            t.i = (it >> 2) & 3;
+            t.j = it & 3;
+            t.ae = ed.f(0, e);
+            t.tau = ed.f(1, e);
+            t.ks = ed.f(ed_ksum<DIM>(), e);
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) {
+                t.gi[f] = ed.f(2 + f * NPE + t.i, e);
+                t.gj[f] = ed.f(2 + f * NPE + t.j, e);
+            }
+        };
+        Item nxt;
+        if (k0 < k1) load(k0, nxt);
+        for (int kk = k0; kk < k1; ++kk) {
+            const Item cur = nxt;
+            if (kk + 1 < k1) load(kk + 1, nxt);
+            const int i = cur.i, j = cur.j;
+            const float ae = cur.ae * k.ref32;
+            const float tau = cur.tau;
+            const float kf = ae * cur.ks;
+            const float(&gi)[DIM] = cur.gi;
+            const float(&gj)[DIM] = cur.gj;
+            float dot = gi[0] * gj[0];
+#pragma unroll
+            for (int f = 1; f < DIM; ++f) dot += gi[f] * gj[f];
+            const float mij = cm * k.mm32[i][j] * ae;
+            const float asj = ae * k.s32[j], asi = ae * k.s32[i];
+            const float ct = tau * inv_dt;
+#pragma unroll
+            for (int f1 = 0; f1 < DIM; ++f1) {
+#pragma unroll
+                for (int f2 = 0; f2 < DIM; ++f2) a[f1][f2] += kf * ((f1 == f2 ? dot : 0.0f) + gi[f2] * gj[f1]);
+                a[f1][f1] += mij;
+                a[f1][DIM] -= asj * gi[f1];
+                a[DIM][f1] += ct * asj * gi[f1] + asi * gj[f1];
+            }
+            a[DIM][DIM] += tau * ae * l_sum * dot;
+        }
+    }
+    const bool bound = fn & F_BOUND;
+    const bool mdir = (fm & F_BOUND) && (fm & F_DIRICHLET);
+    float sn[B], sm[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        sn[f] = scale32[(size_t)f * N + n];
+        sm[f] = scale32[(size_t)f * N + mm];
+    }
+    float out[B * B];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) {
+            float v = a[f1][f2];
+            if ((fn & F_FREE) || (bound && f1 < DIM) || (mdir && f2 < DIM)) v = 0.0f;
+            out[f1 * B + f2] = sn[f1] * v * sm[f2];
+        }
+    store_block32<B>(blk, blk16, p, out);
+}
+
+// FP64 CSR values of the instances whose correction solves run in FP64 (and whose values are
+// not yet current for this assembly), one thread per node pair: the gather and Dirichlet
+// elimination of the FP64 path, each element's share in double-float (pair_item_df).
+template <int DIM>
+__global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const int* __restrict__ pair_node,
+                                                    const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                                                    const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
+                                                    const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
+                                                    EdPlanes ed, const uint8_t* __restrict__ flags,
+                                                    const int* __restrict__ row_ptr, double* __restrict__ val,
+                                                    const double* __restrict__ vbc, const float* __restrict__ f32,
+                                                    Mx m, MxConst k) {
+    constexpr int NPE = DIM + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P) return;
+    const int n = pair_node[t];
+    const int inst = m.node_inst[n];
+    const int* ii = m.ii + inst * I_COUNT;
+    if (!ii[I_ACTIVE] || ii[I_MODE] != MODE_FP64 || ii[I_M64]) return;
+    const int b0 = nbr_ptr[n];
+    const int deg = nbr_ptr[n + 1] - b0;
+    const int rank = t - b0;
+    const int mm = nbr[t];
+    const uint8_t fn = flags[n];
+    if (fn & F_FREE) {
+#pragma unroll
+        for (int f = 0; f <= DIM; ++f) val[row_ptr[n + f * N]] = 1.0;
+        return;
+    }
+    const DF rho = inst_df(f32, inst, F_RHO), inv_dt = inst_df(f32, inst, F_INVDT);
+    const DF l_sum = inst_df(f32, inst, F_LSUM);
+    DF acc[NPE][NPE];
+#pragma unroll
+    for (int a = 0; a < NPE; ++a)
+#pragma unroll
+        for (int b = 0; b < NPE; ++b) acc[a][b] = DF{0.0f, 0.0f};
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const int e = ne_elem[q];
+        int j = -1;
+#pragma unroll
+        for (int jj = 0; jj < NPE; ++jj)
+            if (__ldg(conn + (size_t)jj * E + e) == mm) j = jj;
+        if (j >= 0) pair_item_df<DIM>(ed, e, ne_loc[q], j, rho, inv_dt, l_sum, k, acc);
+    }
+    double out[NPE][NPE];
+#pragma unroll
+    for (int a = 0; a < NPE; ++a)
+#pragma unroll
+        for (int b = 0; b < NPE; ++b) out[a][b] = df_to(acc[a][b]);
+    pspg_write_block<DIM>(n, mm, N, deg, rank, fn, flags[mm], row_ptr, out, true, vbc, nullptr, val, nullptr);
+}
+
+__global__ void k_mx_mark_csr64(int n_inst, Mx m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_inst) return;
+    int* ii = m.ii + i * I_COUNT;
+    if (ii[I_ACTIVE] && ii[I_MODE] == MODE_FP64) ii[I_M64] = 1;
+}
+
+// ---- refinement residual, matrix-free in double-float ----------------------------------------
+//
+// r = b - A x with A applied element by element from the double-float element data (no FP64
+// matrix): k_mx_xdf makes a double-float copy of x with the Dirichlet values in the Dirichlet
+// velocity columns (b - A x over the full matrix at those values equals the eliminated system's
+// residual, :216-229); k_mx_res_elem evaluates each element's A_e x for its d+1 element rows
+// from element-level gradients (grad u, grad p, sums of s_j u_j) and writes one record per
+// element node; k_mx_res_node sums its node's records in ascending element order and forms
+// r = b - A x (identity rows: r = b - x).  Right after a re-assembly this is also the Picard
+// "Ax_f" residual (:366-371).
+
+template <int DIM>
+__global__ void k_mx_xdf(int N, const double* __restrict__ x, const double* __restrict__ vbc,
+                         const uint8_t* __restrict__ flags, Mx m, DF* __restrict__ xdf) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    if (!m.ii[m.node_inst[n] * I_COUNT + I_ACTIVE]) return;
+    const uint8_t fl = flags[n];
+    const bool dir = (fl & F_BOUND) && (fl & F_DIRICHLET);
+#pragma unroll
+    for (int f = 0; f <= DIM; ++f) {
+        const size_t r = (size_t)f * N + n;
+        xdf[r] = df_from(dir && f < DIM ? vbc[r] : x[r]);
+    }
+}
+
+constexpr int RES_ELEM_BLOCK = 64;  // ~136 registers a thread: small blocks keep more warps resident
+
+// A_e x for every element row of the element's nodes (momentum rows of bound nodes are
+// identity rows and get 0): record (e, i) holds d+1 double-float values, 32 bytes.
+template <int DIM>
+__global__ void __launch_bounds__(RES_ELEM_BLOCK) k_mx_res_elem(int E, int N, const int* __restrict__ conn, EdPlanes ed,
+                                                                const uint8_t* __restrict__ flags,
+                                                                const DF* __restrict__ xdf, const float* __restrict__ f32,
+                                                                Mx m, MxConst k, float4* __restrict__ rec) {
+    constexpr int NPE = DIM + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int nd[NPE];
+    load_nodes<DIM>(conn, E, e, nd);
+    const int inst = m.node_inst[nd[0]];
+    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    const DF inv_dt = inst_df(f32, inst, F_INVDT), l_sum = inst_df(f32, inst, F_LSUM);
+    const DF cm = inst_df(f32, inst, F_CM);
+    const DF ae = df_mul(ed.df(0, e), k.ref_df);
+    const DF tau = ed.df(1, e);
+    const DF kf = df_mul(ae, ed.df(ed_ksum<DIM>(), e));
+    DF G[DIM][NPE];
+#pragma unroll
+    for (int f = 0; f < DIM; ++f)
+#pragma unroll
+        for (int j = 0; j < NPE; ++j) G[f][j] = ed.df(2 + f * NPE + j, e);
+    DF u[NPE][DIM], p[NPE];
+#pragma unroll
+    for (int j = 0; j < NPE; ++j) {
+#pragma unroll
+        for (int f = 0; f < DIM; ++f) u[j][f] = xdf[(size_t)f * N + nd[j]];
+        p[j] = xdf[(size_t)DIM * N + nd[j]];
+    }
+    // element-level sums: Gu[a][b] = sum_j dN_j/dx_b u_j[a], grad p, s-weighted sums
+    DF Gu[DIM][DIM], gp[DIM], Su[DIM], Sp{0.0f, 0.0f};
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) {
+            DF s = df_mul(G[b][0], u[0][a]);
+#pragma unroll
+            for (int j = 1; j < NPE; ++j) s = df_fma(G[b][j], u[j][a], s);
+            Gu[a][b] = s;
+        }
+        DF s = df_mul(G[a][0], p[0]);
+#pragma unroll
+        for (int j = 1; j < NPE; ++j) s = df_fma(G[a][j], p[j], s);
+        gp[a] = s;
+        DF t = df_mul(k.s_df[0], u[0][a]);
+#pragma unroll
+        for (int j = 1; j < NPE; ++j) t = df_fma(k.s_df[j], u[j][a], t);
+        Su[a] = t;
+    }
+#pragma unroll
+    for (int j = 0; j < NPE; ++j) Sp = df_fma(k.s_df[j], p[j], Sp);
+    DF div = Gu[0][0];
+#pragma unroll
+    for (int a = 1; a < DIM; ++a) div = df_add(div, Gu[a][a]);
+    DF sym[DIM][DIM];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) sym[a][b] = df_add(Gu[a][b], Gu[b][a]);
+    const DF cma = df_mul(cm, ae);
+    const DF cta = df_mul(df_mul(tau, inv_dt), ae);
+    const DF tla = df_mul(df_mul(tau, ae), l_sum);
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) {
+        DF out[4];
+        // continuity row: (tau/dt) C u + D u + tau L p
+        DF gs = df_mul(G[0][i], Su[0]), gq = df_mul(G[0][i], gp[0]);
+#pragma unroll
+        for (int f = 1; f < DIM; ++f) {
+            gs = df_fma(G[f][i], Su[f], gs);
+            gq = df_fma(G[f][i], gp[f], gq);
+        }
+        out[DIM] = df_add(df_add(df_mul(cta, gs), df_mul(df_mul(ae, k.s_df[i]), div)), df_mul(tla, gq));
+        if (flags[nd[i]] & F_BOUND) {
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) out[a] = DF{0.0f, 0.0f};
+        } else {
+            // momentum rows: (M/dt) u + K u - D^T p
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) {
+                DF mu_ = df_mul(k.mm_df[i][0], u[0][a]);
+#pragma unroll
+                for (int j = 1; j < NPE; ++j) mu_ = df_fma(k.mm_df[i][j], u[j][a], mu_);
+                DF ks = df_mul(G[0][i], sym[a][0]);
+#pragma unroll
+                for (int c = 1; c < DIM; ++c) ks = df_fma(G[c][i], sym[a][c], ks);
+                out[a] = df_sub(df_add(df_mul(cma, mu_), df_mul(kf, ks)), df_mul(df_mul(ae, G[a][i]), Sp));
+            }
+        }
+        if constexpr (DIM == 2) out[3] = DF{0.0f, 0.0f};
+        float4* r = rec + ((size_t)e * NPE + i) * 2;
+        r[0] = make_float4(out[0].h, out[0].l, out[1].h, out[1].l);
+        r[1] = make_float4(out[2].h, out[2].l, out[3].h, out[3].l);
+    }
+}
+
+// r = b - A x of the segment's nodes from the element records, then the seeds of the
+// instance's next correction solve and its Picard / refinement bookkeeping.  `kind`:
 //   RES_SWEEP   after a correction sweep: an FP32 sweep that did not shrink ||r|| tenfold moves
 //               the instance to FP64 mode (and, if ||r|| grew, asks the host to undo it);
 //   RES_PICARD  after a re-assembly: decides the instance's Picard iteration count,
@@ -525,35 +1003,46 @@ __device__ __forceinline__ double row_dot64(int r, bool act, const int* __restri
 //   RES_START   first residual of a step, or after an undo.
 enum : int { RES_SWEEP = 0, RES_PICARD = 1, RES_START = 2 };
 
-template <int G, int DIM>
-__global__ void __launch_bounds__(SPMV_BLOCK) k_mx_resid(Mx m, int N, const int* __restrict__ rp,
-                                                         const int* __restrict__ col, const double* __restrict__ val,
-                                                         const double* __restrict__ b, const double* __restrict__ x,
-                                                         const double* __restrict__ scale, MxConst k,
-                                                         float* __restrict__ W, double* __restrict__ W64, size_t ld,
-                                                         int kind) {
+template <int DIM>
+__global__ void __launch_bounds__(NB) k_mx_res_node(Mx m, int N, const int* __restrict__ ne_ptr,
+                                                    const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
+                                                    const float4* __restrict__ rec, const uint8_t* __restrict__ flags,
+                                                    const double* __restrict__ b, const double* __restrict__ x,
+                                                    const double* __restrict__ scale, MxConst k,
+                                                    float* __restrict__ W, double* __restrict__ W64, size_t ld,
+                                                    int kind) {
+    constexpr int B = DIM + 1, NPE = DIM + 1;
     __shared__ double sh[32];
     const int blk = blockIdx.x;
     const int inst = m.seg[3 * blk];
     int* ii = m.ii + inst * I_COUNT;
     if (!ii[I_ACTIVE]) return;
     const bool fp64 = ii[I_MODE] == MODE_FP64;
-    const int n0 = m.seg[3 * blk + 1], cnt = m.seg[3 * blk + 2] - n0;
-    const int rows = cnt * (DIM + 1);
-    const int lane = threadIdx.x % G;
-    double rr = 0, bb = 0, rs = 0;
-    for (int t0 = 0; t0 < rows; t0 += SPMV_BLOCK / G) {
-        const int t = t0 + threadIdx.x / G;
-        const bool act = t < rows;
-        int r = 0;
-        if (act) {
-            const int f = t / cnt;
-            r = f * N + n0 + (t - f * cnt);
+    const int n = m.seg[3 * blk + 1] + threadIdx.x;
+    double rr = 0, rs = 0;
+    if (n < m.seg[3 * blk + 2]) {
+        const uint8_t fl = flags[n];
+        const bool ident_v = fl & (F_BOUND | F_FREE), ident_p = fl & F_FREE;
+        DF ax[4] = {DF{0.0f, 0.0f}, DF{0.0f, 0.0f}, DF{0.0f, 0.0f}, DF{0.0f, 0.0f}};
+        if (!ident_p) {
+            for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+                const float4* r = rec + ((size_t)__ldg(ne_elem + q) * NPE + __ldg(ne_loc + q)) * 2;
+                const float4 r0 = __ldg(r), r1 = __ldg(r + 1);
+                ax[0] = df_add(ax[0], DF{r0.x, r0.y});
+                ax[1] = df_add(ax[1], DF{r0.z, r0.w});
+                ax[2] = df_add(ax[2], DF{r1.x, r1.y});
+                if constexpr (DIM == 3) ax[3] = df_add(ax[3], DF{r1.z, r1.w});
+            }
         }
-        const double ax = row_dot64<G>(r, act, rp, col, val, x, lane);
-        if (act && lane == 0) {
+#pragma unroll
+        for (int f = 0; f < B; ++f) {
+            const size_t r = (size_t)f * N + n;
             const double bv = b[r];
-            const double rv = bv - ax;
+            double rv;
+            if ((f < DIM && ident_v) || (f == DIM && ident_p))
+                rv = bv - x[r];
+            else
+                rv = df_to(df_sub(df_from(bv), ax[f]));
             if (fp64) {
                 W64[W_R * ld + r] = rv;
                 W64[W_RHAT * ld + r] = rv;
@@ -570,21 +1059,18 @@ __global__ void __launch_bounds__(SPMV_BLOCK) k_mx_resid(Mx m, int N, const int*
                 rs += sv * sv;
             }
             rr += rv * rv;
-            bb += bv * bv;
         }
     }
-    double v[3] = {rr, bb, rs};
-    if (!inst_reduce<SPMV_BLOCK, 3, double>(v, blk, ii[I_B0], ii[I_B1], m.part,
-                                            reinterpret_cast<unsigned*>(ii + I_TICKET), sh))
+    double v[2] = {rr, rs};
+    if (!inst_reduce<NB, 2, double>(v, blk, ii[I_B0], ii[I_B1], m.part, reinterpret_cast<unsigned*>(ii + I_TICKET), sh))
         return;
     if (threadIdx.x != 0) return;
     double* idd = m.id + inst * D_COUNT;
     rr = v[0];
-    bb = v[1];
-    rs = v[2];
+    rs = v[1];
+    const double bb = idd[D_BB];
     const double rr_prev = idd[D_RR];
     idd[D_RR] = rr;
-    idd[D_BB] = bb;
     bool active = true;
     if (kind == RES_PICARD) {
         const double res = sqrt(rr);
@@ -974,15 +1460,41 @@ int read_counters(pfg_ctx* c, Counters* k) {
     return PFG_OK;
 }
 
+// sum_g mu w_g in the order of k_sum's loop (the Newtonian K factor)
+double ksum_newtonian(int dim, double mu) {
+    const GaussConst g = gauss_const(dim);
+    double s = 0;
+    for (int q = 0; q < g.n; ++q) s += mu * g.w[q];
+    return s;
+}
+
+EdPlanes ed_planes(pfg_ctx* c) {
+    const int ned = c->dim == 2 ? ed_count<2>() : ed_count<3>();
+    float* h = ptr<float>(c->edata_df);
+    return EdPlanes{h, h + (size_t)ned * c->E, c->E};
+}
+
+// A, b at the iterate q_iter: element data, node blocks and right-hand side, FP32 pair blocks
+// (and the multigrid's coarse blocks).
 template <int DIM>
 int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     const int N = c->N, E = c->E;
     Mx m = mx_ptrs(c);
+    const EdPlanes ed = ed_planes(c);
+    const bool dfa = c->prm.assembly == PFG_ASM_DOUBLE_FLOAT;
     if (E > 0) {
         prof_begin(c, PH_PSPG_ELEM);
-        k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), q_iter,
-                                                                  m, k.refSize, visc_args(c), ptr<double>(c->edata),
-                                                                  ptr<DF>(c->edata_df));
+        if (c->prm.tau0 > 0) {  // Bingham viscosity from the iterate's strain rates: FP64 element prep
+            k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
+                                                                      q_iter, m, k.refSize, visc_args(c),
+                                                                      const_cast<float*>(ed.h), const_cast<float*>(ed.l));
+        } else {
+            k_mx_gprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->pos), q_iter, m,
+                                                                       ptr<DF>(c->mx_gdf));
+            k_mx_prep_df<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
+                E, N, ptr<int>(c->conn), ptr<DF>(c->mx_gdf), ptr<float>(c->mx_f32), m, k.ref_df, k.inv_pi_df,
+                const_cast<float*>(ed.h), const_cast<float*>(ed.l));
+        }
         prof_end(c, PH_PSPG_ELEM);
         PFG_CHECK_LAUNCH(c);
     }
@@ -991,29 +1503,24 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     if (fa.nodes)
         k_fst<DIM, double><<<div_up(fa.n_nodes, BLOCK), BLOCK, 0, c->stream>>>(
             fa, E, ptr<int>(c->conn), PosF64{ptr<double>(c->pos), N}, N, ptr<double>(c->fst_force));
-    k_mx_rhs<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
-        N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
-        ptr<double>(c->edata), ptr<uint8_t>(c->flags), ptr<double>(c->q_prev), ptr<double>(c->vbc), m, k,
-        ptr<double>(c->rhs), fst_force<double>(c));
+    DF* tdf = k.bq.T ? ptr<DF>(c->mx_tdf) : nullptr;
+    k_mx_vprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->q_prev), k.bq.T, m,
+                                                               ptr<DF>(c->mx_vpdf), tdf);
+    uint16_t* v16 = c->n_mg > 0 ? ptr<uint16_t>(c->val16) : nullptr;
+    auto node_kernel = dfa ? k_mx_node<DIM, true> : k_mx_node<DIM, false>;
+    node_kernel<<<c->n_seg, NB, 0, c->stream>>>(
+        m, N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ed,
+        ptr<uint8_t>(c->flags), ptr<DF>(c->mx_vpdf), tdf, ptr<double>(c->q_prev), ptr<double>(c->vbc),
+        fst_force<double>(c), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<float>(c->mx_f32), k, ptr<double>(c->rhs),
+        ptr<double>(c->mx_scale), ptr<float>(c->mx_scale32), ptr<double>(c->binv), ptr<float>(c->binv32),
+        ptr<float>(c->val32), v16);
     prof_end(c, PH_PSPG_RHS);
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);
-    k_mx_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
-        c->P, N, E, ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(c->ne_ptr),
-        ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<DF>(c->edata_df),
-        ptr<uint8_t>(c->flags), ptr<int>(c->row_ptr), ptr<double>(c->val), ptr<double>(c->vbc), ptr<double>(c->rhs),
-        m, k);
-    double* scale = ptr<double>(c->mx_scale);
-    k_mx_rowscale<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->diag_pos), ptr<double>(c->val), m,
-                                                                  scale);
-    k_mx_scale_bsr<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(c->P, N, ptr<int>(c->pair_node),
-                                                                      ptr<int>(c->nbr_ptr), ptr<int>(c->nbr),
-                                                                      ptr<int>(c->row_ptr), ptr<double>(c->val), scale,
-                                                                      m, ptr<float>(c->val32),
-                                                                      c->n_mg > 0 ? ptr<uint16_t>(c->val16) : nullptr);
-    k_mx_binv<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<int>(c->row_ptr), ptr<double>(c->val),
-                                                              ptr<int>(c->diag_pos), scale, ptr<float>(c->binv32),
-                                                              ptr<double>(c->binv), m);
+    auto pair_kernel = dfa ? k_mx_asm32<DIM, true> : k_mx_asm32<DIM, false>;
+    pair_kernel<<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
+        c->P, N, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->pe_ptr), ptr<int>(c->pe_item), ed,
+        ptr<uint8_t>(c->flags), ptr<float>(c->mx_scale32), ptr<float>(c->mx_f32), m, k, ptr<float>(c->val32), v16);
     prof_end(c, PH_PSPG_PAIRS);
     PFG_CHECK_LAUNCH(c);
     if (c->n_mg > 0) {
@@ -1025,15 +1532,38 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     return PFG_OK;
 }
 
+// FP64 CSR values for the instances in FP64 mode that lack them for this assembly (the FP64
+// correction solves' products); the kernel does nothing for the other instances.
+template <int DIM>
+int mx_csr64(pfg_ctx* c, const MxConst& k) {
+    Mx m = mx_ptrs(c);
+    prof_begin(c, PH_PSPG_PAIRS);
+    k_mx_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
+        c->P, c->N, c->E, ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(c->ne_ptr),
+        ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ed_planes(c), ptr<uint8_t>(c->flags),
+        ptr<int>(c->row_ptr), ptr<double>(c->val), ptr<double>(c->vbc), ptr<float>(c->mx_f32), m, k);
+    k_mx_mark_csr64<<<div_up(c->n_inst, BLOCK), BLOCK, 0, c->stream>>>(c->n_inst, m);
+    prof_end(c, PH_PSPG_PAIRS);
+    PFG_CHECK_LAUNCH(c);
+    return PFG_OK;
+}
+
 template <int DIM>
 int mx_residual(pfg_ctx* c, const MxConst& k, int kind, Counters* cnt) {
     Mx m = mx_ptrs(c);
-    constexpr int G = DIM == 2 ? 8 : 16;
+    const int N = c->N, E = c->E;
     PFG_CUDA(c, cudaMemsetAsync(c->mx_cnt.p, 0, 4 * sizeof(int), c->stream));
     prof_begin(c, PH_RESIDUAL);
-    k_mx_resid<G, DIM><<<c->n_seg, SPMV_BLOCK, 0, c->stream>>>(
-        m, c->N, ptr<int>(c->row_ptr), ptr<int>(c->col), ptr<double>(c->val), ptr<double>(c->rhs), ptr<double>(c->q),
-        ptr<double>(c->mx_scale), k, ptr<float>(c->kv32), ptr<double>(c->kv), (size_t)c->R, kind);
+    k_mx_xdf<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->q), ptr<double>(c->vbc),
+                                                             ptr<uint8_t>(c->flags), m, ptr<DF>(c->mx_xdf));
+    if (E > 0)
+        k_mx_res_elem<DIM><<<div_up(E, RES_ELEM_BLOCK), RES_ELEM_BLOCK, 0, c->stream>>>(
+            E, N, ptr<int>(c->conn), ed_planes(c), ptr<uint8_t>(c->flags), ptr<DF>(c->mx_xdf), ptr<float>(c->mx_f32),
+            m, k, ptr<float4>(c->mx_rec));
+    k_mx_res_node<DIM><<<c->n_seg, NB, 0, c->stream>>>(
+        m, N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<float4>(c->mx_rec),
+        ptr<uint8_t>(c->flags), ptr<double>(c->rhs), ptr<double>(c->q), ptr<double>(c->mx_scale), k,
+        ptr<float>(c->kv32), ptr<double>(c->kv), (size_t)c->R, kind);
     prof_end(c, PH_RESIDUAL);
     PFG_CHECK_LAUNCH(c);
     return read_counters(c, cnt);
@@ -1311,6 +1841,7 @@ int mx_refine(pfg_ctx* c, const MxConst& k, Counters* cnt) {
     for (int sweep = 0; sweep < max_ref && (cnt->need32 > 0 || cnt->need64 > 0); ++sweep) {
         PFG_CUDA(c, cudaMemcpyAsync(c->q_iter_prev.p, c->q.p, sizeof(double) * c->R, cudaMemcpyDeviceToDevice,
                                     c->stream));
+        if (cnt->need64 > 0 && (rc = mx_csr64<DIM>(c, k))) return rc;
         if (c->n_inst > 1) {
             if ((rc = mx_inner_batch<DIM>(c, cnt))) return rc;
         } else {
@@ -1353,6 +1884,28 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
     }
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_ii.p, hi.data(), sizeof(int) * hi.size(), cudaMemcpyHostToDevice, c->stream));
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_id.p, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, c->stream));
+    // per-instance coefficients as double-float pairs (high parts = the FP32 kernels' values)
+    {
+        const double sumw = gauss_const(c->dim).sumw;
+        std::vector<float>& hf = c->h_mx_f32;
+        hf.assign((size_t)K * F_COUNT, 0.0f);
+        auto put = [&](int i, int which, double v) {
+            const float h = (float)v;
+            hf[(size_t)i * F_COUNT + which] = h;
+            hf[(size_t)i * F_COUNT + which + 1] = (float)(v - (double)h);
+        };
+        for (int i = 0; i < K; ++i) {
+            const double rho = hd[(size_t)i * D_COUNT + D_RHO], mu = hd[(size_t)i * D_COUNT + D_MU];
+            put(i, F_RHO, rho);
+            put(i, F_INVDT, 1.0 / dts[i]);
+            put(i, F_LSUM, sumw / rho);
+            put(i, F_CM, rho / dts[i]);
+            put(i, F_MU4R, 4 * mu / rho);
+            put(i, F_KSUM, ksum_newtonian(c->dim, mu));
+        }
+        PFG_CUDA(c, cudaMemcpyAsync(c->mx_f32.p, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice,
+                                    c->stream));
+    }
     // prepare: save the node list, qPrev = states, build A and b at the current geometry
     PFG_CUDA(c, cudaMemcpyAsync(c->pos_save.p, c->pos.p, sizeof(double) * c->dim * c->N, cudaMemcpyDeviceToDevice,
                                 c->stream));
@@ -1398,7 +1951,14 @@ int mx_alloc(pfg_ctx* c) {
     const size_t R = std::max(c->R, 1), N = std::max(c->N, 1), E = std::max(c->E, 1);
     const int ned = c->dim == 2 ? ed_count<2>() : ed_count<3>();
     int rc;
-    if ((rc = ensure(c, c->edata_df, sizeof(DF) * ned * E)) || (rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))) ||
+    const size_t npe = c->dim + 1;
+    if ((rc = ensure(c, c->edata_df, sizeof(DF) * ned * E)) ||
+        (rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))) ||
+        (rc = ensure(c, c->mx_scale32, sizeof(float) * R)) || (rc = ensure(c, c->mx_xdf, sizeof(DF) * R)) ||
+        (rc = ensure(c, c->mx_vpdf, sizeof(DF) * (size_t)c->dim * N)) ||
+        (rc = ensure(c, c->mx_gdf, sizeof(DF) * 2 * (size_t)c->dim * N)) ||
+        (rc = ensure(c, c->mx_tdf, sizeof(DF) * (c->prm.boussinesq ? N : 1))) ||
+        (rc = ensure(c, c->mx_rec, 32 * npe * E)) ||
         (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) || (rc = ensure(c, c->mx_scale, sizeof(double) * R)) ||
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))
@@ -1466,6 +2026,7 @@ int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* 
         (rc = ensure(c, c->mx_sc, 256 * (((size_t)n_inst * M_COUNT * sizeof(float) + 255) / 256) +
                                       sizeof(double) * (size_t)n_inst * M_COUNT)) ||
         (rc = ensure(c, c->mx_part, sizeof(double) * 4 * (size_t)c->n_seg)) ||
+        (rc = ensure(c, c->mx_f32, sizeof(float) * F_COUNT * (size_t)n_inst)) ||
         (rc = ensure(c, c->mx_list, sizeof(int) * 2 * (size_t)c->n_seg)))
         return rc;
     PFG_CUDA(c, cudaMemcpyAsync(c->mx_seg.p, seg.data(), sizeof(int) * seg.size(), cudaMemcpyHostToDevice, c->stream));
