@@ -1,5 +1,6 @@
-"""Mixed-precision PSPG (FP32 assembly and FP32 correction solves, FP64 matrix-free
-refinement residual) and batched instances, against the FP64 oracle, through the C ABI.
+"""Mixed-precision PSPG (FP32 node-pair assembly and FP32 correction solves under FP64
+iterative refinement of a matrix-free double-float residual) and batched instances, against the
+FP64 oracle, through the C ABI.
 
 Tolerances: a Picard step within 1e-8 relative per field of the oracle, because the
 refinement stops on the same FP64 residual test as the plain form
@@ -194,35 +195,82 @@ def test_set_positions_restores_a_step(gpu_lib, c1_mesh):
     assert np.array_equal(ctx.get_states(), q1)
 
 
-def test_c3_full_size_properties(gpu_lib):
-    """The C3 mesh (330k nodes, 1.74M tets) at its own tolerance (relative residual 1e-8):
-    size-independent properties of two Picard steps.  Both forms converge with the same Picard
-    iteration counts, agree to what that tolerance allows, keep the fluid volume (to the PSPG
-    divergence error) and keep the wall nodes fixed."""
+def test_c3_full_size_matches_tight_fp64(gpu_lib):
+    """The C3 mesh (330k nodes, 1.74M tets, 1.32M unknowns) at the bench's tolerances: two Picard
+    steps of the mixed form (FP64 refinement to relative residual C3_MIXED_TOL) against the plain
+    FP64 form with its linear solves taken to 1e-14, i.e. to the accuracy of the reference's
+    direct solver.  Per field within 1e-6 relative, the same Picard iteration counts, positions
+    within 1e-10; wall nodes stay fixed and the fluid volume is kept to the PSPG divergence
+    error.  (A SuperLU oracle step of this 1.32M-unknown system does not finish in 20 minutes;
+    the oracle comparison at C3's parameters is test_c3_parameters_match_oracle.)"""
     from pfem_gb300 import workloads as W
 
     mesh = W.c3()
     N = mesh.n_nodes
-    q0 = M.incomp_initial_states(mesh, column=(0.5, 0.5, 1.0))
+    q0 = M.incomp_initial_states(mesh, column=W.C3_COLUMN)
     bound = (mesh.flags & M.BOUND) != 0
     out = {}
-    for prec in (api.PREC_MIXED, api.PREC_FP64):
+    for prec, tol in ((api.PREC_MIXED, W.C3_MIXED_TOL), (api.PREC_FP64, 1e-14)):
         p = api.default_params(api.KIND_INCOMP_PSPG, 3)
         p.precision = prec
-        p.krylov_rel_tol, p.krylov_abs_tol = 1e-8, 0.0
+        p.krylov_rel_tol, p.krylov_abs_tol = tol, 0.0
+        p.krylov_max_iter = 50000
         ctx = api.Context(p)
         ctx.upload_mesh(mesh)
         ctx.set_states(q0)
         v0 = ctx.volume()
         its = []
         for _ in range(2):
-            st = ctx.picard_step(5e-4)
+            st = ctx.picard_step(W.C3_DT)
             assert st.converged == 1
             its.append(st.picard_iterations)
         x = ctx.get_positions()
         assert np.isfinite(x).all() and np.array_equal(x[:, bound], mesh.pos[:, bound])
         assert abs(ctx.volume() / v0 - 1) < 1e-3, ctx.volume() / v0 - 1
-        out[prec] = (its, ctx.get_states())
+        out[prec] = (its, ctx.get_states(), x)
         ctx.close()
-    assert out[api.PREC_MIXED][0] == out[api.PREC_FP64][0]
-    assert max(field_errs(out[api.PREC_MIXED][1], out[api.PREC_FP64][1], 3, N)) < 1e-3
+    (it_m, q_m, x_m), (it_f, q_f, x_f) = out[api.PREC_MIXED], out[api.PREC_FP64]
+    assert it_m == it_f
+    errs = field_errs(q_m, q_f, 3, N)
+    assert max(errs) <= 1e-6, errs
+    assert np.abs(x_m - x_f).max() / np.abs(x_f).max() < 1e-10
+
+
+def test_c3_parameters_match_oracle(gpu_lib):
+    """C3's tank, column, dt (5e-4), fluid and tolerance on a coarser lattice (h = 0.035, 12k
+    nodes, 49k unknowns: the size at which one SuperLU/COLAMD factorisation of the oracle takes
+    ~16 s; at h = 0.02 it runs for over 20 minutes): one Picard step of the mixed form against
+    the FP64 oracle, within 1e-6 per field with the oracle's Picard iteration count."""
+    from pfem_gb300 import workloads as W
+
+    mesh = W.c3(0.035)
+    N = mesh.n_nodes
+    q0 = M.incomp_initial_states(mesh, column=W.C3_COLUMN)
+    ctx = make_ctx(mesh, krylov_rel_tol=W.C3_MIXED_TOL, krylov_abs_tol=0.0)
+    ctx.set_states(q0)
+    st = ctx.picard_step(W.C3_DT)
+    om = O.OracleMesh(mesh)
+    qo, res = O.pspg_picard_step(om, q0, W.C3_DT, g=gravity(3))
+    assert st.converged == 1 and res.converged
+    assert st.picard_iterations == res.iterations
+    errs = field_errs(ctx.get_states(), qo, 3, N)
+    assert max(errs) <= 1e-6, errs
+    assert np.abs(ctx.get_positions() - om.positions).max() < 1e-12
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_double_float_assembly_matches_oracle(gpu_lib, which, c1_mesh, small3d_mesh):
+    """The FP32 system assembled in double-float arithmetic (PFG_ASM_DOUBLE_FLOAT) steers the
+    correction solves differently but converges to the same FP64 solution: a Picard step within
+    1e-8 of the oracle with its iteration count."""
+    mesh = c1_mesh if which == "c1" else small3d_mesh
+    d, N = mesh.dim, mesh.n_nodes
+    column = (1.0, 2.0) if d == 2 else (0.2, 0.3, 0.3)
+    q0 = M.incomp_initial_states(mesh, column=column)
+    ctx = make_ctx(mesh, assembly=api.ASM_DOUBLE_FLOAT)
+    ctx.set_states(q0)
+    st = ctx.picard_step(1e-3)
+    om = O.OracleMesh(mesh)
+    qo, res = O.pspg_picard_step(om, q0, 1e-3, g=gravity(d))
+    assert st.converged == 1 and st.picard_iterations == res.iterations
+    assert max(field_errs(ctx.get_states(), qo, d, N)) < 1e-8
