@@ -258,7 +258,9 @@ PFG_API int pfg_device_bytes(const pfg_ctx* ctx, size_t* bytes);
  * independent meshes stored back to back, instance i owning nodes
  * [node_offsets[i], node_offsets[i+1]) and only elements among them.  rho[i], mu[i] are the
  * instance's fluid parameters (gamma is shared).  No reference counterpart: the reference runs
- * one Problem per process; this replaces n_inst independent SolverIncompNewton objects. */
+ * one Problem per process; this replaces n_inst independent SolverIncompNewton objects.
+ * Also for weakly compressible contexts in mixed precision (pfg_wc_step_batch): there mu[i] is
+ * per instance, rho[i] must equal rho_star, and surface tension is not available. */
 PFG_API int pfg_set_instances(pfg_ctx* ctx, int32_t n_inst, const int32_t* node_offsets, const double* rho,
                               const double* mu);
 /* One Picard time step of every instance at once (instance i with time step dt[i]); each
@@ -271,6 +273,12 @@ PFG_API int pfg_picard_step_batch(pfg_ctx* ctx, const double* dt, pfg_step_statu
  * of computeNextDT (WCompNewton/Solver.cpp:192-234), which is refreshed after every step.
  * Returns after all steps with a single host synchronisation. */
 PFG_API int pfg_wc_step(pfg_ctx* ctx, double dt, int32_t nsteps, pfg_step_status* status);
+
+/* Batched weakly compressible steps (mixed precision): after pfg_set_instances on a WC context,
+ * every instance steps at once with its own CFL time step (dt <= 0) or the shared fixed dt,
+ * each exactly as it would alone; status[i] receives instance i's dt and time.  The reference
+ * runs one Problem per process; this replaces n_inst independent SolverWCompNewton objects. */
+PFG_API int pfg_wc_step_batch(pfg_ctx* ctx, double dt, int32_t nsteps, pfg_step_status* status);
 
 /* Asynchronous form of pfg_wc_step: enqueues nsteps steps on the context's stream and returns
  * without waiting.  pfg_synchronize waits for all enqueued work and fills the status (dt and

@@ -41,6 +41,7 @@ EXPORTED = (
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
     "pfg_upload_facets", "pfg_set_positions", "pfg_get_spmv_pairs", "pfg_set_temperature",
     "pfg_get_temperature", "pfg_heat_set_bc", "pfg_heat_set_flux", "pfg_heat_step", "pfg_upload_mesh_remap",
+    "pfg_wc_step_batch",
 )
 NUM_PHASES = 17
 
@@ -110,6 +111,7 @@ def load(path=LIB_PATH):
         "pfg_set_dirichlet": ([vp, C.c_int32, ip, dp], C.c_int),
         "pfg_picard_step": ([vp, C.c_double, C.POINTER(StepStatus)], C.c_int),
         "pfg_wc_step": ([vp, C.c_double, C.c_int32, C.POINTER(StepStatus)], C.c_int),
+        "pfg_wc_step_batch": ([vp, C.c_double, C.c_int32, C.POINTER(StepStatus)], C.c_int),
         "pfg_next_dt": ([vp, dp], C.c_int),
         "pfg_set_time": ([vp, C.c_double, C.c_double], C.c_int),
         "pfg_volume": ([vp, dp], C.c_int),
@@ -337,6 +339,13 @@ class Context:
         st = StepStatus()
         self._check(self.L.pfg_wc_step(self.h, float(dt), int(nsteps), C.byref(st)), "pfg_wc_step")
         return st
+
+    def wc_step_batch(self, dt, nsteps=1):
+        """nsteps weakly compressible steps of every instance; one StepStatus per instance."""
+        n = getattr(self, "n_inst", 1)
+        st = (StepStatus * n)()
+        self._check(self.L.pfg_wc_step_batch(self.h, float(dt), int(nsteps), st), "pfg_wc_step_batch")
+        return list(st)
 
     def wc_step_async(self, dt, nsteps=1):
         self._check(self.L.pfg_wc_step_async(self.h, float(dt), int(nsteps)), "pfg_wc_step_async")

@@ -732,10 +732,14 @@ PFG_API int pfg_set_instances(pfg_ctx* c, int32_t n_inst, const int32_t* node_of
                               const double* mu) {
     int rc = check_ctx(c);
     if (rc) return rc;
-    if (c->prm.kind != PFG_KIND_INCOMP_PSPG || c->prm.precision != PFG_PREC_MIXED)
-        return fail(c, PFG_ERR_STATE, "instances need an incompressible context in mixed precision");
+    if (c->prm.precision != PFG_PREC_MIXED)
+        return fail(c, PFG_ERR_STATE, "instances need a context in mixed precision");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
     if (n_inst <= 0 || !node_offsets || !rho || !mu) return fail(c, PFG_ERR_INVALID, "pfg_set_instances: bad arguments");
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT)
+        for (int i = 0; i < n_inst; ++i)
+            if (rho[i] != c->prm.rho_star)
+                return fail(c, PFG_ERR_UNSUPPORTED, "weakly compressible instances share rho* (instance %d)", i);
     if (node_offsets[0] != 0 || node_offsets[n_inst] != c->N)
         return fail(c, PFG_ERR_INVALID, "node offsets must start at 0 and end at the node count %d", c->N);
     for (int i = 0; i < n_inst; ++i) {
@@ -756,6 +760,10 @@ PFG_API int pfg_set_instances(pfg_ctx* c, int32_t n_inst, const int32_t* node_of
         for (int k = 1; k < c->npe; ++k)
             if (inst_of(conn[(size_t)k * c->E + e]) != i0)
                 return fail(c, PFG_ERR_INVALID, "element %d joins nodes of two instances", e);
+    }
+    if (c->prm.kind == PFG_KIND_WC_CDS_DPDT) {
+        if (c->has_facets) return fail(c, PFG_ERR_UNSUPPORTED, "batched weakly compressible steps without facets");
+        return wcm_set_instances(c, n_inst, node_offsets, mu);
     }
     return mx_set_instances(c, n_inst, node_offsets, rho, mu);
 }
@@ -781,6 +789,17 @@ PFG_API int pfg_wc_step(pfg_ctx* c, double dt, int32_t nsteps, pfg_step_status* 
     if ((rc = check_facets(c))) return rc;
     if (nsteps < 0 || !st) return fail(c, PFG_ERR_INVALID, "pfg_wc_step: bad arguments");
     return wc_steps(c, dt, nsteps, st);
+}
+
+PFG_API int pfg_wc_step_batch(pfg_ctx* c, double dt, int32_t nsteps, pfg_step_status* st) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_WC_CDS_DPDT) return fail(c, PFG_ERR_STATE, "context is not weakly compressible");
+    if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
+    if (nsteps < 0 || !st) return fail(c, PFG_ERR_INVALID, "pfg_wc_step_batch: bad arguments");
+    c->wc_pending = 0;
+    if ((rc = wc_enqueue(c, dt, nsteps))) return rc;
+    return wc_sync_batch(c, st);
 }
 
 PFG_API int pfg_wc_step_async(pfg_ctx* c, double dt, int32_t nsteps) {

@@ -485,15 +485,22 @@ __global__ void k_wc_mass(int E, int N, const int* __restrict__ conn, const doub
 }
 
 // dt in both precisions: the plain step reads the double, the mixed step the float copy
-__global__ void k_set_dt(double* tdt, double v) {
-    tdt[T_DT] = v;
-    reinterpret_cast<float*>(tdt + 4)[0] = (float)v;
+// Every instance's time-step slot (8 doubles each; one slot unless the mixed form is batched).
+__global__ void k_set_dt(double* tdt, double v, int n_slots) {
+    for (int i = 0; i < n_slots; ++i) {
+        double* t = tdt + 8 * i;
+        t[T_DT] = v;
+        reinterpret_cast<float*>(t + 4)[0] = (float)v;
+    }
 }
 
-__global__ void k_set_time(double* tdt, double t, double v) {
-    tdt[T_DT] = v;
-    tdt[T_TIME] = t;
-    reinterpret_cast<float*>(tdt + 4)[0] = (float)v;
+__global__ void k_set_time(double* tdt, double t, double v, int n_slots) {
+    for (int i = 0; i < n_slots; ++i) {
+        double* s = tdt + 8 * i;
+        s[T_DT] = v;
+        s[T_TIME] = t;
+        reinterpret_cast<float*>(s + 4)[0] = (float)v;
+    }
 }
 
 bool mixed(pfg_ctx* c) { return c->prm.precision == PFG_PREC_MIXED; }
@@ -627,15 +634,16 @@ int wc_alloc(pfg_ctx* c) {
             return rc;
         PFG_CUDA(c, cudaMemsetAsync(c->ws.p, 0, sizeof(double) * (2 * c->dim + 2) * N, c->stream));
     }
+    c->n_wc_inst = 1;
     PFG_CUDA(c, cudaMemsetAsync(c->wc_dt.p, 0, 64, c->stream));
-    k_set_time<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), c->host_time, c->prm.max_dt);
+    k_set_time<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), c->host_time, c->prm.max_dt, 1);
     PFG_CHECK_LAUNCH(c);
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     return PFG_OK;
 }
 
 int wc_set_time(pfg_ctx* c, double time, double next_dt) {
-    k_set_time<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), time, next_dt);
+    k_set_time<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), time, next_dt, c->n_wc_inst);
     PFG_CHECK_LAUNCH(c);
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     c->host_time = time;
@@ -675,7 +683,7 @@ int wc_get_states(pfg_ctx* c, double* h) {
 int wc_enqueue(pfg_ctx* c, double dt, int nsteps) {
     const bool adapt = !(dt > 0);
     if (!adapt) {
-        k_set_dt<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), dt);
+        k_set_dt<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), dt, c->n_wc_inst);
         PFG_CHECK_LAUNCH(c);
     }
     if (c->prof) {
@@ -703,6 +711,25 @@ int wc_sync(pfg_ctx* c, pfg_step_status* st) {
     st->dt = c->h_scalars[0];
     st->time = c->h_scalars[1];
     c->host_time = st->time;
+    c->wc_pending = 0;
+    return PFG_OK;
+}
+
+// Batched mixed contexts: every instance's dt and time (slot i of wc_dt) into st[i].
+int wc_sync_batch(pfg_ctx* c, pfg_step_status* st) {
+    const int K = c->n_wc_inst;
+    std::vector<double> slots((size_t)8 * K);
+    PFG_CUDA(c, cudaMemcpyAsync(slots.data(), c->wc_dt.p, sizeof(double) * slots.size(), cudaMemcpyDeviceToHost,
+                                c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < K; ++i) {
+        std::memset(&st[i], 0, sizeof(st[i]));
+        st[i].converged = 1;
+        st[i].steps_done = c->wc_pending;
+        st[i].dt = slots[(size_t)8 * i + T_DT];
+        st[i].time = slots[(size_t)8 * i + T_TIME];
+    }
+    c->host_time = st[0].time;
     c->wc_pending = 0;
     return PFG_OK;
 }

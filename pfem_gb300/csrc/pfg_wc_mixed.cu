@@ -68,9 +68,22 @@ WcmConst make_mconst(pfg_ctx* c) {
     return k;
 }
 
-// wc_dt slots: doubles [dt, time, min, ticket], float dt at byte offset 32
+// wc_dt: one 64-byte slot per instance (TSLOT doubles): doubles [dt, time, min, ticket], float dt
+// at byte offset 32 and, for batched contexts, the running CFL minimum as FP32 bits at byte 36
 enum : int { T_DT = 0, T_TIME = 1, T_MIN = 2, T_TICKET = 3 };
+constexpr int TSLOT = 8;
+constexpr unsigned MIN_NONE = 0x7f800000u;  // +inf: no candidate yet
 __device__ __forceinline__ float* dtf_ptr(double* tdt) { return reinterpret_cast<float*>(tdt + 4); }
+__device__ __forceinline__ unsigned* minbits_ptr(double* tdt) { return reinterpret_cast<unsigned*>(tdt + 4) + 1; }
+
+// Independent meshes stored back to back in one context (pfg_set_instances on a mixed WC
+// context): node -> instance map and per-instance [mu, mu sum_g w_g]; node_inst == nullptr
+// for a single mesh.
+struct WcInst {
+    const int* node_inst;
+    const float* f;
+    __device__ __forceinline__ int of(int n) const { return node_inst ? __ldg(node_inst + n) : 0; }
+};
 
 // ---- error-free transforms ------------------------------------------------------------
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -276,13 +289,14 @@ template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* __restrict__ conn,
                                                        const uint8_t* __restrict__ flags, St st,
                                                        const double* __restrict__ tdt, WcmConst k,
-                                                       const int* __restrict__ slot, float* __restrict__ cb) {
+                                                       const int* __restrict__ slot, float* __restrict__ cb,
+                                                       WcInst wi) {
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    const float dt = *dtf_ptr(const_cast<double*>(tdt));
     int nd[NPE];
     load_nodes<DIM>(conn, E, e, nd);
+    const float dt = *dtf_ptr(const_cast<double*>(tdt) + TSLOT * wi.of(nd[0]));
     float xh[NPE][DIM], xl[NPE][DIM], vh[NPE][DIM], vl[NPE][DIM];
 #pragma unroll
     for (int j = 0; j < NPE; ++j) predict_node<DIM>(st, N, nd[j], flags[nd[j]] & F_FIXED, dt, xh[j], xl[j], vh[j], vl[j]);
@@ -328,11 +342,12 @@ __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* 
 // continuity records (ContEquation.inl:396-409), applies the free-node BC and Tait EOS.
 template <int DIM>
 __global__ void k_m_cont_node(int N, const int* __restrict__ ne_ptr, const uint8_t* __restrict__ flags,
-                              const float* __restrict__ cb, WcmConst k, St st, double* __restrict__ tdt) {
+                              const float* __restrict__ cb, WcmConst k, St st, double* __restrict__ tdt,
+                              WcInst wi) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    const float dt = *dtf_ptr(tdt);
-    if (n == 0) tdt[T_TIME] += (double)dt;  // Problem::updateTime
+    if (!wi.node_inst && n == 0) tdt[T_TIME] += (double)*dtf_ptr(tdt);  // Problem::updateTime
     if (n >= N) return;
+    const float dt = *dtf_ptr(tdt + TSLOT * wi.of(n));
     const uint8_t fl = flags[n];
     {
         float xh[DIM], xl[DIM], vh[DIM], vl[DIM];
@@ -370,13 +385,15 @@ __global__ void k_m_cont_node(int N, const int* __restrict__ ne_ptr, const uint8
 // Momentum element kernel (MomEquation.inl:229-302) and the element's CFL length.
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* __restrict__ conn, St st, WcmConst k,
-                                                      const int* __restrict__ slot, float* __restrict__ cb) {
+                                                      const int* __restrict__ slot, float* __restrict__ cb,
+                                                      WcInst wi) {
     using L = Rec<DIM>;
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[NPE];
     load_nodes<DIM>(conn, E, e, nd);
+    const float mu_sum = wi.f ? wi.f[2 * wi.of(nd[0]) + 1] : k.mu_sum;
     float Jh[DIM][DIM], Jl[DIM][DIM], J[DIM][DIM];
     jac_df<DIM>(st, N, nd, Jh, Jl);
 #pragma unroll
@@ -414,7 +431,7 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
         }
 #pragma unroll
     for (int a = 0; a < DIM; ++a) divA += Lg[a][a];
-    const float kf = k.mu_sum / ae;
+    const float kf = mu_sum / ae;
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
         const int q = __ldg(slot + (size_t)e * NPE + i);
@@ -458,7 +475,7 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
 
 // Momentum node kernel (MomEquation.inl:201-226,279-374): sums the node's records, adds the
 // surface tension of its free-surface facets (in FP32), applies the BCs, updates acceleration
-// and velocity.  With `partials`, also the CFL time step of the next
+// and velocity.  With `cfl`, also the CFL time step of the next
 // step (computeNextDT, WCompNewton/Solver.cpp:192-234): the reference's minimum over elements
 // of sc^2 h_e^2 / max_{nodes of e} max(|u|^2, c^2, 4 alpha^2 / h_e^2) equals the minimum over
 // nodes of the same expression at the node's smallest incident h_e (it grows with h_e), and in
@@ -468,11 +485,12 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_node(int N, const int* __restri
                                                       const uint8_t* __restrict__ flags, const float* __restrict__ cb,
                                                       const double* __restrict__ vbc, double* __restrict__ tdt,
                                                       WcmConst k, St st, float* __restrict__ partials,
-                                                      const float* __restrict__ fst) {
+                                                      const float* __restrict__ fst, WcInst wi, bool cfl) {
     using L = Rec<DIM>;
     __shared__ float sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    const float dt = *dtf_ptr(tdt);
+    const int inst = n < N ? wi.of(n) : 0;
+    const float dt = *dtf_ptr(tdt + TSLOT * inst);
     float best = 3.0e38f;
     if (n < N) {
         float m = 0, F[DIM], Wh[DIM], Wl[DIM];
@@ -530,15 +548,29 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_node(int N, const int* __restri
             st.vl[kk] = vl;
             u2 += vh * vh;
         }
-        if (partials && q1 > q0) {
+        if (cfl && q1 > q0) {
             const float rho = k.rho_star + st.rd[n];
             const float m1 = fmaxf(u2, (k.K0 + k.K0p * st.ph[n]) / rho);
-            const float m2 = k.mu / rho;
+            const float m2 = (wi.f ? wi.f[2 * inst] : k.mu) / rho;
             const float maxSq = fmaxf(m1, 4.0f * m2 * m2 / (hmin * hmin));
             best = k.sc * k.sc * hmin * hmin / maxSq;
         }
     }
-    if (!partials) return;
+    if (!cfl) return;
+    if (wi.node_inst) {
+        // per-instance minimum: atomic min of the (positive) FP32 bit patterns, one atomic per
+        // warp when the warp's nodes belong to one instance (min is exact in any order)
+        const int i0 = __shfl_sync(0xffffffffu, inst, 0);
+        if (__all_sync(0xffffffffu, n >= N || inst == i0)) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_down_sync(0xffffffffu, best, o));
+            if ((threadIdx.x & 31) == 0 && best < 3.0e38f)
+                atomicMin(minbits_ptr(tdt + TSLOT * i0), __float_as_uint(best));
+        } else if (n < N && best < 3.0e38f) {
+            atomicMin(minbits_ptr(tdt + TSLOT * inst), __float_as_uint(best));
+        }
+        return;
+    }
     // grid minimum: block minimum, then the last block to finish reduces the block minima
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_down_sync(0xffffffffu, best, o));
@@ -583,9 +615,31 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_node(int N, const int* __restri
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_m_dt(int E, int N, const int* __restrict__ conn, St st,
                                                 const float* __restrict__ nodal, WcmConst k,
-                                                float* __restrict__ partials, double* __restrict__ tdt) {
+                                                float* __restrict__ partials, double* __restrict__ tdt, WcInst wi) {
     __shared__ float sh[32];
     float best = 3.0e38f;
+    if (wi.node_inst) {  // batched: each element's candidate to its instance's minimum
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+            int nd[DIM + 1];
+            load_nodes<DIM>(conn, E, e, nd);
+            float Jh[DIM][DIM], Jl[DIM][DIM], J[DIM][DIM];
+            jac_df<DIM>(st, N, nd, Jh, Jl);
+#pragma unroll
+            for (int r = 0; r < DIM; ++r)
+#pragma unroll
+                for (int c = 0; c < DIM; ++c) J[r][c] = Jh[r][c] + Jl[r][c];
+            const float he = cfl_length<DIM>(J, det_f<DIM>(J) * k.refSize);
+            float m1 = 0, m2 = 0;
+#pragma unroll
+            for (int a = 0; a <= DIM; ++a) {
+                m1 = fmaxf(m1, nodal[nd[a]]);
+                m2 = fmaxf(m2, nodal[(size_t)N + nd[a]]);
+            }
+            const float maxSq = fmaxf(m1, 4.0f * m2 * m2 / (he * he));
+            atomicMin(minbits_ptr(tdt + TSLOT * wi.of(nd[0])), __float_as_uint(k.sc * k.sc * he * he / maxSq));
+        }
+        return;
+    }
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
         int nd[DIM + 1];
         load_nodes<DIM>(conn, E, e, nd);
@@ -645,7 +699,7 @@ __global__ void __launch_bounds__(BLOCK) k_m_dt(int E, int N, const int* __restr
 }
 
 template <int DIM>
-__global__ void k_m_nodal(int N, St st, WcmConst k, float* __restrict__ nodal) {
+__global__ void k_m_nodal(int N, St st, WcmConst k, float* __restrict__ nodal, WcInst wi) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     float u2 = 0;
@@ -653,7 +707,26 @@ __global__ void k_m_nodal(int N, St st, WcmConst k, float* __restrict__ nodal) {
     for (int f = 0; f < DIM; ++f) u2 += st.vh[(size_t)f * N + n] * st.vh[(size_t)f * N + n];
     const float rho = k.rho_star + st.rd[n];
     nodal[n] = fmaxf(u2, (k.K0 + k.K0p * st.ph[n]) / rho);
-    nodal[(size_t)N + n] = k.mu / rho;
+    nodal[(size_t)N + n] = (wi.f ? wi.f[2 * wi.of(n)] : k.mu) / rho;
+}
+
+// Batched contexts, after a step (advance = 1) or a CFL evaluation: each instance's slot takes
+// its new time step dt = min(sqrt(min), maxDT) from the collected minimum (adaptive mode), the
+// time advances by the step's dt (Problem::updateTime), and the minimum is reset.
+__global__ void k_m_finalize(int n_inst, double* __restrict__ tdt, float max_dt, int adapt, int advance) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_inst) return;
+    double* t = tdt + TSLOT * i;
+    if (advance) t[T_TIME] += (double)*dtf_ptr(t);
+    unsigned* mb = minbits_ptr(t);
+    if (adapt && *mb != MIN_NONE) {
+        const float r = __uint_as_float(*mb);
+        const float dtn = fminf(sqrtf(r), max_dt);
+        *dtf_ptr(t) = dtn;
+        t[T_DT] = (double)dtn;
+        t[T_MIN] = (double)r;
+    }
+    *mb = MIN_NONE;
 }
 
 // ---- API conversions (FP64, outside the step) -------------------------------------------
@@ -705,6 +778,10 @@ __global__ void k_m_vbc(int n, const double* __restrict__ vbc, float* __restrict
 
 St st_of(pfg_ctx* c) { return state_ptrs(ptr<float>(c->ws), c->dim, c->N, c->wc_cur); }
 
+WcInst wi_of(pfg_ctx* c) {
+    return c->n_wc_inst > 1 ? WcInst{ptr<int>(c->node_inst), ptr<float>(c->wc_inst)} : WcInst{nullptr, nullptr};
+}
+
 template <int DIM>
 int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
     const int N = c->N, E = c->E;
@@ -717,17 +794,18 @@ int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
     const double* vbcf = reinterpret_cast<const double*>(ptr<float>(c->wc_eld));  // FP32 Dirichlet values
     const int gn = div_up(N, BLOCK), ge = std::max(1, div_up(E, BLOCK));
     const uint8_t* flags = ptr<uint8_t>(c->flags);
+    const WcInst wi = wi_of(c);
     if (E > 0) {
         prof_begin(c, PH_WC_CONT_ELEM);
-        k_m_cont_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), flags, st, tdt, k, slot, cb);
+        k_m_cont_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), flags, st, tdt, k, slot, cb, wi);
         prof_end(c, PH_WC_CONT_ELEM);
     }
     prof_begin(c, PH_WC_CONT_NODE);
-    k_m_cont_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), flags, cb, k, st, tdt);
+    k_m_cont_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), flags, cb, k, st, tdt, wi);
     prof_end(c, PH_WC_CONT_NODE);
     if (E > 0) {
         prof_begin(c, PH_WC_MOM_ELEM);
-        k_m_mom_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, k, slot, cb);
+        k_m_mom_elem<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, k, slot, cb, wi);
         prof_end(c, PH_WC_MOM_ELEM);
     }
     prof_begin(c, PH_WC_MOM_NODE);
@@ -735,8 +813,10 @@ int launch_mstep(pfg_ctx* c, bool adapt, const WcmConst& k) {
     if (fa.nodes)
         k_fst<DIM, float><<<div_up(fa.n_nodes, BLOCK), BLOCK, 0, c->stream>>>(
             fa, E, ptr<int>(c->conn), PosDF{st.xh, st.xl, N}, N, ptr<float>(c->fst_force));
-    k_m_mom_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), flags, cb, vbcf, tdt, k, st,
-                                                   adapt && E > 0 ? partials : nullptr, fst_force<float>(c));
+    k_m_mom_node<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<int>(c->ne_ptr), flags, cb, vbcf, tdt, k, st, partials,
+                                                   fst_force<float>(c), wi, adapt && E > 0);
+    if (wi.node_inst)  // batched: each instance's new dt and time
+        k_m_finalize<<<div_up(c->n_wc_inst, 128), 128, 0, c->stream>>>(c->n_wc_inst, tdt, k.max_dt, adapt && E > 0, 1);
     prof_end(c, PH_WC_MOM_NODE);
     PFG_CHECK_LAUNCH(c);
     return PFG_OK;
@@ -820,14 +900,63 @@ int wcm_next_dt(pfg_ctx* c) {
     float* nodal = ptr<float>(c->wc_nodal);
     const int grid = std::min(c->max_grid, div_up(E, BLOCK));
     float* partials = reinterpret_cast<float*>(ptr<double>(c->red));
+    const WcInst wi = wi_of(c);
     if (c->dim == 2) {
-        k_m_nodal<2><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, st, k, nodal);
-        k_m_dt<2><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, nodal, k, partials, ptr<double>(c->wc_dt));
+        k_m_nodal<2><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, st, k, nodal, wi);
+        k_m_dt<2><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, nodal, k, partials, ptr<double>(c->wc_dt),
+                                                 wi);
     } else {
-        k_m_nodal<3><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, st, k, nodal);
-        k_m_dt<3><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, nodal, k, partials, ptr<double>(c->wc_dt));
+        k_m_nodal<3><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, st, k, nodal, wi);
+        k_m_dt<3><<<grid, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), st, nodal, k, partials, ptr<double>(c->wc_dt),
+                                                 wi);
     }
+    if (wi.node_inst)
+        k_m_finalize<<<div_up(c->n_wc_inst, 128), 128, 0, c->stream>>>(c->n_wc_inst, ptr<double>(c->wc_dt), k.max_dt,
+                                                                      1, 0);
     PFG_CHECK_LAUNCH(c);
+    return PFG_OK;
+}
+
+// Independent meshes stored back to back (node_off), each with its own viscosity; every
+// instance gets its own time-step slot, initialised from the context's current one.
+__global__ void k_m_slots_init(int n_inst, double* __restrict__ tdt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_inst) return;
+    double* t = tdt + TSLOT * i;
+    if (i > 0)
+        for (int k = 0; k < TSLOT; ++k) t[k] = tdt[k];
+    *minbits_ptr(t) = MIN_NONE;
+}
+
+int wcm_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* mu) {
+    wc_release_graphs(c);
+    const GaussConst gc = gauss_const(c->dim);
+    std::vector<float> f((size_t)2 * n_inst);
+    std::vector<int> node_inst((size_t)std::max(c->N, 1));
+    for (int i = 0; i < n_inst; ++i) {
+        double mus = 0;
+        for (int q = 0; q < gc.n; ++q) mus += mu[i] * gc.w[q];
+        f[2 * i] = (float)mu[i];
+        f[2 * i + 1] = (float)mus;
+        for (int n = node_off[i]; n < node_off[i + 1]; ++n) node_inst[n] = i;
+    }
+    int rc;
+    // the first slot keeps its contents: copy it out before the buffer may move
+    double slot0[TSLOT];
+    PFG_CUDA(c, cudaMemcpyAsync(slot0, c->wc_dt.p, sizeof(slot0), cudaMemcpyDeviceToHost, c->stream));
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if ((rc = ensure(c, c->wc_inst, sizeof(float) * f.size())) ||
+        (rc = ensure(c, c->node_inst, sizeof(int) * node_inst.size())) ||
+        (rc = ensure(c, c->wc_dt, sizeof(double) * TSLOT * (size_t)n_inst)))
+        return rc;
+    PFG_CUDA(c, cudaMemcpyAsync(c->wc_dt.p, slot0, sizeof(slot0), cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->wc_inst.p, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice, c->stream));
+    PFG_CUDA(c, cudaMemcpyAsync(c->node_inst.p, node_inst.data(), sizeof(int) * node_inst.size(),
+                                cudaMemcpyHostToDevice, c->stream));
+    k_m_slots_init<<<div_up(n_inst, 128), 128, 0, c->stream>>>(n_inst, ptr<double>(c->wc_dt));
+    PFG_CHECK_LAUNCH(c);
+    PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->n_wc_inst = n_inst;
     return PFG_OK;
 }
 
