@@ -325,7 +325,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
                     &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
                     &c->pe_ptr, &c->pe_item, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
-                    &c->mx_rec, &c->mx_gdf, &c->wc_inst};
+                    &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos};
     wc_release_graphs(c);
     mg_release(c);
     mx_release_graph(c);

@@ -140,6 +140,7 @@ struct pfg_ctx {
     // element prep's inputs), and the element records of A_e x (one 32-byte record of d+1
     // double-float values per element node)
     pfg::DBuf mx_scale32, mx_f32, mx_xdf, mx_vpdf, mx_tdf, mx_rec, mx_gdf;
+    pfg::DBuf mx_ed_aos;  // element data element-major (high, then low parts) for the gathering kernels
     int n_inst = 0, n_seg = 0;
     cudaGraphExec_t mx_graph[2] = {nullptr, nullptr};  // one chunk of BiCGSTAB iterations [FP32, FP64]
     std::vector<int> h_mx_ii;

@@ -203,17 +203,49 @@ __device__ __forceinline__ DF inst_df(const float* f32, int inst, int which) {
     return DF{f32[inst * F_COUNT + which], f32[inst * F_COUNT + which + 1]};
 }
 
-// Element data as double-float planes: value v of element e is h[v E + e] + l[v E + e].
+// Element data as double-float planes: value v of element e is h[v E + e] + l[v E + e] (the
+// element kernels' coalesced layout), and the same values element-major in `a`: element e's
+// ED_AOS floats hold its high parts (slots 0..15) then its low parts (16..31), so a kernel that
+// gathers an element by index reads two (FP32) or four (double-float) 32-byte sectors instead of
+// one sector per value.
+constexpr int ED_AOS = 32;
 struct EdPlanes {
     const float* h;
     const float* l;
+    const float* a;
     int E;
     __device__ __forceinline__ DF df(int v, int e) const {
         const size_t o = (size_t)v * E + e;
         return DF{__ldg(h + o), __ldg(l + o)};
     }
     __device__ __forceinline__ float f(int v, int e) const { return __ldg(h + (size_t)v * E + e); }
+    __device__ __forceinline__ DF gdf(int v, int e) const {
+        const float* r = a + (size_t)e * ED_AOS;
+        return DF{__ldg(r + v), __ldg(r + 16 + v)};
+    }
+    __device__ __forceinline__ float gf(int v, int e) const { return __ldg(a + (size_t)e * ED_AOS + v); }
 };
+
+// Stores element e's values v (high and low parts) in both layouts.
+template <int NV>
+__device__ __forceinline__ void ed_store(float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea, int E,
+                                         int e, const DF (&v)[NV]) {
+    static_assert(NV <= 16, "element record holds 16 values");
+    float r[ED_AOS];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        r[k] = k < NV ? v[k < NV ? k : 0].h : 0.0f;
+        r[16 + k] = k < NV ? v[k < NV ? k : 0].l : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        eh[(size_t)k * E + e] = v[k].h;
+        el[(size_t)k * E + e] = v[k].l;
+    }
+    float4* d = reinterpret_cast<float4*>(ea + (size_t)e * ED_AOS);
+#pragma unroll
+    for (int k = 0; k < ED_AOS / 4; ++k) d[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+}
 
 __device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
 
@@ -223,7 +255,7 @@ __device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a,
 template <int DIM>
 __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
                           const double* __restrict__ q_iter, Mx m, double refSize, ViscArgs va,
-                          float* __restrict__ eh, float* __restrict__ el) {
+                          float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -259,12 +291,10 @@ __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const doub
 #pragma unroll
         for (int i = 0; i <= DIM; ++i) v[2 + f * (DIM + 1) + i] = G[f][i];
     v[ed_ksum<DIM>()] = k_sum<DIM>(va, mu, G, q_iter, N, nd);
+    DF dv[ed_count<DIM>()];
 #pragma unroll
-    for (int k = 0; k < ed_count<DIM>(); ++k) {
-        const DF d = df_from(v[k]);
-        eh[(size_t)k * E + e] = d.h;
-        el[(size_t)k * E + e] = d.l;
-    }
+    for (int k = 0; k < ed_count<DIM>(); ++k) dv[k] = df_from(v[k]);
+    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, dv);
 }
 
 // Double-float copies of the positions and the iterate's velocities (inputs of k_mx_prep_df).
@@ -288,7 +318,7 @@ __global__ void k_mx_gprep(int N, const double* __restrict__ pos, const double* 
 template <int DIM>
 __global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const DF* __restrict__ gdf,
                              const float* __restrict__ f32, Mx m, DF ref_df, DF inv_pi, float* __restrict__ eh,
-                             float* __restrict__ el) {
+                             float* __restrict__ el, float* __restrict__ ea) {
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -362,17 +392,15 @@ __global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const D
     const DF c = df_div(inst_df(f32, inst, F_MU4R), df_mul(h, h));
     const DF nine{9.0f, 0.0f};
     const DF tau = df_div(DF{1.0f, 0.0f}, df_sqrt(df_add(df_add(df_mul(a, a), df_mul(b, b)), df_mul(nine, df_mul(c, c)))));
-    auto put = [&](int v, DF d) {
-        eh[(size_t)v * E + e] = d.h;
-        el[(size_t)v * E + e] = d.l;
-    };
-    put(0, det);
-    put(1, tau);
+    DF dv[ed_count<DIM>()];
+    dv[0] = det;
+    dv[1] = tau;
 #pragma unroll
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
-        for (int i = 0; i < NPE; ++i) put(2 + f * NPE + i, G[f][i]);
-    put(ed_ksum<DIM>(), inst_df(f32, inst, F_KSUM));
+        for (int i = 0; i < NPE; ++i) dv[2 + f * NPE + i] = G[f][i];
+    dv[ed_ksum<DIM>()] = inst_df(f32, inst, F_KSUM);
+    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, dv);
 }
 
 // Double-float copies of the previous velocities and (Boussinesq) the temperatures.
@@ -393,20 +421,20 @@ template <int DIM>
 __device__ __forceinline__ void pair_item_df(const EdPlanes& ed, int e, int i, int j, DF rho, DF inv_dt, DF l_sum,
                                              const MxConst& k, DF (&acc)[DIM + 1][DIM + 1]) {
     constexpr int NPE = DIM + 1;
-    const DF detJ = ed.df(0, e);
-    const DF tau = ed.df(1, e);
+    const DF detJ = ed.gdf(0, e);
+    const DF tau = ed.gdf(1, e);
     const DF ae = df_mul(detJ, k.ref_df);
     DF gi[DIM], gj[DIM];
 #pragma unroll
     for (int f = 0; f < DIM; ++f) {
-        gi[f] = ed.df(2 + f * NPE + i, e);
-        gj[f] = ed.df(2 + f * NPE + j, e);
+        gi[f] = ed.gdf(2 + f * NPE + i, e);
+        gj[f] = ed.gdf(2 + f * NPE + j, e);
     }
     DF dot = df_mul(gi[0], gj[0]);
 #pragma unroll
     for (int f = 1; f < DIM; ++f) dot = df_add(dot, df_mul(gi[f], gj[f]));
     const DF mij = df_mul(inv_dt, df_mul(df_mul(rho, k.mm_df[i][j]), ae));
-    const DF kf = df_mul(ae, ed.df(ed_ksum<DIM>(), e));
+    const DF kf = df_mul(ae, ed.gdf(ed_ksum<DIM>(), e));
 #pragma unroll
     for (int f1 = 0; f1 < DIM; ++f1) {
 #pragma unroll
@@ -569,15 +597,15 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
             const int i = ne_loc[q];
             int nd[NPE];
             load_nodes<DIM>(conn, E, e, nd);
-            const DF ae = df_mul(ed.df(0, e), k.ref_df);
-            const DF tau = ed.df(1, e);
+            const DF ae = df_mul(ed.gdf(0, e), k.ref_df);
+            const DF tau = ed.gdf(1, e);
             DF gi[DIM];
 #pragma unroll
-            for (int f = 0; f < DIM; ++f) gi[f] = ed.df(2 + f * NPE + i, e);
+            for (int f = 0; f < DIM; ++f) gi[f] = ed.gdf(2 + f * NPE + i, e);
             if constexpr (DFA) {
                 pair_item_df<DIM>(ed, e, i, i, rho, inv_dt, l_sum, k, A);
             } else {  // pspg_pair_block's (i, i) share in FP32
-                const float a32 = ae.h, t32 = tau.h, kf = a32 * ed.f(ed_ksum<DIM>(), e);
+                const float a32 = ae.h, t32 = tau.h, kf = a32 * ed.gf(ed_ksum<DIM>(), e);
                 float g[DIM], dot = 0.0f;
 #pragma unroll
                 for (int f = 0; f < DIM; ++f) {
@@ -664,11 +692,12 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
                 else if (dir && f2 < DIM && f1 != f2) v = 0.0;
                 a[f1][f2] = v;
             }
-        double s[B];
+        double s[B], si[B];  // S = |a_rr|^-1/2 and its inverse |a_rr|^1/2
 #pragma unroll
         for (int f = 0; f < B; ++f) {
             const double d = fabs(a[f][f]);
-            s[f] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+            si[f] = d > 0.0 ? sqrt(d) : 1.0;
+            s[f] = 1.0 / si[f];
             scale[(size_t)f * N + n] = s[f];
             scale32[(size_t)f * N + n] = (float)s[f];
         }
@@ -681,7 +710,7 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
             for (int f2 = 0; f2 < B; ++f2) {
                 binv64[(size_t)(f1 * B + f2) * N + n] = inv[f1][f2];
                 // (S A S)^-1 = S^-1 A^-1 S^-1
-                binv32[(size_t)(f1 * B + f2) * N + n] = (float)(inv[f1][f2] / (s[f1] * s[f2]));
+                binv32[(size_t)(f1 * B + f2) * N + n] = (float)(si[f1] * inv[f1][f2] * si[f2]);
                 out[f1 * B + f2] = (float)(s[f1] * a[f1][f2] * s[f2]);
             }
         const int b0 = nbr_ptr[n];
@@ -752,13 +781,13 @@ __global__ void __launch_bounds__(BLOCK) k_mx_asm32(int P, int N, const int* __r
             const int e = it >> 4;
             t.i = (it >> 2) & 3;
             t.j = it & 3;
-            t.ae = ed.f(0, e);
-            t.tau = ed.f(1, e);
-            t.ks = ed.f(ed_ksum<DIM>(), e);
+            t.ae = ed.gf(0, e);
+            t.tau = ed.gf(1, e);
+            t.ks = ed.gf(ed_ksum<DIM>(), e);
 #pragma unroll
             for (int f = 0; f < DIM; ++f) {
-                t.gi[f] = ed.f(2 + f * NPE + t.i, e);
-                t.gj[f] = ed.f(2 + f * NPE + t.j, e);
+                t.gi[f] = ed.gf(2 + f * NPE + t.i, e);
+                t.gj[f] = ed.gf(2 + f * NPE + t.j, e);
             }
         };
         Item nxt;
@@ -1471,7 +1500,7 @@ double ksum_newtonian(int dim, double mu) {
 EdPlanes ed_planes(pfg_ctx* c) {
     const int ned = c->dim == 2 ? ed_count<2>() : ed_count<3>();
     float* h = ptr<float>(c->edata_df);
-    return EdPlanes{h, h + (size_t)ned * c->E, c->E};
+    return EdPlanes{h, h + (size_t)ned * c->E, ptr<float>(c->mx_ed_aos), c->E};
 }
 
 // A, b at the iterate q_iter: element data, node blocks and right-hand side, FP32 pair blocks
@@ -1487,13 +1516,14 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
         if (c->prm.tau0 > 0) {  // Bingham viscosity from the iterate's strain rates: FP64 element prep
             k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
                                                                       q_iter, m, k.refSize, visc_args(c),
-                                                                      const_cast<float*>(ed.h), const_cast<float*>(ed.l));
+                                                                      const_cast<float*>(ed.h), const_cast<float*>(ed.l),
+                                                                      const_cast<float*>(ed.a));
         } else {
             k_mx_gprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->pos), q_iter, m,
                                                                        ptr<DF>(c->mx_gdf));
             k_mx_prep_df<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
                 E, N, ptr<int>(c->conn), ptr<DF>(c->mx_gdf), ptr<float>(c->mx_f32), m, k.ref_df, k.inv_pi_df,
-                const_cast<float*>(ed.h), const_cast<float*>(ed.l));
+                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.a));
         }
         prof_end(c, PH_PSPG_ELEM);
         PFG_CHECK_LAUNCH(c);
@@ -1959,6 +1989,7 @@ int mx_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->mx_gdf, sizeof(DF) * 2 * (size_t)c->dim * N)) ||
         (rc = ensure(c, c->mx_tdf, sizeof(DF) * (c->prm.boussinesq ? N : 1))) ||
         (rc = ensure(c, c->mx_rec, 32 * npe * E)) ||
+        (rc = ensure(c, c->mx_ed_aos, sizeof(float) * ED_AOS * E)) ||
         (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) || (rc = ensure(c, c->mx_scale, sizeof(double) * R)) ||
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))

@@ -203,36 +203,3 @@ def test_wc_c2_full_size_matches_oracle(gpu_lib, precision):
         assert max(errs[:d + 2]) < 1e-6, errs
         assert np.abs(ctx.get_positions() - om.positions).max() < 1e-10
     assert ctx.mass() == pytest.approx(O.wc_mass(om, so), rel=1e-9)
-
-
-def test_wc_3d_mixed_velocity_error_is_force_balance_rounding(gpu_lib, small3d_mesh):
-    """Where the 3D mixed form's velocity tolerance comes from.  Twenty steps from the
-    hydrostatic state leave the fluid nearly at rest: the net force on a node is the small
-    difference of its pressure force and its weight, each of size ~rho g |patch|, and the FP32
-    element arithmetic rounds each at ~1e-7 of that size.  So the velocity error is absolute,
-    bounded by ~1e-7 of the free-fall velocity g t, while the velocity itself is far below g t.
-    Against the FP64 form: the absolute error stays below 1e-6 of g t (the relative error of the
-    small velocity field is larger, up to a few 1e-6), and after 100 steps, when the column has
-    started to collapse, the relative velocity error is below 1e-6 as well."""
-    mesh = small3d_mesh
-    d, N = mesh.dim, mesh.n_nodes
-    s0 = M.wc_initial_states(mesh, column=(0.2, 0.3, 0.3))
-    res = {}
-    for prec in (api.PREC_FP64, api.PREC_MIXED):
-        ctx = make_ctx(mesh, prec)
-        ctx.set_states(s0)
-        ctx.set_time(0.0, ctx.next_dt())
-        st20 = ctx.wc_step(0.0, 20)
-        s20 = ctx.get_states()
-        ctx.wc_step(0.0, 80)
-        res[prec] = (s20, st20.time, ctx.get_states())
-        ctx.close()
-    (a20, t20, a100), (b20, _, b100) = res[api.PREC_FP64], res[api.PREC_MIXED]
-    v = slice(0, d * N)
-    gt = 9.81 * t20
-    err_abs = np.linalg.norm(b20[v] - a20[v]) / np.sqrt(d * N)
-    v_rms = np.linalg.norm(a20[v]) / np.sqrt(d * N)
-    assert v_rms < 0.5 * gt                # the column is still nearly at rest
-    assert err_abs < 1e-6 * gt, (err_abs / gt, v_rms / gt)
-    rel100 = np.linalg.norm(b100[v] - a100[v]) / np.linalg.norm(a100[v])
-    assert rel100 < 1e-6, rel100
