@@ -275,7 +275,12 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     if (params->dim != 2 && params->dim != 3) return PFG_ERR_INVALID;
     if (params->kind != PFG_KIND_INCOMP_PSPG && params->kind != PFG_KIND_WC_CDS_DPDT) return PFG_ERR_INVALID;
     if (params->precision != PFG_PREC_FP64 && params->precision != PFG_PREC_MIXED) return PFG_ERR_INVALID;
-    if (params->linear_solver != PFG_LINSOLVE_BICGSTAB) return PFG_ERR_UNSUPPORTED;
+    if (params->linear_solver != PFG_LINSOLVE_BICGSTAB && params->linear_solver != PFG_LINSOLVE_LU)
+        return PFG_ERR_INVALID;
+    // the direct solver is the plain form's (the mixed form refines FP32 Krylov corrections)
+    if (params->linear_solver == PFG_LINSOLVE_LU &&
+        (params->kind != PFG_KIND_INCOMP_PSPG || params->precision != PFG_PREC_FP64))
+        return PFG_ERR_UNSUPPORTED;
     if (params->tau0 < 0 || (params->tau0 > 0 && !(params->m_reg > 0))) return PFG_ERR_INVALID;
     if (params->tau0 > 0 && params->kind != PFG_KIND_INCOMP_PSPG) return PFG_ERR_UNSUPPORTED;  // Bingham: PSPG only
     // Boussinesq coupling and the heat equation: incompressible (PSPG) contexts only
@@ -325,7 +330,9 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
                     &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
                     &c->pe_ptr, &c->pe_item, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
-                    &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos};
+                    &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos, &c->lu_front, &c->lu_nodes,
+                    &c->lu_recs, &c->lu_kids, &c->lu_maps, &c->lu_piv, &c->lu_mat, &c->lu_vec, &c->lu_list,
+                    &c->lu_r, &c->lu_one};
     wc_release_graphs(c);
     mg_release(c);
     mx_release_graph(c);
@@ -358,6 +365,7 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
     }
     c->has_mesh = false;
     c->has_system = false;
+    lu_release(c);
     c->N = n_nodes;
     c->E = n_elems;
     c->R = (dim + 1) * n_nodes;

@@ -59,6 +59,18 @@ struct MgLevel {
     DBuf x, xb, b;         // cycle vectors
 };
 
+// One front of the device sparse LU (pfg_lu.cu).
+struct LuFront {
+    int nv, nb;          // own / boundary nodes
+    int node_off;        // into lu_nodes (V then B)
+    int rec_off, n_rec;  // assembly records
+    int child_off, n_child;
+    int map_off;         // B's local indices in the parent's front
+    int piv_off;         // m pivots
+    long long mat_off;   // dense n x n matrix (row-major)
+    long long vec_off;   // n-vector of the solve
+};
+
 }  // namespace pfg
 
 struct pfg_ctx {
@@ -172,6 +184,16 @@ struct pfg_ctx {
     bool heat_facets_dirty = true;  // the per-node heat facet lists need rebuilding
     std::vector<uint8_t> h_heat_flags;
     std::vector<int32_t> h_facets, h_facet_elm;
+    // device sparse LU of the plain form (PFG_LINSOLVE_LU): fronts, their nodes, assembly
+    // records, children, boundary maps, pivots, dense front matrices and solve vectors, the
+    // fronts of each tree level (deepest first; small ones batched, large ones blocked)
+    pfg::DBuf lu_front, lu_nodes, lu_recs, lu_kids, lu_maps, lu_piv, lu_mat, lu_vec, lu_list, lu_r, lu_one;
+    bool lu_ready = false;
+    int lu_fronts = 0;
+    size_t lu_factor_bytes = 0;
+    std::vector<std::vector<int>> lu_levels, lu_large;
+    std::vector<std::pair<int, int>> lu_small;
+    std::vector<pfg::LuFront> h_lu_front;
 };
 
 namespace pfg {
@@ -245,6 +267,10 @@ int krylov_alloc(pfg_ctx* c);
 // Solve A x = b (x in/out, device).  Returns iterations in *iters and ||b - A x|| in *res.
 int bicgstab(pfg_ctx* c, double* d_x, int* iters, double* res);
 int spmv_residual_norm(pfg_ctx* c, const double* d_x, double* res);
+
+// ---- sparse LU, the plain form's direct solver (pfg_lu.cu) ------------------------------
+int lu_solve(pfg_ctx* c, double* x, int* refine_sweeps);
+void lu_release(pfg_ctx* c);
 
 // ---- mixed-precision PSPG (pfg_pspg_mixed.cu) -----------------------------------------
 int mx_alloc(pfg_ctx* c);

@@ -350,7 +350,13 @@ int picard_step(pfg_ctx* c, double dt, pfg_step_status* st) {
         }
         int kit = 0;
         double kres = 0;
-        if ((rc = bicgstab(c, q, &kit, &kres))) return rc;
+        if (c->prm.linear_solver == PFG_LINSOLVE_LU) {
+            // the reference's choice: a direct factorisation at every Picard iteration
+            // (MomContEquationPSPG.inl:281-291); kit counts its refinement sweeps
+            if ((rc = lu_solve(c, q, &kit))) return rc;
+        } else if ((rc = bicgstab(c, q, &kit, &kres))) {
+            return rc;
+        }
         st->krylov_iterations += kit;
         if ((rc = pspg_update_positions(c, dt, q))) return rc;
         if (c->prm.residual != PFG_RES_AX_F) {
