@@ -204,15 +204,17 @@ __device__ __forceinline__ DF inst_df(const float* f32, int inst, int which) {
 }
 
 // Element data as double-float planes: value v of element e is h[v E + e] + l[v E + e] (the
-// element kernels' coalesced layout), and the same values element-major in `a`: element e's
-// ED_AOS floats hold its high parts (slots 0..15) then its low parts (16..31), so a kernel that
-// gathers an element by index reads two (FP32) or four (double-float) 32-byte sectors instead of
-// one sector per value.
-constexpr int ED_AOS = 32;
+// element kernels' coalesced layout), and the same values element-major: element e's 16 high
+// parts in ah[16 e ..], its low parts in al[16 e ..], so a kernel that gathers an element by
+// index reads two 32-byte sectors of high parts (FP32 arithmetic), plus two of low parts
+// (double-float), instead of one sector per value.  High and low parts are kept apart so that
+// the FP32 gathers' L2 footprint is the high parts alone.
+constexpr int ED_AOS = 16;
 struct EdPlanes {
     const float* h;
     const float* l;
-    const float* a;
+    const float* ah;
+    const float* al;
     int E;
     __device__ __forceinline__ DF df(int v, int e) const {
         const size_t o = (size_t)v * E + e;
@@ -220,31 +222,34 @@ struct EdPlanes {
     }
     __device__ __forceinline__ float f(int v, int e) const { return __ldg(h + (size_t)v * E + e); }
     __device__ __forceinline__ DF gdf(int v, int e) const {
-        const float* r = a + (size_t)e * ED_AOS;
-        return DF{__ldg(r + v), __ldg(r + 16 + v)};
+        return DF{__ldg(ah + (size_t)e * ED_AOS + v), __ldg(al + (size_t)e * ED_AOS + v)};
     }
-    __device__ __forceinline__ float gf(int v, int e) const { return __ldg(a + (size_t)e * ED_AOS + v); }
+    __device__ __forceinline__ float gf(int v, int e) const { return __ldg(ah + (size_t)e * ED_AOS + v); }
 };
 
 // Stores element e's values v (high and low parts) in both layouts.
 template <int NV>
 __device__ __forceinline__ void ed_store(float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea, int E,
                                          int e, const DF (&v)[NV]) {
-    static_assert(NV <= 16, "element record holds 16 values");
-    float r[ED_AOS];
+    static_assert(NV <= ED_AOS, "element record holds 16 values");
+    float rh[ED_AOS], rl[ED_AOS];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        r[k] = k < NV ? v[k < NV ? k : 0].h : 0.0f;
-        r[16 + k] = k < NV ? v[k < NV ? k : 0].l : 0.0f;
+    for (int k = 0; k < ED_AOS; ++k) {
+        rh[k] = k < NV ? v[k < NV ? k : 0].h : 0.0f;
+        rl[k] = k < NV ? v[k < NV ? k : 0].l : 0.0f;
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         eh[(size_t)k * E + e] = v[k].h;
         el[(size_t)k * E + e] = v[k].l;
     }
-    float4* d = reinterpret_cast<float4*>(ea + (size_t)e * ED_AOS);
+    float4* dh = reinterpret_cast<float4*>(ea + (size_t)e * ED_AOS);
+    float4* dl = reinterpret_cast<float4*>(ea + (size_t)E * ED_AOS + (size_t)e * ED_AOS);
 #pragma unroll
-    for (int k = 0; k < ED_AOS / 4; ++k) d[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+    for (int k = 0; k < ED_AOS / 4; ++k) {
+        dh[k] = make_float4(rh[4 * k], rh[4 * k + 1], rh[4 * k + 2], rh[4 * k + 3]);
+        dl[k] = make_float4(rl[4 * k], rl[4 * k + 1], rl[4 * k + 2], rl[4 * k + 3]);
+    }
 }
 
 __device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
@@ -1500,7 +1505,8 @@ double ksum_newtonian(int dim, double mu) {
 EdPlanes ed_planes(pfg_ctx* c) {
     const int ned = c->dim == 2 ? ed_count<2>() : ed_count<3>();
     float* h = ptr<float>(c->edata_df);
-    return EdPlanes{h, h + (size_t)ned * c->E, ptr<float>(c->mx_ed_aos), c->E};
+    float* a = ptr<float>(c->mx_ed_aos);
+    return EdPlanes{h, h + (size_t)ned * c->E, a, a + (size_t)ED_AOS * c->E, c->E};
 }
 
 // A, b at the iterate q_iter: element data, node blocks and right-hand side, FP32 pair blocks
@@ -1517,13 +1523,13 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
             k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
                                                                       q_iter, m, k.refSize, visc_args(c),
                                                                       const_cast<float*>(ed.h), const_cast<float*>(ed.l),
-                                                                      const_cast<float*>(ed.a));
+                                                                      const_cast<float*>(ed.ah));
         } else {
             k_mx_gprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->pos), q_iter, m,
                                                                        ptr<DF>(c->mx_gdf));
             k_mx_prep_df<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
                 E, N, ptr<int>(c->conn), ptr<DF>(c->mx_gdf), ptr<float>(c->mx_f32), m, k.ref_df, k.inv_pi_df,
-                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.a));
+                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah));
         }
         prof_end(c, PH_PSPG_ELEM);
         PFG_CHECK_LAUNCH(c);
@@ -1989,7 +1995,7 @@ int mx_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->mx_gdf, sizeof(DF) * 2 * (size_t)c->dim * N)) ||
         (rc = ensure(c, c->mx_tdf, sizeof(DF) * (c->prm.boussinesq ? N : 1))) ||
         (rc = ensure(c, c->mx_rec, 32 * npe * E)) ||
-        (rc = ensure(c, c->mx_ed_aos, sizeof(float) * ED_AOS * E)) ||
+        (rc = ensure(c, c->mx_ed_aos, sizeof(float) * 2 * ED_AOS * E)) ||
         (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) || (rc = ensure(c, c->mx_scale, sizeof(double) * R)) ||
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))

@@ -225,14 +225,21 @@ __device__ __forceinline__ void adj_df(const float (&Jh)[DIM][DIM], const float 
     }
 }
 
+// det J from the double-float adjugate and Jacobian: (adj J)_00 = sum_f adj[0][f] J[f][0], with
+// adj[0][f] = G[f][1] (adj_df).  The FP32 determinant of the rounded Jacobian loses ~1e-6 of its
+// value to cancellation on 3D elements; this keeps the element size, and so the lumped masses,
+// at FP32 rounding.
 template <int DIM>
-__device__ __forceinline__ float det_f(const float (&J)[DIM][DIM]) {
-    if constexpr (DIM == 2) {
-        return J[0][0] * J[1][1] - J[1][0] * J[0][1];
-    } else {
-        return J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] + J[0][2] * J[1][0] * J[2][1]
-             - J[2][0] * J[1][1] * J[0][2] - J[2][1] * J[1][2] * J[0][0] - J[2][2] * J[1][0] * J[0][1];
+__device__ __forceinline__ float det_adj(const float (&Jh)[DIM][DIM], const float (&Jl)[DIM][DIM],
+                                         const float (&Gh)[DIM][DIM + 1], const float (&Gl)[DIM][DIM + 1]) {
+    float h = 0.0f, l = 0.0f;
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) {
+        float ph, pl;
+        df_mul(Gh[f][1], Gl[f][1], Jh[f][0], Jl[f][0], ph, pl);
+        df_add(h, l, ph, pl);
     }
+    return h + l;
 }
 
 // Half-step velocity and position update of one node (the start of
@@ -309,9 +316,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_cont_elem(int E, int N, const int* 
             Jl[r][c] = __fsub_rn(xl[c + 1][r], xl[0][r]);
             J[r][c] = Jh[r][c] + Jl[r][c];
         }
-    const float ae = det_f<DIM>(J) * k.refSize;
     float Gh[DIM][NPE], Gl[DIM][NPE];
     adj_df<DIM>(Jh, Jl, Gh, Gl);
+    const float ae = det_adj<DIM>(Jh, Jl, Gh, Gl) * k.refSize;
     float ph[NPE], pl[NPE];
     float adiv = 0;
 #pragma unroll
@@ -400,11 +407,11 @@ __global__ void __launch_bounds__(BLOCK) k_m_mom_elem(int E, int N, const int* _
     for (int r = 0; r < DIM; ++r)
 #pragma unroll
         for (int c = 0; c < DIM; ++c) J[r][c] = Jh[r][c] + Jl[r][c];
-    const float det = det_f<DIM>(J);
-    const float ae = det * k.refSize;
-    const float he = cfl_length<DIM>(J, ae);
     float Gh[DIM][NPE], Gl[DIM][NPE], A[DIM][NPE];
     adj_df<DIM>(Jh, Jl, Gh, Gl);
+    const float det = det_adj<DIM>(Jh, Jl, Gh, Gl);
+    const float ae = det * k.refSize;
+    const float he = cfl_length<DIM>(J, ae);
 #pragma unroll
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
@@ -628,7 +635,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_dt(int E, int N, const int* __restr
             for (int r = 0; r < DIM; ++r)
 #pragma unroll
                 for (int c = 0; c < DIM; ++c) J[r][c] = Jh[r][c] + Jl[r][c];
-            const float he = cfl_length<DIM>(J, det_f<DIM>(J) * k.refSize);
+            float Gh[DIM][DIM + 1], Gl[DIM][DIM + 1];
+            adj_df<DIM>(Jh, Jl, Gh, Gl);
+            const float he = cfl_length<DIM>(J, det_adj<DIM>(Jh, Jl, Gh, Gl) * k.refSize);
             float m1 = 0, m2 = 0;
 #pragma unroll
             for (int a = 0; a <= DIM; ++a) {
@@ -649,7 +658,9 @@ __global__ void __launch_bounds__(BLOCK) k_m_dt(int E, int N, const int* __restr
         for (int r = 0; r < DIM; ++r)
 #pragma unroll
             for (int c = 0; c < DIM; ++c) J[r][c] = Jh[r][c] + Jl[r][c];
-        const float he = cfl_length<DIM>(J, det_f<DIM>(J) * k.refSize);
+        float Gh[DIM][DIM + 1], Gl[DIM][DIM + 1];
+        adj_df<DIM>(Jh, Jl, Gh, Gl);
+        const float he = cfl_length<DIM>(J, det_adj<DIM>(Jh, Jl, Gh, Gl) * k.refSize);
         float m1 = 0, m2 = 0;
 #pragma unroll
         for (int a = 0; a <= DIM; ++a) {

@@ -154,9 +154,10 @@ def test_wc_full_size_properties(gpu_lib):
 @pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_MIXED])
 def test_wc_3d_matches_oracle(gpu_lib, small3d_mesh, precision):
     """3D (tetrahedra): 20 adaptive steps of both forms against the FP64 oracle.  FP64 as in 2D;
-    mixed: pressure and density 1e-6, velocity 5e-6 relative (20 steps from rest the velocity
-    is still small next to the pressure and gravity forces it is the difference of, so the FP32
-    element arithmetic shows more in 3D: 1.9e-6 measured)."""
+    mixed: velocity, pressure and density within 1e-6 relative.  (With the element size taken
+    from an FP32 determinant of the Jacobian, which cancels in 3D, the mixed velocity was 1.8e-6
+    off, uniformly over free-surface and interior nodes from the first steps on: the lumped mass
+    carried the determinant's rounding.  The size now comes from the double-float adjugate.)"""
     mesh = small3d_mesh
     d, N = mesh.dim, mesh.n_nodes
     column = (0.2, 0.3, 0.3)
@@ -178,8 +179,7 @@ def test_wc_3d_matches_oracle(gpu_lib, small3d_mesh, precision):
         assert max(errs) < 1e-10, errs
         assert np.abs(ctx.get_positions() - om.positions).max() < 1e-13
     else:
-        assert max(errs[:d]) < 5e-6, errs
-        assert max(errs[d:d + 2]) < 1e-6, errs
+        assert max(errs[:d + 2]) < 1e-6, errs
         assert np.abs(ctx.get_positions() - om.positions).max() < 1e-10
     assert ctx.mass() == pytest.approx(O.wc_mass(om, so), rel=1e-9)
 
