@@ -891,6 +891,33 @@ def run_gpu_incomp(args):
         ctx.get_states(out=h_out)
     e2e_s = time.perf_counter() - t0
 
+    # the plain form with the device sparse LU (the reference's solver choice), same timed steps
+    plain_lu = None
+    if args.workload == "incomp-c1":
+        p_lu = incomp_params(api, d, api.PREC_FP64, args.workload)
+        p_lu.linear_solver = api.LINSOLVE_LU
+        c_lu = api.Context(p_lu)
+        c_lu.upload_mesh(mesh)
+        c_lu.set_states(q0)
+        for _ in range(Wm):
+            c_lu.picard_step(dt)
+        x_l, q_l = c_lu.get_positions(), c_lu.get_states()
+        lu_ms = 0.0
+        ext_l = torch.cuda.ExternalStream(c_lu.stream)
+        for _ in range(K):
+            c_lu.set_positions(x_l)
+            c_lu.set_states(q_l)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(ext_l):
+                e0.record(ext_l)
+                c_lu.picard_step(dt)
+                e1.record(ext_l)
+            torch.cuda.synchronize()
+            lu_ms += e0.elapsed_time(e1)
+        plain_lu = {"solver": "device sparse LU (nested dissection, multifrontal, FP64)", "value": K / (lu_ms / 1e3),
+                    "mixed_speedup": (K / (total_ms / 1e3)) / (K / (lu_ms / 1e3))}
+        c_lu.close()
+
     cpu = None
     acc_vs_oracle = None
     if rank == 0 and not args.no_cpu_baseline and args.workload == "incomp-c3":
@@ -938,7 +965,9 @@ def run_gpu_incomp(args):
             "dof_per_s": value * R,
             "step_stats": stats,
             "other_precision": {"precision": "fp64" if prec == api.PREC_MIXED else "mixed",
+                                "solver": "block-Jacobi BiCGSTAB" if prec == api.PREC_MIXED else "multigrid BiCGSTAB",
                                 "value": K / (ms_o / 1e3), "step_stats": stats_o},
+            "plain_lu": plain_lu,
             "e2e": {"value": Ke / e2e_s, "unit": cfg["unit"], "h2d_bytes_per_step": int(h_in.nbytes + h_x.nbytes),
                     "d2h_bytes_per_step": int(h_out.nbytes)},
             "roofline": roof,
@@ -1226,6 +1255,31 @@ def run_gpu_batch(args):
     sample_dof = sum(3 * meshes[i].n_nodes for i in sample)
     plain_dof_per_s = plain_dof_steps / (plain_ms / 1e3)
 
+    # the plain form with the device sparse LU on four instances of the sample (one timed step
+    # each, after the warm-up steps)
+    lu_ms, lu_dof = 0.0, 0
+    for i in sample[::max(1, len(sample) // 4)][:4]:
+        m = meshes[i]
+        p_lu = incomp_params(api, 2, api.PREC_FP64, "batch-c4", mu=float(mus[i]))
+        p_lu.linear_solver = api.LINSOLVE_LU
+        c = api.Context(p_lu)
+        c.upload_mesh(m)
+        c.set_states(insts[i].q0)
+        for _ in range(Wm):
+            c.picard_step(dt)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cext = torch.cuda.ExternalStream(c.stream)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(cext):
+            e0.record(cext)
+            c.picard_step(dt)
+            e1.record(cext)
+        torch.cuda.synchronize()
+        lu_ms += e0.elapsed_time(e1)
+        lu_dof += 3 * m.n_nodes
+        c.close()
+    lu_dof_per_s = lu_dof / (lu_ms / 1e3) if lu_ms else None
+
     # phase times of one batched step
     ctx.set_profiling(True)
     ctx.reset_phase_times()
@@ -1259,6 +1313,8 @@ def run_gpu_batch(args):
             "plain_fp64_sample": {"instances": len(sample), "dof": sample_dof, "dof_per_s": plain_dof_per_s,
                                   "speedup_dof_per_s": dof_per_s / world / plain_dof_per_s,
                                   "max_rel_err_vs_plain": max(errs) if errs else None},
+            "plain_lu_sample": {"instances": 4, "dof_per_s": lu_dof_per_s,
+                                "speedup_dof_per_s": dof_per_s / world / lu_dof_per_s if lu_dof_per_s else None},
             "roofline": roof, "phases_ms_per_step": {k: v[0] for k, v in phases.items()},
             "cpu_baseline": None, "clocks": clk,
             "e2e": {"value": n * Ke / e2e_s, "unit": cfg["unit"], "h2d_bytes_per_step": (R + 2 * Ntot) * 8,
