@@ -161,6 +161,18 @@ typedef struct pfg_params {
     double heat_tm;            /* melting temperature Tm                                   */
     double heat_dt_melt;       /* melting range DT                                         */
     double heat_lm;            /* latent heat Lm                                           */
+    /* weakly compressible problem "BoussinesqWC" (kind PFG_KIND_WC_CDS_DPDT with boussinesq =
+       1, plain FP64 precision; WCompNewton/Solver.cpp:72-146, 278-320): every step runs the
+       explicit lumped-mass heat step of HeatEqWCompNewton (heat_k, heat_cv with the node
+       densities, the heat boundary conditions and facets of pfg_heat_set_bc / _set_flux; with
+       heat_phase_change the latent heat heat_lm) between the half-step prediction and the
+       continuity equation; the momentum body force uses rho (1 - alpha_t (T - t_ref)), the
+       surface tension gamma + dgamma_dt (T - t_ref), and with heat_phase_change the
+       Carman-Kozeny damping C (1 - fl)^2 / (fl^3 + eps) of MomEquation.inl:122-130 (fl the
+       liquid fraction over heat_tm, heat_dt_melt); the CFL diffusion parameter is
+       max(mu / rho, k / (cv rho)).  The temperatures are pfg_set_temperature's.              */
+    double ck_c;               /* Carman-Kozeny constant C                                 */
+    double ck_eps;             /* Carman-Kozeny eps                                        */
 } pfg_params;
 
 /* Heat boundary-condition flags per node (the reference's tag flags of HeatEq's BC table,

@@ -66,6 +66,15 @@ class WcParams(C.Structure):
                 ("gamma", C.c_double)]
 
 
+class WcBqParams(C.Structure):
+    """Problem "BoussinesqWC": momentum and heat material of WCompNewton (MomEquation.inl:36-51,
+    HeatEquation.inl:26-45)."""
+    _fields_ = [("alpha", C.c_double), ("Tr", C.c_double), ("dgammaDT", C.c_double), ("phaseChange", C.c_int32),
+                ("fsFlags", C.c_int32), ("C", C.c_double), ("eps", C.c_double), ("Tm", C.c_double), ("DT", C.c_double),
+                ("Lm", C.c_double), ("k", C.c_double), ("cv", C.c_double), ("h", C.c_double), ("Tinf", C.c_double),
+                ("epsRad", C.c_double)]
+
+
 _lib = None
 
 
@@ -100,6 +109,9 @@ def lib():
         L.orc_wc_step.argtypes = [vp, C.POINTER(WcParams), C.c_double, dp, dp]
         L.orc_wc_next_dt.restype = C.c_double
         L.orc_wc_next_dt.argtypes = [vp, C.POINTER(WcParams), dp]
+        L.orc_wc_bq_step.argtypes = [vp, C.POINTER(WcParams), C.POINTER(WcBqParams), C.c_double, dp, dp, u8p, dp, dp]
+        L.orc_wc_bq_next_dt.restype = C.c_double
+        L.orc_wc_bq_next_dt.argtypes = [vp, C.POINTER(WcParams), C.POINTER(WcBqParams), dp]
         L.orc_volume.restype = C.c_double
         L.orc_volume.argtypes = [vp]
         L.orc_wc_mass.restype = C.c_double
@@ -426,6 +438,38 @@ def wc_step(om, params, dt, states, vbc=None):
 
 def wc_next_dt(om, params, states):
     return lib().orc_wc_next_dt(om.h, C.byref(params), _dp(np.ascontiguousarray(states, float)))
+
+
+def wc_bq_params(alpha, t_ref, k, cv, dgamma_dt=0.0, h=0.0, t_inf=0.0, eps_rad=0.0, fs_flags=0, phase_change=None):
+    """phase_change: None or dict(C=, eps=, Tm=, DT=, Lm=)."""
+    b = WcBqParams()
+    b.alpha, b.Tr, b.dgammaDT = alpha, t_ref, dgamma_dt
+    b.k, b.cv, b.h, b.Tinf, b.epsRad = k, cv, h, t_inf, eps_rad
+    b.fsFlags = fs_flags
+    if phase_change:
+        b.phaseChange = 1
+        b.C, b.eps, b.Tm, b.DT, b.Lm = (phase_change[k] for k in ("C", "eps", "Tm", "DT", "Lm"))
+    return b
+
+
+def wc_bq_step(om, params, bq, dt, states, flags, vbc=None, t_bc=None, q_gp=None):
+    """In-place BoussinesqWC step on `states` (float64, (2d+3)*N: v, p, rho, a, T); flags: heat
+    flags per node (HT_*), t_bc the T-Dirichlet values at t + dt, q_gp the Q flux at the facet
+    Gauss points ((F, 3, d))."""
+    N = om.N
+    if vbc is None:
+        vbc = np.zeros(om.dim * N)
+    if t_bc is None:
+        t_bc = np.zeros(N)
+    assert states.dtype == np.float64 and states.flags.c_contiguous and states.size == (2 * om.dim + 3) * N
+    q = _dp(np.ascontiguousarray(q_gp, float)) if q_gp is not None else None
+    lib().orc_wc_bq_step(om.h, C.byref(params), C.byref(bq), float(dt), _dp(states),
+                         _dp(np.ascontiguousarray(vbc, float)), np.ascontiguousarray(flags, np.uint8).ctypes.data_as(
+                             C.POINTER(C.c_uint8)), _dp(np.ascontiguousarray(t_bc, float)), q)
+
+
+def wc_bq_next_dt(om, params, bq, states):
+    return lib().orc_wc_bq_next_dt(om.h, C.byref(params), C.byref(bq), _dp(np.ascontiguousarray(states, float)))
 
 
 def wc_mass(om, states):

@@ -152,6 +152,26 @@ struct WcParams {
     double gamma;      // surface tension coefficient (MomEq "gamma")
 };
 
+// Problem "BoussinesqWC" (WCompNewton/Solver.cpp:72-146): MomEq material (MomEquation.inl:36-51)
+// and HeatEqWCompNewton material (HeatEquation.inl:26-45).  Carman-Kozeny damping in the
+// momentum equation and latent heat in the heat mass factor when phaseChange is set.
+struct WcBqParams {
+    double alpha, Tr, dgammaDT;
+    int32_t phaseChange;   // MomEq: C, eps, Tm, DT given; HeatEq: Tm, DT, Lm given
+    int32_t fsFlags;       // heat flags of the free-surface tag (-2)
+    double C, eps, Tm, DT, Lm;
+    double k, cv, h, Tinf, epsRad;
+};
+
+// Liquid fraction of MomEqWCompNewton::m_getFl (MomEquation.inl:377-381).
+double flWC(double Tm, double DT, double T) {
+    const double d3 = DT * DT * DT;
+    return static_cast<double>(T > Tm - DT / 2) * static_cast<double>(T < Tm + DT / 2) *
+               (-2 / d3 * T * T * T + 6 * Tm / d3 * T * T + (3 / (2 * DT) - 6 * Tm * Tm / d3) * T +
+                (0.5 - 1.5 * Tm / DT + 2 * Tm * Tm * Tm / d3)) +
+           static_cast<double>(T > Tm + DT / 2);
+}
+
 }  // namespace
 
 struct OrcMesh {
@@ -1093,12 +1113,127 @@ void orc_pspg_get(const OrcMesh* m, int32_t* colptr, int32_t* rowidx, double* va
 // srcs/simulation/physics/WCompNewton/Solver.cpp:236-276 without the remesh at :266-272.
 // s = [v (d), p, rho, a (d)] field-major.  vbc: Dirichlet velocities (d x N).
 // ---------------------------------------------------------------------------------------
-void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const double* vbc) {
+}  // extern "C"
+
+namespace {
+
+// HeatEqWCompNewton::solve (HeatEquation.inl:137-158): explicit, lumped mass.  m_buildSystem
+// (:263-317): Me = getM with the factor cv rho_g ((cv + dfl/dT(T_g) Lm) rho_g with phase
+// change, :51-66), lumped; Le = getL with the factor k; FTot = -dt Le T + Me T, summed over the
+// elements in element order.  m_applyBC (:160-261): the flux facets (Q, Qh, Qr; all facet nodes
+// flagged, free-surface facets use fsFlags), then free nodes without a T condition keep T and
+// T-Dirichlet nodes take Tbc.  T <- invM F.
+void wcHeatExplicit(OrcMesh* m, const WcBqParams* b, double dt, const double* rho, double* T, const uint8_t* hf,
+                    const double* Tbc, const double* qgp) {
+    const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    HeatParams hp{};
+    hp.cv = b->cv;
+    hp.Tm = b->Tm;
+    hp.DT = b->DT;
+    std::vector<double> MeL((size_t)E * npe), FTe((size_t)E * npe);
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        const ElemGeom& geo = m->geom[e];
+        double te[4], re[4];
+        for (int k = 0; k < npe; ++k) {
+            te[k] = T[m->node(e, k)];
+            re[k] = rho[m->node(e, k)];
+        }
+        Mat Me = getM(*m, geo, [&](int g) {
+            const double r = nDot(m->gt, g, re, npe);
+            if (!b->phaseChange) return b->cv * r;
+            return (b->cv + dFlDT(hp, nDot(m->gt, g, te, npe)) * b->Lm) * r;
+        });
+        Mat G = getGradN(dim, geo);
+        double ksum = 0;
+        for (int g = 0; g < m->gt.n; ++g) ksum += b->k * m->gt.w[g];
+        Mat Le = getL(*m, geo, ksum, G);
+        for (int i = 0; i < npe; ++i) {
+            double lumped = 0, lt = 0;
+            for (int j = 0; j < npe; ++j) {
+                lumped += Me(i, j);
+                lt += Le(i, j) * te[j];
+            }
+            MeL[(size_t)e * npe + i] = lumped;
+            FTe[(size_t)e * npe + i] = -dt * lt + lumped * te[i];
+        }
+    }
+    std::vector<double> invM(N, 0.0), F(N, 0.0);
+    for (int e = 0; e < E; ++e)
+        for (int i = 0; i < npe; ++i) {
+            invM[m->node(e, i)] += MeL[(size_t)e * npe + i];
+            F[m->node(e, i)] += FTe[(size_t)e * npe + i];
+        }
+    for (int n = 0; n < N; ++n) invM[n] = 1 / invM[n];
+    const FacetGauss fg = facetGauss(dim);
+    constexpr double sigma = 5.670374419e-8;
+    for (int f = 0; f < m->F; ++f) {
+        int nd[3];
+        bool fs = true;
+        for (int k = 0; k < dim; ++k) {
+            nd[k] = m->facets[(size_t)k * m->F + f];
+            fs = fs && (m->flags[nd[k]] & FREE_SURFACE);
+        }
+        bool bq = true, bqh = true, bqr = true;
+        for (int k = 0; k < dim; ++k) {
+            const int fl = fs ? b->fsFlags : hf[nd[k]];
+            bq = bq && (fl & HT_Q);
+            bqh = bqh && (fl & HT_QH);
+            bqr = bqr && (fl & HT_QR);
+        }
+        if (!bq && !bqh && !bqr) continue;
+        double detJ, nrm[3];
+        facetGeometry(*m, f, detJ, nrm);
+        double tf[3];
+        for (int k = 0; k < dim; ++k) tf[k] = T[nd[k]];
+        if (bq) {  // getQN, MatricesBuilder.inl:246-272
+            orientedNormal(*m, f, nrm);
+            double qn[3] = {0, 0, 0};
+            for (int g = 0; g < 3; ++g) {
+                double qdn = 0;
+                for (int d = 0; d < dim; ++d) qdn += qgp[((size_t)f * 3 + g) * dim + d] * nrm[d];
+                const double fact = qdn * fg.w[g];
+                for (int k = 0; k < dim; ++k) qn[k] += fact * fg.sf[g][k];
+            }
+            for (int k = 0; k < dim; ++k) F[nd[k]] -= dt * (qn[k] * fg.ref * detJ);
+        }
+        for (int pass = 0; pass < 2; ++pass) {  // getSGamma (h, then radiation)
+            if (!(pass == 0 ? bqh : bqr)) continue;
+            double sg[3] = {0, 0, 0};
+            for (int g = 0; g < 3; ++g) {
+                double Tg = 0;
+                for (int k = 0; k < dim; ++k) Tg += fg.sf[g][k] * tf[k];
+                const double fac = pass == 0 ? b->h * (Tg - b->Tinf)
+                                             : sigma * b->epsRad * (Tg * Tg * Tg * Tg - b->Tinf * b->Tinf * b->Tinf * b->Tinf);
+                for (int k = 0; k < dim; ++k) sg[k] += fac * fg.sf[g][k] * fg.w[g];
+            }
+            for (int k = 0; k < dim; ++k) F[nd[k]] -= dt * (sg[k] * (detJ * fg.ref));
+        }
+    }
+    for (int n = 0; n < N; ++n) {
+        if (m->isFree[n] && !(hf[n] & HT_T)) {
+            F[n] = T[n];
+            invM[n] = 1;
+        } else if (hf[n] & HT_T) {
+            F[n] = Tbc[n];
+            invM[n] = 1;
+        }
+    }
+    for (int n = 0; n < N; ++n) T[n] = invM[n] * F[n];
+}
+
+// One explicit step of m_solveWCompNewtonNoT (Solver.cpp:236-276) or, with bq, of
+// m_solveBoussinesqWC (:278-320: the heat equation between the half-step prediction and the
+// continuity equation; the momentum body force rho_g (1 - alpha (T_g - Tr)), the Carman-Kozeny
+// term and the temperature-dependent surface tension, MomEquation.inl:105-132).
+void wcStep(OrcMesh* m, const WcParams* p, const WcBqParams* bq, double dt, double* s, const double* vbc,
+            const uint8_t* hf, const double* Tbc, const double* qgp) {
     const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
     double* v = s;
     double* P = s + (size_t)dim * N;
     double* rho = s + (size_t)(dim + 1) * N;
     double* a = s + (size_t)(dim + 2) * N;
+    double* Tn = bq ? s + (size_t)(2 * dim + 2) * N : nullptr;
 
     // v1/2 = v + dt/2 a ; x += dt v1/2 (:249-253, Mesh.cpp:1101-1137)
     std::vector<double> delta((size_t)dim * N);
@@ -1109,6 +1244,7 @@ void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const doub
             delta[(size_t)d * N + n] = v[(size_t)d * N + n] * dt;
         }
     orc_update_positions(m, delta.data());
+    if (bq) wcHeatExplicit(m, bq, dt, rho, Tn, hf, Tbc, qgp);
 
     // ContEqWCompNewton::m_buildSystemdpdt, ContEquation.inl:353-413
     std::vector<double> MeL((size_t)E * npe), F0e((size_t)E * npe);
@@ -1180,8 +1316,20 @@ void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const doub
         for (int g = 0; g < m->gt.n; ++g) sumMu += p->mu * m->gt.w[g];
         Mat K = getK(*m, geo, sumMu, B, ddev);
         Mat D = getD(*m, geo, [](int) { return 1.0; }, B);
-        double Fe[12];
-        getF(*m, geo, [&](int g) { return nDot(m->gt, g, Re, npe); }, p->g, Fe);
+        double Fe[12], Te[4];
+        if (bq)
+            for (int k = 0; k < npe; ++k) Te[k] = Tn[m->node(e, k)];
+        getF(*m, geo, [&](int g) {
+            const double r = nDot(m->gt, g, Re, npe);
+            return bq ? r * (1 - bq->alpha * (nDot(m->gt, g, Te, npe) - bq->Tr)) : r;
+        }, p->g, Fe);
+        Mat M2(npe, npe);
+        const bool ck = bq && bq->phaseChange;
+        if (ck)
+            M2 = getM(*m, geo, [&](int g) {
+                const double fl = flWC(bq->Tm, bq->DT, nDot(m->gt, g, Te, npe));
+                return bq->C * (1 - fl) * (1 - fl) / (fl * fl * fl + bq->eps);
+            });
         for (int r = 0; r < dim * npe; ++r) {
             int i = r % npe;
             double lumped = 0;  // diagBlock + lump: row sum of the scalar block
@@ -1191,7 +1339,14 @@ void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const doub
             for (int c = 0; c < dim * npe; ++c) kv += K(r, c) * Ve[c];
             double dp = 0;
             for (int j = 0; j < npe; ++j) dp += D(j, r) * Pe[j];
-            FT[(size_t)e * dim * npe + r] = -kv + dp + Fe[r];
+            double ft = -kv + dp + Fe[r];
+            if (ck) {  // - diagBlock(M2) V (MomEquation.inl:271-276)
+                const int d = r / npe;
+                double m2v = 0;
+                for (int j = 0; j < npe; ++j) m2v += M2(i, j) * Ve[d * npe + j];
+                ft -= m2v;
+            }
+            FT[(size_t)e * dim * npe + r] = ft;
         }
     }
     std::vector<double> invMv((size_t)dim * N, 0.0), F((size_t)dim * N, 0.0);
@@ -1204,7 +1359,10 @@ void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const doub
             }
     for (size_t k = 0; k < invMv.size(); ++k) invMv[k] = 1 / invMv[k];
     // m_applyBC (:305-374): facet loop (:311-335), then the node loop
-    addSurfaceTension(*m, p->gamma, false, F.data());
+    if (bq)
+        addSurfaceTension(*m, p->gamma, false, F.data(), Tn, bq->dgammaDT, bq->Tr);
+    else
+        addSurfaceTension(*m, p->gamma, false, F.data());
     for (int n = 0; n < N; ++n) {
         if (m->isFree[n] && !m->bound(n)) {
             for (int d = 0; d < dim; ++d) {
@@ -1229,8 +1387,32 @@ void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const doub
         }
 }
 
+}  // namespace
+
+extern "C" {
+
+void orc_wc_step(OrcMesh* m, const WcParams* p, double dt, double* s, const double* vbc) {
+    wcStep(m, p, nullptr, dt, s, vbc, nullptr, nullptr, nullptr);
+}
+
+// BoussinesqWC step: s = [v (d), p, rho, a (d), T] field-major; hf heat flags per node, Tbc
+// the T-Dirichlet values at t + dt, qgp the Q flux at the facet Gauss points (or null).
+void orc_wc_bq_step(OrcMesh* m, const WcParams* p, const WcBqParams* bq, double dt, double* s, const double* vbc,
+                    const uint8_t* hf, const double* Tbc, const double* qgp) {
+    wcStep(m, p, bq, dt, s, vbc, hf, Tbc, qgp);
+}
+
+double wc_next_dt_impl(const OrcMesh* m, const WcParams* p, const WcBqParams* bq, const double* s);
+
 // SolverWCompNewton::computeNextDT, WCompNewton/Solver.cpp:192-234 (adaptDT = true).
-double orc_wc_next_dt(const OrcMesh* m, const WcParams* p, const double* s) {
+double orc_wc_next_dt(const OrcMesh* m, const WcParams* p, const double* s) { return wc_next_dt_impl(m, p, nullptr, s); }
+
+// BoussinesqWC: the diffusion parameter is max(mu / rho, k / (cv rho)) (:215-219).
+double orc_wc_bq_next_dt(const OrcMesh* m, const WcParams* p, const WcBqParams* bq, const double* s) {
+    return wc_next_dt_impl(m, p, bq, s);
+}
+
+double wc_next_dt_impl(const OrcMesh* m, const WcParams* p, const WcBqParams* bq, const double* s) {
     const int dim = m->dim, N = m->N, E = m->E, npe = m->npe;
     const double* v = s;
     const double* P = s + (size_t)dim * N;
@@ -1273,6 +1455,7 @@ double orc_wc_next_dt(const OrcMesh* m, const WcParams* p, const double* s) {
             double u2 = 0;
             for (int d = 0; d < dim; ++d) u2 += v[(size_t)d * N + n] * v[(size_t)d * N + n];
             double alpha = p->mu / rho[n];
+            if (bq) alpha = std::max(alpha, bq->k / (bq->cv * rho[n]));  // HeatEq::getDiffusionParam
             maxSq = std::max(std::max(u2, c2), maxSq);
             maxSq = std::max(maxSq, 4 * alpha * alpha / (he * he));
         }

@@ -65,7 +65,7 @@ class Params(C.Structure):
         ("alpha_t", C.c_double), ("t_ref", C.c_double), ("dgamma_dt", C.c_double),
         ("heat_max_iter", C.c_int32), ("heat_residual", C.c_int32), ("heat_min_res", C.c_double),
         ("heat_phase_change", C.c_int32), ("pad3", C.c_int32), ("heat_tm", C.c_double), ("heat_dt_melt", C.c_double),
-        ("heat_lm", C.c_double),
+        ("heat_lm", C.c_double), ("ck_c", C.c_double), ("ck_eps", C.c_double),
     ]
 
 

@@ -283,9 +283,12 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
         return PFG_ERR_UNSUPPORTED;
     if (params->tau0 < 0 || (params->tau0 > 0 && !(params->m_reg > 0))) return PFG_ERR_INVALID;
     if (params->tau0 > 0 && params->kind != PFG_KIND_INCOMP_PSPG) return PFG_ERR_UNSUPPORTED;  // Bingham: PSPG only
-    // Boussinesq coupling and the heat equation: incompressible (PSPG) contexts only
-    if (params->boussinesq && params->kind != PFG_KIND_INCOMP_PSPG) return PFG_ERR_UNSUPPORTED;
+    // Boussinesq coupling: problem "Boussinesq" (PSPG) or "BoussinesqWC" (WC, plain FP64 form)
     if (params->boussinesq != 0 && params->boussinesq != 1) return PFG_ERR_INVALID;
+    if (params->boussinesq && params->kind == PFG_KIND_WC_CDS_DPDT) {
+        if (params->precision != PFG_PREC_FP64) return PFG_ERR_UNSUPPORTED;
+        if (!(params->heat_cv > 0) || !(params->heat_k >= 0)) return PFG_ERR_INVALID;
+    }
     if (params->heat_fs_flags & ~(PFG_HEAT_Q | PFG_HEAT_QH | PFG_HEAT_QR)) return PFG_ERR_INVALID;
     if (params->heat_residual != PFG_RES_T && params->heat_residual != PFG_RES_AX_F) return PFG_ERR_INVALID;
     if (params->heat_phase_change && !(params->heat_dt_melt > 0)) return PFG_ERR_INVALID;
@@ -329,8 +332,8 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force,
                     &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
                     &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
-                    &c->pe_ptr, &c->pe_item, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
-                    &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos, &c->lu_front, &c->lu_nodes,
+                    &c->pe_ptr, &c->pe_item, &c->el_slot, &c->ne_slot, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
+                    &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos, &c->mx_vsum, &c->wch_rec, &c->lu_front, &c->lu_nodes,
                     &c->lu_recs, &c->lu_kids, &c->lu_maps, &c->lu_piv, &c->lu_mat, &c->lu_vec, &c->lu_list,
                     &c->lu_r, &c->lu_one};
     wc_release_graphs(c);
@@ -397,6 +400,8 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
         if (c->prm.precision == PFG_PREC_MIXED && (rc = mx_alloc(c))) return rc;
     } else {
         if ((rc = wc_alloc(c))) return rc;
+        c->heat_ready = false;  // BoussinesqWC: the temperatures restart at zero with the mesh
+        if (c->prm.boussinesq && (rc = heat_alloc(c))) return rc;
     }
     PFG_CUDA(c, cudaStreamSynchronize(c->stream));
     c->has_mesh = true;
@@ -543,8 +548,8 @@ namespace {
 int check_heat(pfg_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
-    if (c->prm.kind != PFG_KIND_INCOMP_PSPG)
-        return fail(c, PFG_ERR_UNSUPPORTED, "the heat equation needs an incompressible (PSPG) context");
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG && !c->prm.boussinesq)
+        return fail(c, PFG_ERR_UNSUPPORTED, "the heat equation needs an incompressible or a BoussinesqWC context");
     if (!c->has_mesh) return fail(c, PFG_ERR_STATE, "no mesh uploaded");
     return c->heat_ready ? PFG_OK : heat_alloc(c);
 }
@@ -615,6 +620,8 @@ PFG_API int pfg_heat_set_flux(pfg_ctx* c, const double* q_gp) {
 PFG_API int pfg_heat_step(pfg_ctx* c, double dt, pfg_step_status* st) {
     int rc = check_heat(c);
     if (rc) return rc;
+    if (c->prm.kind != PFG_KIND_INCOMP_PSPG)
+        return fail(c, PFG_ERR_UNSUPPORTED, "BoussinesqWC runs its heat step inside pfg_wc_step");
     if (!st) return fail(c, PFG_ERR_INVALID, "null status");
     if (!(dt > 0)) return fail(c, PFG_ERR_INVALID, "dt must be > 0");
     if (!(c->prm.heat_cv * c->prm.rho > 0) || !(c->prm.heat_k >= 0))

@@ -286,6 +286,64 @@ struct HeatFacets {
     int F;
 };
 
+// Subtracts node n's facet terms from its heat right-hand side b, one after the other: dt
+// times the prescribed flux QN, the convection and the radiation SGamma of its listed facets in
+// facet order (HeatEquation.inl:315-375 of either solver), at the facet-node temperatures ts.
+template <int DIM>
+__device__ __forceinline__ void heat_facet_terms(int n, int N, int E, const int* __restrict__ conn,
+                                                 const double* __restrict__ pos, const double* __restrict__ ts,
+                                                 const HeatFacets& hf, const HeatConst& k, double dt, double& b) {
+    constexpr int NPE = DIM + 1;
+    constexpr double sigma = 5.670374419e-8;  // Stefan-Boltzmann constant (:90)
+    for (int q = hf.ptr[n]; q < hf.ptr[n + 1]; ++q) {
+        const int ent = hf.ent[q];
+        const int f = ent >> 2, kk = ent & 3;
+        const uint8_t ff = hf.fflags[f];
+        int fn[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) fn[d] = hf.fnodes[(size_t)d * hf.F + f];
+        const double detJ = facet_detj<DIM>(pos, N, fn);
+        if (ff & HT_Q) {  // getQN, MatricesBuilder.inl:246-272
+            const int e = hf.felem[f];
+            int out = -1;
+#pragma unroll
+            for (int a = 0; a < NPE; ++a) {
+                const int v = conn[(size_t)a * E + e];
+                bool on = false;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) on |= v == fn[d];
+                if (!on) out = v;
+            }
+            double nv[DIM];
+            facet_normal<DIM>(pos, N, fn, out, nv);
+            double qn = 0;
+#pragma unroll
+            for (int g = 0; g < 3; ++g) {
+                double qdn = 0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) qdn += hf.q[((size_t)f * 3 + g) * DIM + d] * nv[d];
+                qn += (qdn * k.fw[g]) * k.fsf[g][kk];
+            }
+            b -= dt * ((qn * k.fref) * detJ);
+        }
+#pragma unroll
+        for (int pass = 0; pass < 2; ++pass) {  // getSGamma, MatricesBuilder.inl:357-370 (:76-94)
+            if (!(ff & (pass == 0 ? HT_QH : HT_QR))) continue;
+            double sg = 0;
+#pragma unroll
+            for (int g = 0; g < 3; ++g) {
+                double T = 0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) T += k.fsf[g][d] * ts[fn[d]];
+                const double fac = pass == 0 ? k.h * (T - k.tinf)
+                                             : sigma * k.eps_rad * (T * T * T * T - k.tinf * k.tinf * k.tinf * k.tinf);
+                sg += (fac * k.fsf[g][kk]) * k.fw[g];
+            }
+            b -= dt * (sg * (detJ * k.fref));
+        }
+    }
+}
+
 // Right-hand side of node n: element gather of cv rho M T_prev (:240-283), the facet terms in
 // facet order (:315-375), the node conditions (:377-393) and the Dirichlet column elimination
 // of row n in ascending column order (the reference's node loop order), which zeroes the
@@ -321,54 +379,7 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
         for (int j = 0; j < NPE; ++j) s += (heat_m<DIM>(k, i, j, te) * ae) * t_prev[nd[j]];
         b += s;
     }
-    constexpr double sigma = 5.670374419e-8;  // Stefan-Boltzmann constant (:90)
-    for (int q = hf.ptr[n]; q < hf.ptr[n + 1]; ++q) {
-        const int ent = hf.ent[q];
-        const int f = ent >> 2, kk = ent & 3;
-        const uint8_t ff = hf.fflags[f];
-        int fn[DIM];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) fn[d] = hf.fnodes[(size_t)d * hf.F + f];
-        const double detJ = facet_detj<DIM>(pos, N, fn);
-        if (ff & HT_Q) {  // getQN, MatricesBuilder.inl:246-272
-            const int e = hf.felem[f];
-            int out = -1;
-#pragma unroll
-            for (int a = 0; a < NPE; ++a) {
-                const int v = conn[(size_t)a * E + e];
-                bool on = false;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) on |= v == fn[d];
-                if (!on) out = v;
-            }
-            double nv[DIM];
-            facet_normal<DIM>(pos, N, fn, out, nv);
-            double qn = 0;
-#pragma unroll
-            for (int g = 0; g < 3; ++g) {
-                double qdn = 0;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) qdn += hf.q[((size_t)f * 3 + g) * DIM + d] * nv[d];
-                qn += (qdn * k.fw[g]) * k.fsf[g][kk];
-            }
-            b -= k.dt * ((qn * k.fref) * detJ);
-        }
-#pragma unroll
-        for (int pass = 0; pass < 2; ++pass) {  // getSGamma, MatricesBuilder.inl:357-370 (:76-94)
-            if (!(ff & (pass == 0 ? HT_QH : HT_QR))) continue;
-            double sg = 0;
-#pragma unroll
-            for (int g = 0; g < 3; ++g) {
-                double T = 0;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) T += k.fsf[g][d] * ts[fn[d]];
-                const double fac = pass == 0 ? k.h * (T - k.tinf)
-                                             : sigma * k.eps_rad * (T * T * T * T - k.tinf * k.tinf * k.tinf * k.tinf);
-                sg += (fac * k.fsf[g][kk]) * k.fw[g];
-            }
-            b -= k.dt * (sg * (detJ * k.fref));
-        }
-    }
+    heat_facet_terms<DIM>(n, N, E, conn, pos, ts, hf, k, k.dt, b);
     const uint8_t h = hflags[n];
     const bool fr = flags[n] & F_FREE;
     if (h & HT_T) {
@@ -615,6 +626,8 @@ __global__ void __launch_bounds__(BLOCK) k_heat_res(int N, const double* __restr
     }
 }
 
+HeatFacets heat_facets(pfg_ctx* c);
+
 template <int DIM>
 void heat_assemble(pfg_ctx* c, const HeatConst& k, const double* tprev, const double* ts) {
     const int N = c->N, E = c->E;
@@ -628,14 +641,7 @@ void heat_assemble(pfg_ctx* c, const HeatConst& k, const double* tprev, const do
             c->P, E, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem),
             ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ptr<double>(c->edata), ptr<uint8_t>(c->flags),
             ptr<uint8_t>(c->heat_flags), ptr<double>(c->heat_val), ts, ptr<DF>(c->edata_df), k);
-    HeatFacets hf;
-    hf.ptr = ptr<int>(c->hf_ptr);
-    hf.ent = ptr<int>(c->hf_ent);
-    hf.fflags = ptr<uint8_t>(c->hf_fflags);
-    hf.fnodes = ptr<int>(c->fc_nodes);
-    hf.felem = ptr<int>(c->fc_elem);
-    hf.q = c->has_heat_q ? ptr<double>(c->heat_q) : nullptr;
-    hf.F = c->F;
+    const HeatFacets hf = heat_facets(c);
     k_heat_rhs<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
         N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
         ptr<double>(c->edata), ptr<double>(c->pos), ptr<uint8_t>(c->flags), ptr<uint8_t>(c->heat_flags), tprev, ts,
@@ -752,6 +758,129 @@ int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
     return PFG_OK;
 }
 
+// ---- explicit heat step of problem BoussinesqWC (HeatEqWCompNewton) ----------------------
+//
+// HeatEqWCompNewton::solve (WCompNewton/HeatEquation.inl:137-158) inside the WC step, after the
+// half-step prediction moved the nodes.  Element: for each element node i the lumped mass
+//   ML_i = |e| sum_g w_g N_i(g) f_g,  f_g = cv rho_g, or (cv + dfl/dT(T_g) Lm) rho_g with phase
+// change (getM with the factor of :51-66, then lump: the row sum of the consistent block), and
+//   FTot_i = -dt (Le T)_i + ML_i T_i,  Le = |e| k_sum gradN^T gradN  (:285-299).
+// Node: sums in ascending element order, the facet terms in facet order, the node conditions
+// (:240-260), T = F / M into a second array (the facet terms read the neighbours' old
+// temperatures), copied back.  dt is read from the step's device dt slot (slot 0).
+template <int DIM>
+__global__ void __launch_bounds__(BLOCK) k_wch_elem(int E, int N, const int* __restrict__ conn,
+                                                    const double* __restrict__ pos, const double* __restrict__ rho,
+                                                    const double* __restrict__ T, const double* __restrict__ tdt,
+                                                    HeatConst k, double* __restrict__ rec) {
+    constexpr int NPE = DIM + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const double dt = tdt[0];
+    int nd[NPE];
+    load_nodes<DIM>(conn, E, e, nd);
+    Geom<DIM> g;
+    compute_geom<DIM>(pos, N, nd, g);
+    double G[DIM][NPE];
+    grad_n<DIM>(g, G);
+    const double ae = g.detJ * k.refSize;
+    double te[NPE], re[NPE], gt[DIM];
+#pragma unroll
+    for (int a = 0; a < NPE; ++a) {
+        te[a] = T[nd[a]];
+        re[a] = rho[nd[a]];
+    }
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) {
+        double t = 0;
+#pragma unroll
+        for (int j = 0; j < NPE; ++j) t += G[f][j] * te[j];
+        gt[f] = t;
+    }
+    double ml[NPE] = {};
+    for (int q = 0; q < k.ng; ++q) {
+        double Tg = 0, rg = 0;
+#pragma unroll
+        for (int a = 0; a < NPE; ++a) {
+            Tg += k.gN[q][a] * te[a];
+            rg += k.gN[q][a] * re[a];
+        }
+        const double f = k.phase ? (k.cv + dfl_dt(k, Tg) * k.lm) * rg : k.cv * rg;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) ml[i] += (f * k.gN[q][i]) * k.gw[q];
+    }
+    double* out = rec + (size_t)e * 2 * NPE;
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) {
+        double lt = 0;
+#pragma unroll
+        for (int f = 0; f < DIM; ++f) lt += G[f][i] * gt[f];
+        const double m = ml[i] * ae;
+        out[i] = m;
+        out[NPE + i] = -dt * ((k.lsum * ae) * lt) + m * te[i];
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(BLOCK) k_wch_node(int N, int E, const int* __restrict__ ne_ptr,
+                                                    const int* __restrict__ ne_elem,
+                                                    const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
+                                                    const double* __restrict__ pos, const uint8_t* __restrict__ flags,
+                                                    const uint8_t* __restrict__ hflags, const double* __restrict__ T,
+                                                    const double* __restrict__ tbc, const double* __restrict__ rec,
+                                                    HeatFacets hf, HeatConst k, const double* __restrict__ tdt,
+                                                    double* __restrict__ tnew) {
+    constexpr int NPE = DIM + 1;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const double dt = tdt[0];
+    double m = 0, F = 0;
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const double* r = rec + (size_t)ne_elem[q] * 2 * NPE;
+        const int i = ne_loc[q];
+        m += r[i];
+        F += r[NPE + i];
+    }
+    heat_facet_terms<DIM>(n, N, E, conn, pos, T, hf, k, dt, F);
+    const uint8_t h = hflags[n];
+    if ((flags[n] & F_FREE) && !(h & HT_T)) tnew[n] = T[n];
+    else if (h & HT_T) tnew[n] = tbc[n];
+    else tnew[n] = (1 / m) * F;
+}
+
+HeatFacets heat_facets(pfg_ctx* c) {
+    HeatFacets hf;
+    hf.ptr = ptr<int>(c->hf_ptr);
+    hf.ent = ptr<int>(c->hf_ent);
+    hf.fflags = ptr<uint8_t>(c->hf_fflags);
+    hf.fnodes = ptr<int>(c->fc_nodes);
+    hf.felem = ptr<int>(c->fc_elem);
+    hf.q = c->has_heat_q ? ptr<double>(c->heat_q) : nullptr;
+    hf.F = c->F;
+    return hf;
+}
+
+template <int DIM>
+int wc_heat_dim(pfg_ctx* c, const double* tdt) {
+    const int N = c->N, E = c->E;
+    const HeatConst k = heat_const(c, 0.0);
+    double* rec = ptr<double>(c->wch_rec);
+    double* T = ptr<double>(c->heat_t);
+    double* tnew = ptr<double>(c->heat_rhs);
+    prof_begin(c, PH_HEAT_ASSEMBLY);
+    if (E > 0)
+        k_wch_elem<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
+            E, N, ptr<int>(c->conn), ptr<double>(c->pos), ptr<double>(c->ws) + (size_t)(DIM + 1) * N, T, tdt, k, rec);
+    k_wch_node<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(
+        N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn),
+        ptr<double>(c->pos), ptr<uint8_t>(c->flags), ptr<uint8_t>(c->heat_flags), T, ptr<double>(c->heat_tbc), rec,
+        heat_facets(c), k, tdt, tnew);
+    PFG_CUDA(c, cudaMemcpyAsync(T, tnew, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    prof_end(c, PH_HEAT_ASSEMBLY);
+    PFG_CHECK_LAUNCH(c);
+    return PFG_OK;
+}
+
 }  // namespace
 
 int heat_alloc(pfg_ctx* c) {
@@ -820,6 +949,33 @@ int heat_build_facets(pfg_ctx* c) {
 
 int heat_step(pfg_ctx* c, double dt, pfg_step_status* st) {
     return c->dim == 2 ? heat_dim<2>(c, dt, st) : heat_dim<3>(c, dt, st);
+}
+
+// Host work before a BoussinesqWC step is launched or captured: heat buffers, the element
+// records and the per-node facet lists.  *changed reports reallocated or rebuilt buffers (a
+// captured step graph holding their old addresses must be dropped).
+int wc_heat_prepare(pfg_ctx* c, bool* changed) {
+    int rc;
+    *changed = false;
+    if (!c->heat_ready) {
+        if ((rc = heat_alloc(c))) return rc;
+        *changed = true;
+    }
+    const size_t need = sizeof(double) * 2 * (size_t)c->npe * std::max(c->E, 1);
+    if (c->wch_rec.cap < need) {
+        if ((rc = ensure(c, c->wch_rec, need))) return rc;
+        *changed = true;
+    }
+    if (c->heat_facets_dirty) {
+        if ((rc = heat_build_facets(c))) return rc;
+        *changed = true;
+    }
+    return PFG_OK;
+}
+
+// Enqueue the explicit heat step of one BoussinesqWC step (graph-capturable).
+int wc_heat_launch(pfg_ctx* c, const double* tdt) {
+    return c->dim == 2 ? wc_heat_dim<2>(c, tdt) : wc_heat_dim<3>(c, tdt);
 }
 
 }  // namespace pfg

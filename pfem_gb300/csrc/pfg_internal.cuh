@@ -94,8 +94,11 @@ struct pfg_ctx {
     // node adjacency (sorted, includes the node) and the node-pair list
     pfg::DBuf nbr_ptr, nbr, pair_node;
     int P = 0;
-    // mixed PSPG: element list of each off-diagonal node pair (e*16 + i*4 + j, ascending e)
+    // mixed PSPG: element list of each off-diagonal node pair (slot(e)*16 + i*4 + j, ascending e)
     pfg::DBuf pe_ptr, pe_item;
+    // mixed assembly: slot of each element in the element-major data (elements ordered by their
+    // smallest node) and the slot of each incidence's element
+    pfg::DBuf el_slot, ne_slot;
     // CSR system
     pfg::DBuf row_ptr, col, val, val32, diag_pos, rhs;
     int64_t nnz = 0;
@@ -153,6 +156,7 @@ struct pfg_ctx {
     // double-float values per element node)
     pfg::DBuf mx_scale32, mx_f32, mx_xdf, mx_vpdf, mx_tdf, mx_rec, mx_gdf;
     pfg::DBuf mx_ed_aos;  // element data element-major (high, then low parts) for the gathering kernels
+    pfg::DBuf mx_vsum;    // per element: sums of the previous velocities over its nodes (double-float)
     int n_inst = 0, n_seg = 0;
     cudaGraphExec_t mx_graph[2] = {nullptr, nullptr};  // one chunk of BiCGSTAB iterations [FP32, FP64]
     std::vector<int> h_mx_ii;
@@ -179,6 +183,7 @@ struct pfg_ctx {
     // flags, and the flux vectors at the facet Gauss points
     pfg::DBuf heat_t, heat_flags, heat_tbc, heat_val, heat_rhs, heat_cg, heat_red;
     pfg::DBuf hf_ptr, hf_ent, hf_fflags, heat_q;
+    pfg::DBuf wch_rec;  // BoussinesqWC heat step: per element node lumped mass and right-hand side
     bool heat_ready = false;  // heat buffers allocated (and zeroed) for the current mesh
     bool has_heat_bc = false, has_heat_q = false;
     bool heat_facets_dirty = true;  // the per-node heat facet lists need rebuilding
@@ -278,6 +283,8 @@ int mx_alloc(pfg_ctx* c);
 int heat_alloc(pfg_ctx* c);
 int heat_build_facets(pfg_ctx* c);
 int heat_step(pfg_ctx* c, double dt, pfg_step_status* st);
+int wc_heat_prepare(pfg_ctx* c, bool* changed);
+int wc_heat_launch(pfg_ctx* c, const double* tdt);
 int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* rho, const double* mu);
 int mx_picard_step(pfg_ctx* c, const double* dts, pfg_step_status* st);
 void mx_release_graph(pfg_ctx* c);

@@ -177,15 +177,44 @@ __device__ __forceinline__ int nbr_rank(const int* __restrict__ nbr, int b0, int
     return lo - b0;
 }
 
+// Slots of the element-major element data of the mixed assembly: the elements in the order of
+// their smallest node (ties by element index), so the elements that a run of consecutive nodes
+// touches sit in a compact range of slots and the node and pair kernels' gathers hit L2.
+// FILL = false counts, per node, the elements whose smallest node it is; FILL = true numbers
+// them from the node's scanned base in its ascending incidence order.
+template <bool FILL>
+__global__ void k_elem_slots(int N, int npe, int E, const int* __restrict__ conn, const int* __restrict__ ne_ptr,
+                             const int* __restrict__ ne_elem, int* __restrict__ count, const int* __restrict__ base,
+                             int* __restrict__ el_slot) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    int k = FILL ? base[n] : 0;
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const int e = ne_elem[q];
+        int mn = conn[e];
+        for (int j = 1; j < npe; ++j) mn = min(mn, conn[(size_t)j * E + e]);
+        if (mn != n) continue;
+        if (FILL) el_slot[e] = k;
+        ++k;
+    }
+    if (!FILL) count[n] = k;
+}
+
+__global__ void k_ne_slots(long long inc, const int* __restrict__ ne_elem, const int* __restrict__ el_slot,
+                           int* __restrict__ ne_slot) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < inc) ne_slot[q] = el_slot[ne_elem[q]];
+}
+
 // Element lists of the off-diagonal node pairs: pair p = (n, m), m != n, lists every element
-// containing both, ascending, as e * 16 + (local index of n) * 4 + (local index of m).  One
+// containing both, ascending, as slot(e) * 16 + (local index of n) * 4 + (local index of m).  One
 // thread per node n owns the lists of n's pairs and walks n's sorted incidences, so each list
 // comes out in ascending element order.  FILL = false counts, FILL = true writes.
 template <bool FILL>
 __global__ void k_pair_items(int N, int npe, int E, const int* __restrict__ conn, const int* __restrict__ ne_ptr,
                              const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
                              const int* __restrict__ nbr_ptr, const int* __restrict__ nbr, int* __restrict__ cnt,
-                             const int* __restrict__ pe_ptr, int* __restrict__ pe_item) {
+                             const int* __restrict__ pe_ptr, int* __restrict__ pe_item, const int* __restrict__ el_slot) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     const int b0 = nbr_ptr[n], b1 = nbr_ptr[n + 1];
@@ -196,7 +225,7 @@ __global__ void k_pair_items(int N, int npe, int E, const int* __restrict__ conn
             if (j == i) continue;
             const int p = b0 + nbr_rank(nbr, b0, b1, conn[(size_t)j * E + e]);
             if (FILL)
-                pe_item[pe_ptr[p] + cnt[p]++] = (e << 4) | (i << 2) | j;
+                pe_item[pe_ptr[p] + cnt[p]++] = (el_slot[e] << 4) | (i << 2) | j;
             else
                 ++cnt[p];
         }
@@ -366,13 +395,29 @@ int build_topology(pfg_ctx* c) {
             cleanup();
             return fail(c, PFG_ERR_UNSUPPORTED, "too many elements for the pair element lists");
         }
+        TRY(ensure(c, c->el_slot, sizeof(int) * (size_t)std::max(E, 1)));
+        TRY(ensure(c, c->ne_slot, sizeof(int) * std::max<long long>(inc, 1)));
+        k_elem_slots<false><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
+                                                                   ptr<int>(c->ne_elem), ptr<int>(cnt), nullptr,
+                                                                   nullptr);
+        PFG_CHECK_LAUNCH(c);
+        TRY(scan_exclusive(c, ptr<int>(cnt), ptr<int>(fill), N, tmp));
+        k_elem_slots<true><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
+                                                                  ptr<int>(c->ne_elem), nullptr, ptr<int>(fill),
+                                                                  ptr<int>(c->el_slot));
+        PFG_CHECK_LAUNCH(c);
+        if (inc > 0) {
+            k_ne_slots<<<div_up(inc, BLOCK), BLOCK, 0, c->stream>>>(inc, ptr<int>(c->ne_elem), ptr<int>(c->el_slot),
+                                                                    ptr<int>(c->ne_slot));
+            PFG_CHECK_LAUNCH(c);
+        }
         TRY(ensure(c, cnt, sizeof(int) * (size_t)std::max(c->P, 1)));
         TRY(ensure(c, c->pe_ptr, sizeof(int) * ((size_t)c->P + 1)));
         PFG_CUDA(c, cudaMemsetAsync(cnt.p, 0, sizeof(int) * (size_t)c->P, c->stream));
         k_pair_items<false><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
                                                                    ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
                                                                    ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
-                                                                   nullptr, nullptr);
+                                                                   nullptr, nullptr, nullptr);
         PFG_CHECK_LAUNCH(c);
         TRY(scan_exclusive(c, ptr<int>(cnt), ptr<int>(c->pe_ptr), c->P, tmp));
         const long long items = (long long)E * npe * (npe - 1);
@@ -381,7 +426,8 @@ int build_topology(pfg_ctx* c) {
         k_pair_items<true><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
                                                                   ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
                                                                   ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
-                                                                  ptr<int>(c->pe_ptr), ptr<int>(c->pe_item));
+                                                                  ptr<int>(c->pe_ptr), ptr<int>(c->pe_item),
+                                                                  ptr<int>(c->el_slot));
         PFG_CHECK_LAUNCH(c);
     }
 

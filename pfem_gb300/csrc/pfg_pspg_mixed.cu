@@ -74,6 +74,10 @@ struct MxConst {
     // factors 1 + alpha Tr and alpha; FP32 copies for the FP32 assembly
     DF mm_df[4][4], s_df[4], ref_df, hsum_df, inv_pi_df, g_df[3], bq_c0, bq_alpha;
     float mm32[4][4], s32[4], ref32;
+    // p1: the tables have the P1 structure M_ij = m0 (1 + delta_ij), s_j = s (exact Gauss
+    // rules), which the node kernel's right-hand side uses to sum velocities per element once
+    bool p1;
+    DF m0_df;
     BoussArgs bq;
     double rtol, atol, eta, min_res;
     int max_iter;
@@ -119,6 +123,14 @@ MxConst mx_const(pfg_ctx* c) {
         for (int j = 0; j < 4; ++j) k.mm32[i][j] = (float)g.MM[i][j];
     }
     k.ref32 = (float)g.refSize;
+    const int npe = c->dim + 1;
+    const double m0 = g.MM[0][1], s0 = g.s[0];
+    k.p1 = m0 > 0 && s0 > 0;
+    for (int i = 0; i < npe; ++i) {
+        k.p1 = k.p1 && std::fabs(g.s[i] - s0) <= 1e-15 * s0;
+        for (int j = 0; j < npe; ++j) k.p1 = k.p1 && std::fabs(g.MM[i][j] - (i == j ? 2.0 : 1.0) * m0) <= 1e-15 * m0;
+    }
+    k.m0_df = split(m0);
     k.rtol = c->prm.krylov_rel_tol;
     k.atol = c->prm.krylov_abs_tol;
     k.eta = c->prm.inner_rel_tol > 0 ? c->prm.inner_rel_tol : 1e-4;
@@ -204,11 +216,12 @@ __device__ __forceinline__ DF inst_df(const float* f32, int inst, int which) {
 }
 
 // Element data as double-float planes: value v of element e is h[v E + e] + l[v E + e] (the
-// element kernels' coalesced layout), and the same values element-major: element e's 16 high
-// parts in ah[16 e ..], its low parts in al[16 e ..], so a kernel that gathers an element by
-// index reads two 32-byte sectors of high parts (FP32 arithmetic), plus two of low parts
-// (double-float), instead of one sector per value.  High and low parts are kept apart so that
-// the FP32 gathers' L2 footprint is the high parts alone.
+// element kernels' coalesced layout), and the same values element-major at the element's slot
+// s (elements ordered by their smallest node): the 16 high parts in ah[16 s ..], the low parts
+// in al[16 s ..], so a kernel that gathers an element reads two 32-byte sectors of high parts
+// (FP32 arithmetic), plus two of low parts (double-float), instead of one sector per value, and
+// the elements of consecutive nodes share sectors and L2 lines.  High and low parts are kept
+// apart so that the FP32 gathers' L2 footprint is the high parts alone; gdf/gf take the slot.
 constexpr int ED_AOS = 16;
 struct EdPlanes {
     const float* h;
@@ -227,10 +240,11 @@ struct EdPlanes {
     __device__ __forceinline__ float gf(int v, int e) const { return __ldg(ah + (size_t)e * ED_AOS + v); }
 };
 
-// Stores element e's values v (high and low parts) in both layouts.
+// Stores element e's values v (high and low parts) in both layouts, the element-major record
+// at the element's slot.
 template <int NV>
 __device__ __forceinline__ void ed_store(float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea, int E,
-                                         int e, const DF (&v)[NV]) {
+                                         int e, int slot, const DF (&v)[NV]) {
     static_assert(NV <= ED_AOS, "element record holds 16 values");
     float rh[ED_AOS], rl[ED_AOS];
 #pragma unroll
@@ -243,8 +257,8 @@ __device__ __forceinline__ void ed_store(float* __restrict__ eh, float* __restri
         eh[(size_t)k * E + e] = v[k].h;
         el[(size_t)k * E + e] = v[k].l;
     }
-    float4* dh = reinterpret_cast<float4*>(ea + (size_t)e * ED_AOS);
-    float4* dl = reinterpret_cast<float4*>(ea + (size_t)E * ED_AOS + (size_t)e * ED_AOS);
+    float4* dh = reinterpret_cast<float4*>(ea + (size_t)slot * ED_AOS);
+    float4* dl = reinterpret_cast<float4*>(ea + (size_t)E * ED_AOS + (size_t)slot * ED_AOS);
 #pragma unroll
     for (int k = 0; k < ED_AOS / 4; ++k) {
         dh[k] = make_float4(rh[4 * k], rh[4 * k + 1], rh[4 * k + 2], rh[4 * k + 3]);
@@ -254,19 +268,40 @@ __device__ __forceinline__ void ed_store(float* __restrict__ eh, float* __restri
 
 __device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
 
+// Sums over the element's nodes of the previous velocities, V_f = sum_j v_jf in double-float,
+// stored element-major at the element's slot as two float4 (high parts, then low parts; one
+// 32-byte sector): with the P1 tables the right-hand side's mass and continuity terms of a node
+// need only these sums.
+template <int DIM>
+__device__ __forceinline__ void elem_vsum(const DF* __restrict__ vp, int N, const int (&nd)[DIM + 1], int e,
+                                          float4* __restrict__ vsum) {
+    DF V[DIM];
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) {
+        V[f] = vp[(size_t)f * N + nd[0]];
+#pragma unroll
+        for (int j = 1; j <= DIM; ++j) V[f] = df_add(V[f], vp[(size_t)f * N + nd[j]]);
+    }
+    vsum[2 * (size_t)e] = make_float4(V[0].h, V[1].h, DIM == 3 ? V[DIM - 1].h : 0.0f, 0.0f);
+    vsum[2 * (size_t)e + 1] = make_float4(V[0].l, V[1].l, DIM == 3 ? V[DIM - 1].l : 0.0f, 0.0f);
+}
+
 // Geometry (Element.cpp:15-135) and tau (MomContEquationPSPG.inl:237-259) of the elements of
 // active instances in FP64, with the Bingham K factor: [detJ, tau, gradN, ksum] stored as
 // double-float planes.
 template <int DIM>
 __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
                           const double* __restrict__ q_iter, Mx m, double refSize, ViscArgs va,
-                          float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea) {
+                          float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea,
+                          const DF* __restrict__ vp, float4* __restrict__ vsum, const int* __restrict__ el_slot) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
     load_nodes<DIM>(conn, E, e, nd);
     const int inst = m.node_inst[nd[0]];
     if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    const int slot = el_slot[e];
+    elem_vsum<DIM>(vp, N, nd, slot, vsum);
     const double rho = m.id[inst * D_COUNT + D_RHO], mu = m.id[inst * D_COUNT + D_MU];
     const double dt = m.id[inst * D_COUNT + D_DT];
     Geom<DIM> g;
@@ -299,7 +334,7 @@ __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const doub
     DF dv[ed_count<DIM>()];
 #pragma unroll
     for (int k = 0; k < ed_count<DIM>(); ++k) dv[k] = df_from(v[k]);
-    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, dv);
+    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, slot, dv);
 }
 
 // Double-float copies of the positions and the iterate's velocities (inputs of k_mx_prep_df).
@@ -323,7 +358,8 @@ __global__ void k_mx_gprep(int N, const double* __restrict__ pos, const double* 
 template <int DIM>
 __global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const DF* __restrict__ gdf,
                              const float* __restrict__ f32, Mx m, DF ref_df, DF inv_pi, float* __restrict__ eh,
-                             float* __restrict__ el, float* __restrict__ ea) {
+                             float* __restrict__ el, float* __restrict__ ea, const DF* __restrict__ vp,
+                             float4* __restrict__ vsum, const int* __restrict__ el_slot) {
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -331,6 +367,8 @@ __global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const D
     load_nodes<DIM>(conn, E, e, nd);
     const int inst = m.node_inst[nd[0]];
     if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    const int slot = el_slot[e];
+    elem_vsum<DIM>(vp, N, nd, slot, vsum);
     DF X[NPE][DIM];
 #pragma unroll
     for (int k = 0; k < NPE; ++k)
@@ -405,7 +443,7 @@ __global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const D
 #pragma unroll
         for (int i = 0; i < NPE; ++i) dv[2 + f * NPE + i] = G[f][i];
     dv[ed_ksum<DIM>()] = inst_df(f32, inst, F_KSUM);
-    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, dv);
+    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, slot, dv);
 }
 
 // Double-float copies of the previous velocities and (Boussinesq) the temperatures.
@@ -460,48 +498,48 @@ __device__ __forceinline__ void pair_item_df(const EdPlanes& ed, int e, int i, i
     acc[DIM][DIM] = df_add(acc[DIM][DIM], df_mul(tau, df_mul(df_mul(ae, l_sum), dot)));
 }
 
-// Inverse of a (d+1)x(d+1) block by Gauss-Jordan elimination with partial pivoting in FP64; a
-// singular block falls back to the inverse of its diagonal.
-template <int B>
-__device__ __forceinline__ void block_inverse(const double (&a0)[B][B], double (&inv)[B][B]) {
-    double a[B][2 * B];
+// Inverse of a (d+1)x(d+1) block by Gauss-Jordan elimination with partial pivoting in the
+// block's own precision; a singular block falls back to the inverse of its diagonal.
+template <int B, class T>
+__device__ __forceinline__ void block_inverse(const T (&a0)[B][B], T (&inv)[B][B]) {
+    T a[B][2 * B];
 #pragma unroll
     for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2) {
             a[f1][f2] = a0[f1][f2];
-            a[f1][B + f2] = (f1 == f2) ? 1.0 : 0.0;
+            a[f1][B + f2] = (f1 == f2) ? T(1) : T(0);
         }
     bool ok = true;
 #pragma unroll
     for (int kk = 0; kk < B; ++kk) {
         int piv = kk;
-        double best = fabs(a[kk][kk]);
+        T best = fabs(a[kk][kk]);
 #pragma unroll
         for (int i = kk + 1; i < B; ++i)
             if (fabs(a[i][kk]) > best) {
                 best = fabs(a[i][kk]);
                 piv = i;
             }
-        if (best == 0.0) ok = false;
+        if (best == T(0)) ok = false;
         // row swap through compile-time indices (keeps the block in registers)
 #pragma unroll
         for (int i = kk + 1; i < B; ++i)
             if (i == piv) {
 #pragma unroll
                 for (int j = 0; j < 2 * B; ++j) {
-                    const double t = a[kk][j];
+                    const T t = a[kk][j];
                     a[kk][j] = a[i][j];
                     a[i][j] = t;
                 }
             }
-        const double inv_p = ok ? 1.0 / a[kk][kk] : 0.0;
+        const T inv_p = ok ? T(1) / a[kk][kk] : T(0);
 #pragma unroll
         for (int j = 0; j < 2 * B; ++j) a[kk][j] *= inv_p;
 #pragma unroll
         for (int i = 0; i < B; ++i) {
             if (i == kk) continue;
-            const double f = a[i][kk];
+            const T f = a[i][kk];
 #pragma unroll
             for (int j = 0; j < 2 * B; ++j) a[i][j] -= f * a[kk][j];
         }
@@ -511,7 +549,7 @@ __device__ __forceinline__ void block_inverse(const double (&a0)[B][B], double (
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2)
             inv[f1][f2] = ok ? a[f1][B + f2]
-                             : ((f1 == f2) ? (a0[f1][f1] != 0.0 ? 1.0 / a0[f1][f1] : 1.0) : 0.0);
+                             : ((f1 == f2) ? (a0[f1][f1] != T(0) ? T(1) / a0[f1][f1] : T(1)) : T(0));
 }
 
 __device__ __forceinline__ int self_rank(const int* __restrict__ nbr, int b0, int b1, int n) {
@@ -555,20 +593,29 @@ __device__ __forceinline__ void store_block32(float* __restrict__ blk, uint16_t*
 // FP32 system's arithmetic: FP32, or double-float with DFA) and right-hand side (double-float)
 // in element order, with the expressions of pspg_pair_block and pspg_node_rhs; then
 // m_applyBCPSPG's node conditions (:189-232; identity rows :108-128, the Dirichlet columns of
-// the node's own block zeroed), the row scales S = |a_rr|^-1/2, the block inverses (FP64, and
-// scaled in FP32), the scaled diagonal block of the FP32 system and ||b||^2 of each instance
-// (the relative tolerance of its linear solves).
+// the node's own block zeroed), the row scales S = |a_rr|^-1/2, the FP32 inverse of the scaled
+// diagonal block (the block-Jacobi smoother), the scaled diagonal block of the FP32 system and
+// ||b||^2 of each instance (the relative tolerance of its linear solves).
+//
+// Right-hand side with the P1 tables (M_ij = m0 (1 + delta_ij), s_j = s) and no Boussinesq
+// factors: for node i of element e with a_e = detJ refSize, tau_e and the element's velocity
+// sums V_e (k_mx_prep*),
+//   b_f = rho s g_f sum_e a_e + (rho m0 / dt) (sum_e a_e V_ef + v_if sum_e a_e)
+//   b_p = hsum sum_f g_f sum_e tau_e a_e g_if + (s / dt) sum_e tau_e a_e (g_i . V_e)
+// which is the element sum of F_i + (M/dt) v_prev and tau H_i + (tau/dt) C v_prev
+// (MomContEquationPSPG.inl:48-96) regrouped; otherwise the element expressions term by term.
 template <int DIM, bool DFA>
 __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* __restrict__ ne_ptr,
-                                                const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
-                                                const int* __restrict__ conn, EdPlanes ed,
-                                                const uint8_t* __restrict__ flags, const DF* __restrict__ vp,
-                                                const DF* __restrict__ tdf, const double* __restrict__ q_prev,
-                                                const double* __restrict__ vbc, const double* __restrict__ fst,
-                                                const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
-                                                const float* __restrict__ f32, MxConst k, double* __restrict__ rhs,
-                                                double* __restrict__ scale, float* __restrict__ scale32,
-                                                double* __restrict__ binv64, float* __restrict__ binv32,
+                                                const int* __restrict__ ne_elem, const int* __restrict__ ne_slot,
+                                                const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
+                                                EdPlanes ed, const uint8_t* __restrict__ flags,
+                                                const DF* __restrict__ vp, const float4* __restrict__ vsum,
+                                                const DF* __restrict__ tdf,
+                                                const double* __restrict__ q_prev, const double* __restrict__ vbc,
+                                                const double* __restrict__ fst, const int* __restrict__ nbr_ptr,
+                                                const int* __restrict__ nbr, const float* __restrict__ f32, MxConst k,
+                                                double* __restrict__ rhs, double* __restrict__ scale,
+                                                float* __restrict__ scale32, float* __restrict__ binv32,
                                                 float* __restrict__ blk, uint16_t* __restrict__ blk16) {
     constexpr int B = DIM + 1, NPE = DIM + 1;
     __shared__ double sh[32];
@@ -578,6 +625,7 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
     if (!ii[I_ACTIVE]) return;
     const int n = m.seg[3 * sb + 1] + threadIdx.x;
     const bool act = n < m.seg[3 * sb + 2];
+    const bool p1 = k.p1 && !tdf;
     double bb = 0;
     if (act) {
         if (n == ii[I_N0]) ii[I_M64] = 0;  // the FP64 CSR values (if any) predate this assembly
@@ -595,13 +643,13 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
             }
         const float cm32 = f32[inst * F_COUNT + F_CM], ct32 = f32[inst * F_COUNT + F_INVDT];
         const float l32 = f32[inst * F_COUNT + F_LSUM];
+        // P1 accumulators: sum a_e, sum a_e V_e, sum tau_e a_e g_i, sum tau_e a_e (g_i . V_e)
+        DF sae{0.0f, 0.0f}, av[DIM], tg[DIM], tc{0.0f, 0.0f};
 #pragma unroll
-        for (int f = 0; f < DIM; ++f) bv[f] = DF{0.0f, 0.0f};
+        for (int f = 0; f < DIM; ++f) bv[f] = av[f] = tg[f] = DF{0.0f, 0.0f};
         for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-            const int e = ne_elem[q];
+            const int e = ne_slot[q];  // element-major data are stored by slot
             const int i = ne_loc[q];
-            int nd[NPE];
-            load_nodes<DIM>(conn, E, e, nd);
             const DF ae = df_mul(ed.gdf(0, e), k.ref_df);
             const DF tau = ed.gdf(1, e);
             DF gi[DIM];
@@ -628,6 +676,24 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
                 }
                 A32[DIM][DIM] += t32 * a32 * l32 * dot;
             }
+            if (p1) {
+                const float4 vh = __ldg(vsum + 2 * (size_t)e), vl = __ldg(vsum + 2 * (size_t)e + 1);
+                const DF V[3] = {DF{vh.x, vl.x}, DF{vh.y, vl.y}, DF{vh.z, vl.z}};
+                const DF ta = df_mul(tau, ae);
+                DF gv = df_mul(gi[0], V[0]);
+#pragma unroll
+                for (int f = 1; f < DIM; ++f) gv = df_add(gv, df_mul(gi[f], V[f]));
+                sae = df_add(sae, ae);
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) {
+                    av[f] = df_add(av[f], df_mul(ae, V[f]));
+                    tg[f] = df_add(tg[f], df_mul(ta, gi[f]));
+                }
+                tc = df_add(tc, df_mul(ta, gv));
+                continue;
+            }
+            int nd[NPE];
+            load_nodes<DIM>(conn, E, ne_elem[q], nd);
             DF fs = k.s_df[i], hs = k.hsum_df;
             if (tdf) {  // Boussinesq factors (MomContEquation.inl:164-199)
                 DF mt{0.0f, 0.0f}, st{0.0f, 0.0f};
@@ -662,6 +728,17 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
             const DF H = df_mul(tau, df_mul(df_mul(ae, hs), gdot));
             bp = df_add(bp, df_add(H, df_mul(df_mul(tau, inv_dt), cv)));
         }
+        if (p1) {
+            const DF cm = df_mul(df_mul(rho, k.m0_df), inv_dt), rs = df_mul(rho, k.s_df[0]);
+            DF hg{0.0f, 0.0f};
+#pragma unroll
+            for (int f = 0; f < DIM; ++f) {
+                const DF mv = df_mul(cm, df_add(av[f], df_mul(sae, vp[(size_t)f * N + n])));
+                bv[f] = df_add(df_mul(df_mul(rs, k.g_df[f]), sae), mv);
+                hg = df_add(hg, df_mul(k.g_df[f], tg[f]));
+            }
+            bp = df_add(df_mul(k.hsum_df, hg), df_mul(df_mul(k.s_df[0], inv_dt), tc));
+        }
         // right-hand side with the node conditions (m_applyBCPSPG :186-232)
         const bool free_n = fl & F_FREE, bound = fl & F_BOUND, dir = bound && (fl & F_DIRICHLET);
         double b[B];
@@ -685,38 +762,40 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
             bb += b[f] * b[f];
         }
         // the node's own block with its identity rows and zeroed Dirichlet columns
-        double a[B][B];
+        float a[B][B];
 #pragma unroll
         for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
             for (int f2 = 0; f2 < B; ++f2) {
-                double v;
-                if constexpr (DFA) v = df_to(A[f1][f2]);
-                else v = (double)A32[f1][f2];
-                if (free_n || (bound && f1 < DIM)) v = (f1 == f2) ? 1.0 : 0.0;
-                else if (dir && f2 < DIM && f1 != f2) v = 0.0;
+                float v;
+                if constexpr (DFA) v = (float)df_to(A[f1][f2]);
+                else v = A32[f1][f2];
+                if (free_n || (bound && f1 < DIM)) v = (f1 == f2) ? 1.0f : 0.0f;
+                else if (dir && f2 < DIM && f1 != f2) v = 0.0f;
                 a[f1][f2] = v;
             }
-        double s[B], si[B];  // S = |a_rr|^-1/2 and its inverse |a_rr|^1/2
+        float s[B];  // S = |a_rr|^-1/2 (FP64 root of the FP32 diagonal)
 #pragma unroll
         for (int f = 0; f < B; ++f) {
-            const double d = fabs(a[f][f]);
-            si[f] = d > 0.0 ? sqrt(d) : 1.0;
-            s[f] = 1.0 / si[f];
-            scale[(size_t)f * N + n] = s[f];
-            scale32[(size_t)f * N + n] = (float)s[f];
+            const double d = fabs((double)a[f][f]);
+            const double sd = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+            scale[(size_t)f * N + n] = sd;
+            s[f] = (float)sd;
+            scale32[(size_t)f * N + n] = s[f];
         }
-        double inv[B][B];
-        block_inverse<B>(a, inv);
+        float sas[B][B], inv[B][B];
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) sas[f1][f2] = s[f1] * a[f1][f2] * s[f2];
+        block_inverse<B>(sas, inv);
         float out[B * B];
 #pragma unroll
         for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
             for (int f2 = 0; f2 < B; ++f2) {
-                binv64[(size_t)(f1 * B + f2) * N + n] = inv[f1][f2];
-                // (S A S)^-1 = S^-1 A^-1 S^-1
-                binv32[(size_t)(f1 * B + f2) * N + n] = (float)(si[f1] * inv[f1][f2] * si[f2]);
-                out[f1 * B + f2] = (float)(s[f1] * a[f1][f2] * s[f2]);
+                binv32[(size_t)(f1 * B + f2) * N + n] = inv[f1][f2];
+                out[f1 * B + f2] = sas[f1][f2];
             }
         const int b0 = nbr_ptr[n];
         store_block32<B>(blk, blk16, b0 + self_rank(nbr, b0, nbr_ptr[n + 1], n), out);
@@ -850,6 +929,7 @@ template <int DIM>
 __global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const int* __restrict__ pair_node,
                                                     const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
                                                     const int* __restrict__ ne_ptr, const int* __restrict__ ne_elem,
+                                                    const int* __restrict__ ne_slot,
                                                     const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
                                                     EdPlanes ed, const uint8_t* __restrict__ flags,
                                                     const int* __restrict__ row_ptr, double* __restrict__ val,
@@ -885,7 +965,7 @@ __global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const i
 #pragma unroll
         for (int jj = 0; jj < NPE; ++jj)
             if (__ldg(conn + (size_t)jj * E + e) == mm) j = jj;
-        if (j >= 0) pair_item_df<DIM>(ed, e, ne_loc[q], j, rho, inv_dt, l_sum, k, acc);
+        if (j >= 0) pair_item_df<DIM>(ed, ne_slot[q], ne_loc[q], j, rho, inv_dt, l_sum, k, acc);
     }
     double out[NPE][NPE];
 #pragma unroll
@@ -893,6 +973,37 @@ __global__ void __launch_bounds__(BLOCK) k_mx_pairs(int P, int N, int E, const i
 #pragma unroll
         for (int b = 0; b < NPE; ++b) out[a][b] = df_to(acc[a][b]);
     pspg_write_block<DIM>(n, mm, N, deg, rank, fn, flags[mm], row_ptr, out, true, vbc, nullptr, val, nullptr);
+}
+
+// FP64 inverses of the diagonal blocks of the FP64 CSR values (block-Jacobi of the FP64
+// correction solves), for the instances k_mx_pairs just assembled: identity rows (free nodes,
+// velocity rows of bound nodes) hold their single diagonal entry.
+template <int DIM>
+__global__ void k_mx_binv64(int N, const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
+                            const int* __restrict__ row_ptr, const double* __restrict__ val,
+                            const uint8_t* __restrict__ flags, Mx m, double* __restrict__ binv) {
+    constexpr int B = DIM + 1;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const int* ii = m.ii + m.node_inst[n] * I_COUNT;
+    if (!ii[I_ACTIVE] || ii[I_MODE] != MODE_FP64 || ii[I_M64]) return;
+    const uint8_t fl = flags[n];
+    const int b0 = nbr_ptr[n], deg = nbr_ptr[n + 1] - b0;
+    const int rank = self_rank(nbr, b0, nbr_ptr[n + 1], n);
+    double a[B][B], inv[B][B];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1) {
+        const bool single = (fl & F_FREE) || ((fl & F_BOUND) && f1 < DIM);
+        const int rp = row_ptr[n + (size_t)f1 * N];
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2)
+            a[f1][f2] = single ? (f1 == f2 ? val[rp] : 0.0) : val[rp + f2 * deg + rank];
+    }
+    block_inverse<B>(a, inv);
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) binv[(size_t)(f1 * B + f2) * N + n] = inv[f1][f2];
 }
 
 __global__ void k_mx_mark_csr64(int n_inst, Mx m) {
@@ -1517,39 +1628,40 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     Mx m = mx_ptrs(c);
     const EdPlanes ed = ed_planes(c);
     const bool dfa = c->prm.assembly == PFG_ASM_DOUBLE_FLOAT;
+    DF* tdf = k.bq.T ? ptr<DF>(c->mx_tdf) : nullptr;
+    float4* vsum = ptr<float4>(c->mx_vsum);
+    prof_begin(c, PH_PSPG_ELEM);
+    k_mx_vprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->q_prev), k.bq.T, m,
+                                                               ptr<DF>(c->mx_vpdf), tdf);
     if (E > 0) {
-        prof_begin(c, PH_PSPG_ELEM);
         if (c->prm.tau0 > 0) {  // Bingham viscosity from the iterate's strain rates: FP64 element prep
-            k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos),
-                                                                      q_iter, m, k.refSize, visc_args(c),
-                                                                      const_cast<float*>(ed.h), const_cast<float*>(ed.l),
-                                                                      const_cast<float*>(ed.ah));
+            k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
+                E, N, ptr<int>(c->conn), ptr<double>(c->pos), q_iter, m, k.refSize, visc_args(c),
+                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf),
+                vsum, ptr<int>(c->el_slot));
         } else {
             k_mx_gprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->pos), q_iter, m,
                                                                        ptr<DF>(c->mx_gdf));
             k_mx_prep_df<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
                 E, N, ptr<int>(c->conn), ptr<DF>(c->mx_gdf), ptr<float>(c->mx_f32), m, k.ref_df, k.inv_pi_df,
-                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah));
+                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf),
+                vsum, ptr<int>(c->el_slot));
         }
-        prof_end(c, PH_PSPG_ELEM);
-        PFG_CHECK_LAUNCH(c);
     }
+    prof_end(c, PH_PSPG_ELEM);
+    PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_RHS);
     const FstArgs fa = fst_args(c);
     if (fa.nodes)
         k_fst<DIM, double><<<div_up(fa.n_nodes, BLOCK), BLOCK, 0, c->stream>>>(
             fa, E, ptr<int>(c->conn), PosF64{ptr<double>(c->pos), N}, N, ptr<double>(c->fst_force));
-    DF* tdf = k.bq.T ? ptr<DF>(c->mx_tdf) : nullptr;
-    k_mx_vprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->q_prev), k.bq.T, m,
-                                                               ptr<DF>(c->mx_vpdf), tdf);
     uint16_t* v16 = c->n_mg > 0 ? ptr<uint16_t>(c->val16) : nullptr;
     auto node_kernel = dfa ? k_mx_node<DIM, true> : k_mx_node<DIM, false>;
     node_kernel<<<c->n_seg, NB, 0, c->stream>>>(
-        m, N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ed,
-        ptr<uint8_t>(c->flags), ptr<DF>(c->mx_vpdf), tdf, ptr<double>(c->q_prev), ptr<double>(c->vbc),
+        m, N, E, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<int>(c->ne_slot), ptr<uint8_t>(c->ne_loc),
+        ptr<int>(c->conn), ed, ptr<uint8_t>(c->flags), ptr<DF>(c->mx_vpdf), vsum, tdf, ptr<double>(c->q_prev), ptr<double>(c->vbc),
         fst_force<double>(c), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<float>(c->mx_f32), k, ptr<double>(c->rhs),
-        ptr<double>(c->mx_scale), ptr<float>(c->mx_scale32), ptr<double>(c->binv), ptr<float>(c->binv32),
-        ptr<float>(c->val32), v16);
+        ptr<double>(c->mx_scale), ptr<float>(c->mx_scale32), ptr<float>(c->binv32), ptr<float>(c->val32), v16);
     prof_end(c, PH_PSPG_RHS);
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);
@@ -1576,8 +1688,12 @@ int mx_csr64(pfg_ctx* c, const MxConst& k) {
     prof_begin(c, PH_PSPG_PAIRS);
     k_mx_pairs<DIM><<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
         c->P, c->N, c->E, ptr<int>(c->pair_node), ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(c->ne_ptr),
-        ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ed_planes(c), ptr<uint8_t>(c->flags),
+        ptr<int>(c->ne_elem), ptr<int>(c->ne_slot), ptr<uint8_t>(c->ne_loc), ptr<int>(c->conn), ed_planes(c),
+        ptr<uint8_t>(c->flags),
         ptr<int>(c->row_ptr), ptr<double>(c->val), ptr<double>(c->vbc), ptr<float>(c->mx_f32), m, k);
+    k_mx_binv64<DIM><<<div_up(c->N, BLOCK), BLOCK, 0, c->stream>>>(c->N, ptr<int>(c->nbr_ptr), ptr<int>(c->nbr),
+                                                                   ptr<int>(c->row_ptr), ptr<double>(c->val),
+                                                                   ptr<uint8_t>(c->flags), m, ptr<double>(c->binv));
     k_mx_mark_csr64<<<div_up(c->n_inst, BLOCK), BLOCK, 0, c->stream>>>(c->n_inst, m);
     prof_end(c, PH_PSPG_PAIRS);
     PFG_CHECK_LAUNCH(c);
@@ -1996,6 +2112,7 @@ int mx_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->mx_tdf, sizeof(DF) * (c->prm.boussinesq ? N : 1))) ||
         (rc = ensure(c, c->mx_rec, 32 * npe * E)) ||
         (rc = ensure(c, c->mx_ed_aos, sizeof(float) * 2 * ED_AOS * E)) ||
+        (rc = ensure(c, c->mx_vsum, 2 * sizeof(float4) * E)) ||
         (rc = ensure(c, c->kv32, sizeof(float) * W_COUNT * R)) || (rc = ensure(c, c->mx_scale, sizeof(double) * R)) ||
         (rc = ensure(c, c->binv32, sizeof(float) * (size_t)(c->dim + 1) * (c->dim + 1) * N)) ||
         (rc = ensure(c, c->mx_cnt, 64)) || (rc = ensure(c, c->node_inst, sizeof(int) * N)))

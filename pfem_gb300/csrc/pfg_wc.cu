@@ -46,7 +46,24 @@ struct WcConst {
     double S;          // sum_i s_i
     double refSize;
     double mu_sum;     // sum_g mu w_g (getK factor)
+    // problem "BoussinesqWC" (MomEquation.inl:36-51, 105-130): body-force factor
+    // rho_g (1 - alpha (T_g - Tr)) and, with phase change, the Carman-Kozeny factor
+    // C (1 - fl_g)^2 / (fl_g^3 + eps) at the element Gauss points; CFL diffusion
+    // max(mu, k / cv) / rho (Solver.cpp:215-219)
+    int bq, ck, ng;
+    double alpha, t_ref, k_cv, ck_c, ck_eps, tm, dtm;
+    double gN[4][4], gw[4];
 };
+
+// Liquid fraction of MomEqWCompNewton::m_getFl (MomEquation.inl:377-381): the cubic smoothstep
+// over the melting range (Tm - DT/2, Tm + DT/2), 1 above it.
+__device__ __forceinline__ double fl_wc(const WcConst& k, double T) {
+    const double d3 = k.dtm * k.dtm * k.dtm;
+    return static_cast<double>(T > k.tm - k.dtm / 2) * static_cast<double>(T < k.tm + k.dtm / 2) *
+               (-2 / d3 * T * T * T + 6 * k.tm / d3 * T * T + (3 / (2 * k.dtm) - 6 * k.tm * k.tm / d3) * T +
+                (0.5 - 1.5 * k.tm / k.dtm + 2 * k.tm * k.tm * k.tm / d3)) +
+           static_cast<double>(T > k.tm + k.dtm / 2);
+}
 
 WcConst make_const(pfg_ctx* c) {
     const GaussConst gc = gauss_const(c->dim);
@@ -68,6 +85,20 @@ WcConst make_const(pfg_ctx* c) {
     k.refSize = gc.refSize;
     k.mu_sum = 0;
     for (int q = 0; q < gc.n; ++q) k.mu_sum += c->prm.mu * gc.w[q];
+    k.bq = c->prm.boussinesq != 0;
+    k.ck = k.bq && c->prm.heat_phase_change != 0;
+    k.ng = gc.n;
+    for (int q = 0; q < 4; ++q) {
+        k.gw[q] = gc.w[q];
+        for (int i = 0; i < 4; ++i) k.gN[q][i] = gc.N[q][i];
+    }
+    k.alpha = c->prm.alpha_t;
+    k.t_ref = c->prm.t_ref;
+    k.k_cv = k.bq ? c->prm.heat_k / c->prm.heat_cv : 0.0;
+    k.ck_c = c->prm.ck_c;
+    k.ck_eps = c->prm.ck_eps;
+    k.tm = c->prm.heat_tm;
+    k.dtm = c->prm.heat_dt_melt;
     return k;
 }
 
@@ -242,10 +273,14 @@ __global__ void k_wc_cont_node(int N, const int* __restrict__ ne_ptr, const int*
 //   MLrho_i = |e| sum_j MM_ij rho_j                      (diagBlock + lump of the rho-mass)
 //   Fs_fi   = -(K v)_fi + A_fi sum_j s_j (p_j - p_i) + MLrho_i g_f
 //   W_fi    = A_fi                                       (FP64; times p_i S at the node)
+//   BoussinesqWC (T != null): the body force |e| sum_g w_g N_i rho_g (1 - alpha (T_g - Tr)) g_f,
+//   and with phase change minus the Carman-Kozeny |e| sum_g w_g N_i ck_g v_f(g)
+//   (diagBlock(getM) V, MomEquation.inl:271-276)
 template <int DIM, class R>
 __global__ void __launch_bounds__(BLOCK) k_wc_mom_elem(int E, int N, const int* __restrict__ conn,
                                                        const double* __restrict__ pos, const double* __restrict__ s,
-                                                       WcConst k, R* __restrict__ elr, double* __restrict__ eld) {
+                                                       WcConst k, R* __restrict__ elr, double* __restrict__ eld,
+                                                       const double* __restrict__ T) {
     using L = ElLayout<DIM>;
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -286,6 +321,34 @@ __global__ void __launch_bounds__(BLOCK) k_wc_mom_elem(int E, int N, const int* 
     // K v with Ddev = [4/3 -2/3; -2/3 4/3] (normal) and 1 (shear), MomEquation.inl:63-83:
     //   (K v)_{f1,i} = mu_sum/|e| [ sum_j (A_i.A_j) v_f1(j) + sum_f2 A_f2,i Lg[f2][f1] - 2/3 A_f1,i divA ]
     const R kf = (R)(k.mu_sum / ae);
+    double fbq[NPE] = {}, ckv[DIM][NPE] = {};
+    if (T) {
+        double te[NPE];
+#pragma unroll
+        for (int a = 0; a < NPE; ++a) te[a] = T[nd[a]];
+        for (int q = 0; q < k.ng; ++q) {
+            double Tg = 0, rg = 0, vg[DIM] = {};
+#pragma unroll
+            for (int a = 0; a < NPE; ++a) {
+                Tg += k.gN[q][a] * te[a];
+                rg += k.gN[q][a] * (double)Rh[a];
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) vg[f] += k.gN[q][a] * (double)V[f][a];
+            }
+            const double fg = rg * (1 - k.alpha * (Tg - k.t_ref));
+            double ckg = 0;
+            if (k.ck) {
+                const double fl = fl_wc(k, Tg);
+                ckg = k.ck_c * (1 - fl) * (1 - fl) / (fl * fl * fl + k.ck_eps);
+            }
+#pragma unroll
+            for (int i = 0; i < NPE; ++i) {
+                fbq[i] += (fg * k.gN[q][i]) * k.gw[q];
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) ckv[f][i] += (ckg * k.gN[q][i] * vg[f]) * k.gw[q];
+            }
+        }
+    }
     R* out = elr + (size_t)e * L::NR;
     double* outd = eld + (size_t)e * L::ND;
 #pragma unroll
@@ -314,7 +377,11 @@ __global__ void __launch_bounds__(BLOCK) k_wc_mom_elem(int E, int N, const int* 
 #pragma unroll
             for (int f2 = 0; f2 < DIM; ++f2) kv += A[f2][i] * Lg[f2][f1];
             kv -= (R)(2.0 / 3.0) * A[f1][i] * divA;
-            out[L::FS + f1 * NPE + i] = -kf * kv + A[f1][i] * dp + mlr * (R)k.g[f1];
+            if (T)
+                out[L::FS + f1 * NPE + i] = -kf * kv + A[f1][i] * dp + (R)(ae * fbq[i]) * (R)k.g[f1] -
+                                            (R)(ae * ckv[f1][i]);
+            else
+                out[L::FS + f1 * NPE + i] = -kf * kv + A[f1][i] * dp + mlr * (R)k.g[f1];
             outd[f1 * NPE + i] = Ad[f1][i];
         }
     }
@@ -378,7 +445,7 @@ __global__ void k_wc_mom_node(int N, const int* __restrict__ ne_ptr, const int* 
         const double p = s[(size_t)DIM * N + n], rho = s[(size_t)(DIM + 1) * N + n];
         const double c2 = (k.K0 + k.K0p * p) / rho;
         nodal[n] = (R)fmax(u2, c2);
-        nodal[(size_t)N + n] = (R)(k.mu / rho);
+        nodal[(size_t)N + n] = (R)(fmax(k.mu, k.k_cv) / rho);
     }
 }
 
@@ -461,7 +528,7 @@ __global__ void k_wc_nodal(int N, int dim, const double* __restrict__ s, WcConst
     for (int f = 0; f < dim; ++f) u2 += s[(size_t)f * N + n] * s[(size_t)f * N + n];
     const double p = s[(size_t)dim * N + n], rho = s[(size_t)(dim + 1) * N + n];
     nodal[n] = (R)fmax(u2, (k.K0 + k.K0p * p) / rho);
-    nodal[(size_t)N + n] = (R)(k.mu / rho);
+    nodal[(size_t)N + n] = (R)(fmax(k.mu, k.k_cv) / rho);
 }
 
 template <int DIM>
@@ -518,6 +585,10 @@ int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
     prof_begin(c, PH_WC_PREDICT);
     k_wc_predict<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<uint8_t>(c->flags), s, ptr<double>(c->pos), tdt);
     prof_end(c, PH_WC_PREDICT);
+    if (k.bq) {  // BoussinesqWC: the heat step between the prediction and the continuity equation
+        int rc = wc_heat_launch(c, tdt);
+        if (rc) return rc;
+    }
     if (E > 0) {
         prof_begin(c, PH_WC_CONT_ELEM);
         k_wc_cont_elem<DIM, R><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, tdt, k,
@@ -531,7 +602,7 @@ int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
     if (E > 0) {
         prof_begin(c, PH_WC_MOM_ELEM);
         k_wc_mom_elem<DIM, R><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, k, elr,
-                                                           eld);
+                                                           eld, k.bq ? ptr<double>(c->heat_t) : nullptr);
         prof_end(c, PH_WC_MOM_ELEM);
     }
     prof_begin(c, PH_WC_MOM_NODE);
@@ -682,6 +753,12 @@ int wc_get_states(pfg_ctx* c, double* h) {
 
 int wc_enqueue(pfg_ctx* c, double dt, int nsteps) {
     const bool adapt = !(dt > 0);
+    if (c->prm.boussinesq) {
+        bool changed = false;
+        int rc = wc_heat_prepare(c, &changed);
+        if (rc) return rc;
+        if (changed) wc_release_graphs(c);
+    }
     if (!adapt) {
         k_set_dt<<<1, 1, 0, c->stream>>>(ptr<double>(c->wc_dt), dt, c->n_wc_inst);
         PFG_CHECK_LAUNCH(c);
