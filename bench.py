@@ -795,12 +795,25 @@ def run_gpu_incomp(args):
     # The bench does not remesh (the remesh is host work outside the path), and without it the
     # thinnest 3D elements invert after a few steps (the Picard step then fails, as the
     # reference's would): every timed step starts from the state after the warm-up steps.
+    tuning = {}
+
     def run(precision, clocks=None):
         ctx = make(precision)
         ext = torch.cuda.ExternalStream(ctx.stream)
         for _ in range(Wm):
             ctx.picard_step(dt)
         x_w, q_w = ctx.get_positions(), ctx.get_states()
+        if precision == api.PREC_MIXED:  # launch shapes for this device and mesh size
+            from pfem_gb300 import tune
+
+            def restore():
+                ctx.set_positions(x_w)
+                ctx.set_states(q_w)
+
+            choice, src = tune.autotune(ctx, d, N, torch.cuda.get_device_name(local), lambda: ctx.picard_step(dt),
+                                        restore)
+            tuning.update(choice)
+            tuning["source"] = src
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
         stats = {"converged": 0, "picard_iterations": 0, "krylov_iterations": 0}
         torch.cuda.synchronize()
@@ -975,6 +988,7 @@ def run_gpu_incomp(args):
             "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": int(round(sum(v[1] for k, v in phases.items() if k != "Krylov SpMV") / Kp * K)),
             "err_vs_fp64": acc_vs_fp64, "err_vs_other_form": acc_vs_other, "err_vs_oracle": acc_vs_oracle,
+            "tuning": tuning or None,
         }
         print(json.dumps(out))
     return 0
@@ -1171,6 +1185,17 @@ def run_gpu_batch(args):
     ext = torch.cuda.ExternalStream(ctx.stream)
     for _ in range(Wm):
         ctx.picard_step_batch(dt)
+    from pfem_gb300 import tune
+
+    x_t, q_t = ctx.get_positions(), ctx.get_states()
+
+    def restore():
+        ctx.set_positions(x_t)
+        ctx.set_states(q_t)
+
+    tuning, tsrc = tune.autotune(ctx, 2, Ntot, torch.cuda.get_device_name(local), lambda: ctx.picard_step_batch(dt),
+                                 restore)
+    tuning = dict(tuning, source=tsrc)
     clocks = ClockSampler(local)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     conv = 0
@@ -1320,6 +1345,7 @@ def run_gpu_batch(args):
             "e2e": {"value": n * Ke / e2e_s, "unit": cfg["unit"], "h2d_bytes_per_step": (R + 2 * Ntot) * 8,
                     "d2h_bytes_per_step": R * 8},
             "gpu_launches": int(round(sum(v[1] for k, v in phases.items() if k != "Krylov SpMV") * K)),
+            "tuning": tuning,
         }
         print(json.dumps(out))
     if world > 1:

@@ -392,6 +392,23 @@ PFG_API int pfg_heat_set_flux(pfg_ctx* ctx, const double* q_gp);
  * temperatures are unchanged.  st->krylov_iterations and st->residual report the solve. */
 PFG_API int pfg_heat_step(pfg_ctx* ctx, double dt, pfg_step_status* st);
 
+/* ---- Launch tuning of the mixed incompressible form ---------------------------------------
+ * Launch shapes of the kernels whose best shape depends on the mesh and the device: lanes per
+ * node of the Krylov SpMV (node_lanes / 2, node_lanes or 2 node_lanes, node_lanes = 4 in 2D
+ * and 8 in 3D), threads per block of the pair assembly (k_mx_asm32: 64, 128 or 256) and of
+ * the element prep (64, 128 or 256), and of the refinement residual's element kernel (32 or
+ * 64).  A zero field keeps the current value.  Results do not depend on the launch shape
+ * except through the order of the SpMV's lane sums.  pfem_gb300.tune sweeps these through a
+ * step from a saved state and caches the choice per device, dimension and mesh size. */
+typedef struct pfg_tuning {
+    int32_t spmv_lanes;
+    int32_t pair_block;
+    int32_t elem_block;
+    int32_t res_block;
+} pfg_tuning;
+PFG_API int pfg_set_tuning(pfg_ctx* ctx, const pfg_tuning* t);
+PFG_API int pfg_get_tuning(pfg_ctx* ctx, pfg_tuning* t);
+
 /* Node pairs ((d+1)^2 blocks) read by the timed Krylov SpMV launches (phase 12) since the last
  * reset: the algorithmic work of those launches in a batch whose converged instances drop out
  * of the products (mixed precision; the plain FP64 form reports 0). */

@@ -41,7 +41,7 @@ EXPORTED = (
     "pfg_get_stream", "pfg_wc_next_dt_noalloc", "pfg_set_instances", "pfg_picard_step_batch", "pfg_device_bytes",
     "pfg_upload_facets", "pfg_set_positions", "pfg_get_spmv_pairs", "pfg_set_temperature",
     "pfg_get_temperature", "pfg_heat_set_bc", "pfg_heat_set_flux", "pfg_heat_step", "pfg_upload_mesh_remap",
-    "pfg_wc_step_batch",
+    "pfg_wc_step_batch", "pfg_set_tuning", "pfg_get_tuning",
 )
 NUM_PHASES = 17
 
@@ -77,6 +77,12 @@ class StepStatus(C.Structure):
     _fields_ = [("converged", C.c_int32), ("picard_iterations", C.c_int32), ("krylov_iterations", C.c_int32),
                 ("steps_done", C.c_int32), ("residual", C.c_double), ("dt", C.c_double), ("time", C.c_double),
                 ("fp64_solves", C.c_int32), ("pad0", C.c_int32)]
+
+
+class Tuning(C.Structure):
+    """pfg_tuning: launch shapes of the tunable mixed-form kernels (0 = keep)."""
+    _fields_ = [("spmv_lanes", C.c_int32), ("pair_block", C.c_int32), ("elem_block", C.c_int32),
+                ("res_block", C.c_int32)]
 
 
 class PfgError(RuntimeError):
@@ -126,6 +132,8 @@ def load(path=LIB_PATH):
         "pfg_get_phase_times": ([vp, dp, i64p], C.c_int),
         "pfg_reset_phase_times": ([vp], C.c_int),
         "pfg_get_spmv_pairs": ([vp, i64p], C.c_int),
+        "pfg_set_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
+        "pfg_get_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
         "pfg_set_temperature": ([vp, dp], C.c_int),
         "pfg_upload_mesh_remap": ([vp, C.c_int32, dp, u8p, C.c_int32, ip, ip, C.c_int32], C.c_int),
         "pfg_get_temperature": ([vp, dp], C.c_int),
@@ -421,6 +429,15 @@ class Context:
         self._check(self.L.pfg_get_phase_times(self.h, _dp(ms), n.ctypes.data_as(C.POINTER(C.c_int64))),
                     "pfg_get_phase_times")
         return {self.L.pfg_phase_name(i).decode(): (float(ms[i]), int(n[i])) for i in range(NUM_PHASES) if n[i]}
+
+    def set_tuning(self, spmv_lanes=0, pair_block=0, elem_block=0, res_block=0):
+        t = Tuning(spmv_lanes, pair_block, elem_block, res_block)
+        self._check(self.L.pfg_set_tuning(self.h, C.byref(t)), "pfg_set_tuning")
+
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self.L.pfg_get_tuning(self.h, C.byref(t)), "pfg_get_tuning")
+        return {k: int(getattr(t, k)) for k, _ in Tuning._fields_}
 
     def spmv_pairs(self):
         """Node pairs read by the timed Krylov SpMV launches since the last reset."""

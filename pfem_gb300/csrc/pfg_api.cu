@@ -214,6 +214,44 @@ PFG_API int pfg_get_phase_times(pfg_ctx* c, double* ms, int64_t* launches) {
     return PFG_OK;
 }
 
+PFG_API int pfg_set_tuning(pfg_ctx* c, const pfg_tuning* t) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!t) return fail(c, PFG_ERR_INVALID, "null tuning");
+    pfg_tuning n = c->tune;
+    const int lanes0 = c->dim == 2 ? 4 : 8;
+    if (t->spmv_lanes) {
+        if (t->spmv_lanes != lanes0 / 2 && t->spmv_lanes != lanes0 && t->spmv_lanes != 2 * lanes0)
+            return fail(c, PFG_ERR_INVALID, "spmv_lanes must be %d, %d or %d", lanes0 / 2, lanes0, 2 * lanes0);
+        n.spmv_lanes = t->spmv_lanes;
+    }
+    auto block_ok = [](int b) { return b == 64 || b == 128 || b == 256; };
+    if (t->pair_block) {
+        if (!block_ok(t->pair_block)) return fail(c, PFG_ERR_INVALID, "pair_block must be 64, 128 or 256");
+        n.pair_block = t->pair_block;
+    }
+    if (t->elem_block) {
+        if (!block_ok(t->elem_block)) return fail(c, PFG_ERR_INVALID, "elem_block must be 64, 128 or 256");
+        n.elem_block = t->elem_block;
+    }
+    if (t->res_block) {
+        if (t->res_block != 32 && t->res_block != 64) return fail(c, PFG_ERR_INVALID, "res_block must be 32 or 64");
+        n.res_block = t->res_block;
+    }
+    c->tune = n;
+    if (c->prm.kind == PFG_KIND_INCOMP_PSPG && c->prm.precision == PFG_PREC_MIXED && c->has_mesh)
+        mx_release_graph(c);  // the captured Krylov chunks hold the previous launch shapes
+    return PFG_OK;
+}
+
+PFG_API int pfg_get_tuning(pfg_ctx* c, pfg_tuning* t) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!t) return fail(c, PFG_ERR_INVALID, "null tuning");
+    *t = c->tune;
+    return PFG_OK;
+}
+
 PFG_API int pfg_get_spmv_pairs(pfg_ctx* c, int64_t* pairs) {
     int rc = check_ctx(c);
     if (rc) return rc;
@@ -298,6 +336,7 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     c->prm = *params;
     c->dim = params->dim;
     c->npe = params->dim + 1;
+    c->tune = pfg_tuning{params->dim == 2 ? 4 : 8, BLOCK, BLOCK, 64};
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64 * sizeof(double));

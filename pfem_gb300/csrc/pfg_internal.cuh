@@ -75,6 +75,7 @@ struct LuFront {
 
 struct pfg_ctx {
     pfg_params prm{};
+    pfg_tuning tune{};  // launch shapes of the tunable mixed-form kernels (pfg_set_tuning)
     int dim = 0, npe = 0;
     int N = 0, E = 0;
     int R = 0;          // incompressible unknowns (dim+1)*N

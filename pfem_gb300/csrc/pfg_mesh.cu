@@ -182,18 +182,26 @@ __device__ __forceinline__ int nbr_rank(const int* __restrict__ nbr, int b0, int
 // touches sit in a compact range of slots and the node and pair kernels' gathers hit L2.
 // FILL = false counts, per node, the elements whose smallest node it is; FILL = true numbers
 // them from the node's scanned base in its ascending incidence order.
+// An element whose node list repeats its smallest node is numbered once, at the first of
+// those local positions.
 template <bool FILL>
 __global__ void k_elem_slots(int N, int npe, int E, const int* __restrict__ conn, const int* __restrict__ ne_ptr,
-                             const int* __restrict__ ne_elem, int* __restrict__ count, const int* __restrict__ base,
-                             int* __restrict__ el_slot) {
+                             const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
+                             int* __restrict__ count, const int* __restrict__ base, int* __restrict__ el_slot) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     int k = FILL ? base[n] : 0;
     for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
         const int e = ne_elem[q];
-        int mn = conn[e];
-        for (int j = 1; j < npe; ++j) mn = min(mn, conn[(size_t)j * E + e]);
-        if (mn != n) continue;
+        int mn = conn[e], jm = 0;
+        for (int j = 1; j < npe; ++j) {
+            const int v = conn[(size_t)j * E + e];
+            if (v < mn) {
+                mn = v;
+                jm = j;
+            }
+        }
+        if (mn != n || ne_loc[q] != jm) continue;
         if (FILL) el_slot[e] = k;
         ++k;
     }
@@ -398,13 +406,13 @@ int build_topology(pfg_ctx* c) {
         TRY(ensure(c, c->el_slot, sizeof(int) * (size_t)std::max(E, 1)));
         TRY(ensure(c, c->ne_slot, sizeof(int) * std::max<long long>(inc, 1)));
         k_elem_slots<false><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
-                                                                   ptr<int>(c->ne_elem), ptr<int>(cnt), nullptr,
-                                                                   nullptr);
+                                                                   ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
+                                                                   ptr<int>(cnt), nullptr, nullptr);
         PFG_CHECK_LAUNCH(c);
         TRY(scan_exclusive(c, ptr<int>(cnt), ptr<int>(fill), N, tmp));
         k_elem_slots<true><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
-                                                                  ptr<int>(c->ne_elem), nullptr, ptr<int>(fill),
-                                                                  ptr<int>(c->el_slot));
+                                                                  ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
+                                                                  nullptr, ptr<int>(fill), ptr<int>(c->el_slot));
         PFG_CHECK_LAUNCH(c);
         if (inc > 0) {
             k_ne_slots<<<div_up(inc, BLOCK), BLOCK, 0, c->stream>>>(inc, ptr<int>(c->ne_elem), ptr<int>(c->el_slot),

@@ -1411,8 +1411,8 @@ __device__ __forceinline__ void node_rows_f64(int n, bool act, int N, const int*
 // walks n's neighbours once (one index and d+1 input values per neighbour) and accumulates
 // all d+1 rows.  One pass: NB x GN threads per segment.  FP32 reads the node-pair blocks of
 // the scaled system, FP64 the field-major CSR of A.
-template <class T, int DIM, int MODE>
-__global__ void __launch_bounds__(NB * node_lanes<DIM>()) k_mx_spmv(Mx m, const int* __restrict__ list,
+template <class T, int DIM, int MODE, int GN>
+__global__ void __launch_bounds__(NB * GN) k_mx_spmv(Mx m, const int* __restrict__ list,
                                                                   T* __restrict__ scb, int cnt_slot, int N,
                                                                   const int* __restrict__ rp,
                                                                   const int* __restrict__ nbr_ptr,
@@ -1420,7 +1420,6 @@ __global__ void __launch_bounds__(NB * node_lanes<DIM>()) k_mx_spmv(Mx m, const 
                                                                   const T* __restrict__ val, T* __restrict__ W,
                                                                   size_t ld) {
     constexpr int B = DIM + 1;
-    constexpr int GN = node_lanes<DIM>();
     constexpr int NT = NB * GN;
     __shared__ double sh[32];
     const int b = list ? list[blockIdx.x] : blockIdx.x;  // segment
@@ -1635,14 +1634,14 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
                                                                ptr<DF>(c->mx_vpdf), tdf);
     if (E > 0) {
         if (c->prm.tau0 > 0) {  // Bingham viscosity from the iterate's strain rates: FP64 element prep
-            k_mx_prep<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
+            k_mx_prep<DIM><<<div_up(E, c->tune.elem_block), c->tune.elem_block, 0, c->stream>>>(
                 E, N, ptr<int>(c->conn), ptr<double>(c->pos), q_iter, m, k.refSize, visc_args(c),
                 const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf),
                 vsum, ptr<int>(c->el_slot));
         } else {
             k_mx_gprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->pos), q_iter, m,
                                                                        ptr<DF>(c->mx_gdf));
-            k_mx_prep_df<DIM><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(
+            k_mx_prep_df<DIM><<<div_up(E, c->tune.elem_block), c->tune.elem_block, 0, c->stream>>>(
                 E, N, ptr<int>(c->conn), ptr<DF>(c->mx_gdf), ptr<float>(c->mx_f32), m, k.ref_df, k.inv_pi_df,
                 const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf),
                 vsum, ptr<int>(c->el_slot));
@@ -1666,7 +1665,7 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);
     auto pair_kernel = dfa ? k_mx_asm32<DIM, true> : k_mx_asm32<DIM, false>;
-    pair_kernel<<<div_up(c->P, BLOCK), BLOCK, 0, c->stream>>>(
+    pair_kernel<<<div_up(c->P, c->tune.pair_block), c->tune.pair_block, 0, c->stream>>>(
         c->P, N, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->pe_ptr), ptr<int>(c->pe_item), ed,
         ptr<uint8_t>(c->flags), ptr<float>(c->mx_scale32), ptr<float>(c->mx_f32), m, k, ptr<float>(c->val32), v16);
     prof_end(c, PH_PSPG_PAIRS);
@@ -1709,7 +1708,7 @@ int mx_residual(pfg_ctx* c, const MxConst& k, int kind, Counters* cnt) {
     k_mx_xdf<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->q), ptr<double>(c->vbc),
                                                              ptr<uint8_t>(c->flags), m, ptr<DF>(c->mx_xdf));
     if (E > 0)
-        k_mx_res_elem<DIM><<<div_up(E, RES_ELEM_BLOCK), RES_ELEM_BLOCK, 0, c->stream>>>(
+        k_mx_res_elem<DIM><<<div_up(E, c->tune.res_block), c->tune.res_block, 0, c->stream>>>(
             E, N, ptr<int>(c->conn), ed_planes(c), ptr<uint8_t>(c->flags), ptr<DF>(c->mx_xdf), ptr<float>(c->mx_f32),
             m, k, ptr<float4>(c->mx_rec));
     k_mx_res_node<DIM><<<c->n_seg, NB, 0, c->stream>>>(
@@ -1804,8 +1803,17 @@ struct KSet {
             prof_begin(c, PH_KRYLOV_SPMV);
             if (c->prof) c->spmv_pairs += c->spmv_list_pairs;
         }
-        k_mx_spmv<T, DIM, MODE><<<grid, NB * node_lanes<DIM>(), 0, c->stream>>>(m, list, scb, slot, N, rp, nptr, nbr,
-                                                                              val, W, ld);
+        // lanes per node: the tuned choice (node_lanes<DIM>() by default)
+        const int gn = c->tune.spmv_lanes;
+        if (gn == node_lanes<DIM>() / 2)
+            k_mx_spmv<T, DIM, MODE, node_lanes<DIM>() / 2><<<grid, NB * gn, 0, c->stream>>>(m, list, scb, slot, N, rp,
+                                                                                          nptr, nbr, val, W, ld);
+        else if (gn == 2 * node_lanes<DIM>())
+            k_mx_spmv<T, DIM, MODE, 2 * node_lanes<DIM>()><<<grid, NB * gn, 0, c->stream>>>(m, list, scb, slot, N, rp,
+                                                                                          nptr, nbr, val, W, ld);
+        else
+            k_mx_spmv<T, DIM, MODE, node_lanes<DIM>()><<<grid, NB * node_lanes<DIM>(), 0, c->stream>>>(
+                m, list, scb, slot, N, rp, nptr, nbr, val, W, ld);
         if (F32) prof_end(c, PH_KRYLOV_SPMV);
     }
 

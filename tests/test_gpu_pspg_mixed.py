@@ -274,3 +274,53 @@ def test_double_float_assembly_matches_oracle(gpu_lib, which, c1_mesh, small3d_m
     qo, res = O.pspg_picard_step(om, q0, 1e-3, g=gravity(d))
     assert st.converged == 1 and st.picard_iterations == res.iterations
     assert max(field_errs(ctx.get_states(), qo, d, N)) < 1e-8
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_launch_shapes_keep_the_solution(gpu_lib, which, c1_mesh, small3d_mesh):
+    """Every tunable launch shape (pfg_set_tuning) gives the oracle's solution: only the order
+    of the SpMV's lane sums changes, and the refinement stops on the same FP64 residual test."""
+    mesh = c1_mesh if which == "c1" else small3d_mesh
+    d, N = mesh.dim, mesh.n_nodes
+    column = (1.0, 2.0) if d == 2 else (0.2, 0.3, 0.3)
+    q0 = M.incomp_initial_states(mesh, column=column)
+    om = O.OracleMesh(mesh)
+    qo, _ = O.pspg_picard_step(om, q0.copy(), 1e-3, g=gravity(d))
+    l0 = 4 if d == 2 else 8
+    for shape in (dict(spmv_lanes=l0 // 2, pair_block=64, elem_block=64, res_block=32),
+                  dict(spmv_lanes=2 * l0, pair_block=128, elem_block=128, res_block=64)):
+        ctx = make_ctx(mesh)
+        ctx.set_states(q0)
+        ctx.set_tuning(**shape)
+        assert ctx.get_tuning() == shape
+        st = ctx.picard_step(1e-3)
+        assert st.converged == 1
+        assert max(field_errs(ctx.get_states(), qo, d, N)) < 1e-8, shape
+    with pytest.raises(api.PfgError):
+        ctx.set_tuning(spmv_lanes=3)
+    with pytest.raises(api.PfgError):
+        ctx.set_tuning(pair_block=96)
+
+
+def test_autotune_applies_and_caches(gpu_lib, c1_mesh, tmp_path):
+    from pfem_gb300 import tune
+
+    mesh = c1_mesh
+    q0 = M.incomp_initial_states(mesh)
+    ctx = make_ctx(mesh)
+    ctx.set_states(q0)
+    x0 = ctx.get_positions()
+    path = str(tmp_path / "tune.json")
+
+    def restore():
+        ctx.set_positions(x0)
+        ctx.set_states(q0)
+
+    choice, src = tune.autotune(ctx, 2, mesh.n_nodes, "test-device", lambda: ctx.picard_step(1e-3), restore,
+                                path=path)
+    assert src == "measured"
+    assert ctx.get_tuning() == {k: choice[k] for k in tune.PHASE}
+    assert all(choice["us"][k] for k in ("spmv_lanes", "pair_block", "elem_block", "res_block"))
+    ctx2 = make_ctx(mesh)
+    choice2, src2 = tune.autotune(ctx2, 2, mesh.n_nodes, "test-device", lambda: None, lambda: None, path=path)
+    assert src2 == "cache" and ctx2.get_tuning() == ctx.get_tuning()
