@@ -103,10 +103,11 @@ struct pfg_ctx {
     // CSR system
     pfg::DBuf row_ptr, col, val, val32, diag_pos, rhs;
     int64_t nnz = 0;
-    // element data [detJ, tau, gradN, ksum] (structure of arrays): FP64, and in the mixed form
-    // double-float as two FP32 planes (high parts, then low parts).  Both are overwritten by the
-    // heat assembly (k_heat_geom stores the heat layout in them): every reader's own assembly
-    // rewrites them first, so no reader may carry them across a heat step.
+    // element data of the plain FP64 form [detJ, tau, gradN, ksum] (structure of arrays), and a
+    // double-float copy used by the heat assembly alone.  edata is overwritten by the heat
+    // assembly (k_heat_geom stores the heat layout in it): every reader's own assembly rewrites
+    // it first, so no reader may carry it across a heat step.  The mixed form keeps its element
+    // data in mx_ed_aos, which no other assembly writes.
     pfg::DBuf edata, edata_df;
     // incompressible states
     pfg::DBuf q, q_prev, q_iter_prev, vbc;

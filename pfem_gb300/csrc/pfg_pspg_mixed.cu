@@ -125,10 +125,12 @@ MxConst mx_const(pfg_ctx* c) {
     k.ref32 = (float)g.refSize;
     const int npe = c->dim + 1;
     const double m0 = g.MM[0][1], s0 = g.s[0];
+    // (the reference's 3D Gauss points carry 15 digits, so its tables have this structure to
+    // ~1e-15 relative: the regrouped sums differ from the table sums by that much)
     k.p1 = m0 > 0 && s0 > 0;
     for (int i = 0; i < npe; ++i) {
-        k.p1 = k.p1 && std::fabs(g.s[i] - s0) <= 1e-15 * s0;
-        for (int j = 0; j < npe; ++j) k.p1 = k.p1 && std::fabs(g.MM[i][j] - (i == j ? 2.0 : 1.0) * m0) <= 1e-15 * m0;
+        k.p1 = k.p1 && std::fabs(g.s[i] - s0) <= 1e-12 * s0;
+        for (int j = 0; j < npe; ++j) k.p1 = k.p1 && std::fabs(g.MM[i][j] - (i == j ? 2.0 : 1.0) * m0) <= 1e-12 * m0;
     }
     k.m0_df = split(m0);
     k.rtol = c->prm.krylov_rel_tol;
@@ -215,47 +217,32 @@ __device__ __forceinline__ DF inst_df(const float* f32, int inst, int which) {
     return DF{f32[inst * F_COUNT + which], f32[inst * F_COUNT + which + 1]};
 }
 
-// Element data as double-float planes: value v of element e is h[v E + e] + l[v E + e] (the
-// element kernels' coalesced layout), and the same values element-major at the element's slot
-// s (elements ordered by their smallest node): the 16 high parts in ah[16 s ..], the low parts
-// in al[16 s ..], so a kernel that gathers an element reads two 32-byte sectors of high parts
-// (FP32 arithmetic), plus two of low parts (double-float), instead of one sector per value, and
-// the elements of consecutive nodes share sectors and L2 lines.  High and low parts are kept
-// apart so that the FP32 gathers' L2 footprint is the high parts alone; gdf/gf take the slot.
+// Element data, double-float, element-major at the element's slot s (elements ordered by their
+// smallest node): the 16 high parts in ah[16 s ..], the low parts in al[16 s ..], so a kernel
+// that gathers an element reads two 32-byte sectors of high parts (FP32 arithmetic), plus two
+// of low parts (double-float), and the elements of consecutive nodes share sectors and L2
+// lines.  High and low parts are kept apart so that the FP32 gathers' L2 footprint is the high
+// parts alone.
 constexpr int ED_AOS = 16;
 struct EdPlanes {
-    const float* h;
-    const float* l;
     const float* ah;
     const float* al;
     int E;
-    __device__ __forceinline__ DF df(int v, int e) const {
-        const size_t o = (size_t)v * E + e;
-        return DF{__ldg(h + o), __ldg(l + o)};
+    __device__ __forceinline__ DF gdf(int v, int s) const {
+        return DF{__ldg(ah + (size_t)s * ED_AOS + v), __ldg(al + (size_t)s * ED_AOS + v)};
     }
-    __device__ __forceinline__ float f(int v, int e) const { return __ldg(h + (size_t)v * E + e); }
-    __device__ __forceinline__ DF gdf(int v, int e) const {
-        return DF{__ldg(ah + (size_t)e * ED_AOS + v), __ldg(al + (size_t)e * ED_AOS + v)};
-    }
-    __device__ __forceinline__ float gf(int v, int e) const { return __ldg(ah + (size_t)e * ED_AOS + v); }
+    __device__ __forceinline__ float gf(int v, int s) const { return __ldg(ah + (size_t)s * ED_AOS + v); }
 };
 
-// Stores element e's values v (high and low parts) in both layouts, the element-major record
-// at the element's slot.
+// Stores element e's values v (high and low parts) element-major at the element's slot.
 template <int NV>
-__device__ __forceinline__ void ed_store(float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea, int E,
-                                         int e, int slot, const DF (&v)[NV]) {
+__device__ __forceinline__ void ed_store(float* __restrict__ ea, int E, int slot, const DF (&v)[NV]) {
     static_assert(NV <= ED_AOS, "element record holds 16 values");
     float rh[ED_AOS], rl[ED_AOS];
 #pragma unroll
     for (int k = 0; k < ED_AOS; ++k) {
         rh[k] = k < NV ? v[k < NV ? k : 0].h : 0.0f;
         rl[k] = k < NV ? v[k < NV ? k : 0].l : 0.0f;
-    }
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        eh[(size_t)k * E + e] = v[k].h;
-        el[(size_t)k * E + e] = v[k].l;
     }
     float4* dh = reinterpret_cast<float4*>(ea + (size_t)slot * ED_AOS);
     float4* dl = reinterpret_cast<float4*>(ea + (size_t)E * ED_AOS + (size_t)slot * ED_AOS);
@@ -292,8 +279,8 @@ __device__ __forceinline__ void elem_vsum(const DF* __restrict__ vp, int N, cons
 template <int DIM>
 __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const double* __restrict__ pos,
                           const double* __restrict__ q_iter, Mx m, double refSize, ViscArgs va,
-                          float* __restrict__ eh, float* __restrict__ el, float* __restrict__ ea,
-                          const DF* __restrict__ vp, float4* __restrict__ vsum, const int* __restrict__ el_slot) {
+                          float* __restrict__ ea, const DF* __restrict__ vp, float4* __restrict__ vsum,
+                          const int* __restrict__ el_slot) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int nd[DIM + 1];
@@ -334,7 +321,7 @@ __global__ void k_mx_prep(int E, int N, const int* __restrict__ conn, const doub
     DF dv[ed_count<DIM>()];
 #pragma unroll
     for (int k = 0; k < ed_count<DIM>(); ++k) dv[k] = df_from(v[k]);
-    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, slot, dv);
+    ed_store<ed_count<DIM>()>(ea, E, slot, dv);
 }
 
 // Double-float copies of the positions and the iterate's velocities (inputs of k_mx_prep_df).
@@ -357,9 +344,8 @@ __global__ void k_mx_gprep(int N, const double* __restrict__ pos, const double* 
 // error-free or double-float one, so the element data agree with the FP64 ones to ~1e-14.
 template <int DIM>
 __global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const DF* __restrict__ gdf,
-                             const float* __restrict__ f32, Mx m, DF ref_df, DF inv_pi, float* __restrict__ eh,
-                             float* __restrict__ el, float* __restrict__ ea, const DF* __restrict__ vp,
-                             float4* __restrict__ vsum, const int* __restrict__ el_slot) {
+                             const float* __restrict__ f32, Mx m, DF ref_df, DF inv_pi, float* __restrict__ ea,
+                             const DF* __restrict__ vp, float4* __restrict__ vsum, const int* __restrict__ el_slot) {
     constexpr int NPE = DIM + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -443,7 +429,7 @@ __global__ void k_mx_prep_df(int E, int N, const int* __restrict__ conn, const D
 #pragma unroll
         for (int i = 0; i < NPE; ++i) dv[2 + f * NPE + i] = G[f][i];
     dv[ed_ksum<DIM>()] = inst_df(f32, inst, F_KSUM);
-    ed_store<ed_count<DIM>()>(eh, el, ea, E, e, slot, dv);
+    ed_store<ed_count<DIM>()>(ea, E, slot, dv);
 }
 
 // Double-float copies of the previous velocities and (Boussinesq) the temperatures.
@@ -1045,6 +1031,7 @@ constexpr int RES_ELEM_BLOCK = 64;  // ~136 registers a thread: small blocks kee
 // identity rows and get 0): record (e, i) holds d+1 double-float values, 32 bytes.
 template <int DIM>
 __global__ void __launch_bounds__(RES_ELEM_BLOCK) k_mx_res_elem(int E, int N, const int* __restrict__ conn, EdPlanes ed,
+                                                                const int* __restrict__ el_slot,
                                                                 const uint8_t* __restrict__ flags,
                                                                 const DF* __restrict__ xdf, const float* __restrict__ f32,
                                                                 Mx m, MxConst k, float4* __restrict__ rec) {
@@ -1055,16 +1042,17 @@ __global__ void __launch_bounds__(RES_ELEM_BLOCK) k_mx_res_elem(int E, int N, co
     load_nodes<DIM>(conn, E, e, nd);
     const int inst = m.node_inst[nd[0]];
     if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    const int es = el_slot[e];  // the element-major data are stored by slot
     const DF inv_dt = inst_df(f32, inst, F_INVDT), l_sum = inst_df(f32, inst, F_LSUM);
     const DF cm = inst_df(f32, inst, F_CM);
-    const DF ae = df_mul(ed.df(0, e), k.ref_df);
-    const DF tau = ed.df(1, e);
-    const DF kf = df_mul(ae, ed.df(ed_ksum<DIM>(), e));
+    const DF ae = df_mul(ed.gdf(0, es), k.ref_df);
+    const DF tau = ed.gdf(1, es);
+    const DF kf = df_mul(ae, ed.gdf(ed_ksum<DIM>(), es));
     DF G[DIM][NPE];
 #pragma unroll
     for (int f = 0; f < DIM; ++f)
 #pragma unroll
-        for (int j = 0; j < NPE; ++j) G[f][j] = ed.df(2 + f * NPE + j, e);
+        for (int j = 0; j < NPE; ++j) G[f][j] = ed.gdf(2 + f * NPE + j, es);
     DF u[NPE][DIM], p[NPE];
 #pragma unroll
     for (int j = 0; j < NPE; ++j) {
@@ -1613,10 +1601,8 @@ double ksum_newtonian(int dim, double mu) {
 }
 
 EdPlanes ed_planes(pfg_ctx* c) {
-    const int ned = c->dim == 2 ? ed_count<2>() : ed_count<3>();
-    float* h = ptr<float>(c->edata_df);
     float* a = ptr<float>(c->mx_ed_aos);
-    return EdPlanes{h, h + (size_t)ned * c->E, a, a + (size_t)ED_AOS * c->E, c->E};
+    return EdPlanes{a, a + (size_t)ED_AOS * c->E, c->E};
 }
 
 // A, b at the iterate q_iter: element data, node blocks and right-hand side, FP32 pair blocks
@@ -1636,15 +1622,13 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
         if (c->prm.tau0 > 0) {  // Bingham viscosity from the iterate's strain rates: FP64 element prep
             k_mx_prep<DIM><<<div_up(E, c->tune.elem_block), c->tune.elem_block, 0, c->stream>>>(
                 E, N, ptr<int>(c->conn), ptr<double>(c->pos), q_iter, m, k.refSize, visc_args(c),
-                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf),
-                vsum, ptr<int>(c->el_slot));
+                const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf), vsum, ptr<int>(c->el_slot));
         } else {
             k_mx_gprep<DIM><<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, ptr<double>(c->pos), q_iter, m,
                                                                        ptr<DF>(c->mx_gdf));
             k_mx_prep_df<DIM><<<div_up(E, c->tune.elem_block), c->tune.elem_block, 0, c->stream>>>(
                 E, N, ptr<int>(c->conn), ptr<DF>(c->mx_gdf), ptr<float>(c->mx_f32), m, k.ref_df, k.inv_pi_df,
-                const_cast<float*>(ed.h), const_cast<float*>(ed.l), const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf),
-                vsum, ptr<int>(c->el_slot));
+                const_cast<float*>(ed.ah), ptr<DF>(c->mx_vpdf), vsum, ptr<int>(c->el_slot));
         }
     }
     prof_end(c, PH_PSPG_ELEM);
@@ -1709,7 +1693,8 @@ int mx_residual(pfg_ctx* c, const MxConst& k, int kind, Counters* cnt) {
                                                              ptr<uint8_t>(c->flags), m, ptr<DF>(c->mx_xdf));
     if (E > 0)
         k_mx_res_elem<DIM><<<div_up(E, c->tune.res_block), c->tune.res_block, 0, c->stream>>>(
-            E, N, ptr<int>(c->conn), ed_planes(c), ptr<uint8_t>(c->flags), ptr<DF>(c->mx_xdf), ptr<float>(c->mx_f32),
+            E, N, ptr<int>(c->conn), ed_planes(c), ptr<int>(c->el_slot), ptr<uint8_t>(c->flags), ptr<DF>(c->mx_xdf),
+            ptr<float>(c->mx_f32),
             m, k, ptr<float4>(c->mx_rec));
     k_mx_res_node<DIM><<<c->n_seg, NB, 0, c->stream>>>(
         m, N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<float4>(c->mx_rec),
@@ -2109,11 +2094,9 @@ int mx_picard(pfg_ctx* c, const double* dts, pfg_step_status* st) {
 
 int mx_alloc(pfg_ctx* c) {
     const size_t R = std::max(c->R, 1), N = std::max(c->N, 1), E = std::max(c->E, 1);
-    const int ned = c->dim == 2 ? ed_count<2>() : ed_count<3>();
     int rc;
     const size_t npe = c->dim + 1;
-    if ((rc = ensure(c, c->edata_df, sizeof(DF) * ned * E)) ||
-        (rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))) ||
+    if ((rc = ensure(c, c->val32, sizeof(float) * (size_t)std::max(c->P, 1) * (c->dim + 1) * (c->dim + 1))) ||
         (rc = ensure(c, c->mx_scale32, sizeof(float) * R)) || (rc = ensure(c, c->mx_xdf, sizeof(DF) * R)) ||
         (rc = ensure(c, c->mx_vpdf, sizeof(DF) * (size_t)c->dim * N)) ||
         (rc = ensure(c, c->mx_gdf, sizeof(DF) * 2 * (size_t)c->dim * N)) ||

@@ -69,7 +69,7 @@ def test_boussinesq_wc_matches_oracle(gpu_lib, which, name, c1_mesh, small3d_mes
     if q is not None:
         ctx.heat_set_flux(q.ravel())
     om = O.OracleMesh(mesh)
-    po = O.wc_params()
+    po = O.wc_params(g=tuple(p.gravity[:d]))
     bq = O.wc_bq_params(ALPHA, TR, K, CV, h=kw.get("heat_h", 0.0), t_inf=kw.get("heat_t_inf", 0.0),
                         eps_rad=kw.get("heat_eps_rad", 0.0), fs_flags=fs, phase_change=PHASE if pc else None)
     so = np.concatenate([s0, T0])
