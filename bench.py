@@ -564,6 +564,9 @@ def incomp_params(api, dim, precision, workload, mu=1e-3):
     if workload == "incomp-c3":
         p.krylov_rel_tol = WL.C3_MIXED_TOL if precision == api.PREC_MIXED else WL.C3_TOL
         p.krylov_abs_tol = 0.0
+    elif workload == "batch-c4":
+        p.krylov_rel_tol, p.krylov_abs_tol = WL.C4_TOL, 0.0
+        p.krylov_max_iter = max(p.krylov_max_iter, 20000)
     return p
 
 
@@ -1328,6 +1331,7 @@ def run_gpu_batch(args):
                        "elements_rank0": int(U.n_elems),
                        "unknowns": R, "nnz": nnz, "dt": dt, "host_meshing_s": mesh_s,
                        "precision": "mixed (FP32 assembly + FP32 BiCGSTAB, double-float refinement residual)",
+                       "linear_tolerance": f"||r|| <= {WL.C4_TOL:g} ||b|| (FP64 residual), both forms",
                        "l2": "working set > L2 (129 MB)",
                        "parallelism": "one batched launch sequence" if world == 1 else
                        f"instances sharded over {world} ranks by node count and memory (no collective)"},

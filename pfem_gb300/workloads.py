@@ -29,6 +29,9 @@ SEED = 20261203
 # 1.6e-4 away).  Its inner FP32 solves are unchanged.
 C3_TOL = 1e-8
 C3_MIXED_TOL = 1e-10
+# C4: both forms solve to relative residual 1e-12 with no absolute floor (the reference's direct
+# solver's accuracy; the default absolute floor 1e-10 is loose for the small instances' ||b||)
+C4_TOL = 1e-12
 C3_DT = 5e-4
 C3_COLUMN = (0.5, 0.5, 1.0)
 
