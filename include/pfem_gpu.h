@@ -173,6 +173,17 @@ typedef struct pfg_params {
        max(mu / rho, k / (cv rho)).  The temperatures are pfg_set_temperature's.              */
     double ck_c;               /* Carman-Kozeny constant C                                 */
     double ck_eps;             /* Carman-Kozeny eps                                        */
+    /* incompressible, solver "FracStep" (MomContEquationFracStep.inl:7-630; plain FP64 form,
+       residual PFG_RES_U or PFG_RES_U_P): per Picard iteration the velocity prediction
+       (M/dt + K) v~ = F + M/dt v_prev + gamma_fs D^T p_prev, the pressure L p = -(rho/dt) D v~
+       + gamma_fs L p_prev and the correction M dv = dt D^T (p - gamma_fs p_prev), each an SPD
+       system solved by Jacobi CG to the Krylov tolerances.  As written in the reference, L is
+       singular (free-surface nodes keep their Laplacian rows with a zero right-hand side): the
+       smallest free-surface node of each connected group of elements (else its smallest node)
+       is pinned to p = 0; fs_pressure_dirichlet = 1 pins every free-surface node instead.      */
+    double gamma_fs;           /* gammaFS in [0, 1]                                        */
+    int32_t frac_step;         /* 1: fractional step instead of PSPG                       */
+    int32_t fs_pressure_dirichlet;
 } pfg_params;
 
 /* Heat boundary-condition flags per node (the reference's tag flags of HeatEq's BC table,

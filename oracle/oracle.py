@@ -66,6 +66,11 @@ class WcParams(C.Structure):
                 ("gamma", C.c_double)]
 
 
+class FsParams(C.Structure):
+    _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double), ("gammaFS", C.c_double),
+                ("g", C.c_double * 3), ("gamma", C.c_double)]
+
+
 class WcBqParams(C.Structure):
     """Problem "BoussinesqWC": momentum and heat material of WCompNewton (MomEquation.inl:36-51,
     HeatEquation.inl:26-45)."""
@@ -109,6 +114,11 @@ def lib():
         L.orc_wc_step.argtypes = [vp, C.POINTER(WcParams), C.c_double, dp, dp]
         L.orc_wc_next_dt.restype = C.c_double
         L.orc_wc_next_dt.argtypes = [vp, C.POINTER(WcParams), dp]
+        L.orc_fs_build.argtypes = [vp, C.POINTER(FsParams), dp, dp, dp, u8p]
+        L.orc_fs_pressure_rhs.argtypes = [vp, C.POINTER(FsParams), dp, dp, u8p]
+        L.orc_fs_velocity_rhs.argtypes = [vp, C.POINTER(FsParams), dp]
+        L.orc_fs_get.restype = C.c_int
+        L.orc_fs_get.argtypes = [vp, C.c_int, ip, ip, dp, dp]
         L.orc_wc_bq_step.argtypes = [vp, C.POINTER(WcParams), C.POINTER(WcBqParams), C.c_double, dp, dp, u8p, dp, dp]
         L.orc_wc_bq_next_dt.restype = C.c_double
         L.orc_wc_bq_next_dt.argtypes = [vp, C.POINTER(WcParams), C.POINTER(WcBqParams), dp]
@@ -331,6 +341,137 @@ def pspg_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), vbc=No
     res.converged = True
     res.iterations = it
     return q_iter, res
+
+
+def fs_gauge(mesh):
+    """Pressure gauge nodes of the fractional step: in every connected group of elements (two
+    elements are connected when they share a node) its smallest free-surface node, or its
+    smallest node when it has none."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import connected_components
+
+    N, E, npe = mesh.n_nodes, mesh.n_elems, mesh.dim + 1
+    conn = np.asarray(mesh.conn)
+    gauge = np.zeros(N, np.uint8)
+    if E == 0:
+        return gauge
+    rows = np.repeat(conn[0], npe - 1)
+    cols = conn[1:].T.ravel()
+    adj = sp.csr_matrix((np.ones(rows.size), (rows, cols)), shape=(N, N))
+    _, lab = connected_components(adj, directed=False)
+    used = np.zeros(N, bool)
+    used[conn.ravel()] = True
+    fs = (np.asarray(mesh.flags) & 2) != 0
+    best = {}
+    for n in np.flatnonzero(used):
+        c = lab[n]
+        key = (0 if fs[n] else 1, n)
+        if c not in best or key < best[c]:
+            best[c] = key
+    for _, n in best.values():
+        gauge[n] = 1
+    return gauge
+
+
+def _fs_system(om, which, R):
+    import scipy.sparse as sp
+
+    nnz = lib().orc_fs_get(om.h, which, None, None, None, None)
+    colptr = np.empty(R + 1, np.int32)
+    rowidx = np.empty(nnz, np.int32)
+    vals = np.empty(nnz)
+    b = np.empty(R)
+    lib().orc_fs_get(om.h, which, _ip(colptr), _ip(rowidx), _dp(vals), _dp(b))
+    return sp.csc_matrix((vals, rowidx, colptr), shape=(R, R)), b
+
+
+def fracstep_picard_step(om, q_prev, dt, rho=1000.0, mu=1e-3, g=(0.0, -9.81), gamma_fs=1.0, vbc=None, max_iter=10,
+                         min_res=1e-6, residual="U", gauge=None, gamma=0.0, mesh=None):
+    """One `MomContEqIncompNewton::solve` with the fractional step (m_setupPicardFracStep,
+    MomContEquationFracStep.inl:463-630): per Picard iteration the three SparseLU solves of
+    the velocity prediction, the pressure (gauge nodes pinned, see fs_gauge) and the velocity
+    correction, then the positions from the saved ones.  residual "U" or "U_P" (the relative
+    change of the iterate over the non-free nodes; "Ax_f" is unsupported there).
+    q_prev = [v (d x N), p (N)].  Returns (q, PicardResult); on failure q_prev and the saved
+    positions."""
+    from scipy.sparse.linalg import splu
+
+    d, N = om.dim, om.N
+    res = PicardResult()
+    gg = tuple(g) + (0.0,) * (3 - len(g))
+    p = FsParams()
+    p.rho, p.mu, p.dt, p.gammaFS, p.gamma = rho, mu, dt, gamma_fs, gamma
+    for i in range(3):
+        p.g[i] = gg[i]
+    q_prev = np.asarray(q_prev, float)
+    v_prev = np.ascontiguousarray(q_prev[:d * N])
+    p_prev = np.ascontiguousarray(q_prev[d * N:(d + 1) * N])
+    if vbc is None:
+        vbc = np.zeros(d * N)
+    vbc = np.ascontiguousarray(vbc, float)
+    if gauge is None:
+        gauge = fs_gauge(mesh)
+    gauge = np.ascontiguousarray(gauge, np.uint8)
+    gp = gauge.ctypes.data_as(C.POINTER(C.c_uint8))
+    free = om.is_free()
+    om.save()
+    q_it_prev = q_prev.copy()
+    r = float("inf")
+    it = 0
+    while r > min_res:
+        if it > max_iter:
+            om.restore()
+            res.iterations = it
+            return q_prev.copy(), res
+        lib().orc_fs_build(om.h, C.byref(p), _dp(v_prev), _dp(p_prev), _dp(vbc), gp)
+        A, b = _fs_system(om, 0, d * N)
+        try:
+            v_t = splu(A, permc_spec="COLAMD").solve(b)
+        except RuntimeError:
+            om.restore()
+            res.iterations = it
+            return q_prev.copy(), res
+        lib().orc_fs_pressure_rhs(om.h, C.byref(p), _dp(np.ascontiguousarray(v_t)), _dp(p_prev), gp)
+        L, bp = _fs_system(om, 1, N)
+        try:
+            p_it = splu(L, permc_spec="COLAMD").solve(bp)
+        except RuntimeError:
+            om.restore()
+            res.iterations = it
+            return q_prev.copy(), res
+        dP = np.ascontiguousarray(p_it - gamma_fs * p_prev)
+        lib().orc_fs_velocity_rhs(om.h, C.byref(p), _dp(dP))
+        M, bv = _fs_system(om, 2, d * N)
+        try:
+            dv = splu(M, permc_spec="COLAMD").solve(bv)
+        except RuntimeError:
+            om.restore()
+            res.iterations = it
+            return q_prev.copy(), res
+        v_it = v_t + dv
+        q_it = np.concatenate([v_it, p_it])
+        om.update_from_save(v_it * dt)
+        # residual closure (:568-629)
+        nf = ~free
+        num = sum(float(np.sum((v_it[f * N:(f + 1) * N][nf] - q_it_prev[f * N:(f + 1) * N][nf]) ** 2)) for f in range(d))
+        den = sum(float(np.sum(q_it_prev[f * N:(f + 1) * N][nf] ** 2)) for f in range(d))
+        r_v = np.finfo(float).max if den == 0 else np.sqrt(num / den)
+        r_p = 0.0
+        if residual == "U_P":
+            pn = p_it[nf] - q_it_prev[d * N:][nf]
+            den_p = float(np.sum(q_it_prev[d * N:][nf] ** 2))
+            r_p = np.finfo(float).max if den_p == 0 else np.sqrt(float(np.sum(pn ** 2)) / den_p)
+        r = max(r_v, r_p)
+        res.residuals.append(r)
+        q_it_prev = q_it
+        if np.isnan(r):
+            om.restore()
+            res.iterations = it + 1
+            return q_prev.copy(), res
+        it += 1
+    res.converged = True
+    res.iterations = it
+    return q_it_prev, res
 
 
 def heat_params(rho, cv, k, h=0.0, t_inf=0.0, eps_rad=0.0, fs_flags=0, phase_change=None):

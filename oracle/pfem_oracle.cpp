@@ -189,6 +189,14 @@ struct OrcMesh {
     // assembled PSPG system, Eigen column-major (CSC) storage
     std::vector<int32_t> colptr, rowidx;
     std::vector<double> vals, b;
+    // fractional step: M (velocity correction), MK_dt (velocity prediction), L (pressure) in
+    // CSC storage with their right-hand sides, and the per-element D^T and L of the step
+    struct Csc {
+        std::vector<int32_t> colptr, rowidx;
+        std::vector<double> vals;
+    } fsM, fsMK, fsL;
+    std::vector<double> fsbV, fsbP, fsbVc;
+    std::vector<std::vector<double>> fsDT, fsLe;
 
     bool bound(int n) const { return flags[n] & BOUND; }
     bool fixed(int n) const { return flags[n] & FIXED; }
@@ -693,30 +701,38 @@ struct Triplet {
 // Eigen's SparseMatrix::setFromTriplets: duplicates are summed in triplet order, storage is
 // column-major with sorted row indices.  A stable sort by (col, row) keeps triplet order
 // inside each duplicate group, then the group is summed left to right.
+void toCsc(const std::vector<Triplet>& indexA, int R, std::vector<int32_t>& colptr, std::vector<int32_t>& rowidx,
+           std::vector<double>& vals);
+
 void setFromTriplets(OrcMesh& m, const std::vector<Triplet>& indexA, int R) {
+    toCsc(indexA, R, m.colptr, m.rowidx, m.vals);
+}
+
+void toCsc(const std::vector<Triplet>& indexA, int R, std::vector<int32_t>& colptr, std::vector<int32_t>& rowidx,
+           std::vector<double>& vals) {
     std::vector<uint32_t> order(indexA.size());
     std::iota(order.begin(), order.end(), 0u);
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
         const Triplet &ta = indexA[a], &tb = indexA[b];
         return ta.col != tb.col ? ta.col < tb.col : ta.row < tb.row;
     });
-    m.colptr.assign(R + 1, 0);
-    m.rowidx.clear();
-    m.vals.clear();
-    m.rowidx.reserve(indexA.size() / 3);
-    m.vals.reserve(indexA.size() / 3);
+    colptr.assign(R + 1, 0);
+    rowidx.clear();
+    vals.clear();
+    rowidx.reserve(indexA.size() / 3);
+    vals.reserve(indexA.size() / 3);
     for (size_t k = 0; k < order.size();) {
         const Triplet& t = indexA[order[k]];
         double s = t.val;
         size_t k2 = k + 1;
         while (k2 < order.size() && indexA[order[k2]].col == t.col && indexA[order[k2]].row == t.row)
             s += indexA[order[k2++]].val;
-        m.rowidx.push_back(t.row);
-        m.vals.push_back(s);
-        m.colptr[t.col + 1]++;
+        rowidx.push_back(t.row);
+        vals.push_back(s);
+        colptr[t.col + 1]++;
         k = k2;
     }
-    for (int c = 0; c < R; ++c) m.colptr[c + 1] += m.colptr[c];
+    for (int c = 0; c < R; ++c) colptr[c + 1] += colptr[c];
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1099,6 +1115,223 @@ void orc_facet_gauss_positions(const OrcMesh* m, double* out) {
                 out[((size_t)f * 3 + g) * dim + d] = J0 * fg.xi[g][0] + J1 * fg.xi[g][1] + m->x(a, d);
             }
     }
+}
+
+// ---------------------------------------------------------------------------------------
+// Fractional step (solver "FracStep"), IncompNewton/MomContEquationFracStep.inl:7-630.
+//
+// One Picard iteration: MK_dt v~ = bV (velocity prediction), L p = bP (pressure), M dv = bVc
+// (velocity correction), v = v~ + dv.  The pressure system of the reference is singular (L has
+// the factor 1, MomContEquation.inl:157-161; every non-free node keeps its Laplacian row and
+// free-surface nodes only lose their right-hand side, :266-300): here each connected group of
+// elements gets a gauge node (its smallest free-surface node, else its smallest node) whose row
+// and column are treated as those of a free node (:303-325), i.e. p = 0 there.
+// ---------------------------------------------------------------------------------------
+struct FsParams {
+    double rho, mu, dt, gammaFS;
+    double g[3];
+    double gamma;  // surface tension of the prediction's right-hand side (:207-243)
+};
+
+namespace {
+
+void fsColumnIdentity(OrcMesh::Csc& A, int col) {  // column col: diagonal 1, the rest 0
+    for (int k = A.colptr[col]; k < A.colptr[col + 1]; ++k) A.vals[k] = A.rowidx[k] == col ? 1.0 : 0.0;
+}
+
+}  // namespace
+
+// m_buildMatFracStep (:7-197) and m_applyBCVAppStep (:199-260) at the current positions, with
+// the previous step's velocities vPrev (d x N) and pressures pPrev (N); vbc the Dirichlet
+// velocities at t + dt; gauge[n] = 1 for the pressure gauge nodes.
+void orc_fs_build(OrcMesh* m, const FsParams* p, const double* vPrev, const double* pPrev, const double* vbc,
+                  const uint8_t* gauge) {
+    const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    const double dt = p->dt;
+    const int tM = dim * npe * npe, tMK = dim * npe * npe + dim * npe * dim * npe, tL = npe * npe;
+    std::vector<Triplet> iM((size_t)tM * E, Triplet{0, 0, 0.0}), iMK((size_t)tMK * E, Triplet{0, 0, 0.0}),
+        iL((size_t)tL * E, Triplet{0, 0, 0.0});
+    const int dbl = 3 * dim * npe;
+    std::vector<std::pair<int32_t, double>> ib((size_t)dbl * E, {0, 0.0});
+    m->fsDT.assign(E, {});
+    m->fsLe.assign(E, {});
+    auto rowSkip = [&](int n) { return m->bound(n) || m->isFree[n]; };
+    auto lSkip = [&](int n) { return m->isFree[n] || (gauge && gauge[n]); };
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        const ElemGeom& geo = m->geom[e];
+        Mat G = getGradN(dim, geo);
+        Mat B = getB(dim, G);
+        Mat Ms = getM(*m, geo, [&](int) { return p->rho; });
+        double sumMu = 0, sumL = 0;
+        for (int g = 0; g < m->gt.n; ++g) {
+            sumMu += p->mu * m->gt.w[g];
+            sumL += 1.0 * m->gt.w[g];
+        }
+        Mat K = getK(*m, geo, sumMu, B, ddevIncomp(dim));
+        Mat D = getD(*m, geo, [](int) { return 1.0; }, B);  // npe x dim*npe
+        Mat Le = getL(*m, geo, sumL, G);
+        double Fe[12];
+        getF(*m, geo, [&](int) { return p->rho; }, p->g, Fe);
+        std::vector<double>& DT = m->fsDT[e];
+        DT.assign((size_t)dim * npe * npe, 0.0);  // D^T, (dim*npe) x npe row-major
+        for (int r = 0; r < dim * npe; ++r)
+            for (int c = 0; c < npe; ++c) DT[(size_t)r * npe + c] = D(c, r);
+        std::vector<double>& LE = m->fsLe[e];
+        LE.assign((size_t)npe * npe, 0.0);
+        for (int i = 0; i < npe; ++i)
+            for (int j = 0; j < npe; ++j) LE[(size_t)i * npe + j] = Le(i, j);
+        double vP[12], pP[4];
+        for (int d = 0; d < dim; ++d)
+            for (int k = 0; k < npe; ++k) vP[d * npe + k] = vPrev[(size_t)d * N + m->node(e, k)];
+        for (int k = 0; k < npe; ++k) pP[k] = pPrev[m->node(e, k)];
+        double MvDt[12], DTp[12];
+        for (int d = 0; d < dim; ++d)
+            for (int i = 0; i < npe; ++i) {
+                double s = 0;
+                for (int j = 0; j < npe; ++j) s += (Ms(i, j) * (1 / dt)) * vP[d * npe + j];
+                MvDt[d * npe + i] = s;
+            }
+        for (int r = 0; r < dim * npe; ++r) {
+            double s = 0;
+            for (int c = 0; c < npe; ++c) s += DT[(size_t)r * npe + c] * pP[c];
+            DTp[r] = p->gammaFS * s;
+        }
+        size_t cM = 0, cMK = 0, cL = 0, cb = 0;
+        for (int i = 0; i < npe; ++i) {
+            const int ni = m->node(e, i);
+            for (int j = 0; j < npe; ++j) {
+                const int nj = m->node(e, j);
+                for (int d = 0; d < dim; ++d) {
+                    if (!rowSkip(ni)) {
+                        iM[(size_t)tM * e + cM] = Triplet{ni + d * N, nj + d * N, Ms(i, j)};
+                        iMK[(size_t)tMK * e + cMK] = Triplet{ni + d * N, nj + d * N, Ms(i, j) * (1 / dt)};
+                    }
+                    cM++;
+                    cMK++;
+                    for (int d2 = 0; d2 < dim; ++d2) {
+                        if (!rowSkip(ni))
+                            iMK[(size_t)tMK * e + cMK] = Triplet{ni + d * N, nj + d2 * N, K(i + d * npe, j + d2 * npe)};
+                        cMK++;
+                    }
+                }
+                if (!lSkip(ni)) iL[(size_t)tL * e + cL] = Triplet{ni, nj, Le(i, j)};
+                cL++;
+            }
+            for (int d = 0; d < dim; ++d)
+                if (!rowSkip(ni)) {
+                    ib[(size_t)dbl * e + cb++] = {ni + d * N, Fe[i + d * npe]};
+                    ib[(size_t)dbl * e + cb++] = {ni + d * N, MvDt[i + d * npe]};
+                    ib[(size_t)dbl * e + cb++] = {ni + d * N, DTp[i + d * npe]};
+                }
+        }
+    }
+    for (int n = 0; n < N; ++n) {
+        if (lSkip(n)) iL.push_back(Triplet{n, n, 1.0});
+        if (rowSkip(n))
+            for (int d = 0; d < dim; ++d) {
+                iMK.push_back(Triplet{n + d * N, n + d * N, 1.0});
+                iM.push_back(Triplet{n + d * N, n + d * N, 1.0});
+            }
+    }
+    toCsc(iM, dim * N, m->fsM.colptr, m->fsM.rowidx, m->fsM.vals);
+    toCsc(iMK, dim * N, m->fsMK.colptr, m->fsMK.rowidx, m->fsMK.vals);
+    toCsc(iL, N, m->fsL.colptr, m->fsL.rowidx, m->fsL.vals);
+    m->fsbV.assign((size_t)dim * N, 0.0);
+    for (const auto& d : ib) m->fsbV[d.first] += d.second;
+    // m_applyBCVAppStep: surface tension of facets with a free-surface node, then the nodes
+    addSurfaceTension(*m, p->gamma, true, m->fsbV.data());
+    for (int n = 0; n < N; ++n) {
+        if (m->isFree[n] && !m->bound(n))
+            for (int d = 0; d < dim; ++d) m->fsbV[n + (size_t)d * N] = vPrev[(size_t)d * N + n] + dt * p->g[d];
+        if (m->dirichlet(n))
+            for (int d = 0; d < dim; ++d) {
+                const int c = n + d * N;
+                const double r = vbc[(size_t)d * N + n];
+                m->fsbV[c] = r;
+                for (int k = m->fsMK.colptr[c]; k < m->fsMK.colptr[c + 1]; ++k) {
+                    if (m->fsMK.rowidx[k] == c) continue;
+                    m->fsbV[m->fsMK.rowidx[k]] -= m->fsMK.vals[k] * r;
+                    m->fsMK.vals[k] = 0;
+                }
+            }
+    }
+    // m_applyBCPCorrStep (:303-325) on L: free nodes (and the gauge nodes)
+    for (int n = 0; n < N; ++n)
+        if (lSkip(n)) fsColumnIdentity(m->fsL, n);
+    // m_applyBCVStep (:389-413) on M: free and bound nodes
+    for (int n = 0; n < N; ++n)
+        if (rowSkip(n))
+            for (int d = 0; d < dim; ++d) fsColumnIdentity(m->fsM, n + d * N);
+}
+
+// m_buildMatPcorrStep (:262-301) with m_applyBCPCorrStep's right-hand side: bP.
+void orc_fs_pressure_rhs(OrcMesh* m, const FsParams* p, const double* vTilde, const double* pPrev,
+                         const uint8_t* gauge) {
+    const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    std::vector<std::pair<int32_t, double>> ib((size_t)2 * npe * E, {0, 0.0});
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        const std::vector<double>& DT = m->fsDT[e];
+        const std::vector<double>& LE = m->fsLe[e];
+        double vt[12], pP[4];
+        for (int d = 0; d < dim; ++d)
+            for (int k = 0; k < npe; ++k) vt[d * npe + k] = vTilde[(size_t)d * N + m->node(e, k)];
+        for (int k = 0; k < npe; ++k) pP[k] = pPrev[m->node(e, k)];
+        size_t cb = 0;
+        for (int i = 0; i < npe; ++i) {
+            double dv = 0, lp = 0;
+            for (int r = 0; r < dim * npe; ++r) dv += DT[(size_t)r * npe + i] * vt[r];
+            for (int j = 0; j < npe; ++j) lp += LE[(size_t)i * npe + j] * pP[j];
+            const int ni = m->node(e, i);
+            if (!m->isFree[ni] && !(m->flags[ni] & FREE_SURFACE)) {
+                ib[(size_t)2 * npe * e + cb++] = {ni, -((p->rho / p->dt) * dv)};
+                ib[(size_t)2 * npe * e + cb++] = {ni, p->gammaFS * lp};
+            }
+        }
+    }
+    m->fsbP.assign(N, 0.0);
+    for (const auto& d : ib) m->fsbP[d.first] += d.second;
+    for (int n = 0; n < N; ++n)
+        if (m->isFree[n] || (gauge && gauge[n])) m->fsbP[n] = 0;
+}
+
+// m_buildMatVStep (:327-387) with m_applyBCVStep's right-hand side: bVc from dp = p - gammaFS p_prev.
+void orc_fs_velocity_rhs(OrcMesh* m, const FsParams* p, const double* dP) {
+    const int dim = m->dim, npe = m->npe, N = m->N, E = m->E;
+    std::vector<std::pair<int32_t, double>> ib((size_t)dim * npe * E, {0, 0.0});
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+        const std::vector<double>& DT = m->fsDT[e];
+        double dp[4];
+        for (int k = 0; k < npe; ++k) dp[k] = dP[m->node(e, k)];
+        size_t cb = 0;
+        for (int i = 0; i < npe; ++i) {
+            const int ni = m->node(e, i);
+            if (m->isFree[ni] || m->bound(ni)) continue;
+            for (int d = 0; d < dim; ++d) {
+                double s = 0;
+                for (int c = 0; c < npe; ++c) s += DT[(size_t)(i + d * npe) * npe + c] * dp[c];
+                ib[(size_t)dim * npe * e + cb++] = {ni + d * N, p->dt * s};
+            }
+        }
+    }
+    m->fsbVc.assign((size_t)dim * N, 0.0);
+    for (const auto& d : ib) m->fsbVc[d.first] += d.second;
+    for (int n = 0; n < N; ++n)
+        if (m->isFree[n] || m->bound(n))
+            for (int d = 0; d < dim; ++d) m->fsbVc[n + (size_t)d * N] = 0;
+}
+
+// which: 0 = MK_dt / bV, 1 = L / bP, 2 = M / bVc.  Returns nnz (arrays may be null).
+int orc_fs_get(const OrcMesh* m, int which, int32_t* colptr, int32_t* rowidx, double* vals, double* b) {
+    const OrcMesh::Csc& A = which == 0 ? m->fsMK : which == 1 ? m->fsL : m->fsM;
+    const std::vector<double>& rhs = which == 0 ? m->fsbV : which == 1 ? m->fsbP : m->fsbVc;
+    if (colptr) std::copy(A.colptr.begin(), A.colptr.end(), colptr);
+    if (rowidx) std::copy(A.rowidx.begin(), A.rowidx.end(), rowidx);
+    if (vals) std::copy(A.vals.begin(), A.vals.end(), vals);
+    if (b) std::copy(rhs.begin(), rhs.end(), b);
+    return (int)A.vals.size();
 }
 
 void orc_pspg_get(const OrcMesh* m, int32_t* colptr, int32_t* rowidx, double* vals, double* b) {

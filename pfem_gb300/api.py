@@ -66,6 +66,7 @@ class Params(C.Structure):
         ("heat_max_iter", C.c_int32), ("heat_residual", C.c_int32), ("heat_min_res", C.c_double),
         ("heat_phase_change", C.c_int32), ("pad3", C.c_int32), ("heat_tm", C.c_double), ("heat_dt_melt", C.c_double),
         ("heat_lm", C.c_double), ("ck_c", C.c_double), ("ck_eps", C.c_double),
+        ("gamma_fs", C.c_double), ("frac_step", C.c_int32), ("fs_pressure_dirichlet", C.c_int32),
     ]
 
 

@@ -331,6 +331,16 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     if (params->heat_residual != PFG_RES_T && params->heat_residual != PFG_RES_AX_F) return PFG_ERR_INVALID;
     if (params->heat_phase_change && !(params->heat_dt_melt > 0)) return PFG_ERR_INVALID;
     if (params->assembly != PFG_ASM_FP32 && params->assembly != PFG_ASM_DOUBLE_FLOAT) return PFG_ERR_INVALID;
+    // fractional step: the plain FP64 form of the incompressible solver, U or U_P residual
+    // (the reference throws for Ax_f, MomContEquationFracStep.inl:626-628)
+    if (params->frac_step != 0 && params->frac_step != 1) return PFG_ERR_INVALID;
+    if (params->frac_step) {
+        if (params->kind != PFG_KIND_INCOMP_PSPG || params->precision != PFG_PREC_FP64 ||
+            params->linear_solver != PFG_LINSOLVE_BICGSTAB || params->boussinesq)
+            return PFG_ERR_UNSUPPORTED;
+        if (!(params->gamma_fs >= 0 && params->gamma_fs <= 1)) return PFG_ERR_INVALID;
+        if (params->residual != PFG_RES_U && params->residual != PFG_RES_U_P) return PFG_ERR_INVALID;
+    }
     pfg_ctx* c = new (std::nothrow) pfg_ctx();
     if (!c) return PFG_ERR_NOMEM;
     c->prm = *params;
@@ -372,7 +382,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
                     &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
                     &c->pe_ptr, &c->pe_item, &c->el_slot, &c->ne_slot, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
-                    &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos, &c->mx_vsum, &c->wch_rec, &c->lu_front, &c->lu_nodes,
+                    &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos, &c->mx_vsum, &c->wch_rec, &c->fs_gauge, &c->fs_rp, &c->fs_col, &c->fs_val, &c->fs_lval, &c->fs_mval, &c->fs_vec, &c->fs_cg, &c->fs_red, &c->lu_front, &c->lu_nodes,
                     &c->lu_recs, &c->lu_kids, &c->lu_maps, &c->lu_piv, &c->lu_mat, &c->lu_vec, &c->lu_list,
                     &c->lu_r, &c->lu_one};
     wc_release_graphs(c);
@@ -432,6 +442,7 @@ PFG_API int pfg_upload_mesh(pfg_ctx* c, int32_t n_nodes, const double* pos, cons
     if ((rc = build_topology(c))) return rc;
     if (c->prm.kind == PFG_KIND_INCOMP_PSPG) {
         if ((rc = pspg_alloc(c)) || (rc = krylov_alloc(c))) return rc;
+        if (c->prm.frac_step && (rc = fs_alloc(c))) return rc;
         // heat buffers: allocated with the mesh for Boussinesq contexts (the assembly reads the
         // temperatures), else on first use of the heat API
         c->heat_ready = false;
@@ -773,6 +784,7 @@ PFG_API int pfg_picard_step(pfg_ctx* c, double dt, pfg_step_status* st) {
         if (c->n_inst != 1) return fail(c, PFG_ERR_STATE, "context holds %d instances: use pfg_picard_step_batch", c->n_inst);
         return mx_picard_step(c, &dt, st);
     }
+    if (c->prm.frac_step) return fs_picard_step(c, dt, st);
     return picard_step(c, dt, st);
 }
 

@@ -412,6 +412,7 @@ __global__ void __launch_bounds__(BLOCK) k_heat_rhs(int N, int E, const int* __r
 
 enum : int { S_GAMMA = 0, S_ALPHA, S_BETA, S_RR, S_TOL2, S_DONE, S_ITERS, S_BB, S_NUM, S_DEN, S_FIRST, S_COUNT };
 enum : int { V_R = 0, V_Z, V_P, V_S, V_W, V_DIAG, V_COUNT };  // V_DIAG holds the inverse diagonal
+static_assert(V_COUNT == CG_VECTORS, "cg_solve's work vectors");
 
 struct CgPtrs {
     double* partials;  // 3 * max_grid
@@ -949,6 +950,41 @@ int heat_build_facets(pfg_ctx* c) {
 
 int heat_step(pfg_ctx* c, double dt, pfg_step_status* st) {
     return c->dim == 2 ? heat_dim<2>(c, dt, st) : heat_dim<3>(c, dt, st);
+}
+
+// Jacobi-preconditioned CG (the Chronopoulos-Gear kernels above) on a scalar CSR system of n
+// rows (rp, col, val; the diagonal among each row's entries), right-hand side b, from the guess
+// in x (overwritten), to ||r|| <= max(rtol ||b||, atol) or max_it iterations.  V holds
+// CG_VECTORS x n work values, red 3 max_grid + 64 partial sums and scalars.
+int cg_solve(pfg_ctx* c, int n, const int* rp, const int* col, const double* val, const double* b, double* x,
+             double* V, double* red, double rtol, double atol, int max_it, int* iters, bool* ok) {
+    CgPtrs kp;
+    kp.partials = red;
+    kp.sc = red + 3 * (size_t)c->max_grid;
+    kp.ticket = reinterpret_cast<unsigned*>(kp.sc + 32);
+    const size_t ld = (size_t)std::max(n, 1);
+    const int grid = std::max(1, std::min(c->max_grid, div_up(n, BLOCK)));
+    max_it = std::max(1, max_it);
+    k_cg_init<<<grid, BLOCK, 0, c->stream>>>(n, rp, col, val, b, x, V, ld, kp, rtol, atol, INFINITY);
+    k_cg_spmv<1><<<grid, BLOCK, 0, c->stream>>>(n, rp, col, val, V, ld, kp, max_it);
+    PFG_CHECK_LAUNCH(c);
+    double* h = c->h_scalars;
+    int done_it = 0;
+    while (done_it < max_it) {
+        const int m = std::min(8, max_it - done_it);
+        for (int it = 0; it < m; ++it) {
+            k_cg_update<<<grid, BLOCK, 0, c->stream>>>(n, x, V, ld, kp);
+            k_cg_spmv<1><<<grid, BLOCK, 0, c->stream>>>(n, rp, col, val, V, ld, kp, max_it);
+        }
+        PFG_CHECK_LAUNCH(c);
+        done_it += m;
+        PFG_CUDA(c, cudaMemcpyAsync(h, kp.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (h[S_DONE] != 0.0) break;
+    }
+    *ok = h[S_DONE] == 1.0;
+    *iters = (int)h[S_ITERS];
+    return PFG_OK;
 }
 
 // Host work before a BoussinesqWC step is launched or captured: heat buffers, the element

@@ -186,6 +186,9 @@ struct pfg_ctx {
     pfg::DBuf heat_t, heat_flags, heat_tbc, heat_val, heat_rhs, heat_cg, heat_red;
     pfg::DBuf hf_ptr, hf_ent, hf_fflags, heat_q;
     pfg::DBuf wch_rec;  // BoussinesqWC heat step: per element node lumped mass and right-hand side
+    // fractional step: gauge nodes, the velocity matrix (CSR), L and M (node-pair layout), work
+    // vectors, CG vectors and partial sums
+    pfg::DBuf fs_gauge, fs_rp, fs_col, fs_val, fs_lval, fs_mval, fs_vec, fs_cg, fs_red;
     bool heat_ready = false;  // heat buffers allocated (and zeroed) for the current mesh
     bool has_heat_bc = false, has_heat_q = false;
     bool heat_facets_dirty = true;  // the per-node heat facet lists need rebuilding
@@ -262,6 +265,10 @@ void upload_constants(int dim);
 // ---- PSPG (pfg_pspg.cu) --------------------------------------------------------------
 int pspg_alloc(pfg_ctx* c);
 int pspg_assemble(pfg_ctx* c, double dt, const double* d_qiter, const double* d_qprev, bool apply_bc);
+int pspg_elem_prep(pfg_ctx* c, double dt, const double* d_qiter);
+// ---- fractional step (pfg_fracstep.cu) ----
+int fs_alloc(pfg_ctx* c);
+int fs_picard_step(pfg_ctx* c, double dt, pfg_step_status* st);
 int pspg_update_positions(pfg_ctx* c, double dt, const double* d_q);
 int pspg_residual(pfg_ctx* c, const double* d_q, double* res_out);
 int picard_step(pfg_ctx* c, double dt, pfg_step_status* st);
@@ -286,6 +293,9 @@ int heat_alloc(pfg_ctx* c);
 int heat_build_facets(pfg_ctx* c);
 int heat_step(pfg_ctx* c, double dt, pfg_step_status* st);
 int wc_heat_prepare(pfg_ctx* c, bool* changed);
+constexpr int CG_VECTORS = 6;  // work vectors of cg_solve
+int cg_solve(pfg_ctx* c, int n, const int* rp, const int* col, const double* val, const double* b, double* x,
+             double* V, double* red, double rtol, double atol, int max_it, int* iters, bool* ok);
 int wc_heat_launch(pfg_ctx* c, const double* tdt);
 int mx_set_instances(pfg_ctx* c, int n_inst, const int* node_off, const double* rho, const double* mu);
 int mx_picard_step(pfg_ctx* c, const double* dts, pfg_step_status* st);

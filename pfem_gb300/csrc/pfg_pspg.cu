@@ -254,6 +254,26 @@ int pspg_alloc(pfg_ctx* c) {
     return PFG_OK;
 }
 
+// Element data [detJ, tau, gradN, ksum] of the current positions into edata (the fractional
+// step uses detJ, gradN and ksum).
+int pspg_elem_prep(pfg_ctx* c, double dt, const double* d_qiter) {
+    const int N = c->N, E = c->E;
+    if (E == 0) return PFG_OK;
+    const GaussConst g = gauss_const(c->dim);
+    prof_begin(c, PH_PSPG_ELEM);
+    if (c->dim == 2)
+        k_elem_prep<2><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), d_qiter,
+                                                                  c->prm.rho, c->prm.mu, dt, g.refSize, visc_args(c),
+                                                                  ptr<double>(c->edata));
+    else
+        k_elem_prep<3><<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), d_qiter,
+                                                                  c->prm.rho, c->prm.mu, dt, g.refSize, visc_args(c),
+                                                                  ptr<double>(c->edata));
+    prof_end(c, PH_PSPG_ELEM);
+    PFG_CHECK_LAUNCH(c);
+    return PFG_OK;
+}
+
 int pspg_assemble(pfg_ctx* c, double dt, const double* d_qiter, const double* d_qprev, bool apply_bc) {
     return c->dim == 2 ? assemble_dim<2>(c, dt, d_qiter, d_qprev, apply_bc)
                        : assemble_dim<3>(c, dt, d_qiter, d_qprev, apply_bc);
