@@ -1369,11 +1369,12 @@ def run_gpu_batch(args):
 
 
 def c5_requests(n, rate, seed=20261203):
-    """The served mix: Poisson arrivals at `rate`; 80% 2D dam breaks (1k-20k fluid nodes,
-    column aspect 0.5-2), 20% 3D (10k-50k fluid nodes; the 200k upper end is cut to keep a
-    bench run within minutes); weakly compressible or incompressible at even odds; mu
-    log-uniform in [1e-3, 1e-1]; WC requests 50-500 explicit steps, incompressible ones 10-50
-    Picard steps in 2D and 5-20 in 3D."""
+    """The served mix: Poisson arrivals at `rate`; 80% 2D (half dam breaks with 1k-20k fluid
+    nodes and column aspect 0.5-2, half sloshing tanks of `examples/2D/sloshing` with
+    h = 0.01-0.03 and its material: rho = 1, mu = 0.01, K0 = 2.2e5, K0' = 7.6), 20% 3D dam
+    breaks with 10k-200k fluid nodes; weakly compressible or incompressible at even odds; dam
+    break mu log-uniform in [1e-3, 1e-1]; WC requests 50-500 explicit steps, incompressible
+    ones 10-50 Picard steps in 2D and 5-20 in 3D."""
     import math
 
     import numpy as np
@@ -1388,12 +1389,28 @@ def c5_requests(n, rate, seed=20261203):
         is3d = rng.random() < 0.2
         wc = rng.random() < 0.5
         mu = math.exp(rng.uniform(math.log(1e-3), math.log(1e-1)))
+        sloshing = (not is3d) and rng.random() < 0.5
+        params, case = None, "dam break"
         if is3d:
-            nf = math.exp(rng.uniform(math.log(1e4), math.log(5e4)))
+            nf = math.exp(rng.uniform(math.log(1e4), math.log(2e5)))
             col = (0.5, 0.5, 1.0)
             h = (0.25 / nf) ** (1 / 3)
             m = M.dam_break_3d(h, seed=seed + i)
             steps = int(rng.integers(50, 501)) if wc else int(rng.integers(5, 21))
+        elif sloshing:
+            h = math.exp(rng.uniform(math.log(0.01), math.log(0.03)))
+            m = M.sloshing_2d(h, seed=seed + i)
+            steps = int(rng.integers(50, 501)) if wc else int(rng.integers(10, 51))
+            kind = api.KIND_WC_CDS_DPDT if wc else api.KIND_INCOMP_PSPG
+            if wc:
+                st = M.sloshing_wc_initial_states(m)
+                params = dict(rho_star=1.0, K0=2.2e5, K0p=7.6, security_coeff=0.1, max_dt=0.1)
+            else:
+                st = np.zeros(3 * m.n_nodes)
+                params = dict(rho=1.0)
+            out.append(SV.Request(kind, m, st, steps, dt=1e-2, mu=0.01, arrival=t, rid=i, params=params,
+                                  case="sloshing"))
+            continue
         else:
             nf = math.exp(rng.uniform(math.log(1e3), math.log(2e4)))
             a = rng.uniform(0.5, 2.0)
@@ -1438,16 +1455,21 @@ def run_gpu_serve(args):
             "metric": "aggregate time-steps/s of a served request mix (C5), with p50/p99 request latency",
             "value": m["steps_per_s"], "unit": "steps/s", "n_gpus": world, "steps": steps, "warmup": 0,
             "ms_per_step": 1e3 * srv.makespan / max(steps, 1), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "mixed", "data": "synthetic (seeded dam breaks, Poisson arrivals)",
+            "vs_baseline": None, "dtype": "mixed",
+            "data": "synthetic (seeded dam breaks and sloshing tanks, Poisson arrivals)",
             "config": {"workload": "served mix (C5)", "requests": args.requests, "rate_per_s": args.rate,
                        "hbm_budget_bytes": budget, "slots": 8, "host_meshing_s": mesh_s,
                        "kinds": {"wc": sum(r.kind == 1 for r in out), "incomp": sum(r.kind == 0 for r in out)},
-                       "dims": {"2d": sum(r.mesh.dim == 2 for r in out), "3d": sum(r.mesh.dim == 3 for r in out)}},
+                       "dims": {"2d": sum(r.mesh.dim == 2 for r in out), "3d": sum(r.mesh.dim == 3 for r in out)},
+                       "cases": {"sloshing": sum(r.case == "sloshing" for r in out),
+                                 "dam break": sum(r.case == "dam break" for r in out)},
+                       "nodes_max": max(r.mesh.n_nodes for r in out)},
             "latency_p50_s": m["latency_p50_s"], "latency_p99_s": m["latency_p99_s"],
             "queue_wait_p50_s": m["queue_wait_p50_s"], "queue_wait_p99_s": m["queue_wait_p99_s"],
             "dof_per_s": m["dof_per_s"], "completed": m["completed"], "failed": m["failed"],
             "errors": [r.error for r in out if r.error][:3],
             "peak_active": srv.peak_active, "peak_estimated_bytes": srv.peak_bytes,
+            "mean_active": m["mean_active"], "slowest_requests": m["slowest"],
             "alone_equals_mix": same,
             "e2e": {"value": m["steps_per_s"], "unit": "steps/s", "h2d_bytes_per_step": int(h2d / max(steps, 1)),
                     "d2h_bytes_per_step": int(d2h / max(steps, 1))},

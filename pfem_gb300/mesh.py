@@ -104,6 +104,36 @@ def dam_break_nodes_2d(h, tank=(4.0, 3.0), column=(1.0, 2.0), jitter=0.1, seed=2
     return pos, flags
 
 
+def sloshing_nodes_2d(h, width=1.0, wall_height=1.2, depth=1.0, amplitude=0.1, jitter=0.1, seed=20261203):
+    """The tank of `examples/2D/sloshing` (geometry.geo: width b = 1, walls up to 1.2 b, free
+    surface y = b + a sin(pi x / b - pi / 2) with a = 0.1, so the water starts at rest with a
+    tilted-cosine surface and sloshes under gravity): walls at spacing h (left, bottom, right;
+    bound and fixed), fluid nodes on a lattice offset by h from the walls under the surface,
+    jittered like the dam break.  Stands in for the example's gmsh mesh, which is not shipped.
+    Returns (pos (2,N), flags (N,))."""
+    W, H = width, wall_height * width
+    walls = np.concatenate([
+        _wall_line((0.0, H), (0.0, 0.0), h),
+        _wall_line((0.0, 0.0), (W, 0.0), h)[1:],
+        _wall_line((W, 0.0), (W, H), h)[1:],
+    ])
+    nx = int(round(W / h))
+    xs = h * np.arange(1, nx)
+    pts = []
+    for x in xs:
+        top = depth + amplitude * np.sin(np.pi * x / W - np.pi / 2)
+        ny = int(np.floor(top / h + 1e-9))
+        for j in range(1, ny + 1):
+            pts.append((x, h * j))
+    fluid = np.asarray(pts, float)
+    rng = np.random.default_rng(seed)
+    fluid = fluid + rng.uniform(-jitter * h, jitter * h, size=fluid.shape)
+    pos = np.concatenate([walls, fluid]).T.copy()
+    flags = np.zeros(pos.shape[1], np.uint8)
+    flags[:walls.shape[0]] = BOUND | FIXED | DIRICHLET
+    return pos, flags
+
+
 def dam_break_nodes_3d(h, tank=(2.0, 0.5, 1.5), column=(0.5, 0.5, 1.0), jitter=0.1, seed=20261203):
     """3D open-top tank (floor and four side walls at spacing h) with a fluid column in the
     x=0 corner region, interior lattice offset by h from the walls and jittered like the 2D
@@ -272,6 +302,11 @@ def dam_break_3d(h=0.01, alpha=1.2, seed=20261203, column=(0.5, 0.5, 1.0), tank=
     return alpha_shape(pos, flags, h, alpha, delete_flying_nodes=True)
 
 
+def sloshing_2d(h=0.02, alpha=1.2, seed=20261203, amplitude=0.1):
+    pos, flags = sloshing_nodes_2d(h, amplitude=amplitude, seed=seed)
+    return alpha_shape(pos, flags, h, alpha, delete_flying_nodes=True)
+
+
 def square_nodes_2d(h, side=1.0, jitter=0.1, seed=20261203):
     """A free square of fluid, no walls: the lattice h * (i, j), 0 <= i, j <= side / h, with the
     interior nodes jittered like the dam-break column (the boundary stays straight).
@@ -339,6 +374,22 @@ def wc_initial_states(mesh, rho_star=1000.0, K0=2.2e7, K0p=7.0, g=9.81, column=(
     inside = (y <= z0) & (mesh.pos[0] <= column[0] + 1.1 * mesh.hchar)
     rho = np.where(inside,
                    rho_star * ((K0p - 1) / K0 * rho_star * g * (z0 - np.minimum(y, z0)) + 1) ** (1 / (K0p - 1)),
+                   rho_star)
+    p = np.where(inside, K0 / K0p * ((rho / rho_star) ** K0p - 1), 0.0)
+    s = np.zeros((2 * d + 2) * N)
+    s[d * N:(d + 1) * N] = p
+    s[(d + 1) * N:(d + 2) * N] = rho
+    return s
+
+
+def sloshing_wc_initial_states(mesh, rho_star=1.0, K0=2.2e5, K0p=7.6, g=9.81, depth=1.0, amplitude=0.1):
+    """`sloshingComp.lua:71-85`: Tait-Murnaghan hydrostatic field under the free surface
+    z0(x) = depth + amplitude sin(pi x - pi / 2), at rest."""
+    d, N = mesh.dim, mesh.n_nodes
+    x, y = mesh.pos[0], mesh.pos[d - 1]
+    z0 = depth + amplitude * np.sin(np.pi * x - np.pi / 2)
+    inside = y <= z0
+    rho = np.where(inside, rho_star * ((K0p - 1) / K0 * rho_star * g * (z0 - np.minimum(y, z0)) + 1) ** (1 / (K0p - 1)),
                    rho_star)
     p = np.where(inside, K0 / K0p * ((rho / rho_star) ** K0p - 1), 0.0)
     s = np.zeros((2 * d + 2) * N)

@@ -39,6 +39,8 @@ class Request:
     remesh: bool = True             # incompressible: remesh after every accepted step
     arrival: float = 0.0            # seconds after the start of the run
     rid: int = -1
+    params: dict | None = None      # further pfg_params fields (e.g. rho, K0, rho_star)
+    case: str = "dam break"
     # filled in by the server
     t_admit: float | None = None
     t_done: float | None = None
@@ -108,6 +110,8 @@ class Server:
             p = api.default_params(req.kind, req.mesh.dim)
             p.precision = req.precision
             p.mu = req.mu
+            for k, v in (req.params or {}).items():
+                setattr(p, k, v)
             p.hbm_budget_bytes = req.estimate_bytes
             if req.kind == api.KIND_INCOMP_PSPG and req.remesh:
                 self._run_incomp(req, p)
@@ -210,9 +214,17 @@ def metrics(reqs, makespan):
     wait = np.array([r.t_admit - r.arrival for r in done]) if done else np.zeros(1)
     steps = sum(r.converged_steps for r in done)
     dof_steps = sum(r.dof * r.converged_steps for r in done)
+    # mean number of requests in service over the run (time-weighted slot occupancy)
+    busy = sum(r.t_done - r.t_admit for r in done)
+    slowest = sorted(done, key=lambda r: r.latency, reverse=True)[:3]
     return {
         "requests": len(reqs), "completed": len(done), "failed": len(reqs) - len(done),
         "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
         "queue_wait_p50_s": float(np.percentile(wait, 50)), "queue_wait_p99_s": float(np.percentile(wait, 99)),
         "makespan_s": makespan, "steps_per_s": steps / makespan, "dof_per_s": dof_steps / makespan,
+        "mean_active": busy / makespan if makespan > 0 else 0.0,
+        "slowest": [{"rid": r.rid, "case": r.case, "dim": r.mesh.dim,
+                     "kind": "wc" if r.kind == api.KIND_WC_CDS_DPDT else "incomp", "nodes": r.mesh.n_nodes,
+                     "steps": r.steps, "queue_wait_s": round(r.t_admit - r.arrival, 3),
+                     "service_s": round(r.t_done - r.t_admit, 3)} for r in slowest],
     }
