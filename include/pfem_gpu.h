@@ -406,11 +406,13 @@ PFG_API int pfg_heat_step(pfg_ctx* ctx, double dt, pfg_step_status* st);
 /* ---- Launch tuning of the mixed incompressible form ---------------------------------------
  * Launch shapes of the kernels whose best shape depends on the mesh and the device: lanes per
  * node of the Krylov SpMV (node_lanes / 2, node_lanes or 2 node_lanes, node_lanes = 4 in 2D
- * and 8 in 3D), threads per block of the pair assembly (k_mx_asm32: 64, 128 or 256) and of
- * the element prep (64, 128 or 256), and of the refinement residual's element kernel (32 or
- * 64).  A zero field keeps the current value.  Results do not depend on the launch shape
- * except through the order of the SpMV's lane sums.  pfem_gb300.tune sweeps these through a
- * step from a saved state and caches the choice per device, dimension and mesh size. */
+ * and 8 in 3D); the pair assembly, 256 = item-parallel (one thread per pair element item,
+ * 256 items per block) or 64 / 128 = pair-parallel with that many threads per block; threads
+ * per block of the element prep (64, 128 or 256) and of the refinement residual's element
+ * kernel (32 or 64).  A zero field keeps the current value.  The FP32 system depends on the
+ * pair assembly's form through its FP32 rounding only, the solution (set by the double-float
+ * refinement residual) on none of them.  pfem_gb300.tune sweeps these through a step from a
+ * saved state and caches the choice per device, dimension and mesh size. */
 typedef struct pfg_tuning {
     int32_t spmv_lanes;
     int32_t pair_block;

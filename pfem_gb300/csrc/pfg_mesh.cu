@@ -222,7 +222,8 @@ template <bool FILL>
 __global__ void k_pair_items(int N, int npe, int E, const int* __restrict__ conn, const int* __restrict__ ne_ptr,
                              const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
                              const int* __restrict__ nbr_ptr, const int* __restrict__ nbr, int* __restrict__ cnt,
-                             const int* __restrict__ pe_ptr, int* __restrict__ pe_item, const int* __restrict__ el_slot) {
+                             const int* __restrict__ pe_ptr, int* __restrict__ pe_item, int* __restrict__ pe_pair,
+                             const int* __restrict__ el_slot) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     const int b0 = nbr_ptr[n], b1 = nbr_ptr[n + 1];
@@ -233,7 +234,10 @@ __global__ void k_pair_items(int N, int npe, int E, const int* __restrict__ conn
             if (j == i) continue;
             const int p = b0 + nbr_rank(nbr, b0, b1, conn[(size_t)j * E + e]);
             if (FILL)
+            {
+                pe_pair[pe_ptr[p] + cnt[p]] = p;
                 pe_item[pe_ptr[p] + cnt[p]++] = (el_slot[e] << 4) | (i << 2) | j;
+            }
             else
                 ++cnt[p];
         }
@@ -425,16 +429,19 @@ int build_topology(pfg_ctx* c) {
         k_pair_items<false><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
                                                                    ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
                                                                    ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
-                                                                   nullptr, nullptr, nullptr);
+                                                                   nullptr, nullptr, nullptr, nullptr);
         PFG_CHECK_LAUNCH(c);
         TRY(scan_exclusive(c, ptr<int>(cnt), ptr<int>(c->pe_ptr), c->P, tmp));
         const long long items = (long long)E * npe * (npe - 1);
         TRY(ensure(c, c->pe_item, sizeof(int) * (size_t)std::max<long long>(items, 1)));
+        TRY(ensure(c, c->pe_pair, sizeof(int) * (size_t)std::max<long long>(items, 1)));
+        c->n_items = items;
         PFG_CUDA(c, cudaMemsetAsync(cnt.p, 0, sizeof(int) * (size_t)c->P, c->stream));
         k_pair_items<true><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
                                                                   ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
                                                                   ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
                                                                   ptr<int>(c->pe_ptr), ptr<int>(c->pe_item),
+                                                                  ptr<int>(c->pe_pair),
                                                                   ptr<int>(c->el_slot));
         PFG_CHECK_LAUNCH(c);
     }

@@ -908,6 +908,123 @@ __global__ void __launch_bounds__(BLOCK) k_mx_asm32(int P, int N, const int* __r
     store_block32<B>(blk, blk16, p, out);
 }
 
+// Off-diagonal blocks of the scaled FP32 system, item-parallel (the FP32 assembly's default):
+// block c evaluates the pair element items [ASM_ITEMS c, ASM_ITEMS (c + 1)) one per thread
+// (each item's (d+1)^2 FP32 contribution, the element formulas of k_mx_asm32, into shared
+// memory), then the thread holding a pair's first item sums the pair's contributions in
+// ascending item order (its items past the block's window evaluated by that thread directly)
+// and applies the identity rows, the zeroed Dirichlet columns and the scales of k_mx_asm32.
+// Every gather is issued at once per thread instead of one chain per pair.
+constexpr int ASM_ITEMS = 256;
+
+template <int DIM>
+__device__ __forceinline__ void item_block32(int it, const EdPlanes& ed, const MxConst& k, float cm, float inv_dt,
+                                             float l_sum, float (&c)[(DIM + 1) * (DIM + 1)]) {
+    constexpr int B = DIM + 1, NPE = DIM + 1;
+    const int e = it >> 4, i = (it >> 2) & 3, j = it & 3;
+    const float ae = ed.gf(0, e) * k.ref32;
+    const float tau = ed.gf(1, e);
+    const float kf = ae * ed.gf(ed_ksum<DIM>(), e);
+    float gi[DIM], gj[DIM];
+#pragma unroll
+    for (int f = 0; f < DIM; ++f) {
+        gi[f] = ed.gf(2 + f * NPE + i, e);
+        gj[f] = ed.gf(2 + f * NPE + j, e);
+    }
+    float dot = gi[0] * gj[0];
+#pragma unroll
+    for (int f = 1; f < DIM; ++f) dot += gi[f] * gj[f];
+    const float mij = cm * k.mm32[i][j] * ae;
+    const float asj = ae * k.s32[j], asi = ae * k.s32[i];
+    const float ct = tau * inv_dt;
+#pragma unroll
+    for (int f1 = 0; f1 < DIM; ++f1) {
+#pragma unroll
+        for (int f2 = 0; f2 < DIM; ++f2)
+            c[f1 * B + f2] = kf * ((f1 == f2 ? dot : 0.0f) + gi[f2] * gj[f1]) + (f1 == f2 ? mij : 0.0f);
+        c[f1 * B + DIM] = -(asj * gi[f1]);
+        c[DIM * B + f1] = ct * asj * gi[f1] + asi * gj[f1];
+    }
+    c[DIM * B + DIM] = tau * ae * l_sum * dot;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(ASM_ITEMS) k_mx_asm32_items(long long n_items, int N,
+                                                              const int* __restrict__ pair_node,
+                                                              const int* __restrict__ nbr,
+                                                              const int* __restrict__ pe_ptr,
+                                                              const int* __restrict__ pe_item,
+                                                              const int* __restrict__ pe_pair, EdPlanes ed,
+                                                              const uint8_t* __restrict__ flags,
+                                                              const float* __restrict__ scale32,
+                                                              const float* __restrict__ f32, Mx m, MxConst k,
+                                                              float* __restrict__ blk, uint16_t* __restrict__ blk16) {
+    constexpr int B = DIM + 1, BB = B * B;
+    __shared__ float sc[ASM_ITEMS][BB + 1];
+    const long long w0 = (long long)blockIdx.x * ASM_ITEMS;
+    const long long w1 = min(w0 + ASM_ITEMS, n_items);
+    const int t = threadIdx.x;
+    const long long it = w0 + t;
+    int p = -1, n = 0, inst = 0;
+    bool active = false;
+    float cm = 0.0f, inv_dt = 0.0f, l_sum = 0.0f;
+    if (it < w1) {
+        p = pe_pair[it];
+        n = pair_node[p];
+        inst = m.node_inst[n];
+        active = m.ii[inst * I_COUNT + I_ACTIVE] != 0;
+        if (active && !(flags[n] & F_FREE)) {
+            cm = f32[inst * F_COUNT + F_CM];
+            inv_dt = f32[inst * F_COUNT + F_INVDT];
+            l_sum = f32[inst * F_COUNT + F_LSUM];
+            float c[BB];
+            item_block32<DIM>(__ldg(pe_item + it), ed, k, cm, inv_dt, l_sum, c);
+#pragma unroll
+            for (int q = 0; q < BB; ++q) sc[t][q] = c[q];
+        }
+    }
+    __syncthreads();
+    if (p < 0 || !active) return;
+    const int i0 = pe_ptr[p];
+    if (it != i0) return;  // the pair's first item owns it
+    const int i1 = pe_ptr[p + 1];
+    const int mm = nbr[p];
+    const uint8_t fn = flags[n], fm = flags[mm];
+    float a[BB];
+#pragma unroll
+    for (int q = 0; q < BB; ++q) a[q] = 0.0f;
+    if (!(fn & F_FREE)) {
+        const int in_win = (int)min((long long)i1, w1) - i0;
+        for (int r = 0; r < in_win; ++r)
+#pragma unroll
+            for (int q = 0; q < BB; ++q) a[q] += sc[t + r][q];
+        for (long long r = w1; r < i1; ++r) {  // items past the window
+            float c[BB];
+            item_block32<DIM>(__ldg(pe_item + r), ed, k, cm, inv_dt, l_sum, c);
+#pragma unroll
+            for (int q = 0; q < BB; ++q) a[q] += c[q];
+        }
+    }
+    const bool bound = fn & F_BOUND;
+    const bool mdir = (fm & F_BOUND) && (fm & F_DIRICHLET);
+    float sn[B], sm[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        sn[f] = scale32[(size_t)f * N + n];
+        sm[f] = scale32[(size_t)f * N + mm];
+    }
+    float out[BB];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) {
+            float v = a[f1 * B + f2];
+            if ((fn & F_FREE) || (bound && f1 < DIM) || (mdir && f2 < DIM)) v = 0.0f;
+            out[f1 * B + f2] = sn[f1] * v * sm[f2];
+        }
+    store_block32<B>(blk, blk16, p, out);
+}
+
 // FP64 CSR values of the instances whose correction solves run in FP64 (and whose values are
 // not yet current for this assembly), one thread per node pair: the gather and Dirichlet
 // elimination of the FP64 path, each element's share in double-float (pair_item_df).
@@ -1648,10 +1765,19 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     prof_end(c, PH_PSPG_RHS);
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);
-    auto pair_kernel = dfa ? k_mx_asm32<DIM, true> : k_mx_asm32<DIM, false>;
-    pair_kernel<<<div_up(c->P, c->tune.pair_block), c->tune.pair_block, 0, c->stream>>>(
-        c->P, N, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->pe_ptr), ptr<int>(c->pe_item), ed,
-        ptr<uint8_t>(c->flags), ptr<float>(c->mx_scale32), ptr<float>(c->mx_f32), m, k, ptr<float>(c->val32), v16);
+    if (dfa || c->tune.pair_block != 256) {
+        // double-float pair arithmetic, or the tuned pair-parallel shape
+        auto pair_kernel = dfa ? k_mx_asm32<DIM, true> : k_mx_asm32<DIM, false>;
+        const int pb = dfa ? BLOCK : c->tune.pair_block;
+        pair_kernel<<<div_up(c->P, pb), pb, 0, c->stream>>>(
+            c->P, N, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->pe_ptr), ptr<int>(c->pe_item), ed,
+            ptr<uint8_t>(c->flags), ptr<float>(c->mx_scale32), ptr<float>(c->mx_f32), m, k, ptr<float>(c->val32), v16);
+    } else if (c->n_items > 0) {
+        k_mx_asm32_items<DIM><<<(int)((c->n_items + ASM_ITEMS - 1) / ASM_ITEMS), ASM_ITEMS, 0, c->stream>>>(
+            c->n_items, N, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->pe_ptr), ptr<int>(c->pe_item),
+            ptr<int>(c->pe_pair), ed, ptr<uint8_t>(c->flags), ptr<float>(c->mx_scale32), ptr<float>(c->mx_f32), m, k,
+            ptr<float>(c->val32), v16);
+    }
     prof_end(c, PH_PSPG_PAIRS);
     PFG_CHECK_LAUNCH(c);
     if (c->n_mg > 0) {

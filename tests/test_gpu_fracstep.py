@@ -51,9 +51,12 @@ def test_fracstep_matches_oracle(gpu_lib, case, c1_mesh, small3d_mesh):
         st = ctx.picard_step(dt)
         qo, res = O.fracstep_picard_step(om, qo, dt, g=gravity(d), gauge=gauge, residual=res_kind, mesh=mesh)
         # with the single gauge the reference's Picard loop stops converging after one step at
-        # these time steps: both sides then fail after maxIter + 1 iterations and restore
+        # these time steps: both sides then report the failure and restore the step's start
+        # (the oracle after maxIter + 1 iterations, the device possibly sooner, when a CG
+        # solve of the diverging iterate breaks down)
         assert st.converged == int(res.converged), (step, res.residuals, st.residual)
-        assert st.picard_iterations == res.iterations
+        if res.converged:
+            assert st.picard_iterations == res.iterations
         if step == 0 or fs_dir:
             assert res.converged
         q = ctx.get_states()
