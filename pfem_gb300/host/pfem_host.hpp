@@ -109,11 +109,43 @@ class Context {
         check(pfg_heat_step(ctx_, dt, &st), "pfg_heat_step");
         return st;
     }
+    // prescribed heat flux at the facet Gauss points, (F, 3, dim); empty clears it
+    void setHeatFlux(const std::vector<double>& qGp) {
+        check(pfg_heat_set_flux(ctx_, qGp.empty() ? nullptr : qGp.data()), "pfg_heat_set_flux");
+    }
+    // independent meshes back to back (instance i owns nodes [off[i], off[i+1])), mixed precision
+    void setInstances(const std::vector<int32_t>& off, const std::vector<double>& rho, const std::vector<double>& mu) {
+        const int32_t n = (int32_t)off.size() - 1;
+        if (n < 1 || rho.size() != (size_t)n || mu.size() != (size_t)n)
+            throw std::runtime_error("setInstances: offsets, rho and mu disagree");
+        check(pfg_set_instances(ctx_, n, off.data(), rho.data(), mu.data()), "pfg_set_instances");
+        instances_ = n;
+    }
+    // one time step per instance (dt[i] for instance i)
+    std::vector<pfg_step_status> picardStepBatch(const std::vector<double>& dt) {
+        if (dt.size() != (size_t)instances_) throw std::runtime_error("picardStepBatch: one dt per instance");
+        std::vector<pfg_step_status> st((size_t)instances_);
+        check(pfg_picard_step_batch(ctx_, dt.data(), st.data()), "pfg_picard_step_batch");
+        return st;
+    }
+    std::vector<pfg_step_status> wcStepBatch(double dt, int nsteps) {
+        std::vector<pfg_step_status> st((size_t)instances_);
+        check(pfg_wc_step_batch(ctx_, dt, nsteps, st.data()), "pfg_wc_step_batch");
+        return st;
+    }
+    // launch shapes of the mixed form's tunable kernels (zero fields keep their value)
+    void setTuning(const pfg_tuning& t) { check(pfg_set_tuning(ctx_, &t), "pfg_set_tuning"); }
+    pfg_tuning tuning() const {
+        pfg_tuning t{};
+        check(pfg_get_tuning(ctx_, &t), "pfg_get_tuning");
+        return t;
+    }
 
   private:
     pfg_ctx* ctx_ = nullptr;
     pfg_params params_{};
     int nodes_ = 0;
+    int instances_ = 1;
 };
 
 // SolverIncompNewton with the PSPG solve on the GPU.
