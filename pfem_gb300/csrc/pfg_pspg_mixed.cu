@@ -917,35 +917,41 @@ __global__ void __launch_bounds__(BLOCK) k_mx_asm32(int P, int N, const int* __r
 // Every gather is issued at once per thread instead of one chain per pair.
 constexpr int ASM_ITEMS = 256;
 
+// One item's block contribution.  Every operation is an explicitly rounded intrinsic, so the
+// inlined copies (shared-memory phase and the owner's items past the window) give the same
+// bits: a pair's block then does not depend on where the block windows fall, and an instance
+// assembled in a batch equals the instance assembled alone.
 template <int DIM>
 __device__ __forceinline__ void item_block32(int it, const EdPlanes& ed, const MxConst& k, float cm, float inv_dt,
                                              float l_sum, float (&c)[(DIM + 1) * (DIM + 1)]) {
     constexpr int B = DIM + 1, NPE = DIM + 1;
     const int e = it >> 4, i = (it >> 2) & 3, j = it & 3;
-    const float ae = ed.gf(0, e) * k.ref32;
+    const float ae = __fmul_rn(ed.gf(0, e), k.ref32);
     const float tau = ed.gf(1, e);
-    const float kf = ae * ed.gf(ed_ksum<DIM>(), e);
+    const float kf = __fmul_rn(ae, ed.gf(ed_ksum<DIM>(), e));
     float gi[DIM], gj[DIM];
 #pragma unroll
     for (int f = 0; f < DIM; ++f) {
         gi[f] = ed.gf(2 + f * NPE + i, e);
         gj[f] = ed.gf(2 + f * NPE + j, e);
     }
-    float dot = gi[0] * gj[0];
+    float dot = __fmul_rn(gi[0], gj[0]);
 #pragma unroll
-    for (int f = 1; f < DIM; ++f) dot += gi[f] * gj[f];
-    const float mij = cm * k.mm32[i][j] * ae;
-    const float asj = ae * k.s32[j], asi = ae * k.s32[i];
-    const float ct = tau * inv_dt;
+    for (int f = 1; f < DIM; ++f) dot = __fmaf_rn(gi[f], gj[f], dot);
+    const float mij = __fmul_rn(__fmul_rn(cm, k.mm32[i][j]), ae);
+    const float asj = __fmul_rn(ae, k.s32[j]), asi = __fmul_rn(ae, k.s32[i]);
+    const float cta = __fmul_rn(__fmul_rn(tau, inv_dt), asj);
 #pragma unroll
     for (int f1 = 0; f1 < DIM; ++f1) {
 #pragma unroll
-        for (int f2 = 0; f2 < DIM; ++f2)
-            c[f1 * B + f2] = kf * ((f1 == f2 ? dot : 0.0f) + gi[f2] * gj[f1]) + (f1 == f2 ? mij : 0.0f);
-        c[f1 * B + DIM] = -(asj * gi[f1]);
-        c[DIM * B + f1] = ct * asj * gi[f1] + asi * gj[f1];
+        for (int f2 = 0; f2 < DIM; ++f2) {
+            const float g2 = f1 == f2 ? __fmaf_rn(gi[f2], gj[f1], dot) : __fmul_rn(gi[f2], gj[f1]);
+            c[f1 * B + f2] = __fmaf_rn(kf, g2, f1 == f2 ? mij : 0.0f);
+        }
+        c[f1 * B + DIM] = -__fmul_rn(asj, gi[f1]);
+        c[DIM * B + f1] = __fmaf_rn(cta, gi[f1], __fmul_rn(asi, gj[f1]));
     }
-    c[DIM * B + DIM] = tau * ae * l_sum * dot;
+    c[DIM * B + DIM] = __fmul_rn(__fmul_rn(__fmul_rn(tau, ae), l_sum), dot);
 }
 
 template <int DIM>
@@ -997,12 +1003,12 @@ __global__ void __launch_bounds__(ASM_ITEMS) k_mx_asm32_items(long long n_items,
         const int in_win = (int)min((long long)i1, w1) - i0;
         for (int r = 0; r < in_win; ++r)
 #pragma unroll
-            for (int q = 0; q < BB; ++q) a[q] += sc[t + r][q];
+            for (int q = 0; q < BB; ++q) a[q] = __fadd_rn(a[q], sc[t + r][q]);
         for (long long r = w1; r < i1; ++r) {  // items past the window
             float c[BB];
             item_block32<DIM>(__ldg(pe_item + r), ed, k, cm, inv_dt, l_sum, c);
 #pragma unroll
-            for (int q = 0; q < BB; ++q) a[q] += c[q];
+            for (int q = 0; q < BB; ++q) a[q] = __fadd_rn(a[q], c[q]);
         }
     }
     const bool bound = fn & F_BOUND;
@@ -1765,7 +1771,7 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     prof_end(c, PH_PSPG_RHS);
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);
-    if (dfa || c->tune.pair_block != 256) {
+    if (dfa || c->tune.pair_block != ASM_ITEMS) {
         // double-float pair arithmetic, or the tuned pair-parallel shape
         auto pair_kernel = dfa ? k_mx_asm32<DIM, true> : k_mx_asm32<DIM, false>;
         const int pb = dfa ? BLOCK : c->tune.pair_block;
