@@ -102,6 +102,7 @@ struct pfg_ctx {
     // mixed assembly: slot of each element in the element-major data (elements ordered by their
     // smallest node) and the slot of each incidence's element
     pfg::DBuf el_slot, ne_slot;
+    pfg::DBuf conn_s;  // connectivity in slot order
     // CSR system
     pfg::DBuf row_ptr, col, val, val32, diag_pos, rhs;
     int64_t nnz = 0;

@@ -214,6 +214,16 @@ __global__ void k_ne_slots(long long inc, const int* __restrict__ ne_elem, const
     if (q < inc) ne_slot[q] = el_slot[ne_elem[q]];
 }
 
+// The connectivity in slot order (conn_s[k E + slot(e)] = conn[k E + e]): the element kernels
+// that run over slots read it coalesced.
+__global__ void k_conn_slots(int E, int npe, const int* __restrict__ conn, const int* __restrict__ el_slot,
+                             int* __restrict__ conn_s) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const int s = el_slot[e];
+    for (int k = 0; k < npe; ++k) conn_s[(size_t)k * E + s] = conn[(size_t)k * E + e];
+}
+
 // Element lists of the off-diagonal node pairs: pair p = (n, m), m != n, lists every element
 // containing both, ascending, as slot(e) * 16 + (local index of n) * 4 + (local index of m).  One
 // thread per node n owns the lists of n's pairs and walks n's sorted incidences, so each list
@@ -421,6 +431,12 @@ int build_topology(pfg_ctx* c) {
         if (inc > 0) {
             k_ne_slots<<<div_up(inc, BLOCK), BLOCK, 0, c->stream>>>(inc, ptr<int>(c->ne_elem), ptr<int>(c->el_slot),
                                                                     ptr<int>(c->ne_slot));
+            PFG_CHECK_LAUNCH(c);
+        }
+        TRY(ensure(c, c->conn_s, sizeof(int) * (size_t)npe * std::max(E, 1)));
+        if (E > 0) {
+            k_conn_slots<<<div_up(E, BLOCK), BLOCK, 0, c->stream>>>(E, npe, ptr<int>(c->conn), ptr<int>(c->el_slot),
+                                                                    ptr<int>(c->conn_s));
             PFG_CHECK_LAUNCH(c);
         }
         TRY(ensure(c, cnt, sizeof(int) * (size_t)std::max(c->P, 1)));

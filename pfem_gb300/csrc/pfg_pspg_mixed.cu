@@ -1153,19 +1153,20 @@ constexpr int RES_ELEM_BLOCK = 64;  // ~136 registers a thread: small blocks kee
 // A_e x for every element row of the element's nodes (momentum rows of bound nodes are
 // identity rows and get 0): record (e, i) holds d+1 double-float values, 32 bytes.
 template <int DIM>
-__global__ void __launch_bounds__(RES_ELEM_BLOCK) k_mx_res_elem(int E, int N, const int* __restrict__ conn, EdPlanes ed,
-                                                                const int* __restrict__ el_slot,
-                                                                const uint8_t* __restrict__ flags,
+__global__ void __launch_bounds__(RES_ELEM_BLOCK) k_mx_res_elem(int E, int N, const int* __restrict__ conn_s,
+                                                                EdPlanes ed, const uint8_t* __restrict__ flags,
                                                                 const DF* __restrict__ xdf, const float* __restrict__ f32,
                                                                 Mx m, MxConst k, float4* __restrict__ rec) {
     constexpr int NPE = DIM + 1;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
+    // one thread per element slot: slot-ordered connectivity, element data and records are
+    // read and written coalesced
+    const int es = blockIdx.x * blockDim.x + threadIdx.x;
+    if (es >= E) return;
+    const int e = es;  // records are kept by slot as well
     int nd[NPE];
-    load_nodes<DIM>(conn, E, e, nd);
+    load_nodes<DIM>(conn_s, E, es, nd);
     const int inst = m.node_inst[nd[0]];
     if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
-    const int es = el_slot[e];  // the element-major data are stored by slot
     const DF inv_dt = inst_df(f32, inst, F_INVDT), l_sum = inst_df(f32, inst, F_LSUM);
     const DF cm = inst_df(f32, inst, F_CM);
     const DF ae = df_mul(ed.gdf(0, es), k.ref_df);
@@ -1261,7 +1262,7 @@ enum : int { RES_SWEEP = 0, RES_PICARD = 1, RES_START = 2 };
 
 template <int DIM>
 __global__ void __launch_bounds__(NB) k_mx_res_node(Mx m, int N, const int* __restrict__ ne_ptr,
-                                                    const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
+                                                    const int* __restrict__ ne_slot, const uint8_t* __restrict__ ne_loc,
                                                     const float4* __restrict__ rec, const uint8_t* __restrict__ flags,
                                                     const double* __restrict__ b, const double* __restrict__ x,
                                                     const double* __restrict__ scale, MxConst k,
@@ -1282,7 +1283,7 @@ __global__ void __launch_bounds__(NB) k_mx_res_node(Mx m, int N, const int* __re
         DF ax[4] = {DF{0.0f, 0.0f}, DF{0.0f, 0.0f}, DF{0.0f, 0.0f}, DF{0.0f, 0.0f}};
         if (!ident_p) {
             for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
-                const float4* r = rec + ((size_t)__ldg(ne_elem + q) * NPE + __ldg(ne_loc + q)) * 2;
+                const float4* r = rec + ((size_t)__ldg(ne_slot + q) * NPE + __ldg(ne_loc + q)) * 2;
                 const float4 r0 = __ldg(r), r1 = __ldg(r + 1);
                 ax[0] = df_add(ax[0], DF{r0.x, r0.y});
                 ax[1] = df_add(ax[1], DF{r0.z, r0.w});
@@ -1825,11 +1826,10 @@ int mx_residual(pfg_ctx* c, const MxConst& k, int kind, Counters* cnt) {
                                                              ptr<uint8_t>(c->flags), m, ptr<DF>(c->mx_xdf));
     if (E > 0)
         k_mx_res_elem<DIM><<<div_up(E, c->tune.res_block), c->tune.res_block, 0, c->stream>>>(
-            E, N, ptr<int>(c->conn), ed_planes(c), ptr<int>(c->el_slot), ptr<uint8_t>(c->flags), ptr<DF>(c->mx_xdf),
-            ptr<float>(c->mx_f32),
+            E, N, ptr<int>(c->conn_s), ed_planes(c), ptr<uint8_t>(c->flags), ptr<DF>(c->mx_xdf), ptr<float>(c->mx_f32),
             m, k, ptr<float4>(c->mx_rec));
     k_mx_res_node<DIM><<<c->n_seg, NB, 0, c->stream>>>(
-        m, N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc), ptr<float4>(c->mx_rec),
+        m, N, ptr<int>(c->ne_ptr), ptr<int>(c->ne_slot), ptr<uint8_t>(c->ne_loc), ptr<float4>(c->mx_rec),
         ptr<uint8_t>(c->flags), ptr<double>(c->rhs), ptr<double>(c->q), ptr<double>(c->mx_scale), k,
         ptr<float>(c->kv32), ptr<double>(c->kv), (size_t)c->R, kind);
     prof_end(c, PH_RESIDUAL);
