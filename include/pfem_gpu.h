@@ -405,8 +405,8 @@ PFG_API int pfg_heat_step(pfg_ctx* ctx, double dt, pfg_step_status* st);
 
 /* ---- Launch tuning of the mixed incompressible form ---------------------------------------
  * Launch shapes of the kernels whose best shape depends on the mesh and the device: lanes per
- * node of the Krylov SpMV (node_lanes / 2, node_lanes or 2 node_lanes, node_lanes = 4 in 2D
- * and 8 in 3D); the pair assembly, 256 = item-parallel (one thread per pair element item,
+ * node of the Krylov SpMV and of the multigrid's level-0 sweeps (node_lanes / 2, node_lanes or
+ * 2 node_lanes, node_lanes = 4 in 2D and 8 in 3D); the pair assembly, 256 = item-parallel (one thread per pair element item,
  * 256 items per block) or 64 / 128 = pair-parallel with that many threads per block; threads
  * per block of the element prep (64, 128 or 256) and of the refinement residual's element
  * kernel (32 or 64).  A zero field keeps the current value.  The FP32 system depends on the
@@ -418,6 +418,7 @@ typedef struct pfg_tuning {
     int32_t pair_block;
     int32_t elem_block;
     int32_t res_block;
+    int32_t mg_lanes;          /* lanes per node of the multigrid's level-0 sweeps (as spmv_lanes) */
 } pfg_tuning;
 PFG_API int pfg_set_tuning(pfg_ctx* ctx, const pfg_tuning* t);
 PFG_API int pfg_get_tuning(pfg_ctx* ctx, pfg_tuning* t);

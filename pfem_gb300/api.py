@@ -83,7 +83,7 @@ class StepStatus(C.Structure):
 class Tuning(C.Structure):
     """pfg_tuning: launch shapes of the tunable mixed-form kernels (0 = keep)."""
     _fields_ = [("spmv_lanes", C.c_int32), ("pair_block", C.c_int32), ("elem_block", C.c_int32),
-                ("res_block", C.c_int32)]
+                ("res_block", C.c_int32), ("mg_lanes", C.c_int32)]
 
 
 class PfgError(RuntimeError):
@@ -431,8 +431,8 @@ class Context:
                     "pfg_get_phase_times")
         return {self.L.pfg_phase_name(i).decode(): (float(ms[i]), int(n[i])) for i in range(NUM_PHASES) if n[i]}
 
-    def set_tuning(self, spmv_lanes=0, pair_block=0, elem_block=0, res_block=0):
-        t = Tuning(spmv_lanes, pair_block, elem_block, res_block)
+    def set_tuning(self, spmv_lanes=0, pair_block=0, elem_block=0, res_block=0, mg_lanes=0):
+        t = Tuning(spmv_lanes, pair_block, elem_block, res_block, mg_lanes)
         self._check(self.L.pfg_set_tuning(self.h, C.byref(t)), "pfg_set_tuning")
 
     def get_tuning(self):

@@ -225,6 +225,11 @@ PFG_API int pfg_set_tuning(pfg_ctx* c, const pfg_tuning* t) {
             return fail(c, PFG_ERR_INVALID, "spmv_lanes must be %d, %d or %d", lanes0 / 2, lanes0, 2 * lanes0);
         n.spmv_lanes = t->spmv_lanes;
     }
+    if (t->mg_lanes) {
+        if (t->mg_lanes != lanes0 / 2 && t->mg_lanes != lanes0 && t->mg_lanes != 2 * lanes0)
+            return fail(c, PFG_ERR_INVALID, "mg_lanes must be %d, %d or %d", lanes0 / 2, lanes0, 2 * lanes0);
+        n.mg_lanes = t->mg_lanes;
+    }
     auto block_ok = [](int b) { return b == 64 || b == 128 || b == 256; };
     if (t->pair_block) {
         if (!block_ok(t->pair_block)) return fail(c, PFG_ERR_INVALID, "pair_block must be 64, 128 or 256");
@@ -348,7 +353,7 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     c->npe = params->dim + 1;
     // pair assembly: the pair-parallel kernel with 128 threads per block (the item-parallel form
     // measured slower on the 2D and 3D dam breaks, the autotuner may still pick it)
-    c->tune = pfg_tuning{params->dim == 2 ? 4 : 8, 128, BLOCK, 64};
+    c->tune = pfg_tuning{params->dim == 2 ? 4 : 8, 128, BLOCK, 64, params->dim == 2 ? 4 : 8};
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64 * sizeof(double));

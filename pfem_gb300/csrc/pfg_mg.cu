@@ -123,12 +123,11 @@ __global__ void k_mg0_smooth0(int N, const int* __restrict__ nbr_ptr, const floa
 }
 
 // r = b - A x at level 0 (V(1,1) cycles), x read through xf
-template <int DIM, class XF>
+template <int DIM, int GN, class XF>
 __global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
                                                    const uint16_t* __restrict__ blk, const float* __restrict__ b, XF xf,
                                                    float* __restrict__ r) {
     constexpr int B = DIM + 1;
-    constexpr int GN = node_lanes<DIM>();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = t / GN, lane = t % GN;
     const bool act = n < N;
@@ -141,12 +140,11 @@ __global__ void __launch_bounds__(256) k_mg0_resid(int N, const int* __restrict_
 
 // One smoothing sweep at level 0, node n over GN lanes: out_n = x_n + omega Binv_n (b - A x)_n,
 // the iterate x read through xf.  A node without neighbours is solved exactly: out_n = Binv_n b_n.
-template <int DIM, class XF>
+template <int DIM, int GN, class XF>
 __global__ void __launch_bounds__(256) k_mg0_post(int N, const int* __restrict__ nbr_ptr, const int* __restrict__ nbr,
                                                   const uint16_t* __restrict__ blk, const float* __restrict__ binv,
                                                   const float* __restrict__ b, XF xf, float* __restrict__ out) {
     constexpr int B = DIM + 1;
-    constexpr int GN = node_lanes<DIM>();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = t / GN, lane = t % GN;
     const bool act = n < N;
@@ -741,10 +739,10 @@ namespace {
 // damped block-Jacobi sweeps (the first reads the prolonged correction directly).  V(1,1)
 // (3D): one sweep from zero and the residual on the way down, the prolonged correction and one
 // sweep on the way up.  Both read the level's matrix twice per level.
-template <int DIM>
+// GN0: lanes per node of the level-0 sweeps (the tuned mg_lanes)
+template <int DIM, int GN0>
 void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     constexpr int B = DIM + 1;
-    constexpr int GN0 = node_lanes<DIM>();
     constexpr int GNB = 4;
     const int N = c->N;
     cudaStream_t s = c->stream;
@@ -768,7 +766,7 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
         MgLevel& L1 = c->mg[0];
         if (PRE) {
             k_mg0_smooth0<DIM><<<g0, BLOCK, 0, s>>>(N, nptr, binv0, b0, x0);
-            k_mg0_resid<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, b0, X0<B>{x0, N}, out0);
+            k_mg0_resid<DIM, GN0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, b0, X0<B>{x0, N}, out0);
         }
         k_mg0_restrict<DIM><<<div_up((long long)L1.n * RL, BLOCK), BLOCK, 0, s>>>(
             L1.n, ptr<int>(L1.mem_ptr), ptr<int>(L1.mem), N, PRE ? out0 : b0, ptr<float>(L1.b));
@@ -846,10 +844,10 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
     const int* agg0 = ptr<int>(c->mg[0].agg);
     const float* xc0 = ptr<float>(c->mg[0].xb);
     if (PRE) {
-        k_mg0_post<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, XPC<B, true>{x0, N, agg0, xc0}, out0);
+        k_mg0_post<DIM, GN0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, XPC<B, true>{x0, N, agg0, xc0}, out0);
     } else {
-        k_mg0_post<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, PC<B>{agg0, xc0}, x0);
-        k_mg0_post<DIM><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, X0<B>{x0, N}, out0);
+        k_mg0_post<DIM, GN0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, PC<B>{agg0, xc0}, x0);
+        k_mg0_post<DIM, GN0><<<g0l, 256, 0, s>>>(N, nptr, nbr, v0, binv0, b0, X0<B>{x0, N}, out0);
     }
 }
 
@@ -857,10 +855,16 @@ void vcycle(pfg_ctx* c, const float* b0, float* out0) {
 
 // out = M^-1 b for the FP32 scaled system (one V-cycle), both field-major R-vectors.
 void mg_apply(pfg_ctx* c, const float* b, float* out) {
-    if (c->dim == 2)
-        vcycle<2>(c, b, out);
-    else
-        vcycle<3>(c, b, out);
+    const int g = c->tune.mg_lanes;
+    if (c->dim == 2) {
+        if (g == 2) vcycle<2, 2>(c, b, out);
+        else if (g == 8) vcycle<2, 8>(c, b, out);
+        else vcycle<2, 4>(c, b, out);
+    } else {
+        if (g == 4) vcycle<3, 4>(c, b, out);
+        else if (g == 16) vcycle<3, 16>(c, b, out);
+        else vcycle<3, 8>(c, b, out);
+    }
 }
 
 }  // namespace pfg

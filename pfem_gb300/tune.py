@@ -1,8 +1,8 @@
 """Autotuner of the mixed incompressible form's launch shapes (pfg_set_tuning).
 
-The shape of four kernels is chosen per device, dimension and mesh size: lanes per node of the
-Krylov SpMV, threads per block of the pair assembly, of the element prep and of the refinement
-residual's element kernel.  Each candidate runs one full Picard step from the same saved state
+The shape of five kernels is chosen per device, dimension and mesh size: lanes per node of the
+Krylov SpMV and of the multigrid's level-0 sweeps, the pair assembly's form and threads per
+block, threads per block of the element prep and of the refinement residual's element kernel.  Each candidate runs one full Picard step from the same saved state
 with the library's phase timers on (direct launches bracketed by CUDA events), and each knob
 takes the value whose phase was fastest per launch; the knobs belong to different phases, so
 one sweep of three steps covers them all (the residual kernel's two shapes alternate).  The
@@ -21,7 +21,7 @@ import os
 
 LANES0 = {2: 4, 3: 8}
 PHASE = {"spmv_lanes": "Krylov SpMV", "pair_block": "PSPG matrix", "elem_block": "PSPG element prep",
-         "res_block": "Picard residual"}
+         "res_block": "Picard residual", "mg_lanes": "Multigrid cycle"}
 
 
 def candidates(dim):
@@ -29,7 +29,8 @@ def candidates(dim):
     lanes = (l0, l0 // 2, 2 * l0)
     blocks = (128, 256, 64)  # pair assembly: 256 = the item-parallel form
     res = (64, 32, 64)
-    return [dict(spmv_lanes=lanes[i], pair_block=blocks[i], elem_block=blocks[i], res_block=res[i]) for i in range(3)]
+    return [dict(spmv_lanes=lanes[i], pair_block=blocks[i], elem_block=blocks[i], res_block=res[i],
+                 mg_lanes=lanes[i]) for i in range(3)]
 
 
 def cache_path():

@@ -287,9 +287,9 @@ def test_launch_shapes_keep_the_solution(gpu_lib, which, c1_mesh, small3d_mesh):
     om = O.OracleMesh(mesh)
     qo, _ = O.pspg_picard_step(om, q0.copy(), 1e-3, g=gravity(d))
     l0 = 4 if d == 2 else 8
-    for shape in (dict(spmv_lanes=l0 // 2, pair_block=64, elem_block=64, res_block=32),
-                  dict(spmv_lanes=2 * l0, pair_block=256, elem_block=128, res_block=64),
-                  dict(spmv_lanes=l0, pair_block=128, elem_block=256, res_block=64)):
+    for shape in (dict(spmv_lanes=l0 // 2, pair_block=64, elem_block=64, res_block=32, mg_lanes=2 * l0),
+                  dict(spmv_lanes=2 * l0, pair_block=256, elem_block=128, res_block=64, mg_lanes=l0 // 2),
+                  dict(spmv_lanes=l0, pair_block=128, elem_block=256, res_block=64, mg_lanes=l0)):
         ctx = make_ctx(mesh)
         ctx.set_states(q0)
         ctx.set_tuning(**shape)

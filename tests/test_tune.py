@@ -29,7 +29,8 @@ class FakeCtx:
         return {"Krylov SpMV": (0.05 * (1 + abs(t["spmv_lanes"] - 4)), 10),
                 "PSPG matrix": (0.2 * (1 + abs(t["pair_block"] - 128) / 64), 2),
                 "PSPG element prep": (0.1 * (1 + abs(t["elem_block"] - 256) / 64), 2),
-                "Picard residual": (0.3 if t["res_block"] == 64 else 0.2, 4)}
+                "Picard residual": (0.3 if t["res_block"] == 64 else 0.2, 4),
+                "Multigrid cycle": (0.1 * (1 + abs(t["mg_lanes"] - 8)), 10)}
 
 
 def test_candidates_cover_each_knob():
@@ -46,7 +47,8 @@ def test_autotune_picks_fastest_and_caches(tmp_path):
     steps = []
     choice, src = tune.autotune(ctx, 3, 330251, "GB300", lambda: steps.append(1), lambda: None, path=path)
     assert src == "measured" and len(steps) == 3
-    assert (choice["spmv_lanes"], choice["pair_block"], choice["elem_block"], choice["res_block"]) == (4, 128, 256, 32)
+    assert (choice["spmv_lanes"], choice["pair_block"], choice["elem_block"], choice["res_block"],
+            choice["mg_lanes"]) == (4, 128, 256, 32, 8)
     assert ctx.t == {k: choice[k] for k in tune.PHASE}
     table = json.load(open(path))
     assert tune.cache_key("GB300", 3, 330251) in table
