@@ -41,6 +41,8 @@ class Request:
     rid: int = -1
     params: dict | None = None      # further pfg_params fields (e.g. rho, K0, rho_star)
     case: str = "dam break"
+    t_device: float = 0.0           # incompressible with remesh: seconds in the device steps
+    t_remesh: float = 0.0           # ... and in the host remesh
     # filled in by the server
     t_admit: float | None = None
     t_done: float | None = None
@@ -112,7 +114,10 @@ class Server:
             p.mu = req.mu
             for k, v in (req.params or {}).items():
                 setattr(p, k, v)
-            p.hbm_budget_bytes = req.estimate_bytes
+            # the context's own cap: twice the admission reserve for a request that remeshes (the
+            # remesh may add nodes; admission reserves 1.5x the initial mesh's estimate)
+            p.hbm_budget_bytes = 2 * req.estimate_bytes if req.kind == api.KIND_INCOMP_PSPG and req.remesh \
+                else req.estimate_bytes
             if req.kind == api.KIND_INCOMP_PSPG and req.remesh:
                 self._run_incomp(req, p)
             else:
@@ -160,6 +165,7 @@ class Server:
                 sol.compute_next_dt()
                 tries += 1
             req.converged_steps = sol.steps
+            req.t_device, req.t_remesh = sol.t_device, sol.t_remesh
             req.result = sol.states()
             req.positions = sol.positions()
             req.device_bytes = sol.ctx.device_bytes()
@@ -226,5 +232,6 @@ def metrics(reqs, makespan):
         "slowest": [{"rid": r.rid, "case": r.case, "dim": r.mesh.dim,
                      "kind": "wc" if r.kind == api.KIND_WC_CDS_DPDT else "incomp", "nodes": r.mesh.n_nodes,
                      "steps": r.steps, "queue_wait_s": round(r.t_admit - r.arrival, 3),
-                     "service_s": round(r.t_done - r.t_admit, 3)} for r in slowest],
+                     "service_s": round(r.t_done - r.t_admit, 3), "device_step_s": round(r.t_device, 3),
+                     "host_remesh_s": round(r.t_remesh, 3)} for r in slowest],
     }

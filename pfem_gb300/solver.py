@@ -13,6 +13,8 @@ time step shrinks.  After each accepted step the host remeshes (`Mesh::remesh`, 
 """
 from __future__ import annotations
 
+import time
+
 import numpy as np
 
 from . import api
@@ -105,6 +107,8 @@ class SolverIncompNewtonGPU(_SolverBase):
         self.coeff_dec = coeff_dt_decrease
         self.solve_succeeded = True
         self.last_status = None
+        self.t_device = 0.0   # wall seconds in the device step calls
+        self.t_remesh = 0.0   # wall seconds in the host remesh and re-upload
 
     def _upload(self, mesh, states, temperature=None):
         super()._upload(mesh, states)
@@ -157,7 +161,9 @@ class SolverIncompNewtonGPU(_SolverBase):
         if heat and self.solve_heat_first and not self._heat():
             self.solve_succeeded = False
             return False
+        t0 = time.perf_counter()
         st = self.ctx.picard_step(self.dt)
+        self.t_device += time.perf_counter() - t0
         self.last_status = st
         self.solve_succeeded = bool(st.converged)
         if self.solve_succeeded and heat and not self.solve_heat_first:
@@ -165,7 +171,9 @@ class SolverIncompNewtonGPU(_SolverBase):
         if self.solve_succeeded:
             self.time += self.dt
             self.steps += 1
+            t0 = time.perf_counter()
             self.remesh()
+            self.t_remesh += time.perf_counter() - t0
         return self.solve_succeeded
 
     def compute_next_dt(self):
