@@ -353,3 +353,62 @@ def test_heat_phase_change_latent_heat(dim):
     t_pl = O.heat_step(om, plain, 1.0, melt, fl)
     assert r["converged"] and r["iterations"] >= 3
     assert np.abs(t_pc - melt).max() < 0.1 * np.abs(t_pl - melt).max()
+
+
+def test_boussinesq_wc_reduces_to_the_wc_step_and_keeps_a_uniform_temperature():
+    """BoussinesqWC (WCompNewton/Solver.cpp:278-320) with alpha = 0 moves the flow exactly as the
+    Newtonian WC step; with no heat boundary terms a uniform temperature stays uniform (the
+    Laplacian rows sum to zero and the lumped mass cancels); a temperature contrast with
+    alpha > 0 changes the velocities."""
+    m = M.dam_break_2d(0.05)
+    N, d = m.n_nodes, 2
+    s0 = M.wc_initial_states(m)
+    p = O.wc_params()
+    fl = np.zeros(N, np.uint8)
+    om1, om2, om3 = O.OracleMesh(m), O.OracleMesh(m), O.OracleMesh(m)
+    s1 = s0.copy()
+    s2 = np.concatenate([s0, np.full(N, 300.0)])
+    s3 = np.concatenate([s0, 300.0 + 80.0 * (m.pos[0] < 0.5)])
+    b0 = O.wc_bq_params(alpha=0.0, t_ref=300.0, k=0.6, cv=4180.0)
+    b1 = O.wc_bq_params(alpha=2e-4, t_ref=300.0, k=1e-9, cv=4180.0)
+    for _ in range(5):
+        dt = O.wc_next_dt(om1, p, s1)
+        assert O.wc_bq_next_dt(om2, p, b0, s2) == dt
+        O.wc_step(om1, p, dt, s1)
+        O.wc_bq_step(om2, p, b0, dt, s2, fl)
+        O.wc_bq_step(om3, p, b1, dt, s3, fl)
+    assert np.array_equal(s1, s2[:(2 * d + 2) * N])
+    T = s2[(2 * d + 2) * N:]
+    assert np.abs(T - 300.0).max() < 1e-10
+    assert np.abs(s3[:d * N] - s1[:d * N]).max() > 1e-9
+
+
+def test_fracstep_keeps_a_hydrostatic_tank_at_rest():
+    """Fractional step (MomContEquationFracStep.inl) on water filling an unjittered tank to the
+    top of its walls, at rest with the hydrostatic pressure and p = 0 pinned on the free surface:
+    the prediction's body force balances D^T p_prev exactly (P1 pressure linear in y), the
+    pressure solve returns p_prev and the correction vanishes, so the velocities stay at
+    rounding level and the pressure is unchanged."""
+    h = 0.05
+    pos, flags = M.dam_break_nodes_2d(h, tank=(1.0, 0.6), column=(1.0 - h, 0.6), jitter=0.0)
+    m = M.alpha_shape(pos, flags, h, 1.2, delete_flying_nodes=True)
+    N, d = m.n_nodes, 2
+    q0 = M.incomp_initial_states(m, column=(1.0, 0.6))
+    fs = ((m.flags & 2) != 0).astype(np.uint8)
+    om = O.OracleMesh(m)
+    q = q0.copy()
+    for _ in range(2):
+        q, res = O.fracstep_picard_step(om, q, 1e-3, gauge=fs)
+        assert res.converged
+    assert np.abs(q[:d * N]).max() < 1e-12
+    assert np.abs(q[d * N:] - q0[d * N:]).max() < 1e-12 * np.abs(q0[d * N:]).max()
+
+
+def test_fracstep_gauge_is_one_node_per_element_group():
+    m = M.dam_break_2d(0.05)
+    g = O.fs_gauge(m)
+    assert g.sum() == 1 and (m.flags[g.astype(bool)] & 2).all()
+    # two separate meshes side by side: one gauge each
+    U, off = M.concat_meshes([m, m])
+    g2 = O.fs_gauge(U)
+    assert g2.sum() == 2 and g2[:off[1]].sum() == 1
