@@ -388,15 +388,10 @@ __device__ __forceinline__ void lu_step(double* A, int n, int m, int k, int c1, 
     const double inv = d != 0.0 ? 1.0 / d : 0.0;
     for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[(size_t)i * n + k] *= inv;
     __syncthreads();
-    // rank-1 update of the trailing rows k+1..n-1, columns k+1..c1-1: 32 consecutive columns per
-    // warp (coalesced row segments), blockDim / 32 rows at a time
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, rows = blockDim.x >> 5;
-    for (int i = k + 1 + ty; i < n; i += rows) {
-        const double l = A[(size_t)i * n + k];
-        if (l == 0.0) continue;
-        double* Ai = A + (size_t)i * n;
-        const double* Ak = A + (size_t)k * n;
-        for (int j = k + 1 + tx; j < c1; j += 32) Ai[j] -= l * Ak[j];
+    const int w = c1 - k - 1, h = n - k - 1;
+    for (int r = threadIdx.x; r < h * w; r += blockDim.x) {
+        const int i = k + 1 + r / w, j = k + 1 + r % w;
+        A[(size_t)i * n + j] -= A[(size_t)i * n + k] * A[(size_t)k * n + j];
     }
     __syncthreads();
 }
