@@ -184,7 +184,23 @@ typedef struct pfg_params {
     double gamma_fs;           /* gammaFS in [0, 1]                                        */
     int32_t frac_step;         /* 1: fractional step instead of PSPG                       */
     int32_t fs_pressure_dirichlet;
+    /* weakly compressible, the continuity equation's form (the SolverWCompNewton id,
+       WCompNewton/Solver.cpp:22-23; ContEquation.inl:123-302): pfg_wc_version.  The density
+       forms run in the plain FP64 form.                                                     */
+    int32_t wc_version;
+    int32_t pad4;
 } pfg_params;
+
+/* Continuity forms of the weakly compressible solver. */
+typedef enum {
+    PFG_WC_DPDT = 0,           /* "CDS_dpdt": p from the lumped mass, D factor K0 + K0' p, free
+                                  nodes p = 0; rho from Tait-Murnaghan                       */
+    PFG_WC_RHO = 1,            /* "CDS_rho": rho = (lumped mass after the move)^-1 times the
+                                  consistent mass before it times rho                        */
+    PFG_WC_DRHODT = 2          /* "CDS_drhodt": rho from the lumped mass, D factor rho;
+                                  both density forms: free and free-surface nodes take rho*,
+                                  p from Tait-Murnaghan                                      */
+} pfg_wc_version;
 
 /* Heat boundary-condition flags per node (the reference's tag flags of HeatEq's BC table,
  * IncompNewton/Solver.cpp:132-170): T Dirichlet, Q prescribed flux, Qh convection, Qr

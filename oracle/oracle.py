@@ -63,7 +63,11 @@ HT_T, HT_Q, HT_QH, HT_QR = 1, 2, 4, 8
 class WcParams(C.Structure):
     _fields_ = [("K0", C.c_double), ("K0p", C.c_double), ("rhoStar", C.c_double), ("mu", C.c_double),
                 ("g", C.c_double * 3), ("meduri", C.c_int), ("sc", C.c_double), ("maxDT", C.c_double),
-                ("gamma", C.c_double)]
+                ("gamma", C.c_double), ("version", C.c_int)]
+
+
+# SolverWCompNewton ids (WCompNewton/Solver.cpp:22-23): the continuity equation's unknown
+WC_DPDT, WC_RHO, WC_DRHODT = 0, 1, 2
 
 
 class FsParams(C.Structure):
@@ -556,7 +560,7 @@ def facet_gauss_positions(om):
 
 
 def wc_params(K0=2.2e7, K0p=7.0, rho_star=1000.0, mu=1e-3, g=(0.0, -9.81), meduri=True, sc=0.3, max_dt=1e-3,
-              gamma=0.0):
+              gamma=0.0, version=WC_DPDT):
     p = WcParams()
     p.K0, p.K0p, p.rhoStar, p.mu = K0, K0p, rho_star, mu
     gg = tuple(g) + (0.0,) * (3 - len(g))
@@ -566,11 +570,13 @@ def wc_params(K0=2.2e7, K0p=7.0, rho_star=1000.0, mu=1e-3, g=(0.0, -9.81), medur
     p.sc = sc
     p.maxDT = max_dt
     p.gamma = gamma
+    p.version = int(version)
     return p
 
 
 def wc_step(om, params, dt, states, vbc=None):
-    """In-place WC explicit step (CDS_dpdt) on `states` (float64, (2d+2)*N)."""
+    """In-place WC explicit step (CDS_dpdt, CDS_rho or CDS_drhodt by params.version) on
+    `states` (float64, (2d+2)*N)."""
     if vbc is None:
         vbc = np.zeros(om.dim * om.N)
     assert states.dtype == np.float64 and states.flags.c_contiguous

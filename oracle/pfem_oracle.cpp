@@ -150,6 +150,7 @@ struct WcParams {
     double sc;         // securityCoeff
     double maxDT;
     double gamma;      // surface tension coefficient (MomEq "gamma")
+    int version;       // SolverWCompNewton id: 0 "CDS_dpdt", 1 "CDS_rho", 2 "CDS_drhodt"
 };
 
 // Problem "BoussinesqWC" (WCompNewton/Solver.cpp:72-146): MomEq material (MomEquation.inl:36-51)
@@ -1468,6 +1469,25 @@ void wcStep(OrcMesh* m, const WcParams* p, const WcBqParams* bq, double dt, doub
     double* a = s + (size_t)(dim + 2) * N;
     double* Tn = bq ? s + (size_t)(2 * dim + 2) * N : nullptr;
 
+    // CDS_rho: ContEqWCompNewton::preCompute -> m_buildF0 (ContEquation.inl:171-175,
+    // 194-230) before the nodes move: F0 = sum_e getM(factor 1) rho_e, consistent mass.
+    std::vector<double> F0rho;
+    if (p->version == 1) {
+        std::vector<double> F0e((size_t)E * npe);
+#pragma omp parallel for
+        for (int e = 0; e < E; ++e) {
+            Mat Me = getM(*m, m->geom[e], [](int) { return 1.0; });
+            for (int i = 0; i < npe; ++i) {
+                double f = 0;
+                for (int j = 0; j < npe; ++j) f += Me(i, j) * rho[m->node(e, j)];
+                F0e[(size_t)e * npe + i] = f;
+            }
+        }
+        F0rho.assign(N, 0.0);
+        for (int e = 0; e < E; ++e)
+            for (int i = 0; i < npe; ++i) F0rho[m->node(e, i)] += F0e[(size_t)e * npe + i];
+    }
+
     // v1/2 = v + dt/2 a ; x += dt v1/2 (:249-253, Mesh.cpp:1101-1137)
     std::vector<double> delta((size_t)dim * N);
 #pragma omp parallel for
@@ -1479,32 +1499,41 @@ void wcStep(OrcMesh* m, const WcParams* p, const WcBqParams* bq, double dt, doub
     orc_update_positions(m, delta.data());
     if (bq) wcHeatExplicit(m, bq, dt, rho, Tn, hf, Tbc, qgp);
 
-    // ContEqWCompNewton::m_buildSystemdpdt, ContEquation.inl:353-413
+    // ContEqWCompNewton::m_buildSystemdpdt (ContEquation.inl:353-413) for CDS_dpdt: the D factor
+    // K0 + K0' p_g and the mass times p; m_buildSystem (:232-302) for CDS_drhodt: the D factor
+    // rho_g and the mass times rho; for CDS_rho only the lumped mass (F0 is m_buildF0's).
+    const int ver = p->version;
+    double* U = ver == 0 ? P : rho;  // the unknown of the continuity equation
     std::vector<double> MeL((size_t)E * npe), F0e((size_t)E * npe);
 #pragma omp parallel for
     for (int e = 0; e < E; ++e) {
         const ElemGeom& geo = m->geom[e];
         Mat Me = getM(*m, geo, [](int) { return 1.0; });
-        double Pe[4], Ve[12];
-        for (int k = 0; k < npe; ++k) Pe[k] = P[m->node(e, k)];
+        double Ue[4], Ve[12];
+        for (int k = 0; k < npe; ++k) Ue[k] = U[m->node(e, k)];
         for (int f = 0; f < dim; ++f)
             for (int k = 0; k < npe; ++k) Ve[f * npe + k] = v[(size_t)f * N + m->node(e, k)];
-        Mat G = getGradN(dim, geo);
-        Mat B = getB(dim, G);
-        Mat D = getD(*m, geo, [&](int g) { return p->K0 + p->K0p * nDot(m->gt, g, Pe, npe); }, B);
+        Mat D;
+        if (ver != 1) {
+            Mat G = getGradN(dim, geo);
+            Mat B = getB(dim, G);
+            D = ver == 0 ? getD(*m, geo, [&](int g) { return p->K0 + p->K0p * nDot(m->gt, g, Ue, npe); }, B)
+                         : getD(*m, geo, [&](int g) { return nDot(m->gt, g, Ue, npe); }, B);
+        }
         for (int i = 0; i < npe; ++i) {
             double lumped = 0;
             for (int j = 0; j < npe; ++j) lumped += Me(i, j);
             MeL[(size_t)e * npe + i] = lumped;
+            if (ver == 1) continue;
             double dv = 0;
             for (int j = 0; j < dim * npe; ++j) dv += D(i, j) * Ve[j];
             double f = -dt * dv;
             if (p->meduri) {
                 double mp = 0;
-                for (int j = 0; j < npe; ++j) mp += Me(i, j) * Pe[j];
+                for (int j = 0; j < npe; ++j) mp += Me(i, j) * Ue[j];
                 f += mp;
             } else {
-                f += lumped * Pe[i];
+                f += lumped * Ue[i];
             }
             F0e[(size_t)e * npe + i] = f;
         }
@@ -1513,20 +1542,36 @@ void wcStep(OrcMesh* m, const WcParams* p, const WcBqParams* bq, double dt, doub
     for (int e = 0; e < E; ++e)
         for (int i = 0; i < npe; ++i) {
             invM[m->node(e, i)] += MeL[(size_t)e * npe + i];
-            F0[m->node(e, i)] += F0e[(size_t)e * npe + i];
+            if (ver != 1) F0[m->node(e, i)] += F0e[(size_t)e * npe + i];
         }
+    if (ver == 1) F0 = F0rho;
     for (int n = 0; n < N; ++n) invM[n] = 1 / invM[n];
-    // m_applyBCdpdt (:334-351)
-    for (int n = 0; n < N; ++n)
-        if (m->isFree[n]) {
-            F0[n] = 0;
-            invM[n] = 1;
-        }
-    // p = invM F0 ; rho from Tait-Murnaghan (:139-146, :319-332)
+    if (ver == 0) {
+        // m_applyBCdpdt (:334-351)
+        for (int n = 0; n < N; ++n)
+            if (m->isFree[n]) {
+                F0[n] = 0;
+                invM[n] = 1;
+            }
+        // p = invM F0 ; rho from Tait-Murnaghan (:139-146, :319-332)
 #pragma omp parallel for
-    for (int n = 0; n < N; ++n) {
-        P[n] = invM[n] * F0[n];
-        rho[n] = std::pow((p->K0p / p->K0) * P[n] + 1, 1 / p->K0p) * p->rhoStar;
+        for (int n = 0; n < N; ++n) {
+            P[n] = invM[n] * F0[n];
+            rho[n] = std::pow((p->K0p / p->K0) * P[n] + 1, 1 / p->K0p) * p->rhoStar;
+        }
+    } else {
+        // m_applyBC (:177-192): free and free-surface nodes take rho*
+        for (int n = 0; n < N; ++n)
+            if (m->isFree[n] || (m->flags[n] & FREE_SURFACE)) {
+                F0[n] = p->rhoStar;
+                invM[n] = 1;
+            }
+        // rho = invM F0 ; p from Tait-Murnaghan (:150-166, :305-317)
+#pragma omp parallel for
+        for (int n = 0; n < N; ++n) {
+            rho[n] = invM[n] * F0[n];
+            P[n] = (p->K0 / p->K0p) * (std::pow(rho[n] / p->rhoStar, p->K0p) - 1);
+        }
     }
 
     // MomEqWCompNewton::m_buildSystem, MomEquation.inl:229-302

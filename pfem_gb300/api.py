@@ -28,6 +28,8 @@ PC_MULTIGRID = 1
 ASM_FP32 = 0
 ASM_DOUBLE_FLOAT = 1
 RES_AX_F, RES_U, RES_U_P, RES_T = 0, 1, 2, 3
+# continuity forms of the weakly compressible solver (pfg_wc_version)
+WC_DPDT, WC_RHO, WC_DRHODT = 0, 1, 2
 
 NODE_BOUND, NODE_FREE_SURFACE, NODE_FIXED, NODE_DIRICHLET, NODE_FREE = 1, 2, 4, 8, 16
 
@@ -67,6 +69,7 @@ class Params(C.Structure):
         ("heat_phase_change", C.c_int32), ("pad3", C.c_int32), ("heat_tm", C.c_double), ("heat_dt_melt", C.c_double),
         ("heat_lm", C.c_double), ("ck_c", C.c_double), ("ck_eps", C.c_double),
         ("gamma_fs", C.c_double), ("frac_step", C.c_int32), ("fs_pressure_dirichlet", C.c_int32),
+        ("wc_version", C.c_int32), ("pad4", C.c_int32),
     ]
 
 

@@ -346,6 +346,11 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
         if (!(params->gamma_fs >= 0 && params->gamma_fs <= 1)) return PFG_ERR_INVALID;
         if (params->residual != PFG_RES_U && params->residual != PFG_RES_U_P) return PFG_ERR_INVALID;
     }
+    // continuity forms of the WC solver: the density forms in the plain FP64 form
+    if (params->wc_version < PFG_WC_DPDT || params->wc_version > PFG_WC_DRHODT) return PFG_ERR_INVALID;
+    if (params->wc_version != PFG_WC_DPDT &&
+        (params->kind != PFG_KIND_WC_CDS_DPDT || params->precision != PFG_PREC_FP64))
+        return PFG_ERR_UNSUPPORTED;
     pfg_ctx* c = new (std::nothrow) pfg_ctx();
     if (!c) return PFG_ERR_NOMEM;
     c->prm = *params;

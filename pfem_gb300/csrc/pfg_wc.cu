@@ -1,8 +1,10 @@
-// Weakly compressible explicit step (CDS_dpdt with the Tait-Murnaghan equation of state).
+// Weakly compressible explicit step (CDS_dpdt, CDS_rho or CDS_drhodt with the Tait-Murnaghan
+// equation of state).
 //
 // Reference: SolverWCompNewton::m_solveWCompNewtonNoT (WCompNewton/Solver.cpp:236-276),
 // ContEqWCompNewton::m_buildSystemdpdt/m_applyBCdpdt/solve (ContEquation.inl:123-169,
-// :334-413), MomEqWCompNewton::m_buildSystem/m_applyBC/solve (MomEquation.inl:201-374) and
+// :334-413), m_buildF0/m_buildSystem/m_applyBC (:171-302) for the density forms,
+// MomEqWCompNewton::m_buildSystem/m_applyBC/solve (MomEquation.inl:201-374) and
 // SolverWCompNewton::computeNextDT (Solver.cpp:192-234).
 //
 // One step is six kernels, captured once into a CUDA graph:
@@ -12,6 +14,10 @@
 //   mom_elem  (element) per element node: lumped rho-mass and FTot = -K v + D^T p + F(rho g)
 //   mom_node  (node)    gather -> a = F / M (with BCs), v = v1/2 + dt/2 a
 //   dt        (element) min over elements of sc^2 h^2 / max(u^2, c^2, 4 alpha^2/h^2) -> next dt
+// The density forms solve the continuity equation for rho and take p from it: CDS_drhodt with the
+// D factor rho_g and the mass times rho; CDS_rho with F0 = M rho built by one more element kernel
+// (rho_pre) before the prediction moves the nodes (ContEqWCompNewton::preCompute) and only the
+// lumped mass after it.  Their boundary condition: free and free-surface nodes take rho*.
 //
 // Precision.  Node state (x, v, p, rho, a) is FP64 in both forms; geometry (J, detJ, the
 // area-weighted shape gradients A_fi = |e| dN_i/dx_f) is FP64; the element arithmetic type R
@@ -41,6 +47,7 @@ struct WcConst {
     double K0, K0p, rho_star, mu, sc, max_dt;
     double g[3];
     int meduri;
+    int ver;           // pfg_wc_version: 0 CDS_dpdt, 1 CDS_rho, 2 CDS_drhodt
     double MM[4][4];   // sum_g w N_i N_j
     double s[4];       // sum_g w N_i
     double S;          // sum_i s_i
@@ -76,6 +83,7 @@ WcConst make_const(pfg_ctx* c) {
     k.max_dt = c->prm.max_dt;
     for (int f = 0; f < 3; ++f) k.g[f] = c->prm.gravity[f];
     k.meduri = c->prm.meduri;
+    k.ver = c->prm.wc_version;
     k.S = 0;
     for (int i = 0; i < 4; ++i) {
         k.s[i] = gc.s[i];
@@ -187,8 +195,38 @@ __global__ void k_wc_predict(int N, const uint8_t* __restrict__ flags, double* _
     }
 }
 
+// CDS_rho, m_buildF0 (ContEquation.inl:194-230) on the positions before the prediction moves
+// them: cont_i = |e| sum_j MM_ij rho_j, the consistent mass times rho.
+template <int DIM>
+__global__ void __launch_bounds__(BLOCK) k_wc_rho_pre(int E, int N, const int* __restrict__ conn,
+                                                      const double* __restrict__ pos, const double* __restrict__ s,
+                                                      WcConst k, double* __restrict__ elr) {
+    using L = ElLayout<DIM>;
+    constexpr int NPE = DIM + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int nd[NPE];
+    load_nodes<DIM>(conn, E, e, nd);
+    Geom<DIM> g;
+    jacobian<DIM>(pos, N, nd, g);
+    const double ae = g.detJ * k.refSize;
+    double Rh[NPE];
+#pragma unroll
+    for (int j = 0; j < NPE; ++j) Rh[j] = s[(size_t)(DIM + 1) * N + nd[j]];
+    double* out = elr + (size_t)e * L::NR;
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) {
+        double mr = 0;
+#pragma unroll
+        for (int j = 0; j < NPE; ++j) mr += k.MM[i][j] * Rh[j];
+        out[L::CONT + i] = ae * mr;
+    }
+}
+
 // Continuity (m_buildSystemdpdt): per element node i, ML_i = |e| s_i and
 //   cont_i = -dt (K0 s_i + K0' sum_j MM_ij p_j) |e| div v  [+ |e| sum_j MM_ij (p_j - p_i)  (Meduri)]
+// CDS_drhodt (m_buildSystem): the same with rho for p and the D factor sum_j MM_ij rho_j;
+// CDS_rho: ML only (cont is k_wc_rho_pre's).
 template <int DIM, class R>
 __global__ void __launch_bounds__(BLOCK) k_wc_cont_elem(int E, int N, const int* __restrict__ conn,
                                                         const double* __restrict__ pos, const double* __restrict__ s,
@@ -206,15 +244,21 @@ __global__ void __launch_bounds__(BLOCK) k_wc_cont_elem(int E, int N, const int*
     double A[DIM][NPE];
     area_gradients<DIM>(g, k.refSize, A);
     const double ae = g.detJ * k.refSize;
+    R* out = elr + (size_t)e * L::NR;
+    if (k.ver == 1) {
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) out[L::ML + i] = (R)(ae * k.s[i]);
+        return;
+    }
+    const int uf = k.ver == 0 ? DIM : DIM + 1;  // the unknown: p (dpdt) or rho (drhodt)
     double P[NPE];
     R adiv = 0;  // |e| div v
 #pragma unroll
     for (int j = 0; j < NPE; ++j) {
-        P[j] = s[(size_t)DIM * N + nd[j]];
+        P[j] = s[(size_t)uf * N + nd[j]];
 #pragma unroll
         for (int f = 0; f < DIM; ++f) adiv += (R)A[f][j] * (R)s[(size_t)f * N + nd[j]];
     }
-    R* out = elr + (size_t)e * L::NR;
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
         R mp = 0, mdp = 0;
@@ -223,7 +267,8 @@ __global__ void __launch_bounds__(BLOCK) k_wc_cont_elem(int E, int N, const int*
             mp += (R)k.MM[i][j] * (R)P[j];
             mdp += (R)k.MM[i][j] * (R)(P[j] - P[i]);
         }
-        const R swn = (R)(k.K0 * k.s[i]) + (R)k.K0p * mp;  // sum_g w (K0 + K0' p_g) N_i
+        // sum_g w (K0 + K0' p_g) N_i, or sum_g w rho_g N_i
+        const R swn = k.ver == 0 ? (R)(k.K0 * k.s[i]) + (R)k.K0p * mp : mp;
         R cont = -(R)dt * swn * adiv;
         if (k.meduri) cont += (R)ae * mdp;
         out[L::ML + i] = (R)(ae * k.s[i]);
@@ -249,6 +294,19 @@ __global__ void k_wc_cont_node(int N, const int* __restrict__ ne_ptr, const int*
     }
     double* P = s + (size_t)DIM * N;
     double* rho = s + (size_t)(DIM + 1) * N;
+    if (k.ver != 0) {
+        // density forms: m_applyBC (ContEquation.inl:177-192), rho = invM F0, then
+        // p = (K0/K0') ((rho/rho*)^K0' - 1) (:305-317); CDS_rho's F0 is the whole consistent
+        // mass product, CDS_drhodt's the difference form as for p
+        double r;
+        if (flags[n] & (F_FREE | F_FREE_SURFACE))
+            r = k.rho_star;
+        else
+            r = k.ver == 1 ? f0 * (1 / m) : rho[n] + (1 / m) * f0;
+        rho[n] = r;
+        P[n] = (k.K0 / k.K0p) * (pow(r / k.rho_star, k.K0p) - 1);
+        return;
+    }
     if (flags[n] & F_FREE) {
         P[n] = 0.0;
         rho[n] = k.rho_star;  // ((K0'/K0) 0 + 1)^(1/K0') rho*
@@ -582,6 +640,11 @@ int launch_step(pfg_ctx* c, bool adapt, const WcConst& k) {
     R* nodal = ptr<R>(c->wc_nodal);
     double* tdt = ptr<double>(c->wc_dt);
     const int gn = div_up(N, BLOCK), ge = std::max(1, div_up(E, BLOCK));
+    if (k.ver == 1 && E > 0) {  // CDS_rho: F0 = M rho on the positions before the move
+        prof_begin(c, PH_WC_CONT_ELEM);
+        k_wc_rho_pre<DIM><<<ge, BLOCK, 0, c->stream>>>(E, N, ptr<int>(c->conn), ptr<double>(c->pos), s, k, elr);
+        prof_end(c, PH_WC_CONT_ELEM);
+    }
     prof_begin(c, PH_WC_PREDICT);
     k_wc_predict<DIM><<<gn, BLOCK, 0, c->stream>>>(N, ptr<uint8_t>(c->flags), s, ptr<double>(c->pos), tdt);
     prof_end(c, PH_WC_PREDICT);

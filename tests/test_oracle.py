@@ -412,3 +412,92 @@ def test_fracstep_gauge_is_one_node_per_element_group():
     U, off = M.concat_meshes([m, m])
     g2 = O.fs_gauge(U)
     assert g2.sum() == 2 and g2[:off[1]].sum() == 1
+
+
+def _lumped_mass(mesh, pos):
+    """|e| / (d + 1) summed per node: the row sums of the P1 consistent mass."""
+    d = mesh.dim
+    X = pos[:, mesh.conn]
+    J = X[:, 1:, :] - X[:, :1, :]
+    vol = np.abs(np.linalg.det(np.moveaxis(J, 2, 0))) / (2.0 if d == 2 else 6.0)
+    ml = np.zeros(mesh.n_nodes)
+    for k in range(d + 1):
+        np.add.at(ml, mesh.conn[k], vol / (d + 1))
+    return ml, vol
+
+
+def test_wc_drhodt_keeps_a_uniform_density_at_rest(wc_small_mesh):
+    """CDS_drhodt (ContEquation.inl:232-302) at rest without gravity: D v = 0 and the mass
+    terms give rho back, so interior densities stay, free-surface and free nodes take rho*, and
+    p follows from Tait-Murnaghan (:305-317)."""
+    mesh = wc_small_mesh
+    d, N = mesh.dim, mesh.n_nodes
+    om = O.OracleMesh(mesh)
+    for meduri in (True, False):
+        p = O.wc_params(g=(0.0,) * d, meduri=meduri, version=O.WC_DRHODT)
+        s = np.zeros((2 * d + 2) * N)
+        rho0 = 1000.0 * 1.001
+        s[(d + 1) * N:(d + 2) * N] = rho0
+        O.wc_step(om, p, 1e-5, s)
+        rho, P = s[(d + 1) * N:(d + 2) * N], s[d * N:(d + 1) * N]
+        fs = ((mesh.flags & M.FREE_SURFACE) != 0) | mesh.is_free()
+        assert np.allclose(rho[~fs], rho0, rtol=1e-14)
+        assert np.all(rho[fs] == p.rhoStar) and np.all(P[fs] == 0.0)
+        expect = (p.K0 / p.K0p) * ((rho0 / p.rhoStar) ** p.K0p - 1)
+        assert np.allclose(P[~fs], expect, rtol=1e-12)
+
+
+def test_wc_rho_conserves_the_discrete_mass(wc_small_mesh):
+    """CDS_rho (m_buildF0 before the move, lumped mass after it, ContEquation.inl:171-230):
+    every node off the free surface has ML_new rho_new = (M_old rho_old) with the consistent P1
+    mass M_ij = |e| (1 + delta_ij) / ((d + 1)(d + 2)), restated here in numpy."""
+    mesh = wc_small_mesh
+    d, N = mesh.dim, mesh.n_nodes
+    om = O.OracleMesh(mesh)
+    p = O.wc_params(version=O.WC_RHO)
+    s = M.wc_initial_states(mesh)
+    rng = np.random.default_rng(3)
+    s[:d * N] = rng.uniform(-0.05, 0.05, d * N) * np.tile(~mesh.is_free(), d)
+    rho_old = s[(d + 1) * N:(d + 2) * N].copy()
+    x_old = om.positions.copy()
+    _, vol = _lumped_mass(mesh, x_old)
+    f0 = np.zeros(N)
+    c = 1.0 / ((d + 1) * (d + 2))
+    for i in range(d + 1):
+        for j in range(d + 1):
+            np.add.at(f0, mesh.conn[i], vol * c * (2.0 if i == j else 1.0) * rho_old[mesh.conn[j]])
+    dt = 1e-4
+    O.wc_step(om, p, dt, s)
+    ml_new, _ = _lumped_mass(mesh, om.positions)
+    rho = s[(d + 1) * N:(d + 2) * N]
+    fs = ((mesh.flags & M.FREE_SURFACE) != 0) | mesh.is_free()
+    assert not np.array_equal(om.positions, x_old)
+    assert np.allclose(ml_new[~fs] * rho[~fs], f0[~fs], rtol=1e-13)
+    assert np.all(rho[fs] == p.rhoStar)
+    P = s[d * N:(d + 1) * N]
+    assert np.allclose(P, (p.K0 / p.K0p) * ((rho / p.rhoStar) ** p.K0p - 1), rtol=1e-12, atol=1e-9)
+
+
+def test_wc_density_forms_agree_with_dpdt_to_first_order(wc_small_mesh):
+    """The three continuity forms discretise the same equation (dp = (K0 + K0' p) / rho drho):
+    over three CFL steps from the hydrostatic column they give interior pressures that agree to
+    a small fraction of the hydrostatic range.  They differ next to the free surface, where the
+    density forms set rho* (p = 0) on the surface nodes and CDS_dpdt solves for them, so the
+    bound is on the median and the 90th percentile."""
+    mesh = wc_small_mesh
+    d, N = mesh.dim, mesh.n_nodes
+    om0 = O.OracleMesh(mesh)
+    s0 = M.wc_initial_states(mesh)
+    dt = O.wc_next_dt(om0, O.wc_params(), s0)
+    out = {}
+    for ver in (O.WC_DPDT, O.WC_RHO, O.WC_DRHODT):
+        om = O.OracleMesh(mesh)
+        s = s0.copy()
+        for _ in range(3):
+            O.wc_step(om, O.wc_params(version=ver), dt, s)
+        out[ver] = s[d * N:(d + 1) * N]
+    inner = ~mesh.is_free() & ((mesh.flags & M.FREE_SURFACE) == 0)
+    scale = s0[d * N:(d + 1) * N].max()
+    for ver in (O.WC_RHO, O.WC_DRHODT):
+        e = np.abs(out[ver] - out[O.WC_DPDT])[inner]
+        assert np.median(e) < 1e-5 * scale and np.quantile(e, 0.9) < 1e-3 * scale, (ver, np.quantile(e, [0.5, 0.9]))
