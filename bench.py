@@ -1471,7 +1471,8 @@ def run_gpu_serve(args):
                        "dims": {"2d": sum(r.mesh.dim == 2 for r in out), "3d": sum(r.mesh.dim == 3 for r in out)},
                        "cases": {"sloshing": sum(r.case == "sloshing" for r in out),
                                  "dam break": sum(r.case == "dam break" for r in out)},
-                       "nodes_max": max(r.mesh.n_nodes for r in out)},
+                       "nodes_max": max(r.mesh.n_nodes for r in out),
+                       "remesh": "C++ host remesh (libpfemremesh.so) after every accepted incompressible step"},
             "latency_p50_s": m["latency_p50_s"], "latency_p99_s": m["latency_p99_s"],
             "queue_wait_p50_s": m["queue_wait_p50_s"], "queue_wait_p99_s": m["queue_wait_p99_s"],
             "dof_per_s": m["dof_per_s"], "completed": m["completed"], "failed": m["failed"],

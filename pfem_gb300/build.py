@@ -75,5 +75,27 @@ def build(force=False, verbose=False, extra=()):
     return LIB
 
 
+REMESH_SRC = os.path.join(HERE, "host", "pfem_remesh.cpp")
+REMESH_LIB = os.path.join(HERE, "libpfemremesh.so")
+
+
+def build_remesh(force=False):
+    """The C++ host remesh, libpfemremesh.so (g++, no CUDA)."""
+    hdr = os.path.join(HERE, "..", "include", "pfem_remesh.h")
+    if (not force and os.path.exists(REMESH_LIB) and
+            os.path.getmtime(REMESH_LIB) >= max(os.path.getmtime(REMESH_SRC), os.path.getmtime(hdr))):
+        return REMESH_LIB
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = REMESH_LIB + f".tmp{os.getpid()}"
+    # no contraction into FMAs: the same roundings on x86 and Arm as the Python host remesh
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-fvisibility=hidden", REMESH_SRC,
+           "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed on {REMESH_SRC}:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, REMESH_LIB)
+    return REMESH_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -197,18 +197,23 @@ def _signed_measure(P, simp):
     return np.linalg.det(A)
 
 
-def alpha_shape(pos, flags, hchar, alpha=1.2, delete_flying_nodes=False):
+def alpha_shape(pos, flags, hchar, alpha=1.2, delete_flying_nodes=False, jitter=None):
     """Delaunay + alpha-shape remesh of a node cloud (`Mesh::triangulateAlphaShape2D/3D`).
 
     Returns a HostMesh.  Free-surface bits are recomputed; the other flag bits are kept.
     With `delete_flying_nodes`, nodes that end up in no element and are not bound are
     removed (`Mesh::deleteFlyingNodes`, `srcs/mesh/Mesh.cpp:251-331`) and the returned mesh
-    carries `node_origin` (old index of each kept node) as an attribute."""
+    carries `node_origin` (old index of each kept node) as an attribute.  `jitter` ((dim, n)
+    array, or a callable of n giving one) replaces the default perturbation the triangulation
+    sees (none in 2D, a seeded 1e-6 h in 3D)."""
     from scipy.spatial import Delaunay
 
     dim = pos.shape[0]
     P = np.ascontiguousarray(pos.T)
-    if dim == 3:
+    if jitter is not None:
+        jig = jitter(P.shape[0]) if callable(jitter) else jitter
+        tri = Delaunay(P + np.ascontiguousarray(np.asarray(jig, float).T))
+    elif dim == 3:
         # The unjittered wall lattice is full of co-spherical point sets, on which Qhull's
         # merging is an order of magnitude slower.  Triangulating a copy moved by 1e-6 h
         # (seeded) breaks the ties, as CGAL's symbolic perturbation does; all geometry below

@@ -97,9 +97,10 @@ class Server:
     """Runs requests with at most `max_active` at a time and their estimated device memory
     summed below `hbm_budget_bytes`."""
 
-    def __init__(self, hbm_budget_bytes: int, max_active: int = 8):
+    def __init__(self, hbm_budget_bytes: int, max_active: int = 8, native_remesh: bool = True):
         self.budget = int(hbm_budget_bytes)
         self.max_active = int(max_active)
+        self.native_remesh = bool(native_remesh)   # the C++ host remesh (else the Python one)
         self._lock = threading.Condition()
         self._active = 0
         self._used = 0
@@ -119,7 +120,7 @@ class Server:
             p.hbm_budget_bytes = 2 * req.estimate_bytes if req.kind == api.KIND_INCOMP_PSPG and req.remesh \
                 else req.estimate_bytes
             if req.kind == api.KIND_INCOMP_PSPG and req.remesh:
-                self._run_incomp(req, p)
+                self._run_incomp(req, p, self.native_remesh)
             else:
                 ctx = api.Context(p)
                 try:
@@ -147,7 +148,7 @@ class Server:
             self._lock.notify_all()
 
     @staticmethod
-    def _run_incomp(req: Request, p):
+    def _run_incomp(req: Request, p, native_remesh=True):
         """`steps` accepted steps of the reference's loop (`IncompNewton/Solver.cpp:216-247`):
         remesh after each accepted step, dt halved after a failed one (at most 4 x steps tries)."""
         m = req.mesh
@@ -155,7 +156,7 @@ class Server:
         pad = 0.1 * (hi - lo)
         box = tuple(lo - pad) + tuple(hi + pad)
         box = box[:2 * m.dim - 1] + (1e30,)  # open at the top: nodes leave only sideways or below
-        prm = RM.RemeshParams(hchar=m.hchar, alpha=m.alpha, bounding_box=box)
+        prm = RM.RemeshParams(hchar=m.hchar, alpha=m.alpha, bounding_box=box, native=native_remesh)
         sol = SO.SolverIncompNewtonGPU(m, req.states, params=p, remesh_params=prm, precision=req.precision,
                                        initial_dt=req.dt, max_dt=req.dt)
         try:

@@ -59,14 +59,15 @@ class _SolverBase:
         return self.ctx.get_positions()
 
     def remesh(self):
-        """`Mesh::remesh` on the host, then the new mesh and remapped states go to the device."""
+        """`Mesh::remesh` on the host, then the new mesh and the states remapped on the host
+        (`RM.apply_origin`) go to the device."""
         if self.remesh_params is None:
             return
         cur = self.mesh.copy()
         cur.pos = self.ctx.get_positions()
         cur.flags = self.ctx.get_flags() & np.uint8(0x0F)
-        new, st = RM.remesh(cur, self.ctx.get_states(), self.remesh_params)
-        self._upload(new, st)
+        new, origin = RM.remesh_map(cur, self.remesh_params)
+        self._upload(new, RM.apply_origin(self.ctx.get_states(), origin, cur.n_nodes))
 
     def close(self):
         self.ctx.close()

@@ -67,3 +67,42 @@ def test_null_arguments_rejected(gpu_lib):
     assert gpu_lib.pfg_destroy(None) == -1
     assert gpu_lib.pfg_last_error(None) == b"null context"
     assert gpu_lib.pfg_version().startswith(b"pfem_gb300")
+
+
+REMESH_HEADER = os.path.join(ROOT, "include", "pfem_remesh.h")
+
+
+def test_remesh_library_exports_every_declared_symbol():
+    from pfem_gb300 import build
+    from pfem_gb300 import remesh as R
+
+    build.build_remesh()
+    lib = R.native_lib()
+    txt = open(REMESH_HEADER).read()
+    syms = sorted(set(re.findall(r"PFR_API\s+[^;(]*?\b(pfr_\w+)\s*\(", txt)))
+    assert len(syms) == 7
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(R.REMESH_EXPORTED) == syms
+
+
+def test_remesh_struct_layout_matches_header():
+    from pfem_gb300 import remesh as R
+
+    src = r"""
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "pfem_remesh.h"
+    int main(void) {
+        printf("%zu %zu %zu\n", sizeof(pfr_params), offsetof(pfr_params, jitter), offsetof(pfr_params, bounding_box));
+        return 0;
+    }
+    """
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe])
+        out = subprocess.check_output([exe]).decode().split()
+    P = R._PfrParams
+    assert [int(x) for x in out] == [ctypes.sizeof(P), P.jitter.offset, P.bounding_box.offset]
