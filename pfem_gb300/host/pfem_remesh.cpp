@@ -226,23 +226,27 @@ int insphere<2>(const double* const* p, const double* q) {
 // (det[p1-p0; p2-p0; p3-p0] > 0) the determinant is negative when q lies inside.
 template <>
 int insphere<3>(const double* const* p, const double* q) {
-    double r[4][3], l[4];
-    for (int k = 0; k < 4; ++k) {
-        for (int c = 0; c < 3; ++c) r[k][c] = p[k][c] - q[c];
-        l[k] = r[k][0] * r[k][0] + r[k][1] * r[k][1] + r[k][2] * r[k][2];
-    }
-    double det = 0, perm = 0;
-    for (int k = 0; k < 4; ++k) {
-        double m[3][3];
-        for (int i = 0, rr = 0; i < 4; ++i) {
-            if (i == k) continue;
-            for (int c = 0; c < 3; ++c) m[rr][c] = r[i][c];
-            ++rr;
-        }
-        const double s = ((k + 3) & 1) ? -1.0 : 1.0;
-        det += s * l[k] * det3(m);
-        perm += l[k] * perm3(m);
-    }
+    // the same determinant from the 2x2 minors of the x, y columns (fewer products)
+    const double ax = p[0][0] - q[0], ay = p[0][1] - q[1], az = p[0][2] - q[2];
+    const double bx = p[1][0] - q[0], by = p[1][1] - q[1], bz = p[1][2] - q[2];
+    const double cx = p[2][0] - q[0], cy = p[2][1] - q[1], cz = p[2][2] - q[2];
+    const double dx = p[3][0] - q[0], dy = p[3][1] - q[1], dz = p[3][2] - q[2];
+    const double axby = ax * by, bxay = bx * ay, bxcy = bx * cy, cxby = cx * by, cxdy = cx * dy, dxcy = dx * cy;
+    const double dxay = dx * ay, axdy = ax * dy, axcy = ax * cy, cxay = cx * ay, bxdy = bx * dy, dxby = dx * by;
+    const double ab = axby - bxay, bc = bxcy - cxby, cd = cxdy - dxcy, da = dxay - axdy, ac = axcy - cxay,
+                 bd = bxdy - dxby;
+    const double abc = az * bc - bz * ac + cz * ab, bcd = bz * cd - cz * bd + dz * bc;
+    const double cda = cz * da + dz * ac + az * cd, dab = dz * ab + az * bd + bz * da;
+    const double al = ax * ax + ay * ay + az * az, bl = bx * bx + by * by + bz * bz;
+    const double cl = cx * cx + cy * cy + cz * cz, dl = dx * dx + dy * dy + dz * dz;
+    const double det = (dl * abc - cl * dab) + (bl * cda - al * bcd);
+    const double abp = std::fabs(axby) + std::fabs(bxay), bcp = std::fabs(bxcy) + std::fabs(cxby);
+    const double cdp = std::fabs(cxdy) + std::fabs(dxcy), dap = std::fabs(dxay) + std::fabs(axdy);
+    const double acp = std::fabs(axcy) + std::fabs(cxay), bdp = std::fabs(bxdy) + std::fabs(dxby);
+    const double perm = dl * (std::fabs(az) * bcp + std::fabs(bz) * acp + std::fabs(cz) * abp) +
+                        cl * (std::fabs(dz) * abp + std::fabs(az) * bdp + std::fabs(bz) * dap) +
+                        bl * (std::fabs(cz) * dap + std::fabs(dz) * acp + std::fabs(az) * cdp) +
+                        al * (std::fabs(bz) * cdp + std::fabs(cz) * bdp + std::fabs(dz) * bcp);
     if (std::fabs(det) > FILTER * perm) return det < 0 ? 1 : -1;
     Ex R[4][3], L[4];
     for (int k = 0; k < 4; ++k) {
@@ -282,6 +286,7 @@ template <int D>
 class Delaunay {
 public:
     static constexpr int V = D + 1;
+    static constexpr int S = 2 * V;  // per simplex in T_: V vertices, then the V neighbours
 
     // pts: n points, D doubles each (interleaved)
     explicit Delaunay(std::vector<double> pts) : P_(std::move(pts)) { n_ = (int)(P_.size() / D); }
@@ -298,16 +303,16 @@ public:
     bool real(int t) const {
         if (!alive_[t]) return false;
         for (int i = 0; i < V; ++i)
-            if (tv_[(size_t)t * V + i] >= n_) return false;
+            if (T_[(size_t)t * S + i] >= n_) return false;
         return true;
     }
-    int vert(int t, int i) const { return tv_[(size_t)t * V + i]; }
-    int nbr(int t, int i) const { return tn_[(size_t)t * V + i]; }
+    int vert(int t, int i) const { return T_[(size_t)t * S + i]; }
+    int nbr(int t, int i) const { return T_[(size_t)t * S + V + i]; }
 
 private:
     std::vector<double> P_;
     int n_ = 0;
-    std::vector<int> tv_, tn_;
+    std::vector<int> T_;  // simplex t: vertices T_[t*S + i], neighbour opposite i T_[t*S + V + i]
     std::vector<uint8_t> alive_;
     std::vector<int> free_;
     std::vector<int> mark_;
@@ -333,8 +338,7 @@ private:
         } else {
             t = (int)alive_.size();
             alive_.push_back(0);
-            tv_.resize(tv_.size() + V);
-            tn_.resize(tn_.size() + V);
+            T_.resize(T_.size() + S);
             mark_.push_back(0);
         }
         alive_[t] = 1;
@@ -367,12 +371,12 @@ private:
         }
         const int t = alloc();
         for (int i = 0; i < V; ++i) {
-            tv_[(size_t)t * V + i] = n_ + i;
-            tn_[(size_t)t * V + i] = -1;
+            T_[(size_t)t * S + i] = n_ + i;
+            T_[(size_t)t * S + V + i] = -1;
         }
         const double* q[V];
         for (int i = 0; i < V; ++i) q[i] = pt(n_ + i);
-        if (orient<D>(q) < 0) std::swap(tv_[(size_t)t * V + D - 1], tv_[(size_t)t * V + D]);
+        if (orient<D>(q) < 0) std::swap(T_[(size_t)t * S + D - 1], T_[(size_t)t * S + D]);
         last_ = t;
     }
 
@@ -436,10 +440,10 @@ private:
             bool moved = false;
             for (int k = 0; k < V; ++k) {
                 const int j = (off + k) % V;
-                for (int i = 0; i < V; ++i) q[i] = pt(tv_[(size_t)t * V + i]);
+                for (int i = 0; i < V; ++i) q[i] = pt(T_[(size_t)t * S + i]);
                 q[j] = pt(p);
                 if (orient<D>(q) < 0) {
-                    const int nb = tn_[(size_t)t * V + j];
+                    const int nb = T_[(size_t)t * S + V + j];
                     if (nb < 0) throw Failure(PFR_ERR_INTERNAL, "point location left the enclosing simplex");
                     t = nb;
                     moved = true;
@@ -452,14 +456,14 @@ private:
 
     bool in_conflict(int t, int p) const {
         const double* q[V];
-        for (int i = 0; i < V; ++i) q[i] = pt(tv_[(size_t)t * V + i]);
+        for (int i = 0; i < V; ++i) q[i] = pt(T_[(size_t)t * S + i]);
         return insphere<D>(q, pt(p)) > 0;
     }
 
     void insert(int p) {
         const int t0 = locate(p);
         for (int i = 0; i < V; ++i) {  // a duplicate of a vertex stays out of the triangulation
-            const double* a = pt(tv_[(size_t)t0 * V + i]);
+            const double* a = pt(T_[(size_t)t0 * S + i]);
             bool same = true;
             for (int c = 0; c < D; ++c) same = same && a[c] == pt(p)[c];
             if (same) return;
@@ -477,7 +481,7 @@ private:
             stack_.pop_back();
             cav_.push_back(c);
             for (int j = 0; j < V; ++j) {
-                const int nb = tn_[(size_t)c * V + j];
+                const int nb = T_[(size_t)c * S + V + j];
                 if (nb < 0) {
                     bnd_.push_back({c, j, -1});
                     continue;
@@ -504,13 +508,13 @@ private:
         for (const Bnd& b : bnd_) {
             const int nt = alloc();
             mark_[nt] = 0;
-            for (int i = 0; i < V; ++i) tv_[(size_t)nt * V + i] = tv_[(size_t)b.c * V + i];
-            tv_[(size_t)nt * V + b.j] = p;
-            tn_[(size_t)nt * V + b.j] = b.nb;
+            for (int i = 0; i < V; ++i) T_[(size_t)nt * S + i] = T_[(size_t)b.c * S + i];
+            T_[(size_t)nt * S + b.j] = p;
+            T_[(size_t)nt * S + V + b.j] = b.nb;
             if (b.nb >= 0)
                 for (int i = 0; i < V; ++i)
-                    if (tn_[(size_t)b.nb * V + i] == b.c) {
-                        tn_[(size_t)b.nb * V + i] = nt;
+                    if (T_[(size_t)b.nb * S + V + i] == b.c) {
+                        T_[(size_t)b.nb * S + V + i] = nt;
                         break;
                     }
             for (int k = 0; k < V; ++k) {
@@ -518,11 +522,11 @@ private:
                 uint64_t key;
                 if constexpr (D == 2) {
                     const int o = 3 - k - b.j;
-                    key = (uint64_t)(uint32_t)tv_[(size_t)nt * V + o] + 1;
+                    key = (uint64_t)(uint32_t)T_[(size_t)nt * S + o] + 1;
                 } else {
                     int r[2], m = 0;
                     for (int i = 0; i < 4; ++i)
-                        if (i != k && i != b.j) r[m++] = tv_[(size_t)nt * V + i];
+                        if (i != k && i != b.j) r[m++] = T_[(size_t)nt * S + i];
                     const uint32_t lo = (uint32_t)std::min(r[0], r[1]), hi = (uint32_t)std::max(r[0], r[1]);
                     key = (((uint64_t)hi << 32) | lo) + 1;
                 }
@@ -531,13 +535,13 @@ private:
                     if (hstamp_[h] != stamp_) {
                         hstamp_[h] = stamp_;
                         hkey_[h] = key;
-                        hval_[h] = nt * V + k;
+                        hval_[h] = nt * S + V + k;
                         break;
                     }
                     if (hkey_[h] == key) {
                         const int o = hval_[h];
-                        tn_[(size_t)nt * V + k] = o / V;
-                        tn_[o] = nt;
+                        T_[(size_t)nt * S + V + k] = o / S;
+                        T_[o] = nt;
                         hkey_[h] = ~0ull;  // matched: a ridge joins exactly two new faces
                         break;
                     }
