@@ -356,8 +356,8 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     c->prm = *params;
     c->dim = params->dim;
     c->npe = params->dim + 1;
-    // pair assembly: the pair-parallel kernel with 128 threads per block (the item-parallel form
-    // measured slower on the 2D and 3D dam breaks, the autotuner may still pick it)
+    // pair assembly: 128 = the row-staged kernel (64 = pair-parallel from global memory, 256 =
+    // item-parallel; the autotuner compares the three)
     c->tune = pfg_tuning{params->dim == 2 ? 4 : 8, 128, BLOCK, 64, params->dim == 2 ? 4 : 8};
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -393,7 +393,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force,
                     &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
                     &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
-                    &c->pe_ptr, &c->pe_item, &c->pe_pair, &c->el_slot, &c->ne_slot, &c->conn_s, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
+                    &c->pe_ptr, &c->pe_item, &c->pe_pair, &c->pe_pos, &c->el_slot, &c->ne_slot, &c->conn_s, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
                     &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos, &c->mx_vsum, &c->wch_rec, &c->fs_gauge, &c->fs_rp, &c->fs_col, &c->fs_val, &c->fs_lval, &c->fs_mval, &c->fs_vec, &c->fs_cg, &c->fs_red, &c->lu_front, &c->lu_nodes,
                     &c->lu_recs, &c->lu_kids, &c->lu_maps, &c->lu_piv, &c->lu_mat, &c->lu_vec, &c->lu_list,
                     &c->lu_r, &c->lu_one};

@@ -98,6 +98,7 @@ struct pfg_ctx {
     // mixed PSPG: element list of each off-diagonal node pair (slot(e)*16 + i*4 + j, ascending e)
     pfg::DBuf pe_ptr, pe_item;
     pfg::DBuf pe_pair;        // the pair of each item (item-parallel pair assembly)
+    pfg::DBuf pe_pos;         // each item as (position in the row's incidences) * 16 + i * 4 + j
     long long n_items = 0;    // pair element items, E (d+1) d
     // mixed assembly: slot of each element in the element-major data (elements ordered by their
     // smallest node) and the slot of each incidence's element

@@ -225,7 +225,9 @@ __global__ void k_conn_slots(int E, int npe, const int* __restrict__ conn, const
 }
 
 // Element lists of the off-diagonal node pairs: pair p = (n, m), m != n, lists every element
-// containing both, ascending, as slot(e) * 16 + (local index of n) * 4 + (local index of m).  One
+// containing both, ascending, as slot(e) * 16 + (local index of n) * 4 + (local index of m), and
+// the same items with the element's position in n's incidence list instead of its slot (pe_pos,
+// for the row-staged assembly).  One
 // thread per node n owns the lists of n's pairs and walks n's sorted incidences, so each list
 // comes out in ascending element order.  FILL = false counts, FILL = true writes.
 template <bool FILL>
@@ -233,7 +235,7 @@ __global__ void k_pair_items(int N, int npe, int E, const int* __restrict__ conn
                              const int* __restrict__ ne_elem, const uint8_t* __restrict__ ne_loc,
                              const int* __restrict__ nbr_ptr, const int* __restrict__ nbr, int* __restrict__ cnt,
                              const int* __restrict__ pe_ptr, int* __restrict__ pe_item, int* __restrict__ pe_pair,
-                             const int* __restrict__ el_slot) {
+                             const int* __restrict__ el_slot, int* __restrict__ pe_pos) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     const int b0 = nbr_ptr[n], b1 = nbr_ptr[n + 1];
@@ -246,6 +248,7 @@ __global__ void k_pair_items(int N, int npe, int E, const int* __restrict__ conn
             if (FILL)
             {
                 pe_pair[pe_ptr[p] + cnt[p]] = p;
+                pe_pos[pe_ptr[p] + cnt[p]] = ((q - ne_ptr[n]) << 4) | (i << 2) | j;
                 pe_item[pe_ptr[p] + cnt[p]++] = (el_slot[e] << 4) | (i << 2) | j;
             }
             else
@@ -445,12 +448,13 @@ int build_topology(pfg_ctx* c) {
         k_pair_items<false><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
                                                                    ptr<int>(c->ne_elem), ptr<uint8_t>(c->ne_loc),
                                                                    ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
-                                                                   nullptr, nullptr, nullptr, nullptr);
+                                                                   nullptr, nullptr, nullptr, nullptr, nullptr);
         PFG_CHECK_LAUNCH(c);
         TRY(scan_exclusive(c, ptr<int>(cnt), ptr<int>(c->pe_ptr), c->P, tmp));
         const long long items = (long long)E * npe * (npe - 1);
         TRY(ensure(c, c->pe_item, sizeof(int) * (size_t)std::max<long long>(items, 1)));
         TRY(ensure(c, c->pe_pair, sizeof(int) * (size_t)std::max<long long>(items, 1)));
+        TRY(ensure(c, c->pe_pos, sizeof(int) * (size_t)std::max<long long>(items, 1)));
         c->n_items = items;
         PFG_CUDA(c, cudaMemsetAsync(cnt.p, 0, sizeof(int) * (size_t)c->P, c->stream));
         k_pair_items<true><<<div_up(N, 128), 128, 0, c->stream>>>(N, npe, E, ptr<int>(c->conn), ptr<int>(c->ne_ptr),
@@ -458,7 +462,7 @@ int build_topology(pfg_ctx* c) {
                                                                   ptr<int>(c->nbr_ptr), ptr<int>(c->nbr), ptr<int>(cnt),
                                                                   ptr<int>(c->pe_ptr), ptr<int>(c->pe_item),
                                                                   ptr<int>(c->pe_pair),
-                                                                  ptr<int>(c->el_slot));
+                                                                  ptr<int>(c->el_slot), ptr<int>(c->pe_pos));
         PFG_CHECK_LAUNCH(c);
     }
 

@@ -202,8 +202,10 @@ __device__ __forceinline__ bool inst_reduce(T (&v)[NV], int b, int b0, int b1, T
 //   k_mx_node    node: its own (d+1)^2 block, its right-hand side in double-float, the node
 //                boundary conditions, the row scales, the block inverses, the scaled diagonal
 //                block of the FP32 system and ||b||^2 per instance;
-//   k_mx_asm32   node pair: the off-diagonal blocks of the scaled FP32 system from the pair's
-//                element list.
+//   k_mx_asm32_rows  node pair: the off-diagonal blocks of the scaled FP32 system from the
+//                pair's element list, the element records of a block's rows staged in shared
+//                memory (k_mx_asm32 reads them from global memory; k_mx_asm32_items is the
+//                item-parallel form; the tuner picks among the three).
 // The FP32 system only steers the correction solves; the refinement residual below is
 // evaluated matrix-free in double-float, so it alone decides the solution.  The FP64 CSR
 // values are assembled (k_mx_pairs, double-float) only for instances whose correction solves
@@ -224,6 +226,9 @@ __device__ __forceinline__ DF inst_df(const float* f32, int inst, int which) {
 // lines.  High and low parts are kept apart so that the FP32 gathers' L2 footprint is the high
 // parts alone.
 constexpr int ED_AOS = 16;
+// row-staged pair assembly: pairs per block and element records staged in shared memory
+constexpr int STAGE_PAIRS = 128;
+constexpr int STAGE_RECORDS = 384;
 struct EdPlanes {
     const float* ah;
     const float* al;
@@ -792,6 +797,57 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
     if (threadIdx.x == 0) m.id[inst * D_COUNT + D_BB] = v[0];
 }
 
+// One pair element item's FP32 contribution to the pair's (d+1)^2 block: element area ae, PSPG
+// tau, viscosity sum ks, shape gradients gi / gj of the pair's nodes (local indices i, j).
+template <int DIM>
+__device__ __forceinline__ void pair_item32(int i, int j, float ae_ref, float tau, float ks, const float (&gi)[DIM],
+                                            const float (&gj)[DIM], float cm, float inv_dt, float l_sum,
+                                            const MxConst& k, float (&a)[DIM + 1][DIM + 1]) {
+    const float ae = ae_ref * k.ref32;
+    const float kf = ae * ks;
+    float dot = gi[0] * gj[0];
+#pragma unroll
+    for (int f = 1; f < DIM; ++f) dot += gi[f] * gj[f];
+    const float mij = cm * k.mm32[i][j] * ae;
+    const float asj = ae * k.s32[j], asi = ae * k.s32[i];
+    const float ct = tau * inv_dt;
+#pragma unroll
+    for (int f1 = 0; f1 < DIM; ++f1) {
+#pragma unroll
+        for (int f2 = 0; f2 < DIM; ++f2) a[f1][f2] += kf * ((f1 == f2 ? dot : 0.0f) + gi[f2] * gj[f1]);
+        a[f1][f1] += mij;
+        a[f1][DIM] -= asj * gi[f1];
+        a[DIM][f1] += ct * asj * gi[f1] + asi * gj[f1];
+    }
+    a[DIM][DIM] += tau * ae * l_sum * dot;
+}
+
+// The row / column BCs and scales of an off-diagonal block, stored with its bfloat16 copy.
+template <int DIM>
+__device__ __forceinline__ void pair_finish32(int p, int n, int mm, uint8_t fn, uint8_t fm, int N,
+                                              const float* __restrict__ scale32, const float (&a)[DIM + 1][DIM + 1],
+                                              float* __restrict__ blk, uint16_t* __restrict__ blk16) {
+    constexpr int B = DIM + 1;
+    const bool bound = fn & F_BOUND;
+    const bool mdir = (fm & F_BOUND) && (fm & F_DIRICHLET);
+    float sn[B], sm[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        sn[f] = scale32[(size_t)f * N + n];
+        sm[f] = scale32[(size_t)f * N + mm];
+    }
+    float out[B * B];
+#pragma unroll
+    for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+        for (int f2 = 0; f2 < B; ++f2) {
+            float v = a[f1][f2];
+            if ((fn & F_FREE) || (bound && f1 < DIM) || (mdir && f2 < DIM)) v = 0.0f;
+            out[f1 * B + f2] = sn[f1] * v * sm[f2];
+        }
+    store_block32<B>(blk, blk16, p, out);
+}
+
 // Off-diagonal blocks of the scaled FP32 system, one thread per node pair p = (n, m), m != n:
 // the pair's elements in ascending order (FP32 arithmetic with the element formulas of
 // pspg_pair_block, or with DFA double-float arithmetic rounded once), the identity rows of
@@ -865,47 +921,91 @@ __global__ void __launch_bounds__(BLOCK) k_mx_asm32(int P, int N, const int* __r
         for (int kk = k0; kk < k1; ++kk) {
             const Item cur = nxt;
             if (kk + 1 < k1) load(kk + 1, nxt);
-            const int i = cur.i, j = cur.j;
-            const float ae = cur.ae * k.ref32;
-            const float tau = cur.tau;
-            const float kf = ae * cur.ks;
-            const float(&gi)[DIM] = cur.gi;
-            const float(&gj)[DIM] = cur.gj;
-            float dot = gi[0] * gj[0];
-#pragma unroll
-            for (int f = 1; f < DIM; ++f) dot += gi[f] * gj[f];
-            const float mij = cm * k.mm32[i][j] * ae;
-            const float asj = ae * k.s32[j], asi = ae * k.s32[i];
-            const float ct = tau * inv_dt;
-#pragma unroll
-            for (int f1 = 0; f1 < DIM; ++f1) {
-#pragma unroll
-                for (int f2 = 0; f2 < DIM; ++f2) a[f1][f2] += kf * ((f1 == f2 ? dot : 0.0f) + gi[f2] * gj[f1]);
-                a[f1][f1] += mij;
-                a[f1][DIM] -= asj * gi[f1];
-                a[DIM][f1] += ct * asj * gi[f1] + asi * gj[f1];
-            }
-            a[DIM][DIM] += tau * ae * l_sum * dot;
+            pair_item32<DIM>(cur.i, cur.j, cur.ae, cur.tau, cur.ks, cur.gi, cur.gj, cm, inv_dt, l_sum, k, a);
         }
     }
-    const bool bound = fn & F_BOUND;
-    const bool mdir = (fm & F_BOUND) && (fm & F_DIRICHLET);
-    float sn[B], sm[B];
-#pragma unroll
-    for (int f = 0; f < B; ++f) {
-        sn[f] = scale32[(size_t)f * N + n];
-        sm[f] = scale32[(size_t)f * N + mm];
+    pair_finish32<DIM>(p, n, mm, fn, fm, N, scale32, a, blk, blk16);
+}
+
+// Row-staged pair assembly (the FP32 default): a block takes 128 consecutive node pairs, which
+// belong to a run of consecutive rows; their element records (contiguous in the node-element
+// incidence arrays) are first copied into shared memory with independent loads, then every
+// thread sums its pair's items from there (same items, order and arithmetic as k_mx_asm32, so
+// the blocks are the same).  A block whose rows hold more records than fit reads them from
+// global memory instead.
+template <int DIM>
+__global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, const int* __restrict__ pair_node,
+                                                               const int* __restrict__ nbr,
+                                                               const int* __restrict__ pe_ptr,
+                                                               const int* __restrict__ pe_pos,
+                                                               const int* __restrict__ ne_ptr,
+                                                               const int* __restrict__ ne_slot, EdPlanes ed,
+                                                               const uint8_t* __restrict__ flags,
+                                                               const float* __restrict__ scale32,
+                                                               const float* __restrict__ f32, Mx m, MxConst k,
+                                                               float* __restrict__ blk, uint16_t* __restrict__ blk16) {
+    constexpr int B = DIM + 1, NPE = DIM + 1;
+    __shared__ float4 srec[STAGE_RECORDS * (ED_AOS / 4)];
+    const int p0 = blockIdx.x * STAGE_PAIRS;
+    const int pe = min(p0 + STAGE_PAIRS, P);
+    const int nf = pair_node[p0], nl = pair_node[pe - 1];
+    const int q0 = ne_ptr[nf], nrec = ne_ptr[nl + 1] - q0;
+    const bool staged = nrec <= STAGE_RECORDS;
+    if (staged) {
+        const float4* src = reinterpret_cast<const float4*>(ed.ah);
+        for (int t = threadIdx.x; t < nrec * (ED_AOS / 4); t += STAGE_PAIRS) {
+            const int r = t / (ED_AOS / 4), c = t % (ED_AOS / 4);
+            srec[t] = __ldg(src + (size_t)__ldg(ne_slot + q0 + r) * (ED_AOS / 4) + c);
+        }
     }
-    float out[B * B];
+    __syncthreads();
+    const int p = p0 + threadIdx.x;
+    if (p >= pe) return;
+    const int n = pair_node[p];
+    const int mm = nbr[p];
+    if (mm == n) return;  // diagonal blocks: k_mx_node
+    const int inst = m.node_inst[n];
+    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
+    const uint8_t fn = flags[n], fm = flags[mm];
+    float a[B][B];
 #pragma unroll
     for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
-        for (int f2 = 0; f2 < B; ++f2) {
-            float v = a[f1][f2];
-            if ((fn & F_FREE) || (bound && f1 < DIM) || (mdir && f2 < DIM)) v = 0.0f;
-            out[f1 * B + f2] = sn[f1] * v * sm[f2];
+        for (int f2 = 0; f2 < B; ++f2) a[f1][f2] = 0.0f;
+    if (!(fn & F_FREE)) {
+        const float cm = f32[inst * F_COUNT + F_CM], inv_dt = f32[inst * F_COUNT + F_INVDT];
+        const float l_sum = f32[inst * F_COUNT + F_LSUM];
+        const int base = ne_ptr[n] - q0;
+        const float* sr = reinterpret_cast<const float*>(srec);
+        for (int kk = pe_ptr[p], k1 = pe_ptr[p + 1]; kk < k1; ++kk) {
+            const int it = __ldg(pe_pos + kk);
+            const int r = base + (it >> 4), i = (it >> 2) & 3, j = it & 3;
+            float ae, tau, ks, gi[DIM], gj[DIM];
+            if (staged) {
+                const float* rec = sr + (size_t)r * ED_AOS;
+                ae = rec[0];
+                tau = rec[1];
+                ks = rec[ed_ksum<DIM>()];
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) {
+                    gi[f] = rec[2 + f * NPE + i];
+                    gj[f] = rec[2 + f * NPE + j];
+                }
+            } else {
+                const int e = __ldg(ne_slot + q0 + r);
+                ae = ed.gf(0, e);
+                tau = ed.gf(1, e);
+                ks = ed.gf(ed_ksum<DIM>(), e);
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) {
+                    gi[f] = ed.gf(2 + f * NPE + i, e);
+                    gj[f] = ed.gf(2 + f * NPE + j, e);
+                }
+            }
+            pair_item32<DIM>(i, j, ae, tau, ks, gi, gj, cm, inv_dt, l_sum, k, a);
         }
-    store_block32<B>(blk, blk16, p, out);
+    }
+    pair_finish32<DIM>(p, n, mm, fn, fm, N, scale32, a, blk, blk16);
 }
 
 // Off-diagonal blocks of the scaled FP32 system, item-parallel (the FP32 assembly's default):
@@ -1772,8 +1872,14 @@ int mx_assemble(pfg_ctx* c, const double* q_iter, const MxConst& k) {
     prof_end(c, PH_PSPG_RHS);
     PFG_CHECK_LAUNCH(c);
     prof_begin(c, PH_PSPG_PAIRS);
-    if (dfa || c->tune.pair_block != ASM_ITEMS) {
-        // double-float pair arithmetic, or the tuned pair-parallel shape
+    if (!dfa && c->tune.pair_block == STAGE_PAIRS) {
+        // the row-staged FP32 pair kernel (default)
+        k_mx_asm32_rows<DIM><<<div_up(c->P, STAGE_PAIRS), STAGE_PAIRS, 0, c->stream>>>(
+            c->P, N, ptr<int>(c->pair_node), ptr<int>(c->nbr), ptr<int>(c->pe_ptr), ptr<int>(c->pe_pos),
+            ptr<int>(c->ne_ptr), ptr<int>(c->ne_slot), ed, ptr<uint8_t>(c->flags), ptr<float>(c->mx_scale32),
+            ptr<float>(c->mx_f32), m, k, ptr<float>(c->val32), v16);
+    } else if (dfa || c->tune.pair_block != ASM_ITEMS) {
+        // double-float pair arithmetic, or the pair-parallel kernel reading global memory
         auto pair_kernel = dfa ? k_mx_asm32<DIM, true> : k_mx_asm32<DIM, false>;
         const int pb = dfa ? BLOCK : c->tune.pair_block;
         pair_kernel<<<div_up(c->P, pb), pb, 0, c->stream>>>(

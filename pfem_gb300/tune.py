@@ -27,7 +27,7 @@ PHASE = {"spmv_lanes": "Krylov SpMV", "pair_block": "PSPG matrix", "elem_block":
 def candidates(dim):
     l0 = LANES0[dim]
     lanes = (l0, l0 // 2, 2 * l0)
-    blocks = (128, 256, 64)  # pair assembly: 256 = the item-parallel form
+    blocks = (128, 256, 64)  # pair assembly: 128 row-staged, 256 item-parallel, 64 pair-parallel
     res = (64, 32, 64)
     return [dict(spmv_lanes=lanes[i], pair_block=blocks[i], elem_block=blocks[i], res_block=res[i],
                  mg_lanes=lanes[i]) for i in range(3)]
