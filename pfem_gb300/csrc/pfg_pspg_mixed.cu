@@ -229,6 +229,7 @@ constexpr int ED_AOS = 16;
 // row-staged pair assembly: pairs per block and element records staged in shared memory
 constexpr int STAGE_PAIRS = 128;
 constexpr int STAGE_RECORDS = 384;
+constexpr int STAGE_ITEMS = 1024;
 struct EdPlanes {
     const float* ah;
     const float* al;
@@ -824,18 +825,12 @@ __device__ __forceinline__ void pair_item32(int i, int j, float ae_ref, float ta
 
 // The row / column BCs and scales of an off-diagonal block, stored with its bfloat16 copy.
 template <int DIM>
-__device__ __forceinline__ void pair_finish32(int p, int n, int mm, uint8_t fn, uint8_t fm, int N,
-                                              const float* __restrict__ scale32, const float (&a)[DIM + 1][DIM + 1],
+__device__ __forceinline__ void pair_finish32(int p, uint8_t fn, uint8_t fm, const float (&sn)[DIM + 1],
+                                              const float (&sm)[DIM + 1], const float (&a)[DIM + 1][DIM + 1],
                                               float* __restrict__ blk, uint16_t* __restrict__ blk16) {
     constexpr int B = DIM + 1;
     const bool bound = fn & F_BOUND;
     const bool mdir = (fm & F_BOUND) && (fm & F_DIRICHLET);
-    float sn[B], sm[B];
-#pragma unroll
-    for (int f = 0; f < B; ++f) {
-        sn[f] = scale32[(size_t)f * N + n];
-        sm[f] = scale32[(size_t)f * N + mm];
-    }
     float out[B * B];
 #pragma unroll
     for (int f1 = 0; f1 < B; ++f1)
@@ -924,15 +919,21 @@ __global__ void __launch_bounds__(BLOCK) k_mx_asm32(int P, int N, const int* __r
             pair_item32<DIM>(cur.i, cur.j, cur.ae, cur.tau, cur.ks, cur.gi, cur.gj, cm, inv_dt, l_sum, k, a);
         }
     }
-    pair_finish32<DIM>(p, n, mm, fn, fm, N, scale32, a, blk, blk16);
+    float sn[B], sm[B];
+#pragma unroll
+    for (int f = 0; f < B; ++f) {
+        sn[f] = scale32[(size_t)f * N + n];
+        sm[f] = scale32[(size_t)f * N + mm];
+    }
+    pair_finish32<DIM>(p, fn, fm, sn, sm, a, blk, blk16);
 }
 
 // Row-staged pair assembly (the FP32 default): a block takes 128 consecutive node pairs, which
-// belong to a run of consecutive rows; their element records (contiguous in the node-element
-// incidence arrays) are first copied into shared memory with independent loads, then every
-// thread sums its pair's items from there (same items, order and arithmetic as k_mx_asm32, so
-// the blocks are the same).  A block whose rows hold more records than fit reads them from
-// global memory instead.
+// belong to a run of consecutive rows.  Their element records (contiguous in the node-element
+// incidence arrays) and their item lists (contiguous in pe_pos) are first copied into shared
+// memory with independent loads; then every thread sums its pair's items from there (same
+// items, order and arithmetic as k_mx_asm32, so the blocks are the same).  A block whose rows
+// hold more records or items than fit reads them from global memory instead.
 template <int DIM>
 __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, const int* __restrict__ pair_node,
                                                                const int* __restrict__ nbr,
@@ -946,25 +947,38 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
                                                                float* __restrict__ blk, uint16_t* __restrict__ blk16) {
     constexpr int B = DIM + 1, NPE = DIM + 1;
     __shared__ float4 srec[STAGE_RECORDS * (ED_AOS / 4)];
+    __shared__ int sitem[STAGE_ITEMS];
     const int p0 = blockIdx.x * STAGE_PAIRS;
     const int pe = min(p0 + STAGE_PAIRS, P);
     const int nf = pair_node[p0], nl = pair_node[pe - 1];
     const int q0 = ne_ptr[nf], nrec = ne_ptr[nl + 1] - q0;
-    const bool staged = nrec <= STAGE_RECORDS;
-    if (staged) {
+    const int i0 = pe_ptr[p0], nit = pe_ptr[pe] - i0;
+    const bool rec_staged = nrec <= STAGE_RECORDS, it_staged = nit <= STAGE_ITEMS;
+    if (rec_staged) {
         const float4* src = reinterpret_cast<const float4*>(ed.ah);
         for (int t = threadIdx.x; t < nrec * (ED_AOS / 4); t += STAGE_PAIRS) {
             const int r = t / (ED_AOS / 4), c = t % (ED_AOS / 4);
             srec[t] = __ldg(src + (size_t)__ldg(ne_slot + q0 + r) * (ED_AOS / 4) + c);
         }
     }
-    __syncthreads();
+    if (it_staged)
+        for (int t = threadIdx.x; t < nit; t += STAGE_PAIRS) sitem[t] = __ldg(pe_pos + i0 + t);
     const int p = p0 + threadIdx.x;
-    if (p >= pe) return;
-    const int n = pair_node[p];
-    const int mm = nbr[p];
-    if (mm == n) return;  // diagonal blocks: k_mx_node
-    const int inst = m.node_inst[n];
+    const bool live = p < pe;
+    int n = 0, mm = 0, inst = 0;
+    float sn[B], sm[B];
+    if (live) {
+        n = pair_node[p];
+        mm = nbr[p];
+        inst = m.node_inst[n];
+#pragma unroll
+        for (int f = 0; f < B; ++f) {
+            sn[f] = scale32[(size_t)f * N + n];
+            sm[f] = scale32[(size_t)f * N + mm];
+        }
+    }
+    __syncthreads();
+    if (!live || mm == n) return;  // diagonal blocks: k_mx_node
     if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
     const uint8_t fn = flags[n], fm = flags[mm];
     float a[B][B];
@@ -978,10 +992,10 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
         const int base = ne_ptr[n] - q0;
         const float* sr = reinterpret_cast<const float*>(srec);
         for (int kk = pe_ptr[p], k1 = pe_ptr[p + 1]; kk < k1; ++kk) {
-            const int it = __ldg(pe_pos + kk);
+            const int it = it_staged ? sitem[kk - i0] : __ldg(pe_pos + kk);
             const int r = base + (it >> 4), i = (it >> 2) & 3, j = it & 3;
             float ae, tau, ks, gi[DIM], gj[DIM];
-            if (staged) {
+            if (rec_staged) {
                 const float* rec = sr + (size_t)r * ED_AOS;
                 ae = rec[0];
                 tau = rec[1];
@@ -1005,7 +1019,7 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
             pair_item32<DIM>(i, j, ae, tau, ks, gi, gj, cm, inv_dt, l_sum, k, a);
         }
     }
-    pair_finish32<DIM>(p, n, mm, fn, fm, N, scale32, a, blk, blk16);
+    pair_finish32<DIM>(p, fn, fm, sn, sm, a, blk, blk16);
 }
 
 // Off-diagonal blocks of the scaled FP32 system, item-parallel (the FP32 assembly's default):
