@@ -228,8 +228,8 @@ __device__ __forceinline__ DF inst_df(const float* f32, int inst, int which) {
 constexpr int ED_AOS = 16;
 // row-staged pair assembly: pairs per block and element records staged in shared memory
 constexpr int STAGE_PAIRS = 128;
-constexpr int STAGE_RECORDS = 384;
-constexpr int STAGE_ITEMS = 1024;
+constexpr int STAGE_RECORDS = 320;
+constexpr int STAGE_ITEMS = 768;
 struct EdPlanes {
     const float* ah;
     const float* al;
@@ -954,44 +954,53 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
     const int q0 = ne_ptr[nf], nrec = ne_ptr[nl + 1] - q0;
     const int i0 = pe_ptr[p0], nit = pe_ptr[pe] - i0;
     const bool rec_staged = nrec <= STAGE_RECORDS, it_staged = nit <= STAGE_ITEMS;
+    // every global load of the block is issued before the barrier: the staging copies (four
+    // in flight per thread) and each thread's own pair data
     if (rec_staged) {
         const float4* src = reinterpret_cast<const float4*>(ed.ah);
+#pragma unroll 4
         for (int t = threadIdx.x; t < nrec * (ED_AOS / 4); t += STAGE_PAIRS) {
             const int r = t / (ED_AOS / 4), c = t % (ED_AOS / 4);
             srec[t] = __ldg(src + (size_t)__ldg(ne_slot + q0 + r) * (ED_AOS / 4) + c);
         }
     }
     if (it_staged)
+#pragma unroll 4
         for (int t = threadIdx.x; t < nit; t += STAGE_PAIRS) sitem[t] = __ldg(pe_pos + i0 + t);
     const int p = p0 + threadIdx.x;
     const bool live = p < pe;
-    int n = 0, mm = 0, inst = 0;
-    float sn[B], sm[B];
+    int n = 0, mm = 0, inst = 0, kb = 0, ke = 0, base = 0, active = 0;
+    uint8_t fn = F_FREE, fm = 0;
+    float sn[B], sm[B], cm = 0.0f, inv_dt = 0.0f, l_sum = 0.0f;
     if (live) {
         n = pair_node[p];
         mm = nbr[p];
+        kb = pe_ptr[p];
+        ke = pe_ptr[p + 1];
         inst = m.node_inst[n];
+        fn = flags[n];
+        fm = flags[mm];
+        base = ne_ptr[n] - q0;
 #pragma unroll
         for (int f = 0; f < B; ++f) {
             sn[f] = scale32[(size_t)f * N + n];
             sm[f] = scale32[(size_t)f * N + mm];
         }
+        active = m.ii[inst * I_COUNT + I_ACTIVE];
+        cm = f32[inst * F_COUNT + F_CM];
+        inv_dt = f32[inst * F_COUNT + F_INVDT];
+        l_sum = f32[inst * F_COUNT + F_LSUM];
     }
     __syncthreads();
-    if (!live || mm == n) return;  // diagonal blocks: k_mx_node
-    if (!m.ii[inst * I_COUNT + I_ACTIVE]) return;
-    const uint8_t fn = flags[n], fm = flags[mm];
+    if (!live || mm == n || !active) return;  // diagonal blocks: k_mx_node
     float a[B][B];
 #pragma unroll
     for (int f1 = 0; f1 < B; ++f1)
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2) a[f1][f2] = 0.0f;
     if (!(fn & F_FREE)) {
-        const float cm = f32[inst * F_COUNT + F_CM], inv_dt = f32[inst * F_COUNT + F_INVDT];
-        const float l_sum = f32[inst * F_COUNT + F_LSUM];
-        const int base = ne_ptr[n] - q0;
         const float* sr = reinterpret_cast<const float*>(srec);
-        for (int kk = pe_ptr[p], k1 = pe_ptr[p + 1]; kk < k1; ++kk) {
+        for (int kk = kb; kk < ke; ++kk) {
             const int it = it_staged ? sitem[kk - i0] : __ldg(pe_pos + kk);
             const int r = base + (it >> 4), i = (it >> 2) & 3, j = it & 3;
             float ae, tau, ks, gi[DIM], gj[DIM];
