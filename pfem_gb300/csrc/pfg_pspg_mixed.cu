@@ -946,7 +946,10 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
                                                                const float* __restrict__ f32, Mx m, MxConst k,
                                                                float* __restrict__ blk, uint16_t* __restrict__ blk16) {
     constexpr int B = DIM + 1, NPE = DIM + 1;
-    __shared__ float4 srec[STAGE_RECORDS * (ED_AOS / 4)];
+    // records at an odd stride (17 floats): the threads of a warp read the same field of
+    // different records from different banks
+    constexpr int RS = ED_AOS + 1;
+    __shared__ float srec[STAGE_RECORDS * RS];
     __shared__ int sitem[STAGE_ITEMS];
     const int p0 = blockIdx.x * STAGE_PAIRS;
     const int pe = min(p0 + STAGE_PAIRS, P);
@@ -961,7 +964,12 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
 #pragma unroll 4
         for (int t = threadIdx.x; t < nrec * (ED_AOS / 4); t += STAGE_PAIRS) {
             const int r = t / (ED_AOS / 4), c = t % (ED_AOS / 4);
-            srec[t] = __ldg(src + (size_t)__ldg(ne_slot + q0 + r) * (ED_AOS / 4) + c);
+            const float4 v = __ldg(src + (size_t)__ldg(ne_slot + q0 + r) * (ED_AOS / 4) + c);
+            float* d = srec + r * RS + 4 * c;
+            d[0] = v.x;
+            d[1] = v.y;
+            d[2] = v.z;
+            d[3] = v.w;
         }
     }
     if (it_staged)
@@ -999,13 +1007,12 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
 #pragma unroll
         for (int f2 = 0; f2 < B; ++f2) a[f1][f2] = 0.0f;
     if (!(fn & F_FREE)) {
-        const float* sr = reinterpret_cast<const float*>(srec);
         for (int kk = kb; kk < ke; ++kk) {
             const int it = it_staged ? sitem[kk - i0] : __ldg(pe_pos + kk);
             const int r = base + (it >> 4), i = (it >> 2) & 3, j = it & 3;
             float ae, tau, ks, gi[DIM], gj[DIM];
             if (rec_staged) {
-                const float* rec = sr + (size_t)r * ED_AOS;
+                const float* rec = srec + r * RS;
                 ae = rec[0];
                 tau = rec[1];
                 ks = rec[ed_ksum<DIM>()];
