@@ -766,13 +766,14 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
                 else if (dir && f2 < DIM && f1 != f2) v = 0.0f;
                 a[f1][f2] = v;
             }
-        float s[B];  // S = |a_rr|^-1/2 (FP64 root of the FP32 diagonal)
+        // S = |a_rr|^-1/2, correctly rounded in FP32 (the FP64 scale of the refinement is its
+        // exact copy, so both precisions scale by the same numbers; no FP64 root or division)
+        float s[B];
 #pragma unroll
         for (int f = 0; f < B; ++f) {
-            const double d = fabs((double)a[f][f]);
-            const double sd = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
-            scale[(size_t)f * N + n] = sd;
-            s[f] = (float)sd;
+            const float d = fabsf(a[f][f]);
+            s[f] = d > 0.0f ? __frsqrt_rn(d) : 1.0f;
+            scale[(size_t)f * N + n] = (double)s[f];
             scale32[(size_t)f * N + n] = s[f];
         }
         float sas[B][B], inv[B][B];
