@@ -597,7 +597,7 @@ __device__ __forceinline__ void store_block32(float* __restrict__ blk, uint16_t*
 // which is the element sum of F_i + (M/dt) v_prev and tau H_i + (tau/dt) C v_prev
 // (MomContEquationPSPG.inl:48-96) regrouped; otherwise the element expressions term by term.
 template <int DIM, bool DFA>
-__global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* __restrict__ ne_ptr,
+__global__ void __launch_bounds__(NB, 10) k_mx_node(Mx m, int N, int E, const int* __restrict__ ne_ptr,
                                                 const int* __restrict__ ne_elem, const int* __restrict__ ne_slot,
                                                 const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
                                                 EdPlanes ed, const uint8_t* __restrict__ flags,
@@ -955,6 +955,10 @@ __global__ void __launch_bounds__(STAGE_PAIRS) k_mx_asm32_rows(int P, int N, con
     const int p0 = blockIdx.x * STAGE_PAIRS;
     const int pe = min(p0 + STAGE_PAIRS, P);
     const int nf = pair_node[p0], nl = pair_node[pe - 1];
+    {  // a block inside one instance that no longer iterates (a batch's converged instance)
+        const int i_f = m.node_inst[nf];
+        if (i_f == m.node_inst[nl] && !m.ii[i_f * I_COUNT + I_ACTIVE]) return;
+    }
     const int q0 = ne_ptr[nf], nrec = ne_ptr[nl + 1] - q0;
     const int i0 = pe_ptr[p0], nit = pe_ptr[pe] - i0;
     const bool rec_staged = nrec <= STAGE_RECORDS, it_staged = nit <= STAGE_ITEMS;
