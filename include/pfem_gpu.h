@@ -423,8 +423,9 @@ PFG_API int pfg_heat_step(pfg_ctx* ctx, double dt, pfg_step_status* st);
  * Launch shapes of the kernels whose best shape depends on the mesh and the device: lanes per
  * node of the Krylov SpMV and of the multigrid's level-0 sweeps (node_lanes / 2, node_lanes or
  * 2 node_lanes, node_lanes = 4 in 2D and 8 in 3D); the pair assembly's form: 128 = row-staged (one thread per node
- * pair, 128 pairs per block, their rows' element records staged in shared memory; default),
- * 64 = pair-parallel reading the element records from global memory, 256 = item-parallel (one
+ * pair, 128 pairs per block, their rows' element records staged in shared memory; the 3D
+ * default), 64 = pair-parallel reading the element records from global memory (the 2D
+ * default), 256 = item-parallel (one
  * thread per pair element item, 256 items per block); threads
  * per block of the element prep (64, 128 or 256) and of the refinement residual's element
  * kernel (32 or 64).  A zero field keeps the current value.  The FP32 system depends on the

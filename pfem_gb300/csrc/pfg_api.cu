@@ -356,9 +356,10 @@ PFG_API int pfg_create(const pfg_params* params, pfg_ctx** out) {
     c->prm = *params;
     c->dim = params->dim;
     c->npe = params->dim + 1;
-    // pair assembly: 128 = the row-staged kernel (64 = pair-parallel from global memory, 256 =
-    // item-parallel; the autotuner compares the three)
-    c->tune = pfg_tuning{params->dim == 2 ? 4 : 8, 128, BLOCK, 64, params->dim == 2 ? 4 : 8};
+    // pair assembly: the row-staged kernel (128) in 3D, where a pair has ~5 element items; in 2D
+    // (~2 items per pair) the pair-parallel kernel reading global memory (64) does as well or
+    // better; 256 = item-parallel.  The autotuner compares the three.
+    c->tune = pfg_tuning{params->dim == 2 ? 4 : 8, params->dim == 2 ? 64 : 128, BLOCK, 64, params->dim == 2 ? 4 : 8};
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64 * sizeof(double));

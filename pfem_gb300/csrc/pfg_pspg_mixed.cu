@@ -597,7 +597,7 @@ __device__ __forceinline__ void store_block32(float* __restrict__ blk, uint16_t*
 // which is the element sum of F_i + (M/dt) v_prev and tau H_i + (tau/dt) C v_prev
 // (MomContEquationPSPG.inl:48-96) regrouped; otherwise the element expressions term by term.
 template <int DIM, bool DFA>
-__global__ void __launch_bounds__(NB, 10) k_mx_node(Mx m, int N, int E, const int* __restrict__ ne_ptr,
+__global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* __restrict__ ne_ptr,
                                                 const int* __restrict__ ne_elem, const int* __restrict__ ne_slot,
                                                 const uint8_t* __restrict__ ne_loc, const int* __restrict__ conn,
                                                 EdPlanes ed, const uint8_t* __restrict__ flags,
