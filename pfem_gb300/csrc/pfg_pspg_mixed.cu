@@ -1497,7 +1497,11 @@ __global__ void __launch_bounds__(NB) k_mx_res_node(Mx m, int N, const int* __re
     // seeds written this pass are valid unless the instance just crossed into FP64
     const bool need32 = need && nmode != MODE_FP64;
     const bool need64 = need && nmode == MODE_FP64 && fp64;
-    const double eta = k.eta;
+    // The correction solve's relative tolerance: eta, loosened for a sweep that needs less than
+    // that to meet the outer test (the last sweep of a solve): 0.2 of the remaining reduction
+    // tol / ||r||, at most 0.01, so that a successful sweep still shrinks ||r|| well past the
+    // tenfold progress test above.
+    const double eta = need && rr > 0.0 ? fmax(k.eta, fmin(0.01, 0.2 * tol / sqrt(rr))) : k.eta;
     sc[M_RHO] = (float)rs;
     sc[M_RHO_OLD] = 1.0f;
     sc[M_ALPHA] = 1.0f;
