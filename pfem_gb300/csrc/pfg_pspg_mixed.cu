@@ -43,7 +43,12 @@ constexpr int SPMV_BLOCK = 256;  // threads of the segment SpMV kernels
 // per-instance int fields
 // I_MODE: precision of the correction solves (0 FP32, 1 FP64); I_ROLL: undo the last sweep
 // I_M64: the FP64 CSR values of the instance are current for this assembly
-enum : int { I_B0 = 0, I_B1, I_N0, I_N1, I_ACTIVE, I_STATUS, I_IT, I_KIT, I_TICKET, I_MODE, I_ROLL, I_M64, I_COUNT = 12 };
+// I_LOOSE: the last correction solve ran at a loosened tolerance; I_TIGHT: loosening is off
+// for the rest of this linear solve
+enum : int {
+    I_B0 = 0, I_B1, I_N0, I_N1, I_ACTIVE, I_STATUS, I_IT, I_KIT, I_TICKET, I_MODE, I_ROLL, I_M64, I_LOOSE, I_TIGHT,
+    I_COUNT = 14
+};
 // correction-solve precision of an instance
 enum : int { MODE_FP32 = 0, MODE_FP64 = 2 };
 // per-instance double fields
@@ -1480,15 +1485,24 @@ __global__ void __launch_bounds__(NB) k_mx_res_node(Mx m, int N, const int* __re
     const double tol = fmax(k.rtol * sqrt(bb), k.atol);
     bool need = active && rr > tol * tol;
     const int mode = ii[I_MODE];  // the mode this pass seeded for
+    if (kind != RES_SWEEP) {  // a new linear solve
+        ii[I_LOOSE] = 0;
+        ii[I_TIGHT] = 0;
+    }
     if (kind == RES_SWEEP && mode == MODE_FP32 && need && !(rr <= 0.01 * rr_prev)) {
-        // an FP32 sweep that did not shrink ||r|| tenfold: FP64 from now on (and, if ||r||
-        // grew, the sweep is undone and the residual recomputed after)
-        ii[I_MODE] = MODE_FP64;
-        if (!(rr <= rr_prev)) {
-            ii[I_ROLL] = 1;
-            idd[D_RR] = rr_prev;
-            atomicAdd(m.cnt + C_ROLLBACK, 1);
-            need = false;
+        if (ii[I_LOOSE] && rr <= rr_prev) {
+            // a loosened sweep that fell short: the rest of this solve runs at eta
+            ii[I_TIGHT] = 1;
+        } else {
+            // an FP32 sweep that did not shrink ||r|| tenfold: FP64 from now on (and, if ||r||
+            // grew, the sweep is undone and the residual recomputed after)
+            ii[I_MODE] = MODE_FP64;
+            if (!(rr <= rr_prev)) {
+                ii[I_ROLL] = 1;
+                idd[D_RR] = rr_prev;
+                atomicAdd(m.cnt + C_ROLLBACK, 1);
+                need = false;
+            }
         }
     }
     const int nmode = ii[I_MODE];
@@ -1499,9 +1513,12 @@ __global__ void __launch_bounds__(NB) k_mx_res_node(Mx m, int N, const int* __re
     const bool need64 = need && nmode == MODE_FP64 && fp64;
     // The correction solve's relative tolerance: eta, loosened for a sweep that needs less than
     // that to meet the outer test (the last sweep of a solve): 0.2 of the remaining reduction
-    // tol / ||r||, at most 0.01, so that a successful sweep still shrinks ||r|| well past the
-    // tenfold progress test above.
-    const double eta = need && rr > 0.0 ? fmax(k.eta, fmin(0.01, 0.2 * tol / sqrt(rr))) : k.eta;
+    // tol / ||r||, at most 0.01.  A loosened sweep that misses the target and the tenfold test
+    // (the FP32 operator's own error adds to its reduction) turns loosening off for the rest of
+    // the solve instead of moving the instance to FP64.
+    const double eta =
+        need && rr > 0.0 && !ii[I_TIGHT] ? fmax(k.eta, fmin(0.01, 0.2 * tol / sqrt(rr))) : k.eta;
+    ii[I_LOOSE] = eta > k.eta;
     sc[M_RHO] = (float)rs;
     sc[M_RHO_OLD] = 1.0f;
     sc[M_ALPHA] = 1.0f;
