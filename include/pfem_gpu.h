@@ -116,7 +116,9 @@ typedef struct pfg_params {
     /* mixed precision, incompressible: */
     double inner_rel_tol;      /* FP32 correction solve stops at this fraction of its
                                   starting residual (0 = 1e-4; defaults: 1e-3 in 2D,
-                                  1e-4 in 3D)                                              */
+                                  5e-4 in 3D); a sweep that needs less to meet the linear
+                                  solve's tolerance stops at 0.2 of the remaining reduction
+                                  (at most 0.01)                                            */
     /* both kinds: */
     double gamma;              /* surface tension coefficient (MomContEq / MomEq "gamma");
                                   >= 1e-15 adds the facet term of m_applyBCPSPG

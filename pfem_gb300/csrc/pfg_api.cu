@@ -300,7 +300,7 @@ PFG_API int pfg_default_params(int32_t kind, int32_t dim, pfg_params* p) {
     p->heat_residual = PFG_RES_T;
     p->refine_max_iter = 30;
     // measured: a 330k-node 3D dam break steps 14% faster at 1e-4, the 2D cases 11% faster at 1e-3
-    p->inner_rel_tol = dim == 3 ? 1e-4 : 1e-3;
+    p->inner_rel_tol = dim == 3 ? 5e-4 : 1e-3;
     p->preconditioner = PFG_PC_MULTIGRID;
     p->K0 = 2.2e7;
     p->K0p = 7.0;
