@@ -79,8 +79,10 @@ __device__ __forceinline__ void block_row_bf16(int n, bool act, const int* __res
     for (int f = 0; f < B; ++f) y[f] = 0;
     const int b0 = act ? nbr_ptr[n] : 0;
     const int b1 = act ? nbr_ptr[n + 1] : 0;
-    // one neighbour block times x_m, added to y
-    auto acc = [&](int p, const float (&xm)[B]) {
+    for (int p = b0 + lane; p < b1; p += GN) {
+        const int mn = __ldg(nbr + p);
+        float xm[B];
+        xf.load(mn, xm);
         if constexpr (B == 4) {
             const uint4* a4 = reinterpret_cast<const uint4*>(blk + (size_t)p * 16);
 #pragma unroll
@@ -98,22 +100,6 @@ __device__ __forceinline__ void block_row_bf16(int n, bool act, const int* __res
                 y[f1] += bf16_lo(w.x) * xm[0] + bf16_hi(w.x) * xm[1] + bf16_lo(w.y) * xm[2];
             }
         }
-    };
-    // two neighbours per step (both indices, then both iterate reads, in flight together), each
-    // lane's products summed in the same order as one at a time
-    int p = b0 + lane;
-    for (; p + GN < b1; p += 2 * GN) {
-        const int m0 = __ldg(nbr + p), m1 = __ldg(nbr + p + GN);
-        float x0[B], x1[B];
-        xf.load(m0, x0);
-        xf.load(m1, x1);
-        acc(p, x0);
-        acc(p + GN, x1);
-    }
-    if (p < b1) {
-        float xm[B];
-        xf.load(__ldg(nbr + p), xm);
-        acc(p, xm);
     }
 #pragma unroll
     for (int f1 = 0; f1 < B; ++f1)

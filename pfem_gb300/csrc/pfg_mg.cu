@@ -199,40 +199,6 @@ __global__ void k_mg0_restrict(int nc, const int* __restrict__ mem_ptr, const in
 // Row operations as device functions, used by the one-level kernels and by the single-block
 // kernel that runs the small coarse levels (k_mg_tail).
 
-// y += (A x)_i over the blocks k0 + lane, k0 + lane + GN, ... of row i, two blocks per step
-// (both column indices, then both iterate reads, in flight together); each lane's products are
-// summed in the same order as one block at a time.
-template <int B, int GN, class XF>
-__device__ __forceinline__ void row_acc(int k0, int k1, int lane, const int* __restrict__ bcol,
-                                        const float* __restrict__ val, const XF& xf, float (&y)[B]) {
-    int k = k0 + lane;
-    for (; k + GN < k1; k += 2 * GN) {
-        const int c0 = bcol[k], c1 = bcol[k + GN];
-        float x0[B], x1[B];
-        xf.load(c0, x0);
-        xf.load(c1, x1);
-        const float* a0 = val + (size_t)k * B * B;
-        const float* a1 = val + (size_t)(k + GN) * B * B;
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1)
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) y[f1] += a0[f1 * B + f2] * x0[f2];
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1)
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) y[f1] += a1[f1 * B + f2] * x1[f2];
-    }
-    if (k < k1) {
-        float xj[B];
-        xf.load(bcol[k], xj);
-        const float* a = val + (size_t)k * B * B;
-#pragma unroll
-        for (int f1 = 0; f1 < B; ++f1)
-#pragma unroll
-            for (int f2 = 0; f2 < B; ++f2) y[f1] += a[f1 * B + f2] * xj[f2];
-    }
-}
-
 // One sweep on block row i over GN lanes (all lanes of the group call it with the same i and
 // act): out_i = x_i + omega Binv_i (b - A x)_i; a row without off-diagonal blocks is solved
 // exactly (out_i = Binv_i b_i).
@@ -245,7 +211,15 @@ __device__ __forceinline__ void post_row(int i, bool act, int lane, const int* _
 #pragma unroll
     for (int f = 0; f < B; ++f) y[f] = 0;
     const int k0 = act ? bptr[i] : 0, k1 = act ? bptr[i + 1] : 0;
-    row_acc<B, GN>(k0, k1, lane, bcol, val, xf, y);
+    for (int k = k0 + lane; k < k1; k += GN) {
+        float xj[B];
+        xf.load(bcol[k], xj);
+        const float* a = val + (size_t)k * B * B;
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) y[f1] += a[f1 * B + f2] * xj[f2];
+    }
 #pragma unroll
     for (int f = 0; f < B; ++f)
 #pragma unroll
@@ -278,7 +252,15 @@ __device__ __forceinline__ void resid_row(int i, bool act, int lane, const int* 
 #pragma unroll
     for (int f = 0; f < B; ++f) y[f] = 0;
     const int k0 = act ? bptr[i] : 0, k1 = act ? bptr[i + 1] : 0;
-    row_acc<B, GN>(k0, k1, lane, bcol, val, xf, y);
+    for (int k = k0 + lane; k < k1; k += GN) {
+        float xj[B];
+        xf.load(bcol[k], xj);
+        const float* a = val + (size_t)k * B * B;
+#pragma unroll
+        for (int f1 = 0; f1 < B; ++f1)
+#pragma unroll
+            for (int f2 = 0; f2 < B; ++f2) y[f1] += a[f1 * B + f2] * xj[f2];
+    }
 #pragma unroll
     for (int f = 0; f < B; ++f)
 #pragma unroll
