@@ -213,26 +213,36 @@ class Remesher {
     }
 
     // remesh the context's mesh in place: positions from the device; incompressible states (and
-    // temperatures) remapped on the device, WC states remapped here (their mean over the origins)
+    // temperatures) remapped on the device, WC states (and BoussinesqWC temperatures) remapped
+    // here (their mean over the origins).  Per-node inputs (Dirichlet values, heat boundary
+    // conditions) belong to the old node numbering: set them again after a remesh.
     void remesh(Context& ctx, Mesh& cur) const {
         Mesh next = remesh(cur, ctx.positions());
         const int w = p_.dim + 1;
         if (ctx.params().kind == PFG_KIND_INCOMP_PSPG) {
             ctx.uploadMeshRemap(next.pos, next.flags, next.conn, next.origin, w);
         } else {
-            const std::vector<double> q = ctx.states();
-            const int nf = ctx.statesPerNode(), n_old = cur.nodes(), n = next.nodes();
-            std::vector<double> out((size_t)nf * n);
-            for (int f = 0; f < nf; ++f)
-                for (int j = 0; j < n; ++j) {
-                    const int32_t* o = &next.origin[(size_t)j * w];
-                    double s = 0.0;
-                    int cnt = 0;
-                    for (int k = 0; k < w && o[k] >= 0; ++k, ++cnt) s += q[(size_t)f * n_old + o[k]];
-                    out[(size_t)f * n + j] = s / cnt;
-                }
+            // WC states (and, for BoussinesqWC, the temperatures) remapped here: each new node
+            // takes the mean of its origins' values, summed in origin order
+            const int n_old = cur.nodes(), n = next.nodes();
+            auto remap = [&](const std::vector<double>& q, int nf) {
+                std::vector<double> out((size_t)nf * n);
+                for (int f = 0; f < nf; ++f)
+                    for (int j = 0; j < n; ++j) {
+                        const int32_t* o = &next.origin[(size_t)j * w];
+                        double s = 0.0;
+                        int cnt = 0;
+                        for (int k = 0; k < w && o[k] >= 0; ++k, ++cnt) s += q[(size_t)f * n_old + o[k]];
+                        out[(size_t)f * n + j] = s / cnt;
+                    }
+                return out;
+            };
+            const std::vector<double> q = remap(ctx.states(), ctx.statesPerNode());
+            const bool heat = ctx.params().boussinesq != 0;
+            const std::vector<double> T = heat ? remap(ctx.temperature(), 1) : std::vector<double>();
             ctx.uploadMesh(next.pos, next.flags, next.conn);
-            ctx.setStates(out);
+            ctx.setStates(q);
+            if (heat) ctx.setTemperature(T);
         }
         if (next.facetCount() && (ctx.params().gamma >= 1e-15 || ctx.params().dgamma_dt >= 1e-15))
             ctx.uploadFacets(next.facets, next.facetElm);
