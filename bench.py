@@ -1055,6 +1055,8 @@ def run_gpu_heat(args):
     flags, tbc, t0 = heat_setup(mesh)
     p = api.default_params(api.KIND_INCOMP_PSPG, 3)
     p.rho, p.heat_k, p.heat_cv = HEAT["rho"], HEAT["k"], HEAT["cv"]
+    mixed = args.precision == "fp32"  # FP32 CG corrections under FP64 refinement; fp64: FP64 CG
+    p.precision = api.PREC_MIXED if mixed else api.PREC_FP64
     ctx = api.Context(p)
     ctx.upload_mesh(mesh)
     ctx.set_temperature(t0)
@@ -1100,12 +1102,14 @@ def run_gpu_heat(args):
     phases = ctx.phase_times()
     ctx.set_profiling(False)
     P = node_pairs(mesh)                            # node pairs (diagonal included)
-    spmv_b = P * (8 + 4) + (N + 1) * 4 + 2 * N * 8   # values + columns, row pointers, p in, Ap out
+    s_b = 4 if mixed else 8                          # the CG's value and vector width
+    spmv_b = P * (s_b + 4) + (N + 1) * 4 + 2 * N * s_b  # values + columns, row pointers, p in, Ap out
     spmv_ms, spmv_n = phases.get("Heat CG SpMV", (0.0, 0))
     peak, peak_kind = hbm_peak()
     achieved = spmv_b * it_p / (spmv_ms / 1e3) / 1e9 if spmv_ms else None
     roof = {"bound": "hbm", "kernel": "Heat CG SpMV", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak if achieved else None, "traffic": NCU_TRAFFIC.get(("heat-c3", "fp64", "Heat CG SpMV")),
+            "frac": achieved / peak if achieved else None,
+            "traffic": None if mixed else NCU_TRAFFIC.get(("heat-c3", "fp64", "Heat CG SpMV")),
             "algorithmic_bytes": spmv_b,
             "avg_launch_us": 1e3 * spmv_ms / max(it_p, 1), "peak_kind": peak_kind,
             "note": "time of all SpMV launches (including the no-op tail of the last 8-iteration chunk) "
@@ -1131,10 +1135,11 @@ def run_gpu_heat(args):
         out = {
             "metric": HEAT["metric"], "value": K / (total_ms / 1e3), "unit": HEAT["unit"], "n_gpus": world,
             "steps": K, "warmup": Wm, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice)",
+            "vs_baseline": None, "dtype": "fp32" if mixed else "f64", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": HEAT["name"], "nodes": N, "elements": int(mesh.n_elems), "node_pairs": P,
                        "dt": dt, "material": "rho 1, k 237, cv 1000 (conduction example)",
-                       "linear_solver": "FP64 Jacobi CG, ||r|| <= max(1e-14 ||b||, 1e-10)",
+                       "linear_solver": ("FP32 Jacobi CG corrections under FP64 refinement of b - A x"
+                                         if mixed else "FP64 Jacobi CG") + ", ||r|| <= max(1e-14 ||b||, 1e-10)",
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas only"},
             "step_stats": {"converged": conv, "cg_iterations": iters},
             "roofline": roof, "phases_ms_per_step": {k: v[0] / Kp for k, v in phases.items()},

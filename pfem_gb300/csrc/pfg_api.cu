@@ -393,7 +393,7 @@ PFG_API int pfg_destroy(pfg_ctx* c) {
                     &c->mx_seg, &c->mx_ii, &c->mx_id, &c->mx_sc, &c->mx_part, &c->mx_cnt, &c->mx_scale,
                     &c->mx_list, &c->fc_nodes, &c->fc_elem, &c->nf_nodes, &c->nf_ptr, &c->nf_ent, &c->fst_force,
                     &c->mg_x0, &c->mg_in64, &c->val16, &c->heat_t, &c->heat_flags, &c->heat_tbc, &c->heat_val,
-                    &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
+                    &c->heat_rhs, &c->heat_cg, &c->heat_red, &c->heat_cg32, &c->heat_rhs32, &c->hf_ptr, &c->hf_ent, &c->hf_fflags, &c->heat_q,
                     &c->pe_ptr, &c->pe_item, &c->pe_pair, &c->pe_pos, &c->el_slot, &c->ne_slot, &c->conn_s, &c->mx_scale32, &c->mx_f32, &c->mx_xdf, &c->mx_vpdf, &c->mx_tdf,
                     &c->mx_rec, &c->mx_gdf, &c->wc_inst, &c->mx_ed_aos, &c->mx_vsum, &c->wch_rec, &c->fs_gauge, &c->fs_rp, &c->fs_col, &c->fs_val, &c->fs_lval, &c->fs_mval, &c->fs_vec, &c->fs_cg, &c->fs_red, &c->lu_front, &c->lu_nodes,
                     &c->lu_recs, &c->lu_kids, &c->lu_maps, &c->lu_piv, &c->lu_mat, &c->lu_vec, &c->lu_list,

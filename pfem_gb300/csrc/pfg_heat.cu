@@ -599,6 +599,133 @@ __global__ void __launch_bounds__(BLOCK) k_cg_update(int N, double* __restrict__
     }
 }
 
+// ---- mixed precision (contexts in PFG_PREC_MIXED): Jacobi CG corrections in FP32 under an FP64
+// refinement of r = b - A x; the same recurrences as above on FP32 vectors, FP64 reductions --------
+enum : int { V32_R = 0, V32_Z, V32_P, V32_S, V32_W, V32_DIAG, V32_D, V32_COUNT };
+
+// the FP32 copy of the matrix values
+__global__ void k_heat_val32(int P, const double* __restrict__ val, float* __restrict__ val32) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P) val32[p] = (float)val[p];
+}
+
+// r = b - A x in FP64, its FP32 copy (the correction solve's right-hand side), ||r||^2 into
+// sc[S_NUM] and ||b||^2 into sc[S_DEN]
+__global__ void __launch_bounds__(BLOCK) k_heat_r64(int N, const int* __restrict__ rp, const int* __restrict__ col,
+                                                    const double* __restrict__ val, const double* __restrict__ b,
+                                                    const double* __restrict__ x, float* __restrict__ rhs32,
+                                                    CgPtrs k) {
+    __shared__ double sh[32];
+    double rr = 0, bb = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        double ax = 0;
+        for (int t = rp[n]; t < rp[n + 1]; ++t) ax += val[t] * x[col[t]];
+        const double r = b[n] - ax;
+        rhs32[n] = (float)r;
+        rr += r * r;
+        bb += b[n] * b[n];
+    }
+    double s1, s2;
+    if (grid_sum2<BLOCK>(rr, bb, k.partials, k.ticket, sh, s1, s2) && threadIdx.x == 0) {
+        k.sc[S_NUM] = s1;
+        k.sc[S_DEN] = s2;
+    }
+}
+
+// d = 0, r = rhs, z = r / diag, p = s = 0 (diag from the FP32 matrix); tolerance eta ||rhs||
+__global__ void __launch_bounds__(BLOCK) k_cg32_init(int N, const int* __restrict__ rp, const int* __restrict__ col,
+                                                     const float* __restrict__ val, const float* __restrict__ rhs,
+                                                     float* __restrict__ V, size_t ld, CgPtrs k, double eta) {
+    __shared__ double sh[32];
+    double bb = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        float d = 1.0f;
+        for (int t = rp[n]; t < rp[n + 1]; ++t)
+            if (col[t] == n) d = val[t];
+        const float r = rhs[n];
+        const float dinv = 1.0f / d;
+        V[V32_R * ld + n] = r;
+        V[V32_Z * ld + n] = r * dinv;
+        V[V32_P * ld + n] = 0.0f;
+        V[V32_S * ld + n] = 0.0f;
+        V[V32_DIAG * ld + n] = dinv;
+        V[V32_D * ld + n] = 0.0f;
+        bb += (double)r * (double)r;
+    }
+    double s1, unused;
+    if (grid_sum2<BLOCK>(bb, 0.0, k.partials, k.ticket, sh, s1, unused) && threadIdx.x == 0) {
+        k.sc[S_BB] = s1;
+        k.sc[S_TOL2] = eta * eta * s1;
+        k.sc[S_ITERS] = 0;
+        k.sc[S_DONE] = 0;
+        k.sc[S_GAMMA] = 0;
+        k.sc[S_ALPHA] = 1;
+        k.sc[S_BETA] = 0;
+        k.sc[S_FIRST] = 1;
+    }
+}
+
+// w = A z with gamma, delta and ||r||^2 (k_cg_spmv on FP32 arrays; each thread's sums in FP32,
+// the grid reduction and the scalars in FP64)
+__global__ void __launch_bounds__(BLOCK) k_cg32_spmv(int N, const int* __restrict__ rp, const int* __restrict__ col,
+                                                     const float* __restrict__ val, float* __restrict__ V, size_t ld,
+                                                     CgPtrs k, int max_it) {
+    __shared__ double sh[32];
+    if (k.sc[S_DONE] != 0.0) return;
+    const float* z = V + V32_Z * ld;
+    const float* r = V + V32_R * ld;
+    float ga = 0, de = 0, rr = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        float w = 0;
+        for (int t = rp[n]; t < rp[n + 1]; ++t) w += val[t] * z[col[t]];
+        V[V32_W * ld + n] = w;
+        const float zn = z[n], rn = r[n];
+        ga += rn * zn;
+        de += w * zn;
+        rr += rn * rn;
+    }
+    double g, s_de, s_rr;
+    if (!grid_sum3<BLOCK>(ga, de, rr, k.partials, k.ticket, sh, g, s_de, s_rr)) return;
+    if (threadIdx.x == 0) {
+        const bool first = k.sc[S_FIRST] != 0.0;
+        const double it = k.sc[S_ITERS] + (first ? 0.0 : 1.0);
+        k.sc[S_ITERS] = it;
+        k.sc[S_FIRST] = 0;
+        k.sc[S_RR] = s_rr;
+        const double gold = k.sc[S_GAMMA];
+        const double beta = gold != 0.0 ? g / gold : 0.0;
+        const double den = s_de - beta * g / k.sc[S_ALPHA];
+        k.sc[S_BETA] = beta;
+        k.sc[S_ALPHA] = den != 0.0 ? g / den : 0.0;
+        k.sc[S_GAMMA] = g;
+        if (s_rr <= k.sc[S_TOL2]) k.sc[S_DONE] = 1;
+        else if (!(s_rr == s_rr) || !(den > 0.0)) k.sc[S_DONE] = 2;
+        else if (it >= max_it) k.sc[S_DONE] = 3;
+    }
+}
+
+// p = z + beta p; s = w + beta s; d += alpha p; r -= alpha s; z = r / diag
+__global__ void __launch_bounds__(BLOCK) k_cg32_update(int N, float* __restrict__ V, size_t ld, CgPtrs k) {
+    if (k.sc[S_DONE] != 0.0) return;
+    const float alpha = (float)k.sc[S_ALPHA], beta = (float)k.sc[S_BETA];
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const float p = V[V32_Z * ld + n] + beta * V[V32_P * ld + n];
+        const float sv = V[V32_W * ld + n] + beta * V[V32_S * ld + n];
+        V[V32_P * ld + n] = p;
+        V[V32_S * ld + n] = sv;
+        V[V32_D * ld + n] += alpha * p;
+        const float r = V[V32_R * ld + n] - alpha * sv;
+        V[V32_R * ld + n] = r;
+        V[V32_Z * ld + n] = r * V[V32_DIAG * ld + n];
+    }
+}
+
+// x += d (the FP32 correction)
+__global__ void k_heat_add_d(int N, const float* __restrict__ d, double* __restrict__ x) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < N) x[n] += (double)d[n];
+}
+
 // Squared relative change of the non-free nodes (residual "T", HeatEquation.inl:153-180):
 // sum (x - xp)^2 and sum xp^2 into sc[S_NUM], sc[S_DEN]; or, with b, ||b - A x||^2 into
 // sc[S_NUM] (residual "Ax_f", :182-185).
@@ -657,7 +784,8 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
     const int N = c->N;
     double* V = ptr<double>(c->heat_cg);
     const size_t ld = (size_t)std::max(N, 1);
-    PFG_CUDA(c, cudaMemcpyAsync(x, tprev, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    if (tprev != x)
+        PFG_CUDA(c, cudaMemcpyAsync(x, tprev, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     const CgPtrs kp = cg_ptrs(c);
     const int grid = std::max(1, std::min(c->max_grid, div_up(N, BLOCK)));
     const int* rp = ptr<int>(c->nbr_ptr);
@@ -690,6 +818,74 @@ int heat_cg(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, boo
     *ok = h[S_DONE] == 1.0;
     st->krylov_iterations += (int)h[S_ITERS];
     return PFG_OK;
+}
+
+// The same solve in mixed precision: from x0 = T_prev, FP64 residuals r = b - A x and FP32 Jacobi
+// CG corrections A d = r (to eta = 1e-4 of ||r||, or, for a sweep that needs less, 0.2 of the
+// remaining reduction, at most 0.01), x += d, until ||r|| meets the FP64 solve's tolerance.  A
+// sweep that does not shrink ||r|| tenfold, a breakdown, or 30 sweeps hand the rest to the FP64
+// CG from the current x.
+int heat_cg_mixed(pfg_ctx* c, const double* tprev, double* x, pfg_step_status* st, bool* ok, double cap) {
+    const int N = c->N, P = c->P;
+    const size_t ld = (size_t)std::max(N, 1);
+    float* V = ptr<float>(c->heat_cg32);
+    float* val32 = V + V32_COUNT * ld;
+    float* rhs32 = ptr<float>(c->heat_rhs32);
+    const int* rp = ptr<int>(c->nbr_ptr);
+    const int* col = ptr<int>(c->nbr);
+    const double* val = ptr<double>(c->heat_val);
+    const CgPtrs kp = cg_ptrs(c);
+    const int grid = std::max(1, std::min(c->max_grid, div_up(N, BLOCK)));
+    PFG_CUDA(c, cudaMemcpyAsync(x, tprev, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    if (P > 0) k_heat_val32<<<div_up(P, BLOCK), BLOCK, 0, c->stream>>>(P, val, val32);
+    const int max_it = std::max(1, c->prm.krylov_max_iter);
+    double* h = c->h_scalars;
+    double rr_prev = INFINITY;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        k_heat_r64<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val, ptr<double>(c->heat_rhs), x, rhs32, kp);
+        PFG_CHECK_LAUNCH(c);
+        PFG_CUDA(c, cudaMemcpyAsync(h, kp.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->stream));
+        PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+        const double rr = h[S_NUM], bnorm = std::sqrt(h[S_DEN]);
+        const double tol = std::fmin(std::fmax(c->prm.krylov_rel_tol * bnorm, c->prm.krylov_abs_tol),
+                                     std::fmax(cap, 2e-16 * bnorm));
+        if (std::isnan(rr)) {
+            *ok = false;
+            return PFG_OK;
+        }
+        if (std::sqrt(rr) <= tol) {
+            *ok = true;
+            return PFG_OK;
+        }
+        if (!(rr <= 0.01 * rr_prev)) break;  // FP32 corrections stopped contracting
+        rr_prev = rr;
+        const double eta = std::fmax(1e-4, std::fmin(0.01, 0.2 * tol / std::sqrt(rr)));
+        k_cg32_init<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val32, rhs32, V, ld, kp, eta);
+        prof_begin(c, PH_HEAT_SPMV);
+        k_cg32_spmv<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val32, V, ld, kp, max_it);
+        prof_end(c, PH_HEAT_SPMV);
+        PFG_CHECK_LAUNCH(c);
+        int done_it = 0;
+        while (done_it < max_it) {
+            const int n = std::min(8, max_it - done_it);
+            for (int it = 0; it < n; ++it) {
+                k_cg32_update<<<grid, BLOCK, 0, c->stream>>>(N, V, ld, kp);
+                prof_begin(c, PH_HEAT_SPMV);
+                k_cg32_spmv<<<grid, BLOCK, 0, c->stream>>>(N, rp, col, val32, V, ld, kp, max_it);
+                prof_end(c, PH_HEAT_SPMV);
+            }
+            PFG_CHECK_LAUNCH(c);
+            done_it += n;
+            PFG_CUDA(c, cudaMemcpyAsync(h, kp.sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->stream));
+            PFG_CUDA(c, cudaStreamSynchronize(c->stream));
+            if (h[S_DONE] != 0.0) break;
+        }
+        st->krylov_iterations += (int)h[S_ITERS];
+        if (h[S_DONE] == 2.0) break;  // breakdown
+        k_heat_add_d<<<div_up(N, BLOCK), BLOCK, 0, c->stream>>>(N, V + V32_D * ld, x);
+        PFG_CHECK_LAUNCH(c);
+    }
+    return heat_cg(c, x, x, st, ok, cap);
 }
 
 // HeatEqIncompNewton::solve through PicardAlgo::solve (PicardAlgo.cpp:31-95): without phase
@@ -725,7 +921,9 @@ int heat_dim(pfg_ctx* c, double dt, pfg_step_status* st) {
             break;
         }
         bool solved = false;
-        int rc = heat_cg(c, tprev, x, st, &solved, axf ? 0.1 * c->prm.heat_min_res : INFINITY);
+        const double cap = axf ? 0.1 * c->prm.heat_min_res : INFINITY;
+        int rc = c->prm.precision == PFG_PREC_MIXED ? heat_cg_mixed(c, tprev, x, st, &solved, cap)
+                                                    : heat_cg(c, tprev, x, st, &solved, cap);
         if (rc) return rc;
         if (!solved) {
             ok = false;
@@ -894,6 +1092,10 @@ int heat_alloc(pfg_ctx* c) {
         (rc = ensure(c, c->heat_red, sizeof(double) * (3 * (size_t)std::max(c->max_grid, 1) + 64))) ||
         (rc = ensure(c, c->hf_ptr, sizeof(int) * (N + 1))) ||
         (rc = ensure(c, c->edata_df, sizeof(DF) * (3 + c->dim * (c->dim + 1)) * (size_t)std::max(c->E, 1))))
+        return rc;
+    if (c->prm.precision == PFG_PREC_MIXED &&
+        ((rc = ensure(c, c->heat_cg32, sizeof(float) * (V32_COUNT * N + P))) ||
+         (rc = ensure(c, c->heat_rhs32, sizeof(float) * N))))
         return rc;
     PFG_CUDA(c, cudaMemsetAsync(c->heat_t.p, 0, sizeof(double) * N, c->stream));
     PFG_CUDA(c, cudaMemsetAsync(c->heat_flags.p, 0, N, c->stream));

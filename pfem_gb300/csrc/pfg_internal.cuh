@@ -188,6 +188,7 @@ struct pfg_ctx {
     // per-node lists of heat facets (facet * 4 + facet-local node) with each facet's flux
     // flags, and the flux vectors at the facet Gauss points
     pfg::DBuf heat_t, heat_flags, heat_tbc, heat_val, heat_rhs, heat_cg, heat_red;
+    pfg::DBuf heat_cg32, heat_rhs32;  // mixed precision: FP32 CG vectors and matrix values, FP32 residual
     pfg::DBuf hf_ptr, hf_ent, hf_fflags, heat_q;
     pfg::DBuf wch_rec;  // BoussinesqWC heat step: per element node lumped mass and right-hand side
     // fractional step: gauge nodes, the velocity matrix (CSR), L and M (node-pair layout), work

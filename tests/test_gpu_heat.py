@@ -60,13 +60,16 @@ def _scenario(mesh, name):
     return fl, tbc, kw, fs, q
 
 
+@pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_MIXED])
 @pytest.mark.parametrize("name", ["none", "dirichlet_convection_radiation", "flux_convection"])
 @pytest.mark.parametrize("which", ["c1", "3d"])
-def test_heat_steps_match_oracle(gpu_lib, which, name, c1_mesh, small3d_mesh):
+def test_heat_steps_match_oracle(gpu_lib, which, name, precision, c1_mesh, small3d_mesh):
+    """FP64 Jacobi CG, or (mixed precision) FP32 CG corrections under FP64 refinement to the same
+    tolerance: within 1e-10 of the oracle's LU steps either way."""
     mesh = c1_mesh if which == "c1" else small3d_mesh
     N = mesh.n_nodes
     fl, tbc, kw, fs, q = _scenario(mesh, name)
-    ctx = make_ctx(mesh, heat_fs_flags=fs, **kw)
+    ctx = make_ctx(mesh, precision, heat_fs_flags=fs, **kw)
     t0 = 300.0 + 100.0 * np.exp(-((mesh.pos[0] - 0.3) ** 2 + (mesh.pos[1] - 0.3) ** 2) / 0.05)
     ctx.set_temperature(t0)
     ctx.heat_set_bc(fl, tbc)
@@ -176,9 +179,10 @@ def test_boussinesq_coupled_steps_match_oracle(gpu_lib, c1_mesh):
 TM, DTM, LM = 933.15, 20.0, 396000.0  # the reference's phase-change example (aluminium)
 
 
+@pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_MIXED])
 @pytest.mark.parametrize("residual", [api.RES_T, api.RES_AX_F])
 @pytest.mark.parametrize("which", ["c1", "3d"])
-def test_heat_phase_change_picard_matches_oracle(gpu_lib, which, residual, c1_mesh, small3d_mesh):
+def test_heat_phase_change_picard_matches_oracle(gpu_lib, which, residual, precision, c1_mesh, small3d_mesh):
     """HeatEqIncompNewton with phase change: Picard iterations on the latent-heat mass factor
     (HeatEquation.inl:60-66, 131-138), the same outcome and iteration count as the oracle.  The
     absolute "Ax_f" residual of this system contracts ~5x per iteration, so in 3D neither side
@@ -186,7 +190,7 @@ def test_heat_phase_change_picard_matches_oracle(gpu_lib, which, residual, c1_me
     mesh = c1_mesh if which == "c1" else small3d_mesh
     N = mesh.n_nodes
     kw = dict(heat_h=500.0, heat_t_inf=300.0, heat_fs_flags=api.HEAT_QH)
-    ctx = make_ctx(mesh, rho=2385.0, heat_cv=1080.0, heat_k=94.03, heat_phase_change=1, heat_tm=TM,
+    ctx = make_ctx(mesh, precision, rho=2385.0, heat_cv=1080.0, heat_k=94.03, heat_phase_change=1, heat_tm=TM,
                    heat_dt_melt=DTM, heat_lm=LM, heat_residual=residual, **kw)
     t0 = np.full(N, TM + 5.0) + 2 * np.sin(3 * mesh.pos[0])
     ctx.set_temperature(t0)
