@@ -644,7 +644,67 @@ __global__ void __launch_bounds__(NB) k_mx_node(Mx m, int N, int E, const int* _
         DF sae{0.0f, 0.0f}, av[DIM], tg[DIM], tc{0.0f, 0.0f};
 #pragma unroll
         for (int f = 0; f < DIM; ++f) bv[f] = av[f] = tg[f] = DF{0.0f, 0.0f};
-        for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; ++q) {
+        const int q_begin = ne_ptr[n], q_end = ne_ptr[n + 1];
+        if (!DFA && p1) {
+            // the default path, software-pipelined: the next incidence's element data are loaded
+            // before this incidence's arithmetic (the same operations as the loop below)
+            struct Inc {
+                DF ae, tau, gi[DIM];
+                float ks;
+                float4 vh, vl;
+                int i;
+            };
+            auto load = [&](int q, Inc& t) {
+                const int e = ne_slot[q];
+                t.i = ne_loc[q];
+                t.ae = ed.gdf(0, e);
+                t.tau = ed.gdf(1, e);
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) t.gi[f] = ed.gdf(2 + f * NPE + t.i, e);
+                t.ks = ed.gf(ed_ksum<DIM>(), e);
+                t.vh = __ldg(vsum + 2 * (size_t)e);
+                t.vl = __ldg(vsum + 2 * (size_t)e + 1);
+            };
+            Inc nxt;
+            if (q_begin < q_end) load(q_begin, nxt);
+            for (int q = q_begin; q < q_end; ++q) {
+                const Inc cur = nxt;
+                if (q + 1 < q_end) load(q + 1, nxt);
+                const int i = cur.i;
+                const DF ae = df_mul(cur.ae, k.ref_df);
+                const DF tau = cur.tau;
+                const float a32 = ae.h, t32 = tau.h, kf = a32 * cur.ks;
+                float g[DIM], dot = 0.0f;
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) {
+                    g[f] = cur.gi[f].h;
+                    dot += g[f] * g[f];
+                }
+                const float mii = cm32 * k.mm32[i][i] * a32, as = a32 * k.s32[i];
+#pragma unroll
+                for (int f1 = 0; f1 < DIM; ++f1) {
+#pragma unroll
+                    for (int f2 = 0; f2 < DIM; ++f2) A32[f1][f2] += kf * ((f1 == f2 ? dot : 0.0f) + g[f2] * g[f1]);
+                    A32[f1][f1] += mii;
+                    A32[f1][DIM] -= as * g[f1];
+                    A32[DIM][f1] += (t32 * ct32 + 1.0f) * as * g[f1];
+                }
+                A32[DIM][DIM] += t32 * a32 * l32 * dot;
+                const DF V[3] = {DF{cur.vh.x, cur.vl.x}, DF{cur.vh.y, cur.vl.y}, DF{cur.vh.z, cur.vl.z}};
+                const DF ta = df_mul(tau, ae);
+                DF gv = df_mul(cur.gi[0], V[0]);
+#pragma unroll
+                for (int f = 1; f < DIM; ++f) gv = df_add(gv, df_mul(cur.gi[f], V[f]));
+                sae = df_add(sae, ae);
+#pragma unroll
+                for (int f = 0; f < DIM; ++f) {
+                    av[f] = df_add(av[f], df_mul(ae, V[f]));
+                    tg[f] = df_add(tg[f], df_mul(ta, cur.gi[f]));
+                }
+                tc = df_add(tc, df_mul(ta, gv));
+            }
+        }
+        for (int q = (!DFA && p1) ? q_end : q_begin; q < q_end; ++q) {
             const int e = ne_slot[q];  // element-major data are stored by slot
             const int i = ne_loc[q];
             const DF ae = df_mul(ed.gdf(0, e), k.ref_df);
