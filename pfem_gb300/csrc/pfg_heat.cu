@@ -676,21 +676,8 @@ __global__ void __launch_bounds__(BLOCK) k_cg32_spmv(int N, const int* __restric
     const float* r = V + V32_R * ld;
     float ga = 0, de = 0, rr = 0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
-        // four entries per step: their columns and values, then the four gathers, in flight
-        // together (the sum in entry order, as one at a time)
         float w = 0;
-        int t = rp[n];
-        const int e = rp[n + 1];
-        for (; t + 3 < e; t += 4) {
-            const int c0 = col[t], c1 = col[t + 1], c2 = col[t + 2], c3 = col[t + 3];
-            const float v0 = val[t], v1 = val[t + 1], v2 = val[t + 2], v3 = val[t + 3];
-            const float z0 = z[c0], z1 = z[c1], z2 = z[c2], z3 = z[c3];
-            w += v0 * z0;
-            w += v1 * z1;
-            w += v2 * z2;
-            w += v3 * z3;
-        }
-        for (; t < e; ++t) w += val[t] * z[col[t]];
+        for (int t = rp[n]; t < rp[n + 1]; ++t) w += val[t] * z[col[t]];
         V[V32_W * ld + n] = w;
         const float zn = z[n], rn = r[n];
         ga += rn * zn;
