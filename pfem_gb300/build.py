@@ -88,8 +88,8 @@ def build_remesh(force=False):
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
     tmp = REMESH_LIB + f".tmp{os.getpid()}"
     # no contraction into FMAs: the same roundings on x86 and Arm as the Python host remesh
-    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-fvisibility=hidden", REMESH_SRC,
-           "-o", tmp]
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", "-shared", "-fPIC", "-fvisibility=hidden",
+           REMESH_SRC, "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"g++ failed on {REMESH_SRC}:\n{r.stdout}\n{r.stderr}")

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -30,6 +31,7 @@
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 struct pfr_mesh {
@@ -700,6 +702,193 @@ void neighbours(int N, int npe, int E, const int32_t* conn, std::vector<int>& pt
 // vertex_triple_index orders it
 constexpr int TRIPLE[4][3] = {{1, 3, 2}, {0, 2, 3}, {0, 3, 1}, {0, 1, 2}};
 
+// Interior simplices of a large 3D cloud from independent triangulations of cells, in parallel.
+//
+// The perturbed points are split into K cells by quantiles along the two longest axes (every
+// point of space in exactly one cell's core box, half-open).  Each cell triangulates the points
+// of its core box widened by a margin m >= 4 alpha h on those axes.  A tetrahedron is taken from
+// the cell holding its centroid (computed from its vertices in ascending index, so every cell
+// computes the same value), when it is interior.  This is the global alpha complex, with the
+// interior flag of the neighbour across each face, under two conditions checked per cell:
+//  * an interior tetrahedron of the global triangulation has its vertices within 2 alpha h of
+//    its centroid, so a cell holds all of them and, its circumsphere being empty of every point,
+//    the tetrahedron is in the cell's triangulation (which is unique for points in general
+//    position); and a taken tetrahedron whose circumsphere lies inside the widened box is empty
+//    of every point, so it is in the global triangulation;
+//  * the neighbour across a face of a taken tetrahedron: if it is interior in the global
+//    triangulation its vertices lie within 4 alpha h of the centroid and it is the cell's
+//    neighbour too; if the cell's neighbour is interior with its circumsphere inside the widened
+//    box it is the global one.
+// A taken tetrahedron, or an interior neighbour of one, whose circumsphere leaves the widened box
+// (a nearly flat tetrahedron of the perturbed points) voids the result: the caller then
+// triangulates serially.  Cells run on up to 16 threads; their results are concatenated in cell
+// order, so the output does not depend on the thread count.
+bool interior_by_cells(const pfr_params& prm, int N, const double* pos, const std::vector<double>& pts, int K,
+                       std::vector<int>& simp, std::vector<double>& vol, std::vector<uint8_t>& nbint) {
+    constexpr int D = 3, V = 4;
+    const double h = prm.hchar;
+    const double alpha2 = (prm.alpha * h) * (prm.alpha * h);
+    const double margin = 4.5 * prm.alpha * h + 10 * prm.jitter * h;
+    double lo[D], hi[D];
+    for (int c = 0; c < D; ++c) lo[c] = hi[c] = pts[c];
+    for (int i = 0; i < N; ++i)
+        for (int c = 0; c < D; ++c) {
+            lo[c] = std::min(lo[c], pts[(size_t)i * D + c]);
+            hi[c] = std::max(hi[c], pts[(size_t)i * D + c]);
+        }
+    int ax[D] = {0, 1, 2};
+    std::sort(ax, ax + D, [&](int a, int b) { return hi[a] - lo[a] > hi[b] - lo[b] || (hi[a] - lo[a] == hi[b] - lo[b] && a < b); });
+    const int a0 = ax[0], a1 = ax[1];
+    int K0 = std::max(1, (int)std::lround(std::sqrt((double)K)));
+    const int K1 = std::max(1, K / K0);
+    struct Cell {
+        double lo0, hi0, lo1, hi1;
+    };
+    std::vector<Cell> cells;
+    std::vector<int> ord(N);
+    std::iota(ord.begin(), ord.end(), 0);
+    auto by = [&](int a) {
+        return [&pts, a](int p, int q) {
+            const double x = pts[(size_t)p * 3 + a], y = pts[(size_t)q * 3 + a];
+            return x < y || (x == y && p < q);
+        };
+    };
+    std::sort(ord.begin(), ord.end(), by(a0));
+    for (int g = 0; g < K0; ++g) {
+        const int b = (int)((long long)N * g / K0), e = (int)((long long)N * (g + 1) / K0);
+        if (b >= e) continue;
+        const double l0 = g == 0 ? -INFINITY : pts[(size_t)ord[b] * 3 + a0];
+        const double h0 = g == K0 - 1 ? INFINITY : pts[(size_t)ord[e] * 3 + a0];
+        std::vector<int> sub(ord.begin() + b, ord.begin() + e);
+        std::sort(sub.begin(), sub.end(), by(a1));
+        const int M = (int)sub.size();
+        for (int k = 0; k < K1; ++k) {
+            const int bb = (int)((long long)M * k / K1), ee = (int)((long long)M * (k + 1) / K1);
+            if (bb >= ee) continue;
+            const double l1 = k == 0 ? -INFINITY : pts[(size_t)sub[bb] * 3 + a1];
+            const double h1 = k == K1 - 1 ? INFINITY : pts[(size_t)sub[ee] * 3 + a1];
+            cells.push_back({l0, h0, l1, h1});
+        }
+    }
+    const int C = (int)cells.size();
+    struct Out {
+        std::vector<int> simp;
+        std::vector<double> vol;
+        std::vector<uint8_t> nbint;
+        bool ok = true;
+    };
+    std::vector<Out> outs(C);
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        for (int ci = next++; ci < C; ci = next++) {
+            const Cell& cl = cells[ci];
+            Out& o = outs[ci];
+            const double w0 = cl.lo0 - margin, W0 = cl.hi0 + margin, w1 = cl.lo1 - margin, W1 = cl.hi1 + margin;
+            std::vector<int> gid;
+            for (int i = 0; i < N; ++i) {
+                const double x0 = pts[(size_t)i * 3 + a0], x1 = pts[(size_t)i * 3 + a1];
+                if (x0 >= w0 && x0 < W0 && x1 >= w1 && x1 < W1) gid.push_back(i);
+            }
+            std::vector<double> lp(gid.size() * 3);
+            for (size_t k = 0; k < gid.size(); ++k)
+                for (int c = 0; c < 3; ++c) lp[k * 3 + c] = pts[(size_t)gid[k] * 3 + c];
+            Delaunay<3> dt(std::move(lp));
+            dt.build();
+            const int S = dt.slots();
+            // per slot: interior (true positions), and whether its perturbed circumsphere lies in
+            // the widened box
+            std::vector<uint8_t> inter(S, 0), inside(S, 0);
+            for (int t = 0; t < S; ++t) {
+                if (!dt.real(t)) continue;
+                int v[V];
+                for (int i = 0; i < V; ++i) v[i] = gid[dt.vert(t, i)];
+                double A[D][D];
+                for (int k = 0; k < D; ++k)
+                    for (int c = 0; c < D; ++c) A[k][c] = pos[(size_t)c * N + v[k + 1]] - pos[(size_t)c * N + v[0]];
+                const double m = std::fabs(det_rows<D>(A));
+                inter[t] = circumradius2<D>(A) <= alpha2 && m > 0.0;
+                if (!inter[t]) continue;
+                double B[D][D], rhs[D], ss = 0;
+                for (int k = 0; k < D; ++k) {
+                    double sk = 0;
+                    for (int c = 0; c < D; ++c) {
+                        B[k][c] = pts[(size_t)v[k + 1] * 3 + c] - pts[(size_t)v[0] * 3 + c];
+                        sk += B[k][c] * B[k][c];
+                    }
+                    rhs[k] = 0.5 * sk;
+                    ss += sk;
+                }
+                const double det = det_rows<D>(B);
+                if (!(std::fabs(det) > 1e-12 * std::pow(ss, 1.5))) continue;  // not inside
+                double cen[D];
+                for (int col = 0; col < D; ++col) {
+                    double Mx[D][D];
+                    for (int r = 0; r < D; ++r)
+                        for (int cc = 0; cc < D; ++cc) Mx[r][cc] = cc == col ? rhs[r] : B[r][cc];
+                    cen[col] = det_rows<D>(Mx) / det;
+                }
+                const double rad = std::sqrt(cen[0] * cen[0] + cen[1] * cen[1] + cen[2] * cen[2]) * (1 + 1e-9);
+                const double c0 = pts[(size_t)v[0] * 3 + a0] + cen[a0], c1 = pts[(size_t)v[0] * 3 + a1] + cen[a1];
+                inside[t] = c0 - rad > w0 && c0 + rad < W0 && c1 - rad > w1 && c1 + rad < W1;
+            }
+            for (int t = 0; t < S && o.ok; ++t) {
+                if (!inter[t]) continue;
+                int v[V], sv[V];
+                for (int i = 0; i < V; ++i) sv[i] = v[i] = gid[dt.vert(t, i)];
+                std::sort(sv, sv + V);
+                double ce0 = 0, ce1 = 0;
+                for (int i = 0; i < V; ++i) {
+                    ce0 += pts[(size_t)sv[i] * 3 + a0];
+                    ce1 += pts[(size_t)sv[i] * 3 + a1];
+                }
+                ce0 *= 0.25;
+                ce1 *= 0.25;
+                if (!(ce0 >= cl.lo0 && ce0 < cl.hi0 && ce1 >= cl.lo1 && ce1 < cl.hi1)) continue;
+                if (!inside[t]) {
+                    o.ok = false;
+                    break;
+                }
+                uint8_t nbi[V];
+                for (int l = 0; l < V; ++l) {
+                    const int u = dt.nbr(t, l);
+                    nbi[l] = u >= 0 && dt.real(u) && inter[u];
+                    if (nbi[l] && !inside[u]) o.ok = false;
+                }
+                double A[D][D];
+                for (int k = 0; k < D; ++k)
+                    for (int c = 0; c < D; ++c) A[k][c] = pos[(size_t)c * N + v[k + 1]] - pos[(size_t)c * N + v[0]];
+                double m = det_rows<D>(A);
+                if (m < 0) {  // positive orientation on the true positions
+                    std::swap(v[D - 1], v[D]);
+                    std::swap(nbi[D - 1], nbi[D]);
+                    m = -m;
+                }
+                for (int i = 0; i < V; ++i) {
+                    o.simp.push_back(v[i]);
+                    o.nbint.push_back(nbi[i]);
+                }
+                o.vol.push_back(m);
+            }
+        }
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int T = (int)std::min<unsigned>(std::min<unsigned>(hw, 16u), (unsigned)C);
+    std::vector<std::thread> th;
+    for (int i = 1; i < T; ++i) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+    simp.clear();
+    vol.clear();
+    nbint.clear();
+    for (const Out& o : outs) {
+        if (!o.ok) return false;
+        simp.insert(simp.end(), o.simp.begin(), o.simp.end());
+        vol.insert(vol.end(), o.vol.begin(), o.vol.end());
+        nbint.insert(nbint.end(), o.nbint.begin(), o.nbint.end());
+    }
+    return true;
+}
+
 template <int D>
 void alpha_shape(const pfr_params& prm, int N, const double* pos, const uint8_t* flags_in, pfr_mesh& out,
                  std::vector<int32_t>& node_origin) {
@@ -712,20 +901,37 @@ void alpha_shape(const pfr_params& prm, int N, const double* pos, const uint8_t*
             if (prm.jitter != 0) x += jitter_unit((uint64_t)i * D + c) * (prm.jitter * h);
             pts[(size_t)i * D + c] = x;
         }
+    std::vector<int> simp;
+    std::vector<double> vol;
+    std::vector<uint8_t> interior, nbint;  // nbint: the neighbour across face l is interior
+    int ns = 0;
+    // large perturbed 3D clouds: interior simplices from cells triangulated in parallel (K fixed
+    // by the node count, so the result does not depend on the machine); serially otherwise, or
+    // when a cell's conditions fail
+    const int K = std::min(16, N / 16384);
+    bool by_cells = false;
+    if constexpr (D == 3) {
+        if (!prm.single_triangulation && prm.jitter > 0 && K >= 2 &&
+            interior_by_cells(prm, N, pos, pts, K, simp, vol, nbint)) {
+            by_cells = true;
+            ns = (int)vol.size();
+            interior.assign(ns, 1);
+        }
+    }
+    if (!by_cells) {
     Delaunay<D> dt(std::move(pts));
     dt.build();
 
     // the simplices of the points (none with an enclosing vertex), in slot order
     const int S = dt.slots();
     std::vector<int> sid(S, -1);
-    std::vector<int> simp, nb;
-    int ns = 0;
+    std::vector<int> nb;
     for (int t = 0; t < S; ++t)
         if (dt.real(t)) sid[t] = ns++;
     simp.resize((size_t)ns * V);
     nb.resize((size_t)ns * V);
-    std::vector<double> vol(ns);
-    std::vector<uint8_t> interior(ns);
+    vol.resize(ns);
+    interior.resize(ns);
     const double alpha2 = (prm.alpha * h) * (prm.alpha * h);
     for (int t = 0; t < S; ++t) {
         const int s = sid[t];
@@ -752,6 +958,13 @@ void alpha_shape(const pfr_params& prm, int N, const double* pos, const uint8_t*
         }
         vol[s] = m;
         interior[s] = circumradius2<D>(A) <= alpha2 && m > 0.0;
+    }
+    nbint.resize((size_t)ns * V);
+    for (int s = 0; s < ns; ++s)
+        for (int l = 0; l < V; ++l) {
+            const int o = nb[(size_t)s * V + l];
+            nbint[(size_t)s * V + l] = o >= 0 && interior[o];
+        }
     }
     std::vector<uint8_t> bound(N), wet(N, 0);
     for (int i = 0; i < N; ++i) bound[i] = (flags_in[i] & BOUND) != 0;
@@ -783,8 +996,7 @@ void alpha_shape(const pfr_params& prm, int N, const double* pos, const uint8_t*
     for (int s = 0; s < ns; ++s) {
         if (!interior[s]) continue;
         for (int l = 0; l < V; ++l) {
-            const int o = nb[(size_t)s * V + l];
-            if (o >= 0 && interior[o]) continue;
+            if (nbint[(size_t)s * V + l]) continue;
             if (!keep[s]) continue;
             const int* v = &simp[(size_t)s * V];
             if constexpr (D == 2) {

@@ -359,7 +359,8 @@ class _PfrParams(C.Structure):
     _fields_ = [("dim", C.c_int32), ("add_on_fs", C.c_int32), ("delete_flying_nodes", C.c_int32),
                 ("laplacian_smoothing_boundaries", C.c_int32), ("hchar", C.c_double), ("alpha", C.c_double),
                 ("omega", C.c_double), ("gamma", C.c_double), ("jitter", C.c_double),
-                ("has_bounding_box", C.c_int32), ("pad0", C.c_int32), ("bounding_box", C.c_double * 6)]
+                ("has_bounding_box", C.c_int32), ("single_triangulation", C.c_int32),
+                ("bounding_box", C.c_double * 6)]
 
 
 REMESH_EXPORTED = ("pfr_default_params", "pfr_remesh", "pfr_alpha_shape", "pfr_mesh_counts", "pfr_mesh_read",
@@ -442,12 +443,14 @@ def _read_native(h, dim, hchar, alpha):
     return mesh, origin
 
 
-def alpha_shape_native(pos, flags, hchar, alpha=1.2, delete_flying_nodes=False, jitter=None):
+def alpha_shape_native(pos, flags, hchar, alpha=1.2, delete_flying_nodes=False, jitter=None, single=False):
     """`M.alpha_shape` through the C++ library; `jitter` is its perturbation amplitude relative
-    to hchar (default 1e-6 in 3D, 0 in 2D).  The result carries `node_origin`."""
+    to hchar (default 1e-6 in 3D, 0 in 2D); `single` forces one triangulation (large 3D clouds
+    are otherwise triangulated in cells in parallel).  The result carries `node_origin`."""
     dim, n = pos.shape
     prm = RemeshParams(hchar=hchar, alpha=alpha, delete_flying_nodes=delete_flying_nodes)
     p = _native_params(dim, prm, jitter)
+    p.single_triangulation = int(single)
     L = native_lib()
     P = np.ascontiguousarray(pos, float)
     F = np.ascontiguousarray(flags, np.uint8)

@@ -168,3 +168,19 @@ def test_errors(lib):
     p.hchar = 0.0
     assert lib.pfr_alpha_shape(C.byref(p), 3, pos.ctypes.data_as(C.POINTER(C.c_double)),
                                flags.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(h)) == -1
+
+
+def test_cells_equal_one_triangulation():
+    """A 3D cloud above the cell threshold (50k nodes) triangulated in cells on several threads
+    gives the simplices, facets, flags and node origins of one triangulation, fresh and moved."""
+    h = (0.25 / 3e4) ** (1 / 3)
+    pos, flags = M.dam_break_nodes_3d(h, seed=1)
+    assert pos.shape[1] >= 32768
+    rng = np.random.default_rng(3)
+    for p in (pos, pos + rng.uniform(-0.3, 0.3, pos.shape) * h * ((flags & M.BOUND) == 0)):
+        one = R.alpha_shape_native(p, flags, h, 1.2, True, single=True)
+        cells = R.alpha_shape_native(p, flags, h, 1.2, True)
+        assert canon_elems(one) == canon_elems(cells)
+        assert canon_facets(one) == canon_facets(cells)
+        assert np.array_equal(one.flags, cells.flags) and np.array_equal(one.node_origin, cells.node_origin)
+        assert positive(cells)
