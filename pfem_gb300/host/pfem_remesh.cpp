@@ -666,33 +666,64 @@ void qr_basic_solve(double (&A)[D][D], double (&b)[D], double (&x)[D]) {
     for (int k = 0; k < nz; ++k) x[perm[k]] = c[k];
 }
 
-// Sorted distinct neighbours of each node (nodes sharing an element with it), CSR.
-void neighbours(int N, int npe, int E, const int32_t* conn, std::vector<int>& ptr, std::vector<int>& idx) {
-    std::vector<int> cnt(N + 1, 0);
-    for (int e = 0; e < E; ++e)
-        for (int a = 0; a < npe; ++a) cnt[conn[(size_t)a * E + e] + 1] += npe - 1;
-    for (int i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
-    std::vector<int> raw(cnt[N]);
-    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-    for (int e = 0; e < E; ++e)
-        for (int a = 0; a < npe; ++a) {
-            const int na = conn[(size_t)a * E + e];
-            for (int b = 0; b < npe; ++b)
-                if (b != a) raw[fill[na]++] = conn[(size_t)b * E + e];
-        }
-    ptr.assign(N + 1, 0);
-    idx.clear();
-    idx.reserve(raw.size() / 2 + 1);
-    for (int i = 0; i < N; ++i) {
-        std::sort(raw.begin() + cnt[i], raw.begin() + cnt[i + 1]);
-        int prev = -1;
-        for (int k = cnt[i]; k < cnt[i + 1]; ++k)
-            if (raw[k] != prev && raw[k] != i) {
-                idx.push_back(raw[k]);
-                prev = raw[k];
-            }
-        ptr[i + 1] = (int)idx.size();
+// Runs f(begin, end) over [0, n) split into contiguous ranges on up to 16 threads.
+template <class F>
+void parallel_ranges(int n, F&& f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int T = (int)std::min<long long>(std::min<unsigned>(hw, 16u), std::max(1, n / 4096));
+    if (T <= 1) {
+        f(0, n);
+        return;
     }
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; ++t)
+        th.emplace_back([&, t] { f((int)((long long)n * t / T), (int)((long long)n * (t + 1) / T)); });
+    f(0, (int)((long long)n / T));
+    for (auto& x : th) x.join();
+}
+
+// Sorted distinct neighbours of each node (nodes sharing an element with it), CSR: the
+// node-element incidence by a counting sort, then each node's list sorted on its own (in
+// parallel; the lists do not depend on the thread count).
+void neighbours(int N, int npe, int E, const int32_t* conn, std::vector<int>& ptr, std::vector<int>& idx) {
+    std::vector<int> ep(N + 1, 0);
+    for (int a = 0; a < npe; ++a)
+        for (int e = 0; e < E; ++e) ++ep[conn[(size_t)a * E + e] + 1];
+    for (int i = 0; i < N; ++i) ep[i + 1] += ep[i];
+    std::vector<int> el(ep[N]), fill(ep.begin(), ep.end() - 1);
+    for (int e = 0; e < E; ++e)
+        for (int a = 0; a < npe; ++a) el[fill[conn[(size_t)a * E + e]]++] = e;
+    // the sorted distinct neighbours of node n into buf
+    auto gather = [&](int n, std::vector<int>& buf) {
+        buf.clear();
+        for (int k = ep[n]; k < ep[n + 1]; ++k) {
+            const int e = el[k];
+            for (int a = 0; a < npe; ++a) {
+                const int m = conn[(size_t)a * E + e];
+                if (m != n) buf.push_back(m);
+            }
+        }
+        std::sort(buf.begin(), buf.end());
+        buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+    };
+    std::vector<int> cnt(N + 1, 0);
+    parallel_ranges(N, [&](int b, int e) {
+        std::vector<int> buf;
+        for (int n = b; n < e; ++n) {
+            gather(n, buf);
+            cnt[n + 1] = (int)buf.size();
+        }
+    });
+    ptr.assign(N + 1, 0);
+    for (int i = 0; i < N; ++i) ptr[i + 1] = ptr[i] + cnt[i + 1];
+    idx.assign(ptr[N], 0);
+    parallel_ranges(N, [&](int b, int e) {
+        std::vector<int> buf;
+        for (int n = b; n < e; ++n) {
+            gather(n, buf);
+            std::copy(buf.begin(), buf.end(), idx.begin() + ptr[n]);
+        }
+    });
 }
 
 // ---------------------------------------------------------------------------------------
