@@ -8,7 +8,9 @@
 // with exact predicates it is star-shaped from the point and its boundary faces are never
 // coplanar with it, so every new simplex has positive volume, co-spherical ties included.
 // Every simplex whose circumradius is at most alpha h has a ball empty of the far enclosing
-// vertices, so the alpha complex does not depend on them.
+// vertices, so the alpha complex does not depend on them.  Large perturbed 3D clouds are
+// triangulated in overlapping cells on several threads (interior_by_cells), which yields the
+// same interior simplices.
 //
 // Predicates: orientation and in-sphere determinants in double precision with a conservative
 // error bound (1e-12 of the sum of the absolute values of their terms); when the bound does not
