@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <exception>
 #include <new>
 #include <numeric>
 #include <stdexcept>
@@ -677,11 +678,21 @@ void parallel_ranges(int n, F&& f) {
         f(0, n);
         return;
     }
+    // an exception in a worker is carried to this thread and rethrown after the joins
+    std::vector<std::exception_ptr> err(T);
+    auto run = [&](int t) {
+        try {
+            f((int)((long long)n * t / T), (int)((long long)n * (t + 1) / T));
+        } catch (...) {
+            err[t] = std::current_exception();
+        }
+    };
     std::vector<std::thread> th;
-    for (int t = 1; t < T; ++t)
-        th.emplace_back([&, t] { f((int)((long long)n * t / T), (int)((long long)n * (t + 1) / T)); });
-    f(0, (int)((long long)n / T));
+    for (int t = 1; t < T; ++t) th.emplace_back(run, t);
+    run(0);
     for (auto& x : th) x.join();
+    for (auto& e : err)
+        if (e) std::rethrow_exception(e);
 }
 
 // Sorted distinct neighbours of each node (nodes sharing an element with it), CSR: the
@@ -809,11 +820,12 @@ bool interior_by_cells(const pfr_params& prm, int N, const double* pos, const st
         std::vector<double> vol;
         std::vector<uint8_t> nbint;
         bool ok = true;
+        std::exception_ptr err;
     };
     std::vector<Out> outs(C);
     std::atomic<int> next{0};
     auto work = [&]() {
-        for (int ci = next++; ci < C; ci = next++) {
+        for (int ci = next++; ci < C; ci = next++) try {
             const Cell& cl = cells[ci];
             Out& o = outs[ci];
             const double w0 = cl.lo0 - margin, W0 = cl.hi0 + margin, w1 = cl.lo1 - margin, W1 = cl.hi1 + margin;
@@ -902,6 +914,8 @@ bool interior_by_cells(const pfr_params& prm, int N, const double* pos, const st
                 }
                 o.vol.push_back(m);
             }
+        } catch (...) {  // carried to the calling thread
+            outs[ci].err = std::current_exception();
         }
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
@@ -910,6 +924,8 @@ bool interior_by_cells(const pfr_params& prm, int N, const double* pos, const st
     for (int i = 1; i < T; ++i) th.emplace_back(work);
     work();
     for (auto& t : th) t.join();
+    for (const Out& o : outs)
+        if (o.err) std::rethrow_exception(o.err);
     simp.clear();
     vol.clear();
     nbint.clear();
