@@ -669,20 +669,26 @@ void qr_basic_solve(double (&A)[D][D], double (&b)[D], double (&x)[D]) {
     for (int k = 0; k < nz; ++k) x[perm[k]] = c[k];
 }
 
-// Runs f(begin, end) over [0, n) split into contiguous ranges on up to 16 threads.
+// Number of contiguous ranges parallel_ranges splits [0, n) into: up to 16, of 4096 items or more.
+inline int range_count(int n) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    return (int)std::max<long long>(1, std::min<long long>(std::min<unsigned>(hw, 16u), n / 4096));
+}
+
+// Runs f(t, begin, end) for each of the range_count(n) contiguous ranges t of [0, n), one thread
+// per range.
 template <class F>
 void parallel_ranges(int n, F&& f) {
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int T = (int)std::min<long long>(std::min<unsigned>(hw, 16u), std::max(1, n / 4096));
+    const int T = range_count(n);
     if (T <= 1) {
-        f(0, n);
+        f(0, 0, n);
         return;
     }
     // an exception in a worker is carried to this thread and rethrown after the joins
     std::vector<std::exception_ptr> err(T);
     auto run = [&](int t) {
         try {
-            f((int)((long long)n * t / T), (int)((long long)n * (t + 1) / T));
+            f(t, (int)((long long)n * t / T), (int)((long long)n * (t + 1) / T));
         } catch (...) {
             err[t] = std::current_exception();
         }
@@ -696,8 +702,9 @@ void parallel_ranges(int n, F&& f) {
 }
 
 // Sorted distinct neighbours of each node (nodes sharing an element with it), CSR: the
-// node-element incidence by a counting sort, then each node's list sorted on its own (in
-// parallel; the lists do not depend on the thread count).
+// node-element incidence by a counting sort, then each range of nodes gathers its lists once
+// into its own buffer (a repeated node is dropped by a per-node stamp) and sorts each list on its
+// own; the buffers are concatenated in node order, so the lists do not depend on the thread count.
 void neighbours(int N, int npe, int E, const int32_t* conn, std::vector<int>& ptr, std::vector<int>& idx) {
     std::vector<int> ep(N + 1, 0);
     for (int a = 0; a < npe; ++a)
@@ -706,37 +713,32 @@ void neighbours(int N, int npe, int E, const int32_t* conn, std::vector<int>& pt
     std::vector<int> el(ep[N]), fill(ep.begin(), ep.end() - 1);
     for (int e = 0; e < E; ++e)
         for (int a = 0; a < npe; ++a) el[fill[conn[(size_t)a * E + e]]++] = e;
-    // the sorted distinct neighbours of node n into buf
-    auto gather = [&](int n, std::vector<int>& buf) {
-        buf.clear();
-        for (int k = ep[n]; k < ep[n + 1]; ++k) {
-            const int e = el[k];
-            for (int a = 0; a < npe; ++a) {
-                const int m = conn[(size_t)a * E + e];
-                if (m != n) buf.push_back(m);
-            }
-        }
-        std::sort(buf.begin(), buf.end());
-        buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
-    };
+    std::vector<std::vector<int>> part(range_count(N));
     std::vector<int> cnt(N + 1, 0);
-    parallel_ranges(N, [&](int b, int e) {
-        std::vector<int> buf;
+    parallel_ranges(N, [&](int t, int b, int e) {
+        std::vector<int> seen(N, -1);  // seen[m] == n: m is already in node n's list
+        std::vector<int>& out = part[t];
         for (int n = b; n < e; ++n) {
-            gather(n, buf);
-            cnt[n + 1] = (int)buf.size();
+            const size_t s0 = out.size();
+            seen[n] = n;
+            for (int k = ep[n]; k < ep[n + 1]; ++k) {
+                const int el_k = el[k];
+                for (int a = 0; a < npe; ++a) {
+                    const int m = conn[(size_t)a * E + el_k];
+                    if (seen[m] != n) {
+                        seen[m] = n;
+                        out.push_back(m);
+                    }
+                }
+            }
+            std::sort(out.begin() + s0, out.end());
+            cnt[n + 1] = (int)(out.size() - s0);
         }
     });
     ptr.assign(N + 1, 0);
     for (int i = 0; i < N; ++i) ptr[i + 1] = ptr[i] + cnt[i + 1];
     idx.assign(ptr[N], 0);
-    parallel_ranges(N, [&](int b, int e) {
-        std::vector<int> buf;
-        for (int n = b; n < e; ++n) {
-            gather(n, buf);
-            std::copy(buf.begin(), buf.end(), idx.begin() + ptr[n]);
-        }
-    });
+    parallel_ranges(N, [&](int t, int b, int) { std::copy(part[t].begin(), part[t].end(), idx.begin() + ptr[b]); });
 }
 
 // ---------------------------------------------------------------------------------------
@@ -748,7 +750,8 @@ constexpr int TRIPLE[4][3] = {{1, 3, 2}, {0, 2, 3}, {0, 3, 1}, {0, 1, 2}};
 
 // Interior simplices of a large 3D cloud from independent triangulations of cells, in parallel.
 //
-// The perturbed points are split into K cells by quantiles along the two longest axes (every
+// The perturbed points are split into K0 x K1 cells (K0 = round(sqrt K), K1 = floor(K / K0)) by
+// quantiles, K0 slabs along the longest axis, each cut into K1 along the second longest (every
 // point of space in exactly one cell's core box, half-open).  Each cell triangulates the points
 // of its core box widened by a margin m >= 4 alpha h on those axes.  A tetrahedron is taken from
 // the cell holding its centroid (computed from its vertices in ascending index, so every cell
