@@ -52,7 +52,7 @@ typedef struct pfr_params {
                                                symbolic perturbation does; all geometry uses
                                                the true positions.  Default 1e-6 in 3D, 0 in 2D */
     int32_t has_bounding_box;               /* boundingBox given                             */
-    int32_t single_triangulation;           /* 0: 3D clouds of 32768 nodes or more with a
+    int32_t single_triangulation;           /* 0: 3D clouds of 16384 nodes or more with a
                                                perturbation are triangulated in cells on up to
                                                16 threads (the same simplices; the element order
                                                depends only on the node count); 1: always one

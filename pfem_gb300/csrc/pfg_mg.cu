@@ -24,7 +24,7 @@
 //     instance, is one aggregate): its block inverse is the exact coarse solve.
 // Coarse levels are stored as block CSR with node-major (d+1)-vectors.
 //
-// Cycle: V(0,2) in 2D, V(1,1) in 3D, with damped node-block Jacobi (omega = 0.9 in 2D, 0.55 in
+// Cycle: V(0,2) in 2D, V(1,1) in 3D, with damped node-block Jacobi (omega = 0.7 in 2D, 0.55 in
 // 3D) on every level; the block
 // inverses are computed in FP64 from the FP32 blocks (the PSPG block's Schur complement cancels
 // heavily) and stored in FP32.  The values are refreshed after every assembly (one gather pass
@@ -45,9 +45,9 @@ namespace {
 
 // Damping of the block-Jacobi smoother, by block size (d+1): the 3D blocks need more damping
 // (at 0.6 the smoother already amplifies some modes of a 3D PSPG system; 0.55 took 9% fewer
-// Krylov iterations than 0.5 on the 3D dam break).  In 2D 0.9 took the fewest (of 0.6 to 1.0,
-// on 2D dam breaks of 1k and 25k nodes).
-__host__ __device__ constexpr float mg_omega(int B) { return B == 3 ? 0.9f : 0.55f; }
+// Krylov iterations than 0.5 on the 3D dam break).  In 2D 0.9 took the fewest iterations on dam
+// breaks but stalled the mixed solves of sloshing tanks, so 2D keeps 0.7.
+__host__ __device__ constexpr float mg_omega(int B) { return B == 3 ? 0.7f : 0.55f; }
 
 // ---- level 0 (field-major CSR) ---------------------------------------------------------------
 

@@ -960,7 +960,7 @@ void alpha_shape(const pfr_params& prm, int N, const double* pos, const uint8_t*
     // large perturbed 3D clouds: interior simplices from cells triangulated in parallel (K fixed
     // by the node count, so the result does not depend on the machine); serially otherwise, or
     // when a cell's conditions fail
-    const int K = std::min(16, N / 16384);
+    const int K = std::min(16, N / 8192);
     bool by_cells = false;
     if constexpr (D == 3) {
         if (!prm.single_triangulation && prm.jitter > 0 && K >= 2 &&

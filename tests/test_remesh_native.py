@@ -175,7 +175,7 @@ def test_cells_equal_one_triangulation():
     gives the simplices, facets, flags and node origins of one triangulation, fresh and moved."""
     h = (0.25 / 3e4) ** (1 / 3)
     pos, flags = M.dam_break_nodes_3d(h, seed=1)
-    assert pos.shape[1] >= 32768
+    assert pos.shape[1] >= 16384
     rng = np.random.default_rng(3)
     for p in (pos, pos + rng.uniform(-0.3, 0.3, pos.shape) * h * ((flags & M.BOUND) == 0)):
         one = R.alpha_shape_native(p, flags, h, 1.2, True, single=True)
