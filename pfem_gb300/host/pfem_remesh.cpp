@@ -843,44 +843,49 @@ bool interior_by_cells(const pfr_params& prm, int N, const double* pos, const st
             Delaunay<3> dt(std::move(lp));
             dt.build();
             const int S = dt.slots();
-            // per slot: interior (true positions), and whether its perturbed circumsphere lies in
+            // per slot, evaluated only for the simplices taken here and their neighbours: bit 0
+            // evaluated, bit 1 interior (true positions), bit 2 its perturbed circumsphere lies in
             // the widened box
-            std::vector<uint8_t> inter(S, 0), inside(S, 0);
-            for (int t = 0; t < S; ++t) {
-                if (!dt.real(t)) continue;
+            std::vector<uint8_t> st(S, 0);
+            auto eval = [&](int t) -> uint8_t {
+                if (st[t]) return st[t];
+                uint8_t r = 1;
                 int v[V];
                 for (int i = 0; i < V; ++i) v[i] = gid[dt.vert(t, i)];
                 double A[D][D];
                 for (int k = 0; k < D; ++k)
                     for (int c = 0; c < D; ++c) A[k][c] = pos[(size_t)c * N + v[k + 1]] - pos[(size_t)c * N + v[0]];
                 const double m = std::fabs(det_rows<D>(A));
-                inter[t] = circumradius2<D>(A) <= alpha2 && m > 0.0;
-                if (!inter[t]) continue;
-                double B[D][D], rhs[D], ss = 0;
-                for (int k = 0; k < D; ++k) {
-                    double sk = 0;
-                    for (int c = 0; c < D; ++c) {
-                        B[k][c] = pts[(size_t)v[k + 1] * 3 + c] - pts[(size_t)v[0] * 3 + c];
-                        sk += B[k][c] * B[k][c];
+                if (circumradius2<D>(A) <= alpha2 && m > 0.0) {
+                    r |= 2;
+                    double B[D][D], rhs[D], ss = 0;
+                    for (int k = 0; k < D; ++k) {
+                        double sk = 0;
+                        for (int c = 0; c < D; ++c) {
+                            B[k][c] = pts[(size_t)v[k + 1] * 3 + c] - pts[(size_t)v[0] * 3 + c];
+                            sk += B[k][c] * B[k][c];
+                        }
+                        rhs[k] = 0.5 * sk;
+                        ss += sk;
                     }
-                    rhs[k] = 0.5 * sk;
-                    ss += sk;
+                    const double det = det_rows<D>(B);
+                    if (std::fabs(det) > 1e-12 * std::pow(ss, 1.5)) {  // else not inside
+                        double cen[D];
+                        for (int col = 0; col < D; ++col) {
+                            double Mx[D][D];
+                            for (int rr = 0; rr < D; ++rr)
+                                for (int cc = 0; cc < D; ++cc) Mx[rr][cc] = cc == col ? rhs[rr] : B[rr][cc];
+                            cen[col] = det_rows<D>(Mx) / det;
+                        }
+                        const double rad = std::sqrt(cen[0] * cen[0] + cen[1] * cen[1] + cen[2] * cen[2]) * (1 + 1e-9);
+                        const double c0 = pts[(size_t)v[0] * 3 + a0] + cen[a0], c1 = pts[(size_t)v[0] * 3 + a1] + cen[a1];
+                        if (c0 - rad > w0 && c0 + rad < W0 && c1 - rad > w1 && c1 + rad < W1) r |= 4;
+                    }
                 }
-                const double det = det_rows<D>(B);
-                if (!(std::fabs(det) > 1e-12 * std::pow(ss, 1.5))) continue;  // not inside
-                double cen[D];
-                for (int col = 0; col < D; ++col) {
-                    double Mx[D][D];
-                    for (int r = 0; r < D; ++r)
-                        for (int cc = 0; cc < D; ++cc) Mx[r][cc] = cc == col ? rhs[r] : B[r][cc];
-                    cen[col] = det_rows<D>(Mx) / det;
-                }
-                const double rad = std::sqrt(cen[0] * cen[0] + cen[1] * cen[1] + cen[2] * cen[2]) * (1 + 1e-9);
-                const double c0 = pts[(size_t)v[0] * 3 + a0] + cen[a0], c1 = pts[(size_t)v[0] * 3 + a1] + cen[a1];
-                inside[t] = c0 - rad > w0 && c0 + rad < W0 && c1 - rad > w1 && c1 + rad < W1;
-            }
+                return st[t] = r;
+            };
             for (int t = 0; t < S && o.ok; ++t) {
-                if (!inter[t]) continue;
+                if (!dt.real(t)) continue;
                 int v[V], sv[V];
                 for (int i = 0; i < V; ++i) sv[i] = v[i] = gid[dt.vert(t, i)];
                 std::sort(sv, sv + V);
@@ -892,15 +897,18 @@ bool interior_by_cells(const pfr_params& prm, int N, const double* pos, const st
                 ce0 *= 0.25;
                 ce1 *= 0.25;
                 if (!(ce0 >= cl.lo0 && ce0 < cl.hi0 && ce1 >= cl.lo1 && ce1 < cl.hi1)) continue;
-                if (!inside[t]) {
+                const uint8_t et = eval(t);
+                if (!(et & 2)) continue;
+                if (!(et & 4)) {
                     o.ok = false;
                     break;
                 }
                 uint8_t nbi[V];
                 for (int l = 0; l < V; ++l) {
                     const int u = dt.nbr(t, l);
-                    nbi[l] = u >= 0 && dt.real(u) && inter[u];
-                    if (nbi[l] && !inside[u]) o.ok = false;
+                    const uint8_t eu = u >= 0 && dt.real(u) ? eval(u) : 0;
+                    nbi[l] = (eu & 2) != 0;
+                    if (nbi[l] && !(eu & 4)) o.ok = false;
                 }
                 double A[D][D];
                 for (int k = 0; k < D; ++k)
